@@ -1,0 +1,92 @@
+"""ctypes binding of the C ABI in include/mpdata.h.
+
+The library is loaded from the package's in-tree build
+(advectionhpctester_gb300/_lib/libmpdata_gb300.so).  There is no fallback: if
+the library is missing, loading raises, and every MPDATA call fails loudly.
+"""
+import ctypes
+import os
+import re
+
+from . import build as _build
+
+_lib = None
+
+P = ctypes.c_void_p
+I = ctypes.c_int
+D = ctypes.c_double
+F = ctypes.c_float
+
+
+class MpdataGrid(ctypes.Structure):
+    _fields_ = [("np", I), ("mp", I), ("lp", I), ("ih", I), ("ibcx", I), ("ibcy", I), ("ibcz", I)]
+
+
+class MpdataOpts(ctypes.Structure):
+    _fields_ = [("iord", I), ("nonos", I), ("gauge", I), ("precision", I), ("predictor", I)]
+
+
+# (name, argtypes, restype) for every symbol include/mpdata.h declares
+SIGNATURES = {
+    "mpdata_ws_create": ([ctypes.POINTER(MpdataGrid), ctypes.POINTER(MpdataOpts), ctypes.POINTER(P)], I),
+    "mpdata_ws_destroy": ([P], I),
+    "mpdata_step_f64": ([P] * 10, I),
+    "mpdata_step_f32": ([P] * 10, I),
+    "mpdata_advec_dwarf_f64": ([I] * 12 + [P] * 8 + [I, I, P], I),
+    "mpdata_advec_dwarf_f32": ([I] * 12 + [P] * 8 + [I, I, P], I),
+    "mpdata_release_cached": ([], I),
+    "mpdata_velprd_f64": ([P] * 8 + [D] * 5 + [P] * 4, I),
+    "mpdata_velprd_f32": ([P] * 8 + [F] * 5 + [P] * 4, I),
+    "mpdata_ws_error": ([P, ctypes.POINTER(I)], I),
+    "mpdata_launch_count": ([], ctypes.c_longlong),
+    "mpdata_ws_profile": ([P, I], I),
+    "mpdata_ws_stage_times": ([P, I, ctypes.POINTER(D), ctypes.POINTER(ctypes.c_longlong)], I),
+    "mpdata_stage_name": ([I], ctypes.c_char_p),
+    "mpdata_strerror": ([I], ctypes.c_char_p),
+    "mpdata_version": ([], ctypes.c_char_p),
+}
+
+
+def header_symbols():
+    """Function names declared in include/mpdata.h."""
+    with open(os.path.join(_build.INCLUDE, "mpdata.h")) as fh:
+        text = fh.read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?[a-z_ ]+\*?\s*\b(mpdata_[a-z0-9_]+)\s*\(", text, re.M)))
+
+
+def lib_path():
+    return _build.LIB
+
+
+def load(build_if_missing=False):
+    """Load the library (optionally building it first)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        if build_if_missing:
+            _build.build()
+        else:
+            raise RuntimeError("MPDATA CUDA library not built (%s); run "
+                               "advectionhpctester_gb300.build.build() first" % path)
+    lib = ctypes.CDLL(path)
+    for name, (argt, rest) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = argt
+        fn.restype = rest
+    _lib = lib
+    return lib
+
+
+class MpdataError(RuntimeError):
+    def __init__(self, code, where=""):
+        msg = load().mpdata_strerror(code).decode()
+        super().__init__("%s failed: %s (code %d)" % (where or "mpdata call", msg, code))
+        self.code = code
+
+
+def check(code, where=""):
+    if code != 0:
+        raise MpdataError(code, where)
+    return code

@@ -1,0 +1,191 @@
+"""Host-side mirror of the reference's MPDATA interface over the C ABI.
+
+Names, argument order and meaning follow the reference:
+
+  advec_dwarf   advection/src_drivers/advec.f90:116-244 (the dwarf driver)
+  Workspace     the module-global scratch of scratch_datafields_modular.f90:119-134,
+                owned explicitly; .step() is upwind3d_gpubc + antidiff3d_*_gpubc,
+                .velprd() is velprd_traj0 + velprdA_to_C + the driver's level roll
+                (module_velprd.f90:15-364, velprd_driver.f90:254-270)
+
+Arrays are CUDA tensors whose memory is Fortran-ordered with the reference's
+halo extents (see `fortran_device` to make one from a numpy array).  Errors
+raise MpdataError instead of the reference's STOP.  There is no CPU path: if
+the CUDA library is not built or no GPU is present, calls fail.
+"""
+import numpy as np
+
+from . import _native
+from ._native import MpdataError, check
+
+try:  # torch provides device memory and streams (plumbing only)
+    import torch
+except ImportError:  # pragma: no cover
+    torch = None
+
+
+def _require_torch():
+    if torch is None:
+        raise RuntimeError("torch is required for device memory")
+
+
+def fortran_device(a, device="cuda", dtype=None):
+    """Copy a Fortran-ordered numpy array to a CUDA tensor with Fortran strides
+    (logical shape equal to the numpy shape)."""
+    _require_torch()
+    a = np.asarray(a)
+    if dtype is not None:
+        a = a.astype(dtype)
+    flat = np.ascontiguousarray(a.reshape(-1, order="F"))
+    t = torch.from_numpy(flat).to(device)
+    return t.reshape(tuple(reversed(a.shape))).permute(*reversed(range(a.ndim)))
+
+
+def fortran_empty(shape, dtype, device="cuda"):
+    _require_torch()
+    t = torch.zeros(tuple(reversed(shape)), dtype=dtype, device=device)
+    return t.permute(*reversed(range(len(shape))))
+
+
+def to_numpy(t):
+    """Fortran-ordered numpy copy of a Fortran-strided tensor."""
+    h = t.detach().permute(*reversed(range(t.ndim))).contiguous().cpu().numpy()
+    return np.asfortranarray(h.transpose(*reversed(range(h.ndim))))
+
+
+def _is_fortran(t):
+    st = 1
+    for n, s in zip(t.shape, t.stride()):
+        if n > 1 and s != st:
+            return False
+        st *= n
+    return True
+
+
+def _ptr(t, dtype, shape=None, name="array"):
+    if t is None:
+        return None
+    if not t.is_cuda:
+        raise ValueError("%s must be a CUDA tensor" % name)
+    if t.dtype != dtype:
+        raise ValueError("%s must be %s, got %s" % (name, dtype, t.dtype))
+    if shape is not None and tuple(t.shape) != tuple(shape):
+        raise ValueError("%s must have shape %s (reference halo extents), got %s"
+                         % (name, tuple(shape), tuple(t.shape)))
+    if not _is_fortran(t):
+        raise ValueError("%s must be Fortran-ordered" % name)
+    return t.data_ptr()
+
+
+def _stream(stream):
+    if stream is None:
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+def shapes(np_, mp, lp, ih):
+    s = (np_ + 2 * ih, mp + 2 * ih, lp + 2 * ih)
+    return dict(psi=s, u1=(s[0] + 1, s[1], s[2]), u2=(s[0], s[1] + 1, s[2]),
+                u3=(s[0], s[1], s[2] + 1), bcx=(mp, lp, 2), bcy=(np_, lp, 2))
+
+
+class Workspace:
+    """Device scratch for one grid and option set (see mpdata_ws_create)."""
+
+    def __init__(self, np_, mp, lp, ih=1, ibcx=0, ibcy=0, ibcz=0, iord=2, nonos=1, gauge=1,
+                 precision=64):
+        _require_torch()
+        self.lib = _native.load()
+        self.grid = _native.MpdataGrid(np_, mp, lp, ih, ibcx, ibcy, ibcz)
+        self.opts = _native.MpdataOpts(iord, nonos, gauge, precision, 0)
+        self.dtype = torch.float64 if precision == 64 else torch.float32
+        self.shapes = shapes(np_, mp, lp, ih)
+        h = _native.P()
+        check(self.lib.mpdata_ws_create(self.grid, self.opts, h), "mpdata_ws_create")
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None):
+            check(self.lib.mpdata_ws_destroy(self.handle), "mpdata_ws_destroy")
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, psi, u1, u2, u3, h, rhr, bcx=None, bcy=None, stream=None):
+        """One MPDATA step, psi updated in place (upwind3d_gpubc +
+        antidiff3d_gauge_gpubc / antidiff3d_standard_gpubc)."""
+        s, d = self.shapes, self.dtype
+        fn = self.lib.mpdata_step_f64 if self.opts.precision == 64 else self.lib.mpdata_step_f32
+        check(fn(self.handle, _ptr(psi, d, s["psi"], "psi"), _ptr(u1, d, s["u1"], "u1"),
+                 _ptr(u2, d, s["u2"], "u2"), _ptr(u3, d, s["u3"], "u3"), _ptr(h, d, s["psi"], "h"),
+                 _ptr(rhr, d, s["psi"], "rhr"), _ptr(bcx, d, s["bcx"], "bcx"),
+                 _ptr(bcy, d, s["bcy"], "bcy"), _stream(stream)), "mpdata_step")
+
+    def velprd(self, ox, oy, oz, h, dxi, dyi, dzi, dt, dt_ratio, u1, u2, u3, u=None, v=None, w=None,
+               stream=None):
+        """Velocity predictor; ox/oy/oz (and u/v/w) are (..., 3) level stacks."""
+        s, d = self.shapes, self.dtype
+        lev = s["psi"] + (3,)
+        fn = self.lib.mpdata_velprd_f64 if self.opts.precision == 64 else self.lib.mpdata_velprd_f32
+        check(fn(self.handle, _ptr(ox, d, lev, "ox"), _ptr(oy, d, lev, "oy"), _ptr(oz, d, lev, "oz"),
+                 _ptr(u, d, lev, "u"), _ptr(v, d, lev, "v"), _ptr(w, d, lev, "w"),
+                 _ptr(h, d, s["psi"], "h"), dxi, dyi, dzi, dt, dt_ratio, _ptr(u1, d, s["u1"], "u1"),
+                 _ptr(u2, d, s["u2"], "u2"), _ptr(u3, d, s["u3"], "u3"), _stream(stream)),
+              "mpdata_velprd")
+
+    def profile(self, enable=True):
+        """Start (or stop) per-stage CUDA-event timing of this workspace."""
+        check(self.lib.mpdata_ws_profile(self.handle, 1 if enable else 0), "mpdata_ws_profile")
+
+    def stage_times(self):
+        """{stage name: (total ms, launches)} accumulated since profile()."""
+        import ctypes
+        n = 16
+        ms = (ctypes.c_double * n)()
+        cnt = (ctypes.c_longlong * n)()
+        rc = self.lib.mpdata_ws_stage_times(self.handle, n, ms, cnt)
+        if rc < 0:
+            check(rc, "mpdata_ws_stage_times")
+        return {self.lib.mpdata_stage_name(i).decode(): (ms[i], cnt[i]) for i in range(rc)}
+
+    def error_word(self):
+        out = _native.I(0)
+        check(self.lib.mpdata_ws_error(self.handle, out), "mpdata_ws_error")
+        return out.value
+
+
+def advec_dwarf(legacyoptmode, t_adv, lupdatemulti, lvertsplit, np_, mp, lp, ih, ipoles, ibcx, ibcy,
+                ibcz, x, x_lr, x_bt, uadv, vadv, wadv, rhr, rhoadv, iord=2, nonos=1, stream=None):
+    """The reference's dwarf driver (advec.f90:116-244) on CUDA tensors."""
+    _require_torch()
+    lib = _native.load()
+    d = x.dtype
+    if d not in (torch.float64, torch.float32):
+        raise ValueError("x must be float64 or float32")
+    s = shapes(np_, mp, lp, ih) if min(np_, mp, lp, ih) > 0 else None
+    g = (lambda k: s[k]) if s else (lambda k: None)
+    fn = lib.mpdata_advec_dwarf_f64 if d == torch.float64 else lib.mpdata_advec_dwarf_f32
+    check(fn(legacyoptmode, t_adv, int(bool(lupdatemulti)), int(bool(lvertsplit)), np_, mp, lp, ih,
+             ipoles, ibcx, ibcy, ibcz, _ptr(x, d, g("psi"), "x"), _ptr(x_lr, d, g("bcx"), "x_lr"),
+             _ptr(x_bt, d, g("bcy"), "x_bt"), _ptr(uadv, d, g("u1"), "uadv"),
+             _ptr(vadv, d, g("u2"), "vadv"), _ptr(wadv, d, g("u3"), "wadv"),
+             _ptr(rhr, d, g("psi"), "rhr"), _ptr(rhoadv, d, g("psi"), "rhoadv"), iord, nonos,
+             _stream(stream)), "advec_dwarf")
+
+
+def release_cached():
+    check(_native.load().mpdata_release_cached(), "mpdata_release_cached")
+
+
+def launch_count():
+    return int(_native.load().mpdata_launch_count())
+
+
+__all__ = ["Workspace", "advec_dwarf", "fortran_device", "fortran_empty", "to_numpy", "MpdataError",
+           "release_cached", "launch_count", "shapes"]

@@ -1,0 +1,145 @@
+/*
+ * mpdata.h — C ABI of the GB300-native MPDATA advection step.
+ *
+ * Drop-in for the hot path of piotrows/advectionHPCtester: the dwarf driver
+ * advec_dwarf and the kernels it dispatches to (upwind, standard and gauge
+ * antidiffusion with the nonoscillatory limiter, boundary/halo fill), plus the
+ * velocity predictor.  Plain pointers and sizes only; every array pointer is a
+ * DEVICE (or managed) pointer to a Fortran column-major array with the
+ * reference's halo extents:
+ *
+ *   psi, h, rhr           (1-ih:np+ih,   1-ih:mp+ih,   1-ih:lp+ih)
+ *   u1 (C-grid x faces)   (1-ih:np+1+ih, 1-ih:mp+ih,   1-ih:lp+ih)
+ *   u2 (C-grid y faces)   (1-ih:np+ih,   1-ih:mp+1+ih, 1-ih:lp+ih)
+ *   u3 (C-grid z faces)   (1-ih:np+ih,   1-ih:mp+ih,   1-ih:lp+1+ih)
+ *   bcx (mp,lp,2), bcy (np,lp,2)  Dirichlet x/y halo values of psi
+ *
+ * Boundary flags per axis (ibcx, ibcy, ibcz):
+ *   0  the reference's single-rank rule: open x/y walls take psi's halo from
+ *      bcx/bcy in the upwind pass and carry zero antidiffusive flux; z walls
+ *      use the mirrored-flux rule f(1) = -f(2), f(lp+1) = -f(lp).
+ *   1  periodic with period n on that axis (face n+1 is face 1; caller halos
+ *      are neither read nor written on that axis).
+ *
+ * Conventions: every call returns 0 on success or a negative MPDATA_E* code;
+ * nothing exits or aborts.  Calls are ordered on the given CUDA stream (NULL
+ * = the legacy default stream) and do not synchronise the host, except where
+ * stated.  One host thread per workspace at a time.
+ */
+#ifndef MPDATA_H
+#define MPDATA_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MPDATA_OK 0
+#define MPDATA_E_DIMS -1        /* bad np/mp/lp/ih or boundary flags */
+#define MPDATA_E_OPTS -2        /* bad legacyoptmode/t_adv/iord/nonos/precision */
+#define MPDATA_E_NULL -3        /* a required pointer is NULL */
+#define MPDATA_E_WS -4          /* workspace missing or built for another grid/options */
+#define MPDATA_E_CUDA -5        /* a CUDA runtime call failed */
+#define MPDATA_E_DEVICE -6      /* the device error word is set (non-finite result) */
+#define MPDATA_E_UNSUPPORTED -7 /* a reference option outside this library's scope */
+
+typedef struct {
+  int np, mp, lp, ih;   /* interior cells per axis and halo width (ih >= 1) */
+  int ibcx, ibcy, ibcz; /* 0 = reference open/wall rule, 1 = periodic */
+} mpdata_grid;
+
+typedef struct {
+  int iord;      /* number of MPDATA passes: 1 = upwind only, 2 = the reference, >= 3 extra corrective passes */
+  int nonos;     /* 1 = nonoscillatory (FCT) limiter, as the reference always does; 0 = off */
+  int gauge;     /* 1 = infinite-gauge form (t_adv=1), 0 = standard form (t_adv=2) */
+  int precision; /* 64 = FP64 arithmetic, 32 = FP32 arithmetic */
+  int predictor; /* reserved for the fused predictor path; 0 */
+} mpdata_opts;
+
+/* Workspace: owns the device scratch that the reference keeps in module
+ * globals (scratch_datafields_modular.f90:119-134: xant, v1..3, f1..3,
+ * f1ns..f3ns, cp, cn).  Replaces allocate_scratch_mpdata_datafields. */
+int mpdata_ws_create(const mpdata_grid* grid, const mpdata_opts* opts, void** ws);
+int mpdata_ws_destroy(void* ws);
+
+/* One MPDATA step on psi (in place): upwind3d_gpubc followed by iord-1
+ * antidiffusive passes.  Replaces the pair of calls
+ *   upwind3d_gpubc   advection/src_algorithms/upwind3d-gpubc.f90:20-201
+ *   antidiff3d_gauge_gpubc / antidiff3d_standard_gpubc
+ *                    advection/src_algorithms/antidiff3d-gauge-gpubc.f90:14-435
+ *                    advection/src_algorithms/antidiff3d-standard-gpubc.f90:14-464
+ * as dispatched by advec_dwarf (advection/src_drivers/advec.f90:234-240).
+ * h is the reference's rhoadv/h, rhr its rhr.  bcx/bcy may be NULL when the
+ * axis is periodic. */
+int mpdata_step_f64(void* ws, double* psi, const double* u1, const double* u2, const double* u3,
+                    const double* h, const double* rhr, const double* bcx, const double* bcy,
+                    void* stream);
+int mpdata_step_f32(void* ws, float* psi, const float* u1, const float* u2, const float* u3,
+                    const float* h, const float* rhr, const float* bcx, const float* bcy,
+                    void* stream);
+
+/* The reference driver itself, same argument order and meaning as
+ * advec_dwarf (advection/src_drivers/advec.f90:116-122):
+ *   legacyoptmode 4 = upwind + antidiffusion, 6 = upwind only (5 is the
+ *   HALOBC upwind, whose body is commented out in the reference: rejected);
+ *   t_adv 1 = gauge, 2 = standard; lupdatemulti and lvertsplit are accepted
+ *   and, as in the reference GPUBC path, change nothing; ipoles must be 0.
+ * x_lr/x_bt are the Dirichlet halo values (bcx/bcy), uadv/vadv/wadv the
+ * C-grid Courant numbers, rhr and rhoadv the densities.  A workspace for the
+ * grid is created on first use and cached (like the reference's module
+ * scratch); mpdata_release_cached frees it.  iord/nonos extend the
+ * reference's fixed choice (iord=2, nonoscillatory on): pass 2 and 1 for the
+ * reference behaviour. */
+int mpdata_advec_dwarf_f64(int legacyoptmode, int t_adv, int lupdatemulti, int lvertsplit,
+                           int np, int mp, int lp, int ih, int ipoles, int ibcx, int ibcy,
+                           int ibcz, double* x, const double* x_lr, const double* x_bt,
+                           const double* uadv, const double* vadv, const double* wadv,
+                           const double* rhr, const double* rhoadv, int iord, int nonos,
+                           void* stream);
+int mpdata_advec_dwarf_f32(int legacyoptmode, int t_adv, int lupdatemulti, int lvertsplit,
+                           int np, int mp, int lp, int ih, int ipoles, int ibcx, int ibcy,
+                           int ibcz, float* x, const float* x_lr, const float* x_bt,
+                           const float* uadv, const float* vadv, const float* wadv,
+                           const float* rhr, const float* rhoadv, int iord, int nonos,
+                           void* stream);
+int mpdata_release_cached(void);
+
+/* Velocity predictor: velprd_traj0 + velprdA_to_C
+ * (advection/src_algorithms/module_velprd.f90:15-89,166-364) followed by the
+ * level roll of velprd_driver (advection/src_algorithms/velprd_driver.f90:254-270).
+ * ox/oy/oz: three psi-shaped levels back to back (0 = n, 1 = n+1/2 written,
+ * 2 = momenta at n-1, overwritten with ox0*h for the next step).
+ * u/v/w: optional physical velocities with the same three levels (NULL to skip).
+ * Writes the C-grid Courant numbers u1/u2/u3 (faces 1..n+1). */
+int mpdata_velprd_f64(void* ws, double* ox, double* oy, double* oz, double* u, double* v,
+                      double* w, const double* h, double dxi, double dyi, double dzi, double dt,
+                      double dt_ratio, double* u1, double* u2, double* u3, void* stream);
+int mpdata_velprd_f32(void* ws, float* ox, float* oy, float* oz, float* u, float* v, float* w,
+                      const float* h, float dxi, float dyi, float dzi, float dt, float dt_ratio,
+                      float* u1, float* u2, float* u3, void* stream);
+
+/* Device error word of a workspace (bit 0: a non-finite value was produced
+ * by the last checked step).  Synchronises the workspace's last stream. */
+int mpdata_ws_error(void* ws, int* error_word);
+
+/* Number of kernels this library launched since process start (all
+ * workspaces), for launch accounting. */
+long long mpdata_launch_count(void);
+
+/* Per-stage kernel timing (replaces the reference's TIMERSCUDA counters,
+ * common/mpi_parallel.f90:7256-7338, without a host sync per timer).
+ * enable=1: record a CUDA event pair on the launching stream around every
+ * kernel of this workspace; enable=0: stop and discard.
+ * mpdata_ws_stage_times synchronises on the recorded events and returns the
+ * accumulated milliseconds and launch counts per stage (nstages entries,
+ * see mpdata_stage_name); the return value is the number of stages. */
+int mpdata_ws_profile(void* ws, int enable);
+int mpdata_ws_stage_times(void* ws, int nstages, double* total_ms, long long* launches);
+const char* mpdata_stage_name(int stage);
+
+const char* mpdata_strerror(int code);
+const char* mpdata_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MPDATA_H */

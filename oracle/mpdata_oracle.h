@@ -1,0 +1,101 @@
+/*
+ * CPU oracle for the MPDATA advection step — TEST INFRASTRUCTURE ONLY.
+ *
+ * A strict-IEEE (no FMA contraction, no fast-math, left-to-right evaluation)
+ * C++ restatement of the reference's MPDATA hot path, written stage by stage
+ * from the reference's Fortran sources:
+ *   upwind            advection/src_algorithms/upwind3d-gpubc.f90:101-198
+ *   standard antidiff advection/src_algorithms/antidiff3d-standard-gpubc.f90:59-462
+ *   gauge antidiff    advection/src_algorithms/antidiff3d-gauge-gpubc.f90:71-430
+ *   point operators   advection/src_algorithms/mpdataoperators.inc:50-96
+ *   halo/BC helpers   advection/src_algorithms/mpdataoperators.inc:253-287,479-584,673-947,1034-1086
+ *   predictor         advection/src_algorithms/module_velprd.f90:15-89,166-520
+ *   state shift       advection/src_algorithms/velprd_driver.f90:254-270
+ *   dispatcher        advection/src_drivers/advec.f90:116-244
+ *
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it,
+ * and only as the checker / the timed CPU baseline.  The product path never
+ * links or calls it.
+ *
+ * Parity pinning: the reference ships one known answer (the 59^3 rotating
+ * sphere "Error L2 norm" 0.0028, advection_dwarf_test_modular.f90:157-158);
+ * the oracle reproduces it (tests/test_oracle_cpu.py).  A second, independent
+ * numpy restatement (oracle/mpdata_np.py) is compared with this one bit for
+ * bit.  No Fortran toolchain exists here or on the GPU host, so field-level
+ * parity against the reference binary itself is unpinned beyond the KAT.
+ *
+ * Arrays are Fortran column-major with the reference's halo extents:
+ *   psi-shaped  (1-ih:np+ih,   1-ih:mp+ih,   1-ih:lp+ih)
+ *   u1          (1-ih:np+1+ih, 1-ih:mp+ih,   1-ih:lp+ih)
+ *   u2          (1-ih:np+ih,   1-ih:mp+1+ih, 1-ih:lp+ih)
+ *   u3          (1-ih:np+ih,   1-ih:mp+ih,   1-ih:lp+1+ih)
+ *   bcx(mp,lp,2), bcy(np,lp,2)
+ *
+ * Boundary flags per axis: ibc = 0 is the reference's single-rank rule (open
+ * x/y with Dirichlet bcx/bcy halos and zero antidiffusive wall flux; z walls
+ * with the mirrored-flux rule f(1)=-f(2), f(lp+1)=-f(lp)); ibc = 1 is a clean
+ * periodic wrap with period n on that axis.
+ */
+#ifndef MPDATA_ORACLE_H
+#define MPDATA_ORACLE_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+  int np, mp, lp, ih;
+  int ibcx, ibcy, ibcz;
+} orc_grid;
+
+/* advec_dwarf (advec.f90:116-244): legacyoptmode 4 = upwind + antidiffusion,
+ * 6 = upwind only; t_adv 1 = gauge, 2 = standard.  iord >= 2 is the number of
+ * MPDATA passes (the reference hard-wires 2; >= 3 follows the published MPDATA
+ * recursion), nonos = 1 enables the FCT limiter (always on in the reference). */
+int orc_advec_dwarf_f64(const orc_grid* g, int legacyoptmode, int t_adv, int iord, int nonos,
+                        double* x, const double* x_lr, const double* x_bt,
+                        const double* uadv, const double* vadv, const double* wadv,
+                        const double* rhr, const double* rhoadv);
+int orc_advec_dwarf_f32(const orc_grid* g, int legacyoptmode, int t_adv, int iord, int nonos,
+                        float* x, const float* x_lr, const float* x_bt,
+                        const float* uadv, const float* vadv, const float* wadv,
+                        const float* rhr, const float* rhoadv);
+
+/* Repeated steps (nsteps calls of the above), for timing and long parity runs. */
+int orc_advec_steps_f64(const orc_grid* g, int nsteps, int legacyoptmode, int t_adv, int iord,
+                        int nonos, double* x, const double* x_lr, const double* x_bt,
+                        const double* uadv, const double* vadv, const double* wadv,
+                        const double* rhr, const double* rhoadv);
+int orc_advec_steps_f32(const orc_grid* g, int nsteps, int legacyoptmode, int t_adv, int iord,
+                        int nonos, float* x, const float* x_lr, const float* x_bt,
+                        const float* uadv, const float* vadv, const float* wadv,
+                        const float* rhr, const float* rhoadv);
+
+/* upwind3d_gpubc alone (upwind3d-gpubc.f90:101-198): writes xant interior. */
+int orc_upwind_f64(const orc_grid* g, const double* x, const double* bcx, const double* bcy,
+                   const double* u1, const double* u2, const double* u3, const double* rhr,
+                   const double* h, double* xant);
+
+/* Velocity predictor velprd_traj0 + velprdA_to_C (module_velprd.f90:15-89,166-364)
+ * followed by the driver's level shift (velprd_driver.f90:254-270).
+ * ox/oy/oz hold three psi-shaped levels back to back (0: n, 1: n+1/2 out,
+ * 2: n-1 momenta); u/v/w (physical velocities, three levels) may be NULL. */
+int orc_velprd_f64(const orc_grid* g, double* ox, double* oy, double* oz, double* u, double* v,
+                   double* w, const double* h, double dxi, double dyi, double dzi, double dt,
+                   double dt_ratio, double* u1, double* u2, double* u3);
+int orc_velprd_f32(const orc_grid* g, float* ox, float* oy, float* oz, float* u, float* v,
+                   float* w, const float* h, float dxi, float dyi, float dzi, float dt,
+                   float dt_ratio, float* u1, float* u2, float* u3);
+
+/* velprdA_to_C_ver2 (module_velprd.f90:366-520): A-grid Courant numbers (psi
+ * shaped, halos overwritten by the one-sided extrapolation) -> C grid. */
+int orc_a_to_c_f64(const orc_grid* g, double* uadv, double* vadv, double* wadv, double* u1,
+                   double* u2, double* u3);
+
+/* Threads used by the OpenMP loops (1 = the serial reference build). */
+void orc_set_threads(int n);
+int orc_get_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

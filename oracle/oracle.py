@@ -1,0 +1,111 @@
+"""ctypes front end of the C++ oracle (test infrastructure only).
+
+Arrays are numpy arrays in Fortran order with the reference's halo extents
+(see mpdata_oracle.h).  Every function mirrors one reference entry point:
+
+  advec_dwarf  advection/src_drivers/advec.f90:116-244
+  upwind       advection/src_algorithms/upwind3d-gpubc.f90:20-201
+  velprd       advection/src_algorithms/module_velprd.f90:15-89,166-364 and
+               advection/src_algorithms/velprd_driver.f90:254-270
+  a_to_c       advection/src_algorithms/module_velprd.f90:366-520
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build_oracle
+
+_lib = None
+
+
+class OrcGrid(ctypes.Structure):
+    _fields_ = [("np", ctypes.c_int), ("mp", ctypes.c_int), ("lp", ctypes.c_int),
+                ("ih", ctypes.c_int), ("ibcx", ctypes.c_int), ("ibcy", ctypes.c_int),
+                ("ibcz", ctypes.c_int)]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build_oracle.build()
+        _lib = ctypes.CDLL(path)
+        P = ctypes.c_void_p
+        I = ctypes.c_int
+        for name in ("orc_advec_dwarf_f64", "orc_advec_dwarf_f32"):
+            f = getattr(_lib, name)
+            f.argtypes = [ctypes.POINTER(OrcGrid), I, I, I, I] + [P] * 8
+            f.restype = I
+        for name in ("orc_advec_steps_f64", "orc_advec_steps_f32"):
+            f = getattr(_lib, name)
+            f.argtypes = [ctypes.POINTER(OrcGrid), I, I, I, I, I] + [P] * 8
+            f.restype = I
+        _lib.orc_upwind_f64.argtypes = [ctypes.POINTER(OrcGrid)] + [P] * 9
+        _lib.orc_upwind_f64.restype = I
+        D = ctypes.c_double
+        F = ctypes.c_float
+        _lib.orc_velprd_f64.argtypes = [ctypes.POINTER(OrcGrid)] + [P] * 7 + [D] * 5 + [P] * 3
+        _lib.orc_velprd_f64.restype = I
+        _lib.orc_velprd_f32.argtypes = [ctypes.POINTER(OrcGrid)] + [P] * 7 + [F] * 5 + [P] * 3
+        _lib.orc_velprd_f32.restype = I
+        _lib.orc_a_to_c_f64.argtypes = [ctypes.POINTER(OrcGrid)] + [P] * 6
+        _lib.orc_a_to_c_f64.restype = I
+        _lib.orc_set_threads.argtypes = [I]
+        _lib.orc_get_threads.restype = I
+    return _lib
+
+
+def set_threads(n):
+    lib().orc_set_threads(int(n))
+
+
+def _ptr(a, dtype):
+    if a is None:
+        return None
+    assert a.dtype == dtype and a.flags.f_contiguous, "oracle arrays must be Fortran-ordered %s" % dtype
+    return a.ctypes.data
+
+
+def grid(np_, mp, lp, ih=1, ibcx=0, ibcy=0, ibcz=0):
+    return OrcGrid(np_, mp, lp, ih, ibcx, ibcy, ibcz)
+
+
+def advec_dwarf(g, x, x_lr, x_bt, uadv, vadv, wadv, rhr, rhoadv, legacyoptmode=4, t_adv=1,
+                iord=2, nonos=1, nsteps=1):
+    """In-place MPDATA step(s) on x; returns nothing, raises on a bad call."""
+    dt = x.dtype
+    fn = {np.float64: "orc_advec_steps_f64", np.float32: "orc_advec_steps_f32"}[dt.type]
+    rc = getattr(lib(), fn)(ctypes.byref(g), int(nsteps), int(legacyoptmode), int(t_adv), int(iord),
+                            int(nonos), _ptr(x, dt), _ptr(x_lr, dt), _ptr(x_bt, dt), _ptr(uadv, dt),
+                            _ptr(vadv, dt), _ptr(wadv, dt), _ptr(rhr, dt), _ptr(rhoadv, dt))
+    if rc != 0:
+        raise ValueError("oracle advec_dwarf failed with code %d" % rc)
+
+
+def upwind(g, x, bcx, bcy, u1, u2, u3, rhr, h):
+    xant = np.zeros_like(x, order="F")
+    d = np.float64
+    rc = lib().orc_upwind_f64(ctypes.byref(g), _ptr(x, d), _ptr(bcx, d), _ptr(bcy, d), _ptr(u1, d),
+                              _ptr(u2, d), _ptr(u3, d), _ptr(rhr, d), _ptr(h, d), _ptr(xant, d))
+    if rc != 0:
+        raise ValueError("oracle upwind failed with code %d" % rc)
+    return xant
+
+
+def velprd(g, ox, oy, oz, h, dxi, dyi, dzi, dt, dt_ratio, u1, u2, u3, u=None, v=None, w=None):
+    """Predictor in place: ox/oy/oz are (..., 3) level stacks, Fortran ordered."""
+    d = ox.dtype
+    fn = {np.float64: "orc_velprd_f64", np.float32: "orc_velprd_f32"}[d.type]
+    rc = getattr(lib(), fn)(ctypes.byref(g), _ptr(ox, d), _ptr(oy, d), _ptr(oz, d), _ptr(u, d),
+                            _ptr(v, d), _ptr(w, d), _ptr(h, d), dxi, dyi, dzi, dt, dt_ratio,
+                            _ptr(u1, d), _ptr(u2, d), _ptr(u3, d))
+    if rc != 0:
+        raise ValueError("oracle velprd failed with code %d" % rc)
+
+
+def a_to_c(g, uadv, vadv, wadv, u1, u2, u3):
+    d = np.float64
+    rc = lib().orc_a_to_c_f64(ctypes.byref(g), _ptr(uadv, d), _ptr(vadv, d), _ptr(wadv, d),
+                              _ptr(u1, d), _ptr(u2, d), _ptr(u3, d))
+    if rc != 0:
+        raise ValueError("oracle a_to_c failed with code %d" % rc)
