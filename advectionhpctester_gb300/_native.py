@@ -22,6 +22,11 @@ class MpdataGrid(ctypes.Structure):
     _fields_ = [("np", I), ("mp", I), ("lp", I), ("ih", I), ("ibcx", I), ("ibcy", I), ("ibcz", I)]
 
 
+class MpdataProblem(ctypes.Structure):
+    _fields_ = [("np", I), ("mp", I), ("lp", I), ("ibcx", I), ("ibcy", I), ("ibcz", I),
+                ("gauge", I), ("velocity_group", I)]
+
+
 class MpdataOpts(ctypes.Structure):
     _fields_ = [("iord", I), ("nonos", I), ("gauge", I), ("precision", I), ("predictor", I)]
 
@@ -37,11 +42,24 @@ SIGNATURES = {
     "mpdata_release_cached": ([], I),
     "mpdata_velprd_f64": ([P] * 8 + [D] * 5 + [P] * 4, I),
     "mpdata_velprd_f32": ([P] * 8 + [F] * 5 + [P] * 4, I),
+    "mpdata_rho_gauge_f64": ([P] * 20 + [D] * 5 + [I, P], I),
+    "mpdata_rho_gauge_f32": ([P] * 20 + [F] * 5 + [I, P], I),
     "mpdata_ws_error": ([P, ctypes.POINTER(I)], I),
     "mpdata_launch_count": ([], ctypes.c_longlong),
     "mpdata_ws_profile": ([P, I], I),
     "mpdata_ws_stage_times": ([P, I, ctypes.POINTER(D), ctypes.POINTER(ctypes.c_longlong)], I),
     "mpdata_stage_name": ([I], ctypes.c_char_p),
+    "mpdata_batch_create": ([I, ctypes.POINTER(MpdataProblem), I, I, I, I, ctypes.POINTER(P)], I),
+    "mpdata_batch_destroy": ([P], I),
+    "mpdata_batch_set": ([P, I] + [P] * 8, I),
+    "mpdata_batch_step": ([P, P], I),
+    "mpdata_batch_graph": ([P, I], I),
+    "mpdata_batch_tune": ([P, P, ctypes.POINTER(I), ctypes.POINTER(I)], I),
+    "mpdata_batch_profile": ([P, I], I),
+    "mpdata_batch_stage_times": ([P, I, ctypes.POINTER(D), ctypes.POINTER(ctypes.c_longlong)], I),
+    "mpdata_mass_f64": ([ctypes.POINTER(MpdataGrid), P, P, P, ctypes.POINTER(D), P], I),
+    "mpdata_mass_f32": ([ctypes.POINTER(MpdataGrid), P, P, P, ctypes.POINTER(D), P], I),
+    "mpdata_error_norms": ([ctypes.POINTER(MpdataGrid), P, I, P, I, ctypes.POINTER(D), P], I),
     "mpdata_strerror": ([I], ctypes.c_char_p),
     "mpdata_version": ([], ctypes.c_char_p),
 }

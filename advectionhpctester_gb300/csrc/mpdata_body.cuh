@@ -1,0 +1,450 @@
+// Per-cell bodies of the MPDATA stage kernels.
+//
+// One problem (a field on a grid, with its velocity, densities and scratch)
+// is described by Prob<R>; every stage body computes one cell (i,j,k) of one
+// problem.  The single-problem kernels pass Prob by value; the batched
+// kernels read it from a device table (many tracers sharing one velocity,
+// many independent domains), so both paths run the same arithmetic.
+//
+// Boundary conditions are index maps applied when a neighbour is read:
+//   psi halo     Dirichlet bcx/bcy (putbcinxh, mpdataoperators.inc:253-287) or wrap
+//   xant halo    reflection x(0)=x(2) (cp_scnd_last_to_halo_xy_fulld, :479-513) or wrap
+//   x_in halo    zero gradient x(0)=x(1) (cp_last_to_halo_xy, :551-584) or wrap
+//   face fields  0 on open x/y walls (flux_x_bcd/flux_y_bcd type 0, :673-811),
+//                mirrored on z walls (flux_z_bc_nohalod type 2, :903-947), or wrap
+// Face fields store the faces 1..n of their own axis; face n+1 is face 1
+// (periodic), zero (open wall) or minus face n (z wall).
+#pragma once
+#include "mpdata_common.cuh"
+
+namespace mpdata {
+
+template <class R>
+struct Prob {
+  Geo g;
+  int stdf;     // 1 = standard form (t_adv=2), 0 = infinite gauge (t_adv=1)
+  int own_vel;  // 1 = this problem writes the velocity-derived scratch (hinv, hm*)
+  int rho;      // density step of mpdata3d_rho_gauge_gpubc: no rhr, upwind fluxes kept
+  Arr<R> psi, u1, u2, u3, h, rhr;
+  const R* bcx;
+  const R* bcy;
+  Arr<R> hinv, hmx, hmy, hmz;  // may be shared by problems with one velocity
+  Arr<R> xant, v1, v2, v3, f1, f2, f3, w1, w2, w3, cp, cn, mx, mn, q;
+  // density step only: outputs and the upwind fluxes of the faces n+1
+  Arr<R> x_incomp, rhoadv, rhr_out, pexe, pexr1, pexr2;
+  R* f1hi;  // (mp,lp)
+  R* f2hi;  // (np,lp)
+  R* f3hi;  // (np,mp)
+};
+
+// ---- read helpers -------------------------------------------------------
+__device__ __forceinline__ int cx(const Geo& g, int i) { return g.bx ? wrapi(i, g.np) : clampi(i, g.np); }
+__device__ __forceinline__ int cy(const Geo& g, int j) { return g.by ? wrapi(j, g.mp) : clampi(j, g.mp); }
+__device__ __forceinline__ int cz(const Geo& g, int k) { return g.bz ? wrapi(k, g.lp) : clampi(k, g.lp); }
+
+// the current (antidiffused) field with the xant halo rule
+template <class R>
+__device__ __forceinline__ R xr(const Geo& g, const Arr<R>& X, int i, int j, int k) {
+  return X.ld(g.bx ? wrapi(i, g.np) : refl(i, g.np), g.by ? wrapi(j, g.mp) : refl(j, g.mp), cz(g, k));
+}
+
+// Face fields.  AIN = the caller's C-grid Courant numbers (faces 1..n+1 are
+// data on open axes); otherwise an antidiffusive field with the wall rule.
+template <class R, bool AIN>
+__device__ __forceinline__ R fx(const Geo& g, const Arr<R>& A, int f, int j, int k) {
+  j = cy(g, j);
+  k = cz(g, k);
+  if (g.bx) return A.ld(wrapi(f, g.np), j, k);
+  if (AIN) return A.ld(f, j, k);
+  return (f <= 1 || f > g.np) ? R(0) : A.ld(f, j, k);
+}
+template <class R, bool AIN>
+__device__ __forceinline__ R fy(const Geo& g, const Arr<R>& A, int i, int f, int k) {
+  i = cx(g, i);
+  k = cz(g, k);
+  if (g.by) return A.ld(i, wrapi(f, g.mp), k);
+  if (AIN) return A.ld(i, f, k);
+  return (f <= 1 || f > g.mp) ? R(0) : A.ld(i, f, k);
+}
+template <class R, bool AIN>
+__device__ __forceinline__ R fz(const Geo& g, const Arr<R>& A, int i, int j, int f) {
+  i = cx(g, i);
+  j = cy(g, j);
+  if (g.bz) return A.ld(i, j, wrapi(f, g.lp));
+  if (AIN) return A.ld(i, j, f);
+  if (f <= 1) return -A.ld(i, j, 2);
+  if (f > g.lp) return -A.ld(i, j, g.lp);
+  return A.ld(i, j, f);
+}
+
+// ---- upwind3d_gpubc (upwind3d-gpubc.f90:101-198) -------------------------
+// ANTIDIFF: an antidiffusive pass follows, so psi's open-wall halo ends the
+// step holding the zero-gradient copy of the old boundary values (written by
+// cp_last_to_halo_xy in the antidiffusion); otherwise it keeps bcx/bcy.
+// HALO: write psi's halo at all (off while autotuning).
+template <class R, bool ANTIDIFF, bool HALO>
+__device__ __forceinline__ void upwind_body(const Prob<R>& P, int i, int j, int k) {
+  const Geo& g = P.g;
+  const Arr<R>& psi = P.psi;
+  const R x = psi.ld(i, j, k);
+  const long bx0 = (long)(j - 1) + (long)g.mp * (k - 1), bxs = (long)g.mp * g.lp;
+  const long by0 = (long)(i - 1) + (long)g.np * (k - 1), bys = (long)g.np * g.lp;
+  const R xim = i > 1 ? psi.ld(i - 1, j, k) : (g.bx ? psi.ld(g.np, j, k) : P.bcx[bx0]);
+  const R xip = i < g.np ? psi.ld(i + 1, j, k) : (g.bx ? psi.ld(1, j, k) : P.bcx[bx0 + bxs]);
+  const R xjm = j > 1 ? psi.ld(i, j - 1, k) : (g.by ? psi.ld(i, g.mp, k) : P.bcy[by0]);
+  const R xjp = j < g.mp ? psi.ld(i, j + 1, k) : (g.by ? psi.ld(i, 1, k) : P.bcy[by0 + bys]);
+  const R hc = P.h.ld(i, j, k);
+  const R hi = R(1) / hc;
+  const R f1p = donor(x, xip, fx<R, true>(g, P.u1, i + 1, j, k));
+  const R f1 = donor(xim, x, P.u1.ld(i, j, k));
+  const R f2p = donor(x, xjp, fy<R, true>(g, P.u2, i, j + 1, k));
+  const R f2 = donor(xjm, x, P.u2.ld(i, j, k));
+  R f3p, f3;
+  if (!g.bz && k == 1) {  // :134-135
+    f3p = donor(x, psi.ld(i, j, k + 1), P.u3.ld(i, j, k + 1));
+    f3 = -f3p;
+  } else if (!g.bz && k == g.lp) {  // :164-165
+    f3 = donor(psi.ld(i, j, k - 1), x, P.u3.ld(i, j, k));
+    f3p = -f3;
+  } else {
+    f3p = donor(x, psi.ld(i, j, cz(g, k + 1)), fz<R, true>(g, P.u3, i, j, k + 1));
+    f3 = donor(psi.ld(i, j, cz(g, k - 1)), x, P.u3.ld(i, j, k));
+  }
+  if (P.rho) {
+    // mpdata3d-rho-gauge-gpubc.f90:137-210: no rhr, division by h, fluxes kept;
+    // rhoadv takes the input x_incomp (:121-123)
+    P.xant.at(i, j, k) = x - (f1p - f1 + f2p - f2 + f3p - f3) / hc;
+    P.f1.at(i, j, k) = f1;
+    P.f2.at(i, j, k) = f2;
+    P.f3.at(i, j, k) = f3;
+    if (i == g.np) P.f1hi[(j - 1) + (long)g.mp * (k - 1)] = f1p;
+    if (j == g.mp) P.f2hi[(i - 1) + (long)g.np * (k - 1)] = f2p;
+    if (k == g.lp) P.f3hi[(i - 1) + (long)g.np * (j - 1)] = f3p;
+    P.rhoadv.at(i, j, k) = P.x_incomp.ld(i, j, k);
+  } else {
+    P.xant.at(i, j, k) = P.rhr.ld(i, j, k) * (x - (f1p - f1 + f2p - f2 + f3p - f3) * hi);
+  }
+  if (ANTIDIFF && P.own_vel) {
+    P.hinv.at(i, j, k) = hi;
+    // reciprocal mean densities of the cell's lower faces, used by every
+    // corrective pass of this step (hmx/hmy/hmz of antidiff3d-*-gpubc.f90)
+    if (g.bx || i > 1) P.hmx.at(i, j, k) = rhm(P.h.ld(cx(g, i - 1), j, k), hc);
+    if (g.by || j > 1) P.hmy.at(i, j, k) = rhm(P.h.ld(i, cy(g, j - 1), k), hc);
+    if (g.bz || k > 1) P.hmz.at(i, j, k) = rhm(P.h.ld(i, j, cz(g, k - 1)), hc);
+  }
+  if (HALO) {
+    if (!g.bx) {
+      if (i == 1) psi.at(0, j, k) = ANTIDIFF ? x : xim;
+      if (i == g.np) psi.at(g.np + 1, j, k) = ANTIDIFF ? x : xip;
+    }
+    if (!g.by) {
+      if (j == 1) psi.at(i, 0, k) = ANTIDIFF ? x : xjm;
+      if (j == g.mp) psi.at(i, g.mp + 1, k) = ANTIDIFF ? x : xjp;
+    }
+  }
+}
+
+// ---- antidiffusive pseudo-velocities --------------------------------------
+// standard form: antidiff3d-standard-gpubc.f90:72-203; gauge form:
+// antidiff3d-gauge-gpubc.f90:89-203.  The k=1 and k=lp planes of a z wall
+// drop the z cross terms of v1/v2, as the reference's boundary kernels do.
+// Each cell computes its lower faces.  AIN: the first corrective pass, whose
+// "a" velocities are the caller's Courant numbers; later passes use the
+// previous pass's limited velocities w1..w3.
+template <class R, bool STD, bool AIN>
+__device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int k) {
+  const Geo& g = P.g;
+  const Arr<R>& X = P.xant;
+  const Arr<R>& A1 = AIN ? P.u1 : P.w1;
+  const Arr<R>& A2 = AIN ? P.u2 : P.w2;
+  const Arr<R>& A3 = AIN ? P.u3 : P.w3;
+  const R ep = Eps<R>::v;
+  const bool zt = g.bz || (k > 1 && k < g.lp);
+#define XX(a, b, c) xr<R>(g, X, (a), (b), (c))
+#define AX(f, b, c) fx<R, AIN>(g, A1, (f), (b), (c))
+#define AY(a, f, c) fy<R, AIN>(g, A2, (a), (f), (c))
+#define AZ(a, b, f) fz<R, AIN>(g, A3, (a), (b), (f))
+  if (g.bx || i > 1) {
+    const R hmx = P.hmx.ld(i, j, k);
+    const R a = AX(i, j, k);
+    R v;
+    if (STD) {
+      v = vdyfa(XX(i - 1, j, k), XX(i, j, k), a, hmx, ep) +
+          vcorra(a, AY(i - 1, j, k) + AY(i - 1, j + 1, k) + AY(i, j + 1, k) + AY(i, j, k),
+                 (fabs(XX(i - 1, j + 1, k)) + fabs(XX(i, j + 1, k))) -
+                     (fabs(XX(i - 1, j - 1, k)) + fabs(XX(i, j - 1, k))),
+                 fabs(XX(i - 1, j + 1, k)) + fabs(XX(i, j + 1, k)) + fabs(XX(i - 1, j - 1, k)) +
+                     fabs(XX(i, j - 1, k)) + ep,
+                 hmx);
+      if (zt)
+        v = v + vcorra(a, AZ(i - 1, j, k) + AZ(i - 1, j, k + 1) + AZ(i, j, k + 1) + AZ(i, j, k),
+                       (fabs(XX(i - 1, j, k + 1)) + fabs(XX(i, j, k + 1))) -
+                           (fabs(XX(i - 1, j, k - 1)) + fabs(XX(i, j, k - 1))),
+                       fabs(XX(i - 1, j, k + 1)) + fabs(XX(i, j, k + 1)) + fabs(XX(i - 1, j, k - 1)) +
+                           fabs(XX(i, j, k - 1)) + ep,
+                       hmx);
+      P.f1.at(i, j, k) = donor(XX(i - 1, j, k), XX(i, j, k), v);
+    } else {
+      const R c2 = (AY(i - 1, j, k) + AY(i - 1, j + 1, k) + AY(i, j + 1, k) + AY(i, j, k)) *
+                   rat4(XX(i - 1, j - 1, k), XX(i, j - 1, k), XX(i - 1, j + 1, k), XX(i, j + 1, k));
+      R cr = c2;
+      if (zt)
+        cr = c2 + (AZ(i - 1, j, k) + AZ(i - 1, j, k + 1) + AZ(i, j, k + 1) + AZ(i, j, k)) *
+                      rat4(XX(i - 1, j, k - 1), XX(i, j, k - 1), XX(i - 1, j, k + 1), XX(i, j, k + 1));
+      v = vdyf(XX(i - 1, j, k), XX(i, j, k), a, hmx) - R(0.125) * a * hmx * cr;
+    }
+    P.v1.at(i, j, k) = v;
+  }
+  if (g.by || j > 1) {
+    const R hmy = P.hmy.ld(i, j, k);
+    const R a = AY(i, j, k);
+    R v;
+    if (STD) {
+      v = vdyfa(XX(i, j - 1, k), XX(i, j, k), a, hmy, ep) +
+          vcorra(a, AX(i, j - 1, k) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j - 1, k),
+                 (fabs(XX(i + 1, j - 1, k)) + fabs(XX(i + 1, j, k))) -
+                     (fabs(XX(i - 1, j - 1, k)) + fabs(XX(i - 1, j, k))),
+                 fabs(XX(i + 1, j - 1, k)) + fabs(XX(i + 1, j, k)) + fabs(XX(i - 1, j - 1, k)) +
+                     fabs(XX(i - 1, j, k)) + ep,
+                 hmy);
+      if (zt)
+        v = v + vcorra(a, AZ(i, j - 1, k) + AZ(i, j, k) + AZ(i, j, k + 1) + AZ(i, j - 1, k + 1),
+                       (fabs(XX(i, j - 1, k + 1)) + fabs(XX(i, j, k + 1))) -
+                           (fabs(XX(i, j - 1, k - 1)) + fabs(XX(i, j, k - 1))),
+                       fabs(XX(i, j - 1, k + 1)) + fabs(XX(i, j, k + 1)) + fabs(XX(i, j - 1, k - 1)) +
+                           fabs(XX(i, j, k - 1)) + ep,
+                       hmy);
+      P.f2.at(i, j, k) = donor(XX(i, j - 1, k), XX(i, j, k), v);
+    } else {
+      const R c1 = (AX(i, j - 1, k) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j - 1, k)) *
+                   rat4(XX(i - 1, j - 1, k), XX(i - 1, j, k), XX(i + 1, j - 1, k), XX(i + 1, j, k));
+      R cr = c1;
+      if (zt)
+        cr = c1 + (AZ(i, j - 1, k) + AZ(i, j, k) + AZ(i, j, k + 1) + AZ(i, j - 1, k + 1)) *
+                      rat4(XX(i, j - 1, k - 1), XX(i, j, k - 1), XX(i, j - 1, k + 1), XX(i, j, k + 1));
+      v = vdyf(XX(i, j - 1, k), XX(i, j, k), a, hmy) - R(0.125) * a * hmy * cr;
+    }
+    P.v2.at(i, j, k) = v;
+  }
+  if (g.bz || k > 1) {
+    const R hmz = P.hmz.ld(i, j, k);
+    const R a = AZ(i, j, k);
+    R v;
+    if (STD) {
+      v = vdyfa(XX(i, j, k - 1), XX(i, j, k), a, hmz, ep) +
+          vcorra(a, AX(i, j, k - 1) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j, k - 1),
+                 (fabs(XX(i + 1, j, k - 1)) + fabs(XX(i + 1, j, k))) -
+                     (fabs(XX(i - 1, j, k - 1)) + fabs(XX(i - 1, j, k))),
+                 fabs(XX(i + 1, j, k - 1)) + fabs(XX(i + 1, j, k)) + fabs(XX(i - 1, j, k - 1)) +
+                     fabs(XX(i - 1, j, k)) + ep,
+                 hmz) +
+          vcorra(a, AY(i, j, k - 1) + AY(i, j + 1, k - 1) + AY(i, j + 1, k) + AY(i, j, k),
+                 (fabs(XX(i, j + 1, k - 1)) + fabs(XX(i, j + 1, k))) -
+                     (fabs(XX(i, j - 1, k - 1)) + fabs(XX(i, j - 1, k))),
+                 fabs(XX(i, j + 1, k - 1)) + fabs(XX(i, j + 1, k)) + fabs(XX(i, j - 1, k - 1)) +
+                     fabs(XX(i, j - 1, k)) + ep,
+                 hmz);
+      P.f3.at(i, j, k) = donor(XX(i, j, k - 1), XX(i, j, k), v);
+    } else {
+      const R cr = (AX(i, j, k - 1) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j, k - 1)) *
+                       rat4(XX(i - 1, j, k - 1), XX(i - 1, j, k), XX(i + 1, j, k - 1), XX(i + 1, j, k)) +
+                   (AY(i, j, k - 1) + AY(i, j + 1, k - 1) + AY(i, j + 1, k) + AY(i, j, k)) *
+                       rat4(XX(i, j - 1, k - 1), XX(i, j - 1, k), XX(i, j + 1, k - 1), XX(i, j + 1, k));
+      v = vdyf(XX(i, j, k - 1), XX(i, j, k), a, hmz) - R(0.125) * a * hmz * cr;
+    }
+    P.v3.at(i, j, k) = v;
+  }
+#undef XX
+#undef AX
+#undef AY
+#undef AZ
+}
+
+template <class R, bool AIN>
+__device__ __forceinline__ void pseudo_body(const Prob<R>& P, int i, int j, int k) {
+  if (P.stdf)
+    pseudo_form<R, true, AIN>(P, i, j, k);
+  else
+    pseudo_form<R, false, AIN>(P, i, j, k);
+}
+
+// ---- limiter bounds and ratios (std :256-348, gauge :238-324) -------------
+// FIRST folds the star of the step's input field x_in (zero-gradient halo)
+// into the bounds, as every first corrective pass does; later passes start
+// from the stored running extrema (KEEP stores them).  The gauge k=1 minimum
+// over x_in, which the reference leaves unset (antidiff3d-gauge-gpubc.f90:249),
+// is computed as in mpdata3d-rho-gauge-gpubc.f90:365-368.  Also stores
+// q = x/rhr, the ratio every later stage divides out.
+template <class R, bool NONOS, bool FIRST, bool KEEP>
+__device__ __forceinline__ void bounds_body(const Prob<R>& P, int i, int j, int k) {
+  const Geo& g = P.g;
+  const Arr<R>& X = P.xant;
+  const R x = X.ld(i, j, k);
+  P.q.at(i, j, k) = P.rho ? x : x / P.rhr.ld(i, j, k);  // x/1 == x for the density step
+  if (!NONOS) return;
+  const bool lo = g.bz || k > 1, hi = g.bz || k < g.lp;
+  R ma, mi;
+  if (FIRST) {
+    const Arr<R>& xin = P.psi;
+    const int im = g.bx ? wrapi(i - 1, g.np) : clampi(i - 1, g.np);
+    const int ip = g.bx ? wrapi(i + 1, g.np) : clampi(i + 1, g.np);
+    const int jm = g.by ? wrapi(j - 1, g.mp) : clampi(j - 1, g.mp);
+    const int jp = g.by ? wrapi(j + 1, g.mp) : clampi(j + 1, g.mp);
+    Extrema<R> e(xin.ld(i, j, k));
+    e.add(xin.ld(im, j, k));
+    e.add(xin.ld(ip, j, k));
+    e.add(xin.ld(i, jm, k));
+    e.add(xin.ld(i, jp, k));
+    if (lo) e.add(xin.ld(i, j, cz(g, k - 1)));
+    if (hi) e.add(xin.ld(i, j, cz(g, k + 1)));
+    e.add(x);
+    e.add(xr<R>(g, X, i - 1, j, k));
+    e.add(xr<R>(g, X, i + 1, j, k));
+    e.add(xr<R>(g, X, i, j - 1, k));
+    e.add(xr<R>(g, X, i, j + 1, k));
+    if (lo) e.add(X.ld(i, j, cz(g, k - 1)));
+    if (hi) e.add(X.ld(i, j, cz(g, k + 1)));
+    ma = e.max();
+    mi = e.min();
+  } else {
+    Extrema<R> e(x);
+    e.add(xr<R>(g, X, i - 1, j, k));
+    e.add(xr<R>(g, X, i + 1, j, k));
+    e.add(xr<R>(g, X, i, j - 1, k));
+    e.add(xr<R>(g, X, i, j + 1, k));
+    if (lo) e.add(X.ld(i, j, cz(g, k - 1)));
+    if (hi) e.add(X.ld(i, j, cz(g, k + 1)));
+    ma = mx2(P.mx.ld(i, j, k), e.max());
+    mi = mn2(P.mn.ld(i, j, k), e.min());
+  }
+  if (KEEP) {
+    P.mx.at(i, j, k) = ma;
+    P.mn.at(i, j, k) = mi;
+  }
+  // fluxes for the bounds: std -> donor fluxes f*ns, gauge -> v itself
+  const Arr<R>& F1 = P.stdf ? P.f1 : P.v1;
+  const Arr<R>& F2 = P.stdf ? P.f2 : P.v2;
+  const Arr<R>& F3 = P.stdf ? P.f3 : P.v3;
+  const R ep = Eps<R>::v;
+  const R e1 = fx<R, false>(g, F1, i + 1, j, k), w1 = fx<R, false>(g, F1, i, j, k);
+  const R e2 = fy<R, false>(g, F2, i, j + 1, k), w2 = fy<R, false>(g, F2, i, j, k);
+  const R e3 = fz<R, false>(g, F3, i, j, k + 1), w3 = fz<R, false>(g, F3, i, j, k);
+  const R hc = P.h.ld(i, j, k);
+  P.cp.at(i, j, k) = (ma - x) * hc / (pn(e1) + pp(w1) + pn(e2) + pp(w2) + pn(e3) + pp(w3) + ep);
+  P.cn.at(i, j, k) = (x - mi) * hc / (pp(e1) + pn(w1) + pp(e2) + pn(w2) + pp(e3) + pn(w3) + ep);
+}
+
+// ---- limited antidiffusive velocities and fluxes --------------------------
+// std: antidiff3d-standard-gpubc.f90:372-407 (sign-aware limited velocity,
+// donor flux of x/rhr); gauge: antidiff3d-gauge-gpubc.f90:343-363 (the
+// limited velocity is the flux).  Lower faces of each cell.
+template <class R>
+__device__ __forceinline__ R vlim_std(R v, R a1, R a2, R xl, R xrr) {
+  return pp(v) * (a1 * possign(xl) + a2 * possign(-xl)) - pn(v) * (a2 * possign(xrr) + a1 * possign(-xrr));
+}
+
+template <class R, bool STD, bool NONOS>
+__device__ __forceinline__ void limit_form(const Prob<R>& P, int i, int j, int k) {
+  const Geo& g = P.g;
+  const Arr<R>& X = P.xant;
+  const R cpc = NONOS ? P.cp.ld(i, j, k) : R(0), cnc = NONOS ? P.cn.ld(i, j, k) : R(0);
+  const R xc = X.ld(i, j, k), qc = STD ? P.q.ld(i, j, k) : R(0);
+  if (g.bx || i > 1) {
+    const int im = wrapi(i - 1, g.np);
+    const R v = P.v1.ld(i, j, k);
+    R w = v;
+    if (NONOS) {
+      const R cpm = P.cp.ld(im, j, k), cnm = P.cn.ld(im, j, k);
+      w = STD ? vlim_std(v, min3(cpc, cnm), min3(cpm, cnc), X.ld(im, j, k), xc)
+              : pp(v) * min3(cpc, cnm) - pn(v) * min3(cpm, cnc);
+    }
+    P.w1.at(i, j, k) = w;
+    if (STD) P.f1.at(i, j, k) = donor(P.q.ld(im, j, k), qc, w);
+  }
+  if (g.by || j > 1) {
+    const int jm = wrapi(j - 1, g.mp);
+    const R v = P.v2.ld(i, j, k);
+    R w = v;
+    if (NONOS) {
+      const R cpm = P.cp.ld(i, jm, k), cnm = P.cn.ld(i, jm, k);
+      w = STD ? vlim_std(v, min3(cpc, cnm), min3(cpm, cnc), X.ld(i, jm, k), xc)
+              : pp(v) * min3(cpc, cnm) - pn(v) * min3(cpm, cnc);
+    }
+    P.w2.at(i, j, k) = w;
+    if (STD) P.f2.at(i, j, k) = donor(P.q.ld(i, jm, k), qc, w);
+  }
+  if (g.bz || k > 1) {
+    const int km = wrapi(k - 1, g.lp);
+    const R v = P.v3.ld(i, j, k);
+    R w = v;
+    if (NONOS) {
+      const R cpm = P.cp.ld(i, j, km), cnm = P.cn.ld(i, j, km);
+      w = STD ? vlim_std(v, min3(cpc, cnm), min3(cpm, cnc), X.ld(i, j, km), xc)
+              : pp(v) * min3(cpc, cnm) - pn(v) * min3(cpm, cnc);
+    }
+    P.w3.at(i, j, k) = w;
+    if (STD) P.f3.at(i, j, k) = donor(P.q.ld(i, j, km), qc, w);
+  }
+}
+
+template <class R, bool NONOS>
+__device__ __forceinline__ void limit_body(const Prob<R>& P, int i, int j, int k) {
+  if (P.stdf)
+    limit_form<R, true, NONOS>(P, i, j, k);
+  else
+    limit_form<R, false, NONOS>(P, i, j, k);
+}
+
+// ---- corrective update (std :431-459, gauge :364-368/396-400/423-427) -----
+// LAST: the last pass writes psi; earlier passes overwrite xant in place (the
+// update reads q, not x).
+template <class R, bool LAST>
+__device__ __forceinline__ void update_body(const Prob<R>& P, int i, int j, int k) {
+  const Geo& g = P.g;
+  const Arr<R>& out = LAST ? P.psi : P.xant;
+  if (P.stdf) {
+    const R d = fx<R, false>(g, P.f1, i + 1, j, k) - fx<R, false>(g, P.f1, i, j, k) +
+                fy<R, false>(g, P.f2, i, j + 1, k) - fy<R, false>(g, P.f2, i, j, k) +
+                fz<R, false>(g, P.f3, i, j, k + 1) - fz<R, false>(g, P.f3, i, j, k);
+    out.at(i, j, k) = P.rhr.ld(i, j, k) * (P.q.ld(i, j, k) - d * P.hinv.ld(i, j, k));
+  } else {
+    const R d = fx<R, false>(g, P.w1, i + 1, j, k) - fx<R, false>(g, P.w1, i, j, k) +
+                fy<R, false>(g, P.w2, i, j + 1, k) - fy<R, false>(g, P.w2, i, j, k) +
+                fz<R, false>(g, P.w3, i, j, k + 1) - fz<R, false>(g, P.w3, i, j, k);
+    const R t = P.q.ld(i, j, k) - d / P.h.ld(i, j, k);
+    out.at(i, j, k) = P.rho ? t : P.rhr.ld(i, j, k) * t;  // rhr == 1 in the density step
+  }
+}
+
+// ---- outputs of the density step (mpdata3d-rho-gauge-gpubc.f90:486-606) ----
+// x_incomp = x*h, pexr1 = x_incomp*pexe, pexr2 = x_incomp, rhr = rhoadv/x_incomp,
+// and the mass fluxes u = upwind flux + limited antidiffusive flux on the
+// cell's lower faces (and the faces n+1 on the last cells).  LINER: the
+// upwind-only branch (:594-606), where psi still has to take xant.
+template <class R, bool LINER>
+__device__ __forceinline__ void rho_out_body(const Prob<R>& P, int i, int j, int k) {
+  const Geo& g = P.g;
+  if (LINER) P.psi.at(i, j, k) = P.xant.ld(i, j, k);
+  const R xv = LINER ? P.xant.ld(i, j, k) : P.psi.ld(i, j, k);
+  const R xc = xv * P.h.ld(i, j, k);
+  P.x_incomp.at(i, j, k) = xc;
+  P.pexr1.at(i, j, k) = xc * P.pexe.ld(i, j, k);
+  P.pexr2.at(i, j, k) = xc;
+  P.rhr_out.at(i, j, k) = P.rhoadv.ld(i, j, k) / xc;
+  P.u1.at(i, j, k) = P.f1.ld(i, j, k) + (LINER ? R(0) : fx<R, false>(g, P.w1, i, j, k));
+  P.u2.at(i, j, k) = P.f2.ld(i, j, k) + (LINER ? R(0) : fy<R, false>(g, P.w2, i, j, k));
+  P.u3.at(i, j, k) = P.f3.ld(i, j, k) + (LINER ? R(0) : fz<R, false>(g, P.w3, i, j, k));
+  if (i == g.np)
+    P.u1.at(g.np + 1, j, k) = P.f1hi[(j - 1) + (long)g.mp * (k - 1)] + (LINER ? R(0) : fx<R, false>(g, P.w1, g.np + 1, j, k));
+  if (j == g.mp)
+    P.u2.at(i, g.mp + 1, k) = P.f2hi[(i - 1) + (long)g.np * (k - 1)] + (LINER ? R(0) : fy<R, false>(g, P.w2, i, g.mp + 1, k));
+  if (k == g.lp)
+    P.u3.at(i, j, g.lp + 1) = P.f3hi[(i - 1) + (long)g.np * (j - 1)] + (LINER ? R(0) : fz<R, false>(g, P.w3, i, j, g.lp + 1));
+}
+
+template <class R>
+__device__ __forceinline__ void copy_body(const Prob<R>& P, int i, int j, int k) {
+  P.psi.at(i, j, k) = P.xant.ld(i, j, k);
+}
+
+}  // namespace mpdata

@@ -4,6 +4,7 @@
 // options, advec.f90:174,203,210).
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -16,10 +17,21 @@
 
 using namespace mpdata;
 
+namespace mpdata {
+template <class R>
+int batch_occupancy(int threads);
+template <class R>
+int run_reduce(Geo g, int mode, const R* a, const R* h, const R* rhr, const void* b, int b_is_f64,
+               double* part, double* out, cudaStream_t s);
+int reduce_blocks();
+}
+
 namespace {
 
 constexpr uint32_t WS_MAGIC = 0x4d504454u;  // "MPDT"
-constexpr int NSCRATCH = 16;                // xant hinv v1..3 f1..3 w1..3 cp cn mx mn q
+constexpr int NFIELD = 15;  // per problem: xant v1..3 f1..3 w1..3 cp cn mx mn q
+constexpr int NVEL = 4;     // per velocity: hinv hmx hmy hmz
+constexpr int NSCRATCH = NFIELD + NVEL;
 
 // Pool-backed event timer: one (start, stop) pair per recorded launch,
 // harvested and recycled when the host asks for the totals.
@@ -72,6 +84,7 @@ struct Workspace {
   mpdata_grid g;
   mpdata_opts o;
   size_t ncell;
+  size_t nhi;  // faces n+1 of the density step's upwind fluxes
   size_t elem;
   void* mem;
   int* d_err;
@@ -110,17 +123,19 @@ Workspace* as_ws(void* p) {
 
 Geo geo_of(const mpdata_grid& g) { return Geo{g.np, g.mp, g.lp, g.ih, g.ibcx, g.ibcy, g.ibcz}; }
 
+// Descriptor of one problem: caller arrays (Fortran layout views) and
+// scratch fields carved from `base` (interior-shaped, ncell elements each).
 template <class R>
-StepPlan<R> make_plan(Workspace* w, R* psi, const R* u1, const R* u2, const R* u3, const R* h,
-                      const R* rhr, const R* bcx, const R* bcy) {
-  const mpdata_grid& g = w->g;
+Prob<R> make_prob(const mpdata_grid& g, int gauge, R* psi, const R* u1, const R* u2, const R* u3,
+                  const R* h, const R* rhr, const R* bcx, const R* bcy, R* base, size_t ncell,
+                  R* vel_base, int own_vel) {
   const int ih = g.ih;
   const int sx = g.np + 2 * ih, sy = g.mp + 2 * ih;
-  StepPlan<R> P;
+  Prob<R> P;
+  memset(&P, 0, sizeof P);
   P.g = geo_of(g);
-  P.iord = w->o.iord;
-  P.nonos = w->o.nonos;
-  P.gauge = w->o.gauge;
+  P.stdf = gauge ? 0 : 1;
+  P.own_vel = own_vel;
   P.psi = caller_view<R>(psi, ih, sx, sy);
   P.u1 = caller_view<R>(const_cast<R*>(u1), ih, sx + 1, sy);
   P.u2 = caller_view<R>(const_cast<R*>(u2), ih, sx, sy + 1);
@@ -129,11 +144,11 @@ StepPlan<R> make_plan(Workspace* w, R* psi, const R* u1, const R* u2, const R* u
   P.rhr = caller_view<R>(const_cast<R*>(rhr), ih, sx, sy);
   P.bcx = bcx;
   P.bcy = bcy;
-  R* base = static_cast<R*>(w->mem);
-  Arr<R>* slots[NSCRATCH] = {&P.xant, &P.hinv, &P.v1, &P.v2, &P.v3, &P.f1, &P.f2, &P.f3,
-                             &P.w1,   &P.w2,   &P.w3, &P.cp, &P.cn, &P.mx, &P.mn, &P.q};
-  for (int s = 0; s < NSCRATCH; s++) *slots[s] = scratch_view<R>(base + (size_t)s * w->ncell, P.g);
-  P.prof = w->prof;
+  Arr<R>* vel[NVEL] = {&P.hinv, &P.hmx, &P.hmy, &P.hmz};
+  for (int s = 0; s < NVEL; s++) *vel[s] = scratch_view<R>(vel_base + (size_t)s * ncell, P.g);
+  Arr<R>* slots[NFIELD] = {&P.xant, &P.v1, &P.v2, &P.v3, &P.f1, &P.f2, &P.f3, &P.w1,
+                           &P.w2,   &P.w3, &P.cp, &P.cn, &P.mx, &P.mn, &P.q};
+  for (int s = 0; s < NFIELD; s++) *slots[s] = scratch_view<R>(base + (size_t)s * ncell, P.g);
   return P;
 }
 
@@ -147,8 +162,10 @@ int step_impl(void* ws, R* psi, const R* u1, const R* u2, const R* u3, const R* 
   if ((!w->g.ibcx && !bcx) || (!w->g.ibcy && !bcy)) return MPDATA_E_NULL;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   w->last = s;
-  StepPlan<R> P = make_plan<R>(w, psi, u1, u2, u3, h, rhr, bcx, bcy);
-  return run_step<R>(P, s) == 0 ? MPDATA_OK : MPDATA_E_CUDA;
+  R* base = static_cast<R*>(w->mem);
+  Prob<R> P = make_prob<R>(w->g, w->o.gauge, psi, u1, u2, u3, h, rhr, bcx, bcy, base, w->ncell,
+                           base + (size_t)NFIELD * w->ncell, 1);
+  return run_step<R>(P, w->o.iord, w->o.nonos, w->prof, s) == 0 ? MPDATA_OK : MPDATA_E_CUDA;
 }
 
 template <class R>
@@ -184,6 +201,39 @@ int velprd_impl(void* ws, R* ox, R* oy, R* oz, R* u, R* v, R* wv, const R* h, R 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   w->last = s;
   return run_predictor<R>(P, s) == 0 ? MPDATA_OK : MPDATA_E_CUDA;
+}
+
+// mpdata3d_rho_gauge_gpubc: predictor, density step, outputs.
+template <class R>
+int rho_impl(void* ws, R* ox, R* oy, R* oz, R* u, R* v, R* wv, R* u1, R* u2, R* u3, R* x_in, R* x_incomp,
+             const R* h, R* rhoadv, R* rhr, const R* pexe, R* pexr1, R* pexr2, const R* bcx, const R* bcy,
+             R dxi, R dyi, R dzi, R dt, R dt_ratio, int liner, void* stream) {
+  Workspace* w = as_ws(ws);
+  if (!w) return MPDATA_E_WS;
+  if (w->elem != sizeof(R)) return MPDATA_E_WS;
+  if (!w->o.gauge) return MPDATA_E_OPTS;  // the reference's density step is the gauge form
+  if (!x_in || !x_incomp || !h || !rhoadv || !rhr || !pexe || !pexr1 || !pexr2) return MPDATA_E_NULL;
+  if ((!w->g.ibcx && !bcx) || (!w->g.ibcy && !bcy)) return MPDATA_E_NULL;
+  int rc = velprd_impl<R>(ws, ox, oy, oz, u, v, wv, h, dxi, dyi, dzi, dt, dt_ratio, u1, u2, u3, stream);
+  if (rc) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  R* base = static_cast<R*>(w->mem);
+  Prob<R> P = make_prob<R>(w->g, 1, x_in, u1, u2, u3, h, h, bcx, bcy, base, w->ncell,
+                           base + (size_t)NFIELD * w->ncell, 1);
+  const mpdata_grid& g = w->g;
+  const int ih = g.ih, sx = g.np + 2 * ih, sy = g.mp + 2 * ih;
+  P.rho = 1;
+  P.x_incomp = caller_view<R>(x_incomp, ih, sx, sy);
+  P.rhoadv = caller_view<R>(rhoadv, ih, sx, sy);
+  P.rhr_out = caller_view<R>(rhr, ih, sx, sy);
+  P.pexe = caller_view<R>(const_cast<R*>(pexe), ih, sx, sy);
+  P.pexr1 = caller_view<R>(pexr1, ih, sx, sy);
+  P.pexr2 = caller_view<R>(pexr2, ih, sx, sy);
+  R* hi = base + (size_t)NSCRATCH * w->ncell;
+  P.f1hi = hi;
+  P.f2hi = hi + (size_t)g.mp * g.lp;
+  P.f3hi = hi + (size_t)g.mp * g.lp + (size_t)g.np * g.lp;
+  return run_step<R>(P, liner ? 1 : w->o.iord, w->o.nonos, w->prof, s) == 0 ? MPDATA_OK : MPDATA_E_CUDA;
 }
 
 // The reference keeps its scratch in module globals allocated once per grid;
@@ -249,7 +299,8 @@ int mpdata_ws_create(const mpdata_grid* grid, const mpdata_opts* opts, void** ws
   w->elem = opts->precision == 64 ? sizeof(double) : sizeof(float);
   w->last = nullptr;
   w->prof = nullptr;
-  if (cudaMalloc(&w->mem, w->ncell * w->elem * NSCRATCH) != cudaSuccess) {
+  w->nhi = (size_t)grid->mp * grid->lp + (size_t)grid->np * grid->lp + (size_t)grid->np * grid->mp;
+  if (cudaMalloc(&w->mem, (w->ncell * NSCRATCH + w->nhi) * w->elem) != cudaSuccess) {
     cudaGetLastError();
     delete w;
     return MPDATA_E_CUDA;
@@ -338,6 +389,23 @@ int mpdata_velprd_f32(void* ws, float* ox, float* oy, float* oz, float* u, float
   return velprd_impl<float>(ws, ox, oy, oz, u, v, w, h, dxi, dyi, dzi, dt, dt_ratio, u1, u2, u3, stream);
 }
 
+int mpdata_rho_gauge_f64(void* ws, double* ox, double* oy, double* oz, double* u, double* v, double* w,
+                         double* u1, double* u2, double* u3, double* x_in, double* x_incomp,
+                         const double* h, double* rhoadv, double* rhr, const double* pexe, double* pexr1,
+                         double* pexr2, const double* bcx, const double* bcy, double dxi, double dyi,
+                         double dzi, double dt, double dt_ratio, int liner, void* stream) {
+  return rho_impl<double>(ws, ox, oy, oz, u, v, w, u1, u2, u3, x_in, x_incomp, h, rhoadv, rhr, pexe, pexr1,
+                          pexr2, bcx, bcy, dxi, dyi, dzi, dt, dt_ratio, liner, stream);
+}
+int mpdata_rho_gauge_f32(void* ws, float* ox, float* oy, float* oz, float* u, float* v, float* w,
+                         float* u1, float* u2, float* u3, float* x_in, float* x_incomp, const float* h,
+                         float* rhoadv, float* rhr, const float* pexe, float* pexr1, float* pexr2,
+                         const float* bcx, const float* bcy, float dxi, float dyi, float dzi, float dt,
+                         float dt_ratio, int liner, void* stream) {
+  return rho_impl<float>(ws, ox, oy, oz, u, v, w, u1, u2, u3, x_in, x_incomp, h, rhoadv, rhr, pexe, pexr1,
+                         pexr2, bcx, bcy, dxi, dyi, dzi, dt, dt_ratio, liner, stream);
+}
+
 int mpdata_ws_error(void* ws, int* error_word) {
   Workspace* w = as_ws(ws);
   if (!w) return MPDATA_E_WS;
@@ -384,7 +452,7 @@ int mpdata_ws_stage_times(void* ws, int nstages, double* total_ms, long long* la
 const char* mpdata_stage_name(int stage) {
   static const char* names[NSTAGE] = {"upwind", "pseudo_velocity", "limiter_bounds", "limited_flux",
                                       "corrective_update", "copy", "predictor_level",
-                                      "predictor_cgrid"};
+                                      "predictor_cgrid", "density_outputs"};
   return (stage >= 0 && stage < NSTAGE) ? names[stage] : "";
 }
 
@@ -403,5 +471,427 @@ const char* mpdata_strerror(int code) {
 }
 
 const char* mpdata_version(void) { return "mpdata-gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"
+
+// ===========================================================================
+// Batches: many problems advanced together (include/mpdata.h, mpdata_batch_*)
+// ===========================================================================
+namespace {
+
+constexpr uint32_t BATCH_MAGIC = 0x4d504242u;  // "MPBB"
+
+struct Batch {
+  uint32_t magic;
+  int nprob, ih, iord, nonos, precision;
+  size_t elem;
+  std::vector<mpdata_problem> pr;
+  std::vector<int> owner;       // first problem of each problem's velocity group
+  std::vector<size_t> foff;     // element offset of each problem's field scratch
+  std::vector<size_t> voff;     // element offset of each problem's velocity scratch
+  std::vector<size_t> ncell;
+  std::vector<int> given;       // arrays set for the problem
+  std::vector<unsigned char> table;  // host image of the Prob table
+  size_t pbytes;                // sizeof(Prob<R>)
+  void* mem;
+  void* d_table;
+  unsigned char* h_stage;       // pinned staging buffer of the table upload
+  cudaEvent_t upload_done;
+  long long* d_prefix;
+  long long tiles;
+  int bx, by, grid;
+  bool dirty;
+  bool use_graph;
+  cudaGraphExec_t gexec;
+  cudaStream_t cap;             // private stream used only for graph capture
+  EventProf* prof;
+  cudaStream_t last;
+};
+
+Batch* as_batch(void* p) {
+  Batch* b = static_cast<Batch*>(p);
+  if (!b || b->magic != BATCH_MAGIC) return nullptr;
+  return b;
+}
+
+mpdata_grid grid_of(const Batch* b, int p) {
+  const mpdata_problem& q = b->pr[p];
+  return mpdata_grid{q.np, q.mp, q.lp, b->ih, q.ibcx, q.ibcy, q.ibcz};
+}
+
+// tile prefix for a block shape (tiles of bx*by cells in one plane)
+std::vector<long long> tile_prefix(const Batch* b, int bx, int by) {
+  std::vector<long long> pre(b->nprob + 1, 0);
+  for (int p = 0; p < b->nprob; p++) {
+    const mpdata_problem& q = b->pr[p];
+    pre[p + 1] = pre[p] + (long long)((q.np + bx - 1) / bx) * ((q.mp + by - 1) / by) * q.lp;
+  }
+  return pre;
+}
+
+int set_shape(Batch* b, int bx, int by, cudaStream_t s) {
+  std::vector<long long> pre = tile_prefix(b, bx, by);
+  if (cudaMemcpyAsync(b->d_prefix, pre.data(), pre.size() * sizeof(long long), cudaMemcpyHostToDevice, s) !=
+      cudaSuccess)
+    return MPDATA_E_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return MPDATA_E_CUDA;  // pre is a local buffer
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int occ = b->precision == 64 ? batch_occupancy<double>(bx * by) : batch_occupancy<float>(bx * by);
+  b->bx = bx;
+  b->by = by;
+  b->tiles = pre.back();
+  long long g = (long long)sms * occ;
+  if (g > b->tiles) g = b->tiles;
+  b->grid = (int)(g > 0 ? g : 1);
+  if (b->gexec) {
+    cudaGraphExecDestroy(b->gexec);
+    b->gexec = nullptr;
+  }
+  return MPDATA_OK;
+}
+
+int upload_table(Batch* b, cudaStream_t s) {
+  if (!b->dirty) return MPDATA_OK;
+  for (int p = 0; p < b->nprob; p++)
+    if (!b->given[p]) return MPDATA_E_NULL;
+  // the previous upload must have finished reading the staging buffer
+  if (cudaEventSynchronize(b->upload_done) != cudaSuccess) return MPDATA_E_CUDA;
+  memcpy(b->h_stage, b->table.data(), b->table.size());
+  if (cudaMemcpyAsync(b->d_table, b->h_stage, b->table.size(), cudaMemcpyHostToDevice, s) != cudaSuccess)
+    return MPDATA_E_CUDA;
+  if (cudaEventRecord(b->upload_done, s) != cudaSuccess) return MPDATA_E_CUDA;
+  b->dirty = false;
+  return MPDATA_OK;
+}
+
+template <class R>
+BatchLaunch<R> launch_of(const Batch* b, int halo) {
+  BatchLaunch<R> L;
+  L.probs = static_cast<const Prob<R>*>(b->d_table);
+  L.prefix = b->d_prefix;
+  L.nprob = b->nprob;
+  L.tiles = b->tiles;
+  L.bx = b->bx;
+  L.by = b->by;
+  L.grid = b->grid;
+  L.iord = b->iord;
+  L.nonos = b->nonos;
+  L.halo = halo;
+  return L;
+}
+
+int batch_run(Batch* b, int halo, Prof* prof, cudaStream_t s) {
+  if (b->precision == 64) return run_batch<double>(launch_of<double>(b, halo), prof, s) ? MPDATA_E_CUDA : MPDATA_OK;
+  return run_batch<float>(launch_of<float>(b, halo), prof, s) ? MPDATA_E_CUDA : MPDATA_OK;
+}
+
+template <class R>
+void write_prob(Batch* b, int p, void* psi, const void* u1, const void* u2, const void* u3, const void* h,
+                const void* rhr, const void* bcx, const void* bcy) {
+  R* base = static_cast<R*>(b->mem);
+  const mpdata_grid g = grid_of(b, p);
+  Prob<R> P = make_prob<R>(g, b->pr[p].gauge, (R*)psi, (const R*)u1, (const R*)u2, (const R*)u3,
+                           (const R*)h, (const R*)rhr, (const R*)bcx, (const R*)bcy, base + b->foff[p],
+                           b->ncell[p], base + b->voff[p], b->owner[p] == p ? 1 : 0);
+  memcpy(b->table.data() + (size_t)p * sizeof(Prob<R>), &P, sizeof P);
+}
+
+// tuned block shapes per (precision, iord, nonos, cells), shared by batches
+std::mutex g_tune_mu;
+struct TuneKey { int prec, iord, nonos; long long cells; int nprob; };
+std::vector<std::pair<TuneKey, std::pair<int, int>>> g_tuned;
+
+TuneKey key_of(const Batch* b) {
+  long long cells = 0;
+  for (size_t p = 0; p < b->ncell.size(); p++) cells += (long long)b->ncell[p];
+  return TuneKey{b->precision, b->iord, b->nonos, cells, b->nprob};
+}
+
+}  // namespace
+
+extern "C" {
+
+int mpdata_batch_create(int nprob, const mpdata_problem* probs, int ih, int iord, int nonos, int precision,
+                        void** batch) {
+  if (!batch) return MPDATA_E_NULL;
+  *batch = nullptr;
+  if (!probs) return MPDATA_E_NULL;
+  if (nprob < 1 || nprob > 65536) return MPDATA_E_DIMS;
+  mpdata_opts o{iord, nonos, 1, precision, 0};
+  int rc = check_opts(&o);
+  if (rc) return rc;
+  Batch* b = new (std::nothrow) Batch();
+  if (!b) return MPDATA_E_CUDA;
+  b->nprob = nprob;
+  b->ih = ih;
+  b->iord = iord;
+  b->nonos = nonos;
+  b->precision = precision;
+  b->elem = precision == 64 ? sizeof(double) : sizeof(float);
+  b->pbytes = precision == 64 ? sizeof(Prob<double>) : sizeof(Prob<float>);
+  b->pr.assign(probs, probs + nprob);
+  b->owner.resize(nprob);
+  b->foff.resize(nprob);
+  b->voff.resize(nprob);
+  b->ncell.resize(nprob);
+  b->given.assign(nprob, 0);
+  size_t off = 0;
+  for (int p = 0; p < nprob; p++) {
+    const mpdata_problem& q = probs[p];
+    if (q.gauge != 0 && q.gauge != 1) { delete b; return MPDATA_E_OPTS; }
+    mpdata_grid g{q.np, q.mp, q.lp, ih, q.ibcx, q.ibcy, q.ibcz};
+    rc = check_grid(&g);
+    if (rc) { delete b; return rc; }
+    b->ncell[p] = (size_t)q.np * q.mp * q.lp;
+    int own = p;
+    for (int r = 0; r < p; r++)
+      if (probs[r].velocity_group == q.velocity_group && b->owner[r] == r) { own = r; break; }
+    if (own != p) {  // sharing a velocity needs the same grid and boundaries
+      const mpdata_problem& o2 = probs[own];
+      if (o2.np != q.np || o2.mp != q.mp || o2.lp != q.lp || o2.ibcx != q.ibcx || o2.ibcy != q.ibcy ||
+          o2.ibcz != q.ibcz) { delete b; return MPDATA_E_DIMS; }
+    }
+    b->owner[p] = own;
+    b->foff[p] = off;
+    off += (size_t)NFIELD * b->ncell[p];
+  }
+  for (int p = 0; p < nprob; p++)
+    if (b->owner[p] == p) {
+      b->voff[p] = off;
+      off += (size_t)NVEL * b->ncell[p];
+    }
+  for (int p = 0; p < nprob; p++) b->voff[p] = b->voff[b->owner[p]];
+  b->table.assign((size_t)nprob * b->pbytes, 0);
+  b->mem = b->d_table = nullptr;
+  b->h_stage = nullptr;
+  b->d_prefix = nullptr;
+  b->upload_done = nullptr;
+  b->gexec = nullptr;
+  b->cap = nullptr;
+  b->prof = nullptr;
+  b->last = nullptr;
+  b->use_graph = false;
+  b->dirty = true;
+  bool ok = cudaMalloc(&b->mem, off * b->elem) == cudaSuccess &&
+            cudaMalloc(&b->d_table, b->table.size()) == cudaSuccess &&
+            cudaMalloc(&b->d_prefix, sizeof(long long) * (nprob + 1)) == cudaSuccess &&
+            cudaMallocHost(&b->h_stage, b->table.size()) == cudaSuccess &&
+            cudaEventCreateWithFlags(&b->upload_done, cudaEventDisableTiming) == cudaSuccess &&
+            cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking) == cudaSuccess;
+  b->magic = BATCH_MAGIC;
+  if (ok) {
+    // default shape, or the tuned one for this batch signature
+    int bx = 32, by = 4;
+    {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      const TuneKey k = key_of(b);
+      for (auto& e : g_tuned)
+        if (!memcmp(&e.first, &k, sizeof k)) { bx = e.second.first; by = e.second.second; }
+    }
+    ok = set_shape(b, bx, by, b->cap) == MPDATA_OK;
+  }
+  if (!ok) {
+    cudaGetLastError();
+    mpdata_batch_destroy(b);
+    return MPDATA_E_CUDA;
+  }
+  *batch = b;
+  return MPDATA_OK;
+}
+
+int mpdata_batch_destroy(void* batch) {
+  Batch* b = as_batch(batch);
+  if (!b) return MPDATA_E_WS;
+  b->magic = 0;
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  delete b->prof;
+  if (b->upload_done) { cudaEventSynchronize(b->upload_done); cudaEventDestroy(b->upload_done); }
+  if (b->cap) cudaStreamDestroy(b->cap);
+  cudaFreeHost(b->h_stage);
+  cudaFree(b->d_prefix);
+  cudaFree(b->d_table);
+  cudaError_t e = cudaFree(b->mem);
+  delete b;
+  return e == cudaSuccess ? MPDATA_OK : MPDATA_E_CUDA;
+}
+
+int mpdata_batch_set(void* batch, int prob, void* psi, const void* u1, const void* u2, const void* u3,
+                     const void* h, const void* rhr, const void* bcx, const void* bcy) {
+  Batch* b = as_batch(batch);
+  if (!b) return MPDATA_E_WS;
+  if (prob < 0 || prob >= b->nprob) return MPDATA_E_DIMS;
+  if (!psi || !u1 || !u2 || !u3 || !h || !rhr) return MPDATA_E_NULL;
+  if ((!b->pr[prob].ibcx && !bcx) || (!b->pr[prob].ibcy && !bcy)) return MPDATA_E_NULL;
+  if (b->precision == 64) write_prob<double>(b, prob, psi, u1, u2, u3, h, rhr, bcx, bcy);
+  else write_prob<float>(b, prob, psi, u1, u2, u3, h, rhr, bcx, bcy);
+  b->given[prob] = 1;
+  b->dirty = true;
+  return MPDATA_OK;
+}
+
+int mpdata_batch_step(void* batch, void* stream) {
+  Batch* b = as_batch(batch);
+  if (!b) return MPDATA_E_WS;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  b->last = s;
+  int rc = upload_table(b, s);
+  if (rc) return rc;
+  if (!b->use_graph) return batch_run(b, 1, b->prof, s);
+  if (!b->gexec) {
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return MPDATA_E_CUDA;
+    rc = batch_run(b, 1, nullptr, b->cap);
+    if (cudaStreamEndCapture(b->cap, &graph) != cudaSuccess || rc) {
+      if (graph) cudaGraphDestroy(graph);
+      cudaGetLastError();
+      return MPDATA_E_CUDA;
+    }
+    cudaError_t e = cudaGraphInstantiate(&b->gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) { b->gexec = nullptr; return MPDATA_E_CUDA; }
+  }
+  return cudaGraphLaunch(b->gexec, s) == cudaSuccess ? MPDATA_OK : MPDATA_E_CUDA;
+}
+
+int mpdata_batch_graph(void* batch, int enable) {
+  Batch* b = as_batch(batch);
+  if (!b) return MPDATA_E_WS;
+  b->use_graph = enable != 0;
+  if (!b->use_graph && b->gexec) {
+    cudaGraphExecDestroy(b->gexec);
+    b->gexec = nullptr;
+  }
+  return MPDATA_OK;
+}
+
+int mpdata_batch_tune(void* batch, void* stream, int* bx_out, int* by_out) {
+  Batch* b = as_batch(batch);
+  if (!b) return MPDATA_E_WS;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int rc = upload_table(b, s);
+  if (rc) return rc;
+  static const int shapes[][2] = {{32, 4}, {32, 8}, {64, 2}, {64, 4}, {128, 1}, {128, 2}, {16, 8}};
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return MPDATA_E_CUDA;
+  float best = 1e30f;
+  int bbx = b->bx, bby = b->by;
+  for (const auto& sh : shapes) {
+    if (set_shape(b, sh[0], sh[1], s)) { rc = MPDATA_E_CUDA; break; }
+    // halo=0: the tuning steps write scratch only, never the caller's psi
+    if ((rc = batch_run(b, 0, nullptr, s))) break;
+    cudaEventRecord(e0, s);
+    for (int r = 0; r < 2 && !rc; r++) rc = batch_run(b, 0, nullptr, s);
+    cudaEventRecord(e1, s);
+    if (rc || cudaEventSynchronize(e1) != cudaSuccess) { rc = MPDATA_E_CUDA; break; }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) { best = ms; bbx = sh[0]; bby = sh[1]; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (set_shape(b, bbx, bby, s)) return MPDATA_E_CUDA;
+  if (rc) return rc;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    const TuneKey k = key_of(b);
+    bool found = false;
+    for (auto& e : g_tuned)
+      if (!memcmp(&e.first, &k, sizeof k)) { e.second = {bbx, bby}; found = true; }
+    if (!found) g_tuned.push_back({k, {bbx, bby}});
+  }
+  if (bx_out) *bx_out = bbx;
+  if (by_out) *by_out = bby;
+  return MPDATA_OK;
+}
+
+int mpdata_batch_profile(void* batch, int enable) {
+  Batch* b = as_batch(batch);
+  if (!b) return MPDATA_E_WS;
+  if (enable && !b->prof) {
+    b->prof = new (std::nothrow) EventProf();
+    if (!b->prof) return MPDATA_E_CUDA;
+  } else if (!enable && b->prof) {
+    cudaStreamSynchronize(b->last);
+    delete b->prof;
+    b->prof = nullptr;
+  }
+  return MPDATA_OK;
+}
+
+int mpdata_batch_stage_times(void* batch, int nstages, double* total_ms, long long* launches) {
+  Batch* b = as_batch(batch);
+  if (!b) return MPDATA_E_WS;
+  if (!total_ms || !launches) return MPDATA_E_NULL;
+  if (nstages < 0) return MPDATA_E_OPTS;
+  const int n = nstages < NSTAGE ? nstages : NSTAGE;
+  for (int i = 0; i < n; i++) { total_ms[i] = 0.0; launches[i] = 0; }
+  if (!b->prof) return NSTAGE;
+  int rc = b->prof->harvest();
+  if (rc) return rc;
+  for (int i = 0; i < n; i++) { total_ms[i] = b->prof->total_ms[i]; launches[i] = b->prof->launches[i]; }
+  return NSTAGE;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// FP64 compensated reductions (mass, error norms)
+// ===========================================================================
+namespace {
+
+template <class R>
+int reduce_impl(const mpdata_grid* grid, int mode, const R* a, const R* h, const R* rhr, const void* b,
+                int b_is_f64, double* host_out, void* stream) {
+  int rc = check_grid(grid);
+  if (rc) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t nb = (size_t)reduce_blocks() * 6 + 4;
+  double* buf = nullptr;
+  if (cudaMallocAsync(&buf, nb * sizeof(double), s) != cudaSuccess) return MPDATA_E_CUDA;
+  rc = run_reduce<R>(geo_of(*grid), mode, a, h, rhr, b, b_is_f64, buf + 4, buf, s) ? MPDATA_E_CUDA : MPDATA_OK;
+  double out[4] = {0, 0, 0, 0};
+  if (!rc && cudaMemcpyAsync(out, buf, sizeof out, cudaMemcpyDeviceToHost, s) != cudaSuccess) rc = MPDATA_E_CUDA;
+  cudaFreeAsync(buf, s);
+  if (!rc && cudaStreamSynchronize(s) != cudaSuccess) rc = MPDATA_E_CUDA;
+  if (!rc) memcpy(host_out, out, sizeof out);
+  return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mpdata_mass_f64(const mpdata_grid* grid, const double* psi, const double* h, const double* rhr,
+                    double* mass, void* stream) {
+  if (!psi || !h || !mass) return MPDATA_E_NULL;
+  double out[4];
+  int rc = reduce_impl<double>(grid, 0, psi, h, rhr, nullptr, 1, out, stream);
+  if (!rc) *mass = out[0];
+  return rc;
+}
+int mpdata_mass_f32(const mpdata_grid* grid, const float* psi, const float* h, const float* rhr,
+                    double* mass, void* stream) {
+  if (!psi || !h || !mass) return MPDATA_E_NULL;
+  double out[4];
+  int rc = reduce_impl<float>(grid, 0, psi, h, rhr, nullptr, 1, out, stream);
+  if (!rc) *mass = out[0];
+  return rc;
+}
+
+int mpdata_error_norms(const mpdata_grid* grid, const void* a, int a_is_f64, const void* b, int b_is_f64,
+                       double* out, void* stream) {
+  if (!a || !b || !out) return MPDATA_E_NULL;
+  double r[4];
+  int rc = a_is_f64 ? reduce_impl<double>(grid, 1, (const double*)a, nullptr, nullptr, b, b_is_f64, r, stream)
+                    : reduce_impl<float>(grid, 1, (const float*)a, nullptr, nullptr, b, b_is_f64, r, stream);
+  if (rc) return rc;
+  out[0] = r[2];             // max |a-b|
+  out[1] = sqrt(r[0]);       // ||a-b||_2
+  out[2] = r[3];             // max |b|
+  out[3] = sqrt(r[1]);       // ||b||_2
+  return MPDATA_OK;
+}
 
 }  // extern "C"

@@ -48,11 +48,57 @@ __device__ __forceinline__ int refl(int i, int n) { return i < 1 ? 2 - i : (i > 
 // zero gradient: x(0)=x(1), x(n+1)=x(n) (cp_last_to_halo_xy, mpdataoperators.inc:551-584)
 __device__ __forceinline__ int clampi(int i, int n) { return i < 1 ? 1 : (i > n ? n : i); }
 
+// ---- order-preserving selects -------------------------------------------
+// On GB300 every FP64 compare, min and max issues on the FP64 pipe, which
+// retires about 2 operations per SM per clock, while the integer pipe retires
+// about 64.  For doubles these selects therefore work on the bit patterns:
+// the order key of x is its bits with the magnitude bits flipped when the
+// sign is set, so signed 64-bit order of keys is IEEE order of values.  Each
+// returns one of its inputs (or +0) bit for bit, as the floating-point forms
+// do; the only difference is that -0 orders below +0.  Float keeps the
+// native FP32 compares (cheap on the FP32/ALU pipes).
+__device__ __forceinline__ long long okey(double x) {
+  const long long b = __double_as_longlong(x);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ double from_okey(long long k) {
+  return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffLL));
+}
+__device__ __forceinline__ bool sgn(double y) { return __double2hiint(y) < 0; }
+__device__ __forceinline__ bool sgn(float y) { return __float_as_int(y) < 0; }
+
+// pp(y) = max(0,y), pn(y) = -min(0,y)  (mpdataoperators.inc:50-59)
+__device__ __forceinline__ double pp(double y) { return sgn(y) ? 0.0 : y; }
+__device__ __forceinline__ double pn(double y) { return sgn(y) ? -y : 0.0; }
+__device__ __forceinline__ float pp(float y) { return y > 0.f ? y : 0.f; }
+__device__ __forceinline__ float pn(float y) { return y < 0.f ? -y : 0.f; }
+__device__ __forceinline__ double mx2(double a, double b) { return okey(a) > okey(b) ? a : b; }
+__device__ __forceinline__ double mn2(double a, double b) { return okey(a) < okey(b) ? a : b; }
+__device__ __forceinline__ float mx2(float a, float b) { return a > b ? a : b; }
+__device__ __forceinline__ float mn2(float a, float b) { return a < b ? a : b; }
+
+// Running max and min over a set of values (the limiter's 7-point stars).
+template <class R> struct Extrema;
+template <> struct Extrema<double> {
+  long long kx, kn;
+  __device__ __forceinline__ explicit Extrema(double v) { kx = kn = okey(v); }
+  __device__ __forceinline__ void add(double v) {
+    const long long k = okey(v);
+    kx = k > kx ? k : kx;
+    kn = k < kn ? k : kn;
+  }
+  __device__ __forceinline__ double max() const { return from_okey(kx); }
+  __device__ __forceinline__ double min() const { return from_okey(kn); }
+};
+template <> struct Extrema<float> {
+  float x, n;
+  __device__ __forceinline__ explicit Extrema(float v) : x(v), n(v) {}
+  __device__ __forceinline__ void add(float v) { x = v > x ? v : x; n = v < n ? v : n; }
+  __device__ __forceinline__ float max() const { return x; }
+  __device__ __forceinline__ float min() const { return n; }
+};
+
 // ---- point operators (device forms of mpdataoperators.inc:50-96) ----
-template <class R> __device__ __forceinline__ R pp(R y) { return y > R(0) ? y : R(0); }
-template <class R> __device__ __forceinline__ R pn(R y) { return y < R(0) ? -y : R(0); }
-template <class R> __device__ __forceinline__ R mx2(R a, R b) { return a > b ? a : b; }
-template <class R> __device__ __forceinline__ R mn2(R a, R b) { return a < b ? a : b; }
 template <class R> __device__ __forceinline__ R donor(R y1, R y2, R a) { return pp(a) * y1 - pn(a) * y2; }
 template <class R> __device__ __forceinline__ R vdyf(R x1, R x2, R a, R rinv) {
   return (fabs(a) - a * a * rinv) * (x2 - x1) * R(0.5);
@@ -66,8 +112,10 @@ template <class R> __device__ __forceinline__ R vdyfa(R x1, R x2, R a, R rinv, R
 template <class R> __device__ __forceinline__ R vcorra(R a, R b, R y1, R y2, R rinv) {
   return -(R(0.125) * a * b * y1 * rinv / y2);
 }
-template <class R> __device__ __forceinline__ R possign(R x) { return signbit(x) ? R(0) : R(1); }
+template <class R> __device__ __forceinline__ R possign(R x) { return sgn(x) ? R(0) : R(1); }
 template <class R> __device__ __forceinline__ R min3(R a, R b) { return mn2(mn2(R(1), a), b); }
+// 1/(0.5*(h1+h2)) == 2/(h1+h2) exactly: the halving is an exact scaling.
+template <class R> __device__ __forceinline__ R rhm(R h1, R h2) { return R(2) / (h1 + h2); }
 
 // ep_nonos (common/epsilons.f90:3)
 template <class R> struct Eps;

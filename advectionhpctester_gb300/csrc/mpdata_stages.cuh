@@ -1,12 +1,12 @@
-// Launch plans for the MPDATA stage kernels.
+// Launch sequences of the MPDATA kernels (host side).
 #pragma once
-#include "mpdata_common.cuh"
+#include "mpdata_body.cuh"
 
 namespace mpdata {
 
 // Stage ids for the optional per-launch CUDA-event timing.
 enum Stage { ST_UPWIND = 0, ST_PSEUDO, ST_BOUNDS, ST_LIMIT, ST_UPDATE, ST_COPY, ST_PRED_LEVEL,
-             ST_PRED_CGRID, NSTAGE };
+             ST_PRED_CGRID, ST_RHO_OUT, NSTAGE };
 
 // Records a pair of CUDA events around each launch when enabled (the events
 // live on the launching stream, so they time exactly that kernel).
@@ -16,22 +16,28 @@ struct Prof {
   virtual ~Prof() {}
 };
 
-// Everything one step needs: caller arrays (Fortran layout views) and the
-// workspace scratch (interior-shaped views).
+// One step of one problem: upwind, then iord-1 corrective passes (and the
+// outputs of the density step when P.rho is set).
 template <class R>
-struct StepPlan {
-  Geo g;
-  int iord, nonos, gauge;
-  Arr<R> psi, u1, u2, u3, h, rhr;
-  const R* bcx;
-  const R* bcy;
-  // scratch
-  Arr<R> xant, hinv, v1, v2, v3, f1, f2, f3, w1, w2, w3, cp, cn, mx, mn, q;
-  Prof* prof;  // NULL = no timing
-};
+int run_step(const Prob<R>& P, int iord, int nonos, Prof* prof, cudaStream_t stream);
 
+// One step of every problem of a batch.  probs/prefix live in device memory:
+// prefix[p] is the first tile of problem p (tiles of bx*by cells in one
+// plane), prefix[nprob] the total.  Each stage is one persistent grid-stride
+// launch of `grid` blocks of bx*by threads over all tiles of all problems.
 template <class R>
-int run_step(const StepPlan<R>& plan, cudaStream_t stream);
+struct BatchLaunch {
+  const Prob<R>* probs;
+  const long long* prefix;
+  int nprob;
+  long long tiles;
+  int bx, by;
+  int grid;
+  int iord, nonos;
+  int halo;  // 0 while autotuning: psi (interior and halo) is not written
+};
+template <class R>
+int run_batch(const BatchLaunch<R>& B, Prof* prof, cudaStream_t stream);
 
 // Velocity predictor (velprd_traj0 + velprdA_to_C + level roll).
 template <class R>
@@ -40,7 +46,7 @@ struct PredPlan {
   long lev;  // elements per psi-shaped level
   R* ox;
   R* oy;
-  R* oz;  // base pointers of the three-level stacks (caller layout)
+  R* oz;  // logical (1,1,1) of level 0 of the three-level stacks (caller layout)
   R* u;
   R* v;
   R* w;  // optional physical velocity stacks

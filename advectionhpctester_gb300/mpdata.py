@@ -139,6 +139,27 @@ class Workspace:
                  _ptr(u2, d, s["u2"], "u2"), _ptr(u3, d, s["u3"], "u3"), _stream(stream)),
               "mpdata_velprd")
 
+    def rho_gauge(self, ox, oy, oz, u1, u2, u3, x_in, x_incomp, h, rhoadv, rhr, pexe, pexr1, pexr2,
+                  dxi, dyi, dzi, dt, dt_ratio, bcx=None, bcy=None, liner=0, u=None, v=None, w=None,
+                  stream=None):
+        """Density step mpdata3d_rho_gauge_gpubc (mpdata3d-rho-gauge-gpubc.f90:23-622):
+        predictor, upwind keeping its fluxes, gauge antidiffusion; writes
+        x_in, x_incomp, rhoadv, rhr, pexr1, pexr2 and the mass fluxes u1..u3."""
+        s, d = self.shapes, self.dtype
+        lev = s["psi"] + (3,)
+        fn = self.lib.mpdata_rho_gauge_f64 if self.opts.precision == 64 else self.lib.mpdata_rho_gauge_f32
+        ps = lambda t, n: _ptr(t, d, s["psi"], n)
+        check(fn(self.handle, _ptr(ox, d, lev, "ox"), _ptr(oy, d, lev, "oy"), _ptr(oz, d, lev, "oz"),
+                 _ptr(u, d, lev, "u"), _ptr(v, d, lev, "v"), _ptr(w, d, lev, "w"), _ptr(u1, d, s["u1"], "u1"),
+                 _ptr(u2, d, s["u2"], "u2"), _ptr(u3, d, s["u3"], "u3"), ps(x_in, "x_in"),
+                 ps(x_incomp, "x_incomp"), ps(h, "h"), ps(rhoadv, "rhoadv"), ps(rhr, "rhr"), ps(pexe, "pexe"),
+                 ps(pexr1, "pexr1"), ps(pexr2, "pexr2"), _ptr(bcx, d, s["bcx"], "bcx"),
+                 _ptr(bcy, d, s["bcy"], "bcy"), dxi, dyi, dzi, dt, dt_ratio, int(liner), _stream(stream)),
+              "mpdata_rho_gauge")
+
+    # the reference's name for the density step
+    mpdata3d_rho_gauge_gpubc = rho_gauge
+
     def profile(self, enable=True):
         """Start (or stop) per-stage CUDA-event timing of this workspace."""
         check(self.lib.mpdata_ws_profile(self.handle, 1 if enable else 0), "mpdata_ws_profile")
@@ -160,6 +181,129 @@ class Workspace:
         return out.value
 
 
+class Batch:
+    """Many MPDATA problems advanced together, one launch per stage
+    (mpdata_batch_*).  `problems` is a list of dicts with keys np, mp, lp and
+    optionally ibcx, ibcy, ibcz (default periodic), gauge (default 1) and
+    velocity_group (default: the problem's own index)."""
+
+    def __init__(self, problems, ih=1, iord=2, nonos=1, precision=64):
+        _require_torch()
+        self.lib = _native.load()
+        arr = (_native.MpdataProblem * len(problems))()
+        self.shapes = []
+        for n, p in enumerate(problems):
+            arr[n] = _native.MpdataProblem(p["np"], p["mp"], p["lp"], p.get("ibcx", 1), p.get("ibcy", 1),
+                                           p.get("ibcz", 1), p.get("gauge", 1), p.get("velocity_group", n))
+            self.shapes.append(shapes(p["np"], p["mp"], p["lp"], ih))
+        self.problems = [dict(p) for p in problems]
+        self.precision = precision
+        self.dtype = torch.float64 if precision == 64 else torch.float32
+        h = _native.P()
+        check(self.lib.mpdata_batch_create(len(problems), arr, ih, iord, nonos, precision, h),
+              "mpdata_batch_create")
+        self.handle = h
+        self._keep = {}
+
+    def set(self, p, psi, u1, u2, u3, h, rhr, bcx=None, bcy=None):
+        s, d = self.shapes[p], self.dtype
+        check(self.lib.mpdata_batch_set(self.handle, p, _ptr(psi, d, s["psi"], "psi"), _ptr(u1, d, s["u1"], "u1"),
+                                        _ptr(u2, d, s["u2"], "u2"), _ptr(u3, d, s["u3"], "u3"),
+                                        _ptr(h, d, s["psi"], "h"), _ptr(rhr, d, s["psi"], "rhr"),
+                                        _ptr(bcx, d, s["bcx"], "bcx"), _ptr(bcy, d, s["bcy"], "bcy")),
+              "mpdata_batch_set")
+        self._keep[p] = (psi, u1, u2, u3, h, rhr, bcx, bcy)  # keep the tensors alive
+
+    def step(self, stream=None):
+        check(self.lib.mpdata_batch_step(self.handle, _stream(stream)), "mpdata_batch_step")
+
+    def graph(self, enable=True):
+        check(self.lib.mpdata_batch_graph(self.handle, 1 if enable else 0), "mpdata_batch_graph")
+
+    def tune(self, stream=None):
+        bx, by = _native.I(0), _native.I(0)
+        check(self.lib.mpdata_batch_tune(self.handle, _stream(stream), bx, by), "mpdata_batch_tune")
+        return bx.value, by.value
+
+    def profile(self, enable=True):
+        check(self.lib.mpdata_batch_profile(self.handle, 1 if enable else 0), "mpdata_batch_profile")
+
+    def stage_times(self):
+        import ctypes
+        n = 16
+        ms = (ctypes.c_double * n)()
+        cnt = (ctypes.c_longlong * n)()
+        rc = self.lib.mpdata_batch_stage_times(self.handle, n, ms, cnt)
+        if rc < 0:
+            check(rc, "mpdata_batch_stage_times")
+        return {self.lib.mpdata_stage_name(i).decode(): (ms[i], cnt[i]) for i in range(rc)}
+
+    def close(self):
+        if getattr(self, "handle", None):
+            check(self.lib.mpdata_batch_destroy(self.handle), "mpdata_batch_destroy")
+            self.handle = None
+            self._keep = {}
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# Field order and antidiffusion choice of CE_advection
+# (advection_CEtimestep_twostep_GPUBC.f90:150-159, 309-339): "mpdata3d" fields
+# take the standard form unless mpdata_alg_choice is 1, "mpdatm3d" fields the
+# gauge form unless it is 2.
+CE_FIELDS = (("th", "mpdata3d"), ("u", "mpdatm3d"), ("v", "mpdatm3d"), ("w", "mpdatm3d"),
+             ("tht", "mpdatm3d"), ("pstr", "mpdatm3d"), ("qv", "mpdata3d"), ("qc", "mpdata3d"),
+             ("qr", "mpdata3d"), ("qi", "mpdata3d"), ("qs", "mpdata3d"), ("qg", "mpdata3d"))
+
+
+def ce_form(kind, mpdata_alg_choice):
+    """1 = gauge, 0 = standard, for a CE_advection field kind."""
+    if mpdata_alg_choice == 1:
+        return 1
+    if mpdata_alg_choice == 2:
+        return 0
+    return 1 if kind == "mpdatm3d" else 0
+
+
+_ce_cache = {}
+
+
+def ce_advection(mpdata_alg_choice, liner, ipoles, ibcx, ibcy, ibcz, np_, mp, lp, ih, rhr, rhoadv,
+                 uadv, vadv, wadv, stream=None, **fields):
+    """The reference's multi-field step CE_advection
+    (advection_CEtimestep_twostep_GPUBC.f90:27-376) on CUDA tensors: every
+    field given as name=(x, x_lr, x_bt) (th, u, v, w, tht, pstr required;
+    qv, qc, qr, qi, qs, qg optional) is advected by the shared velocity in ONE
+    batched step.  liner=1 stops after the upwind pass, as the reference does."""
+    if ipoles != 0:
+        raise MpdataError(-7, "ce_advection")
+    names = [n for n, _ in CE_FIELDS if n in fields]
+    for req in ("th", "u", "v", "w", "tht", "pstr"):
+        if req not in fields:
+            raise ValueError("ce_advection needs field %r" % req)
+    unknown = set(fields) - {n for n, _ in CE_FIELDS}
+    if unknown:
+        raise ValueError("unknown fields %s" % sorted(unknown))
+    kinds = dict(CE_FIELDS)
+    forms = tuple(ce_form(kinds[n], mpdata_alg_choice) for n in names)
+    prec = 64 if uadv.dtype == torch.float64 else 32
+    iord = 1 if liner else 2
+    key = (np_, mp, lp, ih, ibcx, ibcy, ibcz, forms, prec, iord)
+    b = _ce_cache.get(key)
+    if b is None:
+        probs = [dict(np=np_, mp=mp, lp=lp, ibcx=ibcx, ibcy=ibcy, ibcz=ibcz, gauge=f, velocity_group=0)
+                 for f in forms]
+        b = _ce_cache[key] = Batch(probs, ih=ih, iord=iord, nonos=1, precision=prec)
+    for p, n in enumerate(names):
+        x, x_lr, x_bt = fields[n]
+        b.set(p, x, uadv, vadv, wadv, rhoadv, rhr, x_lr, x_bt)
+    b.step(stream)
+
+
 def advec_dwarf(legacyoptmode, t_adv, lupdatemulti, lvertsplit, np_, mp, lp, ih, ipoles, ibcx, ibcy,
                 ibcz, x, x_lr, x_bt, uadv, vadv, wadv, rhr, rhoadv, iord=2, nonos=1, stream=None):
     """The reference's dwarf driver (advec.f90:116-244) on CUDA tensors."""
@@ -179,6 +323,34 @@ def advec_dwarf(legacyoptmode, t_adv, lupdatemulti, lvertsplit, np_, mp, lp, ih,
              _stream(stream)), "advec_dwarf")
 
 
+def mass(psi, h, rhr=None, ibc=(1, 1, 1), ih=1, stream=None):
+    """FP64 Neumaier-compensated sum(h*psi[/rhr]) over the interior."""
+    import ctypes
+    n = [d - 2 * ih for d in psi.shape]
+    g = _native.MpdataGrid(n[0], n[1], n[2], ih, *ibc)
+    lib = _native.load()
+    out = ctypes.c_double(0.0)
+    fn = lib.mpdata_mass_f64 if psi.dtype == torch.float64 else lib.mpdata_mass_f32
+    d = psi.dtype
+    check(fn(g, _ptr(psi, d, None, "psi"), _ptr(h, d, tuple(psi.shape), "h"),
+             _ptr(rhr, d, tuple(psi.shape), "rhr"), out, _stream(stream)), "mpdata_mass")
+    return out.value
+
+
+def error_norms(a, b, ibc=(1, 1, 1), ih=1, stream=None):
+    """(max|a-b|, ||a-b||_2, max|b|, ||b||_2) over the interior, FP64."""
+    import ctypes
+    if tuple(a.shape) != tuple(b.shape):
+        raise ValueError("a and b must have the same shape")
+    n = [d - 2 * ih for d in a.shape]
+    g = _native.MpdataGrid(n[0], n[1], n[2], ih, *ibc)
+    out = (ctypes.c_double * 4)()
+    check(_native.load().mpdata_error_norms(g, _ptr(a, a.dtype, None, "a"), int(a.dtype == torch.float64),
+                                            _ptr(b, b.dtype, None, "b"), int(b.dtype == torch.float64), out,
+                                            _stream(stream)), "mpdata_error_norms")
+    return tuple(out)
+
+
 def release_cached():
     check(_native.load().mpdata_release_cached(), "mpdata_release_cached")
 
@@ -187,5 +359,5 @@ def launch_count():
     return int(_native.load().mpdata_launch_count())
 
 
-__all__ = ["Workspace", "advec_dwarf", "fortran_device", "fortran_empty", "to_numpy", "MpdataError",
-           "release_cached", "launch_count", "shapes"]
+__all__ = ["Workspace", "Batch", "ce_advection", "advec_dwarf", "fortran_device", "fortran_empty", "to_numpy", "MpdataError",
+           "release_cached", "launch_count", "shapes", "mass", "error_norms"]

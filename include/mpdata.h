@@ -117,6 +117,27 @@ int mpdata_velprd_f32(void* ws, float* ox, float* oy, float* oz, float* u, float
                       const float* h, float dxi, float dyi, float dzi, float dt, float dt_ratio,
                       float* u1, float* u2, float* u3, void* stream);
 
+/* Density step of the dycore, mpdata3d_rho_gauge_gpubc
+ * (advection/src_algorithms/mpdata3d-rho-gauge-gpubc.f90:23-622): the
+ * predictor (as mpdata_velprd_*), then rhoadv = x_incomp, an upwind pass
+ * without rhr that keeps its fluxes, gauge antidiffusion with the
+ * nonoscillatory limiter (workspace iord/nonos; the workspace must be gauge),
+ * and the outputs x_incomp = x*h, pexr1 = x_incomp*pexe, pexr2 = x_incomp,
+ * rhr = rhoadv/x_incomp and the mass fluxes u1..u3 = upwind flux + limited
+ * antidiffusive flux (faces 1..n+1, overwriting the Courant numbers).
+ * liner=1 stops after the upwind pass (:594-606). */
+int mpdata_rho_gauge_f64(void* ws, double* ox, double* oy, double* oz, double* u, double* v,
+                         double* w, double* u1, double* u2, double* u3, double* x_in,
+                         double* x_incomp, const double* h, double* rhoadv, double* rhr,
+                         const double* pexe, double* pexr1, double* pexr2, const double* bcx,
+                         const double* bcy, double dxi, double dyi, double dzi, double dt,
+                         double dt_ratio, int liner, void* stream);
+int mpdata_rho_gauge_f32(void* ws, float* ox, float* oy, float* oz, float* u, float* v, float* w,
+                         float* u1, float* u2, float* u3, float* x_in, float* x_incomp,
+                         const float* h, float* rhoadv, float* rhr, const float* pexe, float* pexr1,
+                         float* pexr2, const float* bcx, const float* bcy, float dxi, float dyi,
+                         float dzi, float dt, float dt_ratio, int liner, void* stream);
+
 /* Device error word of a workspace (bit 0: a non-finite value was produced
  * by the last checked step).  Synchronises the workspace's last stream. */
 int mpdata_ws_error(void* ws, int* error_word);
@@ -135,6 +156,62 @@ long long mpdata_launch_count(void);
 int mpdata_ws_profile(void* ws, int enable);
 int mpdata_ws_stage_times(void* ws, int nstages, double* total_ms, long long* launches);
 const char* mpdata_stage_name(int stage);
+
+/* ---- batches -------------------------------------------------------------
+ * Many problems advanced together with ONE launch per stage (a step is a
+ * fixed sequence of about ten persistent launches, replayable as one CUDA
+ * graph).  Covers
+ *  - the reference's multi-tracer step CE_advection, which advects up to 12
+ *    fields that share one velocity with one fused upwind kernel and one
+ *    antidiffusion per field, the form chosen per field group
+ *    (advection/src_drivers/advection_CEtimestep_twostep_GPUBC.f90:27-376,
+ *    3186-3494): problems with the same velocity_group share u1..u3, h, rhr
+ *    and the scratch derived from them (computed once per group);
+ *  - independent domains of uneven sizes (one velocity_group each).
+ * All problems share ih, iord, nonos and precision; each has its own grid,
+ * boundary flags and form.  Array pointers follow mpdata_step_*. */
+typedef struct {
+  int np, mp, lp;
+  int ibcx, ibcy, ibcz;
+  int gauge;          /* 1 = infinite gauge (t_adv=1), 0 = standard (t_adv=2) */
+  int velocity_group; /* problems with equal ids share the velocity and densities */
+} mpdata_problem;
+
+int mpdata_batch_create(int nprob, const mpdata_problem* probs, int ih, int iord, int nonos,
+                        int precision, void** batch);
+int mpdata_batch_destroy(void* batch);
+/* Arrays of problem `prob` (device pointers, float or double as the batch).
+ * Pointers are uploaded with the next step; they may change between steps. */
+int mpdata_batch_set(void* batch, int prob, void* psi, const void* u1, const void* u2,
+                     const void* u3, const void* h, const void* rhr, const void* bcx,
+                     const void* bcy);
+/* One step of every problem (in place on each psi), ordered on `stream`. */
+int mpdata_batch_step(void* batch, void* stream);
+/* enable=1: capture the step's launches into a CUDA graph on the next step
+ * and replay the graph afterwards (one graph launch per step). */
+int mpdata_batch_graph(void* batch, int enable);
+/* Autotuner: times every candidate tile shape (block of bx*by cells) on
+ * this batch with steps that write scratch only (psi untouched), keeps the
+ * fastest, and caches it for batches of the same signature (precision, iord,
+ * nonos, total cells, problem count).  Synchronises the stream. */
+int mpdata_batch_tune(void* batch, void* stream, int* bx, int* by);
+int mpdata_batch_profile(void* batch, int enable);
+int mpdata_batch_stage_times(void* batch, int nstages, double* total_ms, long long* launches);
+
+/* ---- FP64 compensated reductions ------------------------------------------
+ * Global sums over the interior in FP64 Neumaier summation, replacing the
+ * reference's globsum and norms (common/mpi_parallel.f90:826-880,
+ * advection/src_testdata/advection_test_setup.f90:472-617).  Both
+ * synchronise `stream` and return host values.
+ * mass = sum(h*psi), or sum(h*psi/rhr) when rhr is not NULL. */
+int mpdata_mass_f64(const mpdata_grid* grid, const double* psi, const double* h, const double* rhr,
+                    double* mass, void* stream);
+int mpdata_mass_f32(const mpdata_grid* grid, const float* psi, const float* h, const float* rhr,
+                    double* mass, void* stream);
+/* Error of field a against reference b (each FP32 or FP64, psi-shaped):
+ * out[0] = max|a-b|, out[1] = ||a-b||_2, out[2] = max|b|, out[3] = ||b||_2. */
+int mpdata_error_norms(const mpdata_grid* grid, const void* a, int a_is_f64, const void* b,
+                       int b_is_f64, double* out, void* stream);
 
 const char* mpdata_strerror(int code);
 const char* mpdata_version(void);

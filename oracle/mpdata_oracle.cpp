@@ -494,6 +494,15 @@ void limit_update_gauge(const Dims& d, bool nonos, Buf<R>& x, Buf<R>& v1, Buf<R>
       }
 }
 
+// ---- mpdata3d_rho_gauge_gpubc (mpdata3d-rho-gauge-gpubc.f90:23-622) -------
+// Density step: predictor, upwind without rhr that keeps its fluxes
+// (:137-210), gauge antidiffusion (:230-446), then x_incomp, pexr1/2, rhr and
+// the mass fluxes u = upwind flux + limited antidiffusive flux (:461-606).
+template <class R>
+int rho_gauge(const orc_grid* g, R* ox, R* oy, R* oz, R* pu, R* pv, R* pw, R* u1o, R* u2o, R* u3o,
+              R* x_in, R* x_incomp, const R* h_in, R* rhoadv, R* rhr_out, const R* pexe, R* pexr1,
+              R* pexr2, const R* bcx, const R* bcy, R dxi, R dyi, R dzi, R dt, R dt_ratio, int liner);
+
 bool dims_ok(const orc_grid* g) {
   if (!g) return false;
   if (g->ih < 1) return false;
@@ -705,6 +714,130 @@ int velprd(const orc_grid* g, R* ox, R* oy, R* oz, R* u, R* v, R* w, const R* h_
   return 0;
 }
 
+template <class R>
+int rho_gauge(const orc_grid* g, R* ox, R* oy, R* oz, R* pu, R* pv, R* pw, R* u1o, R* u2o, R* u3o,
+              R* x_in, R* x_incomp, const R* h_in, R* rhoadv, R* rhr_out, const R* pexe, R* pexr1,
+              R* pexr2, const R* bcx, const R* bcy, R dxi, R dyi, R dzi, R dt, R dt_ratio, int liner) {
+  if (!dims_ok(g)) return -1;
+  if (!x_in || !x_incomp || !rhoadv || !rhr_out || !pexe || !pexr1 || !pexr2) return -3;
+  const Dims d{g->np, g->mp, g->lp, g->ih, g->ibcx, g->ibcy, g->ibcz};
+  if ((!d.bx && !bcx) || (!d.by && !bcy)) return -3;
+  // velprd_driver (:106-111): predictor into u1..u3, level roll
+  int rc = velprd<R>(g, ox, oy, oz, pu, pv, pw, h_in, dxi, dyi, dzi, dt, dt_ratio, u1o, u2o, u3o);
+  if (rc) return rc;
+  const R ep = R(1e-10);
+  const int NX = d.np + 2, NY = d.mp + 2, NZ = d.lp + 2, ih = d.ih;
+  const int SX = d.np + 2 * ih, SY = d.mp + 2 * ih;
+  V3<R> X = view<R>(x_in, ih, SX, SY), XC = view<R>(x_incomp, ih, SX, SY), RA = view<R>(rhoadv, ih, SX, SY),
+        RO = view<R>(rhr_out, ih, SX, SY), PE = view<R>(const_cast<R*>(pexe), ih, SX, SY),
+        P1 = view<R>(pexr1, ih, SX, SY), P2 = view<R>(pexr2, ih, SX, SY);
+  // rhoadv = x_incomp (:121-123)
+  for (int k = 1; k <= d.lp; k++)
+    for (int j = 1; j <= d.mp; j++)
+      for (int i = 1; i <= d.np; i++) RA(i, j, k) = XC(i, j, k);
+  Buf<R> xin(NX, NY, NZ), h(NX, NY, NZ), ones(NX, NY, NZ);
+  Buf<R> u1(NX + 1, NY, NZ), u2(NX, NY + 1, NZ), u3(NX, NY, NZ + 1);
+  load_cell(xin, x_in, d);
+  load_cell(h, h_in, d);
+  std::fill(ones.d.begin(), ones.d.end(), R(1));
+  load_face(u1, u1o, d, 0);
+  load_face(u2, u2o, d, 1);
+  load_face(u3, u3o, d, 2);
+  if (!d.bx)  // putbcinxh (:124)
+    for (int k = 1; k <= d.lp; k++)
+      for (int j = 1; j <= d.mp; j++) {
+        xin(0, j, k) = bcx[(j - 1) + (long)d.mp * (k - 1)];
+        xin(d.np + 1, j, k) = bcx[(j - 1) + (long)d.mp * (k - 1) + (long)d.mp * d.lp];
+      }
+  if (!d.by)
+    for (int k = 1; k <= d.lp; k++)
+      for (int i = 1; i <= d.np; i++) {
+        xin(i, 0, k) = bcy[(i - 1) + (long)d.np * (k - 1)];
+        xin(i, d.mp + 1, k) = bcy[(i - 1) + (long)d.np * (k - 1) + (long)d.np * d.lp];
+      }
+  // upwind that keeps its fluxes (:137-210); no rhr, division by h
+  Buf<R> xant(NX, NY, NZ), fn1(NX + 1, NY, NZ), fn2(NX, NY + 1, NZ), fn3(NX, NY, NZ + 1);
+  for (int k = 1; k <= d.lp; k++)
+    for (int j = 1; j <= d.mp; j++)
+      for (int i = 1; i <= d.np; i++) {
+        const R x = xin(i, j, k);
+        const R f1p = donor(x, xin(i + 1, j, k), u1(i + 1, j, k));
+        const R f1 = donor(xin(i - 1, j, k), x, u1(i, j, k));
+        const R f2p = donor(x, xin(i, j + 1, k), u2(i, j + 1, k));
+        const R f2 = donor(xin(i, j - 1, k), x, u2(i, j, k));
+        R f3p, f3;
+        if (!d.bz && k == 1) { f3p = donor(x, xin(i, j, k + 1), u3(i, j, k + 1)); f3 = -f3p; }
+        else if (!d.bz && k == d.lp) { f3 = donor(xin(i, j, k - 1), x, u3(i, j, k)); f3p = -f3; }
+        else { f3p = donor(x, xin(i, j, k + 1), u3(i, j, k + 1)); f3 = donor(xin(i, j, k - 1), x, u3(i, j, k)); }
+        xant(i, j, k) = x - (f1p - f1 + f2p - f2 + f3p - f3) / h(i, j, k);
+        fn1(i, j, k) = f1;
+        fn2(i, j, k) = f2;
+        fn3(i, j, k) = f3;
+        if (i == d.np) fn1(d.np + 1, j, k) = f1p;  // :192-197
+        if (j == d.mp) fn2(i, d.mp + 1, k) = f2p;  // :198-203
+        if (k == d.lp) fn3(i, j, d.lp + 1) = f3p;  // :205-210
+      }
+  Buf<R> w1(NX + 1, NY, NZ), w2(NX, NY + 1, NZ), w3(NX, NY, NZ + 1);
+  Buf<R>* xfin = &xant;
+  Buf<R> xnew(NX, NY, NZ);
+  if (!liner) {
+    Buf<R> v1(NX + 1, NY, NZ), v2(NX, NY + 1, NZ), v3(NX, NY, NZ + 1);
+    Buf<R> mx(NX, NY, NZ), mn(NX, NY, NZ), cp(NX, NY, NZ), cn(NX, NY, NZ);
+    Buf<R> xb(NX, NY, NZ);
+    std::copy(xin.d.begin(), xin.d.end(), xb.d.begin());
+    halo_last(xb, d);
+    halo_second_last(xant, d);
+    pseudo_gauge(d, xant, u1, u2, u3, h, v1, v2, v3);
+    bounds_fold(d, xant, mx, mn, true, xb);
+    cpcn(d, xant, mx, mn, h, v1, v2, v3, cp, cn, ep);
+    // with rhr = 1 the gauge update rhr*(xant/rhr - div/h) is xant - div/h (:482-485)
+    limit_update_gauge(d, true, xant, v1, v2, v3, cp, cn, ones, h, w1, w2, w3, xnew);
+    xfin = &xnew;
+  }
+  // outputs (:486-493, 570-606); mass fluxes on faces 1..n+1
+  for (int k = 1; k <= d.lp; k++)
+    for (int j = 1; j <= d.mp; j++)
+      for (int i = 1; i <= d.np; i++) {
+        const R xv = (*xfin)(i, j, k);
+        X(i, j, k) = xv;
+        const R xc = xv * h(i, j, k);
+        XC(i, j, k) = xc;
+        P1(i, j, k) = xc * PE(i, j, k);
+        P2(i, j, k) = xc;
+        RO(i, j, k) = RA(i, j, k) / xc;
+      }
+  // boundary faces of the upwind fluxes follow the same rules as the others
+  if (d.bx) wrap(fn1, d, true, false, false);
+  if (d.by) wrap(fn2, d, false, true, false);
+  if (d.bz) wrap(fn3, d, false, false, true);
+  else
+    for (int j = 1; j <= d.mp; j++)
+      for (int i = 1; i <= d.np; i++) fn3(i, j, 1) = -fn3(i, j, 2);
+  V3<R> U1 = view<R>(u1o, ih, SX + 1, SY), U2 = view<R>(u2o, ih, SX, SY + 1), U3 = view<R>(u3o, ih, SX, SY);
+  for (int k = 1; k <= d.lp + 1; k++)
+    for (int j = 1; j <= d.mp + 1; j++)
+      for (int i = 1; i <= d.np + 1; i++) {
+        if (j <= d.mp && k <= d.lp) U1(i, j, k) = fn1(i, j, k) + (liner ? R(0) : w1(i, j, k));
+        if (i <= d.np && k <= d.lp) U2(i, j, k) = fn2(i, j, k) + (liner ? R(0) : w2(i, j, k));
+        if (i <= d.np && j <= d.mp) U3(i, j, k) = fn3(i, j, k) + (liner ? R(0) : w3(i, j, k));
+      }
+  // psi halo: zero-gradient copy of the old boundary values after the
+  // antidiffusion (cp_last_to_halo_xy, :356), Dirichlet values otherwise
+  if (!d.bx)
+    for (int k = 1; k <= d.lp; k++)
+      for (int j = 1; j <= d.mp; j++) {
+        X(0, j, k) = liner ? xin(0, j, k) : xin(1, j, k);
+        X(d.np + 1, j, k) = liner ? xin(d.np + 1, j, k) : xin(d.np, j, k);
+      }
+  if (!d.by)
+    for (int k = 1; k <= d.lp; k++)
+      for (int i = 1; i <= d.np; i++) {
+        X(i, 0, k) = liner ? xin(i, 0, k) : xin(i, 1, k);
+        X(i, d.mp + 1, k) = liner ? xin(i, d.mp + 1, k) : xin(i, d.mp, k);
+      }
+  return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -772,6 +905,15 @@ int orc_upwind_f64(const orc_grid* g, const double* x, const double* bcx, const 
     for (int j = 1; j <= d.mp; j++)
       for (int i = 1; i <= d.np; i++) XO(i, j, k) = xant(i, j, k);
   return 0;
+}
+
+int orc_rho_gauge_f64(const orc_grid* g, double* ox, double* oy, double* oz, double* u, double* v,
+                      double* w, double* u1, double* u2, double* u3, double* x_in, double* x_incomp,
+                      const double* h, double* rhoadv, double* rhr, const double* pexe, double* pexr1,
+                      double* pexr2, const double* bcx, const double* bcy, double dxi, double dyi,
+                      double dzi, double dt, double dt_ratio, int liner) {
+  return rho_gauge<double>(g, ox, oy, oz, u, v, w, u1, u2, u3, x_in, x_incomp, h, rhoadv, rhr, pexe,
+                           pexr1, pexr2, bcx, bcy, dxi, dyi, dzi, dt, dt_ratio, liner);
 }
 
 int orc_velprd_f64(const orc_grid* g, double* ox, double* oy, double* oz, double* u, double* v,

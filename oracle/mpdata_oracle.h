@@ -19,10 +19,9 @@
  *
  * Parity pinning: the reference ships one known answer (the 59^3 rotating
  * sphere "Error L2 norm" 0.0028, advection_dwarf_test_modular.f90:157-158);
- * the oracle reproduces it (tests/test_oracle_cpu.py).  A second, independent
- * numpy restatement (oracle/mpdata_np.py) is compared with this one bit for
- * bit.  No Fortran toolchain exists here or on the GPU host, so field-level
- * parity against the reference binary itself is unpinned beyond the KAT.
+ * the oracle reproduces it (tests/test_oracle_cpu.py).  No Fortran toolchain
+ * exists here or on the GPU host, so field-level parity against the
+ * reference binary itself is unpinned beyond the KAT.
  *
  * Arrays are Fortran column-major with the reference's halo extents:
  *   psi-shaped  (1-ih:np+ih,   1-ih:mp+ih,   1-ih:lp+ih)
@@ -90,6 +89,17 @@ int orc_velprd_f32(const orc_grid* g, float* ox, float* oy, float* oz, float* u,
  * shaped, halos overwritten by the one-sided extrapolation) -> C grid. */
 int orc_a_to_c_f64(const orc_grid* g, double* uadv, double* vadv, double* wadv, double* u1,
                    double* u2, double* u3);
+
+/* mpdata3d_rho_gauge_gpubc (mpdata3d-rho-gauge-gpubc.f90:23-622): predictor,
+ * upwind keeping its fluxes, gauge antidiffusion (iord=2, nonoscillatory),
+ * then x_incomp = x*h, pexr1 = x_incomp*pexe, pexr2 = x_incomp,
+ * rhr = rhoadv/x_incomp (rhoadv = the input x_incomp), and the mass fluxes
+ * u1..u3 = upwind flux + limited antidiffusive flux.  liner=1: upwind only. */
+int orc_rho_gauge_f64(const orc_grid* g, double* ox, double* oy, double* oz, double* u, double* v,
+                      double* w, double* u1, double* u2, double* u3, double* x_in, double* x_incomp,
+                      const double* h, double* rhoadv, double* rhr, const double* pexe, double* pexr1,
+                      double* pexr2, const double* bcx, const double* bcy, double dxi, double dyi,
+                      double dzi, double dt, double dt_ratio, int liner);
 
 /* Threads used by the OpenMP loops (1 = the serial reference build). */
 void orc_set_threads(int n);

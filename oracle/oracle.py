@@ -48,6 +48,8 @@ def lib():
         _lib.orc_velprd_f64.restype = I
         _lib.orc_velprd_f32.argtypes = [ctypes.POINTER(OrcGrid)] + [P] * 7 + [F] * 5 + [P] * 3
         _lib.orc_velprd_f32.restype = I
+        _lib.orc_rho_gauge_f64.argtypes = [ctypes.POINTER(OrcGrid)] + [P] * 19 + [D] * 5 + [I]
+        _lib.orc_rho_gauge_f64.restype = I
         _lib.orc_a_to_c_f64.argtypes = [ctypes.POINTER(OrcGrid)] + [P] * 6
         _lib.orc_a_to_c_f64.restype = I
         _lib.orc_set_threads.argtypes = [I]
@@ -101,6 +103,18 @@ def velprd(g, ox, oy, oz, h, dxi, dyi, dzi, dt, dt_ratio, u1, u2, u3, u=None, v=
                             _ptr(u1, d), _ptr(u2, d), _ptr(u3, d))
     if rc != 0:
         raise ValueError("oracle velprd failed with code %d" % rc)
+
+
+def rho_gauge(g, ox, oy, oz, u1, u2, u3, x_in, x_incomp, h, rhoadv, rhr, pexe, pexr1, pexr2, bcx,
+              bcy, dxi, dyi, dzi, dt, dt_ratio, liner=0, u=None, v=None, w=None):
+    d = np.float64
+    rc = lib().orc_rho_gauge_f64(ctypes.byref(g), _ptr(ox, d), _ptr(oy, d), _ptr(oz, d), _ptr(u, d),
+                                 _ptr(v, d), _ptr(w, d), _ptr(u1, d), _ptr(u2, d), _ptr(u3, d),
+                                 _ptr(x_in, d), _ptr(x_incomp, d), _ptr(h, d), _ptr(rhoadv, d),
+                                 _ptr(rhr, d), _ptr(pexe, d), _ptr(pexr1, d), _ptr(pexr2, d),
+                                 _ptr(bcx, d), _ptr(bcy, d), dxi, dyi, dzi, dt, dt_ratio, int(liner))
+    if rc != 0:
+        raise ValueError("oracle rho_gauge failed with code %d" % rc)
 
 
 def a_to_c(g, uadv, vadv, wadv, u1, u2, u3):

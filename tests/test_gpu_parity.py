@@ -204,3 +204,40 @@ def test_bad_arguments_raise(M):
         ws.step(d["x"], d["u1"], d["u2"], d["u3"], d["h"], d["rhr"])
     ws.close()
     torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("ibc", [(0, 0, 0), (1, 1, 1), (1, 0, 0)])
+@pytest.mark.parametrize("liner", [0, 1])
+def test_rho_gauge_density_step(M, oracle, ibc, liner):
+    """mpdata3d_rho_gauge_gpubc: every output (x_in, x_incomp, rhoadv, rhr,
+    pexr1, pexr2, mass fluxes u1..u3, the three momentum levels) bit for bit."""
+    import torch
+    n, m, l, ih = 11, 9, 7, 1
+    rng = np.random.default_rng(17 + liner + 2 * sum(ibc))
+    sh = W.shapes(n, m, l, ih)
+    lev = sh["psi"] + (3,)
+    arrs = dict(ox=rng.uniform(-0.3, 0.3, lev), oy=rng.uniform(-0.3, 0.3, lev), oz=rng.uniform(-0.3, 0.3, lev),
+                u1=np.zeros(sh["u1"]), u2=np.zeros(sh["u2"]), u3=np.zeros(sh["u3"]),
+                x_in=rng.uniform(0.5, 1.5, sh["psi"]), x_incomp=rng.uniform(0.5, 1.5, sh["psi"]),
+                h=rng.uniform(0.8, 1.2, sh["psi"]), rhoadv=np.zeros(sh["psi"]), rhr=np.zeros(sh["psi"]),
+                pexe=rng.uniform(0.9, 1.1, sh["psi"]), pexr1=np.zeros(sh["psi"]), pexr2=np.zeros(sh["psi"]),
+                bcx=rng.uniform(0.5, 1.5, sh["bcx"]), bcy=rng.uniform(0.5, 1.5, sh["bcy"]))
+    arrs = {k: np.asfortranarray(v) for k, v in arrs.items()}
+    dv = {k: M.fortran_device(v) for k, v in arrs.items()}
+    ws = M.Workspace(n, m, l, ih, *ibc, iord=2, nonos=1, gauge=1, precision=64)
+    sc = dict(dxi=1.0, dyi=1.0, dzi=1.0, dt=1.0, dt_ratio=1.0)
+    ws.mpdata3d_rho_gauge_gpubc(dv["ox"], dv["oy"], dv["oz"], dv["u1"], dv["u2"], dv["u3"], dv["x_in"],
+                                dv["x_incomp"], dv["h"], dv["rhoadv"], dv["rhr"], dv["pexe"], dv["pexr1"],
+                                dv["pexr2"], bcx=dv["bcx"], bcy=dv["bcy"], liner=liner, **sc)
+    torch.cuda.synchronize()
+    oracle.rho_gauge(oracle.grid(n, m, l, ih, *ibc), arrs["ox"], arrs["oy"], arrs["oz"], arrs["u1"], arrs["u2"],
+                     arrs["u3"], arrs["x_in"], arrs["x_incomp"], arrs["h"], arrs["rhoadv"], arrs["rhr"],
+                     arrs["pexe"], arrs["pexr1"], arrs["pexr2"], arrs["bcx"], arrs["bcy"], liner=liner, **sc)
+    I, J, K = slice(ih, ih + n), slice(ih, ih + m), slice(ih, ih + l)
+    for k in ("x_in", "x_incomp", "rhoadv", "rhr", "pexr1", "pexr2"):
+        np.testing.assert_array_equal(W.interior(M.to_numpy(dv[k])), W.interior(arrs[k]), err_msg=k)
+    np.testing.assert_array_equal(M.to_numpy(dv["x_in"]), arrs["x_in"], err_msg="x_in with halo")
+    np.testing.assert_array_equal(M.to_numpy(dv["u1"])[ih:ih + n + 1, J, K], arrs["u1"][ih:ih + n + 1, J, K])
+    np.testing.assert_array_equal(M.to_numpy(dv["u2"])[I, ih:ih + m + 1, K], arrs["u2"][I, ih:ih + m + 1, K])
+    np.testing.assert_array_equal(M.to_numpy(dv["u3"])[I, J, ih:ih + l + 1], arrs["u3"][I, J, ih:ih + l + 1])
+    ws.close()
