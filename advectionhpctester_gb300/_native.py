@@ -60,6 +60,7 @@ SIGNATURES = {
     "mpdata_mass_f64": ([ctypes.POINTER(MpdataGrid), P, P, P, ctypes.POINTER(D), P], I),
     "mpdata_mass_f32": ([ctypes.POINTER(MpdataGrid), P, P, P, ctypes.POINTER(D), P], I),
     "mpdata_error_norms": ([ctypes.POINTER(MpdataGrid), P, I, P, I, ctypes.POINTER(D), P], I),
+    "mpdata_step_noalloc_f64": ([ctypes.POINTER(MpdataGrid), ctypes.POINTER(MpdataOpts)] + [P] * 9, I),
     "mpdata_strerror": ([I], ctypes.c_char_p),
     "mpdata_version": ([], ctypes.c_char_p),
 }

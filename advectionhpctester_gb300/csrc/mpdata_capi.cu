@@ -466,6 +466,7 @@ const char* mpdata_strerror(int code) {
     case MPDATA_E_CUDA: return "CUDA runtime error";
     case MPDATA_E_DEVICE: return "device error word set (non-finite value)";
     case MPDATA_E_UNSUPPORTED: return "reference option outside this library's scope";
+    case MPDATA_E_TOO_LARGE: return "grid exceeds the 32768-cell scratch of mpdata_step_noalloc_f64";
     default: return "unknown error";
   }
 }

@@ -41,6 +41,7 @@ extern "C" {
 #define MPDATA_E_CUDA -5        /* a CUDA runtime call failed */
 #define MPDATA_E_DEVICE -6      /* the device error word is set (non-finite result) */
 #define MPDATA_E_UNSUPPORTED -7 /* a reference option outside this library's scope */
+#define MPDATA_E_TOO_LARGE -8   /* grid larger than the fixed scratch of mpdata_step_noalloc_f64 */
 
 typedef struct {
   int np, mp, lp, ih;   /* interior cells per axis and halo width (ih >= 1) */
@@ -212,6 +213,23 @@ int mpdata_mass_f32(const mpdata_grid* grid, const float* psi, const float* h, c
  * out[0] = max|a-b|, out[1] = ||a-b||_2, out[2] = max|b|, out[3] = ||b||_2. */
 int mpdata_error_norms(const mpdata_grid* grid, const void* a, int a_is_f64, const void* b,
                        int b_is_f64, double* out, void* stream);
+
+/* ---- a step that allocates nothing ----------------------------------------
+ * No counterpart in the reference.  For callers that must not have the
+ * library allocate device memory (a model that reserves its device memory
+ * up front through its own pool, or whose memory use is fixed at start-up):
+ * the FP64 step of mpdata_step_f64 without a workspace.  Its scratch is one
+ * file-scope device array sized for MPDATA_NOALLOC_MAX_CELLS interior cells
+ * (about 5 MB, held on every GPU that loads the library until exit); larger
+ * grids return MPDATA_E_TOO_LARGE.  No cudaMalloc/cudaFree is called.  The
+ * first call on a device looks up the array's device address, so make it
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU race, so order them (one stream, or synchronise).  Nothing needs
+ * clearing between calls.  opts->precision must be 64. */
+#define MPDATA_NOALLOC_MAX_CELLS 32768
+int mpdata_step_noalloc_f64(const mpdata_grid* grid, const mpdata_opts* opts, double* psi,
+                            const double* u1, const double* u2, const double* u3, const double* h,
+                            const double* rhr, const double* bcx, const double* bcy, void* stream);
 
 const char* mpdata_strerror(int code);
 const char* mpdata_version(void);
