@@ -44,6 +44,12 @@ SIGNATURES = {
     "mpdata_velprd_f32": ([P] * 8 + [F] * 5 + [P] * 4, I),
     "mpdata_rho_gauge_f64": ([P] * 20 + [D] * 5 + [I, P], I),
     "mpdata_rho_gauge_f32": ([P] * 20 + [F] * 5 + [I, P], I),
+    "mpdata_step_adjoint_f64": ([P] * 14, I),
+    "mpdata_step_adjoint_f32": ([P] * 14, I),
+    "mpdata_adjoint_run_f64": ([P, I, I] + [P] * 9 + [ctypes.POINTER(D)] + [P] * 4 +
+                               [ctypes.POINTER(ctypes.c_longlong), P], I),
+    "mpdata_adjoint_run_f32": ([P, I, I] + [P] * 9 + [ctypes.POINTER(D)] + [P] * 4 +
+                               [ctypes.POINTER(ctypes.c_longlong), P], I),
     "mpdata_ws_error": ([P, ctypes.POINTER(I)], I),
     "mpdata_launch_count": ([], ctypes.c_longlong),
     "mpdata_ws_profile": ([P, I], I),

@@ -1,0 +1,444 @@
+// Adjoint of the MPDATA step (infinite-gauge form, one corrective pass,
+// nonoscillatory limiter on or off).  No reference code exists for it; it
+// differentiates the forward step of mpdata_body.cuh exactly, with every
+// branch (pp, pn, min3, the limiter's max/min over the 7-point stars, abs)
+// taken at the forward values ("piecewise at the forward branch").
+//
+// Given psi at the start of a step, the velocities and lambda = dJ/dpsi_new,
+// the step adjoint recomputes the forward intermediates (upwind field, face
+// reciprocals, pseudo-velocities, cp/cn) into the workspace and runs one
+// reverse kernel per forward stage:
+//   update    x_new = rhr*(q - div(w)/h)           -> lambda_xant, lambda_w
+//   limiter   w = pp(v)*A1 - pn(v)*A2              -> lambda_v, lambda_cp, lambda_cn
+//   bounds    cp,cn from the star extrema and v    -> lambda_x, lambda_xant, lambda_v
+//   pseudo    v(xant, u)                           -> lambda_xant, lambda_u
+//   upwind    xant(x, u)                           -> lambda_x, lambda_u
+// Each reverse kernel walks the forward stage's reads (with the same boundary
+// index maps) and scatters the products of the local partial derivatives
+// with atomic adds, so wall faces (constant zero), mirrored z faces and
+// periodic wraps are transposed exactly as the forward reads them.  The
+// summation order of the atomics is not fixed: results agree with the FP64
+// AD oracle to rounding, not bit for bit.
+#include "mpdata_body.cuh"
+#include "mpdata_stages.cuh"
+
+namespace mpdata {
+
+// ---- adjoints of the read maps --------------------------------------------
+template <class R>
+__device__ __forceinline__ void addat(const Arr<R>& A, int i, int j, int k, R v) {
+  atomicAdd(&A.at(i, j, k), v);
+}
+// xr(): the field with the xant halo rule (reflection or wrap)
+template <class R>
+__device__ __forceinline__ void xr_add(const Geo& g, const Arr<R>& L, int i, int j, int k, R v) {
+  addat(L, g.bx ? wrapi(i, g.np) : refl(i, g.np), g.by ? wrapi(j, g.mp) : refl(j, g.mp), cz(g, k), v);
+}
+// fx/fy/fz<AIN>()
+template <class R, bool AIN>
+__device__ __forceinline__ void fx_add(const Geo& g, const Arr<R>& A, int f, int j, int k, R v) {
+  j = cy(g, j);
+  k = cz(g, k);
+  if (g.bx) { addat(A, wrapi(f, g.np), j, k, v); return; }
+  if (AIN) { addat(A, f, j, k, v); return; }
+  if (f <= 1 || f > g.np) return;  // wall faces are the constant 0
+  addat(A, f, j, k, v);
+}
+template <class R, bool AIN>
+__device__ __forceinline__ void fy_add(const Geo& g, const Arr<R>& A, int i, int f, int k, R v) {
+  i = cx(g, i);
+  k = cz(g, k);
+  if (g.by) { addat(A, i, wrapi(f, g.mp), k, v); return; }
+  if (AIN) { addat(A, i, f, k, v); return; }
+  if (f <= 1 || f > g.mp) return;
+  addat(A, i, f, k, v);
+}
+template <class R, bool AIN>
+__device__ __forceinline__ void fz_add(const Geo& g, const Arr<R>& A, int i, int j, int f, R v) {
+  i = cx(g, i);
+  j = cy(g, j);
+  if (g.bz) { addat(A, i, j, wrapi(f, g.lp), v); return; }
+  if (AIN) { addat(A, i, j, f, v); return; }
+  if (f <= 1) { addat(A, i, j, 2, -v); return; }       // face 1 reads -face 2
+  if (f > g.lp) { addat(A, i, j, g.lp, -v); return; }  // face lp+1 reads -face lp
+  addat(A, i, j, f, v);
+}
+
+// derivative conventions of the branches (forward values decide)
+template <class R> __device__ __forceinline__ R dpp(R y) { return sgn(y) ? R(0) : (y > R(0) ? R(1) : R(0)); }
+template <class R> __device__ __forceinline__ R dpn(R y) { return y < R(0) ? R(-1) : R(0); }
+template <class R> __device__ __forceinline__ R dabs(R y) { return sgn(y) ? R(-1) : R(1); }
+
+
+#define ACELL                                                \
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;  \
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;  \
+  const int k = blockIdx.z + 1;                              \
+  if (i > P.g.np || j > P.g.mp) return;                      \
+  const Geo& g = P.g;
+
+// ---- update: x_new = rhr*(q - D/h), D = sum of signed limited fluxes -------
+template <class R>
+__global__ void __launch_bounds__(128) ka_update(const Prob<R> P, const AdjArr<R> A) {
+  ACELL
+  const R ln = A.lam.ld(i, j, k);
+  const R rh = P.rhr.ld(i, j, k);
+  const R lt = rh * ln;                 // d x_new / d t, t = q - D/h
+  A.lxant.at(i, j, k) = lt / rh;        // q = xant/rhr
+  const R lD = -lt / P.h.ld(i, j, k);
+  fx_add<R, false>(g, A.lw1, i + 1, j, k, lD);
+  fx_add<R, false>(g, A.lw1, i, j, k, -lD);
+  fy_add<R, false>(g, A.lw2, i, j + 1, k, lD);
+  fy_add<R, false>(g, A.lw2, i, j, k, -lD);
+  fz_add<R, false>(g, A.lw3, i, j, k + 1, lD);
+  fz_add<R, false>(g, A.lw3, i, j, k, -lD);
+}
+
+// ---- limiter: w = pp(v)*min3(cp(c),cn(c-1)) - pn(v)*min3(cp(c-1),cn(c)) -------
+// min3(a,b) = mn2(mn2(1,a),b): b is taken when b <= t, else a when a <= 1.
+template <class R>
+__device__ __forceinline__ void min3_adj(R a, R b, R lam, const Arr<R>& La, int ia, int ja, int ka,
+                                         const Arr<R>& Lb, int ib, int jb, int kb) {
+  const R t = R(1) < a ? R(1) : a;
+  if (!(t < b)) { addat(Lb, ib, jb, kb, lam); return; }
+  if (!(R(1) < a)) addat(La, ia, ja, ka, lam);
+}
+
+template <class R, bool NONOS>
+__global__ void __launch_bounds__(128) ka_limit(const Prob<R> P, const AdjArr<R> A) {
+  ACELL
+  const R cpc = NONOS ? P.cp.ld(i, j, k) : R(0), cnc = NONOS ? P.cn.ld(i, j, k) : R(0);
+#define LIMIT_FACE(V, LV, LW, IM, JM, KM)                                                  \
+  {                                                                                        \
+    const R v = V.ld(i, j, k);                                                             \
+    const R lw = LW.ld(i, j, k);                                                           \
+    if (!NONOS) {                                                                          \
+      addat(LV, i, j, k, lw);                                                              \
+    } else {                                                                               \
+      const R cpm = P.cp.ld(IM, JM, KM), cnm = P.cn.ld(IM, JM, KM);                        \
+      const R a1 = min3(cpc, cnm), a2 = min3(cpm, cnc);                                    \
+      addat(LV, i, j, k, lw * (dpp(v) * a1 - dpn(v) * a2));                                \
+      min3_adj(cpc, cnm, lw * pp(v), A.lcp, i, j, k, A.lcn, IM, JM, KM);                    \
+      min3_adj(cpm, cnc, -lw * pn(v), A.lcp, IM, JM, KM, A.lcn, i, j, k);                   \
+    }                                                                                      \
+  }
+  if (g.bx || i > 1) LIMIT_FACE(P.v1, A.lv1, A.lw1, wrapi(i - 1, g.np), j, k)
+  if (g.by || j > 1) LIMIT_FACE(P.v2, A.lv2, A.lw2, i, wrapi(j - 1, g.mp), k)
+  if (g.bz || k > 1) LIMIT_FACE(P.v3, A.lv3, A.lw3, i, j, wrapi(k - 1, g.lp))
+#undef LIMIT_FACE
+}
+
+// ---- bounds: cp = (mx-x)h/Dp, cn = (x-mn)h/Dn -------------------------------
+// The extrema are re-folded in the oracle's order (mx2/mn2 trees) so ties go
+// to the same operand: element ids 0..6 are x_in, 7..13 xant.
+template <class R>
+struct Arg {
+  R v;
+  int id;
+};
+template <class R> __device__ __forceinline__ Arg<R> amax(Arg<R> a, Arg<R> b) { return a.v > b.v ? a : b; }
+template <class R> __device__ __forceinline__ Arg<R> amin(Arg<R> a, Arg<R> b) { return a.v < b.v ? a : b; }
+
+template <class R>
+__global__ void __launch_bounds__(128) ka_bounds(const Prob<R> P, const AdjArr<R> A) {
+  ACELL
+  const bool lo = g.bz || k > 1, hi = g.bz || k < g.lp;
+  const Arr<R>& X = P.xant;
+  const Arr<R>& xin = P.psi;
+  // star cells: x_in with the zero-gradient map, xant with the reflection map
+  const int im = g.bx ? wrapi(i - 1, g.np) : clampi(i - 1, g.np);
+  const int ip = g.bx ? wrapi(i + 1, g.np) : clampi(i + 1, g.np);
+  const int jm = g.by ? wrapi(j - 1, g.mp) : clampi(j - 1, g.mp);
+  const int jp = g.by ? wrapi(j + 1, g.mp) : clampi(j + 1, g.mp);
+  const int km = cz(g, k - 1), kp = cz(g, k + 1);
+  const int ri_m = g.bx ? wrapi(i - 1, g.np) : refl(i - 1, g.np), ri_p = g.bx ? wrapi(i + 1, g.np) : refl(i + 1, g.np);
+  const int rj_m = g.by ? wrapi(j - 1, g.mp) : refl(j - 1, g.mp), rj_p = g.by ? wrapi(j + 1, g.mp) : refl(j + 1, g.mp);
+  // element table: (i,j,k) of ids 0..13
+  const int ci[14] = {im, i, ip, i, i, i, i, ri_m, i, ri_p, i, i, i, i};
+  const int cj[14] = {j, j, j, jm, jp, j, j, j, j, j, rj_m, rj_p, j, j};
+  const int ck[14] = {k, k, k, k, k, km, kp, k, k, k, k, k, km, kp};
+  Arg<R> e[14];
+  for (int n = 0; n < 7; n++) e[n] = Arg<R>{xin.ld(ci[n], cj[n], ck[n]), n};
+  for (int n = 7; n < 14; n++) e[n] = Arg<R>{X.ld(ci[n], cj[n], ck[n]), n};
+  Arg<R> ma = amax(amax(amax(e[0], e[1]), amax(e[2], e[3])), e[4]);
+  Arg<R> mi = amin(amin(amin(e[0], e[1]), amin(e[2], e[3])), e[4]);
+  if (lo) { ma = amax(ma, e[5]); mi = amin(mi, e[5]); }
+  if (hi) { ma = amax(ma, e[6]); mi = amin(mi, e[6]); }
+  ma = amax(amax(amax(ma, e[7]), amax(e[8], e[9])), amax(e[10], e[11]));
+  mi = amin(amin(amin(mi, e[7]), amin(e[8], e[9])), amin(e[10], e[11]));
+  if (lo) { ma = amax(ma, e[12]); mi = amin(mi, e[12]); }
+  if (hi) { ma = amax(ma, e[13]); mi = amin(mi, e[13]); }
+
+  const R x = X.ld(i, j, k), hc = P.h.ld(i, j, k);
+  const R lcp = A.lcp.ld(i, j, k), lcn = A.lcn.ld(i, j, k);
+  const R e1 = fx<R, false>(g, P.v1, i + 1, j, k), w1 = fx<R, false>(g, P.v1, i, j, k);
+  const R e2 = fy<R, false>(g, P.v2, i, j + 1, k), w2 = fy<R, false>(g, P.v2, i, j, k);
+  const R e3 = fz<R, false>(g, P.v3, i, j, k + 1), w3 = fz<R, false>(g, P.v3, i, j, k);
+  const R ep = Eps<R>::v;
+  const R Dp = pn(e1) + pp(w1) + pn(e2) + pp(w2) + pn(e3) + pp(w3) + ep;
+  const R Dn = pp(e1) + pn(w1) + pp(e2) + pn(w2) + pp(e3) + pn(w3) + ep;
+  const R cpv = (ma.v - x) * hc / Dp, cnv = (x - mi.v) * hc / Dn;
+  const R lnum_p = lcp * hc / Dp, lnum_n = lcn * hc / Dn;
+  // d cp/d mx, d cp/d x, d cn/d x, d cn/d mn
+  const Arr<R>& Lmax = ma.id < 7 ? A.lx : A.lxant;
+  const Arr<R>& Lmin = mi.id < 7 ? A.lx : A.lxant;
+  addat(Lmax, ci[ma.id], cj[ma.id], ck[ma.id], lnum_p);
+  addat(Lmin, ci[mi.id], cj[mi.id], ck[mi.id], -lnum_n);
+  addat(A.lxant, i, j, k, lnum_n - lnum_p);
+  // d/dD: -c/D
+  const R lDp = -lcp * cpv / Dp, lDn = -lcn * cnv / Dn;
+  // Dp = pn(e)+pp(w)+..., Dn = pp(e)+pn(w)+... over the six faces
+  fx_add<R, false>(g, A.lv1, i + 1, j, k, lDp * dpn(e1) + lDn * dpp(e1));
+  fx_add<R, false>(g, A.lv1, i, j, k, lDp * dpp(w1) + lDn * dpn(w1));
+  fy_add<R, false>(g, A.lv2, i, j + 1, k, lDp * dpn(e2) + lDn * dpp(e2));
+  fy_add<R, false>(g, A.lv2, i, j, k, lDp * dpp(w2) + lDn * dpn(w2));
+  fz_add<R, false>(g, A.lv3, i, j, k + 1, lDp * dpn(e3) + lDn * dpp(e3));
+  fz_add<R, false>(g, A.lv3, i, j, k, lDp * dpp(w3) + lDn * dpn(w3));
+}
+
+// ---- pseudo-velocity (gauge): v = vdyf(xl,xr,a,hm) - 0.125*a*hm*cr ------------
+// cr = S2*rat4(y0,y1,y2,y3) [+ S3*rat4(z0,z1,z2,z3)], S = sums of four u faces.
+template <class R>
+__global__ void __launch_bounds__(128) ka_pseudo(const Prob<R> P, const AdjArr<R> A) {
+  ACELL
+  const Arr<R>& X = P.xant;
+  const bool zt = g.bz || (k > 1 && k < g.lp);
+#define XX(a, b, c) xr<R>(g, X, (a), (b), (c))
+#define LX(a, b, c, v) xr_add<R>(g, A.lxant, (a), (b), (c), (v))
+  // x faces
+  if (g.bx || i > 1) {
+    const R lv = A.lv1.ld(i, j, k);
+    const R hm = P.hmx.ld(i, j, k), a = fx<R, true>(g, P.u1, i, j, k);
+    const R xl = XX(i - 1, j, k), xrr = XX(i, j, k);
+    const R S2 = fy<R, true>(g, P.u2, i - 1, j, k) + fy<R, true>(g, P.u2, i - 1, j + 1, k) +
+                 fy<R, true>(g, P.u2, i, j + 1, k) + fy<R, true>(g, P.u2, i, j, k);
+    const R R2 = rat4(XX(i - 1, j - 1, k), XX(i, j - 1, k), XX(i - 1, j + 1, k), XX(i, j + 1, k));
+    R cr = S2 * R2, S3 = R(0), R3 = R(0);
+    if (zt) {
+      S3 = fz<R, true>(g, P.u3, i - 1, j, k) + fz<R, true>(g, P.u3, i - 1, j, k + 1) +
+           fz<R, true>(g, P.u3, i, j, k + 1) + fz<R, true>(g, P.u3, i, j, k);
+      R3 = rat4(XX(i - 1, j, k - 1), XX(i, j, k - 1), XX(i - 1, j, k + 1), XX(i, j, k + 1));
+      cr = cr + S3 * R3;
+    }
+    const R K = (fabs(a) - a * a * hm) * R(0.5);
+    const R la = lv * ((dabs(a) - R(2) * a * hm) * (xrr - xl) * R(0.5) - R(0.125) * hm * cr);
+    fx_add<R, true>(g, A.gu1, i, j, k, la);
+    LX(i, j, k, lv * K);
+    LX(i - 1, j, k, -lv * K);
+    const R lcr = -lv * R(0.125) * a * hm;
+    const R lS2 = lcr * R2, lR2 = lcr * S2 * R(0.25);
+    fy_add<R, true>(g, A.gu2, i - 1, j, k, lS2);
+    fy_add<R, true>(g, A.gu2, i - 1, j + 1, k, lS2);
+    fy_add<R, true>(g, A.gu2, i, j + 1, k, lS2);
+    fy_add<R, true>(g, A.gu2, i, j, k, lS2);
+    LX(i, j + 1, k, lR2); LX(i - 1, j + 1, k, lR2); LX(i, j - 1, k, -lR2); LX(i - 1, j - 1, k, -lR2);
+    if (zt) {
+      const R lS3 = lcr * R3, lR3 = lcr * S3 * R(0.25);
+      fz_add<R, true>(g, A.gu3, i - 1, j, k, lS3);
+      fz_add<R, true>(g, A.gu3, i - 1, j, k + 1, lS3);
+      fz_add<R, true>(g, A.gu3, i, j, k + 1, lS3);
+      fz_add<R, true>(g, A.gu3, i, j, k, lS3);
+      LX(i, j, k + 1, lR3); LX(i - 1, j, k + 1, lR3); LX(i, j, k - 1, -lR3); LX(i - 1, j, k - 1, -lR3);
+    }
+  }
+  // y faces
+  if (g.by || j > 1) {
+    const R lv = A.lv2.ld(i, j, k);
+    const R hm = P.hmy.ld(i, j, k), a = fy<R, true>(g, P.u2, i, j, k);
+    const R xl = XX(i, j - 1, k), xrr = XX(i, j, k);
+    const R S1 = fx<R, true>(g, P.u1, i, j - 1, k) + fx<R, true>(g, P.u1, i, j, k) +
+                 fx<R, true>(g, P.u1, i + 1, j, k) + fx<R, true>(g, P.u1, i + 1, j - 1, k);
+    const R R1 = rat4(XX(i - 1, j - 1, k), XX(i - 1, j, k), XX(i + 1, j - 1, k), XX(i + 1, j, k));
+    R cr = S1 * R1, S3 = R(0), R3 = R(0);
+    if (zt) {
+      S3 = fz<R, true>(g, P.u3, i, j - 1, k) + fz<R, true>(g, P.u3, i, j, k) +
+           fz<R, true>(g, P.u3, i, j, k + 1) + fz<R, true>(g, P.u3, i, j - 1, k + 1);
+      R3 = rat4(XX(i, j - 1, k - 1), XX(i, j, k - 1), XX(i, j - 1, k + 1), XX(i, j, k + 1));
+      cr = cr + S3 * R3;
+    }
+    const R K = (fabs(a) - a * a * hm) * R(0.5);
+    const R la = lv * ((dabs(a) - R(2) * a * hm) * (xrr - xl) * R(0.5) - R(0.125) * hm * cr);
+    fy_add<R, true>(g, A.gu2, i, j, k, la);
+    LX(i, j, k, lv * K);
+    LX(i, j - 1, k, -lv * K);
+    const R lcr = -lv * R(0.125) * a * hm;
+    const R lS1 = lcr * R1, lR1 = lcr * S1 * R(0.25);
+    fx_add<R, true>(g, A.gu1, i, j - 1, k, lS1);
+    fx_add<R, true>(g, A.gu1, i, j, k, lS1);
+    fx_add<R, true>(g, A.gu1, i + 1, j, k, lS1);
+    fx_add<R, true>(g, A.gu1, i + 1, j - 1, k, lS1);
+    LX(i + 1, j, k, lR1); LX(i + 1, j - 1, k, lR1); LX(i - 1, j, k, -lR1); LX(i - 1, j - 1, k, -lR1);
+    if (zt) {
+      const R lS3 = lcr * R3, lR3 = lcr * S3 * R(0.25);
+      fz_add<R, true>(g, A.gu3, i, j - 1, k, lS3);
+      fz_add<R, true>(g, A.gu3, i, j, k, lS3);
+      fz_add<R, true>(g, A.gu3, i, j, k + 1, lS3);
+      fz_add<R, true>(g, A.gu3, i, j - 1, k + 1, lS3);
+      LX(i, j, k + 1, lR3); LX(i, j - 1, k + 1, lR3); LX(i, j, k - 1, -lR3); LX(i, j - 1, k - 1, -lR3);
+    }
+  }
+  // z faces
+  if (g.bz || k > 1) {
+    const R lv = A.lv3.ld(i, j, k);
+    const R hm = P.hmz.ld(i, j, k), a = fz<R, true>(g, P.u3, i, j, k);
+    const R xl = XX(i, j, k - 1), xrr = XX(i, j, k);
+    const R S1 = fx<R, true>(g, P.u1, i, j, k - 1) + fx<R, true>(g, P.u1, i, j, k) +
+                 fx<R, true>(g, P.u1, i + 1, j, k) + fx<R, true>(g, P.u1, i + 1, j, k - 1);
+    const R R1 = rat4(XX(i - 1, j, k - 1), XX(i - 1, j, k), XX(i + 1, j, k - 1), XX(i + 1, j, k));
+    const R S2 = fy<R, true>(g, P.u2, i, j, k - 1) + fy<R, true>(g, P.u2, i, j + 1, k - 1) +
+                 fy<R, true>(g, P.u2, i, j + 1, k) + fy<R, true>(g, P.u2, i, j, k);
+    const R R2 = rat4(XX(i, j - 1, k - 1), XX(i, j - 1, k), XX(i, j + 1, k - 1), XX(i, j + 1, k));
+    const R cr = S1 * R1 + S2 * R2;
+    const R K = (fabs(a) - a * a * hm) * R(0.5);
+    const R la = lv * ((dabs(a) - R(2) * a * hm) * (xrr - xl) * R(0.5) - R(0.125) * hm * cr);
+    fz_add<R, true>(g, A.gu3, i, j, k, la);
+    LX(i, j, k, lv * K);
+    LX(i, j, k - 1, -lv * K);
+    const R lcr = -lv * R(0.125) * a * hm;
+    const R lS1 = lcr * R1, lR1 = lcr * S1 * R(0.25);
+    fx_add<R, true>(g, A.gu1, i, j, k - 1, lS1);
+    fx_add<R, true>(g, A.gu1, i, j, k, lS1);
+    fx_add<R, true>(g, A.gu1, i + 1, j, k, lS1);
+    fx_add<R, true>(g, A.gu1, i + 1, j, k - 1, lS1);
+    LX(i + 1, j, k, lR1); LX(i + 1, j, k - 1, lR1); LX(i - 1, j, k, -lR1); LX(i - 1, j, k - 1, -lR1);
+    const R lS2 = lcr * R2, lR2 = lcr * S2 * R(0.25);
+    fy_add<R, true>(g, A.gu2, i, j, k - 1, lS2);
+    fy_add<R, true>(g, A.gu2, i, j + 1, k - 1, lS2);
+    fy_add<R, true>(g, A.gu2, i, j + 1, k, lS2);
+    fy_add<R, true>(g, A.gu2, i, j, k, lS2);
+    LX(i, j + 1, k, lR2); LX(i, j + 1, k - 1, lR2); LX(i, j - 1, k, -lR2); LX(i, j - 1, k - 1, -lR2);
+  }
+#undef XX
+#undef LX
+}
+
+// ---- upwind: xant = rhr*(x - D*hinv), D = signed sum of donor fluxes --------
+// F = donor(xl, xr, u) = pp(u)*xl - pn(u)*xr; dF/du = [u>0]*xl + [u<0]*xr.
+// Open-wall neighbours come from bcx/bcy (constants: no gradient).
+template <class R>
+__device__ __forceinline__ void flux_adj(R lF, R xl, R xr_, R u, bool l_var, const Arr<R>& Lx, int li, int lj,
+                                         int lk, bool r_var, int ri, int rj, int rk, R* lu_out) {
+  if (l_var) addat(Lx, li, lj, lk, lF * pp(u));
+  if (r_var) addat(Lx, ri, rj, rk, -lF * pn(u));
+  *lu_out = lF * (dpp(u) * xl - dpn(u) * xr_);
+}
+
+template <class R>
+__global__ void __launch_bounds__(128) ka_upwind(const Prob<R> P, const AdjArr<R> A) {
+  ACELL
+  const Arr<R>& psi = P.psi;
+  const R lxa = A.lxant.ld(i, j, k);
+  const R rh = P.rhr.ld(i, j, k);
+  addat(A.lx, i, j, k, lxa * rh);
+  const R lD = -lxa * rh * P.hinv.ld(i, j, k);
+  const R x = psi.ld(i, j, k);
+  const long bx0 = (long)(j - 1) + (long)g.mp * (k - 1), bxs = (long)g.mp * g.lp;
+  const long by0 = (long)(i - 1) + (long)g.np * (k - 1), bys = (long)g.np * g.lp;
+  const bool im_var = i > 1 || g.bx, ip_var = i < g.np || g.bx, jm_var = j > 1 || g.by, jp_var = j < g.mp || g.by;
+  const int im = wrapi(i - 1, g.np), ip = wrapi(i + 1, g.np), jm = wrapi(j - 1, g.mp), jp = wrapi(j + 1, g.mp);
+  const R xim = im_var ? psi.ld(im, j, k) : P.bcx[bx0];
+  const R xip = ip_var ? psi.ld(ip, j, k) : P.bcx[bx0 + bxs];
+  const R xjm = jm_var ? psi.ld(i, jm, k) : P.bcy[by0];
+  const R xjp = jp_var ? psi.ld(i, jp, k) : P.bcy[by0 + bys];
+  R lu;
+  // x faces: D = F1(i+1) - F1(i) + ...
+  flux_adj(lD, x, xip, fx<R, true>(g, P.u1, i + 1, j, k), true, A.lx, i, j, k, ip_var, ip, j, k, &lu);
+  fx_add<R, true>(g, A.gu1, i + 1, j, k, lu);
+  flux_adj(-lD, xim, x, P.u1.ld(i, j, k), im_var, A.lx, im, j, k, true, i, j, k, &lu);
+  fx_add<R, true>(g, A.gu1, i, j, k, lu);
+  flux_adj(lD, x, xjp, fy<R, true>(g, P.u2, i, j + 1, k), true, A.lx, i, j, k, jp_var, i, jp, k, &lu);
+  fy_add<R, true>(g, A.gu2, i, j + 1, k, lu);
+  flux_adj(-lD, xjm, x, P.u2.ld(i, j, k), jm_var, A.lx, i, jm, k, true, i, j, k, &lu);
+  fy_add<R, true>(g, A.gu2, i, j, k, lu);
+  if (!g.bz && k == 1) {  // F3(1) = -F3(2): D = ... + 2*F3(2)
+    flux_adj(R(2) * lD, x, psi.ld(i, j, k + 1), P.u3.ld(i, j, k + 1), true, A.lx, i, j, k, true, i, j, k + 1, &lu);
+    addat(A.gu3, i, j, k + 1, lu);
+  } else if (!g.bz && k == g.lp) {  // F3(lp+1) = -F3(lp): D = ... - 2*F3(lp)
+    flux_adj(-R(2) * lD, psi.ld(i, j, k - 1), x, P.u3.ld(i, j, k), true, A.lx, i, j, k - 1, true, i, j, k, &lu);
+    addat(A.gu3, i, j, k, lu);
+  } else {
+    const int kp = cz(g, k + 1), km = cz(g, k - 1);
+    flux_adj(lD, x, psi.ld(i, j, kp), fz<R, true>(g, P.u3, i, j, k + 1), true, A.lx, i, j, k, true, i, j, kp, &lu);
+    fz_add<R, true>(g, A.gu3, i, j, k + 1, lu);
+    flux_adj(-lD, psi.ld(i, j, km), x, P.u3.ld(i, j, k), true, A.lx, i, j, km, true, i, j, k, &lu);
+    fz_add<R, true>(g, A.gu3, i, j, k, lu);
+  }
+}
+
+template <class R>
+__global__ void __launch_bounds__(128) ka_store(const Prob<R> P, const AdjArr<R> A) {
+  ACELL
+  A.lam.at(i, j, k) = A.lx.ld(i, j, k);
+}
+
+// J's seed: lambda = psi_N - target on the interior, 0 on the halo.
+template <class R>
+__global__ void __launch_bounds__(128) ka_seed(const Prob<R> P, const Arr<R> psi, const Arr<R> target, Arr<R> lam) {
+  ACELL
+  lam.at(i, j, k) = psi.ld(i, j, k) - target.ld(i, j, k);
+}
+
+// forward recompute kernels (psi's halo is left untouched: HALO=false)
+template <class R>
+__global__ void __launch_bounds__(128) kf_upwind(const Prob<R> P) {
+  ACELL
+  (void)g;
+  upwind_body<R, true, false>(P, i, j, k);
+}
+template <class R>
+__global__ void __launch_bounds__(128) kf_pseudo(const Prob<R> P) {
+  ACELL
+  (void)g;
+  pseudo_body<R, true>(P, i, j, k);
+}
+template <class R, bool NONOS>
+__global__ void __launch_bounds__(128) kf_bounds(const Prob<R> P) {
+  ACELL
+  (void)g;
+  bounds_body<R, NONOS, true, false>(P, i, j, k);
+}
+
+// Forward recompute (upwind, pseudo-velocity, bounds; the update itself is
+// not needed) into P's scratch, then the reverse kernels.  nonos=0 skips the
+// limiter's adjoint (w = v).  `zero` must point at the nine contiguous
+// atomic accumulators lv1..lv3, lw1..lw3, lcp, lcn, lx (9*ncell elements).
+template <class R>
+int run_step_adjoint(const Prob<R>& P, const AdjArr<R>& A, int nonos, R* zero, size_t ncell, cudaStream_t s) {
+  const Geo& g = P.g;
+  const dim3 blk(32, 4, 1);
+  const dim3 grd((g.np + 31) / 32, (g.mp + 3) / 4, g.lp);
+  if (cudaMemsetAsync(zero, 0, 9 * ncell * sizeof(R), s) != cudaSuccess) return -5;
+  kf_upwind<R><<<grd, blk, 0, s>>>(P);
+  kf_pseudo<R><<<grd, blk, 0, s>>>(P);
+  if (nonos) kf_bounds<R, true><<<grd, blk, 0, s>>>(P);
+  else kf_bounds<R, false><<<grd, blk, 0, s>>>(P);
+  ka_update<R><<<grd, blk, 0, s>>>(P, A);
+  if (nonos) {
+    ka_limit<R, true><<<grd, blk, 0, s>>>(P, A);
+    ka_bounds<R><<<grd, blk, 0, s>>>(P, A);
+  } else {
+    ka_limit<R, false><<<grd, blk, 0, s>>>(P, A);
+  }
+  ka_pseudo<R><<<grd, blk, 0, s>>>(P, A);
+  ka_upwind<R><<<grd, blk, 0, s>>>(P, A);
+  ka_store<R><<<grd, blk, 0, s>>>(P, A);
+  add_launches(nonos ? 9 : 8);
+  return cudaGetLastError() == cudaSuccess ? 0 : -5;
+}
+
+template <class R>
+int run_seed(const Prob<R>& P, const Arr<R>& psi, const Arr<R>& target, const Arr<R>& lam, cudaStream_t s) {
+  const Geo& g = P.g;
+  const dim3 blk(32, 4, 1);
+  const dim3 grd((g.np + 31) / 32, (g.mp + 3) / 4, g.lp);
+  ka_seed<R><<<grd, blk, 0, s>>>(P, psi, target, lam);
+  add_launches(1);
+  return cudaGetLastError() == cudaSuccess ? 0 : -5;
+}
+
+template int run_step_adjoint<double>(const Prob<double>&, const AdjArr<double>&, int, double*, size_t, cudaStream_t);
+template int run_step_adjoint<float>(const Prob<float>&, const AdjArr<float>&, int, float*, size_t, cudaStream_t);
+template int run_seed<double>(const Prob<double>&, const Arr<double>&, const Arr<double>&, const Arr<double>&, cudaStream_t);
+template int run_seed<float>(const Prob<float>&, const Arr<float>&, const Arr<float>&, const Arr<float>&, cudaStream_t);
+
+}  // namespace mpdata

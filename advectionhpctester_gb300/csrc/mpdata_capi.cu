@@ -90,6 +90,7 @@ struct Workspace {
   int* d_err;
   cudaStream_t last;
   EventProf* prof;
+  void* adj;  // adjoint scratch (10 fields), allocated on first use
 };
 
 int check_grid(const mpdata_grid* g) {
@@ -299,6 +300,7 @@ int mpdata_ws_create(const mpdata_grid* grid, const mpdata_opts* opts, void** ws
   w->elem = opts->precision == 64 ? sizeof(double) : sizeof(float);
   w->last = nullptr;
   w->prof = nullptr;
+  w->adj = nullptr;
   w->nhi = (size_t)grid->mp * grid->lp + (size_t)grid->np * grid->lp + (size_t)grid->np * grid->mp;
   if (cudaMalloc(&w->mem, (w->ncell * NSCRATCH + w->nhi) * w->elem) != cudaSuccess) {
     cudaGetLastError();
@@ -328,6 +330,7 @@ int mpdata_ws_destroy(void* ws) {
   }
   w->magic = 0;
   delete w->prof;
+  if (w->adj) cudaFree(w->adj);
   cudaError_t e1 = cudaFree(w->mem);
   cudaError_t e2 = cudaFree(w->d_err);
   delete w;
@@ -893,6 +896,177 @@ int mpdata_error_norms(const mpdata_grid* grid, const void* a, int a_is_f64, con
   out[2] = r[3];             // max |b|
   out[3] = sqrt(r[1]);       // ||b||_2
   return MPDATA_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Adjoint (include/mpdata.h, mpdata_step_adjoint_*, mpdata_adjoint_run_*)
+// ===========================================================================
+namespace {
+
+template <class R>
+int adj_plan(Workspace* w, Prob<R>* P, AdjArr<R>* A, const R* psi_in, const R* u1, const R* u2, const R* u3,
+             const R* h, const R* rhr, const R* bcx, const R* bcy, R* lambda, R* gu1, R* gu2, R* gu3) {
+  if (w->elem != sizeof(R)) return MPDATA_E_WS;
+  if (!w->o.gauge || w->o.iord != 2) return MPDATA_E_UNSUPPORTED;  // gauge form, one corrective pass
+  if (!psi_in || !u1 || !u2 || !u3 || !h || !rhr || !lambda || !gu1 || !gu2 || !gu3) return MPDATA_E_NULL;
+  if ((!w->g.ibcx && !bcx) || (!w->g.ibcy && !bcy)) return MPDATA_E_NULL;
+  if (!w->adj && cudaMalloc(&w->adj, 10 * w->ncell * w->elem) != cudaSuccess) {
+    cudaGetLastError();
+    w->adj = nullptr;
+    return MPDATA_E_CUDA;
+  }
+  R* base = static_cast<R*>(w->mem);
+  *P = make_prob<R>(w->g, 1, const_cast<R*>(psi_in), u1, u2, u3, h, rhr, bcx, bcy, base, w->ncell,
+                    base + (size_t)NFIELD * w->ncell, 1);
+  const mpdata_grid& g = w->g;
+  const int ih = g.ih, sx = g.np + 2 * ih, sy = g.mp + 2 * ih;
+  R* a = static_cast<R*>(w->adj);
+  Arr<R>* slots[10] = {&A->lv1, &A->lv2, &A->lv3, &A->lw1, &A->lw2, &A->lw3, &A->lcp, &A->lcn, &A->lx, &A->lxant};
+  for (int f = 0; f < 10; f++) *slots[f] = scratch_view<R>(a + (size_t)f * w->ncell, P->g);
+  A->lam = caller_view<R>(lambda, ih, sx, sy);
+  A->gu1 = caller_view<R>(gu1, ih, sx + 1, sy);
+  A->gu2 = caller_view<R>(gu2, ih, sx, sy + 1);
+  A->gu3 = caller_view<R>(gu3, ih, sx, sy);
+  return MPDATA_OK;
+}
+
+template <class R>
+int step_adjoint_impl(void* ws, const R* psi_in, const R* u1, const R* u2, const R* u3, const R* h, const R* rhr,
+                      const R* bcx, const R* bcy, R* lambda, R* gu1, R* gu2, R* gu3, void* stream) {
+  Workspace* w = as_ws(ws);
+  if (!w) return MPDATA_E_WS;
+  Prob<R> P;
+  AdjArr<R> A;
+  int rc = adj_plan<R>(w, &P, &A, psi_in, u1, u2, u3, h, rhr, bcx, bcy, lambda, gu1, gu2, gu3);
+  if (rc) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  w->last = s;
+  return run_step_adjoint<R>(P, A, w->o.nonos, static_cast<R*>(w->adj), w->ncell, s) ? MPDATA_E_CUDA : MPDATA_OK;
+}
+
+// J = 0.5*|psi_N - target|^2 and its gradients over nsteps steps, with
+// checkpoints every `interval` steps (default ceil(sqrt(nsteps))): the
+// forward run keeps ceil(nsteps/interval) states; the reverse sweep rebuilds
+// each segment's states from its checkpoint and runs the step adjoints
+// backwards.  Peak extra memory: (checkpoints + interval) psi-sized arrays.
+template <class R>
+int adjoint_run_impl(void* ws, int nsteps, int interval, R* psi, const R* u1, const R* u2, const R* u3,
+                     const R* h, const R* rhr, const R* bcx, const R* bcy, const R* target, double* J,
+                     R* g_psi0, R* gu1, R* gu2, R* gu3, long long* peak_bytes, void* stream) {
+  Workspace* w = as_ws(ws);
+  if (!w) return MPDATA_E_WS;
+  if (nsteps < 1 || interval < 0) return MPDATA_E_OPTS;
+  if (!psi || !target || !J || !g_psi0) return MPDATA_E_NULL;
+  Prob<R> P;
+  AdjArr<R> A;
+  int rc = adj_plan<R>(w, &P, &A, psi, u1, u2, u3, h, rhr, bcx, bcy, g_psi0, gu1, gu2, gu3);
+  if (rc) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  w->last = s;
+  int K = interval;
+  if (K == 0) {
+    K = 1;
+    while ((long long)K * K < nsteps) K++;
+  }
+  if (K > nsteps) K = nsteps;
+  const int nck = (nsteps + K - 1) / K;
+  const mpdata_grid& g = w->g;
+  const int ih = g.ih, sx = g.np + 2 * ih, sy = g.mp + 2 * ih;
+  const size_t plen = (size_t)sx * sy * (g.lp + 2 * ih);
+  const size_t pbytes = plen * sizeof(R);
+  R* ck = nullptr;   // nck checkpoints
+  R* seg = nullptr;  // K states of one segment
+  double* red = nullptr;
+  const size_t nred = (size_t)reduce_blocks() * 6 + 4;
+  if (cudaMallocAsync(&ck, pbytes * nck, s) != cudaSuccess || cudaMallocAsync(&seg, pbytes * K, s) != cudaSuccess ||
+      cudaMallocAsync(&red, nred * sizeof(double), s) != cudaSuccess) {
+    cudaGetLastError();
+    if (ck) cudaFreeAsync(ck, s);
+    if (seg) cudaFreeAsync(seg, s);
+    return MPDATA_E_CUDA;
+  }
+  if (peak_bytes)
+    *peak_bytes = (long long)(pbytes * (nck + K)) + (long long)(w->ncell * w->elem * (NSCRATCH + 10));
+  R* base = static_cast<R*>(w->mem);
+  auto fwd = [&](R* state) -> int {
+    Prob<R> F = make_prob<R>(g, 1, state, u1, u2, u3, h, rhr, bcx, bcy, base, w->ncell,
+                             base + (size_t)NFIELD * w->ncell, 1);
+    return run_step<R>(F, 2, w->o.nonos, nullptr, s);
+  };
+  // forward sweep with checkpoints
+  for (int n = 0; n < nsteps && !rc; n++) {
+    if (n % K == 0 &&
+        cudaMemcpyAsync(ck + (size_t)(n / K) * plen, psi, pbytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+      rc = MPDATA_E_CUDA;
+    if (!rc && fwd(psi)) rc = MPDATA_E_CUDA;
+  }
+  // J and the seed lambda = psi_N - target (into g_psi0)
+  double out[4] = {0, 0, 0, 0};
+  if (!rc && run_reduce<R>(P.g, 1, psi, nullptr, nullptr, target, sizeof(R) == 8, red + 4, red, s))
+    rc = MPDATA_E_CUDA;
+  if (!rc && cudaMemcpyAsync(out, red, sizeof out, cudaMemcpyDeviceToHost, s) != cudaSuccess) rc = MPDATA_E_CUDA;
+  if (!rc && cudaMemsetAsync(g_psi0, 0, pbytes, s) != cudaSuccess) rc = MPDATA_E_CUDA;
+  if (!rc && run_seed<R>(P, caller_view<R>(psi, ih, sx, sy), caller_view<R>(const_cast<R*>(target), ih, sx, sy),
+                         A.lam, s))
+    rc = MPDATA_E_CUDA;
+  // reverse sweep, segment by segment
+  for (int c = nck - 1; c >= 0 && !rc; c--) {
+    const int n0 = c * K, n1 = (n0 + K < nsteps) ? n0 + K : nsteps;
+    if (cudaMemcpyAsync(seg, ck + (size_t)c * plen, pbytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+      rc = MPDATA_E_CUDA;
+      break;
+    }
+    for (int n = n0 + 1; n < n1 && !rc; n++) {
+      R* dst = seg + (size_t)(n - n0) * plen;
+      if (cudaMemcpyAsync(dst, dst - plen, pbytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess || fwd(dst))
+        rc = MPDATA_E_CUDA;
+    }
+    for (int n = n1 - 1; n >= n0 && !rc; n--) {
+      Prob<R> B = P;
+      B.psi = caller_view<R>(seg + (size_t)(n - n0) * plen, ih, sx, sy);
+      if (run_step_adjoint<R>(B, A, w->o.nonos, static_cast<R*>(w->adj), w->ncell, s)) rc = MPDATA_E_CUDA;
+    }
+  }
+  cudaFreeAsync(ck, s);
+  cudaFreeAsync(seg, s);
+  cudaFreeAsync(red, s);
+  if (!rc && cudaStreamSynchronize(s) != cudaSuccess) rc = MPDATA_E_CUDA;
+  if (!rc) *J = 0.5 * out[0];
+  return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mpdata_step_adjoint_f64(void* ws, const double* psi_in, const double* u1, const double* u2,
+                            const double* u3, const double* h, const double* rhr, const double* bcx,
+                            const double* bcy, double* lambda, double* g_u1, double* g_u2, double* g_u3,
+                            void* stream) {
+  return step_adjoint_impl<double>(ws, psi_in, u1, u2, u3, h, rhr, bcx, bcy, lambda, g_u1, g_u2, g_u3, stream);
+}
+int mpdata_step_adjoint_f32(void* ws, const float* psi_in, const float* u1, const float* u2, const float* u3,
+                            const float* h, const float* rhr, const float* bcx, const float* bcy,
+                            float* lambda, float* g_u1, float* g_u2, float* g_u3, void* stream) {
+  return step_adjoint_impl<float>(ws, psi_in, u1, u2, u3, h, rhr, bcx, bcy, lambda, g_u1, g_u2, g_u3, stream);
+}
+
+int mpdata_adjoint_run_f64(void* ws, int nsteps, int interval, double* psi, const double* u1,
+                           const double* u2, const double* u3, const double* h, const double* rhr,
+                           const double* bcx, const double* bcy, const double* target, double* J,
+                           double* g_psi0, double* g_u1, double* g_u2, double* g_u3,
+                           long long* peak_bytes, void* stream) {
+  return adjoint_run_impl<double>(ws, nsteps, interval, psi, u1, u2, u3, h, rhr, bcx, bcy, target, J, g_psi0,
+                                  g_u1, g_u2, g_u3, peak_bytes, stream);
+}
+int mpdata_adjoint_run_f32(void* ws, int nsteps, int interval, float* psi, const float* u1, const float* u2,
+                           const float* u3, const float* h, const float* rhr, const float* bcx,
+                           const float* bcy, const float* target, double* J, float* g_psi0, float* g_u1,
+                           float* g_u2, float* g_u3, long long* peak_bytes, void* stream) {
+  return adjoint_run_impl<float>(ws, nsteps, interval, psi, u1, u2, u3, h, rhr, bcx, bcy, target, J, g_psi0,
+                                 g_u1, g_u2, g_u3, peak_bytes, stream);
 }
 
 }  // extern "C"

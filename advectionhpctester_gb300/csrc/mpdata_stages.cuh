@@ -58,6 +58,18 @@ struct PredPlan {
 template <class R>
 int run_predictor(const PredPlan<R>& plan, cudaStream_t stream);
 
+// Adjoint scratch of one problem (mpdata_adjoint.cu).
+template <class R>
+struct AdjArr {
+  Arr<R> lxant, lv1, lv2, lv3, lw1, lw2, lw3, lcp, lcn, lx;
+  Arr<R> lam;            // caller lambda: in dJ/dpsi_new, out dJ/dpsi_in (psi-shaped)
+  Arr<R> gu1, gu2, gu3;  // caller gradients of u1..u3 (C-grid shaped), accumulated
+};
+template <class R>
+int run_step_adjoint(const Prob<R>& P, const AdjArr<R>& A, int nonos, R* zero, size_t ncell, cudaStream_t s);
+template <class R>
+int run_seed(const Prob<R>& P, const Arr<R>& psi, const Arr<R>& target, const Arr<R>& lam, cudaStream_t s);
+
 unsigned long long launch_count();
 void add_launches(int n);
 

@@ -160,6 +160,35 @@ class Workspace:
     # the reference's name for the density step
     mpdata3d_rho_gauge_gpubc = rho_gauge
 
+    def step_adjoint(self, psi_in, u1, u2, u3, h, rhr, lam, g_u1, g_u2, g_u3, bcx=None, bcy=None,
+                     stream=None):
+        """Reverse of one step: lam (dJ/dpsi_new) becomes dJ/dpsi_in; dJ/du is
+        added into g_u1..g_u3.  psi_in is the field at the step's start."""
+        s, d = self.shapes, self.dtype
+        fn = self.lib.mpdata_step_adjoint_f64 if self.opts.precision == 64 else self.lib.mpdata_step_adjoint_f32
+        check(fn(self.handle, _ptr(psi_in, d, s["psi"], "psi_in"), _ptr(u1, d, s["u1"], "u1"),
+                 _ptr(u2, d, s["u2"], "u2"), _ptr(u3, d, s["u3"], "u3"), _ptr(h, d, s["psi"], "h"),
+                 _ptr(rhr, d, s["psi"], "rhr"), _ptr(bcx, d, s["bcx"], "bcx"), _ptr(bcy, d, s["bcy"], "bcy"),
+                 _ptr(lam, d, s["psi"], "lam"), _ptr(g_u1, d, s["u1"], "g_u1"), _ptr(g_u2, d, s["u2"], "g_u2"),
+                 _ptr(g_u3, d, s["u3"], "g_u3"), _stream(stream)), "mpdata_step_adjoint")
+
+    def adjoint_run(self, nsteps, psi, u1, u2, u3, h, rhr, target, g_psi0, g_u1, g_u2, g_u3, bcx=None,
+                    bcy=None, interval=0, stream=None):
+        """J = 0.5*|psi_N - target|^2 after nsteps steps and its gradients with
+        sqrt(N) checkpointing.  psi: psi_0 in, psi_N out.  Returns (J, peak_bytes)."""
+        import ctypes
+        s, d = self.shapes, self.dtype
+        fn = self.lib.mpdata_adjoint_run_f64 if self.opts.precision == 64 else self.lib.mpdata_adjoint_run_f32
+        J = ctypes.c_double(0.0)
+        peak = ctypes.c_longlong(0)
+        check(fn(self.handle, int(nsteps), int(interval), _ptr(psi, d, s["psi"], "psi"), _ptr(u1, d, s["u1"], "u1"),
+                 _ptr(u2, d, s["u2"], "u2"), _ptr(u3, d, s["u3"], "u3"), _ptr(h, d, s["psi"], "h"),
+                 _ptr(rhr, d, s["psi"], "rhr"), _ptr(bcx, d, s["bcx"], "bcx"), _ptr(bcy, d, s["bcy"], "bcy"),
+                 _ptr(target, d, s["psi"], "target"), J, _ptr(g_psi0, d, s["psi"], "g_psi0"),
+                 _ptr(g_u1, d, s["u1"], "g_u1"), _ptr(g_u2, d, s["u2"], "g_u2"), _ptr(g_u3, d, s["u3"], "g_u3"),
+                 peak, _stream(stream)), "mpdata_adjoint_run")
+        return J.value, peak.value
+
     def profile(self, enable=True):
         """Start (or stop) per-stage CUDA-event timing of this workspace."""
         check(self.lib.mpdata_ws_profile(self.handle, 1 if enable else 0), "mpdata_ws_profile")

@@ -139,6 +139,43 @@ int mpdata_rho_gauge_f32(void* ws, float* ox, float* oy, float* oz, float* u, fl
                          float* pexr2, const float* bcx, const float* bcy, float dxi, float dyi,
                          float dzi, float dt, float dt_ratio, int liner, void* stream);
 
+/* ---- adjoint ---------------------------------------------------------------
+ * No reference code: the hand-written reverse of the step (infinite-gauge
+ * form, one corrective pass, limiter on or off), every branch differentiated
+ * at the forward values.  The workspace must be gauge with iord=2.
+ *
+ * mpdata_step_adjoint_*: psi_in is the field at the start of the step (not
+ * modified); on entry lambda holds dJ/dpsi after the step (psi-shaped,
+ * interior used), on exit dJ/dpsi before it; dJ/du1..u3 of this step are
+ * ADDED into g_u1..g_u3 (C-grid shaped).  The forward intermediates are
+ * recomputed into the workspace.  Accumulation uses atomic adds, so results
+ * match the FP64 reference adjoint to rounding, not bit for bit.
+ *
+ * mpdata_adjoint_run_*: J = 0.5*sum((psi_N - target)^2) after nsteps steps
+ * with velocities held fixed; psi holds psi_0 on entry and psi_N on exit;
+ * g_psi0 receives dJ/dpsi_0 and g_u1..g_u3 accumulate dJ/du.  States are
+ * checkpointed every `interval` steps (0 = ceil(sqrt(nsteps))) and each
+ * segment is recomputed in the reverse sweep; peak_bytes (may be NULL)
+ * receives the device memory the run holds.  Synchronises the stream. */
+int mpdata_step_adjoint_f64(void* ws, const double* psi_in, const double* u1, const double* u2,
+                            const double* u3, const double* h, const double* rhr, const double* bcx,
+                            const double* bcy, double* lambda, double* g_u1, double* g_u2,
+                            double* g_u3, void* stream);
+int mpdata_step_adjoint_f32(void* ws, const float* psi_in, const float* u1, const float* u2,
+                            const float* u3, const float* h, const float* rhr, const float* bcx,
+                            const float* bcy, float* lambda, float* g_u1, float* g_u2, float* g_u3,
+                            void* stream);
+int mpdata_adjoint_run_f64(void* ws, int nsteps, int interval, double* psi, const double* u1,
+                           const double* u2, const double* u3, const double* h, const double* rhr,
+                           const double* bcx, const double* bcy, const double* target, double* J,
+                           double* g_psi0, double* g_u1, double* g_u2, double* g_u3,
+                           long long* peak_bytes, void* stream);
+int mpdata_adjoint_run_f32(void* ws, int nsteps, int interval, float* psi, const float* u1,
+                           const float* u2, const float* u3, const float* h, const float* rhr,
+                           const float* bcx, const float* bcy, const float* target, double* J,
+                           float* g_psi0, float* g_u1, float* g_u2, float* g_u3,
+                           long long* peak_bytes, void* stream);
+
 /* Device error word of a workspace (bit 0: a non-finite value was produced
  * by the last checked step).  Synchronises the workspace's last stream. */
 int mpdata_ws_error(void* ws, int* error_word);

@@ -40,6 +40,49 @@ struct Buf {
   inline R& operator()(int i, int j, int k) { return v(i, j, k); }
 };
 
+// abs and sign bit, generic so the step can also run on the AD scalar below
+inline double absv(double x) { return std::fabs(x); }
+inline float absv(float x) { return std::fabs(x); }
+inline bool sgnb(double x) { return std::signbit(x); }
+inline bool sgnb(float x) { return std::signbit(x); }
+
+// ---- reverse-mode AD scalar (for the un-checkpointed FP64 adjoint) --------
+// Every arithmetic result is a tape node with up to two parents and the
+// local partial derivatives; branches (max/min/pp/pn/abs/sign) follow the
+// forward values, so the derivative is taken piecewise at the forward branch.
+struct Tape {
+  std::vector<int> a, b;
+  std::vector<double> da, db;
+  int push(int ia, double pa, int ib, double pb) {
+    a.push_back(ia); da.push_back(pa); b.push_back(ib); db.push_back(pb);
+    return (int)a.size() - 1;
+  }
+};
+Tape* g_tape = nullptr;
+struct AD {
+  double v;
+  int id;  // < 0: constant
+  AD() : v(0.0), id(-1) {}
+  AD(double x) : v(x), id(-1) {}
+};
+inline AD mk(double v, int ia, double pa, int ib, double pb) {
+  AD r(v);
+  if (ia >= 0 || ib >= 0) r.id = g_tape->push(ia, pa, ib, pb);
+  return r;
+}
+inline AD operator+(AD x, AD y) { return mk(x.v + y.v, x.id, 1.0, y.id, 1.0); }
+inline AD operator-(AD x, AD y) { return mk(x.v - y.v, x.id, 1.0, y.id, -1.0); }
+inline AD operator*(AD x, AD y) { return mk(x.v * y.v, x.id, y.v, y.id, x.v); }
+inline AD operator/(AD x, AD y) {
+  const double q = x.v / y.v;
+  return mk(q, x.id, 1.0 / y.v, y.id, -q / y.v);
+}
+inline AD operator-(AD x) { return mk(-x.v, x.id, -1.0, -1, 0.0); }
+inline bool operator>(AD x, AD y) { return x.v > y.v; }
+inline bool operator<(AD x, AD y) { return x.v < y.v; }
+inline AD absv(AD x) { return std::signbit(x.v) ? -x : x; }
+inline bool sgnb(AD x) { return std::signbit(x.v); }
+
 // ---- point operators: mpdataoperators.inc:50-96 (device versions) ----
 template <class R> inline R pp(R y) { return y > R(0) ? y : R(0); }        // max(0,y)
 template <class R> inline R pn(R y) { return y < R(0) ? -y : R(0); }       // -min(0,y)
@@ -48,21 +91,21 @@ template <class R> inline R mn2(R a, R b) { return a < b ? a : b; }
 template <class R> inline R donor(R y1, R y2, R a) { return pp(a) * y1 - pn(a) * y2; }
 // vdyf: (abs(a)-a*a*rinv)*(x2-x1)*.5                            (:65-69)
 template <class R> inline R vdyf(R x1, R x2, R a, R rinv) {
-  return (std::fabs(a) - a * a * rinv) * (x2 - x1) * R(0.5);
+  return (absv(a) - a * a * rinv) * (x2 - x1) * R(0.5);
 }
 // rat4: ((z3+z2)-(z1+z0))*.25                                    (:80-84)
 template <class R> inline R rat4(R z0, R z1, R z2, R z3) { return ((z3 + z2) - (z1 + z0)) * R(0.25); }
 // vdyfa: (abs(a)-a*a*rinv)*(abs(x2)-abs(x1))/(abs(x2)+abs(x1)+ep) (:85-91)
 template <class R> inline R vdyfa(R x1, R x2, R a, R rinv, R ep) {
-  return (std::fabs(a) - a * a * rinv) * (std::fabs(x2) - std::fabs(x1)) /
-         (std::fabs(x2) + std::fabs(x1) + ep);
+  return (absv(a) - a * a * rinv) * (absv(x2) - absv(x1)) /
+         (absv(x2) + absv(x1) + ep);
 }
 // vcorra: -0.125*a*b*y1*rinv/(y2)                                 (:92-96)
 template <class R> inline R vcorra(R a, R b, R y1, R y2, R rinv) {
   return -(R(0.125) * a * b * y1 * rinv / y2);
 }
 // pp(sign(1,x)): 1 when x carries a + sign (IEEE signed zero aware), else 0
-template <class R> inline R possign(R x) { return std::signbit(x) ? R(0) : R(1); }
+template <class R> inline R possign(R x) { return sgnb(x) ? R(0) : R(1); }
 
 struct Dims {
   int np, mp, lp, ih;
@@ -252,17 +295,17 @@ void pseudo_std(const Dims& d, Buf<R>& x, Buf<R>& a1, Buf<R>& a2, Buf<R>& a3, Bu
           const R hmx = R(1) / (R(0.5) * (h(i - 1, j, k) + h(i, j, k)));
           R v = vdyfa(x(i - 1, j, k), x(i, j, k), a1(i, j, k), hmx, ep) +
                 vcorra(a1(i, j, k), a2(i - 1, j, k) + a2(i - 1, j + 1, k) + a2(i, j + 1, k) + a2(i, j, k),
-                       (std::fabs(x(i - 1, j + 1, k)) + std::fabs(x(i, j + 1, k))) -
-                           (std::fabs(x(i - 1, j - 1, k)) + std::fabs(x(i, j - 1, k))),
-                       std::fabs(x(i - 1, j + 1, k)) + std::fabs(x(i, j + 1, k)) +
-                           std::fabs(x(i - 1, j - 1, k)) + std::fabs(x(i, j - 1, k)) + ep,
+                       (absv(x(i - 1, j + 1, k)) + absv(x(i, j + 1, k))) -
+                           (absv(x(i - 1, j - 1, k)) + absv(x(i, j - 1, k))),
+                       absv(x(i - 1, j + 1, k)) + absv(x(i, j + 1, k)) +
+                           absv(x(i - 1, j - 1, k)) + absv(x(i, j - 1, k)) + ep,
                        hmx);
           if (zt)
             v = v + vcorra(a1(i, j, k), a3(i - 1, j, k) + a3(i - 1, j, k + 1) + a3(i, j, k + 1) + a3(i, j, k),
-                           (std::fabs(x(i - 1, j, k + 1)) + std::fabs(x(i, j, k + 1))) -
-                               (std::fabs(x(i - 1, j, k - 1)) + std::fabs(x(i, j, k - 1))),
-                           std::fabs(x(i - 1, j, k + 1)) + std::fabs(x(i, j, k + 1)) +
-                               std::fabs(x(i - 1, j, k - 1)) + std::fabs(x(i, j, k - 1)) + ep,
+                           (absv(x(i - 1, j, k + 1)) + absv(x(i, j, k + 1))) -
+                               (absv(x(i - 1, j, k - 1)) + absv(x(i, j, k - 1))),
+                           absv(x(i - 1, j, k + 1)) + absv(x(i, j, k + 1)) +
+                               absv(x(i - 1, j, k - 1)) + absv(x(i, j, k - 1)) + ep,
                            hmx);
           v1(i, j, k) = v;
           f1(i, j, k) = donor(x(i - 1, j, k), x(i, j, k), v);
@@ -271,17 +314,17 @@ void pseudo_std(const Dims& d, Buf<R>& x, Buf<R>& a1, Buf<R>& a2, Buf<R>& a3, Bu
           const R hmy = R(1) / (R(0.5) * (h(i, j - 1, k) + h(i, j, k)));
           R v = vdyfa(x(i, j - 1, k), x(i, j, k), a2(i, j, k), hmy, ep) +
                 vcorra(a2(i, j, k), a1(i, j - 1, k) + a1(i, j, k) + a1(i + 1, j, k) + a1(i + 1, j - 1, k),
-                       (std::fabs(x(i + 1, j - 1, k)) + std::fabs(x(i + 1, j, k))) -
-                           (std::fabs(x(i - 1, j - 1, k)) + std::fabs(x(i - 1, j, k))),
-                       std::fabs(x(i + 1, j - 1, k)) + std::fabs(x(i + 1, j, k)) +
-                           std::fabs(x(i - 1, j - 1, k)) + std::fabs(x(i - 1, j, k)) + ep,
+                       (absv(x(i + 1, j - 1, k)) + absv(x(i + 1, j, k))) -
+                           (absv(x(i - 1, j - 1, k)) + absv(x(i - 1, j, k))),
+                       absv(x(i + 1, j - 1, k)) + absv(x(i + 1, j, k)) +
+                           absv(x(i - 1, j - 1, k)) + absv(x(i - 1, j, k)) + ep,
                        hmy);
           if (zt)
             v = v + vcorra(a2(i, j, k), a3(i, j - 1, k) + a3(i, j, k) + a3(i, j, k + 1) + a3(i, j - 1, k + 1),
-                           (std::fabs(x(i, j - 1, k + 1)) + std::fabs(x(i, j, k + 1))) -
-                               (std::fabs(x(i, j - 1, k - 1)) + std::fabs(x(i, j, k - 1))),
-                           std::fabs(x(i, j - 1, k + 1)) + std::fabs(x(i, j, k + 1)) +
-                               std::fabs(x(i, j - 1, k - 1)) + std::fabs(x(i, j, k - 1)) + ep,
+                           (absv(x(i, j - 1, k + 1)) + absv(x(i, j, k + 1))) -
+                               (absv(x(i, j - 1, k - 1)) + absv(x(i, j, k - 1))),
+                           absv(x(i, j - 1, k + 1)) + absv(x(i, j, k + 1)) +
+                               absv(x(i, j - 1, k - 1)) + absv(x(i, j, k - 1)) + ep,
                            hmy);
           v2(i, j, k) = v;
           f2(i, j, k) = donor(x(i, j - 1, k), x(i, j, k), v);
@@ -290,16 +333,16 @@ void pseudo_std(const Dims& d, Buf<R>& x, Buf<R>& a1, Buf<R>& a2, Buf<R>& a3, Bu
           const R hmz = R(1) / (R(0.5) * (h(i, j, k - 1) + h(i, j, k)));
           const R v = vdyfa(x(i, j, k - 1), x(i, j, k), a3(i, j, k), hmz, ep) +
                       vcorra(a3(i, j, k), a1(i, j, k - 1) + a1(i, j, k) + a1(i + 1, j, k) + a1(i + 1, j, k - 1),
-                             (std::fabs(x(i + 1, j, k - 1)) + std::fabs(x(i + 1, j, k))) -
-                                 (std::fabs(x(i - 1, j, k - 1)) + std::fabs(x(i - 1, j, k))),
-                             std::fabs(x(i + 1, j, k - 1)) + std::fabs(x(i + 1, j, k)) +
-                                 std::fabs(x(i - 1, j, k - 1)) + std::fabs(x(i - 1, j, k)) + ep,
+                             (absv(x(i + 1, j, k - 1)) + absv(x(i + 1, j, k))) -
+                                 (absv(x(i - 1, j, k - 1)) + absv(x(i - 1, j, k))),
+                             absv(x(i + 1, j, k - 1)) + absv(x(i + 1, j, k)) +
+                                 absv(x(i - 1, j, k - 1)) + absv(x(i - 1, j, k)) + ep,
                              hmz) +
                       vcorra(a3(i, j, k), a2(i, j, k - 1) + a2(i, j + 1, k - 1) + a2(i, j + 1, k) + a2(i, j, k),
-                             (std::fabs(x(i, j + 1, k - 1)) + std::fabs(x(i, j + 1, k))) -
-                                 (std::fabs(x(i, j - 1, k - 1)) + std::fabs(x(i, j - 1, k))),
-                             std::fabs(x(i, j + 1, k - 1)) + std::fabs(x(i, j + 1, k)) +
-                                 std::fabs(x(i, j - 1, k - 1)) + std::fabs(x(i, j - 1, k)) + ep,
+                             (absv(x(i, j + 1, k - 1)) + absv(x(i, j + 1, k))) -
+                                 (absv(x(i, j - 1, k - 1)) + absv(x(i, j - 1, k))),
+                             absv(x(i, j + 1, k - 1)) + absv(x(i, j + 1, k)) +
+                                 absv(x(i, j - 1, k - 1)) + absv(x(i, j - 1, k)) + ep,
                              hmz);
           v3(i, j, k) = v;
           f3(i, j, k) = donor(x(i, j, k - 1), x(i, j, k), v);
@@ -914,6 +957,114 @@ int orc_rho_gauge_f64(const orc_grid* g, double* ox, double* oy, double* oz, dou
                       double dzi, double dt, double dt_ratio, int liner) {
   return rho_gauge<double>(g, ox, oy, oz, u, v, w, u1, u2, u3, x_in, x_incomp, h, rhoadv, rhr, pexe,
                            pexr1, pexr2, bcx, bcy, dxi, dyi, dzi, dt, dt_ratio, liner);
+}
+
+int orc_tangent_adjoint_f64(const orc_grid* g, int t_adv, int iord, int nonos, int nsteps, const double* x0,
+                            const double* bcx, const double* bcy, const double* u1, const double* u2,
+                            const double* u3, const double* rhr, const double* h, const double* target,
+                            double* J, double* xN, double* gx0, double* gu1, double* gu2, double* gu3,
+                            const double* dx0, const double* du1, const double* du2, const double* du3,
+                            double* dJ_tl);
+
+// Un-checkpointed FP64 adjoint by reverse-mode AD of the oracle's own step:
+// J = 0.5*sum((x_N - target)^2) over the interior after nsteps steps with a
+// fixed velocity; gradients with respect to x_0 (interior) and every element
+// of u1..u3 (elements the step never reads get zero).  h, rhr, bcx, bcy are
+// constants.  Single-threaded (one global tape).
+int orc_adjoint_f64(const orc_grid* g, int t_adv, int iord, int nonos, int nsteps, const double* x0,
+                    const double* bcx, const double* bcy, const double* u1, const double* u2,
+                    const double* u3, const double* rhr, const double* h, const double* target,
+                    double* J, double* xN, double* gx0, double* gu1, double* gu2, double* gu3) {
+  return orc_tangent_adjoint_f64(g, t_adv, iord, nonos, nsteps, x0, bcx, bcy, u1, u2, u3, rhr, h, target, J,
+                                 xN, gx0, gu1, gu2, gu3, nullptr, nullptr, nullptr, nullptr, nullptr);
+}
+
+// Same, plus the tangent-linear model on the same tape: with directions
+// dx0 (psi-shaped) and du1..du3 (C-grid shaped), dJ_tl receives
+// sum((x_N - target) * dx_N), the directional derivative of J by forward
+// propagation; the dot-product test compares it with <dx0,gx0> + <du,gu>.
+int orc_tangent_adjoint_f64(const orc_grid* g, int t_adv, int iord, int nonos, int nsteps, const double* x0,
+                            const double* bcx, const double* bcy, const double* u1, const double* u2,
+                            const double* u3, const double* rhr, const double* h, const double* target,
+                            double* J, double* xN, double* gx0, double* gu1, double* gu2, double* gu3,
+                            const double* dx0, const double* du1, const double* du2, const double* du3,
+                            double* dJ_tl) {
+  if (!dims_ok(g)) return -1;
+  if (!x0 || !u1 || !u2 || !u3 || !rhr || !h || !target || !J || !gx0 || !gu1 || !gu2 || !gu3) return -3;
+  const int ih = g->ih;
+  const long SX = g->np + 2 * ih, SY = g->mp + 2 * ih, SZ = g->lp + 2 * ih;
+  const long nps = SX * SY * SZ, n1 = (SX + 1) * SY * SZ, n2 = SX * (SY + 1) * SZ, n3 = SX * SY * (SZ + 1);
+  Tape tape;
+  g_tape = &tape;
+  const int saved = g_threads;
+  g_threads = 1;
+  auto var = [&](double v) { AD r(v); r.id = tape.push(-1, 0.0, -1, 0.0); return r; };
+  std::vector<AD> X(nps), U1(n1), U2(n2), U3(n3), H(nps), RR(nps);
+  std::vector<AD> BX(bcx ? (size_t)g->mp * g->lp * 2 : 0), BY(bcy ? (size_t)g->np * g->lp * 2 : 0);
+  std::vector<int> xid(nps, -1);
+  auto interior = [&](long e) {
+    const long i = e % SX, j = (e / SX) % SY, k = e / (SX * SY);
+    return i >= ih && i < ih + g->np && j >= ih && j < ih + g->mp && k >= ih && k < ih + g->lp;
+  };
+  for (long e = 0; e < nps; e++) {
+    X[e] = interior(e) ? var(x0[e]) : AD(x0[e]);
+    xid[e] = X[e].id;
+    H[e] = AD(h[e]);
+    RR[e] = AD(rhr[e]);
+  }
+  for (long e = 0; e < n1; e++) U1[e] = var(u1[e]);
+  for (long e = 0; e < n2; e++) U2[e] = var(u2[e]);
+  for (long e = 0; e < n3; e++) U3[e] = var(u3[e]);
+  for (size_t e = 0; e < BX.size(); e++) BX[e] = AD(bcx[e]);
+  for (size_t e = 0; e < BY.size(); e++) BY[e] = AD(bcy[e]);
+  const int uid1 = U1[0].id, uid2 = U2[0].id, uid3 = U3[0].id;
+  int rc = 0;
+  for (int s = 0; s < nsteps && !rc; s++)
+    rc = advec<AD>(g, 4, t_adv, iord, nonos, X.data(), bcx ? BX.data() : nullptr,
+                   bcy ? BY.data() : nullptr, U1.data(), U2.data(), U3.data(), RR.data(), H.data());
+  if (rc) { g_tape = nullptr; g_threads = saved; return rc; }
+  if (dJ_tl && dx0 && du1 && du2 && du3) {
+    // forward tangent sweep: tan[n] = da*tan[a] + db*tan[b]; inputs carry the directions
+    std::vector<double> tan(tape.a.size(), 0.0);
+    for (long e = 0; e < nps; e++)
+      if (xid[e] >= 0) tan[xid[e]] = dx0[e];
+    for (long e = 0; e < n1; e++) tan[uid1 + e] = du1[e];
+    for (long e = 0; e < n2; e++) tan[uid2 + e] = du2[e];
+    for (long e = 0; e < n3; e++) tan[uid3 + e] = du3[e];
+    for (size_t n = 0; n < tape.a.size(); n++) {
+      double t = tan[n];
+      if (tape.a[n] >= 0) t += tape.da[n] * tan[tape.a[n]];
+      if (tape.b[n] >= 0) t += tape.db[n] * tan[tape.b[n]];
+      tan[n] = t;
+    }
+    double d = 0.0;
+    for (long e = 0; e < nps; e++)
+      if (interior(e) && X[e].id >= 0) d += (X[e].v - target[e]) * tan[X[e].id];
+    *dJ_tl = d;
+  }
+  std::vector<double> adj(tape.a.size(), 0.0);
+  double jsum = 0.0;
+  for (long e = 0; e < nps; e++) {
+    if (xN) xN[e] = X[e].v;
+    if (!interior(e)) continue;
+    const double r = X[e].v - target[e];
+    jsum += r * r;
+    if (X[e].id >= 0) adj[X[e].id] += r;
+  }
+  *J = 0.5 * jsum;
+  for (long n = (long)tape.a.size() - 1; n >= 0; n--) {
+    const double an = adj[n];
+    if (an == 0.0) continue;
+    if (tape.a[n] >= 0) adj[tape.a[n]] += tape.da[n] * an;
+    if (tape.b[n] >= 0) adj[tape.b[n]] += tape.db[n] * an;
+  }
+  for (long e = 0; e < nps; e++) gx0[e] = xid[e] >= 0 ? adj[xid[e]] : 0.0;
+  for (long e = 0; e < n1; e++) gu1[e] = adj[uid1 + e];
+  for (long e = 0; e < n2; e++) gu2[e] = adj[uid2 + e];
+  for (long e = 0; e < n3; e++) gu3[e] = adj[uid3 + e];
+  g_tape = nullptr;
+  g_threads = saved;
+  return 0;
 }
 
 int orc_velprd_f64(const orc_grid* g, double* ox, double* oy, double* oz, double* u, double* v,

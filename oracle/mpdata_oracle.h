@@ -101,6 +101,25 @@ int orc_rho_gauge_f64(const orc_grid* g, double* ox, double* oy, double* oz, dou
                       double* pexr2, const double* bcx, const double* bcy, double dxi, double dyi,
                       double dzi, double dt, double dt_ratio, int liner);
 
+/* Un-checkpointed FP64 adjoint of nsteps MPDATA steps (reverse-mode AD of
+ * this oracle's own step; branches of max/min/pp/pn/abs/sign taken at the
+ * forward values).  J = 0.5*sum((x_N - target)^2) over the interior; returns
+ * J, x_N (may be NULL) and dJ/dx_0 (psi-shaped), dJ/du1..u3 (C-grid shaped)
+ * for a velocity held fixed over the steps. */
+int orc_adjoint_f64(const orc_grid* g, int t_adv, int iord, int nonos, int nsteps, const double* x0,
+                    const double* bcx, const double* bcy, const double* u1, const double* u2,
+                    const double* u3, const double* rhr, const double* h, const double* target,
+                    double* J, double* xN, double* gx0, double* gu1, double* gu2, double* gu3);
+
+/* orc_adjoint_f64 plus the tangent-linear model on the same tape: dJ_tl =
+ * sum((x_N - target) * dx_N) for the directions dx0, du1..du3. */
+int orc_tangent_adjoint_f64(const orc_grid* g, int t_adv, int iord, int nonos, int nsteps, const double* x0,
+                            const double* bcx, const double* bcy, const double* u1, const double* u2,
+                            const double* u3, const double* rhr, const double* h, const double* target,
+                            double* J, double* xN, double* gx0, double* gu1, double* gu2, double* gu3,
+                            const double* dx0, const double* du1, const double* du2, const double* du3,
+                            double* dJ_tl);
+
 /* Threads used by the OpenMP loops (1 = the serial reference build). */
 void orc_set_threads(int n);
 int orc_get_threads(void);

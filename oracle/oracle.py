@@ -50,6 +50,10 @@ def lib():
         _lib.orc_velprd_f32.restype = I
         _lib.orc_rho_gauge_f64.argtypes = [ctypes.POINTER(OrcGrid)] + [P] * 19 + [D] * 5 + [I]
         _lib.orc_rho_gauge_f64.restype = I
+        _lib.orc_adjoint_f64.argtypes = [ctypes.POINTER(OrcGrid), I, I, I, I] + [P] * 15
+        _lib.orc_adjoint_f64.restype = I
+        _lib.orc_tangent_adjoint_f64.argtypes = [ctypes.POINTER(OrcGrid), I, I, I, I] + [P] * 20
+        _lib.orc_tangent_adjoint_f64.restype = I
         _lib.orc_a_to_c_f64.argtypes = [ctypes.POINTER(OrcGrid)] + [P] * 6
         _lib.orc_a_to_c_f64.restype = I
         _lib.orc_set_threads.argtypes = [I]
@@ -115,6 +119,41 @@ def rho_gauge(g, ox, oy, oz, u1, u2, u3, x_in, x_incomp, h, rhoadv, rhr, pexe, p
                                  _ptr(bcx, d), _ptr(bcy, d), dxi, dyi, dzi, dt, dt_ratio, int(liner))
     if rc != 0:
         raise ValueError("oracle rho_gauge failed with code %d" % rc)
+
+
+def adjoint(g, x0, bcx, bcy, u1, u2, u3, rhr, h, target, t_adv=1, iord=2, nonos=1, nsteps=1):
+    """Returns (J, x_N, dJ/dx0, dJ/du1, dJ/du2, dJ/du3) by AD of the oracle."""
+    d = np.float64
+    J = ctypes.c_double(0.0)
+    xN = np.zeros_like(x0, order="F")
+    gx = np.zeros_like(x0, order="F")
+    g1, g2, g3 = (np.zeros_like(a, order="F") for a in (u1, u2, u3))
+    rc = lib().orc_adjoint_f64(ctypes.byref(g), int(t_adv), int(iord), int(nonos), int(nsteps),
+                               _ptr(x0, d), _ptr(bcx, d), _ptr(bcy, d), _ptr(u1, d), _ptr(u2, d),
+                               _ptr(u3, d), _ptr(rhr, d), _ptr(h, d), _ptr(target, d), ctypes.byref(J),
+                               _ptr(xN, d), _ptr(gx, d), _ptr(g1, d), _ptr(g2, d), _ptr(g3, d))
+    if rc != 0:
+        raise ValueError("oracle adjoint failed with code %d" % rc)
+    return J.value, xN, gx, g1, g2, g3
+
+
+def tangent_dJ(g, x0, bcx, bcy, u1, u2, u3, rhr, h, target, dx0, du1, du2, du3, t_adv=1, iord=2,
+               nonos=1, nsteps=1):
+    """Directional derivative of J along (dx0, du) by the tangent-linear model."""
+    d = np.float64
+    J = ctypes.c_double(0.0)
+    dJ = ctypes.c_double(0.0)
+    gx = np.zeros_like(x0, order="F")
+    g1, g2, g3 = (np.zeros_like(a, order="F") for a in (u1, u2, u3))
+    rc = lib().orc_tangent_adjoint_f64(ctypes.byref(g), int(t_adv), int(iord), int(nonos), int(nsteps),
+                                       _ptr(x0, d), _ptr(bcx, d), _ptr(bcy, d), _ptr(u1, d), _ptr(u2, d),
+                                       _ptr(u3, d), _ptr(rhr, d), _ptr(h, d), _ptr(target, d),
+                                       ctypes.byref(J), None, _ptr(gx, d), _ptr(g1, d), _ptr(g2, d),
+                                       _ptr(g3, d), _ptr(dx0, d), _ptr(du1, d), _ptr(du2, d), _ptr(du3, d),
+                                       ctypes.byref(dJ))
+    if rc != 0:
+        raise ValueError("oracle tangent failed with code %d" % rc)
+    return dJ.value
 
 
 def a_to_c(g, uadv, vadv, wadv, u1, u2, u3):
