@@ -194,14 +194,16 @@ def make_state(nx, ny, nz, dtype_np, seed=20261203, T=200.0):
 
 
 class GpuArm:
-    def __init__(self, nx, ny, nz, precision, T=200.0):
+    def __init__(self, nx, ny, nz, precision, T=200.0, host=None):
         import torch
         from advectionhpctester_gb300 import mpdata as M
         self.torch, self.M = torch, M
         self.nx, self.ny, self.nz, self.T = nx, ny, nz, T
         dnp = np.float64 if precision == 64 else np.float32
         self.tdtype = torch.float64 if precision == 64 else torch.float32
-        f, pats = make_state(nx, ny, nz, dnp, T=T)
+        f, pats = host if host is not None else make_state(nx, ny, nz, np.float64, T=T)
+        f = f.astype(dnp) if f.dtype != dnp else f
+        pats = [p.astype(dnp, order="F") for p in pats]
         self.host = f
         self.pats_host = pats
         dv = lambda a: M.fortran_device(a, dtype=dnp)
@@ -236,8 +238,10 @@ def run_ours(args, ws, rank, local):
     torch.cuda.set_device(local)
     nx, ny, nz = args.grid
     cells = nx * ny * nz
-    arm = GpuArm(nx, ny, nz, args.precision)
+    host = make_state(nx, ny, nz, np.float64)
+    arm = GpuArm(nx, ny, nz, args.precision, host=host)
     stream = torch.cuda.current_stream()
+    mass0 = M.mass(arm.psi, arm.h)
     for n in range(args.warmup):
         arm.step(n)
     torch.cuda.synchronize()
@@ -293,10 +297,251 @@ def run_ours(args, ws, rank, local):
                   roofline=roof, gpu_launches=int(launches), clocks=clocks, stages=stage_json,
                   step_alg_bytes=int(step_alg),
                   step_hbm_frac=round(step_alg / (ms_max / args.steps * 1e-3) / 1e9 / peak, 4))
+    mass1 = M.mass(arm.psi, arm.h)
+    result["mass_rel_drift"] = (mass1 - mass0) / mass0
+    if rank == 0 and ws == 1 and not args.no_extras and args.precision == 64:
+        result["fp32"] = run_fp32_study(args, host, arm, ms_max / args.steps, mass0)
     if rank == 0 and ws == 1 and not args.no_e2e:
         result["e2e"] = run_e2e(arm, args)
     arm.ws.close()
+    del arm
+    if rank == 0 and ws == 1 and not args.no_extras:
+        torch.cuda.empty_cache()
+        result["adjoint"] = run_adjoint_study(args)
+        torch.cuda.empty_cache()
+        result["batch"] = run_batch_study(args)
     return result
+
+
+def run_fp32_study(args, host, arm64, ms64, mass0):
+    """Same workload and steps in FP32 (BASELINE's precision study): speedup
+    over the FP64 run, error against it, and FP64-compensated mass drift."""
+    import torch
+    M = arm64.M
+    nx, ny, nz = args.grid
+    arm = GpuArm(nx, ny, nz, 32, host=host)
+    for n in range(args.warmup):
+        arm.step(n)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for n in range(args.warmup, args.warmup + args.steps):
+        arm.step(n)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    linf, l2, bmax, bl2 = M.error_norms(arm.psi, arm64.psi)
+    m32 = M.mass(arm.psi, arm.h)
+    cells = nx * ny * nz
+    out = {"value": round(cells / (ms * 1e-3) / 1e9, 4), "unit": UNIT, "ms_per_step": round(ms, 4),
+           "speedup_vs_fp64": round(ms64 / ms, 3),
+           "linf_rel_err_vs_fp64": linf / bmax, "l2_rel_err_vs_fp64": l2 / bl2,
+           "steps_compared": args.warmup + args.steps,
+           "mass_rel_drift": (m32 - mass0) / mass0,
+           "note": "FP32 stencil arithmetic, FP64 Neumaier-compensated mass and norms"}
+    arm.ws.close()
+    return out
+
+
+def run_adjoint_study(args, n=(256, 256, 64), nsteps=200):
+    """Adjoint of the gauge iord=2 nonoscillatory step on 256x256x64 periodic,
+    deformational flow held fixed, Gaussian-cone psi, J = 0.5|psi_N - target|^2
+    with a shifted-cone target, sqrt(N) checkpointing."""
+    import torch
+    from advectionhpctester_gb300 import mpdata as M
+    from advectionhpctester_gb300 import workloads as W
+    nx, ny, nz = n
+    f = W.Fields(nx, ny, nz, 1, 1, 1, 1)
+    ua, va, wa = W.deformational_agrid(nx, ny, nz, 0.0, float(nsteps))
+    W.set_c_grid_periodic(f, ua, va, wa)
+    x = (np.arange(nx) + 0.5) / nx
+    y = (np.arange(ny) + 0.5) / ny
+    z = (np.arange(nz) + 0.5) / nz
+    rng = np.random.default_rng(5)
+    off = rng.uniform(-0.1, 0.1, 3)
+
+    def cone(cx, cy, cz):
+        r2 = (x - cx)[:, None, None] ** 2 + (y - cy)[None, :, None] ** 2 + (z - cz)[None, None, :] ** 2
+        return 1.0 + np.exp(-r2 / (2 * 0.1 ** 2))
+    W.interior(f.x)[...] = cone(0.5, 0.5, 0.5)
+    tg = np.zeros_like(f.x)
+    W.interior(tg)[...] = cone(0.5 + off[0], 0.5 + off[1], 0.5 + off[2])
+    d = {k: M.fortran_device(getattr(f, k)) for k in ("x", "u1", "u2", "u3", "h", "rhr")}
+    target = M.fortran_device(tg)
+    ws = M.Workspace(nx, ny, nz, 1, 1, 1, 1, iord=2, nonos=1, gauge=1, precision=64)
+    psi = d["x"].clone()
+    for _ in range(3):
+        ws.step(psi, d["u1"], d["u2"], d["u3"], d["h"], d["rhr"])
+    psi.copy_(d["x"])
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(nsteps):
+        ws.step(psi, d["u1"], d["u2"], d["u3"], d["h"], d["rhr"])
+    e1.record()
+    torch.cuda.synchronize()
+    fwd_ms = e0.elapsed_time(e1)
+    # one step adjoint alone (recompute + reverse)
+    lam = psi.clone()
+    gu = [torch.zeros_like(d[k]) for k in ("u1", "u2", "u3")]
+    ws.step_adjoint(d["x"], d["u1"], d["u2"], d["u3"], d["h"], d["rhr"], lam, *gu)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(10):
+        ws.step_adjoint(d["x"], d["u1"], d["u2"], d["u3"], d["h"], d["rhr"], lam, *gu)
+    e1.record()
+    torch.cuda.synchronize()
+    step_adj_ms = e0.elapsed_time(e1) / 10
+    psi.copy_(d["x"])
+    gx = torch.zeros_like(psi)
+    gu = [torch.zeros_like(d[k]) for k in ("u1", "u2", "u3")]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    J, peak = ws.adjoint_run(nsteps, psi, d["u1"], d["u2"], d["u3"], d["h"], d["rhr"], target, gx, *gu)
+    run_ms = (time.perf_counter() - t0) * 1e3
+    ws.close()
+    cells = nx * ny * nz
+    return {"workload": "adjoint_%dx%dx%d_periodic_gauge_iord2_nonos_N%d" % (nx, ny, nz, nsteps),
+            "forward_ms_per_step": round(fwd_ms / nsteps, 4),
+            "step_adjoint_ms": round(step_adj_ms, 4),
+            "step_adjoint_over_forward": round(step_adj_ms / (fwd_ms / nsteps), 3),
+            "run_ms": round(run_ms, 2), "run_over_forward": round(run_ms / fwd_ms, 3),
+            "checkpoint_interval": int(math.ceil(math.sqrt(nsteps))),
+            "adjoint_gcell_steps_per_s": round(cells * nsteps / (run_ms * 1e-3) / 1e9, 4),
+            "peak_bytes": int(peak), "J": J}
+
+
+def batch_domains(seed=3, count=64):
+    sizes = [(32, 32, 32), (64, 64, 64), (128, 128, 64), (256, 256, 64), (192, 96, 48)]
+    rng = np.random.default_rng(seed)
+    picks = [sizes[i] for i in rng.integers(0, len(sizes), count)]
+    return picks, rng
+
+
+def make_domain_device(n, rng, torch_dtype):
+    """One periodic domain generated on the device: solid-body rotation about
+    z or the deformational flow, Courant U[0.2,0.5], Gaussian plus noise psi."""
+    import torch
+    from advectionhpctester_gb300 import mpdata as M
+    nx, ny, nz = n
+    dev = "cuda"
+    c = float(rng.uniform(0.2, 0.5))
+    kind = int(rng.integers(0, 2))
+    g = torch.Generator(device=dev)
+    g.manual_seed(int(rng.integers(0, 2 ** 31)))
+    sh = M.shapes(nx, ny, nz, 1)
+    t = {k: M.fortran_empty(sh[k], torch_dtype) for k in ("u1", "u2", "u3")}
+    for k in ("psi", "h", "rhr"):
+        t[k] = M.fortran_empty(sh["psi"], torch_dtype)
+    t["h"].fill_(1.0)
+    t["rhr"].fill_(1.0)
+    x = (torch.arange(nx, device=dev, dtype=torch.float64) + 0.5) / nx
+    y = (torch.arange(ny, device=dev, dtype=torch.float64) + 0.5) / ny
+    z = (torch.arange(nz, device=dev, dtype=torch.float64) + 0.5) / nz
+    X, Y, Z = torch.meshgrid(x, y, z, indexing="ij")
+    if kind == 0:  # solid body about z through the centre, on the faces
+        xf = torch.arange(nx, device=dev, dtype=torch.float64) / nx
+        yf = torch.arange(ny, device=dev, dtype=torch.float64) / ny
+        ua = -(Y - 0.5) * torch.ones_like(X)
+        va = (X - 0.5) * torch.ones_like(Y)
+        u1 = -(y[None, :, None] - 0.5).expand(nx, ny, nz) + 0 * xf[:, None, None]
+        u2 = (x[:, None, None] - 0.5).expand(nx, ny, nz) + 0 * yf[None, :, None]
+        u3 = torch.zeros_like(X)
+        s = c / 0.5
+        u1, u2 = u1 * s, u2 * s
+        del ua, va
+    else:
+        ua = torch.sin(math.pi * X) ** 2 * torch.sin(2 * math.pi * Y)
+        va = -torch.sin(math.pi * Y) ** 2 * torch.sin(2 * math.pi * X)
+        wa = 0.1 * torch.sin(2 * math.pi * Z)
+        s = c / 1.1
+        u1 = 0.5 * (ua + torch.roll(ua, 1, 0)) * s
+        u2 = 0.5 * (va + torch.roll(va, 1, 1)) * s
+        u3 = 0.5 * (wa + torch.roll(wa, 1, 2)) * s
+    cx, cy, cz = (float(v) for v in rng.uniform(0.3, 0.7, 3))
+    psi = 1.0 + torch.exp(-((X - cx) ** 2 + (Y - cy) ** 2 + (Z - cz) ** 2) / (2 * 0.1 ** 2))
+    psi = psi + 0.01 * torch.rand(psi.shape, device=dev, dtype=torch.float64, generator=g)
+    t["psi"][1:-1, 1:-1, 1:-1] = psi.to(torch_dtype)
+    t["u1"][1:-2, 1:-1, 1:-1] = u1.to(torch_dtype)
+    t["u1"][-2, 1:-1, 1:-1] = u1[0].to(torch_dtype)
+    t["u2"][1:-1, 1:-2, 1:-1] = u2.to(torch_dtype)
+    t["u2"][1:-1, -2, 1:-1] = u2[:, 0].to(torch_dtype)
+    t["u3"][1:-1, 1:-1, 1:-2] = u3.to(torch_dtype)
+    t["u3"][1:-1, 1:-1, -2] = u3[:, :, 0].to(torch_dtype)
+    return t
+
+
+def run_batch_study(args, steps=10):
+    """BASELINE config 3: 64 periodic domains of uneven sizes (seed 3) in one
+    batch (one CUDA-graph launch per step, tuned tile shape) against a loop of
+    per-domain steps; FP64 and FP32.  Plus 16 tracers sharing one velocity on
+    256x256x64 against 16 separate steps."""
+    import torch
+    from advectionhpctester_gb300 import mpdata as M
+    out = {}
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    for prec, tdt in ((64, torch.float64), (32, torch.float32)):
+        picks, rng = batch_domains()
+        doms = [make_domain_device(n, rng, tdt) for n in picks]
+        cells = sum(a * b * c for a, b, c in picks)
+        probs = [dict(np=n[0], mp=n[1], lp=n[2], gauge=1) for n in picks]
+        b = M.Batch(probs, iord=2, nonos=1, precision=prec)
+        for p, t in enumerate(doms):
+            b.set(p, t["psi"], t["u1"], t["u2"], t["u3"], t["h"], t["rhr"])
+        bx, by = b.tune()
+        b.graph(True)
+        ms_batch = timed(b.step, steps)
+        wss = [M.Workspace(*n, 1, 1, 1, 1, iord=2, nonos=1, gauge=1, precision=prec) for n in picks]
+
+        def loop():
+            for w, t in zip(wss, doms):
+                w.step(t["psi"], t["u1"], t["u2"], t["u3"], t["h"], t["rhr"])
+        ms_loop = timed(loop, steps)
+        for w in wss:
+            w.close()
+        b.close()
+        out["domains_fp%d" % prec] = {
+            "domains": len(picks), "cells": cells, "tile": [bx, by],
+            "graph_gcell_steps_per_s": round(cells / (ms_batch * 1e-3) / 1e9, 4),
+            "loop_gcell_steps_per_s": round(cells / (ms_loop * 1e-3) / 1e9, 4),
+            "speedup_vs_loop": round(ms_loop / ms_batch, 3),
+            "launches_per_step": 5, "graph_launches_per_step": 1}
+        del doms
+        torch.cuda.empty_cache()
+    # 16 tracers sharing one velocity
+    rng = np.random.default_rng(16)
+    base = make_domain_device((256, 256, 64), rng, torch.float64)
+    tr = [base["psi"].clone() * (1.0 + 0.01 * k) for k in range(16)]
+    b = M.Batch([dict(np=256, mp=256, lp=64, gauge=1, velocity_group=0)] * 16, iord=2, nonos=1, precision=64)
+    for p in range(16):
+        b.set(p, tr[p], base["u1"], base["u2"], base["u3"], base["h"], base["rhr"])
+    b.graph(True)
+    ms_b = timed(b.step, steps)
+    w = M.Workspace(256, 256, 64, 1, 1, 1, 1, iord=2, nonos=1, gauge=1, precision=64)
+
+    def loop16():
+        for p in range(16):
+            w.step(tr[p], base["u1"], base["u2"], base["u3"], base["h"], base["rhr"])
+    ms_l = timed(loop16, steps)
+    w.close()
+    b.close()
+    tc = 16 * 256 * 256 * 64
+    out["tracers16_fp64"] = {"tracer_cells": tc,
+                             "batch_gcell_steps_per_s": round(tc / (ms_b * 1e-3) / 1e9, 4),
+                             "loop_gcell_steps_per_s": round(tc / (ms_l * 1e-3) / 1e9, 4),
+                             "speedup_vs_loop": round(ms_l / ms_b, 3)}
+    return out
 
 
 def run_e2e(arm, args):
@@ -417,6 +662,8 @@ def main():
     ap.add_argument("--ref-slab", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the FP32, adjoint and batch studies")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
