@@ -4,10 +4,10 @@
 // The reference advects up to 12 fields that share one velocity with a
 // single fused upwind kernel and one antidiffusion call per field
 // (advection/src_drivers/advection_CEtimestep_twostep_GPUBC.f90:193-339).
-// Here every stage of every problem is one persistent launch: each block
-// takes a contiguous chunk of tiles from the concatenated tile space of all
-// problems and runs the same per-cell bodies as the single-problem path
-// (mpdata_body.cuh) on the problem descriptor it stages in shared memory.
+// Here every stage of every problem is one launch over the concatenated tile
+// space of all problems: each block takes one tile, stages its problem's
+// descriptor in shared memory and runs the same per-cell bodies as the
+// single-problem path (mpdata_body.cuh).
 // Problems of one velocity group share the velocity-derived scratch (1/h and
 // the face reciprocal densities), computed once by the group's first problem.
 #include "mpdata_body.cuh"
@@ -25,72 +25,46 @@ __device__ __forceinline__ void load_prob(Prob<R>& sP, const Prob<R>* __restrict
   for (int w = tid; w < (int)(sizeof(Prob<R>) / 8); w += nt) dst[w] = __ldg(src + w);
 }
 
-// Walk this block's chunk of tiles; BODY sees P (shared), i, j, k.
-#define BATCH_LOOP(BODY)                                                                     \
+// One tile per block.  tiles[blockIdx.x] packs the problem (bits 0-15) and
+// the tile's x index (16-31), y index (32-47) and plane k-1 (48-63); the
+// host builds the list for the current block shape.  BODY sees P (shared),
+// i, j, k.
+#define BATCH_TILE(BODY)                                                                     \
   __shared__ __align__(16) unsigned char sraw[sizeof(Prob<R>)];                              \
   Prob<R>& P = *reinterpret_cast<Prob<R>*>(sraw);                                            \
-  const long long chunk = (tiles + gridDim.x - 1) / gridDim.x;                               \
-  const long long t0 = (long long)blockIdx.x * chunk;                                        \
-  const long long t1 = t0 + chunk < tiles ? t0 + chunk : tiles;                              \
-  int p = -1;                                                                                \
-  long long pend = -1, pbeg = 0;                                                             \
-  int ntx = 1, nty = 1;                                                                      \
-  for (long long t = t0; t < t1; t++) {                                                      \
-    if (t >= pend) {                                                                         \
-      if (p < 0) {                                                                           \
-        int lo = 0, hi = nprob - 1;                                                          \
-        while (lo < hi) {                                                                    \
-          const int mid = (lo + hi + 1) >> 1;                                                \
-          if (__ldg(prefix + mid) <= t) lo = mid; else hi = mid - 1;                         \
-        }                                                                                    \
-        p = lo;                                                                              \
-      } else {                                                                               \
-        do { p++; } while (__ldg(prefix + p + 1) <= t);                                      \
-      }                                                                                      \
-      pbeg = __ldg(prefix + p);                                                              \
-      pend = __ldg(prefix + p + 1);                                                          \
-      __syncthreads();                                                                       \
-      load_prob<R>(P, probs, p);                                                             \
-      __syncthreads();                                                                       \
-      ntx = (P.g.np + blockDim.x - 1) / blockDim.x;                                          \
-      nty = (P.g.mp + blockDim.y - 1) / blockDim.y;                                          \
-    }                                                                                        \
-    long long lt = t - pbeg;                                                                 \
-    const int tx = (int)(lt % ntx);                                                          \
-    lt /= ntx;                                                                               \
-    const int ty = (int)(lt % nty);                                                          \
-    const int k = (int)(lt / nty) + 1;                                                       \
-    const int i = tx * blockDim.x + threadIdx.x + 1;                                         \
-    const int j = ty * blockDim.y + threadIdx.y + 1;                                         \
-    if (i <= P.g.np && j <= P.g.mp) { BODY; }                                                \
-  }
+  const unsigned long long w = __ldg(tiles + blockIdx.x);                                    \
+  load_prob<R>(P, probs, (int)(w & 0xffffu));                                                \
+  __syncthreads();                                                                           \
+  const int i = (int)((w >> 16) & 0xffffu) * (int)blockDim.x + (int)threadIdx.x + 1;         \
+  const int j = (int)((w >> 32) & 0xffffu) * (int)blockDim.y + (int)threadIdx.y + 1;         \
+  const int k = (int)(w >> 48) + 1;                                                          \
+  if (i <= P.g.np && j <= P.g.mp) { BODY; }
 
-#define BATCH_ARGS const Prob<R>* __restrict__ probs, const long long* __restrict__ prefix, int nprob, \
-                   long long tiles
+#define BATCH_ARGS const Prob<R>* __restrict__ probs, const unsigned long long* __restrict__ tiles
 
 template <class R, bool ANTIDIFF, bool HALO>
 __global__ void __launch_bounds__(256) kb_upwind(BATCH_ARGS) {
-  BATCH_LOOP((upwind_body<R, ANTIDIFF, HALO>(P, i, j, k)))
+  BATCH_TILE((upwind_body<R, ANTIDIFF, HALO>(P, i, j, k)))
 }
 template <class R>
 __global__ void __launch_bounds__(256) kb_copy(BATCH_ARGS) {
-  BATCH_LOOP((copy_body<R>(P, i, j, k)))
+  BATCH_TILE((copy_body<R>(P, i, j, k)))
 }
 template <class R, bool AIN>
 __global__ void __launch_bounds__(256) kb_pseudo(BATCH_ARGS) {
-  BATCH_LOOP((pseudo_body<R, AIN>(P, i, j, k)))
+  BATCH_TILE((pseudo_body<R, AIN>(P, i, j, k)))
 }
 template <class R, bool NONOS, bool FIRST, bool KEEP>
 __global__ void __launch_bounds__(256) kb_bounds(BATCH_ARGS) {
-  BATCH_LOOP((bounds_body<R, NONOS, FIRST, KEEP>(P, i, j, k)))
+  BATCH_TILE((bounds_body<R, NONOS, FIRST, KEEP>(P, i, j, k)))
 }
 template <class R, bool NONOS>
 __global__ void __launch_bounds__(256) kb_limit(BATCH_ARGS) {
-  BATCH_LOOP((limit_body<R, NONOS>(P, i, j, k)))
+  BATCH_TILE((limit_body<R, NONOS>(P, i, j, k)))
 }
 template <class R, bool LAST>
 __global__ void __launch_bounds__(256) kb_update(BATCH_ARGS) {
-  BATCH_LOOP((update_body<R, LAST>(P, i, j, k)))
+  BATCH_TILE((update_body<R, LAST>(P, i, j, k)))
 }
 
 #define BLAUNCH(stage, ...)                  \
@@ -104,8 +78,8 @@ __global__ void __launch_bounds__(256) kb_update(BATCH_ARGS) {
 template <class R>
 int run_batch(const BatchLaunch<R>& B, Prof* prof, cudaStream_t s) {
   const dim3 blk(B.bx, B.by, 1);
-  const int G = B.grid;
-#define A B.probs, B.prefix, B.nprob, B.tiles
+  const int G = B.ntiles;
+#define A B.probs, B.tiles
   if (B.iord < 2) {
     if (B.halo) {
       BLAUNCH(ST_UPWIND, (kb_upwind<R, false, true><<<G, blk, 0, s>>>(A)));
@@ -138,17 +112,5 @@ int run_batch(const BatchLaunch<R>& B, Prof* prof, cudaStream_t s) {
 template int run_batch<double>(const BatchLaunch<double>&, Prof*, cudaStream_t);
 template int run_batch<float>(const BatchLaunch<float>&, Prof*, cudaStream_t);
 
-// Resident blocks per SM of the heaviest batched kernel for a block shape.
-template <class R>
-int batch_occupancy(int threads) {
-  int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_pseudo<R, true>, threads, 0) != cudaSuccess) {
-    cudaGetLastError();
-    return 1;
-  }
-  return n > 0 ? n : 1;
-}
-template int batch_occupancy<double>(int);
-template int batch_occupancy<float>(int);
 
 }  // namespace mpdata

@@ -19,8 +19,6 @@ using namespace mpdata;
 
 namespace mpdata {
 template <class R>
-int batch_occupancy(int threads);
-template <class R>
 int run_reduce(Geo g, int mode, const R* a, const R* h, const R* rhr, const void* b, int b_is_f64,
                double* part, double* out, cudaStream_t s);
 int reduce_blocks();
@@ -246,15 +244,23 @@ bool same(const Workspace* w, const mpdata_grid& g, const mpdata_opts& o) {
   return !memcmp(&w->g, &g, sizeof g) && !memcmp(&w->o, &o, sizeof o);
 }
 
+// advec.f90:148-244.  The SELECT on legacyoptmode (and on t_adv for 2 and 4)
+// runs first and stops on a bad value; CASE(5) leaves the upwind pointer
+// unassociated, so the reference's later call through it has no defined
+// result (MPDATA_E_UNSUPPORTED here).  Then lvertsplit=.TRUE. and
+// legacyoptmode 2 do nothing (their calls are commented out, :213-220), 6 runs
+// the upwind step and copies xant back (:221-231), and 4 runs upwind followed
+// by the antidiffusive corrections (:232-241).
 template <class R>
-int advec_dwarf_impl(int legacyoptmode, int t_adv, int np, int mp, int lp, int ih, int ipoles,
-                     int ibcx, int ibcy, int ibcz, R* x, const R* x_lr, const R* x_bt,
+int advec_dwarf_impl(int legacyoptmode, int t_adv, int lvertsplit, int np, int mp, int lp, int ih,
+                     int ipoles, int ibcx, int ibcy, int ibcz, R* x, const R* x_lr, const R* x_bt,
                      const R* uadv, const R* vadv, const R* wadv, const R* rhr, const R* rhoadv,
                      int iord, int nonos, void* stream) {
-  // advec.f90:148-211
-  if (legacyoptmode == 2) return MPDATA_OK;  // CASE(2): the reference's call is commented out
-  if (legacyoptmode != 4 && legacyoptmode != 6) return MPDATA_E_OPTS;
-  if (legacyoptmode == 4 && t_adv != 1 && t_adv != 2) return MPDATA_E_OPTS;
+  if (legacyoptmode != 2 && legacyoptmode != 4 && legacyoptmode != 5 && legacyoptmode != 6)
+    return MPDATA_E_OPTS;
+  if ((legacyoptmode == 2 || legacyoptmode == 4) && t_adv != 1 && t_adv != 2) return MPDATA_E_OPTS;
+  if (lvertsplit || legacyoptmode == 2) return MPDATA_OK;
+  if (legacyoptmode == 5) return MPDATA_E_UNSUPPORTED;
   if (ipoles != 0) return MPDATA_E_UNSUPPORTED;
   mpdata_grid g{np, mp, lp, ih, ibcx, ibcy, ibcz};
   mpdata_opts o{legacyoptmode == 6 ? 1 : iord, legacyoptmode == 6 ? 0 : nonos,
@@ -354,8 +360,7 @@ int mpdata_advec_dwarf_f64(int legacyoptmode, int t_adv, int lupdatemulti, int l
                            const double* vadv, const double* wadv, const double* rhr,
                            const double* rhoadv, int iord, int nonos, void* stream) {
   (void)lupdatemulti;
-  (void)lvertsplit;
-  return advec_dwarf_impl<double>(legacyoptmode, t_adv, np, mp, lp, ih, ipoles, ibcx, ibcy, ibcz, x,
+  return advec_dwarf_impl<double>(legacyoptmode, t_adv, lvertsplit, np, mp, lp, ih, ipoles, ibcx, ibcy, ibcz, x,
                                   x_lr, x_bt, uadv, vadv, wadv, rhr, rhoadv, iord, nonos, stream);
 }
 int mpdata_advec_dwarf_f32(int legacyoptmode, int t_adv, int lupdatemulti, int lvertsplit, int np,
@@ -364,8 +369,7 @@ int mpdata_advec_dwarf_f32(int legacyoptmode, int t_adv, int lupdatemulti, int l
                            const float* vadv, const float* wadv, const float* rhr,
                            const float* rhoadv, int iord, int nonos, void* stream) {
   (void)lupdatemulti;
-  (void)lvertsplit;
-  return advec_dwarf_impl<float>(legacyoptmode, t_adv, np, mp, lp, ih, ipoles, ibcx, ibcy, ibcz, x,
+  return advec_dwarf_impl<float>(legacyoptmode, t_adv, lvertsplit, np, mp, lp, ih, ipoles, ibcx, ibcy, ibcz, x,
                                  x_lr, x_bt, uadv, vadv, wadv, rhr, rhoadv, iord, nonos, stream);
 }
 
@@ -501,9 +505,10 @@ struct Batch {
   void* d_table;
   unsigned char* h_stage;       // pinned staging buffer of the table upload
   cudaEvent_t upload_done;
-  long long* d_prefix;
-  long long tiles;
-  int bx, by, grid;
+  unsigned long long* d_tiles;   // packed tile list of the current block shape
+  size_t tiles_cap;             // capacity of d_tiles (entries)
+  int ntiles;
+  int bx, by;
   bool dirty;
   bool use_graph;
   cudaGraphExec_t gexec;
@@ -523,32 +528,44 @@ mpdata_grid grid_of(const Batch* b, int p) {
   return mpdata_grid{q.np, q.mp, q.lp, b->ih, q.ibcx, q.ibcy, q.ibcz};
 }
 
-// tile prefix for a block shape (tiles of bx*by cells in one plane)
-std::vector<long long> tile_prefix(const Batch* b, int bx, int by) {
-  std::vector<long long> pre(b->nprob + 1, 0);
+// Tile list for a block shape: one 64-bit word per tile of bx*by cells in
+// one plane, packing the problem (bits 0-15), the tile's x and y indices
+// (16-31, 32-47) and its plane k-1 (48-63).  Problems follow one another,
+// and within a problem x varies fastest, then y, then k.
+int set_shape(Batch* b, int bx, int by, cudaStream_t s) {
+  long long total = 0;
   for (int p = 0; p < b->nprob; p++) {
     const mpdata_problem& q = b->pr[p];
-    pre[p + 1] = pre[p] + (long long)((q.np + bx - 1) / bx) * ((q.mp + by - 1) / by) * q.lp;
+    const long long ntx = (q.np + bx - 1) / bx, nty = (q.mp + by - 1) / by;
+    if (ntx > 65536 || nty > 65536) return MPDATA_E_DIMS;
+    total += ntx * nty * q.lp;
   }
-  return pre;
-}
-
-int set_shape(Batch* b, int bx, int by, cudaStream_t s) {
-  std::vector<long long> pre = tile_prefix(b, bx, by);
-  if (cudaMemcpyAsync(b->d_prefix, pre.data(), pre.size() * sizeof(long long), cudaMemcpyHostToDevice, s) !=
-      cudaSuccess)
+  if (total < 1 || total > 0x7fffffffLL) return MPDATA_E_TOO_LARGE;
+  std::vector<unsigned long long> list;
+  list.reserve((size_t)total);
+  for (int p = 0; p < b->nprob; p++) {
+    const mpdata_problem& q = b->pr[p];
+    const int ntx = (q.np + bx - 1) / bx, nty = (q.mp + by - 1) / by;
+    for (int k = 0; k < q.lp; k++)
+      for (int ty = 0; ty < nty; ty++)
+        for (int tx = 0; tx < ntx; tx++)
+          list.push_back((unsigned long long)p | ((unsigned long long)tx << 16) |
+                         ((unsigned long long)ty << 32) | ((unsigned long long)k << 48));
+  }
+  if (list.size() > b->tiles_cap) {
+    if (b->d_tiles && cudaFree(b->d_tiles) != cudaSuccess) return MPDATA_E_CUDA;
+    b->d_tiles = nullptr;
+    b->tiles_cap = 0;
+    if (cudaMalloc(&b->d_tiles, list.size() * sizeof(unsigned long long)) != cudaSuccess) return MPDATA_E_CUDA;
+    b->tiles_cap = list.size();
+  }
+  if (cudaMemcpyAsync(b->d_tiles, list.data(), list.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice,
+                      s) != cudaSuccess)
     return MPDATA_E_CUDA;
-  if (cudaStreamSynchronize(s) != cudaSuccess) return MPDATA_E_CUDA;  // pre is a local buffer
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int occ = b->precision == 64 ? batch_occupancy<double>(bx * by) : batch_occupancy<float>(bx * by);
+  if (cudaStreamSynchronize(s) != cudaSuccess) return MPDATA_E_CUDA;  // list is a local buffer
   b->bx = bx;
   b->by = by;
-  b->tiles = pre.back();
-  long long g = (long long)sms * occ;
-  if (g > b->tiles) g = b->tiles;
-  b->grid = (int)(g > 0 ? g : 1);
+  b->ntiles = (int)total;
   if (b->gexec) {
     cudaGraphExecDestroy(b->gexec);
     b->gexec = nullptr;
@@ -574,12 +591,10 @@ template <class R>
 BatchLaunch<R> launch_of(const Batch* b, int halo) {
   BatchLaunch<R> L;
   L.probs = static_cast<const Prob<R>*>(b->d_table);
-  L.prefix = b->d_prefix;
-  L.nprob = b->nprob;
-  L.tiles = b->tiles;
+  L.tiles = b->d_tiles;
+  L.ntiles = b->ntiles;
   L.bx = b->bx;
   L.by = b->by;
-  L.grid = b->grid;
   L.iord = b->iord;
   L.nonos = b->nonos;
   L.halo = halo;
@@ -670,7 +685,9 @@ int mpdata_batch_create(int nprob, const mpdata_problem* probs, int ih, int iord
   b->table.assign((size_t)nprob * b->pbytes, 0);
   b->mem = b->d_table = nullptr;
   b->h_stage = nullptr;
-  b->d_prefix = nullptr;
+  b->d_tiles = nullptr;
+  b->tiles_cap = 0;
+  b->ntiles = 0;
   b->upload_done = nullptr;
   b->gexec = nullptr;
   b->cap = nullptr;
@@ -680,7 +697,6 @@ int mpdata_batch_create(int nprob, const mpdata_problem* probs, int ih, int iord
   b->dirty = true;
   bool ok = cudaMalloc(&b->mem, off * b->elem) == cudaSuccess &&
             cudaMalloc(&b->d_table, b->table.size()) == cudaSuccess &&
-            cudaMalloc(&b->d_prefix, sizeof(long long) * (nprob + 1)) == cudaSuccess &&
             cudaMallocHost(&b->h_stage, b->table.size()) == cudaSuccess &&
             cudaEventCreateWithFlags(&b->upload_done, cudaEventDisableTiming) == cudaSuccess &&
             cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking) == cudaSuccess;
@@ -694,12 +710,13 @@ int mpdata_batch_create(int nprob, const mpdata_problem* probs, int ih, int iord
       for (auto& e : g_tuned)
         if (!memcmp(&e.first, &k, sizeof k)) { bx = e.second.first; by = e.second.second; }
     }
-    ok = set_shape(b, bx, by, b->cap) == MPDATA_OK;
+    rc = set_shape(b, bx, by, b->cap);
+    ok = rc == MPDATA_OK;
   }
   if (!ok) {
     cudaGetLastError();
     mpdata_batch_destroy(b);
-    return MPDATA_E_CUDA;
+    return rc != MPDATA_OK ? rc : MPDATA_E_CUDA;
   }
   *batch = b;
   return MPDATA_OK;
@@ -714,7 +731,7 @@ int mpdata_batch_destroy(void* batch) {
   if (b->upload_done) { cudaEventSynchronize(b->upload_done); cudaEventDestroy(b->upload_done); }
   if (b->cap) cudaStreamDestroy(b->cap);
   cudaFreeHost(b->h_stage);
-  cudaFree(b->d_prefix);
+  cudaFree(b->d_tiles);
   cudaFree(b->d_table);
   cudaError_t e = cudaFree(b->mem);
   delete b;
@@ -782,7 +799,9 @@ int mpdata_batch_tune(void* batch, void* stream, int* bx_out, int* by_out) {
   float best = 1e30f;
   int bbx = b->bx, bby = b->by;
   for (const auto& sh : shapes) {
-    if (set_shape(b, sh[0], sh[1], s)) { rc = MPDATA_E_CUDA; break; }
+    const int r0 = set_shape(b, sh[0], sh[1], s);
+    if (r0 == MPDATA_E_DIMS || r0 == MPDATA_E_TOO_LARGE) continue;  // shape unusable for these grids
+    if (r0) { rc = r0; break; }
     // halo=0: the tuning steps write scratch only, never the caller's psi
     if ((rc = batch_run(b, 0, nullptr, s))) break;
     cudaEventRecord(e0, s);
@@ -795,8 +814,9 @@ int mpdata_batch_tune(void* batch, void* stream, int* bx_out, int* by_out) {
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  if (set_shape(b, bbx, bby, s)) return MPDATA_E_CUDA;
+  const int r1 = set_shape(b, bbx, bby, s);
   if (rc) return rc;
+  if (r1) return r1;
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     const TuneKey k = key_of(b);

@@ -21,18 +21,16 @@ struct Prof {
 template <class R>
 int run_step(const Prob<R>& P, int iord, int nonos, Prof* prof, cudaStream_t stream);
 
-// One step of every problem of a batch.  probs/prefix live in device memory:
-// prefix[p] is the first tile of problem p (tiles of bx*by cells in one
-// plane), prefix[nprob] the total.  Each stage is one persistent grid-stride
-// launch of `grid` blocks of bx*by threads over all tiles of all problems.
+// One step of every problem of a batch.  probs and tiles live in device
+// memory: tiles[t] packs the problem (bits 0-15), the x and y tile indices
+// (16-31, 32-47) and the plane k-1 (48-63) of tile t, tiles of bx*by cells in
+// one plane.  Each stage is one launch of ntiles blocks of bx*by threads.
 template <class R>
 struct BatchLaunch {
   const Prob<R>* probs;
-  const long long* prefix;
-  int nprob;
-  long long tiles;
+  const unsigned long long* tiles;
+  int ntiles;
   int bx, by;
-  int grid;
   int iord, nonos;
   int halo;  // 0 while autotuning: psi (interior and halo) is not written
 };

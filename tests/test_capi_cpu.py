@@ -54,11 +54,17 @@ def test_calls_without_workspace_fail(native_lib):
     assert native_lib.mpdata_ws_error(None, out) == -4
 
 
-@pytest.mark.parametrize("opt,t_adv,ipoles,code", [
-    (3, 1, 0, -2), (5, 1, 0, -2), (4, 3, 0, -2), (4, 1, 1, -7), (2, 1, 0, 0)])
-def test_advec_dwarf_option_dispatch(native_lib, opt, t_adv, ipoles, code):
-    """advec.f90:148-211: 4/6 run, 2 is the reference's no-op branch, other
-    modes are rejected (the reference STOPs)."""
-    rc = native_lib.mpdata_advec_dwarf_f64(opt, t_adv, 0, 0, 8, 8, 8, 1, ipoles, 0, 0, 0,
+@pytest.mark.parametrize("opt,t_adv,lvertsplit,ipoles,code", [
+    (3, 1, 0, 0, -2), (0, 1, 0, 0, -2), (7, 1, 0, 0, -2),   # commented-out or absent CASEs: STOP
+    (4, 3, 0, 0, -2), (2, 0, 0, 0, -2), (2, 3, 1, 0, -2),   # bad t_adv under 2/4: STOP, even when split
+    (5, 1, 0, 0, -7),                                       # CASE(5): unassociated upwind pointer
+    (4, 1, 1, 1, 0), (6, 1, 1, 0, 0),                       # lvertsplit: the split call is commented out
+    (2, 1, 0, 0, 0), (2, 2, 0, 0, 0),                       # CASE(2): the mpdata3d call is commented out
+    (4, 1, 0, 1, -7)])                                      # ipoles: not on the single-rank path
+def test_advec_dwarf_option_dispatch(native_lib, opt, t_adv, lvertsplit, ipoles, code):
+    """advec.f90:148-244: the SELECT on legacyoptmode/t_adv STOPs on bad values
+    before anything runs; lvertsplit and mode 2 then do nothing; 4 and 6 run
+    (not reached here: every array is NULL, so a running mode would fail)."""
+    rc = native_lib.mpdata_advec_dwarf_f64(opt, t_adv, 0, lvertsplit, 8, 8, 8, 1, ipoles, 0, 0, 0,
                                            *([None] * 8), 2, 1, None)
     assert rc == code
