@@ -66,6 +66,12 @@ SIGNATURES = {
     "mpdata_mass_f64": ([ctypes.POINTER(MpdataGrid), P, P, P, ctypes.POINTER(D), P], I),
     "mpdata_mass_f32": ([ctypes.POINTER(MpdataGrid), P, P, P, ctypes.POINTER(D), P], I),
     "mpdata_error_norms": ([ctypes.POINTER(MpdataGrid), P, I, P, I, ctypes.POINTER(D), P], I),
+    "mpdata_compute_courants_f64": ([P] * 5 + [I] + [D] * 4 + [I] * 4 + [P], I),
+    "mpdata_compute_courants_f32": ([P] * 5 + [I] + [F] * 4 + [I] * 4 + [P], I),
+    "mpdata_velprd_driver_f64": ([ctypes.POINTER(I), ctypes.POINTER(I), I, ctypes.POINTER(D), ctypes.POINTER(D),
+                                  I, I, I, D, D] + [P] * 10 + [I] * 8 + [D] * 4 + [P, P], I),
+    "mpdata_velprd_driver_f32": ([ctypes.POINTER(I), ctypes.POINTER(I), I, ctypes.POINTER(F), ctypes.POINTER(F),
+                                  I, I, I, F, F] + [P] * 10 + [I] * 8 + [F] * 4 + [P, P], I),
     "mpdata_step_noalloc_f64": ([ctypes.POINTER(MpdataGrid), ctypes.POINTER(MpdataOpts)] + [P] * 9, I),
     "mpdata_strerror": ([I], ctypes.c_char_p),
     "mpdata_version": ([], ctypes.c_char_p),

@@ -288,6 +288,10 @@ int advec_dwarf_impl(int legacyoptmode, int t_adv, int lvertsplit, int np, int m
 
 }  // namespace
 
+namespace mpdata {
+int grid_ok(const mpdata_grid* g) { return check_grid(g); }
+}  // namespace mpdata
+
 extern "C" {
 
 int mpdata_ws_create(const mpdata_grid* grid, const mpdata_opts* opts, void** ws) {
@@ -474,6 +478,7 @@ const char* mpdata_strerror(int code) {
     case MPDATA_E_DEVICE: return "device error word set (non-finite value)";
     case MPDATA_E_UNSUPPORTED: return "reference option outside this library's scope";
     case MPDATA_E_TOO_LARGE: return "grid exceeds the 32768-cell scratch of mpdata_step_noalloc_f64";
+    case MPDATA_E_COURANT: return "Courant control failed: above the fatal limit while substepping, or not finite";
     default: return "unknown error";
   }
 }

@@ -1,6 +1,8 @@
 // Velocity predictor: velprd_traj0 (module_velprd.f90:15-89), velprdA_to_C
-// (:166-364) and the level roll of velprd_driver (velprd_driver.f90:254-270).
-// Strict IEEE, same expression order as the reference.
+// (:166-364), the level roll of velprd_driver (velprd_driver.f90:254-270),
+// and the Courant-number maxima the driver steers substepping and adaptive
+// time steps with (common/diagutils.f90:588-672).  Strict IEEE, same
+// expression order as the reference.
 #include "mpdata_common.cuh"
 #include "mpdata_stages.cuh"
 
@@ -31,7 +33,30 @@ __global__ void __launch_bounds__(128) k_pred_level(Geo g, long lev, R* ox, R* o
 
 // C-grid averaging with the open-wall extrapolation 2a(1)-a(2)
 // (module_velprd.f90:197-361), then the level roll (velprd_driver.f90:254-270).
+// The level roll of velprd_driver.f90:254-270 for cell (i,j,k): physical
+// velocities extrapolated into level 1 and copied into level 2, and the
+// level-0 momenta times h stored in level 2 for the next step.
 template <class R>
+__device__ __forceinline__ void roll_cell(long lev, R* ox, R* oy, R* oz, R* pu, R* pv, R* pw, const Arr<R>& h,
+                                          R r, int i, int j, int k) {
+  const long off = (long)(i - 1) + (long)(j - 1) * h.sy + (long)(k - 1) * h.sz;
+  const R hc = h.ld(i, j, k);
+  R* o[3] = {ox, oy, oz};
+  R* p[3] = {pu, pv, pw};
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    if (p[c]) {
+      R* q = p[c] + off;
+      const R p0 = q[0], p2 = q[2 * lev];
+      q[lev] = p0 + r * (p0 - p2);
+      q[2 * lev] = p0;
+    }
+    R* q = o[c] + off;
+    q[2 * lev] = q[0] * hc;
+  }
+}
+
+template <class R, bool ROLL>
 __global__ void __launch_bounds__(128) k_pred_cgrid(Geo g, long lev, R* ox, R* oy, R* oz, R* pu, R* pv,
                                                     R* pw, Arr<R> h, Arr<R> u1, Arr<R> u2, Arr<R> u3,
                                                     R r) {
@@ -83,43 +108,157 @@ __global__ void __launch_bounds__(128) k_pred_cgrid(Geo g, long lev, R* ox, R* o
     }
     u3.at(i, j, k) = R(0.5) * (a + b);
   }
-  if (i <= g.np && j <= g.mp && k <= g.lp) {
-    const long off = (long)(i - 1) + (long)(j - 1) * h.sy + (long)(k - 1) * h.sz;
-    const R hc = h.ld(i, j, k);
-    R* o[3] = {ox, oy, oz};
-    R* p[3] = {pu, pv, pw};
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-      if (p[c]) {
-        R* q = p[c] + off;
-        const R p0 = q[0], p2 = q[2 * lev];
-        q[lev] = p0 + r * (p0 - p2);
-        q[2 * lev] = p0;
-      }
-      R* q = o[c] + off;
-      q[2 * lev] = q[0] * hc;
-    }
-  }
+  if (ROLL && i <= g.np && j <= g.mp && k <= g.lp) roll_cell<R>(lev, ox, oy, oz, pu, pv, pw, h, r, i, j, k);
 }
 
 template <class R>
-int run_predictor(const PredPlan<R>& P, cudaStream_t s) {
+__global__ void __launch_bounds__(128) k_pred_roll(Geo g, long lev, R* ox, R* oy, R* oz, R* pu, R* pv, R* pw,
+                                                   Arr<R> h, R r) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int k = blockIdx.z + 1;
+  if (i > g.np || j > g.mp) return;
+  roll_cell<R>(lev, ox, oy, oz, pu, pv, pw, h, r, i, j, k);
+}
+
+// compute_courants (common/diagutils.f90:588-672): the maxima over the
+// interior of |a_x|+|a_y|+|a_z|, the three pair sums and the three
+// components, where a = gc*ox(level 0) (LEV2 false) or ox(level 1)/h (LEV2
+// true, as dinv=1/h then a product).  A maximum does not depend on the order
+// it is taken in, so per-thread maxima over order keys, a warp shuffle, a
+// shared-memory fold and one 64-bit atomicMax per block give exactly the
+// serial result.  keys[c] holds the unsigned order key of maximum c.
+__device__ __forceinline__ unsigned long long ukey(double x) {
+  return (unsigned long long)okey(x) ^ 0x8000000000000000ULL;
+}
+
+template <class R, bool LEV2>
+__global__ void __launch_bounds__(256) k_courants(Geo g, const R* ox, const R* oy, const R* oz, Arr<R> h, R gc1,
+                                                  R gc2, R gc3, unsigned long long* keys) {
+  unsigned long long m[7];
+#pragma unroll
+  for (int c = 0; c < 7; c++) m[c] = 0ULL;  // below the key of every number
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (i <= g.np && j <= g.mp) {
+    for (int k = blockIdx.z + 1; k <= g.lp; k += gridDim.z) {
+      const long off = (long)(i - 1) + (long)(j - 1) * h.sy + (long)(k - 1) * h.sz;
+      R a, b, c;
+      if (LEV2) {
+        const R dinv = R(1) / h.p[off];
+        a = fabs(ox[off] * dinv);
+        b = fabs(oy[off] * dinv);
+        c = fabs(oz[off] * dinv);
+      } else {
+        a = fabs(gc1 * ox[off]);
+        b = fabs(gc2 * oy[off]);
+        c = fabs(gc3 * oz[off]);
+      }
+      const R v[7] = {a + b + c, a + b, a + c, b + c, a, b, c};
+#pragma unroll
+      for (int q = 0; q < 7; q++) {
+        const unsigned long long kq = ukey((double)v[q]);
+        m[q] = kq > m[q] ? kq : m[q];
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 7; q++)
+    for (int d = 16; d > 0; d >>= 1) {
+      const unsigned long long o = __shfl_xor_sync(0xffffffffu, m[q], d);
+      m[q] = o > m[q] ? o : m[q];
+    }
+  __shared__ unsigned long long sm[8][7];
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x, warp = tid >> 5, nw = (blockDim.x * blockDim.y) >> 5;
+  if ((tid & 31) == 0)
+#pragma unroll
+    for (int q = 0; q < 7; q++) sm[warp][q] = m[q];
+  __syncthreads();
+  if (tid < 7) {
+    unsigned long long r = sm[0][tid];
+    for (int w = 1; w < nw; w++) r = sm[w][tid] > r ? sm[w][tid] : r;
+    atomicMax(keys + tid, r);
+  }
+}
+
+// wadv = 0.5*wadv over its first lp+2*ih planes, halo included
+// (FullXYZDomainWithHaloLoopDC, velprd_driver.f90:250-252)
+template <class R>
+__global__ void k_halve(R* p, long n) {
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x)
+    p[t] = R(0.5) * p[t];
+}
+
+template <class R>
+int run_pred_parts(const PredPlan<R>& P, bool level, bool cgrid, bool roll, cudaStream_t s) {
   const Geo& g = P.g;
   const dim3 blk(32, 4, 1);
   const dim3 g1((g.np + 31) / 32, (g.mp + 3) / 4, g.lp);
   const dim3 g2((g.np + 1 + 31) / 32, (g.mp + 1 + 3) / 4, g.lp + 1);
-  if (P.prof) P.prof->begin(ST_PRED_LEVEL, s);
-  k_pred_level<R><<<g1, blk, 0, s>>>(g, P.lev, P.ox, P.oy, P.oz, P.h, P.gc1, P.gc2, P.gc3, P.dt_ratio);
-  if (P.prof) P.prof->end(ST_PRED_LEVEL, s);
-  if (P.prof) P.prof->begin(ST_PRED_CGRID, s);
-  k_pred_cgrid<R><<<g2, blk, 0, s>>>(g, P.lev, P.ox, P.oy, P.oz, P.u, P.v, P.w, P.h, P.u1, P.u2, P.u3,
-                                     P.dt_ratio);
-  if (P.prof) P.prof->end(ST_PRED_CGRID, s);
-  add_launches(2);
+  int n = 0;
+  if (level) {
+    if (P.prof) P.prof->begin(ST_PRED_LEVEL, s);
+    k_pred_level<R><<<g1, blk, 0, s>>>(g, P.lev, P.ox, P.oy, P.oz, P.h, P.gc1, P.gc2, P.gc3, P.dt_ratio);
+    if (P.prof) P.prof->end(ST_PRED_LEVEL, s);
+    n++;
+  }
+  if (cgrid) {
+    if (P.prof) P.prof->begin(ST_PRED_CGRID, s);
+    if (roll)
+      k_pred_cgrid<R, true><<<g2, blk, 0, s>>>(g, P.lev, P.ox, P.oy, P.oz, P.u, P.v, P.w, P.h, P.u1, P.u2, P.u3,
+                                               P.dt_ratio);
+    else
+      k_pred_cgrid<R, false><<<g2, blk, 0, s>>>(g, P.lev, P.ox, P.oy, P.oz, P.u, P.v, P.w, P.h, P.u1, P.u2, P.u3,
+                                                P.dt_ratio);
+    if (P.prof) P.prof->end(ST_PRED_CGRID, s);
+    n++;
+  } else if (roll) {
+    k_pred_roll<R><<<g1, blk, 0, s>>>(g, P.lev, P.ox, P.oy, P.oz, P.u, P.v, P.w, P.h, P.dt_ratio);
+    n++;
+  }
+  add_launches(n);
+  return cudaGetLastError() == cudaSuccess ? 0 : -5;
+}
+
+template <class R>
+int run_predictor(const PredPlan<R>& P, cudaStream_t s) {
+  return run_pred_parts<R>(P, true, true, true, s);
+}
+
+template <class R>
+int run_courants(const PredPlan<R>& P, int level, R dxi, R dyi, R dzi, R dt, unsigned long long* keys,
+                 cudaStream_t s) {
+  const Geo& g = P.g;
+  const dim3 blk(32, 8, 1);
+  const int gx = (g.np + 31) / 32, gy = (g.mp + 7) / 8;
+  int gz = 1216 / (gx * gy);
+  gz = gz < 1 ? 1 : (gz > g.lp ? g.lp : gz);
+  const dim3 grid(gx, gy, gz);
+  if (level == 2)
+    k_courants<R, true><<<grid, blk, 0, s>>>(g, P.ox + P.lev, P.oy + P.lev, P.oz + P.lev, P.h, R(0), R(0), R(0),
+                                             keys);
+  else  // diagutils.f90:624-626
+    k_courants<R, false><<<grid, blk, 0, s>>>(g, P.ox, P.oy, P.oz, P.h, dt * dxi, dt * dyi, dt * dzi, keys);
+  add_launches(1);
+  return cudaGetLastError() == cudaSuccess ? 0 : -5;
+}
+
+template <class R>
+int run_halve(R* p, long n, cudaStream_t s) {
+  k_halve<R><<<1216, 256, 0, s>>>(p, n);
+  add_launches(1);
   return cudaGetLastError() == cudaSuccess ? 0 : -5;
 }
 
 template int run_predictor<double>(const PredPlan<double>&, cudaStream_t);
 template int run_predictor<float>(const PredPlan<float>&, cudaStream_t);
+template int run_pred_parts<double>(const PredPlan<double>&, bool, bool, bool, cudaStream_t);
+template int run_pred_parts<float>(const PredPlan<float>&, bool, bool, bool, cudaStream_t);
+template int run_courants<double>(const PredPlan<double>&, int, double, double, double, double,
+                                  unsigned long long*, cudaStream_t);
+template int run_courants<float>(const PredPlan<float>&, int, float, float, float, float, unsigned long long*,
+                                 cudaStream_t);
+template int run_halve<double>(double*, long, cudaStream_t);
+template int run_halve<float>(float*, long, cudaStream_t);
 
 }  // namespace mpdata

@@ -55,6 +55,19 @@ struct PredPlan {
 
 template <class R>
 int run_predictor(const PredPlan<R>& plan, cudaStream_t stream);
+// The pieces separately: level = the n+1/2 momenta into level 1
+// (velprd_traj0_adapt_dt), cgrid = velprdA_to_C of level 1, roll = the
+// driver's level roll; roll without cgrid runs the roll alone.
+template <class R>
+int run_pred_parts(const PredPlan<R>& plan, bool level, bool cgrid, bool roll, cudaStream_t stream);
+// compute_courants of momentum level 1 (gc*ox at level 0) or 2 (ox at level 1
+// over h): folds the seven maxima into keys[0..6] (unsigned order keys of
+// doubles, atomicMax), which the caller initialises.
+template <class R>
+int run_courants(const PredPlan<R>& plan, int level, R dxi, R dyi, R dzi, R dt, unsigned long long* keys,
+                 cudaStream_t stream);
+template <class R>
+int run_halve(R* p, long n, cudaStream_t stream);
 
 // Adjoint scratch of one problem (mpdata_adjoint.cu).
 template <class R>

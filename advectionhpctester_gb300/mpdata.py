@@ -352,6 +352,53 @@ def advec_dwarf(legacyoptmode, t_adv, lupdatemulti, lvertsplit, np_, mp, lp, ih,
              _stream(stream)), "advec_dwarf")
 
 
+def compute_courants(ntimelevel, ox, oy, oz, h, dxi, dyi, dzi, dt, np_, mp, lp, ih, stream=None):
+    """compute_courants (common/diagutils.f90:588-672) on CUDA level stacks
+    ox/oy/oz (..., 3): returns (cr3d, crxy, crxz, cryz, crx, cry, crz)."""
+    _require_torch()
+    import ctypes
+    lib = _native.load()
+    d = ox.dtype
+    s = shapes(np_, mp, lp, ih)
+    lev = s["psi"] + (3,)
+    ct = ctypes.c_double if d == torch.float64 else ctypes.c_float
+    cr = (ct * 7)()
+    fn = lib.mpdata_compute_courants_f64 if d == torch.float64 else lib.mpdata_compute_courants_f32
+    check(fn(ctypes.cast(cr, ctypes.c_void_p), _ptr(ox, d, lev, "ox"), _ptr(oy, d, lev, "oy"),
+             _ptr(oz, d, lev, "oz"), _ptr(h, d, s["psi"], "h"), int(ntimelevel), dxi, dyi, dzi, dt,
+             np_, mp, lp, ih, _stream(stream)), "mpdata_compute_courants")
+    return tuple(float(c) for c in cr)
+
+
+def velprd_driver(state, ox, oy, oz, u, v, w, uadv, vadv, wadv, h, ipoles, ibcx, ibcy, ibcz, np_, mp, lp, ih,
+                  dxi, dyi, dzi, dt, stream=None):
+    """velprd_driver (advection/src_algorithms/velprd_driver.f90:16-270) on
+    CUDA tensors.  state is a dict with the reference's scalars: nsubsteps,
+    nsubsteps_o, dtn, dtnold (INOUT, updated in place), lsubstepping,
+    ltimeadapt, lvertsplit, lcrdiag_nphlf, crmaxlim, dtmax.  Returns the last
+    (cr3d, crxy, crxz, cryz, crx, cry, crz, cr_for_dt, dt_ratio)."""
+    _require_torch()
+    import ctypes
+    lib = _native.load()
+    d = ox.dtype
+    s = shapes(np_, mp, lp, ih)
+    lev = s["psi"] + (3,)
+    R = ctypes.c_double if d == torch.float64 else ctypes.c_float
+    ns, nso = ctypes.c_int(state["nsubsteps"]), ctypes.c_int(state["nsubsteps_o"])
+    dtn, dtnold = R(state["dtn"]), R(state["dtnold"])
+    diag = (ctypes.c_double * 9)()
+    fn = lib.mpdata_velprd_driver_f64 if d == torch.float64 else lib.mpdata_velprd_driver_f32
+    check(fn(ctypes.byref(ns), ctypes.byref(nso), int(state["lsubstepping"]), ctypes.byref(dtn),
+             ctypes.byref(dtnold), int(state["ltimeadapt"]), int(state["lvertsplit"]), int(state["lcrdiag_nphlf"]),
+             state["crmaxlim"], state["dtmax"], _ptr(ox, d, lev, "ox"), _ptr(oy, d, lev, "oy"),
+             _ptr(oz, d, lev, "oz"), _ptr(u, d, lev, "u"), _ptr(v, d, lev, "v"), _ptr(w, d, lev, "w"),
+             _ptr(uadv, d, s["u1"], "uadv"), _ptr(vadv, d, s["u2"], "vadv"), _ptr(wadv, d, s["u3"], "wadv"),
+             _ptr(h, d, s["psi"], "h"), ipoles, ibcx, ibcy, ibcz, np_, mp, lp, ih, dxi, dyi, dzi, dt,
+             ctypes.cast(diag, ctypes.c_void_p), _stream(stream)), "mpdata_velprd_driver")
+    state.update(nsubsteps=ns.value, nsubsteps_o=nso.value, dtn=dtn.value, dtnold=dtnold.value)
+    return tuple(diag)
+
+
 def mass(psi, h, rhr=None, ibc=(1, 1, 1), ih=1, stream=None):
     """FP64 Neumaier-compensated sum(h*psi[/rhr]) over the interior."""
     import ctypes

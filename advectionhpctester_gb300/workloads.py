@@ -268,3 +268,30 @@ def random_fields(np_, mp, lp, ih=1, ibc=(0, 0, 0), seed=0, courant=0.3, dtype=n
     f.bcx[...] = rng.uniform(0.5, 1.5, f.bcx.shape)
     f.bcy[...] = rng.uniform(0.5, 1.5, f.bcy.shape)
     return f.astype(dtype) if dtype != np.float64 else f
+
+
+def predictor_case(np_, mp, lp, ih=1, courant=2.0, seed=0, dtype=np.float64):
+    """Seeded inputs of the predictor and its Courant control: momentum
+    stacks ox/oy/oz and physical velocities u/v/w (psi-shaped x 3 levels,
+    Fortran order), h in [0.8,1.2], dx = dy = dz = 1 and dt = 1, with level 0
+    scaled so that the level-1 Courant maximum |ox|+|oy|+|oz| is about
+    `courant`; level 2 (n-1 momenta) is level 0 times h plus 10% noise."""
+    rng = np.random.default_rng(seed)
+    s = (np_ + 2 * ih, mp + 2 * ih, lp + 2 * ih, 3)
+    h = np.asfortranarray(rng.uniform(0.8, 1.2, s[:3]))
+    st = {}
+    for name in ("ox", "oy", "oz"):
+        a = np.zeros(s, order="F")
+        a[..., 0] = rng.uniform(-1.0, 1.0, s[:3]) * (courant / 3.0)
+        a[..., 2] = a[..., 0] * h * (1.0 + 0.1 * rng.uniform(-1.0, 1.0, s[:3]))
+        st[name] = a
+    for name in ("u", "v", "w"):
+        st[name] = np.asfortranarray(rng.uniform(-1.0, 1.0, s))
+    st["h"] = h
+    shp = shapes(np_, mp, lp, ih)
+    st["uadv"] = np.zeros(shp["u1"], order="F")
+    st["vadv"] = np.zeros(shp["u2"], order="F")
+    st["wadv"] = np.asfortranarray(rng.uniform(-1.0, 1.0, shp["u3"]))  # lvertsplit halves it
+    if dtype != np.float64:
+        st = {k: np.asfortranarray(v.astype(dtype)) for k, v in st.items()}
+    return st

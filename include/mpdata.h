@@ -42,6 +42,7 @@ extern "C" {
 #define MPDATA_E_DEVICE -6      /* the device error word is set (non-finite result) */
 #define MPDATA_E_UNSUPPORTED -7 /* a reference option outside this library's scope */
 #define MPDATA_E_TOO_LARGE -8   /* grid larger than the fixed scratch of mpdata_step_noalloc_f64 */
+#define MPDATA_E_COURANT -9     /* Courant control failed (above the fatal limit, or not finite) */
 
 typedef struct {
   int np, mp, lp, ih;   /* interior cells per axis and halo width (ih >= 1) */
@@ -250,6 +251,44 @@ int mpdata_mass_f32(const mpdata_grid* grid, const float* psi, const float* h, c
  * out[0] = max|a-b|, out[1] = ||a-b||_2, out[2] = max|b|, out[3] = ||b||_2. */
 int mpdata_error_norms(const mpdata_grid* grid, const void* a, int a_is_f64, const void* b,
                        int b_is_f64, double* out, void* stream);
+
+/* ---- Courant control of the predictor ------------------------------------
+ * compute_courants (common/diagutils.f90:588-672): cr[0..6] = the maxima over
+ * the interior of cr3d, crxy, crxz, cryz, crx, cry, crz.  ntimelevel 1 uses
+ * |dt*dxi*ox(level 0)| (and y, z alike), 2 uses |ox(level 1)/h|.  ox/oy/oz are
+ * the three-level momentum stacks (1-ih:np+ih, 1-ih:mp+ih, 1-ih:lp+ih, 0:2),
+ * h psi-shaped.  Synchronises the stream (the reference's globmax does too).
+ * ntimelevel other than 1 or 2: MPDATA_E_OPTS (the reference STOPs). */
+int mpdata_compute_courants_f64(double* cr, const double* ox, const double* oy, const double* oz,
+                                const double* h, int ntimelevel, double dxi, double dyi, double dzi,
+                                double dt, int np, int mp, int lp, int ih, void* stream);
+int mpdata_compute_courants_f32(float* cr, const float* ox, const float* oy, const float* oz,
+                                const float* h, int ntimelevel, float dxi, float dyi, float dzi,
+                                float dt, int np, int mp, int lp, int ih, void* stream);
+/* velprd_driver (advection/src_algorithms/velprd_driver.f90:16-270), same
+ * argument order: the predictor with substepping (lsubstepping) or an
+ * adaptive time step (ltimeadapt), Courant diagnosed at n (lcrdiag_nphlf=0)
+ * or n+1/2, the split-scheme Courant rule and wadv halving (lvertsplit), then
+ * the level roll.  nsubsteps, nsubsteps_o, dtn and dtnold are INOUT host
+ * scalars; u/v/w (physical velocity stacks) may be NULL.  diag, when not NULL,
+ * receives the last cr3d, crxy, crxz, cryz, crx, cry, crz, cr_for_dt and
+ * dt_ratio.  Synchronises the stream once per Courant evaluation.  Both
+ * lsubstepping and ltimeadapt: MPDATA_E_OPTS; Courant above 10 per substep
+ * while substepping, or a non-finite Courant number: MPDATA_E_COURANT. */
+int mpdata_velprd_driver_f64(int* nsubsteps, int* nsubsteps_o, int lsubstepping, double* dtn,
+                             double* dtnold, int ltimeadapt, int lvertsplit, int lcrdiag_nphlf,
+                             double crmaxlim, double dtmax, double* ox, double* oy, double* oz,
+                             double* u, double* v, double* w, double* uadv, double* vadv,
+                             double* wadv, const double* h, int ipoles, int ibcx, int ibcy, int ibcz,
+                             int np, int mp, int lp, int ih, double dxi, double dyi, double dzi,
+                             double dt, double* diag, void* stream);
+int mpdata_velprd_driver_f32(int* nsubsteps, int* nsubsteps_o, int lsubstepping, float* dtn,
+                             float* dtnold, int ltimeadapt, int lvertsplit, int lcrdiag_nphlf,
+                             float crmaxlim, float dtmax, float* ox, float* oy, float* oz, float* u,
+                             float* v, float* w, float* uadv, float* vadv, float* wadv,
+                             const float* h, int ipoles, int ibcx, int ibcy, int ibcz, int np, int mp,
+                             int lp, int ih, float dxi, float dyi, float dzi, float dt, double* diag,
+                             void* stream);
 
 /* ---- a step that allocates nothing ----------------------------------------
  * No counterpart in the reference.  For callers that must not have the

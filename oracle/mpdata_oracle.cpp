@@ -5,6 +5,7 @@
 #include "mpdata_oracle.h"
 
 #include <cmath>
+#include <limits>
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -667,34 +668,59 @@ int advec(const orc_grid* g, int opt, int t_adv, int iord, int nonos, R* x, cons
   return 0;
 }
 
-// ---- velprd_traj0 + velprdA_to_C + driver shift ----
+// ---- velprd_traj0, velprdA_to_C, the driver's level roll ----
+// Three-level momentum stacks ox/oy/oz (level stride lev), psi-shaped levels.
 template <class R>
-int velprd(const orc_grid* g, R* ox, R* oy, R* oz, R* u, R* v, R* w, const R* h_in, R dxi, R dyi,
-           R dzi, R dt, R dt_ratio, R* u1o, R* u2o, R* u3o) {
-  if (!dims_ok(g)) return -1;
-  if (!ox || !oy || !oz || !h_in || !u1o || !u2o || !u3o) return -3;
-  const Dims d{g->np, g->mp, g->lp, g->ih, g->ibcx, g->ibcy, g->ibcz};
-  const int ih = d.ih, SX = d.np + 2 * ih, SY = d.mp + 2 * ih, SZ = d.lp + 2 * ih;
-  const long lev = (long)SX * SY * SZ;
-  V3<R> H = view<R>(const_cast<R*>(h_in), ih, SX, SY);
-  R* o[3] = {ox, oy, oz};
+struct Pred {
+  Dims d;
+  int SX, SY;
+  long lev;
+  R* o[3];
+  R* phys[3];
+  V3<R> H;
+};
+
+template <class R>
+Pred<R> pred_of(const Dims& d, R* ox, R* oy, R* oz, R* u, R* v, R* w, const R* h_in) {
+  Pred<R> p;
+  p.d = d;
+  p.SX = d.np + 2 * d.ih;
+  p.SY = d.mp + 2 * d.ih;
+  p.lev = (long)p.SX * p.SY * (d.lp + 2 * d.ih);
+  p.o[0] = ox; p.o[1] = oy; p.o[2] = oz;
+  p.phys[0] = u; p.phys[1] = v; p.phys[2] = w;
+  p.H = view<R>(const_cast<R*>(h_in), d.ih, p.SX, p.SY);
+  return p;
+}
+
+// velprd_traj0 / velprd_traj0_adapt_dt (module_velprd.f90:60-83, :133-156):
+// n+1/2 momenta times dt/dx into level 1
+template <class R>
+void pred_level(const Pred<R>& p, R dt, R dxi, R dyi, R dzi, R dt_ratio) {
+  const Dims& d = p.d;
   const R gc[3] = {dt * dxi, dt * dyi, dt * dzi};  // module_velprd.f90:52-54
-  // module_velprd.f90:60-83 — n+1/2 momenta into level 1
   for (int c = 0; c < 3; c++) {
-    V3<R> O0 = view<R>(o[c], ih, SX, SY), O1 = view<R>(o[c] + lev, ih, SX, SY),
-          O2 = view<R>(o[c] + 2 * lev, ih, SX, SY);
+    V3<R> O0 = view<R>(p.o[c], d.ih, p.SX, p.SY), O1 = view<R>(p.o[c] + p.lev, d.ih, p.SX, p.SY),
+          O2 = view<R>(p.o[c] + 2 * p.lev, d.ih, p.SX, p.SY);
 #pragma omp parallel for num_threads(g_threads) schedule(static)
     for (int k = 1; k <= d.lp; k++)
       for (int j = 1; j <= d.mp; j++)
         for (int i = 1; i <= d.np; i++) {
-          const R a0 = O0(i, j, k) * H(i, j, k);
+          const R a0 = O0(i, j, k) * p.H(i, j, k);
           const R a2 = O2(i, j, k);
           const R a1 = a0 + dt_ratio * (a0 - a2);
           O1(i, j, k) = R(0.5) * (a1 + a0) * gc[c];
         }
   }
-  // velprdA_to_C (:197-361): halo extrapolation on open walls, then averaging
-  V3<R> A1 = view<R>(ox + lev, ih, SX, SY), A2 = view<R>(oy + lev, ih, SX, SY), A3 = view<R>(oz + lev, ih, SX, SY);
+}
+
+// velprdA_to_C (:197-361) of level 1: halo extrapolation on open walls, then averaging
+template <class R>
+void pred_a_to_c(const Pred<R>& p, R* u1o, R* u2o, R* u3o) {
+  const Dims& d = p.d;
+  const int SX = p.SX, SY = p.SY, ih = d.ih;
+  V3<R> A1 = view<R>(p.o[0] + p.lev, ih, SX, SY), A2 = view<R>(p.o[1] + p.lev, ih, SX, SY),
+        A3 = view<R>(p.o[2] + p.lev, ih, SX, SY);
   if (!d.bx)
     for (int k = 1; k <= d.lp; k++)
       for (int j = 1; j <= d.mp; j++) {
@@ -734,25 +760,188 @@ int velprd(const orc_grid* g, R* ox, R* oy, R* oz, R* u, R* v, R* w, const R* h_
           U3(i, j, k) = R(0.5) * (A3(i, j, kk) + A3(i, j, wz(kk - 1)));
         }
       }
-  // velprd_driver.f90:254-270 — roll levels, store n momenta for the next step
-  R* phys[3] = {u, v, w};
+}
+
+// velprd_driver.f90:254-270 — roll levels, store n momenta for the next step
+template <class R>
+void pred_roll(const Pred<R>& p, R dt_ratio) {
+  const Dims& d = p.d;
+  const int SX = p.SX, SY = p.SY, ih = d.ih;
   for (int c = 0; c < 3; c++) {
-    V3<R> O0 = view<R>(o[c], ih, SX, SY), O2 = view<R>(o[c] + 2 * lev, ih, SX, SY);
+    V3<R> O0 = view<R>(p.o[c], ih, SX, SY), O2 = view<R>(p.o[c] + 2 * p.lev, ih, SX, SY);
     V3<R> P0{nullptr, 0, 0, 0}, P1{nullptr, 0, 0, 0}, P2{nullptr, 0, 0, 0};
-    if (phys[c]) {
-      P0 = view<R>(phys[c], ih, SX, SY); P1 = view<R>(phys[c] + lev, ih, SX, SY);
-      P2 = view<R>(phys[c] + 2 * lev, ih, SX, SY);
+    R* ph = p.phys[c];
+    if (ph) {
+      P0 = view<R>(ph, ih, SX, SY);
+      P1 = view<R>(ph + p.lev, ih, SX, SY);
+      P2 = view<R>(ph + 2 * p.lev, ih, SX, SY);
     }
 #pragma omp parallel for num_threads(g_threads) schedule(static)
     for (int k = 1; k <= d.lp; k++)
       for (int j = 1; j <= d.mp; j++)
         for (int i = 1; i <= d.np; i++) {
-          if (phys[c]) {
+          if (ph) {
             P1(i, j, k) = P0(i, j, k) + dt_ratio * (P0(i, j, k) - P2(i, j, k));
             P2(i, j, k) = P0(i, j, k);
           }
-          O2(i, j, k) = O0(i, j, k) * H(i, j, k);
+          O2(i, j, k) = O0(i, j, k) * p.H(i, j, k);
         }
+  }
+}
+
+// velprd_traj0 + velprdA_to_C + the driver's level roll, as the driver's
+// plain path runs them (velprd_driver.f90:236-270)
+template <class R>
+int velprd(const orc_grid* g, R* ox, R* oy, R* oz, R* u, R* v, R* w, const R* h_in, R dxi, R dyi,
+           R dzi, R dt, R dt_ratio, R* u1o, R* u2o, R* u3o) {
+  if (!dims_ok(g)) return -1;
+  if (!ox || !oy || !oz || !h_in || !u1o || !u2o || !u3o) return -3;
+  const Dims d{g->np, g->mp, g->lp, g->ih, g->ibcx, g->ibcy, g->ibcz};
+  const Pred<R> p = pred_of<R>(d, ox, oy, oz, u, v, w, h_in);
+  pred_level<R>(p, dt, dxi, dyi, dzi, dt_ratio);
+  pred_a_to_c<R>(p, u1o, u2o, u3o);
+  pred_roll<R>(p, dt_ratio);
+  return 0;
+}
+
+// compute_courants (common/diagutils.f90:606-654): serial maxima over the
+// interior, starting from -HUGE
+template <class R>
+void courants(const Pred<R>& p, int level, R dxi, R dyi, R dzi, R dt, R cr[7]) {
+  const Dims& d = p.d;
+  for (int c = 0; c < 7; c++) cr[c] = -std::numeric_limits<R>::max();
+  const int lv = level == 2 ? 1 : 0;
+  V3<R> X = view<R>(p.o[0] + lv * p.lev, d.ih, p.SX, p.SY), Y = view<R>(p.o[1] + lv * p.lev, d.ih, p.SX, p.SY),
+        Z = view<R>(p.o[2] + lv * p.lev, d.ih, p.SX, p.SY);
+  const R gc1 = dt * dxi, gc2 = dt * dyi, gc3 = dt * dzi;
+  auto mx = [](R a, R b) { return a > b ? a : b; };
+  for (int k = 1; k <= d.lp; k++)
+    for (int j = 1; j <= d.mp; j++)
+      for (int i = 1; i <= d.np; i++) {
+        R a, b, c;
+        if (level == 2) {
+          const R dinv = R(1) / p.H(i, j, k);
+          a = std::fabs(X(i, j, k) * dinv);
+          b = std::fabs(Y(i, j, k) * dinv);
+          c = std::fabs(Z(i, j, k) * dinv);
+        } else {
+          a = std::fabs(gc1 * X(i, j, k));
+          b = std::fabs(gc2 * Y(i, j, k));
+          c = std::fabs(gc3 * Z(i, j, k));
+        }
+        cr[0] = mx(cr[0], a + b + c);
+        cr[1] = mx(cr[1], a + b);
+        cr[2] = mx(cr[2], a + c);
+        cr[3] = mx(cr[3], b + c);
+        cr[4] = mx(cr[4], a);
+        cr[5] = mx(cr[5], b);
+        cr[6] = mx(cr[6], c);
+      }
+}
+
+// velprd_driver (velprd_driver.f90:16-270), scalars in R.  Returns 0, -2
+// (substepping with adaptivity, the STOP at :74), -9 (the STOP at :123, or a
+// non-finite Courant number that would loop forever).
+template <class R>
+int velprd_driver(const orc_grid* g, int* nsubsteps, int* nsubsteps_o, int lsubstepping, R* dtn, R* dtnold,
+                  int ltimeadapt, int lvertsplit, int lcrdiag_nphlf, R crmaxlim, R dtmax, R* ox, R* oy, R* oz,
+                  R* u, R* v, R* w, R* uadv, R* vadv, R* wadv, const R* h, R dxi, R dyi, R dzi, R dt,
+                  double* diag) {
+  if (!dims_ok(g)) return -1;
+  if (!nsubsteps || !nsubsteps_o || !dtn || !dtnold || !ox || !oy || !oz || !uadv || !vadv || !wadv || !h)
+    return -3;
+  if (lsubstepping && ltimeadapt) return -2;
+  const Dims d{g->np, g->mp, g->lp, g->ih, g->ibcx, g->ibcy, g->ibcz};
+  const Pred<R> p = pred_of<R>(d, ox, oy, oz, u, v, w, h);
+  const R TINYR = std::numeric_limits<R>::min();
+  R cr[7];
+  auto split = [&]() { return (cr[1] > R(0.5) * cr[6] ? cr[1] : R(0.5) * cr[6]) + TINYR; };
+  auto traj0 = [&](R dtx, R r) {
+    pred_level<R>(p, dtx, dxi, dyi, dzi, r);
+    pred_a_to_c<R>(p, uadv, vadv, wadv);
+  };
+  R dt_ratio = R(1);
+  R dtntemp = *dtn;
+  if (lsubstepping && *nsubsteps == 1) dt_ratio = (dt / (R(0.0f) * *nsubsteps + R(1))) / (dt / *nsubsteps_o);
+  if (lsubstepping) dtntemp = dt;
+  if (ltimeadapt) dtntemp = *dtn;
+  if (lcrdiag_nphlf) {
+    pred_level<R>(p, dtntemp, dxi, dyi, dzi, dt_ratio);  // velprd_traj0_adapt_dt
+    courants<R>(p, 2, dxi, dyi, dzi, dtntemp, cr);
+  } else {
+    courants<R>(p, 1, dxi, dyi, dzi, dtntemp, cr);
+  }
+  R cr_for_dt = cr[0];
+  if (lvertsplit) cr_for_dt = split();
+  if (lsubstepping) {
+    bool ok = true;
+    if (cr_for_dt > crmaxlim && *nsubsteps == 1) {
+      *nsubsteps = (int)std::ceil(cr_for_dt);
+      if (cr_for_dt / *nsubsteps > crmaxlim) *nsubsteps += 1;
+      ok = false;
+    } else if (cr_for_dt / *nsubsteps > R(10) && *nsubsteps > 1) {
+      return -9;
+    }
+    *dtn = dt / *nsubsteps;
+    if (lvertsplit) {
+      dt_ratio = *dtn / *dtnold;
+      traj0(*dtn, dt_ratio);
+      courants<R>(p, 2, dxi, dyi, dzi, *dtn, cr);
+      cr_for_dt = cr[0];
+    }
+    for (int round = 0; !ok; round++) {
+      if (round >= 10000 || !(cr_for_dt == cr_for_dt)) return -9;
+      dt_ratio = *dtn / *dtnold;
+      traj0(*dtn, dt_ratio);
+      courants<R>(p, 2, dxi, dyi, dzi, *dtn, cr);
+      cr_for_dt = cr[0];
+      if (lvertsplit) cr_for_dt = split();
+      if (cr_for_dt <= crmaxlim) {
+        ok = true;
+      } else {
+        *nsubsteps += 1;
+        *dtn = dt / *nsubsteps;
+      }
+    }
+    *nsubsteps_o = *nsubsteps;
+    *dtnold = *dtn;
+    *dtn = dt / *nsubsteps;
+    if (*nsubsteps > 1 || !lcrdiag_nphlf)
+      traj0(*dtn, dt_ratio);
+    else
+      pred_a_to_c<R>(p, uadv, vadv, wadv);
+  } else if (ltimeadapt) {
+    R crmaxlimtemp = crmaxlim;
+    *dtnold = *dtn;
+    for (int round = 0;; round++) {
+      if (round >= 10000 || !(cr_for_dt == cr_for_dt)) return -9;
+      R t = (crmaxlimtemp / (std::fabs(cr_for_dt) + TINYR)) * *dtn;
+      t = t < dtmax ? t : dtmax;
+      if (t > *dtnold && ((t - *dtnold) / *dtnold) > R(0.1f)) *dtn = t;
+      if (t <= *dtnold) *dtn = t;
+      dt_ratio = *dtn / *dtnold;
+      traj0(*dtn, dt_ratio);
+      courants<R>(p, 2, dxi, dyi, dzi, *dtn, cr);
+      cr_for_dt = cr[0];
+      if (lvertsplit) cr_for_dt = split();
+      if (cr_for_dt <= crmaxlim) break;
+      crmaxlimtemp = R(0.99f) * crmaxlimtemp;
+    }
+  } else {
+    if (!lcrdiag_nphlf)
+      traj0(*dtn, dt_ratio);
+    else
+      pred_a_to_c<R>(p, uadv, vadv, wadv);
+  }
+  if (lvertsplit) {  // FullXYZDomainWithHaloLoopDC: k = 1-ih .. lp+ih, halo included
+    const long n = (long)p.SX * p.SY * (d.lp + 2 * d.ih);
+    for (long t = 0; t < n; t++) wadv[t] = R(0.5f) * wadv[t];
+  }
+  pred_roll<R>(p, dt_ratio);
+  if (diag) {
+    for (int c = 0; c < 7; c++) diag[c] = (double)cr[c];
+    diag[7] = (double)cr_for_dt;
+    diag[8] = (double)dt_ratio;
   }
   return 0;
 }
@@ -1076,6 +1265,41 @@ int orc_velprd_f32(const orc_grid* g, float* ox, float* oy, float* oz, float* u,
                    float* w, const float* h, float dxi, float dyi, float dzi, float dt,
                    float dt_ratio, float* u1, float* u2, float* u3) {
   return velprd<float>(g, ox, oy, oz, u, v, w, h, dxi, dyi, dzi, dt, dt_ratio, u1, u2, u3);
+}
+
+int orc_compute_courants_f64(const orc_grid* g, int ntimelevel, double* ox, double* oy, double* oz, const double* h,
+                             double dxi, double dyi, double dzi, double dt, double* cr) {
+  if (!dims_ok(g)) return -1;
+  if (ntimelevel != 1 && ntimelevel != 2) return -2;
+  const Dims d{g->np, g->mp, g->lp, g->ih, g->ibcx, g->ibcy, g->ibcz};
+  courants<double>(pred_of<double>(d, ox, oy, oz, nullptr, nullptr, nullptr, h), ntimelevel, dxi, dyi, dzi, dt, cr);
+  return 0;
+}
+int orc_compute_courants_f32(const orc_grid* g, int ntimelevel, float* ox, float* oy, float* oz, const float* h,
+                             float dxi, float dyi, float dzi, float dt, float* cr) {
+  if (!dims_ok(g)) return -1;
+  if (ntimelevel != 1 && ntimelevel != 2) return -2;
+  const Dims d{g->np, g->mp, g->lp, g->ih, g->ibcx, g->ibcy, g->ibcz};
+  courants<float>(pred_of<float>(d, ox, oy, oz, nullptr, nullptr, nullptr, h), ntimelevel, dxi, dyi, dzi, dt, cr);
+  return 0;
+}
+int orc_velprd_driver_f64(const orc_grid* g, int* nsubsteps, int* nsubsteps_o, int lsubstepping, double* dtn,
+                          double* dtnold, int ltimeadapt, int lvertsplit, int lcrdiag_nphlf, double crmaxlim,
+                          double dtmax, double* ox, double* oy, double* oz, double* u, double* v, double* w,
+                          double* uadv, double* vadv, double* wadv, const double* h, double dxi, double dyi,
+                          double dzi, double dt, double* diag) {
+  return velprd_driver<double>(g, nsubsteps, nsubsteps_o, lsubstepping, dtn, dtnold, ltimeadapt, lvertsplit,
+                               lcrdiag_nphlf, crmaxlim, dtmax, ox, oy, oz, u, v, w, uadv, vadv, wadv, h, dxi,
+                               dyi, dzi, dt, diag);
+}
+int orc_velprd_driver_f32(const orc_grid* g, int* nsubsteps, int* nsubsteps_o, int lsubstepping, float* dtn,
+                          float* dtnold, int ltimeadapt, int lvertsplit, int lcrdiag_nphlf, float crmaxlim,
+                          float dtmax, float* ox, float* oy, float* oz, float* u, float* v, float* w,
+                          float* uadv, float* vadv, float* wadv, const float* h, float dxi, float dyi, float dzi,
+                          float dt, double* diag) {
+  return velprd_driver<float>(g, nsubsteps, nsubsteps_o, lsubstepping, dtn, dtnold, ltimeadapt, lvertsplit,
+                              lcrdiag_nphlf, crmaxlim, dtmax, ox, oy, oz, u, v, w, uadv, vadv, wadv, h, dxi, dyi,
+                              dzi, dt, diag);
 }
 
 // velprdA_to_C_ver2 (module_velprd.f90:366-520): the C-grid averaging of given

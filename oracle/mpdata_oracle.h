@@ -11,6 +11,8 @@
  *   halo/BC helpers   advection/src_algorithms/mpdataoperators.inc:253-287,479-584,673-947,1034-1086
  *   predictor         advection/src_algorithms/module_velprd.f90:15-89,166-520
  *   state shift       advection/src_algorithms/velprd_driver.f90:254-270
+ *   Courant control   advection/src_algorithms/velprd_driver.f90:16-252,
+ *                     common/diagutils.f90:588-672
  *   dispatcher        advection/src_drivers/advec.f90:116-244
  *
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it,
@@ -84,6 +86,28 @@ int orc_velprd_f64(const orc_grid* g, double* ox, double* oy, double* oz, double
 int orc_velprd_f32(const orc_grid* g, float* ox, float* oy, float* oz, float* u, float* v,
                    float* w, const float* h, float dxi, float dyi, float dzi, float dt,
                    float dt_ratio, float* u1, float* u2, float* u3);
+
+/* compute_courants (common/diagutils.f90:588-672): cr[0..6] = cr3d, crxy, crxz,
+ * cryz, crx, cry, crz.  ntimelevel 1: |dt*dxi*ox(level 0)|; 2: |ox(level 1)/h|. */
+int orc_compute_courants_f64(const orc_grid* g, int ntimelevel, double* ox, double* oy, double* oz,
+                             const double* h, double dxi, double dyi, double dzi, double dt, double* cr);
+int orc_compute_courants_f32(const orc_grid* g, int ntimelevel, float* ox, float* oy, float* oz,
+                             const float* h, float dxi, float dyi, float dzi, float dt, float* cr);
+/* velprd_driver (advection/src_algorithms/velprd_driver.f90:16-270): Courant
+ * control (substepping, adaptive dt, n or n+1/2 diagnosis, split rule), the
+ * predictor and the level roll.  diag (9 doubles, may be NULL): the last seven
+ * Courant maxima, cr_for_dt, dt_ratio.  Returns 0, -2 (both substepping and
+ * adaptivity), -9 (Courant above 10 per substep, or not finite). */
+int orc_velprd_driver_f64(const orc_grid* g, int* nsubsteps, int* nsubsteps_o, int lsubstepping,
+                          double* dtn, double* dtnold, int ltimeadapt, int lvertsplit, int lcrdiag_nphlf,
+                          double crmaxlim, double dtmax, double* ox, double* oy, double* oz, double* u,
+                          double* v, double* w, double* uadv, double* vadv, double* wadv, const double* h,
+                          double dxi, double dyi, double dzi, double dt, double* diag);
+int orc_velprd_driver_f32(const orc_grid* g, int* nsubsteps, int* nsubsteps_o, int lsubstepping,
+                          float* dtn, float* dtnold, int ltimeadapt, int lvertsplit, int lcrdiag_nphlf,
+                          float crmaxlim, float dtmax, float* ox, float* oy, float* oz, float* u, float* v,
+                          float* w, float* uadv, float* vadv, float* wadv, const float* h, float dxi,
+                          float dyi, float dzi, float dt, double* diag);
 
 /* velprdA_to_C_ver2 (module_velprd.f90:366-520): A-grid Courant numbers (psi
  * shaped, halos overwritten by the one-sided extrapolation) -> C grid. */

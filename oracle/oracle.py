@@ -56,6 +56,14 @@ def lib():
         _lib.orc_tangent_adjoint_f64.restype = I
         _lib.orc_a_to_c_f64.argtypes = [ctypes.POINTER(OrcGrid)] + [P] * 6
         _lib.orc_a_to_c_f64.restype = I
+        for name, R in (("f64", D), ("f32", F)):
+            f = getattr(_lib, "orc_compute_courants_" + name)
+            f.argtypes = [ctypes.POINTER(OrcGrid), I] + [P] * 4 + [R] * 4 + [P]
+            f.restype = I
+            f = getattr(_lib, "orc_velprd_driver_" + name)
+            f.argtypes = ([ctypes.POINTER(OrcGrid), ctypes.POINTER(I), ctypes.POINTER(I), I, ctypes.POINTER(R),
+                           ctypes.POINTER(R), I, I, I, R, R] + [P] * 10 + [R] * 4 + [P])
+            f.restype = I
         _lib.orc_set_threads.argtypes = [I]
         _lib.orc_get_threads.restype = I
     return _lib
@@ -107,6 +115,39 @@ def velprd(g, ox, oy, oz, h, dxi, dyi, dzi, dt, dt_ratio, u1, u2, u3, u=None, v=
                             _ptr(u1, d), _ptr(u2, d), _ptr(u3, d))
     if rc != 0:
         raise ValueError("oracle velprd failed with code %d" % rc)
+
+
+def compute_courants(g, ntimelevel, ox, oy, oz, h, dxi, dyi, dzi, dt):
+    """compute_courants of level stacks ox/oy/oz (..., 3): the seven maxima
+    (cr3d, crxy, crxz, cryz, crx, cry, crz) as an array of the field dtype."""
+    d = ox.dtype
+    sfx = {np.float64: "f64", np.float32: "f32"}[d.type]
+    cr = np.zeros(7, dtype=d)
+    rc = getattr(lib(), "orc_compute_courants_" + sfx)(ctypes.byref(g), int(ntimelevel), _ptr(ox, d), _ptr(oy, d),
+                                                       _ptr(oz, d), _ptr(h, d), dxi, dyi, dzi, dt, _ptr(cr, d))
+    if rc != 0:
+        raise ValueError("oracle compute_courants failed with code %d" % rc)
+    return cr
+
+
+def velprd_driver(g, state, ox, oy, oz, uadv, vadv, wadv, h, dxi, dyi, dzi, dt, u=None, v=None, w=None):
+    """velprd_driver in place.  state: dict with nsubsteps, nsubsteps_o, dtn,
+    dtnold (updated), lsubstepping, ltimeadapt, lvertsplit, lcrdiag_nphlf,
+    crmaxlim, dtmax.  Returns (code, diag[9])."""
+    d = ox.dtype
+    sfx = {np.float64: "f64", np.float32: "f32"}[d.type]
+    R = ctypes.c_double if d == np.float64 else ctypes.c_float
+    ns, nso = ctypes.c_int(state["nsubsteps"]), ctypes.c_int(state["nsubsteps_o"])
+    dtn, dtnold = R(state["dtn"]), R(state["dtnold"])
+    diag = np.zeros(9)
+    rc = getattr(lib(), "orc_velprd_driver_" + sfx)(
+        ctypes.byref(g), ctypes.byref(ns), ctypes.byref(nso), int(state["lsubstepping"]), ctypes.byref(dtn),
+        ctypes.byref(dtnold), int(state["ltimeadapt"]), int(state["lvertsplit"]), int(state["lcrdiag_nphlf"]),
+        state["crmaxlim"], state["dtmax"], _ptr(ox, d), _ptr(oy, d), _ptr(oz, d), _ptr(u, d), _ptr(v, d),
+        _ptr(w, d), _ptr(uadv, d), _ptr(vadv, d), _ptr(wadv, d), _ptr(h, d), dxi, dyi, dzi, dt,
+        _ptr(diag, np.float64))
+    state.update(nsubsteps=ns.value, nsubsteps_o=nso.value, dtn=dtn.value, dtnold=dtnold.value)
+    return rc, diag
 
 
 def rho_gauge(g, ox, oy, oz, u1, u2, u3, x_in, x_incomp, h, rhoadv, rhr, pexe, pexr1, pexr2, bcx,
