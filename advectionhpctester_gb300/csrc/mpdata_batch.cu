@@ -27,8 +27,8 @@ __device__ __forceinline__ void load_prob(Prob<R>& sP, const Prob<R>* __restrict
 
 // One tile per block.  tiles[blockIdx.x] packs the problem (bits 0-15) and
 // the tile's x index (16-31), y index (32-47) and plane k-1 (48-63); the
-// host builds the list for the current block shape.  BODY sees P (shared),
-// i, j, k.
+// host builds the list for the current block shape.  BODY(IN) sees P
+// (shared), i, j, k; interior warps take IN = true.
 #define BATCH_TILE(BODY)                                                                     \
   __shared__ __align__(16) unsigned char sraw[sizeof(Prob<R>)];                              \
   Prob<R>& P = *reinterpret_cast<Prob<R>*>(sraw);                                            \
@@ -38,33 +38,52 @@ __device__ __forceinline__ void load_prob(Prob<R>& sP, const Prob<R>* __restrict
   const int i = (int)((w >> 16) & 0xffffu) * (int)blockDim.x + (int)threadIdx.x + 1;         \
   const int j = (int)((w >> 32) & 0xffffu) * (int)blockDim.y + (int)threadIdx.y + 1;         \
   const int k = (int)(w >> 48) + 1;                                                          \
-  if (i <= P.g.np && j <= P.g.mp) { BODY; }
+  const bool win = warp_interior(P.g, i, j, k);                                              \
+  if (i <= P.g.np && j <= P.g.mp) {                                                          \
+    if (win) {                                                                               \
+      BODY(true);                                                                            \
+    } else {                                                                                 \
+      BODY(false);                                                                           \
+    }                                                                                        \
+  }
 
 #define BATCH_ARGS const Prob<R>* __restrict__ probs, const unsigned long long* __restrict__ tiles
 
 template <class R, bool ANTIDIFF, bool HALO>
 __global__ void __launch_bounds__(256) kb_upwind(BATCH_ARGS) {
-  BATCH_TILE((upwind_body<R, ANTIDIFF, HALO>(P, i, j, k)))
+#define B(IN) upwind_body<R, ANTIDIFF, HALO, IN>(P, i, j, k)
+  BATCH_TILE(B)
+#undef B
 }
 template <class R>
 __global__ void __launch_bounds__(256) kb_copy(BATCH_ARGS) {
-  BATCH_TILE((copy_body<R>(P, i, j, k)))
+#define B(IN) copy_body<R>(P, i, j, k)
+  BATCH_TILE(B)
+#undef B
 }
 template <class R, bool AIN>
 __global__ void __launch_bounds__(256) kb_pseudo(BATCH_ARGS) {
-  BATCH_TILE((pseudo_body<R, AIN>(P, i, j, k)))
+#define B(IN) pseudo_body<R, AIN, IN>(P, i, j, k)
+  BATCH_TILE(B)
+#undef B
 }
 template <class R, bool NONOS, bool FIRST, bool KEEP>
 __global__ void __launch_bounds__(256) kb_bounds(BATCH_ARGS) {
-  BATCH_TILE((bounds_body<R, NONOS, FIRST, KEEP>(P, i, j, k)))
+#define B(IN) bounds_body<R, NONOS, FIRST, KEEP, IN>(P, i, j, k)
+  BATCH_TILE(B)
+#undef B
 }
 template <class R, bool NONOS>
 __global__ void __launch_bounds__(256) kb_limit(BATCH_ARGS) {
-  BATCH_TILE((limit_body<R, NONOS>(P, i, j, k)))
+#define B(IN) limit_body<R, NONOS, IN>(P, i, j, k)
+  BATCH_TILE(B)
+#undef B
 }
 template <class R, bool LAST>
 __global__ void __launch_bounds__(256) kb_update(BATCH_ARGS) {
-  BATCH_TILE((update_body<R, LAST>(P, i, j, k)))
+#define B(IN) update_body<R, LAST, IN>(P, i, j, k)
+  BATCH_TILE(B)
+#undef B
 }
 
 #define BLAUNCH(stage, ...)                  \

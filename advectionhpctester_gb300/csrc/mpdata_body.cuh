@@ -38,36 +38,46 @@ struct Prob {
 };
 
 // ---- read helpers -------------------------------------------------------
-__device__ __forceinline__ int cx(const Geo& g, int i) { return g.bx ? wrapi(i, g.np) : clampi(i, g.np); }
-__device__ __forceinline__ int cy(const Geo& g, int j) { return g.by ? wrapi(j, g.mp) : clampi(j, g.mp); }
-__device__ __forceinline__ int cz(const Geo& g, int k) { return g.bz ? wrapi(k, g.lp) : clampi(k, g.lp); }
+// IN: the caller guarantees that every index is inside [1, n] and every face
+// inside [2, n] (a cell in [2, n-1] on every axis reading its +-1
+// neighbours), where every boundary map is the identity.
+template <bool IN = false>
+__device__ __forceinline__ int cx(const Geo& g, int i) { return IN ? i : (g.bx ? wrapi(i, g.np) : clampi(i, g.np)); }
+template <bool IN = false>
+__device__ __forceinline__ int cy(const Geo& g, int j) { return IN ? j : (g.by ? wrapi(j, g.mp) : clampi(j, g.mp)); }
+template <bool IN = false>
+__device__ __forceinline__ int cz(const Geo& g, int k) { return IN ? k : (g.bz ? wrapi(k, g.lp) : clampi(k, g.lp)); }
 
 // the current (antidiffused) field with the xant halo rule
-template <class R>
+template <class R, bool IN = false>
 __device__ __forceinline__ R xr(const Geo& g, const Arr<R>& X, int i, int j, int k) {
+  if (IN) return X.ld(i, j, k);
   return X.ld(g.bx ? wrapi(i, g.np) : refl(i, g.np), g.by ? wrapi(j, g.mp) : refl(j, g.mp), cz(g, k));
 }
 
 // Face fields.  AIN = the caller's C-grid Courant numbers (faces 1..n+1 are
 // data on open axes); otherwise an antidiffusive field with the wall rule.
-template <class R, bool AIN>
+template <class R, bool AIN, bool IN = false>
 __device__ __forceinline__ R fx(const Geo& g, const Arr<R>& A, int f, int j, int k) {
+  if (IN) return A.ld(f, j, k);
   j = cy(g, j);
   k = cz(g, k);
   if (g.bx) return A.ld(wrapi(f, g.np), j, k);
   if (AIN) return A.ld(f, j, k);
   return (f <= 1 || f > g.np) ? R(0) : A.ld(f, j, k);
 }
-template <class R, bool AIN>
+template <class R, bool AIN, bool IN = false>
 __device__ __forceinline__ R fy(const Geo& g, const Arr<R>& A, int i, int f, int k) {
+  if (IN) return A.ld(i, f, k);
   i = cx(g, i);
   k = cz(g, k);
   if (g.by) return A.ld(i, wrapi(f, g.mp), k);
   if (AIN) return A.ld(i, f, k);
   return (f <= 1 || f > g.mp) ? R(0) : A.ld(i, f, k);
 }
-template <class R, bool AIN>
+template <class R, bool AIN, bool IN = false>
 __device__ __forceinline__ R fz(const Geo& g, const Arr<R>& A, int i, int j, int f) {
+  if (IN) return A.ld(i, j, f);
   i = cx(g, i);
   j = cy(g, j);
   if (g.bz) return A.ld(i, j, wrapi(f, g.lp));
@@ -77,38 +87,47 @@ __device__ __forceinline__ R fz(const Geo& g, const Arr<R>& A, int i, int j, int
   return A.ld(i, j, f);
 }
 
+// Warp-uniform choice of the interior path: true when every lane of the warp
+// holds a cell in [2, n-1] on every axis, where the bodies' reads (all within
+// +-1 of the cell) need no boundary map.  Every lane of a full warp calls it,
+// before any lane returns.
+__device__ __forceinline__ bool warp_interior(const Geo& g, int i, int j, int k) {
+  const bool in = i >= 2 && i < g.np && j >= 2 && j < g.mp && k >= 2 && k < g.lp;
+  return __all_sync(0xffffffffu, in);
+}
+
 // ---- upwind3d_gpubc (upwind3d-gpubc.f90:101-198) -------------------------
 // ANTIDIFF: an antidiffusive pass follows, so psi's open-wall halo ends the
 // step holding the zero-gradient copy of the old boundary values (written by
 // cp_last_to_halo_xy in the antidiffusion); otherwise it keeps bcx/bcy.
 // HALO: write psi's halo at all (off while autotuning).
-template <class R, bool ANTIDIFF, bool HALO>
+template <class R, bool ANTIDIFF, bool HALO, bool IN = false>
 __device__ __forceinline__ void upwind_body(const Prob<R>& P, int i, int j, int k) {
   const Geo& g = P.g;
   const Arr<R>& psi = P.psi;
   const R x = psi.ld(i, j, k);
   const long bx0 = (long)(j - 1) + (long)g.mp * (k - 1), bxs = (long)g.mp * g.lp;
   const long by0 = (long)(i - 1) + (long)g.np * (k - 1), bys = (long)g.np * g.lp;
-  const R xim = i > 1 ? psi.ld(i - 1, j, k) : (g.bx ? psi.ld(g.np, j, k) : P.bcx[bx0]);
-  const R xip = i < g.np ? psi.ld(i + 1, j, k) : (g.bx ? psi.ld(1, j, k) : P.bcx[bx0 + bxs]);
-  const R xjm = j > 1 ? psi.ld(i, j - 1, k) : (g.by ? psi.ld(i, g.mp, k) : P.bcy[by0]);
-  const R xjp = j < g.mp ? psi.ld(i, j + 1, k) : (g.by ? psi.ld(i, 1, k) : P.bcy[by0 + bys]);
+  const R xim = (IN || i > 1) ? psi.ld(i - 1, j, k) : (g.bx ? psi.ld(g.np, j, k) : P.bcx[bx0]);
+  const R xip = (IN || i < g.np) ? psi.ld(i + 1, j, k) : (g.bx ? psi.ld(1, j, k) : P.bcx[bx0 + bxs]);
+  const R xjm = (IN || j > 1) ? psi.ld(i, j - 1, k) : (g.by ? psi.ld(i, g.mp, k) : P.bcy[by0]);
+  const R xjp = (IN || j < g.mp) ? psi.ld(i, j + 1, k) : (g.by ? psi.ld(i, 1, k) : P.bcy[by0 + bys]);
   const R hc = P.h.ld(i, j, k);
   const R hi = R(1) / hc;
-  const R f1p = donor(x, xip, fx<R, true>(g, P.u1, i + 1, j, k));
+  const R f1p = donor(x, xip, fx<R, true, IN>(g, P.u1, i + 1, j, k));
   const R f1 = donor(xim, x, P.u1.ld(i, j, k));
-  const R f2p = donor(x, xjp, fy<R, true>(g, P.u2, i, j + 1, k));
+  const R f2p = donor(x, xjp, fy<R, true, IN>(g, P.u2, i, j + 1, k));
   const R f2 = donor(xjm, x, P.u2.ld(i, j, k));
   R f3p, f3;
-  if (!g.bz && k == 1) {  // :134-135
+  if (!IN && !g.bz && k == 1) {  // :134-135
     f3p = donor(x, psi.ld(i, j, k + 1), P.u3.ld(i, j, k + 1));
     f3 = -f3p;
-  } else if (!g.bz && k == g.lp) {  // :164-165
+  } else if (!IN && !g.bz && k == g.lp) {  // :164-165
     f3 = donor(psi.ld(i, j, k - 1), x, P.u3.ld(i, j, k));
     f3p = -f3;
   } else {
-    f3p = donor(x, psi.ld(i, j, cz(g, k + 1)), fz<R, true>(g, P.u3, i, j, k + 1));
-    f3 = donor(psi.ld(i, j, cz(g, k - 1)), x, P.u3.ld(i, j, k));
+    f3p = donor(x, psi.ld(i, j, cz<IN>(g, k + 1)), fz<R, true, IN>(g, P.u3, i, j, k + 1));
+    f3 = donor(psi.ld(i, j, cz<IN>(g, k - 1)), x, P.u3.ld(i, j, k));
   }
   if (P.rho) {
     // mpdata3d-rho-gauge-gpubc.f90:137-210: no rhr, division by h, fluxes kept;
@@ -128,11 +147,11 @@ __device__ __forceinline__ void upwind_body(const Prob<R>& P, int i, int j, int 
     P.hinv.at(i, j, k) = hi;
     // reciprocal mean densities of the cell's lower faces, used by every
     // corrective pass of this step (hmx/hmy/hmz of antidiff3d-*-gpubc.f90)
-    if (g.bx || i > 1) P.hmx.at(i, j, k) = rhm(P.h.ld(cx(g, i - 1), j, k), hc);
-    if (g.by || j > 1) P.hmy.at(i, j, k) = rhm(P.h.ld(i, cy(g, j - 1), k), hc);
-    if (g.bz || k > 1) P.hmz.at(i, j, k) = rhm(P.h.ld(i, j, cz(g, k - 1)), hc);
+    if (IN || g.bx || i > 1) P.hmx.at(i, j, k) = rhm(P.h.ld(cx<IN>(g, i - 1), j, k), hc);
+    if (IN || g.by || j > 1) P.hmy.at(i, j, k) = rhm(P.h.ld(i, cy<IN>(g, j - 1), k), hc);
+    if (IN || g.bz || k > 1) P.hmz.at(i, j, k) = rhm(P.h.ld(i, j, cz<IN>(g, k - 1)), hc);
   }
-  if (HALO) {
+  if (HALO && !IN) {
     if (!g.bx) {
       if (i == 1) psi.at(0, j, k) = ANTIDIFF ? x : xim;
       if (i == g.np) psi.at(g.np + 1, j, k) = ANTIDIFF ? x : xip;
@@ -151,7 +170,7 @@ __device__ __forceinline__ void upwind_body(const Prob<R>& P, int i, int j, int 
 // Each cell computes its lower faces.  AIN: the first corrective pass, whose
 // "a" velocities are the caller's Courant numbers; later passes use the
 // previous pass's limited velocities w1..w3.
-template <class R, bool STD, bool AIN>
+template <class R, bool STD, bool AIN, bool IN = false>
 __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int k) {
   const Geo& g = P.g;
   const Arr<R>& X = P.xant;
@@ -159,12 +178,12 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
   const Arr<R>& A2 = AIN ? P.u2 : P.w2;
   const Arr<R>& A3 = AIN ? P.u3 : P.w3;
   const R ep = Eps<R>::v;
-  const bool zt = g.bz || (k > 1 && k < g.lp);
-#define XX(a, b, c) xr<R>(g, X, (a), (b), (c))
-#define AX(f, b, c) fx<R, AIN>(g, A1, (f), (b), (c))
-#define AY(a, f, c) fy<R, AIN>(g, A2, (a), (f), (c))
-#define AZ(a, b, f) fz<R, AIN>(g, A3, (a), (b), (f))
-  if (g.bx || i > 1) {
+  const bool zt = IN || g.bz || (k > 1 && k < g.lp);
+#define XX(a, b, c) xr<R, IN>(g, X, (a), (b), (c))
+#define AX(f, b, c) fx<R, AIN, IN>(g, A1, (f), (b), (c))
+#define AY(a, f, c) fy<R, AIN, IN>(g, A2, (a), (f), (c))
+#define AZ(a, b, f) fz<R, AIN, IN>(g, A3, (a), (b), (f))
+  if (IN || g.bx || i > 1) {
     const R hmx = P.hmx.ld(i, j, k);
     const R a = AX(i, j, k);
     R v;
@@ -195,7 +214,7 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
     }
     P.v1.at(i, j, k) = v;
   }
-  if (g.by || j > 1) {
+  if (IN || g.by || j > 1) {
     const R hmy = P.hmy.ld(i, j, k);
     const R a = AY(i, j, k);
     R v;
@@ -226,7 +245,7 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
     }
     P.v2.at(i, j, k) = v;
   }
-  if (g.bz || k > 1) {
+  if (IN || g.bz || k > 1) {
     const R hmz = P.hmz.ld(i, j, k);
     const R a = AZ(i, j, k);
     R v;
@@ -260,12 +279,12 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
 #undef AZ
 }
 
-template <class R, bool AIN>
+template <class R, bool AIN, bool IN = false>
 __device__ __forceinline__ void pseudo_body(const Prob<R>& P, int i, int j, int k) {
   if (P.stdf)
-    pseudo_form<R, true, AIN>(P, i, j, k);
+    pseudo_form<R, true, AIN, IN>(P, i, j, k);
   else
-    pseudo_form<R, false, AIN>(P, i, j, k);
+    pseudo_form<R, false, AIN, IN>(P, i, j, k);
 }
 
 // ---- limiter bounds and ratios (std :256-348, gauge :238-324) -------------
@@ -275,45 +294,43 @@ __device__ __forceinline__ void pseudo_body(const Prob<R>& P, int i, int j, int 
 // over x_in, which the reference leaves unset (antidiff3d-gauge-gpubc.f90:249),
 // is computed as in mpdata3d-rho-gauge-gpubc.f90:365-368.  Also stores
 // q = x/rhr, the ratio every later stage divides out.
-template <class R, bool NONOS, bool FIRST, bool KEEP>
+template <class R, bool NONOS, bool FIRST, bool KEEP, bool IN = false>
 __device__ __forceinline__ void bounds_body(const Prob<R>& P, int i, int j, int k) {
   const Geo& g = P.g;
   const Arr<R>& X = P.xant;
   const R x = X.ld(i, j, k);
   P.q.at(i, j, k) = P.rho ? x : x / P.rhr.ld(i, j, k);  // x/1 == x for the density step
   if (!NONOS) return;
-  const bool lo = g.bz || k > 1, hi = g.bz || k < g.lp;
+  const bool lo = IN || g.bz || k > 1, hi = IN || g.bz || k < g.lp;
   R ma, mi;
   if (FIRST) {
     const Arr<R>& xin = P.psi;
-    const int im = g.bx ? wrapi(i - 1, g.np) : clampi(i - 1, g.np);
-    const int ip = g.bx ? wrapi(i + 1, g.np) : clampi(i + 1, g.np);
-    const int jm = g.by ? wrapi(j - 1, g.mp) : clampi(j - 1, g.mp);
-    const int jp = g.by ? wrapi(j + 1, g.mp) : clampi(j + 1, g.mp);
+    const int im = cx<IN>(g, i - 1), ip = cx<IN>(g, i + 1);
+    const int jm = cy<IN>(g, j - 1), jp = cy<IN>(g, j + 1);
     Extrema<R> e(xin.ld(i, j, k));
     e.add(xin.ld(im, j, k));
     e.add(xin.ld(ip, j, k));
     e.add(xin.ld(i, jm, k));
     e.add(xin.ld(i, jp, k));
-    if (lo) e.add(xin.ld(i, j, cz(g, k - 1)));
-    if (hi) e.add(xin.ld(i, j, cz(g, k + 1)));
+    if (lo) e.add(xin.ld(i, j, cz<IN>(g, k - 1)));
+    if (hi) e.add(xin.ld(i, j, cz<IN>(g, k + 1)));
     e.add(x);
-    e.add(xr<R>(g, X, i - 1, j, k));
-    e.add(xr<R>(g, X, i + 1, j, k));
-    e.add(xr<R>(g, X, i, j - 1, k));
-    e.add(xr<R>(g, X, i, j + 1, k));
-    if (lo) e.add(X.ld(i, j, cz(g, k - 1)));
-    if (hi) e.add(X.ld(i, j, cz(g, k + 1)));
+    e.add(xr<R, IN>(g, X, i - 1, j, k));
+    e.add(xr<R, IN>(g, X, i + 1, j, k));
+    e.add(xr<R, IN>(g, X, i, j - 1, k));
+    e.add(xr<R, IN>(g, X, i, j + 1, k));
+    if (lo) e.add(X.ld(i, j, cz<IN>(g, k - 1)));
+    if (hi) e.add(X.ld(i, j, cz<IN>(g, k + 1)));
     ma = e.max();
     mi = e.min();
   } else {
     Extrema<R> e(x);
-    e.add(xr<R>(g, X, i - 1, j, k));
-    e.add(xr<R>(g, X, i + 1, j, k));
-    e.add(xr<R>(g, X, i, j - 1, k));
-    e.add(xr<R>(g, X, i, j + 1, k));
-    if (lo) e.add(X.ld(i, j, cz(g, k - 1)));
-    if (hi) e.add(X.ld(i, j, cz(g, k + 1)));
+    e.add(xr<R, IN>(g, X, i - 1, j, k));
+    e.add(xr<R, IN>(g, X, i + 1, j, k));
+    e.add(xr<R, IN>(g, X, i, j - 1, k));
+    e.add(xr<R, IN>(g, X, i, j + 1, k));
+    if (lo) e.add(X.ld(i, j, cz<IN>(g, k - 1)));
+    if (hi) e.add(X.ld(i, j, cz<IN>(g, k + 1)));
     ma = mx2(P.mx.ld(i, j, k), e.max());
     mi = mn2(P.mn.ld(i, j, k), e.min());
   }
@@ -326,9 +343,9 @@ __device__ __forceinline__ void bounds_body(const Prob<R>& P, int i, int j, int 
   const Arr<R>& F2 = P.stdf ? P.f2 : P.v2;
   const Arr<R>& F3 = P.stdf ? P.f3 : P.v3;
   const R ep = Eps<R>::v;
-  const R e1 = fx<R, false>(g, F1, i + 1, j, k), w1 = fx<R, false>(g, F1, i, j, k);
-  const R e2 = fy<R, false>(g, F2, i, j + 1, k), w2 = fy<R, false>(g, F2, i, j, k);
-  const R e3 = fz<R, false>(g, F3, i, j, k + 1), w3 = fz<R, false>(g, F3, i, j, k);
+  const R e1 = fx<R, false, IN>(g, F1, i + 1, j, k), w1 = fx<R, false, IN>(g, F1, i, j, k);
+  const R e2 = fy<R, false, IN>(g, F2, i, j + 1, k), w2 = fy<R, false, IN>(g, F2, i, j, k);
+  const R e3 = fz<R, false, IN>(g, F3, i, j, k + 1), w3 = fz<R, false, IN>(g, F3, i, j, k);
   const R hc = P.h.ld(i, j, k);
   P.cp.at(i, j, k) = (ma - x) * hc / (pn(e1) + pp(w1) + pn(e2) + pp(w2) + pn(e3) + pp(w3) + ep);
   P.cn.at(i, j, k) = (x - mi) * hc / (pp(e1) + pn(w1) + pp(e2) + pn(w2) + pp(e3) + pn(w3) + ep);
@@ -343,14 +360,14 @@ __device__ __forceinline__ R vlim_std(R v, R a1, R a2, R xl, R xrr) {
   return pp(v) * (a1 * possign(xl) + a2 * possign(-xl)) - pn(v) * (a2 * possign(xrr) + a1 * possign(-xrr));
 }
 
-template <class R, bool STD, bool NONOS>
+template <class R, bool STD, bool NONOS, bool IN = false>
 __device__ __forceinline__ void limit_form(const Prob<R>& P, int i, int j, int k) {
   const Geo& g = P.g;
   const Arr<R>& X = P.xant;
   const R cpc = NONOS ? P.cp.ld(i, j, k) : R(0), cnc = NONOS ? P.cn.ld(i, j, k) : R(0);
   const R xc = X.ld(i, j, k), qc = STD ? P.q.ld(i, j, k) : R(0);
-  if (g.bx || i > 1) {
-    const int im = wrapi(i - 1, g.np);
+  if (IN || g.bx || i > 1) {
+    const int im = IN ? i - 1 : wrapi(i - 1, g.np);
     const R v = P.v1.ld(i, j, k);
     R w = v;
     if (NONOS) {
@@ -361,8 +378,8 @@ __device__ __forceinline__ void limit_form(const Prob<R>& P, int i, int j, int k
     P.w1.at(i, j, k) = w;
     if (STD) P.f1.at(i, j, k) = donor(P.q.ld(im, j, k), qc, w);
   }
-  if (g.by || j > 1) {
-    const int jm = wrapi(j - 1, g.mp);
+  if (IN || g.by || j > 1) {
+    const int jm = IN ? j - 1 : wrapi(j - 1, g.mp);
     const R v = P.v2.ld(i, j, k);
     R w = v;
     if (NONOS) {
@@ -373,8 +390,8 @@ __device__ __forceinline__ void limit_form(const Prob<R>& P, int i, int j, int k
     P.w2.at(i, j, k) = w;
     if (STD) P.f2.at(i, j, k) = donor(P.q.ld(i, jm, k), qc, w);
   }
-  if (g.bz || k > 1) {
-    const int km = wrapi(k - 1, g.lp);
+  if (IN || g.bz || k > 1) {
+    const int km = IN ? k - 1 : wrapi(k - 1, g.lp);
     const R v = P.v3.ld(i, j, k);
     R w = v;
     if (NONOS) {
@@ -387,30 +404,30 @@ __device__ __forceinline__ void limit_form(const Prob<R>& P, int i, int j, int k
   }
 }
 
-template <class R, bool NONOS>
+template <class R, bool NONOS, bool IN = false>
 __device__ __forceinline__ void limit_body(const Prob<R>& P, int i, int j, int k) {
   if (P.stdf)
-    limit_form<R, true, NONOS>(P, i, j, k);
+    limit_form<R, true, NONOS, IN>(P, i, j, k);
   else
-    limit_form<R, false, NONOS>(P, i, j, k);
+    limit_form<R, false, NONOS, IN>(P, i, j, k);
 }
 
 // ---- corrective update (std :431-459, gauge :364-368/396-400/423-427) -----
 // LAST: the last pass writes psi; earlier passes overwrite xant in place (the
 // update reads q, not x).
-template <class R, bool LAST>
+template <class R, bool LAST, bool IN = false>
 __device__ __forceinline__ void update_body(const Prob<R>& P, int i, int j, int k) {
   const Geo& g = P.g;
   const Arr<R>& out = LAST ? P.psi : P.xant;
   if (P.stdf) {
-    const R d = fx<R, false>(g, P.f1, i + 1, j, k) - fx<R, false>(g, P.f1, i, j, k) +
-                fy<R, false>(g, P.f2, i, j + 1, k) - fy<R, false>(g, P.f2, i, j, k) +
-                fz<R, false>(g, P.f3, i, j, k + 1) - fz<R, false>(g, P.f3, i, j, k);
+    const R d = fx<R, false, IN>(g, P.f1, i + 1, j, k) - fx<R, false, IN>(g, P.f1, i, j, k) +
+                fy<R, false, IN>(g, P.f2, i, j + 1, k) - fy<R, false, IN>(g, P.f2, i, j, k) +
+                fz<R, false, IN>(g, P.f3, i, j, k + 1) - fz<R, false, IN>(g, P.f3, i, j, k);
     out.at(i, j, k) = P.rhr.ld(i, j, k) * (P.q.ld(i, j, k) - d * P.hinv.ld(i, j, k));
   } else {
-    const R d = fx<R, false>(g, P.w1, i + 1, j, k) - fx<R, false>(g, P.w1, i, j, k) +
-                fy<R, false>(g, P.w2, i, j + 1, k) - fy<R, false>(g, P.w2, i, j, k) +
-                fz<R, false>(g, P.w3, i, j, k + 1) - fz<R, false>(g, P.w3, i, j, k);
+    const R d = fx<R, false, IN>(g, P.w1, i + 1, j, k) - fx<R, false, IN>(g, P.w1, i, j, k) +
+                fy<R, false, IN>(g, P.w2, i, j + 1, k) - fy<R, false, IN>(g, P.w2, i, j, k) +
+                fz<R, false, IN>(g, P.w3, i, j, k + 1) - fz<R, false, IN>(g, P.w3, i, j, k);
     const R t = P.q.ld(i, j, k) - d / P.h.ld(i, j, k);
     out.at(i, j, k) = P.rho ? t : P.rhr.ld(i, j, k) * t;  // rhr == 1 in the density step
   }

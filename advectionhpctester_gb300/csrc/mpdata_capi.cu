@@ -101,6 +101,8 @@ int check_grid(const mpdata_grid* g) {
     return MPDATA_E_DIMS;
   // launch geometry: grid.y = ceil((mp+1)/4), grid.z = lp+1
   if (g->mp > 4 * 65535 - 8 || g->lp > 65534 || g->np > (1 << 30)) return MPDATA_E_DIMS;
+  // 32-bit strides: the largest plane (a C-grid array, halo included) stays below 2^31 elements
+  if ((long long)(g->np + 2 * g->ih + 1) * (g->mp + 2 * g->ih + 1) >= (1LL << 31)) return MPDATA_E_DIMS;
   return MPDATA_OK;
 }
 

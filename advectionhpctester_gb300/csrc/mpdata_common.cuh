@@ -15,29 +15,30 @@ struct Geo {
 
 // View of a 3-D Fortran-ordered array; p points at the logical element
 // (1,1,1), so halo elements sit at negative offsets inside the caller's
-// allocation.  Indices are the reference's 1-based (i,j,k).
+// allocation.  Indices are the reference's 1-based (i,j,k).  The strides are
+// 32-bit (the host rejects grids whose planes, halos included, reach 2^31
+// elements), so each term of an offset is one 32x32->64 multiply-add.
 template <class R>
 struct Arr {
   R* p;
-  long sy, sz;
-  __device__ __forceinline__ R ld(int i, int j, int k) const {
-    return p[(long)(i - 1) + (long)(j - 1) * sy + (long)(k - 1) * sz];
+  int sy, sz;
+  __device__ __forceinline__ long off(int i, int j, int k) const {
+    return (long)(i - 1) + (long)(j - 1) * sy + (long)(k - 1) * sz;
   }
-  __device__ __forceinline__ R& at(int i, int j, int k) const {
-    return p[(long)(i - 1) + (long)(j - 1) * sy + (long)(k - 1) * sz];
-  }
+  __device__ __forceinline__ R ld(int i, int j, int k) const { return p[off(i, j, k)]; }
+  __device__ __forceinline__ R& at(int i, int j, int k) const { return p[off(i, j, k)]; }
 };
 
 // Caller arrays with halo width ih: extents (n0, n1, *) along x and y.
 template <class R>
 inline Arr<R> caller_view(R* base, int ih, int n0, int n1) {
   const long sy = n0, sz = (long)n0 * n1;
-  return Arr<R>{base + ih + ih * sy + ih * sz, sy, sz};
+  return Arr<R>{base + ih + ih * sy + ih * sz, (int)sy, (int)sz};
 }
 // Workspace scratch: interior cells (or faces 1..n along the own axis), no halo.
 template <class R>
 inline Arr<R> scratch_view(R* base, const Geo& g) {
-  return Arr<R>{base, (long)g.np, (long)g.np * g.mp};
+  return Arr<R>{base, g.np, (int)((long)g.np * g.mp)};
 }
 
 // ---- index maps for reads one cell outside [1, n] ----

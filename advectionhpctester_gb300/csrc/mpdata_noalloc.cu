@@ -62,7 +62,7 @@ int scratch_on_device(double** out) {
 
 Arr<double> caller(const double* base, int ih, int n0, int n1) {
   const long sy = n0, sz = (long)n0 * n1;
-  return Arr<double>{const_cast<double*>(base) + ih + ih * sy + ih * sz, sy, sz};
+  return Arr<double>{const_cast<double*>(base) + ih + ih * sy + ih * sz, (int)sy, (int)sz};
 }
 
 }  // namespace
@@ -106,7 +106,7 @@ extern "C" int mpdata_step_noalloc_f64(const mpdata_grid* grid, const mpdata_opt
                                         &P.w1,   &P.w2, &P.w3, &P.cp, &P.cn, &P.mx, &P.mn,
                                         &P.q,    &P.hinv, &P.hmx, &P.hmy, &P.hmz};
   for (int f = 0; f < NOALLOC_FIELDS; f++)
-    *slots[f] = Arr<double>{scratch + (size_t)f * ncell, (long)g.np, (long)g.np * g.mp};
+    *slots[f] = Arr<double>{scratch + (size_t)f * ncell, g.np, g.np * g.mp};
   return run_step<double>(P, opts->iord, opts->nonos, nullptr, static_cast<cudaStream_t>(stream)) == 0
              ? MPDATA_OK
              : MPDATA_E_CUDA;

@@ -17,10 +17,24 @@ namespace mpdata {
   const int k = blockIdx.z + 1;                             \
   if (i > P.g.np || j > P.g.mp) return;
 
+// Interior warps take the body without boundary maps (IN = true).
+#define CELL_DISPATCH(BODY)                                 \
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1; \
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1; \
+  const int k = blockIdx.z + 1;                             \
+  const bool win = warp_interior(P.g, i, j, k);             \
+  if (i > P.g.np || j > P.g.mp) return;                     \
+  if (win) {                                                \
+    BODY(true);                                             \
+  } else {                                                  \
+    BODY(false);                                            \
+  }
+
 template <class R, bool ANTIDIFF>
 __global__ void __launch_bounds__(128) k_upwind(const Prob<R> P) {
-  CELL_INDEX
-  upwind_body<R, ANTIDIFF, true>(P, i, j, k);
+#define B(IN) upwind_body<R, ANTIDIFF, true, IN>(P, i, j, k)
+  CELL_DISPATCH(B)
+#undef B
 }
 template <class R>
 __global__ void __launch_bounds__(128) k_copy(const Prob<R> P) {
@@ -29,23 +43,27 @@ __global__ void __launch_bounds__(128) k_copy(const Prob<R> P) {
 }
 template <class R, bool AIN>
 __global__ void __launch_bounds__(128) k_pseudo(const Prob<R> P) {
-  CELL_INDEX
-  pseudo_body<R, AIN>(P, i, j, k);
+#define B(IN) pseudo_body<R, AIN, IN>(P, i, j, k)
+  CELL_DISPATCH(B)
+#undef B
 }
 template <class R, bool NONOS, bool FIRST, bool KEEP>
 __global__ void __launch_bounds__(128) k_bounds(const Prob<R> P) {
-  CELL_INDEX
-  bounds_body<R, NONOS, FIRST, KEEP>(P, i, j, k);
+#define B(IN) bounds_body<R, NONOS, FIRST, KEEP, IN>(P, i, j, k)
+  CELL_DISPATCH(B)
+#undef B
 }
 template <class R, bool NONOS>
 __global__ void __launch_bounds__(128) k_limit(const Prob<R> P) {
-  CELL_INDEX
-  limit_body<R, NONOS>(P, i, j, k);
+#define B(IN) limit_body<R, NONOS, IN>(P, i, j, k)
+  CELL_DISPATCH(B)
+#undef B
 }
 template <class R, bool LAST>
 __global__ void __launch_bounds__(128) k_update(const Prob<R> P) {
-  CELL_INDEX
-  update_body<R, LAST>(P, i, j, k);
+#define B(IN) update_body<R, LAST, IN>(P, i, j, k)
+  CELL_DISPATCH(B)
+#undef B
 }
 
 template <class R, bool LINER>

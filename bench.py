@@ -46,25 +46,38 @@ UNIT = "Gcell-steps/s"
 #   predictor level  r o0 x3 o2 x3 h  w o1 x3                    10
 #   predictor cgrid  r o1 x3 o0 x3 h  w u1..3 o2 x3              13
 def stage_elems(stage, gauge, iord):
+    """Compulsory fields read + written per cell by one launch of a stage
+    (interior cells, each field once; ncu DRAM bytes agree within 4%)."""
     keep = iord > 2
     if stage == "upwind":
-        return 8.0
+        return 11.0                                   # psi,u1..3,h,rhr -> xant,1/h,hmx,hmy,hmz
     if stage == "pseudo_velocity":
-        return 8.0 if gauge else 11.0
+        return 10.0 if gauge else 13.0                # xant,a1..3,hm1..3 -> v1..3 (+f1..3 std)
     if stage == "limiter_bounds":
-        first = 9.0 + (2.0 if keep else 0.0)          # reads psi, writes mx/mn when kept
-        later = 13.0                                  # reads and writes mx/mn
+        first = 10.0 + (2.0 if keep else 0.0)         # xant,rhr,psi,F1..3,h -> q,cp,cn (+mx,mn kept)
+        later = 13.0                                  # xant,rhr,mx,mn,F1..3,h -> q,mx,mn,cp,cn
         n = max(iord - 1, 1)
         return (first + later * (n - 1)) / n
     if stage == "limited_flux":
-        return 9.0 if gauge else 13.0
+        return 8.0 if gauge else 13.0                 # cp,cn,v1..3 -> w1..3 (+xant,q -> f1..3 std)
     if stage == "corrective_update":
-        return 7.0
+        return 7.0                                    # w1..3 (f1..3),q,h (1/h),rhr -> psi
     if stage == "predictor_level":
         return 10.0
     if stage == "predictor_cgrid":
         return 13.0
     return 2.0
+
+
+# DRAM bytes and FP64 instructions per cell of the dominant kernel (k_pseudo,
+# gauge form), from an ncu capture of every stage kernel at 384x384x64
+# (dram__bytes_read.sum + dram__bytes_write.sum, and
+# smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on.sum, per cell).
+# Both grow in proportion to the cells of a launch.
+NCU_PSEUDO = {64: {"dram_bytes_per_cell": 78.6, "fp64_inst_per_cell": 81.0},
+              32: {"dram_bytes_per_cell": 38.2, "fp64_inst_per_cell": 0.0}}
+# GB300 issues 2 FP64 instructions per SM per clock (1.25 TFLOP/s nominal FMA).
+FP64_INST_PER_SM_CLK = 2.0
 
 
 def load_peaks():
@@ -274,11 +287,23 @@ def run_ours(args, ws, rank, local):
     avg_ms = tot_ms / max(nl, 1)
     alg_bytes = stage_elems(name, True, 3) * elem * cells
     achieved = alg_bytes / (avg_ms * 1e-3) / 1e9
+    ncu = NCU_PSEUDO[args.precision] if name == "pseudo_velocity" else None
+    traffic = int(ncu["dram_bytes_per_cell"] * cells) if ncu else None
     roof = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peak,
-            "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+            "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
             "peak_source": peak_kind, "alg_bytes_per_launch": int(alg_bytes),
             "avg_launch_ms": round(avg_ms, 4),
-            "note": "FP64-ALU bound on GB300 (FP64 ~1.2 TFLOP/s); see fp64_pipe"}
+            "traffic_source": "ncu DRAM bytes per cell of this kernel at 384x384x64, scaled by cells"}
+    if args.precision == 64 and ncu:
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        mhz = clocks.get("sm_max_mhz") or 2070.0
+        fp64_peak = FP64_INST_PER_SM_CLK * sms * mhz * 1e6 / 1e9
+        fp64_ach = ncu["fp64_inst_per_cell"] * cells / (avg_ms * 1e-3) / 1e9
+        roof["fp64_pipe"] = {"achieved": round(fp64_ach, 1), "peak": round(fp64_peak, 1),
+                             "unit": "G FP64 inst/s", "frac": round(fp64_ach / fp64_peak, 4),
+                             "inst_per_cell": ncu["fp64_inst_per_cell"],
+                             "note": "the binding roof: 2 FP64 instructions per SM per clock at the "
+                                     "sampled maximum SM clock; DRAM runs at the hbm frac"}
     stage_json = {k: {"ms_total": round(v[0], 3), "launches": int(v[1]),
                       "share": round(v[0] / max(sum(t for t, _ in stages.values()), 1e-9), 4)}
                   for k, v in stages.items() if v[1]}
