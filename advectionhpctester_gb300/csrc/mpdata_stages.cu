@@ -41,8 +41,24 @@ __global__ void __launch_bounds__(128) k_copy(const Prob<R> P) {
   CELL_INDEX
   copy_body<R>(P, i, j, k);
 }
+// Minimum resident 128-thread blocks per SM asked of the register allocator
+// for the pseudo-velocity kernel, whose interior path keeps ~60 neighbour
+// loads in flight: FP32 is latency-bound and gains from 8 blocks (64
+// registers, a 16-byte spill); FP64 is FP64-pipe-bound and keeps its 80.
+// Build-time overridable for tuning sweeps.
+#ifndef MPDATA_MINB_PSEUDO_F32
+#define MPDATA_MINB_PSEUDO_F32 8
+#endif
+#ifndef MPDATA_MINB_PSEUDO_F64
+#define MPDATA_MINB_PSEUDO_F64 1
+#endif
+template <class R>
+struct PseudoMinBlocks {
+  static constexpr int v = sizeof(R) == 4 ? MPDATA_MINB_PSEUDO_F32 : MPDATA_MINB_PSEUDO_F64;
+};
+
 template <class R, bool AIN>
-__global__ void __launch_bounds__(128) k_pseudo(const Prob<R> P) {
+__global__ void __launch_bounds__(128, PseudoMinBlocks<R>::v) k_pseudo(const Prob<R> P) {
 #define B(IN) pseudo_body<R, AIN, IN>(P, i, j, k)
   CELL_DISPATCH(B)
 #undef B

@@ -237,11 +237,23 @@ class GpuArm:
         for c in range(3):
             self.torch.mul(self.pats[c], fac if c < 2 else 1.0, out=self.o[c][..., 0])
 
+    def dynamics_from(self, n, pats):
+        fac = time_factor(n, self.T)
+        for c in range(3):
+            self.torch.mul(pats[c], fac if c < 2 else 1.0, out=self.o[c][..., 0])
+
     def step(self, n):
         self.dynamics(n)
         self.ws.velprd(self.o[0], self.o[1], self.o[2], self.h, 1.0, 1.0, 1.0, 1.0, 1.0,
                        self.u1, self.u2, self.u3)
         self.ws.step(self.psi, self.u1, self.u2, self.u3, self.h, self.rhr)
+
+    def step_on(self, n, b):
+        """One step on the buffer set b (psi, pats, h, rhr), current stream."""
+        self.dynamics_from(n, b["pats"])
+        self.ws.velprd(self.o[0], self.o[1], self.o[2], b["h"], 1.0, 1.0, 1.0, 1.0, 1.0,
+                       self.u1, self.u2, self.u3)
+        self.ws.step(b["psi"], self.u1, self.u2, self.u3, b["h"], b["rhr"])
 
 
 def run_ours(args, ws, rank, local):
@@ -326,8 +338,13 @@ def run_ours(args, ws, rank, local):
     result["mass_rel_drift"] = (mass1 - mass0) / mass0
     if rank == 0 and ws == 1 and not args.no_extras and args.precision == 64:
         result["fp32"] = run_fp32_study(args, host, arm, ms_max / args.steps, mass0)
-    if rank == 0 and ws == 1 and not args.no_e2e:
-        result["e2e"] = run_e2e(arm, args)
+    if not args.no_e2e:
+        barrier(ws)
+        e2e = run_e2e(arm, args)
+        ms_e2e = max_over_ranks(e2e["ms_per_step"], ws)
+        e2e["value"] = round(ws * cells / (ms_e2e * 1e-3) / 1e9, 4)
+        e2e["ms_per_step"] = round(ms_e2e, 4)
+        result["e2e"] = e2e
     arm.ws.close()
     del arm
     if rank == 0 and ws == 1 and not args.no_extras:
@@ -335,6 +352,8 @@ def run_ours(args, ws, rank, local):
         result["adjoint"] = run_adjoint_study(args)
         torch.cuda.empty_cache()
         result["batch"] = run_batch_study(args)
+        torch.cuda.empty_cache()
+        result["precision_768x768x160"] = run_precision_study(args, nsteps=args.precision_steps)
     return result
 
 
@@ -365,6 +384,107 @@ def run_fp32_study(args, host, arm64, ms64, mass0):
            "mass_rel_drift": (m32 - mass0) / mass0,
            "note": "FP32 stencil arithmetic, FP64 Neumaier-compensated mass and norms"}
     arm.ws.close()
+    return out
+
+
+class DevArm:
+    """A workload built on the device: the deformational A-grid flow (u, v
+    scaled by cos(pi t/T), w steady) through the predictor, psi from a
+    callable, h = rhr = 1, periodic; iord and precision as given."""
+
+    def __init__(self, nx, ny, nz, precision, iord, psi_fn, T=200.0, courant=0.5):
+        import torch
+        from advectionhpctester_gb300 import mpdata as M
+        self.torch, self.M, self.T = torch, M, T
+        dt = torch.float64 if precision == 64 else torch.float32
+        sh = M.shapes(nx, ny, nz, 1)
+        emp = lambda shape: M.fortran_empty(shape, dt)
+        inner = lambda t: t.permute(2, 1, 0)[1:nz + 1, 1:ny + 1, 1:nx + 1].permute(2, 1, 0)
+        x = (torch.arange(nx, device="cuda", dtype=torch.float64) + 0.5) / nx
+        y = (torch.arange(ny, device="cuda", dtype=torch.float64) + 0.5) / ny
+        z = (torch.arange(nz, device="cuda", dtype=torch.float64) + 0.5) / nz
+        sc = courant / 1.1
+        pat = [(torch.sin(math.pi * x) ** 2)[:, None, None] * torch.sin(2 * math.pi * y)[None, :, None] * sc,
+               -(torch.sin(math.pi * y) ** 2)[None, :, None] * torch.sin(2 * math.pi * x)[:, None, None] * sc,
+               0.1 * torch.sin(2 * math.pi * z)[None, None, :] * sc]
+        self.pats = []
+        for a in pat:
+            t = emp(sh["psi"])
+            t.zero_()
+            inner(t).copy_(a.expand(nx, ny, nz))
+            self.pats.append(t)
+        self.psi = emp(sh["psi"])
+        self.psi.zero_()
+        inner(self.psi).copy_(psi_fn(x, y, z))
+        self.h = emp(sh["psi"])
+        self.h.fill_(1.0)
+        self.rhr = emp(sh["psi"])
+        self.rhr.fill_(1.0)
+        self.u1, self.u2, self.u3 = emp(sh["u1"]), emp(sh["u2"]), emp(sh["u3"])
+        for u in (self.u1, self.u2, self.u3):
+            u.zero_()
+        self.o = [M.fortran_empty(sh["psi"] + (3,), dt) for _ in range(3)]
+        for c in range(3):
+            self.o[c].zero_()
+            self.o[c][..., 2].copy_(self.pats[c] * (time_factor(-1, T) if c < 2 else 1.0))
+        self.ws = M.Workspace(nx, ny, nz, 1, 1, 1, 1, iord=iord, nonos=1, gauge=1, precision=precision)
+
+    def step(self, n):
+        fac = time_factor(n, self.T)
+        for c in range(3):
+            self.torch.mul(self.pats[c], fac if c < 2 else 1.0, out=self.o[c][..., 0])
+        self.ws.velprd(self.o[0], self.o[1], self.o[2], self.h, 1.0, 1.0, 1.0, 1.0, 1.0,
+                       self.u1, self.u2, self.u3)
+        self.ws.step(self.psi, self.u1, self.u2, self.u3, self.h, self.rhr)
+
+    def close(self):
+        self.ws.close()
+
+
+def run_precision_study(args, n=(768, 768, 160), nsteps=500):
+    """FP32 against FP64 on 768x768x160 periodic, the deformational flow through
+    the predictor, gauge iord=2 nonoscillatory, psi = 1 inside [0.25,0.75]^3
+    and 0.1 outside plus 1e-3 U[-1,1] (seed 4): throughput of each, error of
+    FP32 against FP64 after the same steps, FP64-compensated mass drift."""
+    import torch
+    from advectionhpctester_gb300 import mpdata as M
+    nx, ny, nz = n
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(4)
+    noise = (torch.rand((nx, ny, nz), device="cuda", dtype=torch.float64, generator=gen) * 2 - 1) * 1e-3
+
+    def psi_fn(x, y, z):
+        box = (((x >= 0.25) & (x <= 0.75))[:, None, None] & ((y >= 0.25) & (y <= 0.75))[None, :, None]
+               & ((z >= 0.25) & (z <= 0.75))[None, None, :])
+        return torch.where(box, 1.0, 0.1).to(torch.float64) + noise
+
+    out = {"workload": "box_%dx%dx%d_periodic_gauge_iord2_nonos_predictor" % n, "steps": nsteps}
+    arms, mass0 = {}, {}
+    for prec in (64, 32):
+        arm = DevArm(nx, ny, nz, prec, 2, psi_fn)
+        mass0[prec] = M.mass(arm.psi, arm.h)
+        arm.step(0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for k in range(1, nsteps):
+            arm.step(k)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / (nsteps - 1)
+        out["fp%d_gcell_steps_per_s" % prec] = round(nx * ny * nz / (ms * 1e-3) / 1e9, 4)
+        out["fp%d_ms_per_step" % prec] = round(ms, 4)
+        m = M.mass(arm.psi, arm.h)
+        out["fp%d_mass_rel_drift" % prec] = (m - mass0[prec]) / mass0[prec]
+        arms[prec] = arm
+    linf, l2, bmax, bl2 = M.error_norms(arms[32].psi, arms[64].psi)
+    out["fp32_speedup"] = round(out["fp64_ms_per_step"] / out["fp32_ms_per_step"], 3)
+    out["linf_rel_err_fp32_vs_fp64"] = linf / bmax
+    out["l2_rel_err_fp32_vs_fp64"] = l2 / bl2
+    for a in arms.values():
+        a.close()
+    del arms
+    torch.cuda.empty_cache()
     return out
 
 
@@ -572,40 +692,65 @@ def run_batch_study(args, steps=10):
 def run_e2e(arm, args):
     """Same metric through the public API with host buffers: every step copies
     psi, the A-grid Courant numbers, h and rhr from pinned host memory and
-    reads psi back."""
+    reads psi back.  The copies run on their own streams into two alternating
+    device buffer sets, so step n's upload and step n-1's read-back overlap
+    step n's compute; events order each buffer's upload, compute and
+    read-back.  The timed region spans the first upload to the last
+    read-back."""
     torch, M = arm.torch, arm.M
-    stream = torch.cuda.current_stream()
+    comp = torch.cuda.current_stream()
+    up, down = torch.cuda.Stream(), torch.cuda.Stream()
     pin = lambda t: t.detach().cpu().pin_memory()
     hpsi = pin(arm.psi)
     hpat = [pin(p) for p in arm.pats]
     hh, hrhr = pin(arm.h), pin(arm.rhr)
-    out = torch.empty_like(hpsi).pin_memory()
+    outs = [torch.empty_like(hpsi).pin_memory() for _ in range(2)]
     cells = arm.nx * arm.ny * arm.nz
     bi = sum(t.numel() * t.element_size() for t in [hpsi, hh, hrhr] + hpat)
-    bo = out.numel() * out.element_size()
-    steps = max(3, args.steps // 2)
+    bo = outs[0].numel() * outs[0].element_size()
+    steps = max(6, args.steps)
+    bufs = [dict(psi=arm.psi, pats=arm.pats, h=arm.h, rhr=arm.rhr),
+            dict(psi=torch.empty_like(arm.psi), pats=[torch.empty_like(p) for p in arm.pats],
+                 h=torch.empty_like(arm.h), rhr=torch.empty_like(arm.rhr))]
+    ev_in = [torch.cuda.Event() for _ in range(2)]
+    ev_done = [torch.cuda.Event() for _ in range(2)]
+    ev_out = [torch.cuda.Event() for _ in range(2)]
 
-    def one(n):
-        arm.psi.copy_(hpsi, non_blocking=True)
-        for c in range(3):
-            arm.pats[c].copy_(hpat[c], non_blocking=True)
-        arm.h.copy_(hh, non_blocking=True)
-        arm.rhr.copy_(hrhr, non_blocking=True)
-        arm.step(n)
-        out.copy_(arm.psi, non_blocking=True)
+    def issue(n):
+        k = n % 2
+        b = bufs[k]
+        with torch.cuda.stream(up):
+            up.wait_event(ev_out[k])      # step n-2 has been read back from this set
+            b["psi"].copy_(hpsi, non_blocking=True)
+            for c in range(3):
+                b["pats"][c].copy_(hpat[c], non_blocking=True)
+            b["h"].copy_(hh, non_blocking=True)
+            b["rhr"].copy_(hrhr, non_blocking=True)
+            ev_in[k].record(up)
+        comp.wait_event(ev_in[k])
+        arm.step_on(n, b)
+        ev_done[k].record(comp)
+        with torch.cuda.stream(down):
+            down.wait_event(ev_done[k])
+            outs[k].copy_(b["psi"], non_blocking=True)
+            ev_out[k].record(down)
 
-    one(0)
+    for n in range(2):  # warm the streams and buffers
+        issue(n)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
+    e0.record(comp)
+    up.wait_stream(comp)
     for n in range(steps):
-        one(n)
-    e1.record(stream)
+        issue(n)
+    comp.wait_stream(down)
+    e1.record(comp)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     return {"value": round(cells * steps / (ms * 1e-3) / 1e9, 4), "unit": UNIT,
             "h2d_bytes_per_step": int(bi), "d2h_bytes_per_step": int(bo), "steps": steps,
-            "ms_per_step": round(ms / steps, 4)}
+            "ms_per_step": round(ms / steps, 4),
+            "overlap": "double-buffered: upload and read-back streams beside the compute stream"}
 
 
 # --------------------------------------------------------------------------
@@ -688,7 +833,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the FP32, adjoint and batch studies")
+                    help="skip the FP32, adjoint, batch and 768x768x160 precision studies")
+    ap.add_argument("--precision-steps", type=int, default=500,
+                    help="steps of the 768x768x160 FP32-vs-FP64 study")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -704,10 +851,14 @@ def main():
             nx, ny, _ = args.grid
             v, done, total = time_oracle(nx, ny, args.ref_slab, 50, 1, args.precision,
                                          os.cpu_count() or 1, budget_s=15.0)
+            v1, done1, total1 = time_oracle(nx, ny, args.ref_slab, 20, 1, args.precision, 1, budget_s=8.0)
             result["cpu_baseline"] = {
                 "value": round(v, 6), "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
                 "sample": "%d steps (%.1f s) of a %dx%dx%d periodic slab of the same workload, "
-                          "CPU oracle with OpenMP on all host threads" % (done, total, nx, ny, args.ref_slab)}
+                          "CPU oracle with OpenMP on all host threads" % (done, total, nx, ny, args.ref_slab),
+                "single_thread": {"value": round(v1, 6), "cores": 1,
+                                  "sample": "%d steps (%.1f s) of the same slab, one thread (the "
+                                            "reference's CPU build is serial)" % (done1, total1)}}
         print(json.dumps(result), flush=True)
 
 
