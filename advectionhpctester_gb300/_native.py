@@ -72,6 +72,10 @@ SIGNATURES = {
                                   I, I, I, D, D] + [P] * 10 + [I] * 8 + [D] * 4 + [P, P], I),
     "mpdata_velprd_driver_f32": ([ctypes.POINTER(I), ctypes.POINTER(I), I, ctypes.POINTER(F), ctypes.POINTER(F),
                                   I, I, I, F, F] + [P] * 10 + [I] * 8 + [F] * 4 + [P, P], I),
+    "mpdata_pnet_out_chunk_f64": ([ctypes.c_char_p, ctypes.c_char_p] + [I] * 6 + [P] + [I] * 5 + [P], I),
+    "mpdata_pnet_out_chunk_f32": ([ctypes.c_char_p, ctypes.c_char_p] + [I] * 6 + [P] + [I] * 5 + [P], I),
+    "mpdata_pnet_in_chunk_f64": ([ctypes.c_char_p, ctypes.c_char_p, I, P] + [I] * 5 + [P], I),
+    "mpdata_pnet_in_chunk_f32": ([ctypes.c_char_p, ctypes.c_char_p, I, P] + [I] * 5 + [P], I),
     "mpdata_step_noalloc_f64": ([ctypes.POINTER(MpdataGrid), ctypes.POINTER(MpdataOpts)] + [P] * 9, I),
     "mpdata_strerror": ([I], ctypes.c_char_p),
     "mpdata_version": ([], ctypes.c_char_p),

@@ -481,6 +481,7 @@ const char* mpdata_strerror(int code) {
     case MPDATA_E_UNSUPPORTED: return "reference option outside this library's scope";
     case MPDATA_E_TOO_LARGE: return "grid exceeds the 32768-cell scratch of mpdata_step_noalloc_f64";
     case MPDATA_E_COURANT: return "Courant control failed: above the fatal limit while substepping, or not finite";
+    case MPDATA_E_IO: return "field file missing, unreadable, not netCDF classic, or without the variable";
     default: return "unknown error";
   }
 }

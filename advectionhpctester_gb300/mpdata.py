@@ -399,6 +399,42 @@ def velprd_driver(state, ox, oy, oz, u, v, w, uadv, vadv, wadv, h, ipoles, ibcx,
     return tuple(diag)
 
 
+def pnet_out_chunk(var_name, file_name, imode, ifrmd, var, np_, mp, lp, ih, stream=None):
+    """pnet_out_chunk (common/mpi_parallel.f90:7481) for the full 3-D modes
+    (imode 0 float, 1 double, 34 float without time) from a psi-shaped
+    Fortran-ordered CUDA tensor or numpy array; writes netCDF classic
+    (64-bit offset)."""
+    lib = _native.load()
+    dev = torch is not None and isinstance(var, torch.Tensor)
+    if dev:
+        d = var.dtype
+        ptr = _ptr(var, d, shapes(np_, mp, lp, ih)["psi"], "var")
+        f64 = d == torch.float64
+    else:
+        if not var.flags.f_contiguous:
+            raise ValueError("var must be Fortran-ordered")
+        ptr = var.ctypes.data
+        f64 = var.dtype == np.float64
+    fn = lib.mpdata_pnet_out_chunk_f64 if f64 else lib.mpdata_pnet_out_chunk_f32
+    check(fn(var_name.encode(), str(file_name).encode(), int(imode), 0, 0, 0, int(ifrmd), 0, ptr, np_, mp, lp,
+             ih, 1 if dev else 0, _stream(stream) if dev else None), "mpdata_pnet_out_chunk")
+
+
+def pnet_in_chunk(var_name, file_name, ifrmd, var, np_, mp, lp, ih, stream=None):
+    """Frame ifrmd of a netCDF classic variable into the interior of var."""
+    lib = _native.load()
+    dev = torch is not None and isinstance(var, torch.Tensor)
+    if dev:
+        ptr = _ptr(var, var.dtype, shapes(np_, mp, lp, ih)["psi"], "var")
+        f64 = var.dtype == torch.float64
+    else:
+        ptr = var.ctypes.data
+        f64 = var.dtype == np.float64
+    fn = lib.mpdata_pnet_in_chunk_f64 if f64 else lib.mpdata_pnet_in_chunk_f32
+    check(fn(var_name.encode(), str(file_name).encode(), int(ifrmd), ptr, np_, mp, lp, ih, 1 if dev else 0,
+             _stream(stream) if dev else None), "mpdata_pnet_in_chunk")
+
+
 def mass(psi, h, rhr=None, ibc=(1, 1, 1), ih=1, stream=None):
     """FP64 Neumaier-compensated sum(h*psi[/rhr]) over the interior."""
     import ctypes

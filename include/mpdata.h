@@ -43,6 +43,7 @@ extern "C" {
 #define MPDATA_E_UNSUPPORTED -7 /* a reference option outside this library's scope */
 #define MPDATA_E_TOO_LARGE -8   /* grid larger than the fixed scratch of mpdata_step_noalloc_f64 */
 #define MPDATA_E_COURANT -9     /* Courant control failed (above the fatal limit, or not finite) */
+#define MPDATA_E_IO -10         /* field file missing, unreadable, not netCDF classic, or without the variable */
 
 typedef struct {
   int np, mp, lp, ih;   /* interior cells per axis and halo width (ih >= 1) */
@@ -289,6 +290,33 @@ int mpdata_velprd_driver_f32(int* nsubsteps, int* nsubsteps_o, int lsubstepping,
                              const float* h, int ipoles, int ibcx, int ibcy, int ibcz, int np, int mp,
                              int lp, int ih, float dxi, float dyi, float dzi, float dt, double* diag,
                              void* stream);
+
+/* ---- field output and input (netCDF classic, 64-bit offset) --------------
+ * pnet_out_chunk (common/mpi_parallel.f90:7481-8176), single rank, same
+ * argument order plus on_device (1: var is a device pointer, 0: host) and
+ * stream.  imode 0 writes the interior of the psi-shaped var as a float
+ * (x,y,z,t) variable, 1 as a double one, 34 as a float (x,y,z) variable; the
+ * other modes (staggered, halo, planes, lines, points) return
+ * MPDATA_E_UNSUPPORTED, and ia1..ia3/imem are unused.  At ifrmd == 0 the
+ * file, the dimensions x, y, z, t (unlimited) and the variable are created if
+ * absent; the interior is written as frame ifrmd+1 (record ifrmd).  Frames
+ * between the last record and ifrmd hold the netCDF default fill value.  A
+ * variable's slab must stay below 4 GiB (MPDATA_E_TOO_LARGE).  Files are
+ * readable by any netCDF-3 reader.  Synchronises the stream. */
+int mpdata_pnet_out_chunk_f64(const char* var_name, const char* file_name, int imode, int ia1,
+                              int ia2, int ia3, int ifrmd, int imem, const double* var, int np,
+                              int mp, int lp, int ih, int on_device, void* stream);
+int mpdata_pnet_out_chunk_f32(const char* var_name, const char* file_name, int imode, int ia1,
+                              int ia2, int ia3, int ifrmd, int imem, const float* var, int np,
+                              int mp, int lp, int ih, int on_device, void* stream);
+/* No counterpart in the reference (its restarts read netCDF through
+ * PnetCDF): frame ifrmd of a float or double (x,y,z[,t]) variable into the
+ * interior of a psi-shaped var (halo untouched), converted to the array's
+ * precision.  Synchronises the stream. */
+int mpdata_pnet_in_chunk_f64(const char* var_name, const char* file_name, int ifrmd, double* var,
+                             int np, int mp, int lp, int ih, int on_device, void* stream);
+int mpdata_pnet_in_chunk_f32(const char* var_name, const char* file_name, int ifrmd, float* var,
+                             int np, int mp, int lp, int ih, int on_device, void* stream);
 
 /* ---- a step that allocates nothing ----------------------------------------
  * No counterpart in the reference.  For callers that must not have the
