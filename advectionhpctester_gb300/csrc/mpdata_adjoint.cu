@@ -1,18 +1,24 @@
-// Adjoint of the MPDATA step (infinite-gauge form, one corrective pass,
-// nonoscillatory limiter on or off).  No reference code exists for it; it
-// differentiates the forward step of mpdata_body.cuh exactly, with every
-// branch (pp, pn, min3, the limiter's max/min over the 7-point stars, abs)
-// taken at the forward values ("piecewise at the forward branch").
+// Adjoint of the MPDATA step (infinite-gauge form, iord >= 2 corrective
+// passes, nonoscillatory limiter on or off).  No reference code exists for
+// it; it differentiates the forward step of mpdata_body.cuh exactly, with
+// every branch (pp, pn, min3, the limiter's max/min over the 7-point stars
+// and over the running extrema of earlier passes, abs) taken at the forward
+// values ("piecewise at the forward branch").
 //
 // Given psi at the start of a step, the velocities and lambda = dJ/dpsi_new,
-// the step adjoint recomputes the forward intermediates (upwind field, face
-// reciprocals, pseudo-velocities, cp/cn) into the workspace and runs one
-// reverse kernel per forward stage:
-//   update    x_new = rhr*(q - div(w)/h)           -> lambda_xant, lambda_w
+// the step adjoint first records the forward step pass by pass (upwind field,
+// face reciprocals; per pass its input field, pseudo-velocities, limiter
+// ratios, limited velocities and running extrema), then runs one reverse
+// kernel per forward stage, last pass first:
+//   update    x_out = rhr*(q - div(w)/h)           -> lambda_x, lambda_w
 //   limiter   w = pp(v)*A1 - pn(v)*A2              -> lambda_v, lambda_cp, lambda_cn
-//   bounds    cp,cn from the star extrema and v    -> lambda_x, lambda_xant, lambda_v
-//   pseudo    v(xant, u)                           -> lambda_xant, lambda_u
-//   upwind    xant(x, u)                           -> lambda_x, lambda_u
+//   bounds    cp,cn from the extrema and v         -> lambda_x, lambda_v, and lambda of
+//                                                     the step input (first pass) or of
+//                                                     the previous pass's extrema
+//   pseudo    v(x, a)                              -> lambda_x, and lambda_a: the
+//                                                     velocity gradient (first pass) or
+//                                                     the previous pass's lambda_w
+//   upwind    xant(psi, u)                         -> lambda_psi, lambda_u
 // Each reverse kernel walks the forward stage's reads (with the same boundary
 // index maps) and scatters the products of the local partial derivatives
 // with atomic adds, so wall faces (constant zero), mirrored z faces and
@@ -139,13 +145,17 @@ struct Arg {
 template <class R> __device__ __forceinline__ Arg<R> amax(Arg<R> a, Arg<R> b) { return a.v > b.v ? a : b; }
 template <class R> __device__ __forceinline__ Arg<R> amin(Arg<R> a, Arg<R> b) { return a.v < b.v ? a : b; }
 
-template <class R>
+// FIRST: the fold starts from the step input's star (ids 0..6); later passes
+// start from the previous pass's running extrema (id 14).  The current
+// field's star is ids 7..13.  The adjoint of this pass's extrema is the
+// cp/cn part plus what the next pass carried back (lmx, lmn).
+template <class R, bool FIRST>
 __global__ void __launch_bounds__(128) ka_bounds(const Prob<R> P, const AdjArr<R> A) {
   ACELL
   const bool lo = g.bz || k > 1, hi = g.bz || k < g.lp;
   const Arr<R>& X = P.xant;
   const Arr<R>& xin = P.psi;
-  // star cells: x_in with the zero-gradient map, xant with the reflection map
+  // star cells: x_in with the zero-gradient map, the current field with the reflection map
   const int im = g.bx ? wrapi(i - 1, g.np) : clampi(i - 1, g.np);
   const int ip = g.bx ? wrapi(i + 1, g.np) : clampi(i + 1, g.np);
   const int jm = g.by ? wrapi(j - 1, g.mp) : clampi(j - 1, g.mp);
@@ -153,17 +163,23 @@ __global__ void __launch_bounds__(128) ka_bounds(const Prob<R> P, const AdjArr<R
   const int km = cz(g, k - 1), kp = cz(g, k + 1);
   const int ri_m = g.bx ? wrapi(i - 1, g.np) : refl(i - 1, g.np), ri_p = g.bx ? wrapi(i + 1, g.np) : refl(i + 1, g.np);
   const int rj_m = g.by ? wrapi(j - 1, g.mp) : refl(j - 1, g.mp), rj_p = g.by ? wrapi(j + 1, g.mp) : refl(j + 1, g.mp);
-  // element table: (i,j,k) of ids 0..13
-  const int ci[14] = {im, i, ip, i, i, i, i, ri_m, i, ri_p, i, i, i, i};
-  const int cj[14] = {j, j, j, jm, jp, j, j, j, j, j, rj_m, rj_p, j, j};
-  const int ck[14] = {k, k, k, k, k, km, kp, k, k, k, k, k, km, kp};
+  // element table: (i,j,k) of ids 0..13; id 14 is the previous extremum at (i,j,k)
+  const int ci[15] = {im, i, ip, i, i, i, i, ri_m, i, ri_p, i, i, i, i, i};
+  const int cj[15] = {j, j, j, jm, jp, j, j, j, j, j, rj_m, rj_p, j, j, j};
+  const int ck[15] = {k, k, k, k, k, km, kp, k, k, k, k, k, km, kp, k};
   Arg<R> e[14];
-  for (int n = 0; n < 7; n++) e[n] = Arg<R>{xin.ld(ci[n], cj[n], ck[n]), n};
   for (int n = 7; n < 14; n++) e[n] = Arg<R>{X.ld(ci[n], cj[n], ck[n]), n};
-  Arg<R> ma = amax(amax(amax(e[0], e[1]), amax(e[2], e[3])), e[4]);
-  Arg<R> mi = amin(amin(amin(e[0], e[1]), amin(e[2], e[3])), e[4]);
-  if (lo) { ma = amax(ma, e[5]); mi = amin(mi, e[5]); }
-  if (hi) { ma = amax(ma, e[6]); mi = amin(mi, e[6]); }
+  Arg<R> ma, mi;
+  if (FIRST) {
+    for (int n = 0; n < 7; n++) e[n] = Arg<R>{xin.ld(ci[n], cj[n], ck[n]), n};
+    ma = amax(amax(amax(e[0], e[1]), amax(e[2], e[3])), e[4]);
+    mi = amin(amin(amin(e[0], e[1]), amin(e[2], e[3])), e[4]);
+    if (lo) { ma = amax(ma, e[5]); mi = amin(mi, e[5]); }
+    if (hi) { ma = amax(ma, e[6]); mi = amin(mi, e[6]); }
+  } else {
+    ma = Arg<R>{A.mxp.ld(i, j, k), 14};
+    mi = Arg<R>{A.mnp.ld(i, j, k), 14};
+  }
   ma = amax(amax(amax(ma, e[7]), amax(e[8], e[9])), amax(e[10], e[11]));
   mi = amin(amin(amin(mi, e[7]), amin(e[8], e[9])), amin(e[10], e[11]));
   if (lo) { ma = amax(ma, e[12]); mi = amin(mi, e[12]); }
@@ -179,11 +195,12 @@ __global__ void __launch_bounds__(128) ka_bounds(const Prob<R> P, const AdjArr<R
   const R Dn = pp(e1) + pn(w1) + pp(e2) + pn(w2) + pp(e3) + pn(w3) + ep;
   const R cpv = (ma.v - x) * hc / Dp, cnv = (x - mi.v) * hc / Dn;
   const R lnum_p = lcp * hc / Dp, lnum_n = lcn * hc / Dn;
-  // d cp/d mx, d cp/d x, d cn/d x, d cn/d mn
-  const Arr<R>& Lmax = ma.id < 7 ? A.lx : A.lxant;
-  const Arr<R>& Lmin = mi.id < 7 ? A.lx : A.lxant;
-  addat(Lmax, ci[ma.id], cj[ma.id], ck[ma.id], lnum_p);
-  addat(Lmin, ci[mi.id], cj[mi.id], ck[mi.id], -lnum_n);
+  // d cp/d mx, d cn/d mn (plus the carried adjoints of the extrema), d/d x
+  const R lma = lnum_p + A.lmx.ld(i, j, k), lmi = -lnum_n + A.lmn.ld(i, j, k);
+  if (ma.id == 14) addat(A.lmxp, i, j, k, lma);
+  else addat(ma.id < 7 ? A.lx : A.lxant, ci[ma.id], cj[ma.id], ck[ma.id], lma);
+  if (mi.id == 14) addat(A.lmnp, i, j, k, lmi);
+  else addat(mi.id < 7 ? A.lx : A.lxant, ci[mi.id], cj[mi.id], ck[mi.id], lmi);
   addat(A.lxant, i, j, k, lnum_n - lnum_p);
   // d/dD: -c/D
   const R lDp = -lcp * cpv / Dp, lDn = -lcn * cnv / Dn;
@@ -197,115 +214,121 @@ __global__ void __launch_bounds__(128) ka_bounds(const Prob<R> P, const AdjArr<R
 }
 
 // ---- pseudo-velocity (gauge): v = vdyf(xl,xr,a,hm) - 0.125*a*hm*cr ------------
-// cr = S2*rat4(y0,y1,y2,y3) [+ S3*rat4(z0,z1,z2,z3)], S = sums of four u faces.
-template <class R>
+// cr = S2*rat4(y0,y1,y2,y3) [+ S3*rat4(z0,z1,z2,z3)], S = sums of four a faces.
+// AIN: a = the caller's Courant numbers (gradient into gu); otherwise a = the
+// previous pass's limited velocities, read with the wall rule (gradient into
+// that pass's lambda_w).
+template <class R, bool AIN>
 __global__ void __launch_bounds__(128) ka_pseudo(const Prob<R> P, const AdjArr<R> A) {
   ACELL
   const Arr<R>& X = P.xant;
+  const Arr<R>& U1 = AIN ? P.u1 : P.w1;
+  const Arr<R>& U2 = AIN ? P.u2 : P.w2;
+  const Arr<R>& U3 = AIN ? P.u3 : P.w3;
   const bool zt = g.bz || (k > 1 && k < g.lp);
 #define XX(a, b, c) xr<R>(g, X, (a), (b), (c))
 #define LX(a, b, c, v) xr_add<R>(g, A.lxant, (a), (b), (c), (v))
   // x faces
   if (g.bx || i > 1) {
     const R lv = A.lv1.ld(i, j, k);
-    const R hm = P.hmx.ld(i, j, k), a = fx<R, true>(g, P.u1, i, j, k);
+    const R hm = P.hmx.ld(i, j, k), a = fx<R, AIN>(g, U1, i, j, k);
     const R xl = XX(i - 1, j, k), xrr = XX(i, j, k);
-    const R S2 = fy<R, true>(g, P.u2, i - 1, j, k) + fy<R, true>(g, P.u2, i - 1, j + 1, k) +
-                 fy<R, true>(g, P.u2, i, j + 1, k) + fy<R, true>(g, P.u2, i, j, k);
+    const R S2 = fy<R, AIN>(g, U2, i - 1, j, k) + fy<R, AIN>(g, U2, i - 1, j + 1, k) +
+                 fy<R, AIN>(g, U2, i, j + 1, k) + fy<R, AIN>(g, U2, i, j, k);
     const R R2 = rat4(XX(i - 1, j - 1, k), XX(i, j - 1, k), XX(i - 1, j + 1, k), XX(i, j + 1, k));
     R cr = S2 * R2, S3 = R(0), R3 = R(0);
     if (zt) {
-      S3 = fz<R, true>(g, P.u3, i - 1, j, k) + fz<R, true>(g, P.u3, i - 1, j, k + 1) +
-           fz<R, true>(g, P.u3, i, j, k + 1) + fz<R, true>(g, P.u3, i, j, k);
+      S3 = fz<R, AIN>(g, U3, i - 1, j, k) + fz<R, AIN>(g, U3, i - 1, j, k + 1) +
+           fz<R, AIN>(g, U3, i, j, k + 1) + fz<R, AIN>(g, U3, i, j, k);
       R3 = rat4(XX(i - 1, j, k - 1), XX(i, j, k - 1), XX(i - 1, j, k + 1), XX(i, j, k + 1));
       cr = cr + S3 * R3;
     }
     const R K = (fabs(a) - a * a * hm) * R(0.5);
     const R la = lv * ((dabs(a) - R(2) * a * hm) * (xrr - xl) * R(0.5) - R(0.125) * hm * cr);
-    fx_add<R, true>(g, A.gu1, i, j, k, la);
+    fx_add<R, AIN>(g, A.la1, i, j, k, la);
     LX(i, j, k, lv * K);
     LX(i - 1, j, k, -lv * K);
     const R lcr = -lv * R(0.125) * a * hm;
     const R lS2 = lcr * R2, lR2 = lcr * S2 * R(0.25);
-    fy_add<R, true>(g, A.gu2, i - 1, j, k, lS2);
-    fy_add<R, true>(g, A.gu2, i - 1, j + 1, k, lS2);
-    fy_add<R, true>(g, A.gu2, i, j + 1, k, lS2);
-    fy_add<R, true>(g, A.gu2, i, j, k, lS2);
+    fy_add<R, AIN>(g, A.la2, i - 1, j, k, lS2);
+    fy_add<R, AIN>(g, A.la2, i - 1, j + 1, k, lS2);
+    fy_add<R, AIN>(g, A.la2, i, j + 1, k, lS2);
+    fy_add<R, AIN>(g, A.la2, i, j, k, lS2);
     LX(i, j + 1, k, lR2); LX(i - 1, j + 1, k, lR2); LX(i, j - 1, k, -lR2); LX(i - 1, j - 1, k, -lR2);
     if (zt) {
       const R lS3 = lcr * R3, lR3 = lcr * S3 * R(0.25);
-      fz_add<R, true>(g, A.gu3, i - 1, j, k, lS3);
-      fz_add<R, true>(g, A.gu3, i - 1, j, k + 1, lS3);
-      fz_add<R, true>(g, A.gu3, i, j, k + 1, lS3);
-      fz_add<R, true>(g, A.gu3, i, j, k, lS3);
+      fz_add<R, AIN>(g, A.la3, i - 1, j, k, lS3);
+      fz_add<R, AIN>(g, A.la3, i - 1, j, k + 1, lS3);
+      fz_add<R, AIN>(g, A.la3, i, j, k + 1, lS3);
+      fz_add<R, AIN>(g, A.la3, i, j, k, lS3);
       LX(i, j, k + 1, lR3); LX(i - 1, j, k + 1, lR3); LX(i, j, k - 1, -lR3); LX(i - 1, j, k - 1, -lR3);
     }
   }
   // y faces
   if (g.by || j > 1) {
     const R lv = A.lv2.ld(i, j, k);
-    const R hm = P.hmy.ld(i, j, k), a = fy<R, true>(g, P.u2, i, j, k);
+    const R hm = P.hmy.ld(i, j, k), a = fy<R, AIN>(g, U2, i, j, k);
     const R xl = XX(i, j - 1, k), xrr = XX(i, j, k);
-    const R S1 = fx<R, true>(g, P.u1, i, j - 1, k) + fx<R, true>(g, P.u1, i, j, k) +
-                 fx<R, true>(g, P.u1, i + 1, j, k) + fx<R, true>(g, P.u1, i + 1, j - 1, k);
+    const R S1 = fx<R, AIN>(g, U1, i, j - 1, k) + fx<R, AIN>(g, U1, i, j, k) +
+                 fx<R, AIN>(g, U1, i + 1, j, k) + fx<R, AIN>(g, U1, i + 1, j - 1, k);
     const R R1 = rat4(XX(i - 1, j - 1, k), XX(i - 1, j, k), XX(i + 1, j - 1, k), XX(i + 1, j, k));
     R cr = S1 * R1, S3 = R(0), R3 = R(0);
     if (zt) {
-      S3 = fz<R, true>(g, P.u3, i, j - 1, k) + fz<R, true>(g, P.u3, i, j, k) +
-           fz<R, true>(g, P.u3, i, j, k + 1) + fz<R, true>(g, P.u3, i, j - 1, k + 1);
+      S3 = fz<R, AIN>(g, U3, i, j - 1, k) + fz<R, AIN>(g, U3, i, j, k) +
+           fz<R, AIN>(g, U3, i, j, k + 1) + fz<R, AIN>(g, U3, i, j - 1, k + 1);
       R3 = rat4(XX(i, j - 1, k - 1), XX(i, j, k - 1), XX(i, j - 1, k + 1), XX(i, j, k + 1));
       cr = cr + S3 * R3;
     }
     const R K = (fabs(a) - a * a * hm) * R(0.5);
     const R la = lv * ((dabs(a) - R(2) * a * hm) * (xrr - xl) * R(0.5) - R(0.125) * hm * cr);
-    fy_add<R, true>(g, A.gu2, i, j, k, la);
+    fy_add<R, AIN>(g, A.la2, i, j, k, la);
     LX(i, j, k, lv * K);
     LX(i, j - 1, k, -lv * K);
     const R lcr = -lv * R(0.125) * a * hm;
     const R lS1 = lcr * R1, lR1 = lcr * S1 * R(0.25);
-    fx_add<R, true>(g, A.gu1, i, j - 1, k, lS1);
-    fx_add<R, true>(g, A.gu1, i, j, k, lS1);
-    fx_add<R, true>(g, A.gu1, i + 1, j, k, lS1);
-    fx_add<R, true>(g, A.gu1, i + 1, j - 1, k, lS1);
+    fx_add<R, AIN>(g, A.la1, i, j - 1, k, lS1);
+    fx_add<R, AIN>(g, A.la1, i, j, k, lS1);
+    fx_add<R, AIN>(g, A.la1, i + 1, j, k, lS1);
+    fx_add<R, AIN>(g, A.la1, i + 1, j - 1, k, lS1);
     LX(i + 1, j, k, lR1); LX(i + 1, j - 1, k, lR1); LX(i - 1, j, k, -lR1); LX(i - 1, j - 1, k, -lR1);
     if (zt) {
       const R lS3 = lcr * R3, lR3 = lcr * S3 * R(0.25);
-      fz_add<R, true>(g, A.gu3, i, j - 1, k, lS3);
-      fz_add<R, true>(g, A.gu3, i, j, k, lS3);
-      fz_add<R, true>(g, A.gu3, i, j, k + 1, lS3);
-      fz_add<R, true>(g, A.gu3, i, j - 1, k + 1, lS3);
+      fz_add<R, AIN>(g, A.la3, i, j - 1, k, lS3);
+      fz_add<R, AIN>(g, A.la3, i, j, k, lS3);
+      fz_add<R, AIN>(g, A.la3, i, j, k + 1, lS3);
+      fz_add<R, AIN>(g, A.la3, i, j - 1, k + 1, lS3);
       LX(i, j, k + 1, lR3); LX(i, j - 1, k + 1, lR3); LX(i, j, k - 1, -lR3); LX(i, j - 1, k - 1, -lR3);
     }
   }
   // z faces
   if (g.bz || k > 1) {
     const R lv = A.lv3.ld(i, j, k);
-    const R hm = P.hmz.ld(i, j, k), a = fz<R, true>(g, P.u3, i, j, k);
+    const R hm = P.hmz.ld(i, j, k), a = fz<R, AIN>(g, U3, i, j, k);
     const R xl = XX(i, j, k - 1), xrr = XX(i, j, k);
-    const R S1 = fx<R, true>(g, P.u1, i, j, k - 1) + fx<R, true>(g, P.u1, i, j, k) +
-                 fx<R, true>(g, P.u1, i + 1, j, k) + fx<R, true>(g, P.u1, i + 1, j, k - 1);
+    const R S1 = fx<R, AIN>(g, U1, i, j, k - 1) + fx<R, AIN>(g, U1, i, j, k) +
+                 fx<R, AIN>(g, U1, i + 1, j, k) + fx<R, AIN>(g, U1, i + 1, j, k - 1);
     const R R1 = rat4(XX(i - 1, j, k - 1), XX(i - 1, j, k), XX(i + 1, j, k - 1), XX(i + 1, j, k));
-    const R S2 = fy<R, true>(g, P.u2, i, j, k - 1) + fy<R, true>(g, P.u2, i, j + 1, k - 1) +
-                 fy<R, true>(g, P.u2, i, j + 1, k) + fy<R, true>(g, P.u2, i, j, k);
+    const R S2 = fy<R, AIN>(g, U2, i, j, k - 1) + fy<R, AIN>(g, U2, i, j + 1, k - 1) +
+                 fy<R, AIN>(g, U2, i, j + 1, k) + fy<R, AIN>(g, U2, i, j, k);
     const R R2 = rat4(XX(i, j - 1, k - 1), XX(i, j - 1, k), XX(i, j + 1, k - 1), XX(i, j + 1, k));
     const R cr = S1 * R1 + S2 * R2;
     const R K = (fabs(a) - a * a * hm) * R(0.5);
     const R la = lv * ((dabs(a) - R(2) * a * hm) * (xrr - xl) * R(0.5) - R(0.125) * hm * cr);
-    fz_add<R, true>(g, A.gu3, i, j, k, la);
+    fz_add<R, AIN>(g, A.la3, i, j, k, la);
     LX(i, j, k, lv * K);
     LX(i, j, k - 1, -lv * K);
     const R lcr = -lv * R(0.125) * a * hm;
     const R lS1 = lcr * R1, lR1 = lcr * S1 * R(0.25);
-    fx_add<R, true>(g, A.gu1, i, j, k - 1, lS1);
-    fx_add<R, true>(g, A.gu1, i, j, k, lS1);
-    fx_add<R, true>(g, A.gu1, i + 1, j, k, lS1);
-    fx_add<R, true>(g, A.gu1, i + 1, j, k - 1, lS1);
+    fx_add<R, AIN>(g, A.la1, i, j, k - 1, lS1);
+    fx_add<R, AIN>(g, A.la1, i, j, k, lS1);
+    fx_add<R, AIN>(g, A.la1, i + 1, j, k, lS1);
+    fx_add<R, AIN>(g, A.la1, i + 1, j, k - 1, lS1);
     LX(i + 1, j, k, lR1); LX(i + 1, j, k - 1, lR1); LX(i - 1, j, k, -lR1); LX(i - 1, j, k - 1, -lR1);
     const R lS2 = lcr * R2, lR2 = lcr * S2 * R(0.25);
-    fy_add<R, true>(g, A.gu2, i, j, k - 1, lS2);
-    fy_add<R, true>(g, A.gu2, i, j + 1, k - 1, lS2);
-    fy_add<R, true>(g, A.gu2, i, j + 1, k, lS2);
-    fy_add<R, true>(g, A.gu2, i, j, k, lS2);
+    fy_add<R, AIN>(g, A.la2, i, j, k - 1, lS2);
+    fy_add<R, AIN>(g, A.la2, i, j + 1, k - 1, lS2);
+    fy_add<R, AIN>(g, A.la2, i, j + 1, k, lS2);
+    fy_add<R, AIN>(g, A.la2, i, j, k, lS2);
     LX(i, j + 1, k, lR2); LX(i, j + 1, k - 1, lR2); LX(i, j - 1, k, -lR2); LX(i, j - 1, k - 1, -lR2);
   }
 #undef XX
@@ -378,51 +401,151 @@ __global__ void __launch_bounds__(128) ka_seed(const Prob<R> P, const Arr<R> psi
   lam.at(i, j, k) = psi.ld(i, j, k) - target.ld(i, j, k);
 }
 
-// forward recompute kernels (psi's halo is left untouched: HALO=false)
+// forward record kernels (psi's halo is left untouched: HALO=false)
 template <class R>
 __global__ void __launch_bounds__(128) kf_upwind(const Prob<R> P) {
   ACELL
   (void)g;
   upwind_body<R, true, false>(P, i, j, k);
 }
-template <class R>
+template <class R, bool AIN>
 __global__ void __launch_bounds__(128) kf_pseudo(const Prob<R> P) {
   ACELL
   (void)g;
-  pseudo_body<R, true>(P, i, j, k);
+  pseudo_body<R, AIN>(P, i, j, k);
 }
-template <class R, bool NONOS>
+template <class R, bool NONOS, bool FIRST, bool KEEP>
 __global__ void __launch_bounds__(128) kf_bounds(const Prob<R> P) {
   ACELL
   (void)g;
-  bounds_body<R, NONOS, true, false>(P, i, j, k);
+  bounds_body<R, NONOS, FIRST, KEEP>(P, i, j, k);
+}
+template <class R, bool NONOS>
+__global__ void __launch_bounds__(128) kf_limit(const Prob<R> P) {
+  ACELL
+  (void)g;
+  limit_body<R, NONOS>(P, i, j, k);
+}
+template <class R>
+__global__ void __launch_bounds__(128) kf_update(const Prob<R> P) {
+  ACELL
+  (void)g;
+  update_body<R, false>(P, i, j, k);
 }
 
-// Forward recompute (upwind, pseudo-velocity, bounds; the update itself is
-// not needed) into P's scratch, then the reverse kernels.  nonos=0 skips the
-// limiter's adjoint (w = v).  `zero` must point at the nine contiguous
-// atomic accumulators lv1..lv3, lw1..lw3, lcp, lcn, lx (9*ncell elements).
+// The values of pass t: its input field, pseudo-velocities, ratios and
+// extrema from the records; `a` selects the "a" velocities the pass's
+// pseudo-velocity read (the previous pass's limited ones) or its own
+// limited velocities (for the limiter's forward).
 template <class R>
-int run_step_adjoint(const Prob<R>& P, const AdjArr<R>& A, int nonos, R* zero, size_t ncell, cudaStream_t s) {
+Prob<R> pass_prob(const Prob<R>& P, const AdjPlan<R>& A, int t, bool prev_w) {
+  Prob<R> Q = P;
+  Q.xant = A.x[t];
+  Q.v1 = A.v[t][0];
+  Q.v2 = A.v[t][1];
+  Q.v3 = A.v[t][2];
+  Q.cp = A.cp[t];
+  Q.cn = A.cn[t];
+  Q.mx = A.mx[t];
+  Q.mn = A.mn[t];
+  const int tw = prev_w ? (t > 0 ? t - 1 : 0) : t;
+  Q.w1 = A.w[tw][0];
+  Q.w2 = A.w[tw][1];
+  Q.w3 = A.w[tw][2];
+  return Q;
+}
+
+template <class R>
+int run_step_adjoint(const Prob<R>& P, const AdjPlan<R>& A, int nonos, cudaStream_t s) {
   const Geo& g = P.g;
   const dim3 blk(32, 4, 1);
   const dim3 grd((g.np + 31) / 32, (g.mp + 3) / 4, g.lp);
-  if (cudaMemsetAsync(zero, 0, 9 * ncell * sizeof(R), s) != cudaSuccess) return -5;
-  kf_upwind<R><<<grd, blk, 0, s>>>(P);
-  kf_pseudo<R><<<grd, blk, 0, s>>>(P);
-  if (nonos) kf_bounds<R, true><<<grd, blk, 0, s>>>(P);
-  else kf_bounds<R, false><<<grd, blk, 0, s>>>(P);
-  ka_update<R><<<grd, blk, 0, s>>>(P, A);
-  if (nonos) {
-    ka_limit<R, true><<<grd, blk, 0, s>>>(P, A);
-    ka_bounds<R><<<grd, blk, 0, s>>>(P, A);
-  } else {
-    ka_limit<R, false><<<grd, blk, 0, s>>>(P, A);
+  const int np_ = A.npass;
+  const bool keep = np_ > 1;
+  const size_t ncell = (size_t)g.np * g.mp * g.lp;
+  int n = 0;
+  if (cudaMemsetAsync(A.acc, 0, A.acc_elems * sizeof(R), s) != cudaSuccess) return -5;
+  // ---- forward records
+  Prob<R> F = P;
+  F.xant = A.x[0];
+  kf_upwind<R><<<grd, blk, 0, s>>>(F);
+  n++;
+  for (int t = 0; t < np_; t++) {
+    const Prob<R> Qa = pass_prob(P, A, t, true);
+    if (t == 0) kf_pseudo<R, true><<<grd, blk, 0, s>>>(Qa);
+    else kf_pseudo<R, false><<<grd, blk, 0, s>>>(Qa);
+    const Prob<R> Q = pass_prob(P, A, t, false);
+    if (nonos && keep && t > 0) {  // the running extrema continue from the previous pass
+      if (cudaMemcpyAsync(A.mx[t].p, A.mx[t - 1].p, ncell * sizeof(R), cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+          cudaMemcpyAsync(A.mn[t].p, A.mn[t - 1].p, ncell * sizeof(R), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+        return -5;
+    }
+    if (!nonos) kf_bounds<R, false, true, false><<<grd, blk, 0, s>>>(Q);
+    else if (!keep) kf_bounds<R, true, true, false><<<grd, blk, 0, s>>>(Q);
+    else if (t == 0) kf_bounds<R, true, true, true><<<grd, blk, 0, s>>>(Q);
+    else kf_bounds<R, true, false, true><<<grd, blk, 0, s>>>(Q);
+    if (nonos) kf_limit<R, true><<<grd, blk, 0, s>>>(Q);
+    else kf_limit<R, false><<<grd, blk, 0, s>>>(Q);
+    n += 3;
+    if (t < np_ - 1) {
+      Prob<R> U = Q;
+      U.xant = A.x[t + 1];
+      kf_update<R><<<grd, blk, 0, s>>>(U);
+      n++;
+    }
   }
-  ka_pseudo<R><<<grd, blk, 0, s>>>(P, A);
-  ka_upwind<R><<<grd, blk, 0, s>>>(P, A);
-  ka_store<R><<<grd, blk, 0, s>>>(P, A);
-  add_launches(nonos ? 9 : 8);
+  // ---- reverse, last pass first
+  for (int t = np_ - 1; t >= 0; t--) {
+    if (t < np_ - 1 && cudaMemsetAsync(A.pass_acc, 0, A.pass_acc_elems * sizeof(R), s) != cudaSuccess) return -5;
+    const Prob<R> Q = pass_prob(P, A, t, true);
+    AdjArr<R> a{};
+    a.lxant = A.lx[t];
+    a.lv1 = A.lv[0];
+    a.lv2 = A.lv[1];
+    a.lv3 = A.lv[2];
+    a.lw1 = A.lw[t][0];
+    a.lw2 = A.lw[t][1];
+    a.lw3 = A.lw[t][2];
+    a.lcp = A.lcp;
+    a.lcn = A.lcn;
+    a.lx = A.lxin;
+    a.lam = t == np_ - 1 ? A.lam : A.lx[t + 1];
+    a.gu1 = A.gu1;
+    a.gu2 = A.gu2;
+    a.gu3 = A.gu3;
+    a.la1 = t == 0 ? A.gu1 : A.lw[t - 1][0];
+    a.la2 = t == 0 ? A.gu2 : A.lw[t - 1][1];
+    a.la3 = t == 0 ? A.gu3 : A.lw[t - 1][2];
+    a.lmx = A.lmx[t];
+    a.lmn = A.lmn[t];
+    a.lmxp = A.lmx[t > 0 ? t - 1 : 0];
+    a.lmnp = A.lmn[t > 0 ? t - 1 : 0];
+    a.mxp = A.mx[t > 0 ? t - 1 : 0];
+    a.mnp = A.mn[t > 0 ? t - 1 : 0];
+    ka_update<R><<<grd, blk, 0, s>>>(Q, a);
+    if (nonos) {
+      ka_limit<R, true><<<grd, blk, 0, s>>>(Q, a);
+      if (t == 0) ka_bounds<R, true><<<grd, blk, 0, s>>>(Q, a);
+      else ka_bounds<R, false><<<grd, blk, 0, s>>>(Q, a);
+      n++;
+    } else {
+      ka_limit<R, false><<<grd, blk, 0, s>>>(Q, a);
+    }
+    if (t == 0) ka_pseudo<R, true><<<grd, blk, 0, s>>>(Q, a);
+    else ka_pseudo<R, false><<<grd, blk, 0, s>>>(Q, a);
+    n += 3;
+  }
+  AdjArr<R> a0{};
+  a0.lxant = A.lx[0];
+  a0.lx = A.lxin;
+  a0.gu1 = A.gu1;
+  a0.gu2 = A.gu2;
+  a0.gu3 = A.gu3;
+  a0.lam = A.lam;
+  ka_upwind<R><<<grd, blk, 0, s>>>(P, a0);
+  ka_store<R><<<grd, blk, 0, s>>>(P, a0);
+  n += 2;
+  add_launches(n);
   return cudaGetLastError() == cudaSuccess ? 0 : -5;
 }
 
@@ -436,8 +559,8 @@ int run_seed(const Prob<R>& P, const Arr<R>& psi, const Arr<R>& target, const Ar
   return cudaGetLastError() == cudaSuccess ? 0 : -5;
 }
 
-template int run_step_adjoint<double>(const Prob<double>&, const AdjArr<double>&, int, double*, size_t, cudaStream_t);
-template int run_step_adjoint<float>(const Prob<float>&, const AdjArr<float>&, int, float*, size_t, cudaStream_t);
+template int run_step_adjoint<double>(const Prob<double>&, const AdjPlan<double>&, int, cudaStream_t);
+template int run_step_adjoint<float>(const Prob<float>&, const AdjPlan<float>&, int, cudaStream_t);
 template int run_seed<double>(const Prob<double>&, const Arr<double>&, const Arr<double>&, const Arr<double>&, cudaStream_t);
 template int run_seed<float>(const Prob<float>&, const Arr<float>&, const Arr<float>&, const Arr<float>&, cudaStream_t);
 

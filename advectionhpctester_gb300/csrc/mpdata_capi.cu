@@ -934,13 +934,15 @@ int mpdata_error_norms(const mpdata_grid* grid, const void* a, int a_is_f64, con
 namespace {
 
 template <class R>
-int adj_plan(Workspace* w, Prob<R>* P, AdjArr<R>* A, const R* psi_in, const R* u1, const R* u2, const R* u3,
+int adj_plan(Workspace* w, Prob<R>* P, AdjPlan<R>* A, const R* psi_in, const R* u1, const R* u2, const R* u3,
              const R* h, const R* rhr, const R* bcx, const R* bcy, R* lambda, R* gu1, R* gu2, R* gu3) {
   if (w->elem != sizeof(R)) return MPDATA_E_WS;
-  if (!w->o.gauge || w->o.iord != 2) return MPDATA_E_UNSUPPORTED;  // gauge form, one corrective pass
+  const int iord = w->o.iord;
+  if (!w->o.gauge || iord < 2 || iord - 1 > kAdjMaxPass) return MPDATA_E_UNSUPPORTED;  // gauge form only
   if (!psi_in || !u1 || !u2 || !u3 || !h || !rhr || !lambda || !gu1 || !gu2 || !gu3) return MPDATA_E_NULL;
   if ((!w->g.ibcx && !bcx) || (!w->g.ibcy && !bcy)) return MPDATA_E_NULL;
-  if (!w->adj && cudaMalloc(&w->adj, 10 * w->ncell * w->elem) != cudaSuccess) {
+  const size_t nrec = adj_record_fields(iord), nacc = adj_acc_fields(iord), n = w->ncell;
+  if (!w->adj && cudaMalloc(&w->adj, (nrec + nacc) * n * w->elem) != cudaSuccess) {
     cudaGetLastError();
     w->adj = nullptr;
     return MPDATA_E_CUDA;
@@ -951,8 +953,32 @@ int adj_plan(Workspace* w, Prob<R>* P, AdjArr<R>* A, const R* psi_in, const R* u
   const mpdata_grid& g = w->g;
   const int ih = g.ih, sx = g.np + 2 * ih, sy = g.mp + 2 * ih;
   R* a = static_cast<R*>(w->adj);
-  Arr<R>* slots[10] = {&A->lv1, &A->lv2, &A->lv3, &A->lw1, &A->lw2, &A->lw3, &A->lcp, &A->lcn, &A->lx, &A->lxant};
-  for (int f = 0; f < 10; f++) *slots[f] = scratch_view<R>(a + (size_t)f * w->ncell, P->g);
+  size_t f = 0;
+  auto next = [&]() { return scratch_view<R>(a + (f++) * n, P->g); };
+  A->npass = iord - 1;
+  for (int t = 0; t < A->npass; t++) {
+    A->x[t] = next();
+    for (int c = 0; c < 3; c++) A->v[t][c] = next();
+    for (int c = 0; c < 3; c++) A->w[t][c] = next();
+    A->cp[t] = next();
+    A->cn[t] = next();
+    A->mx[t] = next();
+    A->mn[t] = next();
+  }
+  A->acc = a + f * n;  // the accumulators, contiguous
+  for (int t = 0; t < A->npass; t++) {
+    A->lx[t] = next();
+    for (int c = 0; c < 3; c++) A->lw[t][c] = next();
+    A->lmx[t] = next();
+    A->lmn[t] = next();
+  }
+  A->pass_acc = a + f * n;
+  for (int c = 0; c < 3; c++) A->lv[c] = next();
+  A->lcp = next();
+  A->lcn = next();
+  A->pass_acc_elems = 5 * n;
+  A->lxin = next();
+  A->acc_elems = (size_t)(a + f * n - A->acc);
   A->lam = caller_view<R>(lambda, ih, sx, sy);
   A->gu1 = caller_view<R>(gu1, ih, sx + 1, sy);
   A->gu2 = caller_view<R>(gu2, ih, sx, sy + 1);
@@ -966,12 +992,12 @@ int step_adjoint_impl(void* ws, const R* psi_in, const R* u1, const R* u2, const
   Workspace* w = as_ws(ws);
   if (!w) return MPDATA_E_WS;
   Prob<R> P;
-  AdjArr<R> A;
+  AdjPlan<R> A;
   int rc = adj_plan<R>(w, &P, &A, psi_in, u1, u2, u3, h, rhr, bcx, bcy, lambda, gu1, gu2, gu3);
   if (rc) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   w->last = s;
-  return run_step_adjoint<R>(P, A, w->o.nonos, static_cast<R*>(w->adj), w->ncell, s) ? MPDATA_E_CUDA : MPDATA_OK;
+  return run_step_adjoint<R>(P, A, w->o.nonos, s) ? MPDATA_E_CUDA : MPDATA_OK;
 }
 
 // J = 0.5*|psi_N - target|^2 and its gradients over nsteps steps, with
@@ -988,7 +1014,7 @@ int adjoint_run_impl(void* ws, int nsteps, int interval, R* psi, const R* u1, co
   if (nsteps < 1 || interval < 0) return MPDATA_E_OPTS;
   if (!psi || !target || !J || !g_psi0) return MPDATA_E_NULL;
   Prob<R> P;
-  AdjArr<R> A;
+  AdjPlan<R> A;
   int rc = adj_plan<R>(w, &P, &A, psi, u1, u2, u3, h, rhr, bcx, bcy, g_psi0, gu1, gu2, gu3);
   if (rc) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -1016,12 +1042,14 @@ int adjoint_run_impl(void* ws, int nsteps, int interval, R* psi, const R* u1, co
     return MPDATA_E_CUDA;
   }
   if (peak_bytes)
-    *peak_bytes = (long long)(pbytes * (nck + K)) + (long long)(w->ncell * w->elem * (NSCRATCH + 10));
+    *peak_bytes = (long long)(pbytes * (nck + K)) +
+                  (long long)(w->ncell * w->elem *
+                              (NSCRATCH + adj_record_fields(w->o.iord) + adj_acc_fields(w->o.iord)));
   R* base = static_cast<R*>(w->mem);
   auto fwd = [&](R* state) -> int {
     Prob<R> F = make_prob<R>(g, 1, state, u1, u2, u3, h, rhr, bcx, bcy, base, w->ncell,
                              base + (size_t)NFIELD * w->ncell, 1);
-    return run_step<R>(F, 2, w->o.nonos, nullptr, s);
+    return run_step<R>(F, w->o.iord, w->o.nonos, nullptr, s);
   };
   // forward sweep with checkpoints
   for (int n = 0; n < nsteps && !rc; n++) {
@@ -1054,7 +1082,7 @@ int adjoint_run_impl(void* ws, int nsteps, int interval, R* psi, const R* u1, co
     for (int n = n1 - 1; n >= n0 && !rc; n--) {
       Prob<R> B = P;
       B.psi = caller_view<R>(seg + (size_t)(n - n0) * plen, ih, sx, sy);
-      if (run_step_adjoint<R>(B, A, w->o.nonos, static_cast<R*>(w->adj), w->ncell, s)) rc = MPDATA_E_CUDA;
+      if (run_step_adjoint<R>(B, A, w->o.nonos, s)) rc = MPDATA_E_CUDA;
     }
   }
   cudaFreeAsync(ck, s);

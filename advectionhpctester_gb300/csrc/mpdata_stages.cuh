@@ -69,15 +69,47 @@ int run_courants(const PredPlan<R>& plan, int level, R dxi, R dyi, R dzi, R dt, 
 template <class R>
 int run_halve(R* p, long n, cudaStream_t stream);
 
-// Adjoint scratch of one problem (mpdata_adjoint.cu).
+// Adjoint of one step (mpdata_adjoint.cu), gauge form, iord >= 2.
+// Reverse-kernel arguments of one corrective pass: where each adjoint lives.
 template <class R>
 struct AdjArr {
-  Arr<R> lxant, lv1, lv2, lv3, lw1, lw2, lw3, lcp, lcn, lx;
-  Arr<R> lam;            // caller lambda: in dJ/dpsi_new, out dJ/dpsi_in (psi-shaped)
-  Arr<R> gu1, gu2, gu3;  // caller gradients of u1..u3 (C-grid shaped), accumulated
+  Arr<R> lxant;             // adjoint of the pass's input field (written first by the update's reverse)
+  Arr<R> lv1, lv2, lv3;     // adjoints of the pseudo-velocities
+  Arr<R> lw1, lw2, lw3;     // adjoints of the limited velocities (the next pass's pseudo adds too)
+  Arr<R> lcp, lcn;          // adjoints of the limiter ratios
+  Arr<R> lx;                // adjoint of the step's input psi
+  Arr<R> lam;               // adjoint of the pass's output (the caller's lambda for the last pass)
+  Arr<R> gu1, gu2, gu3;     // caller gradients of u1..u3 (C-grid shaped), accumulated
+  Arr<R> la1, la2, la3;     // adjoint of the pass's "a" velocities: gu (first pass) or the previous lw
+  Arr<R> lmx, lmn;          // adjoint of this pass's running extrema carried from the next pass
+  Arr<R> lmxp, lmnp;        // ... of the previous pass's extrema (added when they win the fold)
+  Arr<R> mxp, mnp;          // the previous pass's running extrema (values)
 };
+
+// Arena of the step adjoint: per-pass forward records and accumulators.
+constexpr int kAdjMaxPass = 7;  // iord <= 8
 template <class R>
-int run_step_adjoint(const Prob<R>& P, const AdjArr<R>& A, int nonos, R* zero, size_t ncell, cudaStream_t s);
+struct AdjPlan {
+  int npass;                                    // iord - 1
+  Arr<R> x[kAdjMaxPass];                        // each pass's input field
+  Arr<R> v[kAdjMaxPass][3], w[kAdjMaxPass][3];  // pseudo and limited velocities
+  Arr<R> cp[kAdjMaxPass], cn[kAdjMaxPass];
+  Arr<R> mx[kAdjMaxPass], mn[kAdjMaxPass];      // running extrema after each pass
+  Arr<R> lx[kAdjMaxPass], lw[kAdjMaxPass][3], lmx[kAdjMaxPass], lmn[kAdjMaxPass];
+  Arr<R> lv[3], lcp, lcn;                       // reused by every pass
+  Arr<R> lxin;                                  // adjoint of the step's input psi
+  Arr<R> lam;                                   // caller lambda: in dJ/dpsi_new, out dJ/dpsi_in
+  Arr<R> gu1, gu2, gu3;                         // caller gradients of u1..u3
+  R* acc;                                       // the accumulators, contiguous
+  size_t acc_elems, pass_acc_elems;             // all of them; the per-pass block (lv, lcp, lcn)
+  R* pass_acc;
+};
+// Fields of the arena for iord passes: records, then accumulators.
+inline size_t adj_record_fields(int iord) { return (size_t)(iord - 1) * 11; }  // x, v*3, w*3, cp, cn, mx, mn
+inline size_t adj_acc_fields(int iord) { return (size_t)(iord - 1) * 6 + 5 + 1; }  // lx, lw*3, lmx, lmn; lv*3, lcp, lcn; lxin
+
+template <class R>
+int run_step_adjoint(const Prob<R>& P, const AdjPlan<R>& A, int nonos, cudaStream_t s);
 template <class R>
 int run_seed(const Prob<R>& P, const Arr<R>& psi, const Arr<R>& target, const Arr<R>& lam, cudaStream_t s);
 

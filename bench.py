@@ -488,8 +488,9 @@ def run_precision_study(args, n=(768, 768, 160), nsteps=500):
     return out
 
 
-def run_adjoint_study(args, n=(256, 256, 64), nsteps=200):
-    """Adjoint of the gauge iord=2 nonoscillatory step on 256x256x64 periodic,
+def run_adjoint_study(args, n=(256, 256, 64), nsteps=200, iord=3):
+    """Adjoint of the gauge nonoscillatory step (iord=3, the headline scheme)
+    on 256x256x64 periodic,
     deformational flow held fixed, Gaussian-cone psi, J = 0.5|psi_N - target|^2
     with a shifted-cone target, sqrt(N) checkpointing."""
     import torch
@@ -513,7 +514,7 @@ def run_adjoint_study(args, n=(256, 256, 64), nsteps=200):
     W.interior(tg)[...] = cone(0.5 + off[0], 0.5 + off[1], 0.5 + off[2])
     d = {k: M.fortran_device(getattr(f, k)) for k in ("x", "u1", "u2", "u3", "h", "rhr")}
     target = M.fortran_device(tg)
-    ws = M.Workspace(nx, ny, nz, 1, 1, 1, 1, iord=2, nonos=1, gauge=1, precision=64)
+    ws = M.Workspace(nx, ny, nz, 1, 1, 1, 1, iord=iord, nonos=1, gauge=1, precision=64)
     psi = d["x"].clone()
     for _ in range(3):
         ws.step(psi, d["u1"], d["u2"], d["u3"], d["h"], d["rhr"])
@@ -546,7 +547,7 @@ def run_adjoint_study(args, n=(256, 256, 64), nsteps=200):
     run_ms = (time.perf_counter() - t0) * 1e3
     ws.close()
     cells = nx * ny * nz
-    return {"workload": "adjoint_%dx%dx%d_periodic_gauge_iord2_nonos_N%d" % (nx, ny, nz, nsteps),
+    return {"workload": "adjoint_%dx%dx%d_periodic_gauge_iord%d_nonos_N%d" % (nx, ny, nz, iord, nsteps),
             "forward_ms_per_step": round(fwd_ms / nsteps, 4),
             "step_adjoint_ms": round(step_adj_ms, 4),
             "step_adjoint_over_forward": round(step_adj_ms / (fwd_ms / nsteps), 3),

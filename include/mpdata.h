@@ -143,14 +143,16 @@ int mpdata_rho_gauge_f32(void* ws, float* ox, float* oy, float* oz, float* u, fl
 
 /* ---- adjoint ---------------------------------------------------------------
  * No reference code: the hand-written reverse of the step (infinite-gauge
- * form, one corrective pass, limiter on or off), every branch differentiated
- * at the forward values.  The workspace must be gauge with iord=2.
+ * form, every corrective pass of iord 2 to 8, limiter on or off), every
+ * branch differentiated at the forward values.  The workspace must be gauge
+ * (standard form: MPDATA_E_UNSUPPORTED); its adjoint arena holds 17*(iord-1)+6
+ * extra fields (the forward records and accumulators of every pass).
  *
  * mpdata_step_adjoint_*: psi_in is the field at the start of the step (not
  * modified); on entry lambda holds dJ/dpsi after the step (psi-shaped,
  * interior used), on exit dJ/dpsi before it; dJ/du1..u3 of this step are
- * ADDED into g_u1..g_u3 (C-grid shaped).  The forward intermediates are
- * recomputed into the workspace.  Accumulation uses atomic adds, so results
+ * ADDED into g_u1..g_u3 (C-grid shaped).  The forward step is recomputed
+ * pass by pass into the workspace's adjoint arena.  Accumulation uses atomic adds, so results
  * match the FP64 reference adjoint to rounding, not bit for bit.
  *
  * mpdata_adjoint_run_*: J = 0.5*sum((psi_N - target)^2) after nsteps steps

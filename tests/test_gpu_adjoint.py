@@ -1,4 +1,4 @@
-"""GPU adjoint of the MPDATA step (gauge form, one corrective pass) against
+"""GPU adjoint of the MPDATA step (gauge form, iord 2 to 4) against
 the oracle's FP64 un-checkpointed adjoint (reverse-mode AD of the oracle's
 own step): single-step reverse, sqrt(N)-checkpointed run, the dot-product
 test against the oracle's tangent-linear model, and central finite
@@ -30,14 +30,14 @@ def problem(n, ibc, seed):
     return f, target
 
 
-def gpu_adjoint_run(M, f, target, nsteps, nonos=1, interval=0, precision=64):
+def gpu_adjoint_run(M, f, target, nsteps, nonos=1, interval=0, precision=64, iord=2):
     import torch
     dt = np.float64 if precision == 64 else np.float32
     d = {k: M.fortran_device(getattr(f, k), dtype=dt) for k in ("x", "u1", "u2", "u3", "h", "rhr", "bcx", "bcy")}
     tg = M.fortran_device(target, dtype=dt)
     gx = torch.zeros_like(d["x"])
     gu = [torch.zeros_like(d[k]) for k in ("u1", "u2", "u3")]
-    ws = M.Workspace(f.np, f.mp, f.lp, f.ih, f.ibcx, f.ibcy, f.ibcz, iord=2, nonos=nonos, gauge=1,
+    ws = M.Workspace(f.np, f.mp, f.lp, f.ih, f.ibcx, f.ibcy, f.ibcz, iord=iord, nonos=nonos, gauge=1,
                      precision=precision)
     J, peak = ws.adjoint_run(nsteps, d["x"], d["u1"], d["u2"], d["u3"], d["h"], d["rhr"], tg, gx, *gu,
                              d["bcx"], d["bcy"], interval=interval)
@@ -46,18 +46,22 @@ def gpu_adjoint_run(M, f, target, nsteps, nonos=1, interval=0, precision=64):
     return out
 
 
-def oracle_adjoint(oracle, f, target, nsteps, nonos=1):
+def oracle_adjoint(oracle, f, target, nsteps, nonos=1, iord=2):
     g = oracle.grid(f.np, f.mp, f.lp, f.ih, f.ibcx, f.ibcy, f.ibcz)
-    return oracle.adjoint(g, f.x, f.bcx, f.bcy, f.u1, f.u2, f.u3, f.rhr, f.h, target, t_adv=1, iord=2,
+    return oracle.adjoint(g, f.x, f.bcx, f.bcy, f.u1, f.u2, f.u3, f.rhr, f.h, target, t_adv=1, iord=iord,
                           nonos=nonos, nsteps=nsteps)
 
 
+@pytest.mark.parametrize("iord", [2, 3, 4])
 @pytest.mark.parametrize("ibc", [(1, 1, 1), (0, 0, 0), (1, 0, 0)])
 @pytest.mark.parametrize("nonos", [1, 0])
-def test_single_step_adjoint_matches_oracle(M, oracle, ibc, nonos):
+def test_single_step_adjoint_matches_oracle(M, oracle, ibc, nonos, iord):
+    """Every corrective pass reversed: the later passes' "a" velocities are
+    the previous pass's limited ones and their bounds continue the previous
+    pass's running extrema."""
     f, target = problem((12, 10, 8), ibc, seed=31)
-    J, xN, gx, g1, g2, g3, _ = gpu_adjoint_run(M, f, target, 1, nonos=nonos)
-    Jo, xNo, gxo, g1o, g2o, g3o = oracle_adjoint(oracle, f, target, 1, nonos=nonos)
+    J, xN, gx, g1, g2, g3, _ = gpu_adjoint_run(M, f, target, 1, nonos=nonos, iord=iord)
+    Jo, xNo, gxo, g1o, g2o, g3o = oracle_adjoint(oracle, f, target, 1, nonos=nonos, iord=iord)
     np.testing.assert_array_equal(W.interior(xN), W.interior(xNo))
     assert abs(J - Jo) <= 1e-13 * abs(Jo)
     assert rel(gx, gxo) <= 1e-12
@@ -65,35 +69,37 @@ def test_single_step_adjoint_matches_oracle(M, oracle, ibc, nonos):
         assert rel(a, b) <= 1e-12
 
 
+@pytest.mark.parametrize("iord", [2, 3])
 @pytest.mark.parametrize("ibc", [(1, 1, 1), (0, 0, 0)])
-def test_checkpointed_run_matches_unCheckpointed_oracle(M, oracle, ibc):
+def test_checkpointed_run_matches_unCheckpointed_oracle(M, oracle, ibc, iord):
     """7 steps, checkpoints every 3 (segments of 3, 3, 1) against the
     oracle's un-checkpointed FP64 adjoint."""
     f, target = problem((12, 10, 8), ibc, seed=41)
-    J, _, gx, g1, g2, g3, peak = gpu_adjoint_run(M, f, target, 7, interval=3)
-    Jo, _, gxo, g1o, g2o, g3o = oracle_adjoint(oracle, f, target, 7)
+    J, _, gx, g1, g2, g3, peak = gpu_adjoint_run(M, f, target, 7, interval=3, iord=iord)
+    Jo, _, gxo, g1o, g2o, g3o = oracle_adjoint(oracle, f, target, 7, iord=iord)
     assert abs(J - Jo) <= 1e-12 * abs(Jo)
     assert rel(gx, gxo) <= 1e-11
     for a, b in ((g1, g1o), (g2, g2o), (g3, g3o)):
         assert rel(a, b) <= 1e-11
     assert peak > 0
     # default interval ceil(sqrt(7)) = 3 gives the same gradients
-    J2, _, gx2, *_ = gpu_adjoint_run(M, f, target, 7)
+    J2, _, gx2, *_ = gpu_adjoint_run(M, f, target, 7, iord=iord)
     assert rel(gx2, gx) <= 1e-13
 
 
-def test_dot_product_against_tangent_linear(M, oracle):
+@pytest.mark.parametrize("iord", [2, 3])
+def test_dot_product_against_tangent_linear(M, oracle, iord):
     """<dx0, dJ/dx0> + <du, dJ/du> from the GPU adjoint equals the oracle
     tangent-linear derivative of J along (dx0, du) to 1e-12."""
     f, target = problem((12, 10, 8), (1, 1, 1), seed=51)
     nsteps = 4
-    J, _, gx, g1, g2, g3, _ = gpu_adjoint_run(M, f, target, nsteps)
+    J, _, gx, g1, g2, g3, _ = gpu_adjoint_run(M, f, target, nsteps, iord=iord)
     rng = np.random.default_rng(52)
     for trial in range(3):
         dx = np.asfortranarray(rng.uniform(-1, 1, f.x.shape))
         du = [np.asfortranarray(rng.uniform(-1, 1, a.shape)) for a in (f.u1, f.u2, f.u3)]
         tl = oracle.tangent_dJ(oracle.grid(12, 10, 8, 1, 1, 1, 1), f.x, f.bcx, f.bcy, f.u1, f.u2, f.u3, f.rhr,
-                               f.h, target, dx, *du, nsteps=nsteps)
+                               f.h, target, dx, *du, nsteps=nsteps, iord=iord)
         dot = (gx * dx).sum() + (g1 * du[0]).sum() + (g2 * du[1]).sum() + (g3 * du[2]).sum()
         assert abs(dot - tl) <= 1e-12 * abs(tl), (trial, dot, tl)
 
