@@ -1,5 +1,5 @@
-// Adjoint of the MPDATA step (infinite-gauge form, iord >= 2 corrective
-// passes, nonoscillatory limiter on or off).  No reference code exists for
+// Adjoint of the MPDATA step (infinite-gauge and standard forms, iord >= 2
+// corrective passes, nonoscillatory limiter on or off).  No reference code exists for
 // it; it differentiates the forward step of mpdata_body.cuh exactly, with
 // every branch (pp, pn, min3, the limiter's max/min over the 7-point stars
 // and over the running extrema of earlier passes, abs) taken at the forward
@@ -11,7 +11,9 @@
 // ratios, limited velocities and running extrema), then runs one reverse
 // kernel per forward stage, last pass first:
 //   update    x_out = rhr*(q - div(w)/h)           -> lambda_x, lambda_w
+//             (standard: rhr*(q - div(g)*hinv), g the limited donor fluxes of q)
 //   limiter   w = pp(v)*A1 - pn(v)*A2              -> lambda_v, lambda_cp, lambda_cn
+//             (standard: the sign-aware vlim_std and g = donor(q, w))
 //   bounds    cp,cn from the extrema and v         -> lambda_x, lambda_v, and lambda of
 //                                                     the step input (first pass) or of
 //                                                     the previous pass's extrema
@@ -149,7 +151,9 @@ template <class R> __device__ __forceinline__ Arg<R> amin(Arg<R> a, Arg<R> b) { 
 // start from the previous pass's running extrema (id 14).  The current
 // field's star is ids 7..13.  The adjoint of this pass's extrema is the
 // cp/cn part plus what the next pass carried back (lmx, lmn).
-template <class R, bool FIRST>
+// STD: the fluxes of the bounds are the unlimited donor fluxes f*ns (their
+// adjoint goes to lf); gauge: the pseudo-velocities themselves (lv).
+template <class R, bool FIRST, bool STD>
 __global__ void __launch_bounds__(128) ka_bounds(const Prob<R> P, const AdjArr<R> A) {
   ACELL
   const bool lo = g.bz || k > 1, hi = g.bz || k < g.lp;
@@ -187,9 +191,15 @@ __global__ void __launch_bounds__(128) ka_bounds(const Prob<R> P, const AdjArr<R
 
   const R x = X.ld(i, j, k), hc = P.h.ld(i, j, k);
   const R lcp = A.lcp.ld(i, j, k), lcn = A.lcn.ld(i, j, k);
-  const R e1 = fx<R, false>(g, P.v1, i + 1, j, k), w1 = fx<R, false>(g, P.v1, i, j, k);
-  const R e2 = fy<R, false>(g, P.v2, i, j + 1, k), w2 = fy<R, false>(g, P.v2, i, j, k);
-  const R e3 = fz<R, false>(g, P.v3, i, j, k + 1), w3 = fz<R, false>(g, P.v3, i, j, k);
+  const Arr<R>& F1 = STD ? P.f1 : P.v1;
+  const Arr<R>& F2 = STD ? P.f2 : P.v2;
+  const Arr<R>& F3 = STD ? P.f3 : P.v3;
+  const Arr<R>& LF1 = STD ? A.lf1 : A.lv1;
+  const Arr<R>& LF2 = STD ? A.lf2 : A.lv2;
+  const Arr<R>& LF3 = STD ? A.lf3 : A.lv3;
+  const R e1 = fx<R, false>(g, F1, i + 1, j, k), w1 = fx<R, false>(g, F1, i, j, k);
+  const R e2 = fy<R, false>(g, F2, i, j + 1, k), w2 = fy<R, false>(g, F2, i, j, k);
+  const R e3 = fz<R, false>(g, F3, i, j, k + 1), w3 = fz<R, false>(g, F3, i, j, k);
   const R ep = Eps<R>::v;
   const R Dp = pn(e1) + pp(w1) + pn(e2) + pp(w2) + pn(e3) + pp(w3) + ep;
   const R Dn = pp(e1) + pn(w1) + pp(e2) + pn(w2) + pp(e3) + pn(w3) + ep;
@@ -205,12 +215,12 @@ __global__ void __launch_bounds__(128) ka_bounds(const Prob<R> P, const AdjArr<R
   // d/dD: -c/D
   const R lDp = -lcp * cpv / Dp, lDn = -lcn * cnv / Dn;
   // Dp = pn(e)+pp(w)+..., Dn = pp(e)+pn(w)+... over the six faces
-  fx_add<R, false>(g, A.lv1, i + 1, j, k, lDp * dpn(e1) + lDn * dpp(e1));
-  fx_add<R, false>(g, A.lv1, i, j, k, lDp * dpp(w1) + lDn * dpn(w1));
-  fy_add<R, false>(g, A.lv2, i, j + 1, k, lDp * dpn(e2) + lDn * dpp(e2));
-  fy_add<R, false>(g, A.lv2, i, j, k, lDp * dpp(w2) + lDn * dpn(w2));
-  fz_add<R, false>(g, A.lv3, i, j, k + 1, lDp * dpn(e3) + lDn * dpp(e3));
-  fz_add<R, false>(g, A.lv3, i, j, k, lDp * dpp(w3) + lDn * dpn(w3));
+  fx_add<R, false>(g, LF1, i + 1, j, k, lDp * dpn(e1) + lDn * dpp(e1));
+  fx_add<R, false>(g, LF1, i, j, k, lDp * dpp(w1) + lDn * dpn(w1));
+  fy_add<R, false>(g, LF2, i, j + 1, k, lDp * dpn(e2) + lDn * dpp(e2));
+  fy_add<R, false>(g, LF2, i, j, k, lDp * dpp(w2) + lDn * dpn(w2));
+  fz_add<R, false>(g, LF3, i, j, k + 1, lDp * dpn(e3) + lDn * dpp(e3));
+  fz_add<R, false>(g, LF3, i, j, k, lDp * dpp(w3) + lDn * dpn(w3));
 }
 
 // ---- pseudo-velocity (gauge): v = vdyf(xl,xr,a,hm) - 0.125*a*hm*cr ------------
@@ -335,6 +345,196 @@ __global__ void __launch_bounds__(128) ka_pseudo(const Prob<R> P, const AdjArr<R
 #undef LX
 }
 
+// ---- standard form (antidiff3d-standard-gpubc.f90) ---------------------------
+// update: x_out = rhr*(q - d*hinv), d = signed sum of the limited fluxes g
+template <class R>
+__global__ void __launch_bounds__(128) ka_update_std(const Prob<R> P, const AdjArr<R> A) {
+  ACELL
+  const R lt = P.rhr.ld(i, j, k) * A.lam.ld(i, j, k);
+  addat(A.lq, i, j, k, lt);
+  const R lD = -lt * P.hinv.ld(i, j, k);
+  fx_add<R, false>(g, A.lg1, i + 1, j, k, lD);
+  fx_add<R, false>(g, A.lg1, i, j, k, -lD);
+  fy_add<R, false>(g, A.lg2, i, j + 1, k, lD);
+  fy_add<R, false>(g, A.lg2, i, j, k, -lD);
+  fz_add<R, false>(g, A.lg3, i, j, k + 1, lD);
+  fz_add<R, false>(g, A.lg3, i, j, k, -lD);
+}
+
+// limiter: w = vlim_std(v, a1, a2, x(c-1), x(c)) with a1 = min3(cp(c), cn(c-1)),
+// a2 = min3(cp(c-1), cn(c)); g = donor(q(c-1), q(c), w).  possign() is
+// piecewise constant: only v, a1 and a2 carry a derivative through it.
+template <class R, bool NONOS>
+__global__ void __launch_bounds__(128) ka_limit_std(const Prob<R> P, const AdjArr<R> A) {
+  ACELL
+  const Arr<R>& X = P.xant;
+  const R cpc = NONOS ? P.cp.ld(i, j, k) : R(0), cnc = NONOS ? P.cn.ld(i, j, k) : R(0);
+  const R xc = X.ld(i, j, k), qc = P.q.ld(i, j, k);
+#define LIMIT_STD_FACE(V, LV, LW, LG, IM, JM, KM)                                                       \
+  {                                                                                                     \
+    const R v = V.ld(i, j, k);                                                                          \
+    const R xl = X.ld(IM, JM, KM), ql = P.q.ld(IM, JM, KM);                                             \
+    R w = v, a1 = R(0), a2 = R(0), cpm = R(0), cnm = R(0);                                              \
+    if (NONOS) {                                                                                        \
+      cpm = P.cp.ld(IM, JM, KM);                                                                        \
+      cnm = P.cn.ld(IM, JM, KM);                                                                        \
+      a1 = min3(cpc, cnm);                                                                              \
+      a2 = min3(cpm, cnc);                                                                              \
+      w = vlim_std(v, a1, a2, xl, xc);                                                                  \
+    }                                                                                                   \
+    const R lg = LG.ld(i, j, k);                                                                        \
+    addat(A.lq, IM, JM, KM, lg * pp(w));                                                                \
+    addat(A.lq, i, j, k, -lg * pn(w));                                                                  \
+    const R lw = LW.ld(i, j, k) + lg * (dpp(w) * ql - dpn(w) * qc);                                     \
+    if (!NONOS) {                                                                                       \
+      addat(LV, i, j, k, lw);                                                                           \
+    } else {                                                                                            \
+      const R sl = possign(xl), sml = possign(-xl), sr = possign(xc), smr = possign(-xc);              \
+      addat(LV, i, j, k, lw * (dpp(v) * (a1 * sl + a2 * sml) - dpn(v) * (a2 * sr + a1 * smr)));         \
+      min3_adj(cpc, cnm, lw * (pp(v) * sl - pn(v) * smr), A.lcp, i, j, k, A.lcn, IM, JM, KM);          \
+      min3_adj(cpm, cnc, lw * (pp(v) * sml - pn(v) * sr), A.lcp, IM, JM, KM, A.lcn, i, j, k);          \
+    }                                                                                                   \
+  }
+  if (g.bx || i > 1) LIMIT_STD_FACE(P.v1, A.lv1, A.lw1, A.lg1, wrapi(i - 1, g.np), j, k)
+  if (g.by || j > 1) LIMIT_STD_FACE(P.v2, A.lv2, A.lw2, A.lg2, i, wrapi(j - 1, g.mp), k)
+  if (g.bz || k > 1) LIMIT_STD_FACE(P.v3, A.lv3, A.lw3, A.lg3, i, j, wrapi(k - 1, g.lp))
+#undef LIMIT_STD_FACE
+}
+
+// vcorra(a, b, y1, y2, hm) = -(0.125*a*b*y1*hm/y2) with y1 = (|p1|+|p2|)-(|m1|+|m2|),
+// y2 = |p1|+|p2|+|m1|+|m2|+ep; returns dv/da and dv/db, scatters dv/dx.
+template <class R>
+struct VcTerm {
+  R lb;  // lambda of b
+  R la;  // lambda of a
+};
+template <class R>
+__device__ __forceinline__ VcTerm<R> vcorra_adj(const Geo& g, const Arr<R>& X, const Arr<R>& LX, R lv, R a, R b,
+                                                R hm, int pi1, int pj1, int pk1, int pi2, int pj2, int pk2,
+                                                int mi1, int mj1, int mk1, int mi2, int mj2, int mk2) {
+  const R p1 = xr<R>(g, X, pi1, pj1, pk1), p2 = xr<R>(g, X, pi2, pj2, pk2);
+  const R m1 = xr<R>(g, X, mi1, mj1, mk1), m2 = xr<R>(g, X, mi2, mj2, mk2);
+  const R y1 = (fabs(p1) + fabs(p2)) - (fabs(m1) + fabs(m2));
+  const R y2 = fabs(p1) + fabs(p2) + fabs(m1) + fabs(m2) + Eps<R>::v;
+  const R t = -R(0.125) * hm;
+  const R dy1 = t * a * b / y2, dy2 = -t * a * b * y1 / (y2 * y2);
+  xr_add<R>(g, LX, pi1, pj1, pk1, lv * (dy1 + dy2) * dabs(p1));
+  xr_add<R>(g, LX, pi2, pj2, pk2, lv * (dy1 + dy2) * dabs(p2));
+  xr_add<R>(g, LX, mi1, mj1, mk1, lv * (dy2 - dy1) * dabs(m1));
+  xr_add<R>(g, LX, mi2, mj2, mk2, lv * (dy2 - dy1) * dabs(m2));
+  return VcTerm<R>{lv * t * a * y1 / y2, lv * t * b * y1 / y2};
+}
+
+// pseudo-velocity: f*ns = donor(xl, xr, v) first, then
+// v = vdyfa(xl, xr, a, hm) + vcorra(cross 1) [+ vcorra(cross 2)], and the
+// q = x/rhr of the limiter's fluxes back into x.
+template <class R, bool AIN>
+__global__ void __launch_bounds__(128) ka_pseudo_std(const Prob<R> P, const AdjArr<R> A) {
+  ACELL
+  const Arr<R>& X = P.xant;
+  const Arr<R>& U1 = AIN ? P.u1 : P.w1;
+  const Arr<R>& U2 = AIN ? P.u2 : P.w2;
+  const Arr<R>& U3 = AIN ? P.u3 : P.w3;
+  const R ep = Eps<R>::v;
+  const bool zt = g.bz || (k > 1 && k < g.lp);
+  addat(A.lxant, i, j, k, A.lq.ld(i, j, k) / P.rhr.ld(i, j, k));
+#define XX(a, b, c) xr<R>(g, X, (a), (b), (c))
+#define LX(a, b, c, v) xr_add<R>(g, A.lxant, (a), (b), (c), (v))
+  // the face's own velocity, donor flux and vdyfa; returns lambda of v after f*ns
+#define FACE_HEAD(LV, LF, V, AF, HM, XLI, XLJ, XLK)                                                     \
+  const R v = V.ld(i, j, k), hm = HM.ld(i, j, k), a = AF;                                           \
+  const R xl = XX(XLI, XLJ, XLK), xrr = XX(i, j, k);                                                \
+  const R lf = LF.ld(i, j, k);                                                                      \
+  LX(XLI, XLJ, XLK, lf * pp(v));                                                                    \
+  LX(i, j, k, -lf * pn(v));                                                                         \
+  const R lv = LV.ld(i, j, k) + lf * (dpp(v) * xl - dpn(v) * xrr);                                  \
+  const R K = fabs(a) - a * a * hm, N = fabs(xrr) - fabs(xl), Dd = fabs(xrr) + fabs(xl) + ep;       \
+  R la = lv * (dabs(a) - R(2) * a * hm) * N / Dd;                                                   \
+  LX(i, j, k, lv * K * dabs(xrr) * (Dd - N) / (Dd * Dd));                                           \
+  LX(XLI, XLJ, XLK, -lv * K * dabs(xl) * (Dd + N) / (Dd * Dd));
+  if (g.bx || i > 1) {
+    FACE_HEAD(A.lv1, A.lf1, P.v1, (fx<R, AIN>(g, U1, i, j, k)), P.hmx, i - 1, j, k)
+    {
+      const R b = fy<R, AIN>(g, U2, i - 1, j, k) + fy<R, AIN>(g, U2, i - 1, j + 1, k) +
+                  fy<R, AIN>(g, U2, i, j + 1, k) + fy<R, AIN>(g, U2, i, j, k);
+      const VcTerm<R> c = vcorra_adj<R>(g, X, A.lxant, lv, a, b, hm, i - 1, j + 1, k, i, j + 1, k, i - 1, j - 1, k,
+                                        i, j - 1, k);
+      la += c.la;
+      fy_add<R, AIN>(g, A.la2, i - 1, j, k, c.lb);
+      fy_add<R, AIN>(g, A.la2, i - 1, j + 1, k, c.lb);
+      fy_add<R, AIN>(g, A.la2, i, j + 1, k, c.lb);
+      fy_add<R, AIN>(g, A.la2, i, j, k, c.lb);
+    }
+    if (zt) {
+      const R b = fz<R, AIN>(g, U3, i - 1, j, k) + fz<R, AIN>(g, U3, i - 1, j, k + 1) +
+                  fz<R, AIN>(g, U3, i, j, k + 1) + fz<R, AIN>(g, U3, i, j, k);
+      const VcTerm<R> c = vcorra_adj<R>(g, X, A.lxant, lv, a, b, hm, i - 1, j, k + 1, i, j, k + 1, i - 1, j, k - 1,
+                                        i, j, k - 1);
+      la += c.la;
+      fz_add<R, AIN>(g, A.la3, i - 1, j, k, c.lb);
+      fz_add<R, AIN>(g, A.la3, i - 1, j, k + 1, c.lb);
+      fz_add<R, AIN>(g, A.la3, i, j, k + 1, c.lb);
+      fz_add<R, AIN>(g, A.la3, i, j, k, c.lb);
+    }
+    fx_add<R, AIN>(g, A.la1, i, j, k, la);
+  }
+  if (g.by || j > 1) {
+    FACE_HEAD(A.lv2, A.lf2, P.v2, (fy<R, AIN>(g, U2, i, j, k)), P.hmy, i, j - 1, k)
+    {
+      const R b = fx<R, AIN>(g, U1, i, j - 1, k) + fx<R, AIN>(g, U1, i, j, k) + fx<R, AIN>(g, U1, i + 1, j, k) +
+                  fx<R, AIN>(g, U1, i + 1, j - 1, k);
+      const VcTerm<R> c = vcorra_adj<R>(g, X, A.lxant, lv, a, b, hm, i + 1, j - 1, k, i + 1, j, k, i - 1, j - 1, k,
+                                        i - 1, j, k);
+      la += c.la;
+      fx_add<R, AIN>(g, A.la1, i, j - 1, k, c.lb);
+      fx_add<R, AIN>(g, A.la1, i, j, k, c.lb);
+      fx_add<R, AIN>(g, A.la1, i + 1, j, k, c.lb);
+      fx_add<R, AIN>(g, A.la1, i + 1, j - 1, k, c.lb);
+    }
+    if (zt) {
+      const R b = fz<R, AIN>(g, U3, i, j - 1, k) + fz<R, AIN>(g, U3, i, j, k) + fz<R, AIN>(g, U3, i, j, k + 1) +
+                  fz<R, AIN>(g, U3, i, j - 1, k + 1);
+      const VcTerm<R> c = vcorra_adj<R>(g, X, A.lxant, lv, a, b, hm, i, j - 1, k + 1, i, j, k + 1, i, j - 1, k - 1,
+                                        i, j, k - 1);
+      la += c.la;
+      fz_add<R, AIN>(g, A.la3, i, j - 1, k, c.lb);
+      fz_add<R, AIN>(g, A.la3, i, j, k, c.lb);
+      fz_add<R, AIN>(g, A.la3, i, j, k + 1, c.lb);
+      fz_add<R, AIN>(g, A.la3, i, j - 1, k + 1, c.lb);
+    }
+    fy_add<R, AIN>(g, A.la2, i, j, k, la);
+  }
+  if (g.bz || k > 1) {
+    FACE_HEAD(A.lv3, A.lf3, P.v3, (fz<R, AIN>(g, U3, i, j, k)), P.hmz, i, j, k - 1)
+    {
+      const R b = fx<R, AIN>(g, U1, i, j, k - 1) + fx<R, AIN>(g, U1, i, j, k) + fx<R, AIN>(g, U1, i + 1, j, k) +
+                  fx<R, AIN>(g, U1, i + 1, j, k - 1);
+      const VcTerm<R> c = vcorra_adj<R>(g, X, A.lxant, lv, a, b, hm, i + 1, j, k - 1, i + 1, j, k, i - 1, j, k - 1,
+                                        i - 1, j, k);
+      la += c.la;
+      fx_add<R, AIN>(g, A.la1, i, j, k - 1, c.lb);
+      fx_add<R, AIN>(g, A.la1, i, j, k, c.lb);
+      fx_add<R, AIN>(g, A.la1, i + 1, j, k, c.lb);
+      fx_add<R, AIN>(g, A.la1, i + 1, j, k - 1, c.lb);
+    }
+    {
+      const R b = fy<R, AIN>(g, U2, i, j, k - 1) + fy<R, AIN>(g, U2, i, j + 1, k - 1) +
+                  fy<R, AIN>(g, U2, i, j + 1, k) + fy<R, AIN>(g, U2, i, j, k);
+      const VcTerm<R> c = vcorra_adj<R>(g, X, A.lxant, lv, a, b, hm, i, j + 1, k - 1, i, j + 1, k, i, j - 1, k - 1,
+                                        i, j - 1, k);
+      la += c.la;
+      fy_add<R, AIN>(g, A.la2, i, j, k - 1, c.lb);
+      fy_add<R, AIN>(g, A.la2, i, j + 1, k - 1, c.lb);
+      fy_add<R, AIN>(g, A.la2, i, j + 1, k, c.lb);
+      fy_add<R, AIN>(g, A.la2, i, j, k, c.lb);
+    }
+    fz_add<R, AIN>(g, A.la3, i, j, k, la);
+  }
+#undef FACE_HEAD
+#undef XX
+#undef LX
+}
+
 // ---- upwind: xant = rhr*(x - D*hinv), D = signed sum of donor fluxes --------
 // F = donor(xl, xr, u) = pp(u)*xl - pn(u)*xr; dF/du = [u>0]*xl + [u<0]*xr.
 // Open-wall neighbours come from bcx/bcy (constants: no gradient).
@@ -448,6 +648,10 @@ Prob<R> pass_prob(const Prob<R>& P, const AdjPlan<R>& A, int t, bool prev_w) {
   Q.cn = A.cn[t];
   Q.mx = A.mx[t];
   Q.mn = A.mn[t];
+  Q.q = A.q[t];
+  Q.f1 = A.fns[t][0];  // standard form: the unlimited donor fluxes of the pass
+  Q.f2 = A.fns[t][1];
+  Q.f3 = A.fns[t][2];
   const int tw = prev_w ? (t > 0 ? t - 1 : 0) : t;
   Q.w1 = A.w[tw][0];
   Q.w2 = A.w[tw][1];
@@ -484,11 +688,17 @@ int run_step_adjoint(const Prob<R>& P, const AdjPlan<R>& A, int nonos, cudaStrea
     else if (!keep) kf_bounds<R, true, true, false><<<grd, blk, 0, s>>>(Q);
     else if (t == 0) kf_bounds<R, true, true, true><<<grd, blk, 0, s>>>(Q);
     else kf_bounds<R, true, false, true><<<grd, blk, 0, s>>>(Q);
-    if (nonos) kf_limit<R, true><<<grd, blk, 0, s>>>(Q);
-    else kf_limit<R, false><<<grd, blk, 0, s>>>(Q);
+    // the limited fluxes (standard form) go to the workspace scratch: only
+    // the update reads them
+    Prob<R> L = Q;
+    L.f1 = P.f1;
+    L.f2 = P.f2;
+    L.f3 = P.f3;
+    if (nonos) kf_limit<R, true><<<grd, blk, 0, s>>>(L);
+    else kf_limit<R, false><<<grd, blk, 0, s>>>(L);
     n += 3;
     if (t < np_ - 1) {
-      Prob<R> U = Q;
+      Prob<R> U = L;
       U.xant = A.x[t + 1];
       kf_update<R><<<grd, blk, 0, s>>>(U);
       n++;
@@ -522,17 +732,38 @@ int run_step_adjoint(const Prob<R>& P, const AdjPlan<R>& A, int nonos, cudaStrea
     a.lmnp = A.lmn[t > 0 ? t - 1 : 0];
     a.mxp = A.mx[t > 0 ? t - 1 : 0];
     a.mnp = A.mn[t > 0 ? t - 1 : 0];
-    ka_update<R><<<grd, blk, 0, s>>>(Q, a);
-    if (nonos) {
-      ka_limit<R, true><<<grd, blk, 0, s>>>(Q, a);
-      if (t == 0) ka_bounds<R, true><<<grd, blk, 0, s>>>(Q, a);
-      else ka_bounds<R, false><<<grd, blk, 0, s>>>(Q, a);
-      n++;
+    a.lg1 = A.lg[0];
+    a.lg2 = A.lg[1];
+    a.lg3 = A.lg[2];
+    a.lf1 = A.lf[0];
+    a.lf2 = A.lf[1];
+    a.lf3 = A.lf[2];
+    a.lq = A.lq;
+    if (P.stdf) {
+      ka_update_std<R><<<grd, blk, 0, s>>>(Q, a);
+      if (nonos) {
+        ka_limit_std<R, true><<<grd, blk, 0, s>>>(Q, a);
+        if (t == 0) ka_bounds<R, true, true><<<grd, blk, 0, s>>>(Q, a);
+        else ka_bounds<R, false, true><<<grd, blk, 0, s>>>(Q, a);
+        n++;
+      } else {
+        ka_limit_std<R, false><<<grd, blk, 0, s>>>(Q, a);
+      }
+      if (t == 0) ka_pseudo_std<R, true><<<grd, blk, 0, s>>>(Q, a);
+      else ka_pseudo_std<R, false><<<grd, blk, 0, s>>>(Q, a);
     } else {
-      ka_limit<R, false><<<grd, blk, 0, s>>>(Q, a);
+      ka_update<R><<<grd, blk, 0, s>>>(Q, a);
+      if (nonos) {
+        ka_limit<R, true><<<grd, blk, 0, s>>>(Q, a);
+        if (t == 0) ka_bounds<R, true, false><<<grd, blk, 0, s>>>(Q, a);
+        else ka_bounds<R, false, false><<<grd, blk, 0, s>>>(Q, a);
+        n++;
+      } else {
+        ka_limit<R, false><<<grd, blk, 0, s>>>(Q, a);
+      }
+      if (t == 0) ka_pseudo<R, true><<<grd, blk, 0, s>>>(Q, a);
+      else ka_pseudo<R, false><<<grd, blk, 0, s>>>(Q, a);
     }
-    if (t == 0) ka_pseudo<R, true><<<grd, blk, 0, s>>>(Q, a);
-    else ka_pseudo<R, false><<<grd, blk, 0, s>>>(Q, a);
     n += 3;
   }
   AdjArr<R> a0{};

@@ -938,7 +938,7 @@ int adj_plan(Workspace* w, Prob<R>* P, AdjPlan<R>* A, const R* psi_in, const R* 
              const R* h, const R* rhr, const R* bcx, const R* bcy, R* lambda, R* gu1, R* gu2, R* gu3) {
   if (w->elem != sizeof(R)) return MPDATA_E_WS;
   const int iord = w->o.iord;
-  if (!w->o.gauge || iord < 2 || iord - 1 > kAdjMaxPass) return MPDATA_E_UNSUPPORTED;  // gauge form only
+  if (iord < 2 || iord - 1 > kAdjMaxPass) return MPDATA_E_UNSUPPORTED;
   if (!psi_in || !u1 || !u2 || !u3 || !h || !rhr || !lambda || !gu1 || !gu2 || !gu3) return MPDATA_E_NULL;
   if ((!w->g.ibcx && !bcx) || (!w->g.ibcy && !bcy)) return MPDATA_E_NULL;
   const size_t nrec = adj_record_fields(iord), nacc = adj_acc_fields(iord), n = w->ncell;
@@ -948,7 +948,7 @@ int adj_plan(Workspace* w, Prob<R>* P, AdjPlan<R>* A, const R* psi_in, const R* 
     return MPDATA_E_CUDA;
   }
   R* base = static_cast<R*>(w->mem);
-  *P = make_prob<R>(w->g, 1, const_cast<R*>(psi_in), u1, u2, u3, h, rhr, bcx, bcy, base, w->ncell,
+  *P = make_prob<R>(w->g, w->o.gauge, const_cast<R*>(psi_in), u1, u2, u3, h, rhr, bcx, bcy, base, w->ncell,
                     base + (size_t)NFIELD * w->ncell, 1);
   const mpdata_grid& g = w->g;
   const int ih = g.ih, sx = g.np + 2 * ih, sy = g.mp + 2 * ih;
@@ -964,6 +964,8 @@ int adj_plan(Workspace* w, Prob<R>* P, AdjPlan<R>* A, const R* psi_in, const R* 
     A->cn[t] = next();
     A->mx[t] = next();
     A->mn[t] = next();
+    for (int c = 0; c < 3; c++) A->fns[t][c] = next();
+    A->q[t] = next();
   }
   A->acc = a + f * n;  // the accumulators, contiguous
   for (int t = 0; t < A->npass; t++) {
@@ -976,7 +978,10 @@ int adj_plan(Workspace* w, Prob<R>* P, AdjPlan<R>* A, const R* psi_in, const R* 
   for (int c = 0; c < 3; c++) A->lv[c] = next();
   A->lcp = next();
   A->lcn = next();
-  A->pass_acc_elems = 5 * n;
+  for (int c = 0; c < 3; c++) A->lg[c] = next();
+  for (int c = 0; c < 3; c++) A->lf[c] = next();
+  A->lq = next();
+  A->pass_acc_elems = 12 * n;
   A->lxin = next();
   A->acc_elems = (size_t)(a + f * n - A->acc);
   A->lam = caller_view<R>(lambda, ih, sx, sy);
@@ -1047,7 +1052,7 @@ int adjoint_run_impl(void* ws, int nsteps, int interval, R* psi, const R* u1, co
                               (NSCRATCH + adj_record_fields(w->o.iord) + adj_acc_fields(w->o.iord)));
   R* base = static_cast<R*>(w->mem);
   auto fwd = [&](R* state) -> int {
-    Prob<R> F = make_prob<R>(g, 1, state, u1, u2, u3, h, rhr, bcx, bcy, base, w->ncell,
+    Prob<R> F = make_prob<R>(g, w->o.gauge, state, u1, u2, u3, h, rhr, bcx, bcy, base, w->ncell,
                              base + (size_t)NFIELD * w->ncell, 1);
     return run_step<R>(F, w->o.iord, w->o.nonos, nullptr, s);
   };

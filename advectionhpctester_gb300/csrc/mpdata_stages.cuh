@@ -84,6 +84,10 @@ struct AdjArr {
   Arr<R> lmx, lmn;          // adjoint of this pass's running extrema carried from the next pass
   Arr<R> lmxp, lmnp;        // ... of the previous pass's extrema (added when they win the fold)
   Arr<R> mxp, mnp;          // the previous pass's running extrema (values)
+  // standard form only
+  Arr<R> lg1, lg2, lg3;     // adjoints of the limited donor fluxes of x/rhr
+  Arr<R> lf1, lf2, lf3;     // adjoints of the unlimited donor fluxes f*ns
+  Arr<R> lq;                // adjoint of q = x/rhr
 };
 
 // Arena of the step adjoint: per-pass forward records and accumulators.
@@ -95,8 +99,10 @@ struct AdjPlan {
   Arr<R> v[kAdjMaxPass][3], w[kAdjMaxPass][3];  // pseudo and limited velocities
   Arr<R> cp[kAdjMaxPass], cn[kAdjMaxPass];
   Arr<R> mx[kAdjMaxPass], mn[kAdjMaxPass];      // running extrema after each pass
+  Arr<R> fns[kAdjMaxPass][3], q[kAdjMaxPass];   // standard form: unlimited donor fluxes, x/rhr
   Arr<R> lx[kAdjMaxPass], lw[kAdjMaxPass][3], lmx[kAdjMaxPass], lmn[kAdjMaxPass];
   Arr<R> lv[3], lcp, lcn;                       // reused by every pass
+  Arr<R> lg[3], lf[3], lq;                      // reused by every pass (standard form)
   Arr<R> lxin;                                  // adjoint of the step's input psi
   Arr<R> lam;                                   // caller lambda: in dJ/dpsi_new, out dJ/dpsi_in
   Arr<R> gu1, gu2, gu3;                         // caller gradients of u1..u3
@@ -105,8 +111,10 @@ struct AdjPlan {
   R* pass_acc;
 };
 // Fields of the arena for iord passes: records, then accumulators.
-inline size_t adj_record_fields(int iord) { return (size_t)(iord - 1) * 11; }  // x, v*3, w*3, cp, cn, mx, mn
-inline size_t adj_acc_fields(int iord) { return (size_t)(iord - 1) * 6 + 5 + 1; }  // lx, lw*3, lmx, lmn; lv*3, lcp, lcn; lxin
+// records per pass: x, v*3, w*3, cp, cn, mx, mn, fns*3, q
+inline size_t adj_record_fields(int iord) { return (size_t)(iord - 1) * 15; }
+// accumulators: per pass lx, lw*3, lmx, lmn; shared lv*3, lcp, lcn, lg*3, lf*3, lq; lxin
+inline size_t adj_acc_fields(int iord) { return (size_t)(iord - 1) * 6 + 12 + 1; }
 
 template <class R>
 int run_step_adjoint(const Prob<R>& P, const AdjPlan<R>& A, int nonos, cudaStream_t s);

@@ -143,9 +143,9 @@ int mpdata_rho_gauge_f32(void* ws, float* ox, float* oy, float* oz, float* u, fl
 
 /* ---- adjoint ---------------------------------------------------------------
  * No reference code: the hand-written reverse of the step (infinite-gauge
- * form, every corrective pass of iord 2 to 8, limiter on or off), every
- * branch differentiated at the forward values.  The workspace must be gauge
- * (standard form: MPDATA_E_UNSUPPORTED); its adjoint arena holds 17*(iord-1)+6
+ * and standard forms, every corrective pass of iord 2 to 8, limiter on or
+ * off), every branch differentiated at the forward values.  iord=1:
+ * MPDATA_E_UNSUPPORTED.  The workspace's adjoint arena holds 21*(iord-1)+13
  * extra fields (the forward records and accumulators of every pass).
  *
  * mpdata_step_adjoint_*: psi_in is the field at the start of the step (not

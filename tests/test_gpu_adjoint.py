@@ -1,4 +1,4 @@
-"""GPU adjoint of the MPDATA step (gauge form, iord 2 to 4) against
+"""GPU adjoint of the MPDATA step (gauge and standard forms, iord 2 to 4) against
 the oracle's FP64 un-checkpointed adjoint (reverse-mode AD of the oracle's
 own step): single-step reverse, sqrt(N)-checkpointed run, the dot-product
 test against the oracle's tangent-linear model, and central finite
@@ -23,21 +23,21 @@ def rel(a, b):
     return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
 
 
-def problem(n, ibc, seed):
-    f = W.random_fields(*n, ibc=ibc, seed=seed, courant=0.25)
+def problem(n, ibc, seed, sign_change=False):
+    f = W.random_fields(*n, ibc=ibc, seed=seed, courant=0.25, sign_change=sign_change)
     rng = np.random.default_rng(seed + 1)
     target = np.asfortranarray(f.x * 0.9 + rng.uniform(-0.05, 0.05, f.x.shape))
     return f, target
 
 
-def gpu_adjoint_run(M, f, target, nsteps, nonos=1, interval=0, precision=64, iord=2):
+def gpu_adjoint_run(M, f, target, nsteps, nonos=1, interval=0, precision=64, iord=2, gauge=1):
     import torch
     dt = np.float64 if precision == 64 else np.float32
     d = {k: M.fortran_device(getattr(f, k), dtype=dt) for k in ("x", "u1", "u2", "u3", "h", "rhr", "bcx", "bcy")}
     tg = M.fortran_device(target, dtype=dt)
     gx = torch.zeros_like(d["x"])
     gu = [torch.zeros_like(d[k]) for k in ("u1", "u2", "u3")]
-    ws = M.Workspace(f.np, f.mp, f.lp, f.ih, f.ibcx, f.ibcy, f.ibcz, iord=iord, nonos=nonos, gauge=1,
+    ws = M.Workspace(f.np, f.mp, f.lp, f.ih, f.ibcx, f.ibcy, f.ibcz, iord=iord, nonos=nonos, gauge=gauge,
                      precision=precision)
     J, peak = ws.adjoint_run(nsteps, d["x"], d["u1"], d["u2"], d["u3"], d["h"], d["rhr"], tg, gx, *gu,
                              d["bcx"], d["bcy"], interval=interval)
@@ -46,10 +46,10 @@ def gpu_adjoint_run(M, f, target, nsteps, nonos=1, interval=0, precision=64, ior
     return out
 
 
-def oracle_adjoint(oracle, f, target, nsteps, nonos=1, iord=2):
+def oracle_adjoint(oracle, f, target, nsteps, nonos=1, iord=2, gauge=1):
     g = oracle.grid(f.np, f.mp, f.lp, f.ih, f.ibcx, f.ibcy, f.ibcz)
-    return oracle.adjoint(g, f.x, f.bcx, f.bcy, f.u1, f.u2, f.u3, f.rhr, f.h, target, t_adv=1, iord=iord,
-                          nonos=nonos, nsteps=nsteps)
+    return oracle.adjoint(g, f.x, f.bcx, f.bcy, f.u1, f.u2, f.u3, f.rhr, f.h, target, t_adv=1 if gauge else 2,
+                          iord=iord, nonos=nonos, nsteps=nsteps)
 
 
 @pytest.mark.parametrize("iord", [2, 3, 4])
@@ -151,10 +151,37 @@ def test_fp32_adjoint_tracks_fp64(M):
     assert rel(g132.astype(np.float64), g164) <= 1e-4
 
 
+@pytest.mark.parametrize("iord", [2, 3])
+@pytest.mark.parametrize("ibc", [(1, 1, 1), (0, 0, 0), (0, 1, 0)])
+@pytest.mark.parametrize("nonos", [1, 0])
+def test_standard_form_adjoint_matches_oracle(M, oracle, ibc, nonos, iord):
+    """Standard form (t_adv=2) on a field that changes sign: vdyfa/vcorra
+    with their absolute values, the unlimited donor fluxes of the bounds, the
+    sign-aware limited velocity and the donor fluxes of x/rhr."""
+    f, target = problem((12, 10, 8), ibc, seed=81, sign_change=True)
+    J, xN, gx, g1, g2, g3, _ = gpu_adjoint_run(M, f, target, 1, nonos=nonos, iord=iord, gauge=0)
+    Jo, xNo, gxo, g1o, g2o, g3o = oracle_adjoint(oracle, f, target, 1, nonos=nonos, iord=iord, gauge=0)
+    np.testing.assert_array_equal(W.interior(xN), W.interior(xNo))
+    assert abs(J - Jo) <= 1e-13 * abs(Jo)
+    assert rel(gx, gxo) <= 1e-12
+    for a, b in ((g1, g1o), (g2, g2o), (g3, g3o)):
+        assert rel(a, b) <= 1e-12
+
+
+def test_standard_form_checkpointed_run(M, oracle):
+    f, target = problem((12, 10, 8), (1, 1, 1), seed=91, sign_change=True)
+    J, _, gx, g1, g2, g3, _ = gpu_adjoint_run(M, f, target, 5, interval=2, iord=2, gauge=0)
+    Jo, _, gxo, g1o, g2o, g3o = oracle_adjoint(oracle, f, target, 5, iord=2, gauge=0)
+    assert abs(J - Jo) <= 1e-12 * abs(Jo)
+    assert rel(gx, gxo) <= 1e-11
+    for a, b in ((g1, g1o), (g2, g2o), (g3, g3o)):
+        assert rel(a, b) <= 1e-11
+
+
 def test_adjoint_rejects_unsupported(M):
     import torch
-    ws = M.Workspace(8, 8, 8, 1, 1, 1, 1, iord=2, nonos=1, gauge=0, precision=64)
+    ws = M.Workspace(8, 8, 8, 1, 1, 1, 1, iord=1, nonos=1, gauge=1, precision=64)
     z = [M.fortran_empty(ws.shapes[k], torch.float64) for k in ("psi", "u1", "u2", "u3", "psi", "psi", "psi")]
-    with pytest.raises(M.MpdataError):  # standard form has no adjoint here
+    with pytest.raises(M.MpdataError):  # iord=1 is the upwind step alone: nothing to reverse here
         ws.step_adjoint(z[0], z[1], z[2], z[3], z[4], z[5], z[6], z[1].clone(), z[2].clone(), z[3].clone())
     ws.close()
