@@ -488,11 +488,13 @@ def run_precision_study(args, n=(768, 768, 160), nsteps=500):
     return out
 
 
-def run_adjoint_study(args, n=(256, 256, 64), nsteps=200, iord=3):
-    """Adjoint of the gauge nonoscillatory step (iord=3, the headline scheme)
-    on 256x256x64 periodic,
+def run_adjoint_study(args, n=(256, 256, 64), nsteps=200, iord=2, fd_dirs=32):
+    """Adjoint of the gauge nonoscillatory iord=2 step on 256x256x64 periodic,
     deformational flow held fixed, Gaussian-cone psi, J = 0.5|psi_N - target|^2
-    with a shifted-cone target, sqrt(N) checkpointing."""
+    with a seeded shifted-cone target, sqrt(N) checkpointing; FP64 and FP32.
+    The FP64 gradient is checked by central finite differences of J (GPU
+    forward runs, eps = 1e-6) along fd_dirs seeded random directions in
+    (psi_0, u1, u2, u3)."""
     import torch
     from advectionhpctester_gb300 import mpdata as M
     from advectionhpctester_gb300 import workloads as W
@@ -512,49 +514,133 @@ def run_adjoint_study(args, n=(256, 256, 64), nsteps=200, iord=3):
     W.interior(f.x)[...] = cone(0.5, 0.5, 0.5)
     tg = np.zeros_like(f.x)
     W.interior(tg)[...] = cone(0.5 + off[0], 0.5 + off[1], 0.5 + off[2])
-    d = {k: M.fortran_device(getattr(f, k)) for k in ("x", "u1", "u2", "u3", "h", "rhr")}
-    target = M.fortran_device(tg)
-    ws = M.Workspace(nx, ny, nz, 1, 1, 1, 1, iord=iord, nonos=1, gauge=1, precision=64)
-    psi = d["x"].clone()
-    for _ in range(3):
-        ws.step(psi, d["u1"], d["u2"], d["u3"], d["h"], d["rhr"])
-    psi.copy_(d["x"])
-    torch.cuda.synchronize()
+    cells = nx * ny * nz
+    out = {"workload": "adjoint_%dx%dx%d_periodic_gauge_iord%d_nonos_N%d" % (nx, ny, nz, iord, nsteps),
+           "checkpoint_interval": int(math.ceil(math.sqrt(nsteps)))}
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(nsteps):
-        ws.step(psi, d["u1"], d["u2"], d["u3"], d["h"], d["rhr"])
-    e1.record()
-    torch.cuda.synchronize()
-    fwd_ms = e0.elapsed_time(e1)
-    # one step adjoint alone (recompute + reverse)
-    lam = psi.clone()
-    gu = [torch.zeros_like(d[k]) for k in ("u1", "u2", "u3")]
-    ws.step_adjoint(d["x"], d["u1"], d["u2"], d["u3"], d["h"], d["rhr"], lam, *gu)
-    torch.cuda.synchronize()
-    e0.record()
-    for _ in range(10):
+    for prec, dt in ((64, torch.float64), (32, torch.float32)):
+        d = {k: M.fortran_device(getattr(f, k), dtype=np.float64 if prec == 64 else np.float32)
+             for k in ("x", "u1", "u2", "u3", "h", "rhr")}
+        target = M.fortran_device(tg, dtype=np.float64 if prec == 64 else np.float32)
+        ws = M.Workspace(nx, ny, nz, 1, 1, 1, 1, iord=iord, nonos=1, gauge=1, precision=prec)
+        psi = d["x"].clone()
+        for _ in range(3):
+            ws.step(psi, d["u1"], d["u2"], d["u3"], d["h"], d["rhr"])
+        psi.copy_(d["x"])
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(nsteps):
+            ws.step(psi, d["u1"], d["u2"], d["u3"], d["h"], d["rhr"])
+        e1.record()
+        torch.cuda.synchronize()
+        fwd_ms = e0.elapsed_time(e1)
+        lam = psi.clone()
+        gu = [torch.zeros_like(d[k]) for k in ("u1", "u2", "u3")]
         ws.step_adjoint(d["x"], d["u1"], d["u2"], d["u3"], d["h"], d["rhr"], lam, *gu)
-    e1.record()
-    torch.cuda.synchronize()
-    step_adj_ms = e0.elapsed_time(e1) / 10
-    psi.copy_(d["x"])
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(10):
+            ws.step_adjoint(d["x"], d["u1"], d["u2"], d["u3"], d["h"], d["rhr"], lam, *gu)
+        e1.record()
+        torch.cuda.synchronize()
+        step_adj_ms = e0.elapsed_time(e1) / 10
+        psi.copy_(d["x"])
+        gx = torch.zeros_like(psi)
+        gu = [torch.zeros_like(d[k]) for k in ("u1", "u2", "u3")]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        J, peak = ws.adjoint_run(nsteps, psi, d["u1"], d["u2"], d["u3"], d["h"], d["rhr"], target, gx, *gu)
+        run_ms = (time.perf_counter() - t0) * 1e3
+        res = {"forward_ms_per_step": round(fwd_ms / nsteps, 4), "step_adjoint_ms": round(step_adj_ms, 4),
+               "step_adjoint_over_forward": round(step_adj_ms / (fwd_ms / nsteps), 3),
+               "run_ms": round(run_ms, 2), "run_over_forward": round(run_ms / fwd_ms, 3),
+               "adjoint_gcell_steps_per_s": round(cells * nsteps / (run_ms * 1e-3) / 1e9, 4),
+               "peak_bytes": int(peak), "J": J}
+        if prec == 64 and fd_dirs:
+            res["fd_check"] = fd_checks(M, f, tg, d, target, nsteps, fd_dirs, nx, ny, nz, iord)
+        out["fp%d" % prec] = res
+        ws.close()
+        del d, target, psi, lam, gx, gu
+        torch.cuda.empty_cache()
+    return out
+
+
+def fd_checks(M, f, tg, d, target, nsteps, ndirs, nx, ny, nz, iord):
+    """Central differences of J against the adjoint gradient, where J is
+    differentiable.  The limiter makes J piecewise smooth: wherever the
+    updated field is its own star extremum (or two star values tie) the
+    forward point sits on a kink, and a central difference averages the two
+    one-sided slopes.  So: (1) the same flow, cone and N with the limiter
+    off, (2) one step with the limiter on, the cone plus 1e-3 seeded noise
+    breaking the exact ties of its flat far field."""
+    import torch
+    from advectionhpctester_gb300 import workloads as W
+    out = {}
+    ws0 = M.Workspace(nx, ny, nz, 1, 1, 1, 1, iord=iord, nonos=0, gauge=1, precision=64)
+    psi = d["x"].clone()
     gx = torch.zeros_like(psi)
     gu = [torch.zeros_like(d[k]) for k in ("u1", "u2", "u3")]
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    J, peak = ws.adjoint_run(nsteps, psi, d["u1"], d["u2"], d["u3"], d["h"], d["rhr"], target, gx, *gu)
-    run_ms = (time.perf_counter() - t0) * 1e3
-    ws.close()
-    cells = nx * ny * nz
-    return {"workload": "adjoint_%dx%dx%d_periodic_gauge_iord%d_nonos_N%d" % (nx, ny, nz, iord, nsteps),
-            "forward_ms_per_step": round(fwd_ms / nsteps, 4),
-            "step_adjoint_ms": round(step_adj_ms, 4),
-            "step_adjoint_over_forward": round(step_adj_ms / (fwd_ms / nsteps), 3),
-            "run_ms": round(run_ms, 2), "run_over_forward": round(run_ms / fwd_ms, 3),
-            "checkpoint_interval": int(math.ceil(math.sqrt(nsteps))),
-            "adjoint_gcell_steps_per_s": round(cells * nsteps / (run_ms * 1e-3) / 1e9, 4),
-            "peak_bytes": int(peak), "J": J}
+    ws0.adjoint_run(nsteps, psi, d["u1"], d["u2"], d["u3"], d["h"], d["rhr"], target, gx, *gu)
+    out["limiter_off_N%d" % nsteps] = adjoint_fd_check(ws0, d, target, gx, gu, nsteps, ndirs, nx, ny, nz)
+    ws0.close()
+    noisy = f.x.copy()
+    W.interior(noisy)[...] += 1e-3 * np.random.default_rng(7).random((nx, ny, nz))
+    dn = dict(d)
+    dn["x"] = M.fortran_device(noisy)
+    ws1 = M.Workspace(nx, ny, nz, 1, 1, 1, 1, iord=iord, nonos=1, gauge=1, precision=64)
+    psi = dn["x"].clone()
+    gx = torch.zeros_like(psi)
+    gu = [torch.zeros_like(d[k]) for k in ("u1", "u2", "u3")]
+    ws1.adjoint_run(1, psi, d["u1"], d["u2"], d["u3"], d["h"], d["rhr"], target, gx, *gu)
+    out["limiter_on_N1_noise1e-3"] = adjoint_fd_check(ws1, dn, target, gx, gu, 1, ndirs, nx, ny, nz)
+    ws1.close()
+    return out
+
+
+def adjoint_fd_check(ws, d, target, gx, gu, nsteps, ndirs, nx, ny, nz, eps=1e-6):
+    """Central differences (J(p + eps e) - J(p - eps e)) / (2 eps) against
+    <e, grad J> along ndirs unit directions (seed 6): half in psi_0 (interior
+    cells), half in the velocities (interior faces with |u| >= 1e-6, away
+    from the kinks of pp, pn and |u| at u = 0).  The difference of J is
+    summed cell by cell as 0.5 (psi+ - psi-)(psi+ + psi- - 2 target), which
+    keeps about 7 significant digits where J(+) - J(-) would keep 4."""
+    import torch
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(6)
+    inner = lambda t: t.permute(2, 1, 0)[1:nz + 1, 1:ny + 1, 1:nx + 1].permute(2, 1, 0)
+
+    def final(psi0, u):
+        psi = psi0.clone()
+        for _ in range(nsteps):
+            ws.step(psi, u[0], u[1], u[2], d["h"], d["rhr"])
+        return inner(psi).clone()
+
+    errs = []
+    u0 = [d["u1"], d["u2"], d["u3"]]
+    tin = inner(target)
+    for n in range(ndirs):
+        epsi = torch.zeros_like(d["x"])
+        eu = [torch.zeros_like(t) for t in u0]
+        if n % 2 == 0:
+            inner(epsi).copy_(torch.randn((nx, ny, nz), device="cuda", dtype=torch.float64, generator=gen))
+        else:
+            for t, u in zip(eu, u0):
+                r = torch.randn((nx, ny, nz), device="cuda", dtype=torch.float64, generator=gen)
+                inner(t).copy_(torch.where(inner(u).abs() >= 1e-6, r, torch.zeros_like(r)))
+        norm = math.sqrt(float((epsi * epsi).sum()) + sum(float((t * t).sum()) for t in eu))
+        epsi /= norm
+        for t in eu:
+            t /= norm
+        dot = float((gx * epsi).sum()) + sum(float((g * t).sum()) for g, t in zip(gu, eu))
+
+        def shifted(sign):  # clones keep the Fortran strides; the shift is in place
+            xs = d["x"].clone().add_(epsi, alpha=sign * eps)
+            return xs, [a.clone().add_(b, alpha=sign * eps) for a, b in zip(u0, eu)]
+        pp_, pm_ = final(*shifted(1.0)), final(*shifted(-1.0))
+        fd = float((0.5 * (pp_ - pm_) * (pp_ + pm_ - 2.0 * tin)).sum()) / (2 * eps)
+        errs.append(abs(fd - dot) / max(abs(dot), 1e-300))
+    errs = sorted(errs)
+    return {"directions": ndirs, "eps": eps, "max_rel_err": errs[-1], "median_rel_err": errs[len(errs) // 2]}
 
 
 def batch_domains(seed=3, count=64):
@@ -617,7 +703,7 @@ def make_domain_device(n, rng, torch_dtype):
     return t
 
 
-def run_batch_study(args, steps=10):
+def run_batch_study(args, steps=100):
     """BASELINE config 3: 64 periodic domains of uneven sizes (seed 3) in one
     batch (one CUDA-graph launch per step, tuned tile shape) against a loop of
     per-domain steps; FP64 and FP32.  Plus 16 tracers sharing one velocity on
