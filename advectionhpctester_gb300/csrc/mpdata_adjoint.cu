@@ -37,14 +37,18 @@ template <class R>
 __device__ __forceinline__ void addat(const Arr<R>& A, int i, int j, int k, R v) {
   atomicAdd(&A.at(i, j, k), v);
 }
-// xr(): the field with the xant halo rule (reflection or wrap)
-template <class R>
+// xr(): the field with the xant halo rule (reflection or wrap).  IN: the
+// index is inside the grid (a cell in [2, n-1] reading +-1), the map is the
+// identity.
+template <class R, bool IN = false>
 __device__ __forceinline__ void xr_add(const Geo& g, const Arr<R>& L, int i, int j, int k, R v) {
+  if (IN) { addat(L, i, j, k, v); return; }
   addat(L, g.bx ? wrapi(i, g.np) : refl(i, g.np), g.by ? wrapi(j, g.mp) : refl(j, g.mp), cz(g, k), v);
 }
 // fx/fy/fz<AIN>()
-template <class R, bool AIN>
+template <class R, bool AIN, bool IN = false>
 __device__ __forceinline__ void fx_add(const Geo& g, const Arr<R>& A, int f, int j, int k, R v) {
+  if (IN) { addat(A, f, j, k, v); return; }
   j = cy(g, j);
   k = cz(g, k);
   if (g.bx) { addat(A, wrapi(f, g.np), j, k, v); return; }
@@ -52,8 +56,9 @@ __device__ __forceinline__ void fx_add(const Geo& g, const Arr<R>& A, int f, int
   if (f <= 1 || f > g.np) return;  // wall faces are the constant 0
   addat(A, f, j, k, v);
 }
-template <class R, bool AIN>
+template <class R, bool AIN, bool IN = false>
 __device__ __forceinline__ void fy_add(const Geo& g, const Arr<R>& A, int i, int f, int k, R v) {
+  if (IN) { addat(A, i, f, k, v); return; }
   i = cx(g, i);
   k = cz(g, k);
   if (g.by) { addat(A, i, wrapi(f, g.mp), k, v); return; }
@@ -61,8 +66,9 @@ __device__ __forceinline__ void fy_add(const Geo& g, const Arr<R>& A, int i, int
   if (f <= 1 || f > g.mp) return;
   addat(A, i, f, k, v);
 }
-template <class R, bool AIN>
+template <class R, bool AIN, bool IN = false>
 __device__ __forceinline__ void fz_add(const Geo& g, const Arr<R>& A, int i, int j, int f, R v) {
+  if (IN) { addat(A, i, j, f, v); return; }
   i = cx(g, i);
   j = cy(g, j);
   if (g.bz) { addat(A, i, j, wrapi(f, g.lp), v); return; }
@@ -78,6 +84,20 @@ template <class R> __device__ __forceinline__ R dpn(R y) { return y < R(0) ? R(-
 template <class R> __device__ __forceinline__ R dabs(R y) { return sgn(y) ? R(-1) : R(1); }
 
 
+// Reverse kernels: the body is a device function of (i,j,k) templated on
+// IN; warps away from every wall take IN = true.
+#define ADISPATCH(CALL)                                      \
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;  \
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;  \
+  const int k = blockIdx.z + 1;                              \
+  const bool win = warp_interior(P.g, i, j, k);              \
+  if (i > P.g.np || j > P.g.mp) return;                      \
+  if (win) {                                                 \
+    CALL(true);                                              \
+  } else {                                                   \
+    CALL(false);                                             \
+  }
+
 #define ACELL                                                \
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;  \
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;  \
@@ -86,20 +106,26 @@ template <class R> __device__ __forceinline__ R dabs(R y) { return sgn(y) ? R(-1
   const Geo& g = P.g;
 
 // ---- update: x_new = rhr*(q - D/h), D = sum of signed limited fluxes -------
-template <class R>
-__global__ void __launch_bounds__(128) ka_update(const Prob<R> P, const AdjArr<R> A) {
-  ACELL
+template <class R, bool IN>
+__device__ __forceinline__ void ka_update_cell(const Prob<R>& P, const AdjArr<R>& A, int i, int j, int k) {
+  const Geo& g = P.g;
   const R ln = A.lam.ld(i, j, k);
   const R rh = P.rhr.ld(i, j, k);
   const R lt = rh * ln;                 // d x_new / d t, t = q - D/h
   A.lxant.at(i, j, k) = lt / rh;        // q = xant/rhr
   const R lD = -lt / P.h.ld(i, j, k);
-  fx_add<R, false>(g, A.lw1, i + 1, j, k, lD);
-  fx_add<R, false>(g, A.lw1, i, j, k, -lD);
-  fy_add<R, false>(g, A.lw2, i, j + 1, k, lD);
-  fy_add<R, false>(g, A.lw2, i, j, k, -lD);
-  fz_add<R, false>(g, A.lw3, i, j, k + 1, lD);
-  fz_add<R, false>(g, A.lw3, i, j, k, -lD);
+  fx_add<R, false, IN>(g, A.lw1, i + 1, j, k, lD);
+  fx_add<R, false, IN>(g, A.lw1, i, j, k, -lD);
+  fy_add<R, false, IN>(g, A.lw2, i, j + 1, k, lD);
+  fy_add<R, false, IN>(g, A.lw2, i, j, k, -lD);
+  fz_add<R, false, IN>(g, A.lw3, i, j, k + 1, lD);
+  fz_add<R, false, IN>(g, A.lw3, i, j, k, -lD);
+}
+template <class R>
+__global__ void __launch_bounds__(128) ka_update(const Prob<R> P, const AdjArr<R> A) {
+#define C(IN) ka_update_cell<R, IN>(P, A, i, j, k)
+  ADISPATCH(C)
+#undef C
 }
 
 // ---- limiter: w = pp(v)*min3(cp(c),cn(c-1)) - pn(v)*min3(cp(c-1),cn(c)) -------
@@ -112,9 +138,9 @@ __device__ __forceinline__ void min3_adj(R a, R b, R lam, const Arr<R>& La, int 
   if (!(R(1) < a)) addat(La, ia, ja, ka, lam);
 }
 
-template <class R, bool NONOS>
-__global__ void __launch_bounds__(128) ka_limit(const Prob<R> P, const AdjArr<R> A) {
-  ACELL
+template <class R, bool NONOS, bool IN>
+__device__ __forceinline__ void ka_limit_cell(const Prob<R>& P, const AdjArr<R>& A, int i, int j, int k) {
+  const Geo& g = P.g;
   const R cpc = NONOS ? P.cp.ld(i, j, k) : R(0), cnc = NONOS ? P.cn.ld(i, j, k) : R(0);
 #define LIMIT_FACE(V, LV, LW, IM, JM, KM)                                                  \
   {                                                                                        \
@@ -130,10 +156,16 @@ __global__ void __launch_bounds__(128) ka_limit(const Prob<R> P, const AdjArr<R>
       min3_adj(cpm, cnc, -lw * pn(v), A.lcp, IM, JM, KM, A.lcn, i, j, k);                   \
     }                                                                                      \
   }
-  if (g.bx || i > 1) LIMIT_FACE(P.v1, A.lv1, A.lw1, wrapi(i - 1, g.np), j, k)
-  if (g.by || j > 1) LIMIT_FACE(P.v2, A.lv2, A.lw2, i, wrapi(j - 1, g.mp), k)
-  if (g.bz || k > 1) LIMIT_FACE(P.v3, A.lv3, A.lw3, i, j, wrapi(k - 1, g.lp))
+  if (IN || g.bx || i > 1) LIMIT_FACE(P.v1, A.lv1, A.lw1, (IN ? i - 1 : wrapi(i - 1, g.np)), j, k)
+  if (IN || g.by || j > 1) LIMIT_FACE(P.v2, A.lv2, A.lw2, i, (IN ? j - 1 : wrapi(j - 1, g.mp)), k)
+  if (IN || g.bz || k > 1) LIMIT_FACE(P.v3, A.lv3, A.lw3, i, j, (IN ? k - 1 : wrapi(k - 1, g.lp)))
 #undef LIMIT_FACE
+}
+template <class R, bool NONOS>
+__global__ void __launch_bounds__(128) ka_limit(const Prob<R> P, const AdjArr<R> A) {
+#define C(IN) ka_limit_cell<R, NONOS, IN>(P, A, i, j, k)
+  ADISPATCH(C)
+#undef C
 }
 
 // ---- bounds: cp = (mx-x)h/Dp, cn = (x-mn)h/Dn -------------------------------
@@ -153,20 +185,20 @@ template <class R> __device__ __forceinline__ Arg<R> amin(Arg<R> a, Arg<R> b) { 
 // cp/cn part plus what the next pass carried back (lmx, lmn).
 // STD: the fluxes of the bounds are the unlimited donor fluxes f*ns (their
 // adjoint goes to lf); gauge: the pseudo-velocities themselves (lv).
-template <class R, bool FIRST, bool STD>
-__global__ void __launch_bounds__(128) ka_bounds(const Prob<R> P, const AdjArr<R> A) {
-  ACELL
-  const bool lo = g.bz || k > 1, hi = g.bz || k < g.lp;
+template <class R, bool FIRST, bool STD, bool IN>
+__device__ __forceinline__ void ka_bounds_cell(const Prob<R>& P, const AdjArr<R>& A, int i, int j, int k) {
+  const Geo& g = P.g;
+  const bool lo = IN || g.bz || k > 1, hi = IN || g.bz || k < g.lp;
   const Arr<R>& X = P.xant;
   const Arr<R>& xin = P.psi;
   // star cells: x_in with the zero-gradient map, the current field with the reflection map
-  const int im = g.bx ? wrapi(i - 1, g.np) : clampi(i - 1, g.np);
-  const int ip = g.bx ? wrapi(i + 1, g.np) : clampi(i + 1, g.np);
-  const int jm = g.by ? wrapi(j - 1, g.mp) : clampi(j - 1, g.mp);
-  const int jp = g.by ? wrapi(j + 1, g.mp) : clampi(j + 1, g.mp);
-  const int km = cz(g, k - 1), kp = cz(g, k + 1);
-  const int ri_m = g.bx ? wrapi(i - 1, g.np) : refl(i - 1, g.np), ri_p = g.bx ? wrapi(i + 1, g.np) : refl(i + 1, g.np);
-  const int rj_m = g.by ? wrapi(j - 1, g.mp) : refl(j - 1, g.mp), rj_p = g.by ? wrapi(j + 1, g.mp) : refl(j + 1, g.mp);
+  const int im = IN ? i - 1 : (g.bx ? wrapi(i - 1, g.np) : clampi(i - 1, g.np));
+  const int ip = IN ? i + 1 : (g.bx ? wrapi(i + 1, g.np) : clampi(i + 1, g.np));
+  const int jm = IN ? j - 1 : (g.by ? wrapi(j - 1, g.mp) : clampi(j - 1, g.mp));
+  const int jp = IN ? j + 1 : (g.by ? wrapi(j + 1, g.mp) : clampi(j + 1, g.mp));
+  const int km = cz<IN>(g, k - 1), kp = cz<IN>(g, k + 1);
+  const int ri_m = IN ? i - 1 : (g.bx ? wrapi(i - 1, g.np) : refl(i - 1, g.np)), ri_p = IN ? i + 1 : (g.bx ? wrapi(i + 1, g.np) : refl(i + 1, g.np));
+  const int rj_m = IN ? j - 1 : (g.by ? wrapi(j - 1, g.mp) : refl(j - 1, g.mp)), rj_p = IN ? j + 1 : (g.by ? wrapi(j + 1, g.mp) : refl(j + 1, g.mp));
   // element table: (i,j,k) of ids 0..13; id 14 is the previous extremum at (i,j,k)
   const int ci[15] = {im, i, ip, i, i, i, i, ri_m, i, ri_p, i, i, i, i, i};
   const int cj[15] = {j, j, j, jm, jp, j, j, j, j, j, rj_m, rj_p, j, j, j};
@@ -197,9 +229,9 @@ __global__ void __launch_bounds__(128) ka_bounds(const Prob<R> P, const AdjArr<R
   const Arr<R>& LF1 = STD ? A.lf1 : A.lv1;
   const Arr<R>& LF2 = STD ? A.lf2 : A.lv2;
   const Arr<R>& LF3 = STD ? A.lf3 : A.lv3;
-  const R e1 = fx<R, false>(g, F1, i + 1, j, k), w1 = fx<R, false>(g, F1, i, j, k);
-  const R e2 = fy<R, false>(g, F2, i, j + 1, k), w2 = fy<R, false>(g, F2, i, j, k);
-  const R e3 = fz<R, false>(g, F3, i, j, k + 1), w3 = fz<R, false>(g, F3, i, j, k);
+  const R e1 = fx<R, false, IN>(g, F1, i + 1, j, k), w1 = fx<R, false, IN>(g, F1, i, j, k);
+  const R e2 = fy<R, false, IN>(g, F2, i, j + 1, k), w2 = fy<R, false, IN>(g, F2, i, j, k);
+  const R e3 = fz<R, false, IN>(g, F3, i, j, k + 1), w3 = fz<R, false, IN>(g, F3, i, j, k);
   const R ep = Eps<R>::v;
   const R Dp = pn(e1) + pp(w1) + pn(e2) + pp(w2) + pn(e3) + pp(w3) + ep;
   const R Dn = pp(e1) + pn(w1) + pp(e2) + pn(w2) + pp(e3) + pn(w3) + ep;
@@ -215,12 +247,18 @@ __global__ void __launch_bounds__(128) ka_bounds(const Prob<R> P, const AdjArr<R
   // d/dD: -c/D
   const R lDp = -lcp * cpv / Dp, lDn = -lcn * cnv / Dn;
   // Dp = pn(e)+pp(w)+..., Dn = pp(e)+pn(w)+... over the six faces
-  fx_add<R, false>(g, LF1, i + 1, j, k, lDp * dpn(e1) + lDn * dpp(e1));
-  fx_add<R, false>(g, LF1, i, j, k, lDp * dpp(w1) + lDn * dpn(w1));
-  fy_add<R, false>(g, LF2, i, j + 1, k, lDp * dpn(e2) + lDn * dpp(e2));
-  fy_add<R, false>(g, LF2, i, j, k, lDp * dpp(w2) + lDn * dpn(w2));
-  fz_add<R, false>(g, LF3, i, j, k + 1, lDp * dpn(e3) + lDn * dpp(e3));
-  fz_add<R, false>(g, LF3, i, j, k, lDp * dpp(w3) + lDn * dpn(w3));
+  fx_add<R, false, IN>(g, LF1, i + 1, j, k, lDp * dpn(e1) + lDn * dpp(e1));
+  fx_add<R, false, IN>(g, LF1, i, j, k, lDp * dpp(w1) + lDn * dpn(w1));
+  fy_add<R, false, IN>(g, LF2, i, j + 1, k, lDp * dpn(e2) + lDn * dpp(e2));
+  fy_add<R, false, IN>(g, LF2, i, j, k, lDp * dpp(w2) + lDn * dpn(w2));
+  fz_add<R, false, IN>(g, LF3, i, j, k + 1, lDp * dpn(e3) + lDn * dpp(e3));
+  fz_add<R, false, IN>(g, LF3, i, j, k, lDp * dpp(w3) + lDn * dpn(w3));
+}
+template <class R, bool FIRST, bool STD>
+__global__ void __launch_bounds__(128) ka_bounds(const Prob<R> P, const AdjArr<R> A) {
+#define C(IN) ka_bounds_cell<R, FIRST, STD, IN>(P, A, i, j, k)
+  ADISPATCH(C)
+#undef C
 }
 
 // ---- pseudo-velocity (gauge): v = vdyf(xl,xr,a,hm) - 0.125*a*hm*cr ------------
@@ -228,145 +266,157 @@ __global__ void __launch_bounds__(128) ka_bounds(const Prob<R> P, const AdjArr<R
 // AIN: a = the caller's Courant numbers (gradient into gu); otherwise a = the
 // previous pass's limited velocities, read with the wall rule (gradient into
 // that pass's lambda_w).
-template <class R, bool AIN>
-__global__ void __launch_bounds__(128) ka_pseudo(const Prob<R> P, const AdjArr<R> A) {
-  ACELL
+template <class R, bool AIN, bool IN>
+__device__ __forceinline__ void ka_pseudo_cell(const Prob<R>& P, const AdjArr<R>& A, int i, int j, int k) {
+  const Geo& g = P.g;
   const Arr<R>& X = P.xant;
   const Arr<R>& U1 = AIN ? P.u1 : P.w1;
   const Arr<R>& U2 = AIN ? P.u2 : P.w2;
   const Arr<R>& U3 = AIN ? P.u3 : P.w3;
-  const bool zt = g.bz || (k > 1 && k < g.lp);
-#define XX(a, b, c) xr<R>(g, X, (a), (b), (c))
-#define LX(a, b, c, v) xr_add<R>(g, A.lxant, (a), (b), (c), (v))
+  const bool zt = IN || g.bz || (k > 1 && k < g.lp);
+#define XX(a, b, c) xr<R, IN>(g, X, (a), (b), (c))
+#define LX(a, b, c, v) xr_add<R, IN>(g, A.lxant, (a), (b), (c), (v))
   // x faces
-  if (g.bx || i > 1) {
+  if (IN || g.bx || i > 1) {
     const R lv = A.lv1.ld(i, j, k);
-    const R hm = P.hmx.ld(i, j, k), a = fx<R, AIN>(g, U1, i, j, k);
+    const R hm = P.hmx.ld(i, j, k), a = fx<R, AIN, IN>(g, U1, i, j, k);
     const R xl = XX(i - 1, j, k), xrr = XX(i, j, k);
-    const R S2 = fy<R, AIN>(g, U2, i - 1, j, k) + fy<R, AIN>(g, U2, i - 1, j + 1, k) +
-                 fy<R, AIN>(g, U2, i, j + 1, k) + fy<R, AIN>(g, U2, i, j, k);
+    const R S2 = fy<R, AIN, IN>(g, U2, i - 1, j, k) + fy<R, AIN, IN>(g, U2, i - 1, j + 1, k) +
+                 fy<R, AIN, IN>(g, U2, i, j + 1, k) + fy<R, AIN, IN>(g, U2, i, j, k);
     const R R2 = rat4(XX(i - 1, j - 1, k), XX(i, j - 1, k), XX(i - 1, j + 1, k), XX(i, j + 1, k));
     R cr = S2 * R2, S3 = R(0), R3 = R(0);
     if (zt) {
-      S3 = fz<R, AIN>(g, U3, i - 1, j, k) + fz<R, AIN>(g, U3, i - 1, j, k + 1) +
-           fz<R, AIN>(g, U3, i, j, k + 1) + fz<R, AIN>(g, U3, i, j, k);
+      S3 = fz<R, AIN, IN>(g, U3, i - 1, j, k) + fz<R, AIN, IN>(g, U3, i - 1, j, k + 1) +
+           fz<R, AIN, IN>(g, U3, i, j, k + 1) + fz<R, AIN, IN>(g, U3, i, j, k);
       R3 = rat4(XX(i - 1, j, k - 1), XX(i, j, k - 1), XX(i - 1, j, k + 1), XX(i, j, k + 1));
       cr = cr + S3 * R3;
     }
     const R K = (fabs(a) - a * a * hm) * R(0.5);
     const R la = lv * ((dabs(a) - R(2) * a * hm) * (xrr - xl) * R(0.5) - R(0.125) * hm * cr);
-    fx_add<R, AIN>(g, A.la1, i, j, k, la);
+    fx_add<R, AIN, IN>(g, A.la1, i, j, k, la);
     LX(i, j, k, lv * K);
     LX(i - 1, j, k, -lv * K);
     const R lcr = -lv * R(0.125) * a * hm;
     const R lS2 = lcr * R2, lR2 = lcr * S2 * R(0.25);
-    fy_add<R, AIN>(g, A.la2, i - 1, j, k, lS2);
-    fy_add<R, AIN>(g, A.la2, i - 1, j + 1, k, lS2);
-    fy_add<R, AIN>(g, A.la2, i, j + 1, k, lS2);
-    fy_add<R, AIN>(g, A.la2, i, j, k, lS2);
+    fy_add<R, AIN, IN>(g, A.la2, i - 1, j, k, lS2);
+    fy_add<R, AIN, IN>(g, A.la2, i - 1, j + 1, k, lS2);
+    fy_add<R, AIN, IN>(g, A.la2, i, j + 1, k, lS2);
+    fy_add<R, AIN, IN>(g, A.la2, i, j, k, lS2);
     LX(i, j + 1, k, lR2); LX(i - 1, j + 1, k, lR2); LX(i, j - 1, k, -lR2); LX(i - 1, j - 1, k, -lR2);
     if (zt) {
       const R lS3 = lcr * R3, lR3 = lcr * S3 * R(0.25);
-      fz_add<R, AIN>(g, A.la3, i - 1, j, k, lS3);
-      fz_add<R, AIN>(g, A.la3, i - 1, j, k + 1, lS3);
-      fz_add<R, AIN>(g, A.la3, i, j, k + 1, lS3);
-      fz_add<R, AIN>(g, A.la3, i, j, k, lS3);
+      fz_add<R, AIN, IN>(g, A.la3, i - 1, j, k, lS3);
+      fz_add<R, AIN, IN>(g, A.la3, i - 1, j, k + 1, lS3);
+      fz_add<R, AIN, IN>(g, A.la3, i, j, k + 1, lS3);
+      fz_add<R, AIN, IN>(g, A.la3, i, j, k, lS3);
       LX(i, j, k + 1, lR3); LX(i - 1, j, k + 1, lR3); LX(i, j, k - 1, -lR3); LX(i - 1, j, k - 1, -lR3);
     }
   }
   // y faces
-  if (g.by || j > 1) {
+  if (IN || g.by || j > 1) {
     const R lv = A.lv2.ld(i, j, k);
-    const R hm = P.hmy.ld(i, j, k), a = fy<R, AIN>(g, U2, i, j, k);
+    const R hm = P.hmy.ld(i, j, k), a = fy<R, AIN, IN>(g, U2, i, j, k);
     const R xl = XX(i, j - 1, k), xrr = XX(i, j, k);
-    const R S1 = fx<R, AIN>(g, U1, i, j - 1, k) + fx<R, AIN>(g, U1, i, j, k) +
-                 fx<R, AIN>(g, U1, i + 1, j, k) + fx<R, AIN>(g, U1, i + 1, j - 1, k);
+    const R S1 = fx<R, AIN, IN>(g, U1, i, j - 1, k) + fx<R, AIN, IN>(g, U1, i, j, k) +
+                 fx<R, AIN, IN>(g, U1, i + 1, j, k) + fx<R, AIN, IN>(g, U1, i + 1, j - 1, k);
     const R R1 = rat4(XX(i - 1, j - 1, k), XX(i - 1, j, k), XX(i + 1, j - 1, k), XX(i + 1, j, k));
     R cr = S1 * R1, S3 = R(0), R3 = R(0);
     if (zt) {
-      S3 = fz<R, AIN>(g, U3, i, j - 1, k) + fz<R, AIN>(g, U3, i, j, k) +
-           fz<R, AIN>(g, U3, i, j, k + 1) + fz<R, AIN>(g, U3, i, j - 1, k + 1);
+      S3 = fz<R, AIN, IN>(g, U3, i, j - 1, k) + fz<R, AIN, IN>(g, U3, i, j, k) +
+           fz<R, AIN, IN>(g, U3, i, j, k + 1) + fz<R, AIN, IN>(g, U3, i, j - 1, k + 1);
       R3 = rat4(XX(i, j - 1, k - 1), XX(i, j, k - 1), XX(i, j - 1, k + 1), XX(i, j, k + 1));
       cr = cr + S3 * R3;
     }
     const R K = (fabs(a) - a * a * hm) * R(0.5);
     const R la = lv * ((dabs(a) - R(2) * a * hm) * (xrr - xl) * R(0.5) - R(0.125) * hm * cr);
-    fy_add<R, AIN>(g, A.la2, i, j, k, la);
+    fy_add<R, AIN, IN>(g, A.la2, i, j, k, la);
     LX(i, j, k, lv * K);
     LX(i, j - 1, k, -lv * K);
     const R lcr = -lv * R(0.125) * a * hm;
     const R lS1 = lcr * R1, lR1 = lcr * S1 * R(0.25);
-    fx_add<R, AIN>(g, A.la1, i, j - 1, k, lS1);
-    fx_add<R, AIN>(g, A.la1, i, j, k, lS1);
-    fx_add<R, AIN>(g, A.la1, i + 1, j, k, lS1);
-    fx_add<R, AIN>(g, A.la1, i + 1, j - 1, k, lS1);
+    fx_add<R, AIN, IN>(g, A.la1, i, j - 1, k, lS1);
+    fx_add<R, AIN, IN>(g, A.la1, i, j, k, lS1);
+    fx_add<R, AIN, IN>(g, A.la1, i + 1, j, k, lS1);
+    fx_add<R, AIN, IN>(g, A.la1, i + 1, j - 1, k, lS1);
     LX(i + 1, j, k, lR1); LX(i + 1, j - 1, k, lR1); LX(i - 1, j, k, -lR1); LX(i - 1, j - 1, k, -lR1);
     if (zt) {
       const R lS3 = lcr * R3, lR3 = lcr * S3 * R(0.25);
-      fz_add<R, AIN>(g, A.la3, i, j - 1, k, lS3);
-      fz_add<R, AIN>(g, A.la3, i, j, k, lS3);
-      fz_add<R, AIN>(g, A.la3, i, j, k + 1, lS3);
-      fz_add<R, AIN>(g, A.la3, i, j - 1, k + 1, lS3);
+      fz_add<R, AIN, IN>(g, A.la3, i, j - 1, k, lS3);
+      fz_add<R, AIN, IN>(g, A.la3, i, j, k, lS3);
+      fz_add<R, AIN, IN>(g, A.la3, i, j, k + 1, lS3);
+      fz_add<R, AIN, IN>(g, A.la3, i, j - 1, k + 1, lS3);
       LX(i, j, k + 1, lR3); LX(i, j - 1, k + 1, lR3); LX(i, j, k - 1, -lR3); LX(i, j - 1, k - 1, -lR3);
     }
   }
   // z faces
-  if (g.bz || k > 1) {
+  if (IN || g.bz || k > 1) {
     const R lv = A.lv3.ld(i, j, k);
-    const R hm = P.hmz.ld(i, j, k), a = fz<R, AIN>(g, U3, i, j, k);
+    const R hm = P.hmz.ld(i, j, k), a = fz<R, AIN, IN>(g, U3, i, j, k);
     const R xl = XX(i, j, k - 1), xrr = XX(i, j, k);
-    const R S1 = fx<R, AIN>(g, U1, i, j, k - 1) + fx<R, AIN>(g, U1, i, j, k) +
-                 fx<R, AIN>(g, U1, i + 1, j, k) + fx<R, AIN>(g, U1, i + 1, j, k - 1);
+    const R S1 = fx<R, AIN, IN>(g, U1, i, j, k - 1) + fx<R, AIN, IN>(g, U1, i, j, k) +
+                 fx<R, AIN, IN>(g, U1, i + 1, j, k) + fx<R, AIN, IN>(g, U1, i + 1, j, k - 1);
     const R R1 = rat4(XX(i - 1, j, k - 1), XX(i - 1, j, k), XX(i + 1, j, k - 1), XX(i + 1, j, k));
-    const R S2 = fy<R, AIN>(g, U2, i, j, k - 1) + fy<R, AIN>(g, U2, i, j + 1, k - 1) +
-                 fy<R, AIN>(g, U2, i, j + 1, k) + fy<R, AIN>(g, U2, i, j, k);
+    const R S2 = fy<R, AIN, IN>(g, U2, i, j, k - 1) + fy<R, AIN, IN>(g, U2, i, j + 1, k - 1) +
+                 fy<R, AIN, IN>(g, U2, i, j + 1, k) + fy<R, AIN, IN>(g, U2, i, j, k);
     const R R2 = rat4(XX(i, j - 1, k - 1), XX(i, j - 1, k), XX(i, j + 1, k - 1), XX(i, j + 1, k));
     const R cr = S1 * R1 + S2 * R2;
     const R K = (fabs(a) - a * a * hm) * R(0.5);
     const R la = lv * ((dabs(a) - R(2) * a * hm) * (xrr - xl) * R(0.5) - R(0.125) * hm * cr);
-    fz_add<R, AIN>(g, A.la3, i, j, k, la);
+    fz_add<R, AIN, IN>(g, A.la3, i, j, k, la);
     LX(i, j, k, lv * K);
     LX(i, j, k - 1, -lv * K);
     const R lcr = -lv * R(0.125) * a * hm;
     const R lS1 = lcr * R1, lR1 = lcr * S1 * R(0.25);
-    fx_add<R, AIN>(g, A.la1, i, j, k - 1, lS1);
-    fx_add<R, AIN>(g, A.la1, i, j, k, lS1);
-    fx_add<R, AIN>(g, A.la1, i + 1, j, k, lS1);
-    fx_add<R, AIN>(g, A.la1, i + 1, j, k - 1, lS1);
+    fx_add<R, AIN, IN>(g, A.la1, i, j, k - 1, lS1);
+    fx_add<R, AIN, IN>(g, A.la1, i, j, k, lS1);
+    fx_add<R, AIN, IN>(g, A.la1, i + 1, j, k, lS1);
+    fx_add<R, AIN, IN>(g, A.la1, i + 1, j, k - 1, lS1);
     LX(i + 1, j, k, lR1); LX(i + 1, j, k - 1, lR1); LX(i - 1, j, k, -lR1); LX(i - 1, j, k - 1, -lR1);
     const R lS2 = lcr * R2, lR2 = lcr * S2 * R(0.25);
-    fy_add<R, AIN>(g, A.la2, i, j, k - 1, lS2);
-    fy_add<R, AIN>(g, A.la2, i, j + 1, k - 1, lS2);
-    fy_add<R, AIN>(g, A.la2, i, j + 1, k, lS2);
-    fy_add<R, AIN>(g, A.la2, i, j, k, lS2);
+    fy_add<R, AIN, IN>(g, A.la2, i, j, k - 1, lS2);
+    fy_add<R, AIN, IN>(g, A.la2, i, j + 1, k - 1, lS2);
+    fy_add<R, AIN, IN>(g, A.la2, i, j + 1, k, lS2);
+    fy_add<R, AIN, IN>(g, A.la2, i, j, k, lS2);
     LX(i, j + 1, k, lR2); LX(i, j + 1, k - 1, lR2); LX(i, j - 1, k, -lR2); LX(i, j - 1, k - 1, -lR2);
   }
 #undef XX
 #undef LX
 }
+template <class R, bool AIN>
+__global__ void __launch_bounds__(128) ka_pseudo(const Prob<R> P, const AdjArr<R> A) {
+#define C(IN) ka_pseudo_cell<R, AIN, IN>(P, A, i, j, k)
+  ADISPATCH(C)
+#undef C
+}
 
 // ---- standard form (antidiff3d-standard-gpubc.f90) ---------------------------
 // update: x_out = rhr*(q - d*hinv), d = signed sum of the limited fluxes g
-template <class R>
-__global__ void __launch_bounds__(128) ka_update_std(const Prob<R> P, const AdjArr<R> A) {
-  ACELL
+template <class R, bool IN>
+__device__ __forceinline__ void ka_update_std_cell(const Prob<R>& P, const AdjArr<R>& A, int i, int j, int k) {
+  const Geo& g = P.g;
   const R lt = P.rhr.ld(i, j, k) * A.lam.ld(i, j, k);
   addat(A.lq, i, j, k, lt);
   const R lD = -lt * P.hinv.ld(i, j, k);
-  fx_add<R, false>(g, A.lg1, i + 1, j, k, lD);
-  fx_add<R, false>(g, A.lg1, i, j, k, -lD);
-  fy_add<R, false>(g, A.lg2, i, j + 1, k, lD);
-  fy_add<R, false>(g, A.lg2, i, j, k, -lD);
-  fz_add<R, false>(g, A.lg3, i, j, k + 1, lD);
-  fz_add<R, false>(g, A.lg3, i, j, k, -lD);
+  fx_add<R, false, IN>(g, A.lg1, i + 1, j, k, lD);
+  fx_add<R, false, IN>(g, A.lg1, i, j, k, -lD);
+  fy_add<R, false, IN>(g, A.lg2, i, j + 1, k, lD);
+  fy_add<R, false, IN>(g, A.lg2, i, j, k, -lD);
+  fz_add<R, false, IN>(g, A.lg3, i, j, k + 1, lD);
+  fz_add<R, false, IN>(g, A.lg3, i, j, k, -lD);
+}
+template <class R>
+__global__ void __launch_bounds__(128) ka_update_std(const Prob<R> P, const AdjArr<R> A) {
+#define C(IN) ka_update_std_cell<R, IN>(P, A, i, j, k)
+  ADISPATCH(C)
+#undef C
 }
 
 // limiter: w = vlim_std(v, a1, a2, x(c-1), x(c)) with a1 = min3(cp(c), cn(c-1)),
 // a2 = min3(cp(c-1), cn(c)); g = donor(q(c-1), q(c), w).  possign() is
 // piecewise constant: only v, a1 and a2 carry a derivative through it.
-template <class R, bool NONOS>
-__global__ void __launch_bounds__(128) ka_limit_std(const Prob<R> P, const AdjArr<R> A) {
-  ACELL
+template <class R, bool NONOS, bool IN>
+__device__ __forceinline__ void ka_limit_std_cell(const Prob<R>& P, const AdjArr<R>& A, int i, int j, int k) {
+  const Geo& g = P.g;
   const Arr<R>& X = P.xant;
   const R cpc = NONOS ? P.cp.ld(i, j, k) : R(0), cnc = NONOS ? P.cn.ld(i, j, k) : R(0);
   const R xc = X.ld(i, j, k), qc = P.q.ld(i, j, k);
@@ -395,10 +445,16 @@ __global__ void __launch_bounds__(128) ka_limit_std(const Prob<R> P, const AdjAr
       min3_adj(cpm, cnc, lw * (pp(v) * sml - pn(v) * sr), A.lcp, IM, JM, KM, A.lcn, i, j, k);          \
     }                                                                                                   \
   }
-  if (g.bx || i > 1) LIMIT_STD_FACE(P.v1, A.lv1, A.lw1, A.lg1, wrapi(i - 1, g.np), j, k)
-  if (g.by || j > 1) LIMIT_STD_FACE(P.v2, A.lv2, A.lw2, A.lg2, i, wrapi(j - 1, g.mp), k)
-  if (g.bz || k > 1) LIMIT_STD_FACE(P.v3, A.lv3, A.lw3, A.lg3, i, j, wrapi(k - 1, g.lp))
+  if (IN || g.bx || i > 1) LIMIT_STD_FACE(P.v1, A.lv1, A.lw1, A.lg1, (IN ? i - 1 : wrapi(i - 1, g.np)), j, k)
+  if (IN || g.by || j > 1) LIMIT_STD_FACE(P.v2, A.lv2, A.lw2, A.lg2, i, (IN ? j - 1 : wrapi(j - 1, g.mp)), k)
+  if (IN || g.bz || k > 1) LIMIT_STD_FACE(P.v3, A.lv3, A.lw3, A.lg3, i, j, (IN ? k - 1 : wrapi(k - 1, g.lp)))
 #undef LIMIT_STD_FACE
+}
+template <class R, bool NONOS>
+__global__ void __launch_bounds__(128) ka_limit_std(const Prob<R> P, const AdjArr<R> A) {
+#define C(IN) ka_limit_std_cell<R, NONOS, IN>(P, A, i, j, k)
+  ADISPATCH(C)
+#undef C
 }
 
 // vcorra(a, b, y1, y2, hm) = -(0.125*a*b*y1*hm/y2) with y1 = (|p1|+|p2|)-(|m1|+|m2|),
@@ -408,38 +464,38 @@ struct VcTerm {
   R lb;  // lambda of b
   R la;  // lambda of a
 };
-template <class R>
+template <class R, bool IN>
 __device__ __forceinline__ VcTerm<R> vcorra_adj(const Geo& g, const Arr<R>& X, const Arr<R>& LX, R lv, R a, R b,
                                                 R hm, int pi1, int pj1, int pk1, int pi2, int pj2, int pk2,
                                                 int mi1, int mj1, int mk1, int mi2, int mj2, int mk2) {
-  const R p1 = xr<R>(g, X, pi1, pj1, pk1), p2 = xr<R>(g, X, pi2, pj2, pk2);
-  const R m1 = xr<R>(g, X, mi1, mj1, mk1), m2 = xr<R>(g, X, mi2, mj2, mk2);
+  const R p1 = xr<R, IN>(g, X, pi1, pj1, pk1), p2 = xr<R, IN>(g, X, pi2, pj2, pk2);
+  const R m1 = xr<R, IN>(g, X, mi1, mj1, mk1), m2 = xr<R, IN>(g, X, mi2, mj2, mk2);
   const R y1 = (fabs(p1) + fabs(p2)) - (fabs(m1) + fabs(m2));
   const R y2 = fabs(p1) + fabs(p2) + fabs(m1) + fabs(m2) + Eps<R>::v;
   const R t = -R(0.125) * hm;
   const R dy1 = t * a * b / y2, dy2 = -t * a * b * y1 / (y2 * y2);
-  xr_add<R>(g, LX, pi1, pj1, pk1, lv * (dy1 + dy2) * dabs(p1));
-  xr_add<R>(g, LX, pi2, pj2, pk2, lv * (dy1 + dy2) * dabs(p2));
-  xr_add<R>(g, LX, mi1, mj1, mk1, lv * (dy2 - dy1) * dabs(m1));
-  xr_add<R>(g, LX, mi2, mj2, mk2, lv * (dy2 - dy1) * dabs(m2));
+  xr_add<R, IN>(g, LX, pi1, pj1, pk1, lv * (dy1 + dy2) * dabs(p1));
+  xr_add<R, IN>(g, LX, pi2, pj2, pk2, lv * (dy1 + dy2) * dabs(p2));
+  xr_add<R, IN>(g, LX, mi1, mj1, mk1, lv * (dy2 - dy1) * dabs(m1));
+  xr_add<R, IN>(g, LX, mi2, mj2, mk2, lv * (dy2 - dy1) * dabs(m2));
   return VcTerm<R>{lv * t * a * y1 / y2, lv * t * b * y1 / y2};
 }
 
 // pseudo-velocity: f*ns = donor(xl, xr, v) first, then
 // v = vdyfa(xl, xr, a, hm) + vcorra(cross 1) [+ vcorra(cross 2)], and the
 // q = x/rhr of the limiter's fluxes back into x.
-template <class R, bool AIN>
-__global__ void __launch_bounds__(128) ka_pseudo_std(const Prob<R> P, const AdjArr<R> A) {
-  ACELL
+template <class R, bool AIN, bool IN>
+__device__ __forceinline__ void ka_pseudo_std_cell(const Prob<R>& P, const AdjArr<R>& A, int i, int j, int k) {
+  const Geo& g = P.g;
   const Arr<R>& X = P.xant;
   const Arr<R>& U1 = AIN ? P.u1 : P.w1;
   const Arr<R>& U2 = AIN ? P.u2 : P.w2;
   const Arr<R>& U3 = AIN ? P.u3 : P.w3;
   const R ep = Eps<R>::v;
-  const bool zt = g.bz || (k > 1 && k < g.lp);
+  const bool zt = IN || g.bz || (k > 1 && k < g.lp);
   addat(A.lxant, i, j, k, A.lq.ld(i, j, k) / P.rhr.ld(i, j, k));
-#define XX(a, b, c) xr<R>(g, X, (a), (b), (c))
-#define LX(a, b, c, v) xr_add<R>(g, A.lxant, (a), (b), (c), (v))
+#define XX(a, b, c) xr<R, IN>(g, X, (a), (b), (c))
+#define LX(a, b, c, v) xr_add<R, IN>(g, A.lxant, (a), (b), (c), (v))
   // the face's own velocity, donor flux and vdyfa; returns lambda of v after f*ns
 #define FACE_HEAD(LV, LF, V, AF, HM, XLI, XLJ, XLK)                                                     \
   const R v = V.ld(i, j, k), hm = HM.ld(i, j, k), a = AF;                                           \
@@ -452,87 +508,93 @@ __global__ void __launch_bounds__(128) ka_pseudo_std(const Prob<R> P, const AdjA
   R la = lv * (dabs(a) - R(2) * a * hm) * N / Dd;                                                   \
   LX(i, j, k, lv * K * dabs(xrr) * (Dd - N) / (Dd * Dd));                                           \
   LX(XLI, XLJ, XLK, -lv * K * dabs(xl) * (Dd + N) / (Dd * Dd));
-  if (g.bx || i > 1) {
-    FACE_HEAD(A.lv1, A.lf1, P.v1, (fx<R, AIN>(g, U1, i, j, k)), P.hmx, i - 1, j, k)
+  if (IN || g.bx || i > 1) {
+    FACE_HEAD(A.lv1, A.lf1, P.v1, (fx<R, AIN, IN>(g, U1, i, j, k)), P.hmx, i - 1, j, k)
     {
-      const R b = fy<R, AIN>(g, U2, i - 1, j, k) + fy<R, AIN>(g, U2, i - 1, j + 1, k) +
-                  fy<R, AIN>(g, U2, i, j + 1, k) + fy<R, AIN>(g, U2, i, j, k);
-      const VcTerm<R> c = vcorra_adj<R>(g, X, A.lxant, lv, a, b, hm, i - 1, j + 1, k, i, j + 1, k, i - 1, j - 1, k,
+      const R b = fy<R, AIN, IN>(g, U2, i - 1, j, k) + fy<R, AIN, IN>(g, U2, i - 1, j + 1, k) +
+                  fy<R, AIN, IN>(g, U2, i, j + 1, k) + fy<R, AIN, IN>(g, U2, i, j, k);
+      const VcTerm<R> c = vcorra_adj<R, IN>(g, X, A.lxant, lv, a, b, hm, i - 1, j + 1, k, i, j + 1, k, i - 1, j - 1, k,
                                         i, j - 1, k);
       la += c.la;
-      fy_add<R, AIN>(g, A.la2, i - 1, j, k, c.lb);
-      fy_add<R, AIN>(g, A.la2, i - 1, j + 1, k, c.lb);
-      fy_add<R, AIN>(g, A.la2, i, j + 1, k, c.lb);
-      fy_add<R, AIN>(g, A.la2, i, j, k, c.lb);
+      fy_add<R, AIN, IN>(g, A.la2, i - 1, j, k, c.lb);
+      fy_add<R, AIN, IN>(g, A.la2, i - 1, j + 1, k, c.lb);
+      fy_add<R, AIN, IN>(g, A.la2, i, j + 1, k, c.lb);
+      fy_add<R, AIN, IN>(g, A.la2, i, j, k, c.lb);
     }
     if (zt) {
-      const R b = fz<R, AIN>(g, U3, i - 1, j, k) + fz<R, AIN>(g, U3, i - 1, j, k + 1) +
-                  fz<R, AIN>(g, U3, i, j, k + 1) + fz<R, AIN>(g, U3, i, j, k);
-      const VcTerm<R> c = vcorra_adj<R>(g, X, A.lxant, lv, a, b, hm, i - 1, j, k + 1, i, j, k + 1, i - 1, j, k - 1,
+      const R b = fz<R, AIN, IN>(g, U3, i - 1, j, k) + fz<R, AIN, IN>(g, U3, i - 1, j, k + 1) +
+                  fz<R, AIN, IN>(g, U3, i, j, k + 1) + fz<R, AIN, IN>(g, U3, i, j, k);
+      const VcTerm<R> c = vcorra_adj<R, IN>(g, X, A.lxant, lv, a, b, hm, i - 1, j, k + 1, i, j, k + 1, i - 1, j, k - 1,
                                         i, j, k - 1);
       la += c.la;
-      fz_add<R, AIN>(g, A.la3, i - 1, j, k, c.lb);
-      fz_add<R, AIN>(g, A.la3, i - 1, j, k + 1, c.lb);
-      fz_add<R, AIN>(g, A.la3, i, j, k + 1, c.lb);
-      fz_add<R, AIN>(g, A.la3, i, j, k, c.lb);
+      fz_add<R, AIN, IN>(g, A.la3, i - 1, j, k, c.lb);
+      fz_add<R, AIN, IN>(g, A.la3, i - 1, j, k + 1, c.lb);
+      fz_add<R, AIN, IN>(g, A.la3, i, j, k + 1, c.lb);
+      fz_add<R, AIN, IN>(g, A.la3, i, j, k, c.lb);
     }
-    fx_add<R, AIN>(g, A.la1, i, j, k, la);
+    fx_add<R, AIN, IN>(g, A.la1, i, j, k, la);
   }
-  if (g.by || j > 1) {
-    FACE_HEAD(A.lv2, A.lf2, P.v2, (fy<R, AIN>(g, U2, i, j, k)), P.hmy, i, j - 1, k)
+  if (IN || g.by || j > 1) {
+    FACE_HEAD(A.lv2, A.lf2, P.v2, (fy<R, AIN, IN>(g, U2, i, j, k)), P.hmy, i, j - 1, k)
     {
-      const R b = fx<R, AIN>(g, U1, i, j - 1, k) + fx<R, AIN>(g, U1, i, j, k) + fx<R, AIN>(g, U1, i + 1, j, k) +
-                  fx<R, AIN>(g, U1, i + 1, j - 1, k);
-      const VcTerm<R> c = vcorra_adj<R>(g, X, A.lxant, lv, a, b, hm, i + 1, j - 1, k, i + 1, j, k, i - 1, j - 1, k,
+      const R b = fx<R, AIN, IN>(g, U1, i, j - 1, k) + fx<R, AIN, IN>(g, U1, i, j, k) + fx<R, AIN, IN>(g, U1, i + 1, j, k) +
+                  fx<R, AIN, IN>(g, U1, i + 1, j - 1, k);
+      const VcTerm<R> c = vcorra_adj<R, IN>(g, X, A.lxant, lv, a, b, hm, i + 1, j - 1, k, i + 1, j, k, i - 1, j - 1, k,
                                         i - 1, j, k);
       la += c.la;
-      fx_add<R, AIN>(g, A.la1, i, j - 1, k, c.lb);
-      fx_add<R, AIN>(g, A.la1, i, j, k, c.lb);
-      fx_add<R, AIN>(g, A.la1, i + 1, j, k, c.lb);
-      fx_add<R, AIN>(g, A.la1, i + 1, j - 1, k, c.lb);
+      fx_add<R, AIN, IN>(g, A.la1, i, j - 1, k, c.lb);
+      fx_add<R, AIN, IN>(g, A.la1, i, j, k, c.lb);
+      fx_add<R, AIN, IN>(g, A.la1, i + 1, j, k, c.lb);
+      fx_add<R, AIN, IN>(g, A.la1, i + 1, j - 1, k, c.lb);
     }
     if (zt) {
-      const R b = fz<R, AIN>(g, U3, i, j - 1, k) + fz<R, AIN>(g, U3, i, j, k) + fz<R, AIN>(g, U3, i, j, k + 1) +
-                  fz<R, AIN>(g, U3, i, j - 1, k + 1);
-      const VcTerm<R> c = vcorra_adj<R>(g, X, A.lxant, lv, a, b, hm, i, j - 1, k + 1, i, j, k + 1, i, j - 1, k - 1,
+      const R b = fz<R, AIN, IN>(g, U3, i, j - 1, k) + fz<R, AIN, IN>(g, U3, i, j, k) + fz<R, AIN, IN>(g, U3, i, j, k + 1) +
+                  fz<R, AIN, IN>(g, U3, i, j - 1, k + 1);
+      const VcTerm<R> c = vcorra_adj<R, IN>(g, X, A.lxant, lv, a, b, hm, i, j - 1, k + 1, i, j, k + 1, i, j - 1, k - 1,
                                         i, j, k - 1);
       la += c.la;
-      fz_add<R, AIN>(g, A.la3, i, j - 1, k, c.lb);
-      fz_add<R, AIN>(g, A.la3, i, j, k, c.lb);
-      fz_add<R, AIN>(g, A.la3, i, j, k + 1, c.lb);
-      fz_add<R, AIN>(g, A.la3, i, j - 1, k + 1, c.lb);
+      fz_add<R, AIN, IN>(g, A.la3, i, j - 1, k, c.lb);
+      fz_add<R, AIN, IN>(g, A.la3, i, j, k, c.lb);
+      fz_add<R, AIN, IN>(g, A.la3, i, j, k + 1, c.lb);
+      fz_add<R, AIN, IN>(g, A.la3, i, j - 1, k + 1, c.lb);
     }
-    fy_add<R, AIN>(g, A.la2, i, j, k, la);
+    fy_add<R, AIN, IN>(g, A.la2, i, j, k, la);
   }
-  if (g.bz || k > 1) {
-    FACE_HEAD(A.lv3, A.lf3, P.v3, (fz<R, AIN>(g, U3, i, j, k)), P.hmz, i, j, k - 1)
+  if (IN || g.bz || k > 1) {
+    FACE_HEAD(A.lv3, A.lf3, P.v3, (fz<R, AIN, IN>(g, U3, i, j, k)), P.hmz, i, j, k - 1)
     {
-      const R b = fx<R, AIN>(g, U1, i, j, k - 1) + fx<R, AIN>(g, U1, i, j, k) + fx<R, AIN>(g, U1, i + 1, j, k) +
-                  fx<R, AIN>(g, U1, i + 1, j, k - 1);
-      const VcTerm<R> c = vcorra_adj<R>(g, X, A.lxant, lv, a, b, hm, i + 1, j, k - 1, i + 1, j, k, i - 1, j, k - 1,
+      const R b = fx<R, AIN, IN>(g, U1, i, j, k - 1) + fx<R, AIN, IN>(g, U1, i, j, k) + fx<R, AIN, IN>(g, U1, i + 1, j, k) +
+                  fx<R, AIN, IN>(g, U1, i + 1, j, k - 1);
+      const VcTerm<R> c = vcorra_adj<R, IN>(g, X, A.lxant, lv, a, b, hm, i + 1, j, k - 1, i + 1, j, k, i - 1, j, k - 1,
                                         i - 1, j, k);
       la += c.la;
-      fx_add<R, AIN>(g, A.la1, i, j, k - 1, c.lb);
-      fx_add<R, AIN>(g, A.la1, i, j, k, c.lb);
-      fx_add<R, AIN>(g, A.la1, i + 1, j, k, c.lb);
-      fx_add<R, AIN>(g, A.la1, i + 1, j, k - 1, c.lb);
+      fx_add<R, AIN, IN>(g, A.la1, i, j, k - 1, c.lb);
+      fx_add<R, AIN, IN>(g, A.la1, i, j, k, c.lb);
+      fx_add<R, AIN, IN>(g, A.la1, i + 1, j, k, c.lb);
+      fx_add<R, AIN, IN>(g, A.la1, i + 1, j, k - 1, c.lb);
     }
     {
-      const R b = fy<R, AIN>(g, U2, i, j, k - 1) + fy<R, AIN>(g, U2, i, j + 1, k - 1) +
-                  fy<R, AIN>(g, U2, i, j + 1, k) + fy<R, AIN>(g, U2, i, j, k);
-      const VcTerm<R> c = vcorra_adj<R>(g, X, A.lxant, lv, a, b, hm, i, j + 1, k - 1, i, j + 1, k, i, j - 1, k - 1,
+      const R b = fy<R, AIN, IN>(g, U2, i, j, k - 1) + fy<R, AIN, IN>(g, U2, i, j + 1, k - 1) +
+                  fy<R, AIN, IN>(g, U2, i, j + 1, k) + fy<R, AIN, IN>(g, U2, i, j, k);
+      const VcTerm<R> c = vcorra_adj<R, IN>(g, X, A.lxant, lv, a, b, hm, i, j + 1, k - 1, i, j + 1, k, i, j - 1, k - 1,
                                         i, j - 1, k);
       la += c.la;
-      fy_add<R, AIN>(g, A.la2, i, j, k - 1, c.lb);
-      fy_add<R, AIN>(g, A.la2, i, j + 1, k - 1, c.lb);
-      fy_add<R, AIN>(g, A.la2, i, j + 1, k, c.lb);
-      fy_add<R, AIN>(g, A.la2, i, j, k, c.lb);
+      fy_add<R, AIN, IN>(g, A.la2, i, j, k - 1, c.lb);
+      fy_add<R, AIN, IN>(g, A.la2, i, j + 1, k - 1, c.lb);
+      fy_add<R, AIN, IN>(g, A.la2, i, j + 1, k, c.lb);
+      fy_add<R, AIN, IN>(g, A.la2, i, j, k, c.lb);
     }
-    fz_add<R, AIN>(g, A.la3, i, j, k, la);
+    fz_add<R, AIN, IN>(g, A.la3, i, j, k, la);
   }
 #undef FACE_HEAD
 #undef XX
 #undef LX
+}
+template <class R, bool AIN>
+__global__ void __launch_bounds__(128) ka_pseudo_std(const Prob<R> P, const AdjArr<R> A) {
+#define C(IN) ka_pseudo_std_cell<R, AIN, IN>(P, A, i, j, k)
+  ADISPATCH(C)
+#undef C
 }
 
 // ---- upwind: xant = rhr*(x - D*hinv), D = signed sum of donor fluxes --------
@@ -546,9 +608,9 @@ __device__ __forceinline__ void flux_adj(R lF, R xl, R xr_, R u, bool l_var, con
   *lu_out = lF * (dpp(u) * xl - dpn(u) * xr_);
 }
 
-template <class R>
-__global__ void __launch_bounds__(128) ka_upwind(const Prob<R> P, const AdjArr<R> A) {
-  ACELL
+template <class R, bool IN>
+__device__ __forceinline__ void ka_upwind_cell(const Prob<R>& P, const AdjArr<R>& A, int i, int j, int k) {
+  const Geo& g = P.g;
   const Arr<R>& psi = P.psi;
   const R lxa = A.lxant.ld(i, j, k);
   const R rh = P.rhr.ld(i, j, k);
@@ -557,35 +619,41 @@ __global__ void __launch_bounds__(128) ka_upwind(const Prob<R> P, const AdjArr<R
   const R x = psi.ld(i, j, k);
   const long bx0 = (long)(j - 1) + (long)g.mp * (k - 1), bxs = (long)g.mp * g.lp;
   const long by0 = (long)(i - 1) + (long)g.np * (k - 1), bys = (long)g.np * g.lp;
-  const bool im_var = i > 1 || g.bx, ip_var = i < g.np || g.bx, jm_var = j > 1 || g.by, jp_var = j < g.mp || g.by;
-  const int im = wrapi(i - 1, g.np), ip = wrapi(i + 1, g.np), jm = wrapi(j - 1, g.mp), jp = wrapi(j + 1, g.mp);
+  const bool im_var = IN || i > 1 || g.bx, ip_var = IN || i < g.np || g.bx, jm_var = IN || j > 1 || g.by, jp_var = IN || j < g.mp || g.by;
+  const int im = IN ? i - 1 : wrapi(i - 1, g.np), ip = IN ? i + 1 : wrapi(i + 1, g.np), jm = IN ? j - 1 : wrapi(j - 1, g.mp), jp = IN ? j + 1 : wrapi(j + 1, g.mp);
   const R xim = im_var ? psi.ld(im, j, k) : P.bcx[bx0];
   const R xip = ip_var ? psi.ld(ip, j, k) : P.bcx[bx0 + bxs];
   const R xjm = jm_var ? psi.ld(i, jm, k) : P.bcy[by0];
   const R xjp = jp_var ? psi.ld(i, jp, k) : P.bcy[by0 + bys];
   R lu;
   // x faces: D = F1(i+1) - F1(i) + ...
-  flux_adj(lD, x, xip, fx<R, true>(g, P.u1, i + 1, j, k), true, A.lx, i, j, k, ip_var, ip, j, k, &lu);
-  fx_add<R, true>(g, A.gu1, i + 1, j, k, lu);
+  flux_adj(lD, x, xip, fx<R, true, IN>(g, P.u1, i + 1, j, k), true, A.lx, i, j, k, ip_var, ip, j, k, &lu);
+  fx_add<R, true, IN>(g, A.gu1, i + 1, j, k, lu);
   flux_adj(-lD, xim, x, P.u1.ld(i, j, k), im_var, A.lx, im, j, k, true, i, j, k, &lu);
-  fx_add<R, true>(g, A.gu1, i, j, k, lu);
-  flux_adj(lD, x, xjp, fy<R, true>(g, P.u2, i, j + 1, k), true, A.lx, i, j, k, jp_var, i, jp, k, &lu);
-  fy_add<R, true>(g, A.gu2, i, j + 1, k, lu);
+  fx_add<R, true, IN>(g, A.gu1, i, j, k, lu);
+  flux_adj(lD, x, xjp, fy<R, true, IN>(g, P.u2, i, j + 1, k), true, A.lx, i, j, k, jp_var, i, jp, k, &lu);
+  fy_add<R, true, IN>(g, A.gu2, i, j + 1, k, lu);
   flux_adj(-lD, xjm, x, P.u2.ld(i, j, k), jm_var, A.lx, i, jm, k, true, i, j, k, &lu);
-  fy_add<R, true>(g, A.gu2, i, j, k, lu);
-  if (!g.bz && k == 1) {  // F3(1) = -F3(2): D = ... + 2*F3(2)
+  fy_add<R, true, IN>(g, A.gu2, i, j, k, lu);
+  if (!IN && !g.bz && k == 1) {  // F3(1) = -F3(2): D = ... + 2*F3(2)
     flux_adj(R(2) * lD, x, psi.ld(i, j, k + 1), P.u3.ld(i, j, k + 1), true, A.lx, i, j, k, true, i, j, k + 1, &lu);
     addat(A.gu3, i, j, k + 1, lu);
-  } else if (!g.bz && k == g.lp) {  // F3(lp+1) = -F3(lp): D = ... - 2*F3(lp)
+  } else if (!IN && !g.bz && k == g.lp) {  // F3(lp+1) = -F3(lp): D = ... - 2*F3(lp)
     flux_adj(-R(2) * lD, psi.ld(i, j, k - 1), x, P.u3.ld(i, j, k), true, A.lx, i, j, k - 1, true, i, j, k, &lu);
     addat(A.gu3, i, j, k, lu);
   } else {
-    const int kp = cz(g, k + 1), km = cz(g, k - 1);
-    flux_adj(lD, x, psi.ld(i, j, kp), fz<R, true>(g, P.u3, i, j, k + 1), true, A.lx, i, j, k, true, i, j, kp, &lu);
-    fz_add<R, true>(g, A.gu3, i, j, k + 1, lu);
+    const int kp = cz<IN>(g, k + 1), km = cz<IN>(g, k - 1);
+    flux_adj(lD, x, psi.ld(i, j, kp), fz<R, true, IN>(g, P.u3, i, j, k + 1), true, A.lx, i, j, k, true, i, j, kp, &lu);
+    fz_add<R, true, IN>(g, A.gu3, i, j, k + 1, lu);
     flux_adj(-lD, psi.ld(i, j, km), x, P.u3.ld(i, j, k), true, A.lx, i, j, km, true, i, j, k, &lu);
-    fz_add<R, true>(g, A.gu3, i, j, k, lu);
+    fz_add<R, true, IN>(g, A.gu3, i, j, k, lu);
   }
+}
+template <class R>
+__global__ void __launch_bounds__(128) ka_upwind(const Prob<R> P, const AdjArr<R> A) {
+#define C(IN) ka_upwind_cell<R, IN>(P, A, i, j, k)
+  ADISPATCH(C)
+#undef C
 }
 
 template <class R>
@@ -601,37 +669,51 @@ __global__ void __launch_bounds__(128) ka_seed(const Prob<R> P, const Arr<R> psi
   lam.at(i, j, k) = psi.ld(i, j, k) - target.ld(i, j, k);
 }
 
-// forward record kernels (psi's halo is left untouched: HALO=false)
+// forward record kernels (psi's halo is left untouched: HALO=false); warps
+// away from every wall take the bodies without boundary maps, as the
+// forward stage kernels do
+#define FCELL(BODY)                                          \
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;  \
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;  \
+  const int k = blockIdx.z + 1;                              \
+  const bool win = warp_interior(P.g, i, j, k);              \
+  if (i > P.g.np || j > P.g.mp) return;                      \
+  if (win) {                                                 \
+    BODY(true);                                              \
+  } else {                                                   \
+    BODY(false);                                             \
+  }
 template <class R>
 __global__ void __launch_bounds__(128) kf_upwind(const Prob<R> P) {
-  ACELL
-  (void)g;
-  upwind_body<R, true, false>(P, i, j, k);
+#define B(IN) upwind_body<R, true, false, IN>(P, i, j, k)
+  FCELL(B)
+#undef B
 }
 template <class R, bool AIN>
 __global__ void __launch_bounds__(128) kf_pseudo(const Prob<R> P) {
-  ACELL
-  (void)g;
-  pseudo_body<R, AIN>(P, i, j, k);
+#define B(IN) pseudo_body<R, AIN, IN>(P, i, j, k)
+  FCELL(B)
+#undef B
 }
 template <class R, bool NONOS, bool FIRST, bool KEEP>
 __global__ void __launch_bounds__(128) kf_bounds(const Prob<R> P) {
-  ACELL
-  (void)g;
-  bounds_body<R, NONOS, FIRST, KEEP>(P, i, j, k);
+#define B(IN) bounds_body<R, NONOS, FIRST, KEEP, IN>(P, i, j, k)
+  FCELL(B)
+#undef B
 }
 template <class R, bool NONOS>
 __global__ void __launch_bounds__(128) kf_limit(const Prob<R> P) {
-  ACELL
-  (void)g;
-  limit_body<R, NONOS>(P, i, j, k);
+#define B(IN) limit_body<R, NONOS, IN>(P, i, j, k)
+  FCELL(B)
+#undef B
 }
 template <class R>
 __global__ void __launch_bounds__(128) kf_update(const Prob<R> P) {
-  ACELL
-  (void)g;
-  update_body<R, false>(P, i, j, k);
+#define B(IN) update_body<R, false, IN>(P, i, j, k)
+  FCELL(B)
+#undef B
 }
+#undef FCELL
 
 // The values of pass t: its input field, pseudo-velocities, ratios and
 // extrema from the records; `a` selects the "a" velocities the pass's
