@@ -51,6 +51,7 @@ SIGNATURES = {
     "mpdata_adjoint_run_f32": ([P, I, I] + [P] * 9 + [ctypes.POINTER(D)] + [P] * 4 +
                                [ctypes.POINTER(ctypes.c_longlong), P], I),
     "mpdata_ws_error": ([P, ctypes.POINTER(I)], I),
+    "mpdata_ws_bound_violations": ([P, P, D, ctypes.POINTER(ctypes.c_longlong), P], I),
     "mpdata_launch_count": ([], ctypes.c_longlong),
     "mpdata_ws_profile": ([P, I], I),
     "mpdata_ws_stage_times": ([P, I, ctypes.POINTER(D), ctypes.POINTER(ctypes.c_longlong)], I),

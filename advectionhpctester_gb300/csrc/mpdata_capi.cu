@@ -22,6 +22,9 @@ template <class R>
 int run_reduce(Geo g, int mode, const R* a, const R* h, const R* rhr, const void* b, int b_is_f64,
                double* part, double* out, cudaStream_t s);
 int reduce_blocks();
+template <class R>
+int run_bound_violations(Geo g, const Arr<R>& psi, const Arr<R>& mx, const Arr<R>& mn, double tol,
+                         unsigned long long* count, cudaStream_t s);
 }
 
 namespace {
@@ -294,6 +297,20 @@ namespace mpdata {
 int grid_ok(const mpdata_grid* g) { return check_grid(g); }
 }  // namespace mpdata
 
+namespace {
+// psi (caller layout) against the running extrema the workspace's last step kept
+template <class R>
+int count_violations(Workspace* w, const void* psi, double tol, unsigned long long* d, cudaStream_t s) {
+  R* base = static_cast<R*>(w->mem);
+  R* x = const_cast<R*>(static_cast<const R*>(psi));
+  const Prob<R> P = make_prob<R>(w->g, w->o.gauge, x, x, x, x, x, x, nullptr, nullptr, base, w->ncell,
+                                 base + (size_t)NFIELD * w->ncell, 1);
+  return run_bound_violations<R>(P.g, P.psi, P.mx, P.mn, tol, d, s) ? MPDATA_E_CUDA : MPDATA_OK;
+}
+}  // namespace
+
+
+
 extern "C" {
 
 int mpdata_ws_create(const mpdata_grid* grid, const mpdata_opts* opts, void** ws) {
@@ -430,6 +447,25 @@ int mpdata_ws_error(void* ws, int* error_word) {
 }
 
 long long mpdata_launch_count(void) { return (long long)launch_count(); }
+
+int mpdata_ws_bound_violations(void* ws, const void* psi, double tol, long long* count, void* stream) {
+  Workspace* w = as_ws(ws);
+  if (!w) return MPDATA_E_WS;
+  if (!psi || !count) return MPDATA_E_NULL;
+  if (!w->o.nonos || w->o.iord < 3) return MPDATA_E_UNSUPPORTED;  // the extrema are kept from iord 3 on
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  unsigned long long* d = nullptr;
+  if (cudaMallocAsync(&d, sizeof *d, s) != cudaSuccess) return MPDATA_E_CUDA;
+  int rc = cudaMemsetAsync(d, 0, sizeof *d, s) == cudaSuccess ? MPDATA_OK : MPDATA_E_CUDA;
+  if (!rc) rc = w->elem == sizeof(double) ? count_violations<double>(w, psi, tol, d, s)
+                                          : count_violations<float>(w, psi, tol, d, s);
+  unsigned long long h = 0;
+  if (!rc && cudaMemcpyAsync(&h, d, sizeof h, cudaMemcpyDeviceToHost, s) != cudaSuccess) rc = MPDATA_E_CUDA;
+  cudaFreeAsync(d, s);
+  if (!rc && cudaStreamSynchronize(s) != cudaSuccess) rc = MPDATA_E_CUDA;
+  if (!rc) *count = (long long)h;
+  return rc;
+}
 
 int mpdata_ws_profile(void* ws, int enable) {
   Workspace* w = as_ws(ws);

@@ -130,4 +130,35 @@ template int run_reduce<float>(Geo, int, const float*, const float*, const float
                                double*, double*, cudaStream_t);
 int reduce_blocks() { return RED_BLOCKS; }
 
+// Limiter-bound violations: interior cells whose value lies outside
+// [mn - tol, mx + tol], mn/mx the running extrema the nonoscillatory limiter
+// kept over the step.  psi, mx and mn are views (logical (1,1,1) bases).
+template <class R>
+__global__ void __launch_bounds__(256) k_bound_violations(Geo g, Arr<R> psi, Arr<R> mx, Arr<R> mn, double tol,
+                                                           unsigned long long* count) {
+  unsigned long long c = 0;
+  const long n = (long)g.np * g.mp * g.lp;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.np) + 1;
+    const long r = t / g.np;
+    const int j = (int)(r % g.mp) + 1, k = (int)(r / g.mp) + 1;
+    const double v = (double)psi.ld(i, j, k);
+    if (v > (double)mx.ld(i, j, k) + tol || v < (double)mn.ld(i, j, k) - tol) c++;
+  }
+  for (int d = 16; d > 0; d >>= 1) c += __shfl_xor_sync(0xffffffffu, c, d);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, c);
+}
+
+template <class R>
+int run_bound_violations(Geo g, const Arr<R>& psi, const Arr<R>& mx, const Arr<R>& mn, double tol,
+                         unsigned long long* count, cudaStream_t s) {
+  k_bound_violations<R><<<RED_BLOCKS, 256, 0, s>>>(g, psi, mx, mn, tol, count);
+  add_launches(1);
+  return cudaGetLastError() == cudaSuccess ? 0 : -5;
+}
+template int run_bound_violations<double>(Geo, const Arr<double>&, const Arr<double>&, const Arr<double>&,
+                                          double, unsigned long long*, cudaStream_t);
+template int run_bound_violations<float>(Geo, const Arr<float>&, const Arr<float>&, const Arr<float>&, double,
+                                         unsigned long long*, cudaStream_t);
+
 }  // namespace mpdata

@@ -204,6 +204,16 @@ class Workspace:
             check(rc, "mpdata_ws_stage_times")
         return {self.lib.mpdata_stage_name(i).decode(): (ms[i], cnt[i]) for i in range(rc)}
 
+    def bound_violations(self, psi, tol=0.0, stream=None):
+        """Cells of psi outside the limiter's running extrema of the last step
+        (nonos, iord >= 3)."""
+        import ctypes
+        out = ctypes.c_longlong(0)
+        check(self.lib.mpdata_ws_bound_violations(self.handle, _ptr(psi, self.dtype, self.shapes["psi"], "psi"),
+                                                  float(tol), ctypes.byref(out), _stream(stream)),
+              "mpdata_ws_bound_violations")
+        return out.value
+
     def error_word(self):
         out = _native.I(0)
         check(self.lib.mpdata_ws_error(self.handle, out), "mpdata_ws_error")

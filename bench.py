@@ -336,6 +336,10 @@ def run_ours(args, ws, rank, local):
                   step_hbm_frac=round(step_alg / (ms_max / args.steps * 1e-3) / 1e9 / peak, 4))
     mass1 = M.mass(arm.psi, arm.h)
     result["mass_rel_drift"] = (mass1 - mass0) / mass0
+    # the last step's output against the running extrema its limiter kept (h = rhr = 1 here)
+    tol = 1e-12 * float(arm.psi.abs().max())
+    result["limiter_bound_violations"] = {"count": arm.ws.bound_violations(arm.psi, tol), "cells": cells,
+                                          "tol": tol, "step": "the last timed step"}
     if rank == 0 and ws == 1 and not args.no_extras and args.precision == 64:
         result["fp32"] = run_fp32_study(args, host, arm, ms_max / args.steps, mass0)
     if not args.no_e2e:

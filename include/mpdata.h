@@ -183,6 +183,15 @@ int mpdata_adjoint_run_f32(void* ws, int nsteps, int interval, float* psi, const
 /* Device error word of a workspace (bit 0: a non-finite value was produced
  * by the last checked step).  Synchronises the workspace's last stream. */
 int mpdata_ws_error(void* ws, int* error_word);
+/* Limiter-bound check of the metric "limiter bounds never violated": the
+ * number of interior cells of psi (caller layout, the workspace's precision)
+ * outside [mn - tol, mx + tol], where mn/mx are the running extrema the
+ * nonoscillatory limiter kept during the workspace's last step (x_in and every
+ * pass's stars).  The workspace must have nonos = 1 and iord >= 3 (iord 2
+ * keeps no extrema: MPDATA_E_UNSUPPORTED).  With h = rhr = 1 the step's
+ * output lies inside the bounds; otherwise the bounds apply to x before the
+ * rhr scaling.  Synchronises the stream. */
+int mpdata_ws_bound_violations(void* ws, const void* psi, double tol, long long* count, void* stream);
 
 /* Number of kernels this library launched since process start (all
  * workspaces), for launch accounting. */

@@ -102,6 +102,32 @@ def test_edge_sizes_reference_bc(M, oracle, n):
     np.testing.assert_array_equal(out, g.x)
 
 
+@pytest.mark.parametrize("gauge", [1, 0])
+@pytest.mark.parametrize("ibc", [(1, 1, 1), (0, 0, 0)])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_limiter_bounds_never_violated(M, gauge, ibc, dtype):
+    """With h = rhr = 1, every step's output lies inside the running extrema
+    the nonoscillatory limiter kept (x_in and every pass's stars), counted on
+    the device after each of 5 steps; one cell pushed out of its bounds is
+    counted."""
+    import torch
+    f = W.random_fields(40, 24, 12, ibc=ibc, seed=23, courant=0.4, sign_change=not gauge)
+    f.h[...] = 1.0
+    f.rhr[...] = 1.0
+    f = f.astype(dtype) if dtype != np.float64 else f
+    d, _ = dev(M, f)
+    ws = M.Workspace(f.np, f.mp, f.lp, f.ih, *ibc, iord=3, nonos=1, gauge=gauge,
+                     precision=64 if dtype == np.float64 else 32)
+    tol = (1e-12 if dtype == np.float64 else 1e-5) * float(np.abs(f.x).max())
+    for _ in range(5):
+        ws.step(d["x"], d["u1"], d["u2"], d["u3"], d["h"], d["rhr"], d["bcx"], d["bcy"])
+        assert ws.bound_violations(d["x"], tol) == 0
+    bad = d["x"].clone()
+    bad[5, 6, 7] += 10.0
+    assert ws.bound_violations(bad, tol) == 1
+    ws.close()
+
+
 def test_solid_body_100_steps_fp64(M, oracle):
     """64x64x32 periodic solid-body rotation, standard MPDATA, 100 steps:
     L-inf relative error <= 1e-12 (bit-exact expected), mass conserved."""
