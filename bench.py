@@ -362,7 +362,7 @@ def run_ours(args, ws, rank, local):
 
 
 def run_fp32_study(args, host, arm64, ms64, mass0):
-    """Same workload and steps in FP32 (BASELINE's precision study): speedup
+    """Same workload and steps in FP32 (the precision study): speedup
     over the FP64 run, error against it, and FP64-compensated mass drift."""
     import torch
     M = arm64.M
@@ -708,7 +708,7 @@ def make_domain_device(n, rng, torch_dtype):
 
 
 def run_batch_study(args, steps=100):
-    """BASELINE config 3: 64 periodic domains of uneven sizes (seed 3) in one
+    """Batching: 64 periodic domains of uneven sizes (seed 3) in one
     batch (one CUDA-graph launch per step, tuned tile shape) against a loop of
     per-domain steps; FP64 and FP32.  Plus 16 tracers sharing one velocity on
     256x256x64 against 16 separate steps."""
