@@ -113,7 +113,7 @@ __device__ __forceinline__ void upwind_body(const Prob<R>& P, int i, int j, int 
   const R xjm = (IN || j > 1) ? psi.ld(i, j - 1, k) : (g.by ? psi.ld(i, g.mp, k) : P.bcy[by0]);
   const R xjp = (IN || j < g.mp) ? psi.ld(i, j + 1, k) : (g.by ? psi.ld(i, 1, k) : P.bcy[by0 + bys]);
   const R hc = P.h.ld(i, j, k);
-  const R hi = R(1) / hc;
+  const R hi = rcp1(hc);
   const R f1p = donor(x, xip, fx<R, true, IN>(g, P.u1, i + 1, j, k));
   const R f1 = donor(xim, x, P.u1.ld(i, j, k));
   const R f2p = donor(x, xjp, fy<R, true, IN>(g, P.u2, i, j + 1, k));
@@ -132,7 +132,7 @@ __device__ __forceinline__ void upwind_body(const Prob<R>& P, int i, int j, int 
   if (P.rho) {
     // mpdata3d-rho-gauge-gpubc.f90:137-210: no rhr, division by h, fluxes kept;
     // rhoadv takes the input x_incomp (:121-123)
-    P.xant.at(i, j, k) = x - (f1p - f1 + f2p - f2 + f3p - f3) / hc;
+    P.xant.at(i, j, k) = x - div1(f1p - f1 + f2p - f2 + f3p - f3, hc);
     P.f1.at(i, j, k) = f1;
     P.f2.at(i, j, k) = f2;
     P.f3.at(i, j, k) = f3;
@@ -141,7 +141,7 @@ __device__ __forceinline__ void upwind_body(const Prob<R>& P, int i, int j, int 
     if (k == g.lp) P.f3hi[(i - 1) + (long)g.np * (j - 1)] = f3p;
     P.rhoadv.at(i, j, k) = P.x_incomp.ld(i, j, k);
   } else {
-    P.xant.at(i, j, k) = P.rhr.ld(i, j, k) * (x - (f1p - f1 + f2p - f2 + f3p - f3) * hi);
+    P.xant.at(i, j, k) = mul1(x - mul1(f1p - f1 + f2p - f2 + f3p - f3, hi), P.rhr.ld(i, j, k));
   }
   if (ANTIDIFF && P.own_vel) {
     P.hinv.at(i, j, k) = hi;
@@ -210,7 +210,7 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
       if (zt)
         cr = c2 + (AZ(i - 1, j, k) + AZ(i - 1, j, k + 1) + AZ(i, j, k + 1) + AZ(i, j, k)) *
                       rat4(XX(i - 1, j, k - 1), XX(i, j, k - 1), XX(i - 1, j, k + 1), XX(i, j, k + 1));
-      v = vdyf(XX(i - 1, j, k), XX(i, j, k), a, hmx) - R(0.125) * a * hmx * cr;
+      v = vdyf(XX(i - 1, j, k), XX(i, j, k), a, hmx) - mul1(R(0.125) * a, hmx) * cr;
     }
     P.v1.at(i, j, k) = v;
   }
@@ -241,7 +241,7 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
       if (zt)
         cr = c1 + (AZ(i, j - 1, k) + AZ(i, j, k) + AZ(i, j, k + 1) + AZ(i, j - 1, k + 1)) *
                       rat4(XX(i, j - 1, k - 1), XX(i, j, k - 1), XX(i, j - 1, k + 1), XX(i, j, k + 1));
-      v = vdyf(XX(i, j - 1, k), XX(i, j, k), a, hmy) - R(0.125) * a * hmy * cr;
+      v = vdyf(XX(i, j - 1, k), XX(i, j, k), a, hmy) - mul1(R(0.125) * a, hmy) * cr;
     }
     P.v2.at(i, j, k) = v;
   }
@@ -269,7 +269,7 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
                        rat4(XX(i - 1, j, k - 1), XX(i - 1, j, k), XX(i + 1, j, k - 1), XX(i + 1, j, k)) +
                    (AY(i, j, k - 1) + AY(i, j + 1, k - 1) + AY(i, j + 1, k) + AY(i, j, k)) *
                        rat4(XX(i, j - 1, k - 1), XX(i, j - 1, k), XX(i, j + 1, k - 1), XX(i, j + 1, k));
-      v = vdyf(XX(i, j, k - 1), XX(i, j, k), a, hmz) - R(0.125) * a * hmz * cr;
+      v = vdyf(XX(i, j, k - 1), XX(i, j, k), a, hmz) - mul1(R(0.125) * a, hmz) * cr;
     }
     P.v3.at(i, j, k) = v;
   }
@@ -299,7 +299,7 @@ __device__ __forceinline__ void bounds_body(const Prob<R>& P, int i, int j, int 
   const Geo& g = P.g;
   const Arr<R>& X = P.xant;
   const R x = X.ld(i, j, k);
-  P.q.at(i, j, k) = P.rho ? x : x / P.rhr.ld(i, j, k);  // x/1 == x for the density step
+  P.q.at(i, j, k) = P.rho ? x : div1(x, P.rhr.ld(i, j, k));  // x/1 == x for the density step
   if (!NONOS) return;
   const bool lo = IN || g.bz || k > 1, hi = IN || g.bz || k < g.lp;
   R ma, mi;
@@ -347,8 +347,8 @@ __device__ __forceinline__ void bounds_body(const Prob<R>& P, int i, int j, int 
   const R e2 = fy<R, false, IN>(g, F2, i, j + 1, k), w2 = fy<R, false, IN>(g, F2, i, j, k);
   const R e3 = fz<R, false, IN>(g, F3, i, j, k + 1), w3 = fz<R, false, IN>(g, F3, i, j, k);
   const R hc = P.h.ld(i, j, k);
-  P.cp.at(i, j, k) = (ma - x) * hc / (pn(e1) + pp(w1) + pn(e2) + pp(w2) + pn(e3) + pp(w3) + ep);
-  P.cn.at(i, j, k) = (x - mi) * hc / (pp(e1) + pn(w1) + pp(e2) + pn(w2) + pp(e3) + pn(w3) + ep);
+  P.cp.at(i, j, k) = mul1(ma - x, hc) / (pn(e1) + pp(w1) + pn(e2) + pp(w2) + pn(e3) + pp(w3) + ep);
+  P.cn.at(i, j, k) = mul1(x - mi, hc) / (pp(e1) + pn(w1) + pp(e2) + pn(w2) + pp(e3) + pn(w3) + ep);
 }
 
 // ---- limited antidiffusive velocities and fluxes --------------------------
@@ -423,13 +423,13 @@ __device__ __forceinline__ void update_body(const Prob<R>& P, int i, int j, int 
     const R d = fx<R, false, IN>(g, P.f1, i + 1, j, k) - fx<R, false, IN>(g, P.f1, i, j, k) +
                 fy<R, false, IN>(g, P.f2, i, j + 1, k) - fy<R, false, IN>(g, P.f2, i, j, k) +
                 fz<R, false, IN>(g, P.f3, i, j, k + 1) - fz<R, false, IN>(g, P.f3, i, j, k);
-    out.at(i, j, k) = P.rhr.ld(i, j, k) * (P.q.ld(i, j, k) - d * P.hinv.ld(i, j, k));
+    out.at(i, j, k) = mul1(P.q.ld(i, j, k) - mul1(d, P.hinv.ld(i, j, k)), P.rhr.ld(i, j, k));
   } else {
     const R d = fx<R, false, IN>(g, P.w1, i + 1, j, k) - fx<R, false, IN>(g, P.w1, i, j, k) +
                 fy<R, false, IN>(g, P.w2, i, j + 1, k) - fy<R, false, IN>(g, P.w2, i, j, k) +
                 fz<R, false, IN>(g, P.w3, i, j, k + 1) - fz<R, false, IN>(g, P.w3, i, j, k);
-    const R t = P.q.ld(i, j, k) - d / P.h.ld(i, j, k);
-    out.at(i, j, k) = P.rho ? t : P.rhr.ld(i, j, k) * t;  // rhr == 1 in the density step
+    const R t = P.q.ld(i, j, k) - div1(d, P.h.ld(i, j, k));
+    out.at(i, j, k) = P.rho ? t : mul1(t, P.rhr.ld(i, j, k));  // rhr == 1 in the density step
   }
 }
 

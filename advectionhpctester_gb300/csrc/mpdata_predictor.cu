@@ -24,7 +24,7 @@ __global__ void __launch_bounds__(128) k_pred_level(Geo g, long lev, R* ox, R* o
 #pragma unroll
   for (int c = 0; c < 3; c++) {
     R* p0 = o[c] + off;
-    const R a0 = p0[0] * hc;
+    const R a0 = mul1(p0[0], hc);
     const R a2 = p0[2 * lev];
     const R a1 = a0 + r * (a0 - a2);
     p0[lev] = R(0.5) * (a1 + a0) * gc[c];
@@ -52,7 +52,7 @@ __device__ __forceinline__ void roll_cell(long lev, R* ox, R* oy, R* oz, R* pu, 
       q[2 * lev] = p0;
     }
     R* q = o[c] + off;
-    q[2 * lev] = q[0] * hc;
+    q[2 * lev] = mul1(q[0], hc);
   }
 }
 

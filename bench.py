@@ -342,6 +342,8 @@ def run_ours(args, ws, rank, local):
                                           "tol": tol, "step": "the last timed step"}
     if rank == 0 and ws == 1 and not args.no_extras and args.precision == 64:
         result["fp32"] = run_fp32_study(args, host, arm, ms_max / args.steps, mass0)
+    if rank == 0 and ws == 1 and not args.no_extras:
+        result["variable_density"] = run_density_study(args, host, ms_max / args.steps)
     if not args.no_e2e:
         barrier(ws)
         e2e = run_e2e(arm, args)
@@ -389,6 +391,43 @@ def run_fp32_study(args, host, arm64, ms64, mass0):
            "note": "FP32 stencil arithmetic, FP64 Neumaier-compensated mass and norms"}
     arm.ws.close()
     return out
+
+
+def run_density_study(args, host, ms_unit, amp=0.1, phase=1.0):
+    """The headline step with a variable fluid density.  The reference's test
+    application uses unit density (advection_test_setup.f90:630-631); its
+    perturbed set-up (advection_test_setup.f90:745-759) uses
+    h = 1 + amp*sin(2pi i/n + phase 2pi/3)*cos(2pi j/m + 2 phase 2pi/3)*cos(2pi k/l + 3 phase 2pi/3),
+    used here with rhr = 1/h.  The kernels skip multiplications and divisions by an
+    exact 1.0, so this line shows the general-density throughput beside the headline."""
+    import torch
+    nx, ny, nz = args.grid
+    arm = GpuArm(nx, ny, nz, args.precision, host=host)
+    dt = arm.tdtype
+    ax = lambda n, s: torch.arange(1, n + 1, device="cuda", dtype=torch.float64) * (2 * math.pi / n) + s
+    tp = 2 * math.pi / 3
+    noise = (torch.sin(ax(nx, phase * tp))[:, None, None] * torch.cos(ax(ny, 2 * phase * tp))[None, :, None]
+             * torch.cos(ax(nz, 3 * phase * tp))[None, None, :]) * amp
+    inner = lambda t: t.permute(2, 1, 0)[1:nz + 1, 1:ny + 1, 1:nx + 1].permute(2, 1, 0)
+    inner(arm.h).copy_((1.0 + noise).to(dt))
+    inner(arm.rhr).copy_((1.0 / (1.0 + noise)).to(dt))
+    for c in range(3):
+        arm.o[c][..., 2].mul_(arm.h)
+    for n in range(args.warmup):
+        arm.step(n)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for n in range(args.warmup, args.warmup + args.steps):
+        arm.step(n)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    arm.ws.close()
+    cells = nx * ny * nz
+    return {"value": round(cells / (ms * 1e-3) / 1e9, 4), "unit": UNIT, "ms_per_step": round(ms, 4),
+            "vs_unit_density": round(ms_unit / ms, 3),
+            "density": "h = 1 + %.2f sin cos cos (reference perturbed set-up), rhr = 1/h" % amp}
 
 
 class DevArm:
