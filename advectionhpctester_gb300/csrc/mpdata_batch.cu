@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(256) kb_pseudo(BATCH_ARGS) {
 }
 template <class R, bool NONOS, bool FIRST, bool KEEP>
 __global__ void __launch_bounds__(256) kb_bounds(BATCH_ARGS) {
-#define B(IN) bounds_body<R, NONOS, FIRST, KEEP, IN>(P, i, j, k)
+#define B(IN) bounds_body<R, NONOS, FIRST, KEEP, IN, true>(P, i, j, k)
   BATCH_TILE(B)
 #undef B
 }

@@ -96,6 +96,18 @@ __device__ __forceinline__ bool warp_interior(const Geo& g, int i, int j, int k)
   return __all_sync(0xffffffffu, in);
 }
 
+// True when hmx, hmy and hmz are exactly 1 at every cell of the warp (FP64
+// only; FP32 kernels are bound by instruction issue and keep the products).
+template <class R>
+__device__ __forceinline__ bool warp_unit_faces(const Prob<R>& P, int i, int j, int k) {
+  if constexpr (sizeof(R) == 8) {
+    const bool u = is_one(P.hmx.ld(i, j, k)) && is_one(P.hmy.ld(i, j, k)) && is_one(P.hmz.ld(i, j, k));
+    return __all_sync(0xffffffffu, u);
+  } else {
+    return false;
+  }
+}
+
 // ---- upwind3d_gpubc (upwind3d-gpubc.f90:101-198) -------------------------
 // ANTIDIFF: an antidiffusive pass follows, so psi's open-wall halo ends the
 // step holding the zero-gradient copy of the old boundary values (written by
@@ -169,8 +181,9 @@ __device__ __forceinline__ void upwind_body(const Prob<R>& P, int i, int j, int 
 // drop the z cross terms of v1/v2, as the reference's boundary kernels do.
 // Each cell computes its lower faces.  AIN: the first corrective pass, whose
 // "a" velocities are the caller's Courant numbers; later passes use the
-// previous pass's limited velocities w1..w3.
-template <class R, bool STD, bool AIN, bool IN = false>
+// previous pass's limited velocities w1..w3.  U: the three face reciprocal
+// densities of every cell of the warp are exactly 1 (warp_unit_faces).
+template <class R, bool STD, bool AIN, bool IN = false, bool U = false>
 __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int k) {
   const Geo& g = P.g;
   const Arr<R>& X = P.xant;
@@ -188,15 +201,15 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
     const R a = AX(i, j, k);
     R v;
     if (STD) {
-      v = vdyfa(XX(i - 1, j, k), XX(i, j, k), a, hmx, ep) +
-          vcorra(a, AY(i - 1, j, k) + AY(i - 1, j + 1, k) + AY(i, j + 1, k) + AY(i, j, k),
+      v = vdyfa_u<U>(XX(i - 1, j, k), XX(i, j, k), a, hmx, ep) +
+          vcorra_u<U>(a, AY(i - 1, j, k) + AY(i - 1, j + 1, k) + AY(i, j + 1, k) + AY(i, j, k),
                  (fabs(XX(i - 1, j + 1, k)) + fabs(XX(i, j + 1, k))) -
                      (fabs(XX(i - 1, j - 1, k)) + fabs(XX(i, j - 1, k))),
                  fabs(XX(i - 1, j + 1, k)) + fabs(XX(i, j + 1, k)) + fabs(XX(i - 1, j - 1, k)) +
                      fabs(XX(i, j - 1, k)) + ep,
                  hmx);
       if (zt)
-        v = v + vcorra(a, AZ(i - 1, j, k) + AZ(i - 1, j, k + 1) + AZ(i, j, k + 1) + AZ(i, j, k),
+        v = v + vcorra_u<U>(a, AZ(i - 1, j, k) + AZ(i - 1, j, k + 1) + AZ(i, j, k + 1) + AZ(i, j, k),
                        (fabs(XX(i - 1, j, k + 1)) + fabs(XX(i, j, k + 1))) -
                            (fabs(XX(i - 1, j, k - 1)) + fabs(XX(i, j, k - 1))),
                        fabs(XX(i - 1, j, k + 1)) + fabs(XX(i, j, k + 1)) + fabs(XX(i - 1, j, k - 1)) +
@@ -205,12 +218,12 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
       P.f1.at(i, j, k) = donor(XX(i - 1, j, k), XX(i, j, k), v);
     } else {
       const R c2 = (AY(i - 1, j, k) + AY(i - 1, j + 1, k) + AY(i, j + 1, k) + AY(i, j, k)) *
-                   rat4(XX(i - 1, j - 1, k), XX(i, j - 1, k), XX(i - 1, j + 1, k), XX(i, j + 1, k));
+                   dif4(XX(i - 1, j - 1, k), XX(i, j - 1, k), XX(i - 1, j + 1, k), XX(i, j + 1, k));
       R cr = c2;
       if (zt)
         cr = c2 + (AZ(i - 1, j, k) + AZ(i - 1, j, k + 1) + AZ(i, j, k + 1) + AZ(i, j, k)) *
-                      rat4(XX(i - 1, j, k - 1), XX(i, j, k - 1), XX(i - 1, j, k + 1), XX(i, j, k + 1));
-      v = vdyf(XX(i - 1, j, k), XX(i, j, k), a, hmx) - mul1(R(0.125) * a, hmx) * cr;
+                      dif4(XX(i - 1, j, k - 1), XX(i, j, k - 1), XX(i - 1, j, k + 1), XX(i, j, k + 1));
+      v = vdyf_u<U>(XX(i - 1, j, k), XX(i, j, k), a, hmx) - hmul<U>(R(0.03125) * a, hmx) * cr;
     }
     P.v1.at(i, j, k) = v;
   }
@@ -219,15 +232,15 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
     const R a = AY(i, j, k);
     R v;
     if (STD) {
-      v = vdyfa(XX(i, j - 1, k), XX(i, j, k), a, hmy, ep) +
-          vcorra(a, AX(i, j - 1, k) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j - 1, k),
+      v = vdyfa_u<U>(XX(i, j - 1, k), XX(i, j, k), a, hmy, ep) +
+          vcorra_u<U>(a, AX(i, j - 1, k) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j - 1, k),
                  (fabs(XX(i + 1, j - 1, k)) + fabs(XX(i + 1, j, k))) -
                      (fabs(XX(i - 1, j - 1, k)) + fabs(XX(i - 1, j, k))),
                  fabs(XX(i + 1, j - 1, k)) + fabs(XX(i + 1, j, k)) + fabs(XX(i - 1, j - 1, k)) +
                      fabs(XX(i - 1, j, k)) + ep,
                  hmy);
       if (zt)
-        v = v + vcorra(a, AZ(i, j - 1, k) + AZ(i, j, k) + AZ(i, j, k + 1) + AZ(i, j - 1, k + 1),
+        v = v + vcorra_u<U>(a, AZ(i, j - 1, k) + AZ(i, j, k) + AZ(i, j, k + 1) + AZ(i, j - 1, k + 1),
                        (fabs(XX(i, j - 1, k + 1)) + fabs(XX(i, j, k + 1))) -
                            (fabs(XX(i, j - 1, k - 1)) + fabs(XX(i, j, k - 1))),
                        fabs(XX(i, j - 1, k + 1)) + fabs(XX(i, j, k + 1)) + fabs(XX(i, j - 1, k - 1)) +
@@ -236,12 +249,12 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
       P.f2.at(i, j, k) = donor(XX(i, j - 1, k), XX(i, j, k), v);
     } else {
       const R c1 = (AX(i, j - 1, k) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j - 1, k)) *
-                   rat4(XX(i - 1, j - 1, k), XX(i - 1, j, k), XX(i + 1, j - 1, k), XX(i + 1, j, k));
+                   dif4(XX(i - 1, j - 1, k), XX(i - 1, j, k), XX(i + 1, j - 1, k), XX(i + 1, j, k));
       R cr = c1;
       if (zt)
         cr = c1 + (AZ(i, j - 1, k) + AZ(i, j, k) + AZ(i, j, k + 1) + AZ(i, j - 1, k + 1)) *
-                      rat4(XX(i, j - 1, k - 1), XX(i, j, k - 1), XX(i, j - 1, k + 1), XX(i, j, k + 1));
-      v = vdyf(XX(i, j - 1, k), XX(i, j, k), a, hmy) - mul1(R(0.125) * a, hmy) * cr;
+                      dif4(XX(i, j - 1, k - 1), XX(i, j, k - 1), XX(i, j - 1, k + 1), XX(i, j, k + 1));
+      v = vdyf_u<U>(XX(i, j - 1, k), XX(i, j, k), a, hmy) - hmul<U>(R(0.03125) * a, hmy) * cr;
     }
     P.v2.at(i, j, k) = v;
   }
@@ -250,14 +263,14 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
     const R a = AZ(i, j, k);
     R v;
     if (STD) {
-      v = vdyfa(XX(i, j, k - 1), XX(i, j, k), a, hmz, ep) +
-          vcorra(a, AX(i, j, k - 1) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j, k - 1),
+      v = vdyfa_u<U>(XX(i, j, k - 1), XX(i, j, k), a, hmz, ep) +
+          vcorra_u<U>(a, AX(i, j, k - 1) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j, k - 1),
                  (fabs(XX(i + 1, j, k - 1)) + fabs(XX(i + 1, j, k))) -
                      (fabs(XX(i - 1, j, k - 1)) + fabs(XX(i - 1, j, k))),
                  fabs(XX(i + 1, j, k - 1)) + fabs(XX(i + 1, j, k)) + fabs(XX(i - 1, j, k - 1)) +
                      fabs(XX(i - 1, j, k)) + ep,
                  hmz) +
-          vcorra(a, AY(i, j, k - 1) + AY(i, j + 1, k - 1) + AY(i, j + 1, k) + AY(i, j, k),
+          vcorra_u<U>(a, AY(i, j, k - 1) + AY(i, j + 1, k - 1) + AY(i, j + 1, k) + AY(i, j, k),
                  (fabs(XX(i, j + 1, k - 1)) + fabs(XX(i, j + 1, k))) -
                      (fabs(XX(i, j - 1, k - 1)) + fabs(XX(i, j - 1, k))),
                  fabs(XX(i, j + 1, k - 1)) + fabs(XX(i, j + 1, k)) + fabs(XX(i, j - 1, k - 1)) +
@@ -266,10 +279,10 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
       P.f3.at(i, j, k) = donor(XX(i, j, k - 1), XX(i, j, k), v);
     } else {
       const R cr = (AX(i, j, k - 1) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j, k - 1)) *
-                       rat4(XX(i - 1, j, k - 1), XX(i - 1, j, k), XX(i + 1, j, k - 1), XX(i + 1, j, k)) +
+                       dif4(XX(i - 1, j, k - 1), XX(i - 1, j, k), XX(i + 1, j, k - 1), XX(i + 1, j, k)) +
                    (AY(i, j, k - 1) + AY(i, j + 1, k - 1) + AY(i, j + 1, k) + AY(i, j, k)) *
-                       rat4(XX(i, j - 1, k - 1), XX(i, j - 1, k), XX(i, j + 1, k - 1), XX(i, j + 1, k));
-      v = vdyf(XX(i, j, k - 1), XX(i, j, k), a, hmz) - mul1(R(0.125) * a, hmz) * cr;
+                       dif4(XX(i, j - 1, k - 1), XX(i, j - 1, k), XX(i, j + 1, k - 1), XX(i, j + 1, k));
+      v = vdyf_u<U>(XX(i, j, k - 1), XX(i, j, k), a, hmz) - hmul<U>(R(0.03125) * a, hmz) * cr;
     }
     P.v3.at(i, j, k) = v;
   }
@@ -279,12 +292,12 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
 #undef AZ
 }
 
-template <class R, bool AIN, bool IN = false>
+template <class R, bool AIN, bool IN = false, bool U = false>
 __device__ __forceinline__ void pseudo_body(const Prob<R>& P, int i, int j, int k) {
   if (P.stdf)
-    pseudo_form<R, true, AIN, IN>(P, i, j, k);
+    pseudo_form<R, true, AIN, IN, U>(P, i, j, k);
   else
-    pseudo_form<R, false, AIN, IN>(P, i, j, k);
+    pseudo_form<R, false, AIN, IN, U>(P, i, j, k);
 }
 
 // ---- limiter bounds and ratios (std :256-348, gauge :238-324) -------------
@@ -293,8 +306,10 @@ __device__ __forceinline__ void pseudo_body(const Prob<R>& P, int i, int j, int 
 // from the stored running extrema (KEEP stores them).  The gauge k=1 minimum
 // over x_in, which the reference leaves unset (antidiff3d-gauge-gpubc.f90:249),
 // is computed as in mpdata3d-rho-gauge-gpubc.f90:365-368.  Also stores
-// q = x/rhr, the ratio every later stage divides out.
-template <class R, bool NONOS, bool FIRST, bool KEEP, bool IN = false>
+// q = x/rhr, the ratio every later stage divides out.  CL: cp and cn are read
+// only through min3 (the forward limiter), so a ratio >= 1 may be stored as 1
+// (lim_ratio); the adjoint's records keep the exact quotients.
+template <class R, bool NONOS, bool FIRST, bool KEEP, bool IN = false, bool CL = false>
 __device__ __forceinline__ void bounds_body(const Prob<R>& P, int i, int j, int k) {
   const Geo& g = P.g;
   const Arr<R>& X = P.xant;
@@ -347,8 +362,10 @@ __device__ __forceinline__ void bounds_body(const Prob<R>& P, int i, int j, int 
   const R e2 = fy<R, false, IN>(g, F2, i, j + 1, k), w2 = fy<R, false, IN>(g, F2, i, j, k);
   const R e3 = fz<R, false, IN>(g, F3, i, j, k + 1), w3 = fz<R, false, IN>(g, F3, i, j, k);
   const R hc = P.h.ld(i, j, k);
-  P.cp.at(i, j, k) = mul1(ma - x, hc) / (pn(e1) + pp(w1) + pn(e2) + pp(w2) + pn(e3) + pp(w3) + ep);
-  P.cn.at(i, j, k) = mul1(x - mi, hc) / (pp(e1) + pn(w1) + pp(e2) + pn(w2) + pp(e3) + pn(w3) + ep);
+  const R np_ = mul1(ma - x, hc), dp = pn(e1) + pp(w1) + pn(e2) + pp(w2) + pn(e3) + pp(w3) + ep;
+  const R nn = mul1(x - mi, hc), dn = pp(e1) + pn(w1) + pp(e2) + pn(w2) + pp(e3) + pn(w3) + ep;
+  P.cp.at(i, j, k) = CL ? lim_ratio(np_, dp) : np_ / dp;
+  P.cn.at(i, j, k) = CL ? lim_ratio(nn, dn) : nn / dn;
 }
 
 // ---- limited antidiffusive velocities and fluxes --------------------------

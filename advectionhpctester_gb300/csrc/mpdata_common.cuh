@@ -118,6 +118,23 @@ __device__ __forceinline__ float mul1(float x, float r) { return x * r; }
 __device__ __forceinline__ float div1(float x, float r) { return x / r; }
 __device__ __forceinline__ float rcp1(float r) { return 1.0f / r; }
 
+// Limiter ratio n/d (n >= 0, d >= ep > 0) where the only reader takes
+// min(1, n/d, ...): when n >= d and d is finite the IEEE quotient is >= 1, so
+// 1 is returned without dividing and the minimum is unchanged bit for bit.
+// NaN operands (n above +Inf, d not a positive finite number) divide as usual.
+// The test runs on the integer pipe: for non-negative numbers the bit
+// patterns order as the values do.
+__device__ __forceinline__ double lim_ratio(double n, double d) {
+  const long long nb = __double_as_longlong(n), db = __double_as_longlong(d), inf = 0x7FF0000000000000LL;
+  if (db > 0 && db < inf && nb >= db && nb <= inf) return 1.0;
+  return div_call(n, d);
+}
+__device__ __forceinline__ float lim_ratio(float n, float d) {
+  const int nb = __float_as_int(n), db = __float_as_int(d), inf = 0x7F800000;
+  if (db > 0 && db < inf && nb >= db && nb <= inf) return 1.0f;
+  return n / d;
+}
+
 // ---- point operators (device forms of mpdataoperators.inc:50-96) ----
 template <class R> __device__ __forceinline__ R donor(R y1, R y2, R a) { return pp(a) * y1 - pn(a) * y2; }
 template <class R> __device__ __forceinline__ R vdyf(R x1, R x2, R a, R rinv) {
@@ -132,6 +149,24 @@ template <class R> __device__ __forceinline__ R vdyfa(R x1, R x2, R a, R rinv, R
 template <class R> __device__ __forceinline__ R vcorra(R a, R b, R y1, R y2, R rinv) {
   return -(mul1(R(0.125) * a * b * y1, rinv) / y2);
 }
+// Forms of the pseudo-velocity operators for the stage kernels.  U: every face
+// density of the warp is exactly 1, so the products by it are dropped (exact,
+// as above).  dif4 is rat4 without its factor 0.25, which the caller folds into
+// the 0.125 of the cross term (0.125*0.25 = 0.03125).  Scaling by a power of
+// two commutes with rounding, so the folded form gives the same bits as
+// rat4's order whenever no intermediate is subnormal (|value| < 2^-1022 in
+// FP64, 2^-126 in FP32), and differs by at most a subnormal ulp otherwise.
+template <bool U, class R> __device__ __forceinline__ R hmul(R x, R hm) { return U ? x : x * hm; }
+template <bool U, class R> __device__ __forceinline__ R vdyf_u(R x1, R x2, R a, R hm) {
+  return (fabs(a) - hmul<U>(a * a, hm)) * (x2 - x1) * R(0.5);
+}
+template <bool U, class R> __device__ __forceinline__ R vdyfa_u(R x1, R x2, R a, R hm, R ep) {
+  return (fabs(a) - hmul<U>(a * a, hm)) * (fabs(x2) - fabs(x1)) / (fabs(x2) + fabs(x1) + ep);
+}
+template <bool U, class R> __device__ __forceinline__ R vcorra_u(R a, R b, R y1, R y2, R hm) {
+  return -(hmul<U>(R(0.125) * a * b * y1, hm) / y2);
+}
+template <class R> __device__ __forceinline__ R dif4(R z0, R z1, R z2, R z3) { return (z3 + z2) - (z1 + z0); }
 template <class R> __device__ __forceinline__ R possign(R x) { return sgn(x) ? R(0) : R(1); }
 template <class R> __device__ __forceinline__ R min3(R a, R b) { return mn2(mn2(R(1), a), b); }
 // 1/(0.5*(h1+h2)) == 2/(h1+h2) exactly: the halving is an exact scaling.

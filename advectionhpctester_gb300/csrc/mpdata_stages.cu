@@ -59,13 +59,21 @@ struct PseudoMinBlocks {
 
 template <class R, bool AIN>
 __global__ void __launch_bounds__(128, PseudoMinBlocks<R>::v) k_pseudo(const Prob<R> P) {
-#define B(IN) pseudo_body<R, AIN, IN>(P, i, j, k)
-  CELL_DISPATCH(B)
-#undef B
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int k = blockIdx.z + 1;
+  const bool win = warp_interior(P.g, i, j, k);
+  if (i > P.g.np || j > P.g.mp) return;
+  if (!win)
+    pseudo_body<R, AIN, false>(P, i, j, k);
+  else if (warp_unit_faces(P, i, j, k))
+    pseudo_body<R, AIN, true, true>(P, i, j, k);
+  else
+    pseudo_body<R, AIN, true>(P, i, j, k);
 }
 template <class R, bool NONOS, bool FIRST, bool KEEP>
 __global__ void __launch_bounds__(128) k_bounds(const Prob<R> P) {
-#define B(IN) bounds_body<R, NONOS, FIRST, KEEP, IN>(P, i, j, k)
+#define B(IN) bounds_body<R, NONOS, FIRST, KEEP, IN, true>(P, i, j, k)
   CELL_DISPATCH(B)
 #undef B
 }
