@@ -108,12 +108,25 @@ __device__ __forceinline__ bool warp_unit_faces(const Prob<R>& P, int i, int j, 
   }
 }
 
+// True when h (and rhr, outside the density step) is exactly 1 at every cell
+// of the warp (FP64 only).  Bodies instantiated with U drop the products and
+// quotients by these densities: exact, as x*1 == x/1 == x.
+template <class R>
+__device__ __forceinline__ bool warp_unit_cell(const Prob<R>& P, int i, int j, int k) {
+  if constexpr (sizeof(R) == 8) {
+    const bool u = is_one(P.h.ld(i, j, k)) && (P.rho || is_one(P.rhr.ld(i, j, k)));
+    return __all_sync(0xffffffffu, u);
+  } else {
+    return false;
+  }
+}
+
 // ---- upwind3d_gpubc (upwind3d-gpubc.f90:101-198) -------------------------
 // ANTIDIFF: an antidiffusive pass follows, so psi's open-wall halo ends the
 // step holding the zero-gradient copy of the old boundary values (written by
 // cp_last_to_halo_xy in the antidiffusion); otherwise it keeps bcx/bcy.
 // HALO: write psi's halo at all (off while autotuning).
-template <class R, bool ANTIDIFF, bool HALO, bool IN = false>
+template <class R, bool ANTIDIFF, bool HALO, bool IN = false, bool U = false>
 __device__ __forceinline__ void upwind_body(const Prob<R>& P, int i, int j, int k) {
   const Geo& g = P.g;
   const Arr<R>& psi = P.psi;
@@ -125,7 +138,7 @@ __device__ __forceinline__ void upwind_body(const Prob<R>& P, int i, int j, int 
   const R xjm = (IN || j > 1) ? psi.ld(i, j - 1, k) : (g.by ? psi.ld(i, g.mp, k) : P.bcy[by0]);
   const R xjp = (IN || j < g.mp) ? psi.ld(i, j + 1, k) : (g.by ? psi.ld(i, 1, k) : P.bcy[by0 + bys]);
   const R hc = P.h.ld(i, j, k);
-  const R hi = rcp1(hc);
+  const R hi = U ? R(1) : rcp1(hc);
   const R f1p = donor(x, xip, fx<R, true, IN>(g, P.u1, i + 1, j, k));
   const R f1 = donor(xim, x, P.u1.ld(i, j, k));
   const R f2p = donor(x, xjp, fy<R, true, IN>(g, P.u2, i, j + 1, k));
@@ -144,7 +157,8 @@ __device__ __forceinline__ void upwind_body(const Prob<R>& P, int i, int j, int 
   if (P.rho) {
     // mpdata3d-rho-gauge-gpubc.f90:137-210: no rhr, division by h, fluxes kept;
     // rhoadv takes the input x_incomp (:121-123)
-    P.xant.at(i, j, k) = x - div1(f1p - f1 + f2p - f2 + f3p - f3, hc);
+    const R sum = f1p - f1 + f2p - f2 + f3p - f3;
+    P.xant.at(i, j, k) = x - (U ? sum : div1(sum, hc));
     P.f1.at(i, j, k) = f1;
     P.f2.at(i, j, k) = f2;
     P.f3.at(i, j, k) = f3;
@@ -153,7 +167,8 @@ __device__ __forceinline__ void upwind_body(const Prob<R>& P, int i, int j, int 
     if (k == g.lp) P.f3hi[(i - 1) + (long)g.np * (j - 1)] = f3p;
     P.rhoadv.at(i, j, k) = P.x_incomp.ld(i, j, k);
   } else {
-    P.xant.at(i, j, k) = mul1(x - mul1(f1p - f1 + f2p - f2 + f3p - f3, hi), P.rhr.ld(i, j, k));
+    const R sum = f1p - f1 + f2p - f2 + f3p - f3;
+    P.xant.at(i, j, k) = U ? x - sum : (x - sum * hi) * P.rhr.ld(i, j, k);
   }
   if (ANTIDIFF && P.own_vel) {
     P.hinv.at(i, j, k) = hi;
@@ -309,12 +324,12 @@ __device__ __forceinline__ void pseudo_body(const Prob<R>& P, int i, int j, int 
 // q = x/rhr, the ratio every later stage divides out.  CL: cp and cn are read
 // only through min3 (the forward limiter), so a ratio >= 1 may be stored as 1
 // (lim_ratio); the adjoint's records keep the exact quotients.
-template <class R, bool NONOS, bool FIRST, bool KEEP, bool IN = false, bool CL = false>
+template <class R, bool NONOS, bool FIRST, bool KEEP, bool IN = false, bool CL = false, bool U = false>
 __device__ __forceinline__ void bounds_body(const Prob<R>& P, int i, int j, int k) {
   const Geo& g = P.g;
   const Arr<R>& X = P.xant;
   const R x = X.ld(i, j, k);
-  P.q.at(i, j, k) = P.rho ? x : div1(x, P.rhr.ld(i, j, k));  // x/1 == x for the density step
+  P.q.at(i, j, k) = (P.rho || U) ? x : div1(x, P.rhr.ld(i, j, k));  // x/1 == x for the density step
   if (!NONOS) return;
   const bool lo = IN || g.bz || k > 1, hi = IN || g.bz || k < g.lp;
   R ma, mi;
@@ -361,9 +376,9 @@ __device__ __forceinline__ void bounds_body(const Prob<R>& P, int i, int j, int 
   const R e1 = fx<R, false, IN>(g, F1, i + 1, j, k), w1 = fx<R, false, IN>(g, F1, i, j, k);
   const R e2 = fy<R, false, IN>(g, F2, i, j + 1, k), w2 = fy<R, false, IN>(g, F2, i, j, k);
   const R e3 = fz<R, false, IN>(g, F3, i, j, k + 1), w3 = fz<R, false, IN>(g, F3, i, j, k);
-  const R hc = P.h.ld(i, j, k);
-  const R np_ = mul1(ma - x, hc), dp = pn(e1) + pp(w1) + pn(e2) + pp(w2) + pn(e3) + pp(w3) + ep;
-  const R nn = mul1(x - mi, hc), dn = pp(e1) + pn(w1) + pp(e2) + pn(w2) + pp(e3) + pn(w3) + ep;
+  const R hc = U ? R(1) : P.h.ld(i, j, k);
+  const R np_ = U ? ma - x : (ma - x) * hc, dp = pn(e1) + pp(w1) + pn(e2) + pp(w2) + pn(e3) + pp(w3) + ep;
+  const R nn = U ? x - mi : (x - mi) * hc, dn = pp(e1) + pn(w1) + pp(e2) + pn(w2) + pp(e3) + pn(w3) + ep;
   P.cp.at(i, j, k) = CL ? lim_ratio(np_, dp) : np_ / dp;
   P.cn.at(i, j, k) = CL ? lim_ratio(nn, dn) : nn / dn;
 }
@@ -374,7 +389,7 @@ __device__ __forceinline__ void bounds_body(const Prob<R>& P, int i, int j, int 
 // limited velocity is the flux).  Lower faces of each cell.
 template <class R>
 __device__ __forceinline__ R vlim_std(R v, R a1, R a2, R xl, R xrr) {
-  return pp(v) * (a1 * possign(xl) + a2 * possign(-xl)) - pn(v) * (a2 * possign(xrr) + a1 * possign(-xrr));
+  return donor(a1 * possign(xl) + a2 * possign(-xl), a2 * possign(xrr) + a1 * possign(-xrr), v);
 }
 
 template <class R, bool STD, bool NONOS, bool IN = false>
@@ -390,7 +405,7 @@ __device__ __forceinline__ void limit_form(const Prob<R>& P, int i, int j, int k
     if (NONOS) {
       const R cpm = P.cp.ld(im, j, k), cnm = P.cn.ld(im, j, k);
       w = STD ? vlim_std(v, min3(cpc, cnm), min3(cpm, cnc), X.ld(im, j, k), xc)
-              : pp(v) * min3(cpc, cnm) - pn(v) * min3(cpm, cnc);
+              : donor(min3(cpc, cnm), min3(cpm, cnc), v);
     }
     P.w1.at(i, j, k) = w;
     if (STD) P.f1.at(i, j, k) = donor(P.q.ld(im, j, k), qc, w);
@@ -402,7 +417,7 @@ __device__ __forceinline__ void limit_form(const Prob<R>& P, int i, int j, int k
     if (NONOS) {
       const R cpm = P.cp.ld(i, jm, k), cnm = P.cn.ld(i, jm, k);
       w = STD ? vlim_std(v, min3(cpc, cnm), min3(cpm, cnc), X.ld(i, jm, k), xc)
-              : pp(v) * min3(cpc, cnm) - pn(v) * min3(cpm, cnc);
+              : donor(min3(cpc, cnm), min3(cpm, cnc), v);
     }
     P.w2.at(i, j, k) = w;
     if (STD) P.f2.at(i, j, k) = donor(P.q.ld(i, jm, k), qc, w);
@@ -414,7 +429,7 @@ __device__ __forceinline__ void limit_form(const Prob<R>& P, int i, int j, int k
     if (NONOS) {
       const R cpm = P.cp.ld(i, j, km), cnm = P.cn.ld(i, j, km);
       w = STD ? vlim_std(v, min3(cpc, cnm), min3(cpm, cnc), X.ld(i, j, km), xc)
-              : pp(v) * min3(cpc, cnm) - pn(v) * min3(cpm, cnc);
+              : donor(min3(cpc, cnm), min3(cpm, cnc), v);
     }
     P.w3.at(i, j, k) = w;
     if (STD) P.f3.at(i, j, k) = donor(P.q.ld(i, j, km), qc, w);
@@ -432,7 +447,7 @@ __device__ __forceinline__ void limit_body(const Prob<R>& P, int i, int j, int k
 // ---- corrective update (std :431-459, gauge :364-368/396-400/423-427) -----
 // LAST: the last pass writes psi; earlier passes overwrite xant in place (the
 // update reads q, not x).
-template <class R, bool LAST, bool IN = false>
+template <class R, bool LAST, bool IN = false, bool U = false>
 __device__ __forceinline__ void update_body(const Prob<R>& P, int i, int j, int k) {
   const Geo& g = P.g;
   const Arr<R>& out = LAST ? P.psi : P.xant;
@@ -440,13 +455,13 @@ __device__ __forceinline__ void update_body(const Prob<R>& P, int i, int j, int 
     const R d = fx<R, false, IN>(g, P.f1, i + 1, j, k) - fx<R, false, IN>(g, P.f1, i, j, k) +
                 fy<R, false, IN>(g, P.f2, i, j + 1, k) - fy<R, false, IN>(g, P.f2, i, j, k) +
                 fz<R, false, IN>(g, P.f3, i, j, k + 1) - fz<R, false, IN>(g, P.f3, i, j, k);
-    out.at(i, j, k) = mul1(P.q.ld(i, j, k) - mul1(d, P.hinv.ld(i, j, k)), P.rhr.ld(i, j, k));
+    out.at(i, j, k) = U ? P.q.ld(i, j, k) - d : (P.q.ld(i, j, k) - d * P.hinv.ld(i, j, k)) * P.rhr.ld(i, j, k);
   } else {
     const R d = fx<R, false, IN>(g, P.w1, i + 1, j, k) - fx<R, false, IN>(g, P.w1, i, j, k) +
                 fy<R, false, IN>(g, P.w2, i, j + 1, k) - fy<R, false, IN>(g, P.w2, i, j, k) +
                 fz<R, false, IN>(g, P.w3, i, j, k + 1) - fz<R, false, IN>(g, P.w3, i, j, k);
-    const R t = P.q.ld(i, j, k) - div1(d, P.h.ld(i, j, k));
-    out.at(i, j, k) = P.rho ? t : mul1(t, P.rhr.ld(i, j, k));  // rhr == 1 in the density step
+    const R t = P.q.ld(i, j, k) - (U ? d : div1(d, P.h.ld(i, j, k)));
+    out.at(i, j, k) = (P.rho || U) ? t : t * P.rhr.ld(i, j, k);  // rhr == 1 in the density step
   }
 }
 

@@ -136,7 +136,19 @@ __device__ __forceinline__ float lim_ratio(float n, float d) {
 }
 
 // ---- point operators (device forms of mpdataoperators.inc:50-96) ----
-template <class R> __device__ __forceinline__ R donor(R y1, R y2, R a) { return pp(a) * y1 - pn(a) * y2; }
+__device__ __forceinline__ float donor(float y1, float y2, float a) { return pp(a) * y1 - pn(a) * y2; }
+// FP64 donor flux pp(a)*y1 - pn(a)*y2 with one multiplication.  For finite
+// operands one of the two products is a zero, and rounding is symmetric in
+// sign, so a nonzero result is a*y1 (a > 0) or -((-a)*y2) = a*y2 (a <= 0).
+// When that product is zero, the two signed zeros the reference subtracts
+// give -0 exactly when y1's sign bit is set and y2's is not, whatever a is;
+// that zero is returned.  The tests are integer operations, which leave the
+// FP64 pipe (the bound of every FP64 stage) to the multiplication.
+__device__ __forceinline__ double donor(double y1, double y2, double a) {
+  const double m = a * (__double_as_longlong(a) > 0 ? y1 : y2);
+  if ((__double_as_longlong(m) << 1) != 0) return m;
+  return (sgn(y1) && !sgn(y2)) ? -0.0 : 0.0;
+}
 template <class R> __device__ __forceinline__ R vdyf(R x1, R x2, R a, R rinv) {
   return (fabs(a) - mul1(a * a, rinv)) * (x2 - x1) * R(0.5);
 }

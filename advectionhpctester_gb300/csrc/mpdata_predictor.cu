@@ -8,27 +8,52 @@
 
 namespace mpdata {
 
-// n+1/2 momenta times dt/dx into level 1 (module_velprd.f90:60-83)
-template <class R>
-__global__ void __launch_bounds__(128) k_pred_level(Geo g, long lev, R* ox, R* oy, R* oz, Arr<R> h,
-                                                    R gc1, R gc2, R gc3, R r) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int k = blockIdx.z + 1;
-  if (i > g.np || j > g.mp) return;
-  const R hc = h.ld(i, j, k);
+// n+1/2 momenta times dt/dx into level 1 (module_velprd.f90:60-83):
+// 0.5*(a1+a0)*gc, taken as (a1+a0)*hgc with hgc = 0.5*gc formed on the host
+// (scaling by 0.5 commutes with rounding unless a value is subnormal).  R1:
+// the time-step ratio r is exactly 1, so r*(a0-a2) is a0-a2.  A warp whose
+// densities are all exactly 1 takes a0 = ox(level 0) without the product.
+template <class R, bool U, bool R1>
+__device__ __forceinline__ void pred_level_cell(long lev, long off, R* ox, R* oy, R* oz, R hc, R hg1, R hg2,
+                                                R hg3, R r) {
   R* o[3] = {ox, oy, oz};
-  const R gc[3] = {gc1, gc2, gc3};
-  // ox/oy/oz point at the logical (1,1,1) of level 0; levels are psi-shaped
-  const long off = (long)(i - 1) + (long)(j - 1) * h.sy + (long)(k - 1) * h.sz;
+  const R hg[3] = {hg1, hg2, hg3};
 #pragma unroll
   for (int c = 0; c < 3; c++) {
     R* p0 = o[c] + off;
-    const R a0 = mul1(p0[0], hc);
+    const R a0 = U ? p0[0] : p0[0] * hc;
     const R a2 = p0[2 * lev];
-    const R a1 = a0 + r * (a0 - a2);
-    p0[lev] = R(0.5) * (a1 + a0) * gc[c];
+    const R a1 = a0 + (R1 ? a0 - a2 : r * (a0 - a2));
+    p0[lev] = (a1 + a0) * hg[c];
   }
+}
+
+// True on every lane when each live lane's density is exactly 1 (FP64; FP32
+// kernels keep the products).  Called by all 32 lanes before any returns.
+template <class R>
+__device__ __forceinline__ bool warp_unit_h(bool live, const Arr<R>& h, int i, int j, int k) {
+  if constexpr (sizeof(R) == 8) {
+    return __all_sync(0xffffffffu, !live || is_one(h.ld(i, j, k)));
+  } else {
+    return false;
+  }
+}
+
+template <class R, bool R1>
+__global__ void __launch_bounds__(128) k_pred_level(Geo g, long lev, R* ox, R* oy, R* oz, Arr<R> h,
+                                                    R hg1, R hg2, R hg3, R r) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int k = blockIdx.z + 1;
+  const bool live = i <= g.np && j <= g.mp;
+  const bool unit = warp_unit_h<R>(live, h, i, j, k);
+  if (!live) return;
+  // ox/oy/oz point at the logical (1,1,1) of level 0; levels are psi-shaped
+  const long off = (long)(i - 1) + (long)(j - 1) * h.sy + (long)(k - 1) * h.sz;
+  if (unit)
+    pred_level_cell<R, true, R1>(lev, off, ox, oy, oz, R(1), hg1, hg2, hg3, r);
+  else
+    pred_level_cell<R, false, R1>(lev, off, ox, oy, oz, h.ld(i, j, k), hg1, hg2, hg3, r);
 }
 
 // C-grid averaging with the open-wall extrapolation 2a(1)-a(2)
@@ -36,11 +61,11 @@ __global__ void __launch_bounds__(128) k_pred_level(Geo g, long lev, R* ox, R* o
 // The level roll of velprd_driver.f90:254-270 for cell (i,j,k): physical
 // velocities extrapolated into level 1 and copied into level 2, and the
 // level-0 momenta times h stored in level 2 for the next step.
-template <class R>
+template <class R, bool U = false>
 __device__ __forceinline__ void roll_cell(long lev, R* ox, R* oy, R* oz, R* pu, R* pv, R* pw, const Arr<R>& h,
                                           R r, int i, int j, int k) {
   const long off = (long)(i - 1) + (long)(j - 1) * h.sy + (long)(k - 1) * h.sz;
-  const R hc = h.ld(i, j, k);
+  const R hc = U ? R(1) : h.ld(i, j, k);
   R* o[3] = {ox, oy, oz};
   R* p[3] = {pu, pv, pw};
 #pragma unroll
@@ -52,7 +77,7 @@ __device__ __forceinline__ void roll_cell(long lev, R* ox, R* oy, R* oz, R* pu, 
       q[2 * lev] = p0;
     }
     R* q = o[c] + off;
-    q[2 * lev] = mul1(q[0], hc);
+    q[2 * lev] = U ? q[0] : q[0] * hc;
   }
 }
 
@@ -63,6 +88,8 @@ __global__ void __launch_bounds__(128) k_pred_cgrid(Geo g, long lev, R* ox, R* o
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int k = blockIdx.z + 1;
+  const bool rl = ROLL && i <= g.np && j <= g.mp && k <= g.lp;
+  const bool unit = ROLL && warp_unit_h<R>(rl, h, i, j, k);
   if (i > g.np + 1 || j > g.mp + 1) return;
   // level-1 views (ox etc. point at the logical (1,1,1) of level 0)
   const Arr<R> A1{ox + lev, h.sy, h.sz}, A2{oy + lev, h.sy, h.sz}, A3{oz + lev, h.sy, h.sz};
@@ -108,7 +135,12 @@ __global__ void __launch_bounds__(128) k_pred_cgrid(Geo g, long lev, R* ox, R* o
     }
     u3.at(i, j, k) = R(0.5) * (a + b);
   }
-  if (ROLL && i <= g.np && j <= g.mp && k <= g.lp) roll_cell<R>(lev, ox, oy, oz, pu, pv, pw, h, r, i, j, k);
+  if (rl) {
+    if (unit)
+      roll_cell<R, true>(lev, ox, oy, oz, pu, pv, pw, h, r, i, j, k);
+    else
+      roll_cell<R>(lev, ox, oy, oz, pu, pv, pw, h, r, i, j, k);
+  }
 }
 
 template <class R>
@@ -198,7 +230,11 @@ int run_pred_parts(const PredPlan<R>& P, bool level, bool cgrid, bool roll, cuda
   int n = 0;
   if (level) {
     if (P.prof) P.prof->begin(ST_PRED_LEVEL, s);
-    k_pred_level<R><<<g1, blk, 0, s>>>(g, P.lev, P.ox, P.oy, P.oz, P.h, P.gc1, P.gc2, P.gc3, P.dt_ratio);
+    const R hg1 = R(0.5) * P.gc1, hg2 = R(0.5) * P.gc2, hg3 = R(0.5) * P.gc3;
+    if (P.dt_ratio == R(1))
+      k_pred_level<R, true><<<g1, blk, 0, s>>>(g, P.lev, P.ox, P.oy, P.oz, P.h, hg1, hg2, hg3, P.dt_ratio);
+    else
+      k_pred_level<R, false><<<g1, blk, 0, s>>>(g, P.lev, P.ox, P.oy, P.oz, P.h, hg1, hg2, hg3, P.dt_ratio);
     if (P.prof) P.prof->end(ST_PRED_LEVEL, s);
     n++;
   }

@@ -30,10 +30,26 @@ namespace mpdata {
     BODY(false);                                            \
   }
 
+// As CELL_DISPATCH, with the unit-density instantiation (BODY(IN, U)) for
+// interior warps whose densities are all exactly 1.
+#define CELL_DISPATCH_U(BODY)                               \
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1; \
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1; \
+  const int k = blockIdx.z + 1;                             \
+  const bool win = warp_interior(P.g, i, j, k);             \
+  if (i > P.g.np || j > P.g.mp) return;                     \
+  if (!win) {                                               \
+    BODY(false, false);                                     \
+  } else if (warp_unit_cell(P, i, j, k)) {                  \
+    BODY(true, true);                                       \
+  } else {                                                  \
+    BODY(true, false);                                      \
+  }
+
 template <class R, bool ANTIDIFF>
 __global__ void __launch_bounds__(128) k_upwind(const Prob<R> P) {
-#define B(IN) upwind_body<R, ANTIDIFF, true, IN>(P, i, j, k)
-  CELL_DISPATCH(B)
+#define B(IN, U) upwind_body<R, ANTIDIFF, true, IN, U>(P, i, j, k)
+  CELL_DISPATCH_U(B)
 #undef B
 }
 template <class R>
@@ -73,8 +89,8 @@ __global__ void __launch_bounds__(128, PseudoMinBlocks<R>::v) k_pseudo(const Pro
 }
 template <class R, bool NONOS, bool FIRST, bool KEEP>
 __global__ void __launch_bounds__(128) k_bounds(const Prob<R> P) {
-#define B(IN) bounds_body<R, NONOS, FIRST, KEEP, IN, true>(P, i, j, k)
-  CELL_DISPATCH(B)
+#define B(IN, U) bounds_body<R, NONOS, FIRST, KEEP, IN, true, U>(P, i, j, k)
+  CELL_DISPATCH_U(B)
 #undef B
 }
 template <class R, bool NONOS>
@@ -85,8 +101,8 @@ __global__ void __launch_bounds__(128) k_limit(const Prob<R> P) {
 }
 template <class R, bool LAST>
 __global__ void __launch_bounds__(128) k_update(const Prob<R> P) {
-#define B(IN) update_body<R, LAST, IN>(P, i, j, k)
-  CELL_DISPATCH(B)
+#define B(IN, U) update_body<R, LAST, IN, U>(P, i, j, k)
+  CELL_DISPATCH_U(B)
 #undef B
 }
 
