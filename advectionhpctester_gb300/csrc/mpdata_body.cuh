@@ -25,6 +25,7 @@ struct Prob {
   int stdf;     // 1 = standard form (t_adv=2), 0 = infinite gauge (t_adv=1)
   int own_vel;  // 1 = this problem writes the velocity-derived scratch (hinv, hm*)
   int rho;      // density step of mpdata3d_rho_gauge_gpubc: no rhr, upwind fluxes kept
+  int pairs;    // gauge pseudo-velocity: pair sums of xant in cp, cn, q (k_pairs)
   Arr<R> psi, u1, u2, u3, h, rhr;
   const R* bcx;
   const R* bcy;
@@ -197,8 +198,10 @@ __device__ __forceinline__ void upwind_body(const Prob<R>& P, int i, int j, int 
 // Each cell computes its lower faces.  AIN: the first corrective pass, whose
 // "a" velocities are the caller's Courant numbers; later passes use the
 // previous pass's limited velocities w1..w3.  U: the three face reciprocal
-// densities of every cell of the warp are exactly 1 (warp_unit_faces).
-template <class R, bool STD, bool AIN, bool IN = false, bool U = false>
+// densities of every cell of the warp are exactly 1 (warp_unit_faces).  PS
+// (gauge, interior warps): the pair sums of xant the rat4 terms start with
+// are read from cp, cn and q, where k_pairs stored them.
+template <class R, bool STD, bool AIN, bool IN = false, bool U = false, bool PS = false>
 __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int k) {
   const Geo& g = P.g;
   const Arr<R>& X = P.xant;
@@ -232,12 +235,15 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
                        hmx);
       P.f1.at(i, j, k) = donor(XX(i - 1, j, k), XX(i, j, k), v);
     } else {
-      const R c2 = (AY(i - 1, j, k) + AY(i - 1, j + 1, k) + AY(i, j + 1, k) + AY(i, j, k)) *
-                   dif4(XX(i - 1, j - 1, k), XX(i, j - 1, k), XX(i - 1, j + 1, k), XX(i, j + 1, k));
+      const R d2 = PS ? P.cp.ld(i, j + 1, k) - P.cp.ld(i, j - 1, k)
+                      : dif4(XX(i - 1, j - 1, k), XX(i, j - 1, k), XX(i - 1, j + 1, k), XX(i, j + 1, k));
+      const R c2 = (AY(i - 1, j, k) + AY(i - 1, j + 1, k) + AY(i, j + 1, k) + AY(i, j, k)) * d2;
       R cr = c2;
-      if (zt)
-        cr = c2 + (AZ(i - 1, j, k) + AZ(i - 1, j, k + 1) + AZ(i, j, k + 1) + AZ(i, j, k)) *
-                      dif4(XX(i - 1, j, k - 1), XX(i, j, k - 1), XX(i - 1, j, k + 1), XX(i, j, k + 1));
+      if (zt) {
+        const R d3 = PS ? P.cp.ld(i, j, k + 1) - P.cp.ld(i, j, k - 1)
+                        : dif4(XX(i - 1, j, k - 1), XX(i, j, k - 1), XX(i - 1, j, k + 1), XX(i, j, k + 1));
+        cr = c2 + (AZ(i - 1, j, k) + AZ(i - 1, j, k + 1) + AZ(i, j, k + 1) + AZ(i, j, k)) * d3;
+      }
       v = vdyf_u<U>(XX(i - 1, j, k), XX(i, j, k), a, hmx) - hmul<U>(R(0.03125) * a, hmx) * cr;
     }
     P.v1.at(i, j, k) = v;
@@ -263,12 +269,15 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
                        hmy);
       P.f2.at(i, j, k) = donor(XX(i, j - 1, k), XX(i, j, k), v);
     } else {
-      const R c1 = (AX(i, j - 1, k) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j - 1, k)) *
-                   dif4(XX(i - 1, j - 1, k), XX(i - 1, j, k), XX(i + 1, j - 1, k), XX(i + 1, j, k));
+      const R d1 = PS ? P.cn.ld(i + 1, j, k) - P.cn.ld(i - 1, j, k)
+                      : dif4(XX(i - 1, j - 1, k), XX(i - 1, j, k), XX(i + 1, j - 1, k), XX(i + 1, j, k));
+      const R c1 = (AX(i, j - 1, k) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j - 1, k)) * d1;
       R cr = c1;
-      if (zt)
-        cr = c1 + (AZ(i, j - 1, k) + AZ(i, j, k) + AZ(i, j, k + 1) + AZ(i, j - 1, k + 1)) *
-                      dif4(XX(i, j - 1, k - 1), XX(i, j, k - 1), XX(i, j - 1, k + 1), XX(i, j, k + 1));
+      if (zt) {
+        const R d3 = PS ? P.cn.ld(i, j, k + 1) - P.cn.ld(i, j, k - 1)
+                        : dif4(XX(i, j - 1, k - 1), XX(i, j, k - 1), XX(i, j - 1, k + 1), XX(i, j, k + 1));
+        cr = c1 + (AZ(i, j - 1, k) + AZ(i, j, k) + AZ(i, j, k + 1) + AZ(i, j - 1, k + 1)) * d3;
+      }
       v = vdyf_u<U>(XX(i, j - 1, k), XX(i, j, k), a, hmy) - hmul<U>(R(0.03125) * a, hmy) * cr;
     }
     P.v2.at(i, j, k) = v;
@@ -293,10 +302,12 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
                  hmz);
       P.f3.at(i, j, k) = donor(XX(i, j, k - 1), XX(i, j, k), v);
     } else {
-      const R cr = (AX(i, j, k - 1) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j, k - 1)) *
-                       dif4(XX(i - 1, j, k - 1), XX(i - 1, j, k), XX(i + 1, j, k - 1), XX(i + 1, j, k)) +
-                   (AY(i, j, k - 1) + AY(i, j + 1, k - 1) + AY(i, j + 1, k) + AY(i, j, k)) *
-                       dif4(XX(i, j - 1, k - 1), XX(i, j - 1, k), XX(i, j + 1, k - 1), XX(i, j + 1, k));
+      const R d1 = PS ? P.q.ld(i + 1, j, k) - P.q.ld(i - 1, j, k)
+                      : dif4(XX(i - 1, j, k - 1), XX(i - 1, j, k), XX(i + 1, j, k - 1), XX(i + 1, j, k));
+      const R d2 = PS ? P.q.ld(i, j + 1, k) - P.q.ld(i, j - 1, k)
+                      : dif4(XX(i, j - 1, k - 1), XX(i, j - 1, k), XX(i, j + 1, k - 1), XX(i, j + 1, k));
+      const R cr = (AX(i, j, k - 1) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j, k - 1)) * d1 +
+                   (AY(i, j, k - 1) + AY(i, j + 1, k - 1) + AY(i, j + 1, k) + AY(i, j, k)) * d2;
       v = vdyf_u<U>(XX(i, j, k - 1), XX(i, j, k), a, hmz) - hmul<U>(R(0.03125) * a, hmz) * cr;
     }
     P.v3.at(i, j, k) = v;
@@ -307,12 +318,12 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
 #undef AZ
 }
 
-template <class R, bool AIN, bool IN = false, bool U = false>
+template <class R, bool AIN, bool IN = false, bool U = false, bool PS = false>
 __device__ __forceinline__ void pseudo_body(const Prob<R>& P, int i, int j, int k) {
   if (P.stdf)
     pseudo_form<R, true, AIN, IN, U>(P, i, j, k);
   else
-    pseudo_form<R, false, AIN, IN, U>(P, i, j, k);
+    pseudo_form<R, false, AIN, IN, U, PS>(P, i, j, k);
 }
 
 // ---- limiter bounds and ratios (std :256-348, gauge :238-324) -------------
@@ -321,16 +332,21 @@ __device__ __forceinline__ void pseudo_body(const Prob<R>& P, int i, int j, int 
 // from the stored running extrema (KEEP stores them).  The gauge k=1 minimum
 // over x_in, which the reference leaves unset (antidiff3d-gauge-gpubc.f90:249),
 // is computed as in mpdata3d-rho-gauge-gpubc.f90:365-368.  Also stores
-// q = x/rhr, the ratio every later stage divides out.  CL: cp and cn are read
-// only through min3 (the forward limiter), so a ratio >= 1 may be stored as 1
-// (lim_ratio); the adjoint's records keep the exact quotients.
-template <class R, bool NONOS, bool FIRST, bool KEEP, bool IN = false, bool CL = false, bool U = false>
-__device__ __forceinline__ void bounds_body(const Prob<R>& P, int i, int j, int k) {
+// q = x/rhr, the ratio every later stage divides out.  cp and cn are read
+// only through min3 by the forward limiter, so a ratio >= 1 may be stored as 1.
+// CLM 0: exact quotients (the adjoint's records); 1: lim_ratio per cell;
+// 2: nothing stored, the four operands returned for the caller to divide.
+template <class R>
+struct RatioOps {
+  R np, dp, nn, dn;
+};
+template <class R, bool NONOS, bool FIRST, bool KEEP, bool IN = false, int CLM = 0, bool U = false>
+__device__ __forceinline__ RatioOps<R> bounds_body(const Prob<R>& P, int i, int j, int k) {
   const Geo& g = P.g;
   const Arr<R>& X = P.xant;
   const R x = X.ld(i, j, k);
   P.q.at(i, j, k) = (P.rho || U) ? x : div1(x, P.rhr.ld(i, j, k));  // x/1 == x for the density step
-  if (!NONOS) return;
+  if (!NONOS) return {};
   const bool lo = IN || g.bz || k > 1, hi = IN || g.bz || k < g.lp;
   R ma, mi;
   if (FIRST) {
@@ -377,10 +393,34 @@ __device__ __forceinline__ void bounds_body(const Prob<R>& P, int i, int j, int 
   const R e2 = fy<R, false, IN>(g, F2, i, j + 1, k), w2 = fy<R, false, IN>(g, F2, i, j, k);
   const R e3 = fz<R, false, IN>(g, F3, i, j, k + 1), w3 = fz<R, false, IN>(g, F3, i, j, k);
   const R hc = U ? R(1) : P.h.ld(i, j, k);
-  const R np_ = U ? ma - x : (ma - x) * hc, dp = pn(e1) + pp(w1) + pn(e2) + pp(w2) + pn(e3) + pp(w3) + ep;
-  const R nn = U ? x - mi : (x - mi) * hc, dn = pp(e1) + pn(w1) + pp(e2) + pn(w2) + pp(e3) + pn(w3) + ep;
-  P.cp.at(i, j, k) = CL ? lim_ratio(np_, dp) : np_ / dp;
-  P.cn.at(i, j, k) = CL ? lim_ratio(nn, dn) : nn / dn;
+  const R np_ = U ? ma - x : (ma - x) * hc, nn = U ? x - mi : (x - mi) * hc;
+  R dp, dn;
+  if constexpr (sizeof(R) == 8) {
+    // dp = pn(e1)+pp(w1)+pn(e2)+pp(w2)+pn(e3)+pp(w3)+ep and dn, its mirror,
+    // left to right.  Each flux f is nonzero in at most one of the two sums,
+    // as |f|, and adding +0 to a sum of non-negative terms changes no bit, so
+    // each |f| is added to its own sum only, in the same order: 6 FP64 adds
+    // instead of 12.
+    dp = R(0);
+    dn = R(0);
+    const R f[6] = {e1, w1, e2, w2, e3, w3};
+#pragma unroll
+    for (int t = 0; t < 6; t++) {
+      const bool to_p = (t & 1) ? !sgn(f[t]) : sgn(f[t]);  // e: pn into dp; w: pp into dp
+      const R a = (to_p ? dp : dn) + fabs(f[t]);
+      dp = to_p ? a : dp;
+      dn = to_p ? dn : a;
+    }
+    dp = dp + ep;
+    dn = dn + ep;
+  } else {
+    dp = pn(e1) + pp(w1) + pn(e2) + pp(w2) + pn(e3) + pp(w3) + ep;
+    dn = pp(e1) + pn(w1) + pp(e2) + pn(w2) + pp(e3) + pn(w3) + ep;
+  }
+  if (CLM == 2) return {np_, dp, nn, dn};
+  P.cp.at(i, j, k) = CLM ? lim_ratio(np_, dp) : np_ / dp;
+  P.cn.at(i, j, k) = CLM ? lim_ratio(nn, dn) : nn / dn;
+  return {};
 }
 
 // ---- limited antidiffusive velocities and fluxes --------------------------

@@ -501,7 +501,7 @@ int mpdata_ws_stage_times(void* ws, int nstages, double* total_ms, long long* la
 const char* mpdata_stage_name(int stage) {
   static const char* names[NSTAGE] = {"upwind", "pseudo_velocity", "limiter_bounds", "limited_flux",
                                       "corrective_update", "copy", "predictor_level",
-                                      "predictor_cgrid", "density_outputs"};
+                                      "predictor_cgrid", "density_outputs", "pair_sums"};
   return (stage >= 0 && stage < NSTAGE) ? names[stage] : "";
 }
 

@@ -68,9 +68,27 @@ __device__ __forceinline__ double from_okey(long long k) {
 __device__ __forceinline__ bool sgn(double y) { return __double2hiint(y) < 0; }
 __device__ __forceinline__ bool sgn(float y) { return __float_as_int(y) < 0; }
 
+// -y and y != 0 as integer operations on the two 32-bit halves.  Written in
+// PTX so that the compiler cannot turn them back into an FP64 negation (a
+// DADD) or an FP64 compare (a DSETP), both of which issue on the FP64 pipe.
+// IEEE negation is exactly a flip of the sign bit.
+__device__ __forceinline__ double neg_bits(double y) {
+  double r;
+  asm("{\n\t.reg .b32 lo, hi;\n\tmov.b64 {lo, hi}, %1;\n\txor.b32 hi, hi, 0x80000000;\n\t"
+      "mov.b64 %0, {lo, hi};\n\t}"
+      : "=d"(r)
+      : "d"(y));
+  return r;
+}
+__device__ __forceinline__ bool nonzero_bits(double y) {
+  unsigned lo, hi;
+  asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(hi) : "d"(y));
+  return ((hi << 1) | lo) != 0u;
+}
+
 // pp(y) = max(0,y), pn(y) = -min(0,y)  (mpdataoperators.inc:50-59)
 __device__ __forceinline__ double pp(double y) { return sgn(y) ? 0.0 : y; }
-__device__ __forceinline__ double pn(double y) { return sgn(y) ? -y : 0.0; }
+__device__ __forceinline__ double pn(double y) { return sgn(y) ? neg_bits(y) : 0.0; }
 __device__ __forceinline__ float pp(float y) { return y > 0.f ? y : 0.f; }
 __device__ __forceinline__ float pn(float y) { return y < 0.f ? -y : 0.f; }
 __device__ __forceinline__ double mx2(double a, double b) { return okey(a) > okey(b) ? a : b; }
@@ -124,11 +142,11 @@ __device__ __forceinline__ float rcp1(float r) { return 1.0f / r; }
 // NaN operands (n above +Inf, d not a positive finite number) divide as usual.
 // The test runs on the integer pipe: for non-negative numbers the bit
 // patterns order as the values do.
-__device__ __forceinline__ double lim_ratio(double n, double d) {
+__device__ __forceinline__ bool ratio_ge1(double n, double d) {
   const long long nb = __double_as_longlong(n), db = __double_as_longlong(d), inf = 0x7FF0000000000000LL;
-  if (db > 0 && db < inf && nb >= db && nb <= inf) return 1.0;
-  return div_call(n, d);
+  return db > 0 && db < inf && nb >= db && nb <= inf;
 }
+__device__ __forceinline__ double lim_ratio(double n, double d) { return ratio_ge1(n, d) ? 1.0 : div_call(n, d); }
 __device__ __forceinline__ float lim_ratio(float n, float d) {
   const int nb = __float_as_int(n), db = __float_as_int(d), inf = 0x7F800000;
   if (db > 0 && db < inf && nb >= db && nb <= inf) return 1.0f;
@@ -146,7 +164,7 @@ __device__ __forceinline__ float donor(float y1, float y2, float a) { return pp(
 // FP64 pipe (the bound of every FP64 stage) to the multiplication.
 __device__ __forceinline__ double donor(double y1, double y2, double a) {
   const double m = a * (__double_as_longlong(a) > 0 ? y1 : y2);
-  if ((__double_as_longlong(m) << 1) != 0) return m;
+  if (nonzero_bits(m)) return m;
   return (sgn(y1) && !sgn(y2)) ? -0.0 : 0.0;
 }
 template <class R> __device__ __forceinline__ R vdyf(R x1, R x2, R a, R rinv) {

@@ -2,7 +2,11 @@
 allocations, for profilers (ncu) and quick timing.
 
   python -m advectionhpctester_gb300.profile_case --grid 384 384 64 --steps 2 \
-      [--precision 64|32] [--std] [--iord 3] [--bc periodic|reference]
+      [--precision 64|32] [--std] [--iord 3] [--bc periodic|reference] \
+      [--workload random|deformational]
+
+random: seeded random fields with h, rhr in [0.8, 1.2]; deformational: the
+periodic deformational flow with unit densities (the benchmark's fields).
 
 Prints the CUDA-event time per step and the per-stage times.
 """
@@ -21,6 +25,7 @@ def main(argv=None):
     ap.add_argument("--std", action="store_true", help="standard form (default: gauge)")
     ap.add_argument("--iord", type=int, default=3)
     ap.add_argument("--bc", choices=["periodic", "reference"], default="periodic")
+    ap.add_argument("--workload", choices=["random", "deformational"], default="random")
     a = ap.parse_args(argv)
 
     import torch
@@ -33,7 +38,12 @@ def main(argv=None):
     nx, ny, nz = a.grid
     ibc = (1, 1, 1) if a.bc == "periodic" else (0, 0, 0)
     dnp = np.float64 if a.precision == 64 else np.float32
-    f = W.random_fields(nx, ny, nz, ibc=ibc, seed=1, courant=0.25, dtype=dnp)
+    if a.workload == "deformational":
+        if a.bc != "periodic":
+            ap.error("the deformational workload is periodic")
+        f = W.deformational(nx, ny, nz, dtype=dnp)
+    else:
+        f = W.random_fields(nx, ny, nz, ibc=ibc, seed=1, courant=0.25, dtype=dnp)
     d = {k: M.fortran_device(getattr(f, k)) for k in ("x", "u1", "u2", "u3", "h", "rhr", "bcx", "bcy")}
     del f
     ws = M.Workspace(nx, ny, nz, 1, *ibc, iord=a.iord, nonos=1, gauge=0 if a.std else 1,
@@ -51,7 +61,8 @@ def main(argv=None):
     torch.cuda.synchronize()
     st = ws.stage_times()
     ms = e0.elapsed_time(e1) / a.steps
-    print(json.dumps({"grid": a.grid, "precision": a.precision, "form": "std" if a.std else "gauge",
+    print(json.dumps({"grid": a.grid, "workload": a.workload, "precision": a.precision,
+                      "form": "std" if a.std else "gauge",
                       "iord": a.iord, "bc": a.bc, "ms_per_step": round(ms, 4),
                       "gcell_steps_per_s": round(nx * ny * nz / (ms * 1e-3) / 1e9, 4),
                       "stages_ms": {k: round(v[0] / a.steps, 4) for k, v in st.items() if v[1]}}))

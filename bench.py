@@ -38,21 +38,27 @@ UNIT = "Gcell-steps/s"
 
 # Algorithmic (compulsory) device bytes per cell per launch of each stage:
 # every array a kernel must read or write, once.  Units: elements per cell.
-#   upwind   r psi u1 u2 u3 h rhr          w xant hinv            8
-#   pseudo   r xant a1 a2 a3 h             w v1 v2 v3 (+fn1..3)   8 (11 std)
-#   bounds   r xant psi|mx,mn h rhr F1..3  w cp cn q (+mx mn)     9..13
-#   limit    r xant v1..3 cp cn (+q)       w w1..3 (+f1..3)       9 (13 std)
-#   update   r q rhr h|hinv F1..3          w out                  7
-#   predictor level  r o0 x3 o2 x3 h  w o1 x3                    10
-#   predictor cgrid  r o1 x3 o0 x3 h  w u1..3 o2 x3              13
-def stage_elems(stage, gauge, iord):
+#   upwind   r psi u1..3 h rhr                w xant hinv hmx hmy hmz   11
+#   pairs    r xant                           w Sx Sy Sz                 4 (FP64 gauge only)
+#   pseudo   r xant a1..3 hm1..3 (+Sx Sy Sz)  w v1..3 (+f1..3 std)      10, 13 FP64 gauge (13 std)
+#   bounds   r xant psi|mx,mn h rhr F1..3     w q cp cn (+mx mn)        10..13
+#   limit    r cp cn v1..3 (+xant q)          w w1..3 (+f1..3)          8 (13 std)
+#   update   r q rhr h|hinv F1..3             w out                     7
+#   predictor level  r o0 x3 o2 x3 h  w o1 x3                            10
+#   predictor cgrid  r o1 x3 o0 x3 h  w u1..3 o2 x3                      13
+def stage_elems(stage, gauge, iord, precision=64):
     """Compulsory fields read + written per cell by one launch of a stage
     (interior cells, each field once; ncu DRAM bytes agree within 4%)."""
     keep = iord > 2
+    pairs = gauge and precision == 64                 # FP64 gauge: pair sums precomputed
     if stage == "upwind":
         return 11.0                                   # psi,u1..3,h,rhr -> xant,1/h,hmx,hmy,hmz
+    if stage == "pair_sums":
+        return 4.0                                    # xant -> Sx,Sy,Sz
     if stage == "pseudo_velocity":
-        return 10.0 if gauge else 13.0                # xant,a1..3,hm1..3 -> v1..3 (+f1..3 std)
+        if not gauge:
+            return 13.0                               # xant,a1..3,hm1..3 -> v1..3,f1..3
+        return 13.0 if pairs else 10.0                # xant,a1..3,hm1..3 (+Sx,Sy,Sz) -> v1..3
     if stage == "limiter_bounds":
         first = 10.0 + (2.0 if keep else 0.0)         # xant,rhr,psi,F1..3,h -> q,cp,cn (+mx,mn kept)
         later = 13.0                                  # xant,rhr,mx,mn,F1..3,h -> q,mx,mn,cp,cn
@@ -297,7 +303,7 @@ def run_ours(args, ws, rank, local):
     dom = max(stages.items(), key=lambda kv: kv[1][0])
     name, (tot_ms, nl) = dom
     avg_ms = tot_ms / max(nl, 1)
-    alg_bytes = stage_elems(name, True, 3) * elem * cells
+    alg_bytes = stage_elems(name, True, 3, args.precision) * elem * cells
     achieved = alg_bytes / (avg_ms * 1e-3) / 1e9
     ncu = NCU_PSEUDO[args.precision] if name == "pseudo_velocity" else None
     traffic = int(ncu["dram_bytes_per_cell"] * cells) if ncu else None
@@ -319,7 +325,8 @@ def run_ours(args, ws, rank, local):
     stage_json = {k: {"ms_total": round(v[0], 3), "launches": int(v[1]),
                       "share": round(v[0] / max(sum(t for t, _ in stages.values()), 1e-9), 4)}
                   for k, v in stages.items() if v[1]}
-    step_alg = sum(stage_elems(k, True, 3) * elem * cells * v[1] for k, v in stages.items()) / args.steps
+    step_alg = sum(stage_elems(k, True, 3, args.precision) * elem * cells * v[1]
+                   for k, v in stages.items()) / args.steps
     result = dict(metric=METRIC, value=round(value, 4), unit=UNIT, n_gpus=ws, steps=args.steps,
                   warmup=args.warmup, ms_per_step=round(ms_max / args.steps, 4), higher_is_better=True,
                   scaling="weak", vs_baseline=None, dtype="f64" if args.precision == 64 else "f32",
