@@ -33,9 +33,14 @@
 namespace mpdata {
 
 // ---- adjoints of the read maps --------------------------------------------
+// Adding a zero changes no accumulator (they start at +0), so zero
+// contributions, frequent where the limiter is inactive, skip the atomic; the
+// test is an integer one on the FP64 bit pattern.
+__device__ __forceinline__ bool nonzero(double v) { return nonzero_bits(v); }
+__device__ __forceinline__ bool nonzero(float v) { return v != 0.0f; }
 template <class R>
 __device__ __forceinline__ void addat(const Arr<R>& A, int i, int j, int k, R v) {
-  atomicAdd(&A.at(i, j, k), v);
+  if (nonzero(v)) atomicAdd(&A.at(i, j, k), v);
 }
 // xr(): the field with the xant halo rule (reflection or wrap).  IN: the
 // index is inside the grid (a cell in [2, n-1] reading +-1), the map is the
@@ -78,9 +83,10 @@ __device__ __forceinline__ void fz_add(const Geo& g, const Arr<R>& A, int i, int
   addat(A, i, j, f, v);
 }
 
-// derivative conventions of the branches (forward values decide)
-template <class R> __device__ __forceinline__ R dpp(R y) { return sgn(y) ? R(0) : (y > R(0) ? R(1) : R(0)); }
-template <class R> __device__ __forceinline__ R dpn(R y) { return y < R(0) ? R(-1) : R(0); }
+// derivative conventions of the branches (forward values decide); the
+// tests are integer ones on the sign bit and the magnitude bits
+template <class R> __device__ __forceinline__ R dpp(R y) { return (!sgn(y) && nonzero(y)) ? R(1) : R(0); }
+template <class R> __device__ __forceinline__ R dpn(R y) { return (sgn(y) && nonzero(y)) ? R(-1) : R(0); }
 template <class R> __device__ __forceinline__ R dabs(R y) { return sgn(y) ? R(-1) : R(1); }
 
 
@@ -130,12 +136,19 @@ __global__ void __launch_bounds__(128) ka_update(const Prob<R> P, const AdjArr<R
 
 // ---- limiter: w = pp(v)*min3(cp(c),cn(c-1)) - pn(v)*min3(cp(c-1),cn(c)) -------
 // min3(a,b) = mn2(mn2(1,a),b): b is taken when b <= t, else a when a <= 1.
+// The ratios are non-negative (or RATIO_CAP), so for doubles their bit
+// patterns order as their values and the compares run on the integer pipe.
+__device__ __forceinline__ bool lt_nonneg(double a, double b) {
+  return __double_as_longlong(a) < __double_as_longlong(b);
+}
+__device__ __forceinline__ bool lt_nonneg(float a, float b) { return a < b; }
 template <class R>
 __device__ __forceinline__ void min3_adj(R a, R b, R lam, const Arr<R>& La, int ia, int ja, int ka,
                                          const Arr<R>& Lb, int ib, int jb, int kb) {
-  const R t = R(1) < a ? R(1) : a;
-  if (!(t < b)) { addat(Lb, ib, jb, kb, lam); return; }
-  if (!(R(1) < a)) addat(La, ia, ja, ka, lam);
+  const bool a_over = lt_nonneg(R(1), a);
+  const R t = a_over ? R(1) : a;
+  if (!lt_nonneg(t, b)) { addat(Lb, ib, jb, kb, lam); return; }
+  if (!a_over) addat(La, ia, ja, ka, lam);
 }
 
 template <class R, bool NONOS, bool IN>
@@ -150,10 +163,13 @@ __device__ __forceinline__ void ka_limit_cell(const Prob<R>& P, const AdjArr<R>&
       addat(LV, i, j, k, lw);                                                              \
     } else {                                                                               \
       const R cpm = P.cp.ld(IM, JM, KM), cnm = P.cn.ld(IM, JM, KM);                        \
-      const R a1 = min3(cpc, cnm), a2 = min3(cpm, cnc);                                    \
-      addat(LV, i, j, k, lw * (dpp(v) * a1 - dpn(v) * a2));                                \
-      min3_adj(cpc, cnm, lw * pp(v), A.lcp, i, j, k, A.lcn, IM, JM, KM);                    \
-      min3_adj(cpm, cnc, -lw * pn(v), A.lcp, IM, JM, KM, A.lcn, i, j, k);                   \
+      /* dw/dv = a1 (v > 0), a2 (v < 0), 0; dw/da1 = pp(v), dw/da2 = -pn(v): */          \
+      /* one of them is v, the other zero */                                              \
+      const bool vz = !nonzero(v), vn = sgn(v);                                             \
+      const R m = lw * v;                                                                   \
+      if (!vz) addat(LV, i, j, k, lw * (vn ? min3(cpm, cnc) : min3(cpc, cnm)));             \
+      if (!vz && !vn) min3_adj(cpc, cnm, m, A.lcp, i, j, k, A.lcn, IM, JM, KM);             \
+      if (!vz && vn) min3_adj(cpm, cnc, m, A.lcp, IM, JM, KM, A.lcn, i, j, k);              \
     }                                                                                      \
   }
   if (IN || g.bx || i > 1) LIMIT_FACE(P.v1, A.lv1, A.lw1, (IN ? i - 1 : wrapi(i - 1, g.np)), j, k)
@@ -171,13 +187,30 @@ __global__ void __launch_bounds__(128) ka_limit(const Prob<R> P, const AdjArr<R>
 // ---- bounds: cp = (mx-x)h/Dp, cn = (x-mn)h/Dn -------------------------------
 // The extrema are re-folded in the oracle's order (mx2/mn2 trees) so ties go
 // to the same operand: element ids 0..6 are x_in, 7..13 xant.
+// FP64 values compare through their order keys on the integer pipe (equal
+// values tie the same way; -0 orders below +0, as in the forward's folds).
+__device__ __forceinline__ long long ord_key(double v) { return okey(v); }
+__device__ __forceinline__ float ord_key(float v) { return v; }
 template <class R>
 struct Arg {
   R v;
+  decltype(ord_key(R(0))) key;
   int id;
 };
-template <class R> __device__ __forceinline__ Arg<R> amax(Arg<R> a, Arg<R> b) { return a.v > b.v ? a : b; }
-template <class R> __device__ __forceinline__ Arg<R> amin(Arg<R> a, Arg<R> b) { return a.v < b.v ? a : b; }
+template <class R> __device__ __forceinline__ Arg<R> mkarg(R v, int id) { return Arg<R>{v, ord_key(v), id}; }
+template <class R> __device__ __forceinline__ Arg<R> amax(Arg<R> a, Arg<R> b) { return a.key > b.key ? a : b; }
+template <class R> __device__ __forceinline__ Arg<R> amin(Arg<R> a, Arg<R> b) { return a.key < b.key ? a : b; }
+
+// Adjoint of the bounds' denominators onto one flux f: Dp holds pn(f) and
+// Dn pp(f) for an outflow face (e), the reverse for an inflow face (w); a
+// zero flux contributes to neither.
+template <class R>
+__device__ __forceinline__ R lflux(R f, R lDp, R lDn, bool inflow) {
+  if (!nonzero(f)) return R(0);
+  const bool neg = sgn(f);
+  if (inflow) return neg ? -lDn : lDp;
+  return neg ? -lDp : lDn;
+}
 
 // FIRST: the fold starts from the step input's star (ids 0..6); later passes
 // start from the previous pass's running extrema (id 14).  The current
@@ -204,17 +237,17 @@ __device__ __forceinline__ void ka_bounds_cell(const Prob<R>& P, const AdjArr<R>
   const int cj[15] = {j, j, j, jm, jp, j, j, j, j, j, rj_m, rj_p, j, j, j};
   const int ck[15] = {k, k, k, k, k, km, kp, k, k, k, k, k, km, kp, k};
   Arg<R> e[14];
-  for (int n = 7; n < 14; n++) e[n] = Arg<R>{X.ld(ci[n], cj[n], ck[n]), n};
+  for (int n = 7; n < 14; n++) e[n] = mkarg(X.ld(ci[n], cj[n], ck[n]), n);
   Arg<R> ma, mi;
   if (FIRST) {
-    for (int n = 0; n < 7; n++) e[n] = Arg<R>{xin.ld(ci[n], cj[n], ck[n]), n};
+    for (int n = 0; n < 7; n++) e[n] = mkarg(xin.ld(ci[n], cj[n], ck[n]), n);
     ma = amax(amax(amax(e[0], e[1]), amax(e[2], e[3])), e[4]);
     mi = amin(amin(amin(e[0], e[1]), amin(e[2], e[3])), e[4]);
     if (lo) { ma = amax(ma, e[5]); mi = amin(mi, e[5]); }
     if (hi) { ma = amax(ma, e[6]); mi = amin(mi, e[6]); }
   } else {
-    ma = Arg<R>{A.mxp.ld(i, j, k), 14};
-    mi = Arg<R>{A.mnp.ld(i, j, k), 14};
+    ma = mkarg(A.mxp.ld(i, j, k), 14);
+    mi = mkarg(A.mnp.ld(i, j, k), 14);
   }
   ma = amax(amax(amax(ma, e[7]), amax(e[8], e[9])), amax(e[10], e[11]));
   mi = amin(amin(amin(mi, e[7]), amin(e[8], e[9])), amin(e[10], e[11]));
@@ -232,27 +265,34 @@ __device__ __forceinline__ void ka_bounds_cell(const Prob<R>& P, const AdjArr<R>
   const R e1 = fx<R, false, IN>(g, F1, i + 1, j, k), w1 = fx<R, false, IN>(g, F1, i, j, k);
   const R e2 = fy<R, false, IN>(g, F2, i, j + 1, k), w2 = fy<R, false, IN>(g, F2, i, j, k);
   const R e3 = fz<R, false, IN>(g, F3, i, j, k + 1), w3 = fz<R, false, IN>(g, F3, i, j, k);
-  const R ep = Eps<R>::v;
-  const R Dp = pn(e1) + pp(w1) + pn(e2) + pp(w2) + pn(e3) + pp(w3) + ep;
-  const R Dn = pp(e1) + pn(w1) + pp(e2) + pn(w2) + pp(e3) + pn(w3) + ep;
-  const R cpv = (ma.v - x) * hc / Dp, cnv = (x - mi.v) * hc / Dn;
-  const R lnum_p = lcp * hc / Dp, lnum_n = lcn * hc / Dn;
-  // d cp/d mx, d cn/d mn (plus the carried adjoints of the extrema), d/d x
+  // d cp/d mx, d cn/d mn (plus the carried adjoints of the extrema), d/d x,
+  // and d/dD = -c/D.  cp = num/Dp: lnum = lcp*h/Dp, lDp = -lnum*(mx-x)/Dp,
+  // with one reciprocal per denominator; both vanish where the limiter did
+  // not select the ratio (lcp = 0), as they mostly do.
+  R lnum_p = R(0), lnum_n = R(0), lDp = R(0), lDn = R(0);
+  if (nonzero(lcp) || nonzero(lcn)) {
+    const R ep = Eps<R>::v;
+    const R Dp = pn(e1) + pp(w1) + pn(e2) + pp(w2) + pn(e3) + pp(w3) + ep;
+    const R Dn = pp(e1) + pn(w1) + pp(e2) + pn(w2) + pp(e3) + pn(w3) + ep;
+    const R rp = R(1) / Dp, rn = R(1) / Dn;
+    lnum_p = lcp * hc * rp;
+    lnum_n = lcn * hc * rn;
+    lDp = -(lnum_p * (ma.v - x)) * rp;
+    lDn = -(lnum_n * (x - mi.v)) * rn;
+  }
   const R lma = lnum_p + A.lmx.ld(i, j, k), lmi = -lnum_n + A.lmn.ld(i, j, k);
   if (ma.id == 14) addat(A.lmxp, i, j, k, lma);
   else addat(ma.id < 7 ? A.lx : A.lxant, ci[ma.id], cj[ma.id], ck[ma.id], lma);
   if (mi.id == 14) addat(A.lmnp, i, j, k, lmi);
   else addat(mi.id < 7 ? A.lx : A.lxant, ci[mi.id], cj[mi.id], ck[mi.id], lmi);
   addat(A.lxant, i, j, k, lnum_n - lnum_p);
-  // d/dD: -c/D
-  const R lDp = -lcp * cpv / Dp, lDn = -lcn * cnv / Dn;
   // Dp = pn(e)+pp(w)+..., Dn = pp(e)+pn(w)+... over the six faces
-  fx_add<R, false, IN>(g, LF1, i + 1, j, k, lDp * dpn(e1) + lDn * dpp(e1));
-  fx_add<R, false, IN>(g, LF1, i, j, k, lDp * dpp(w1) + lDn * dpn(w1));
-  fy_add<R, false, IN>(g, LF2, i, j + 1, k, lDp * dpn(e2) + lDn * dpp(e2));
-  fy_add<R, false, IN>(g, LF2, i, j, k, lDp * dpp(w2) + lDn * dpn(w2));
-  fz_add<R, false, IN>(g, LF3, i, j, k + 1, lDp * dpn(e3) + lDn * dpp(e3));
-  fz_add<R, false, IN>(g, LF3, i, j, k, lDp * dpp(w3) + lDn * dpn(w3));
+  fx_add<R, false, IN>(g, LF1, i + 1, j, k, lflux(e1, lDp, lDn, false));
+  fx_add<R, false, IN>(g, LF1, i, j, k, lflux(w1, lDp, lDn, true));
+  fy_add<R, false, IN>(g, LF2, i, j + 1, k, lflux(e2, lDp, lDn, false));
+  fy_add<R, false, IN>(g, LF2, i, j, k, lflux(w2, lDp, lDn, true));
+  fz_add<R, false, IN>(g, LF3, i, j, k + 1, lflux(e3, lDp, lDn, false));
+  fz_add<R, false, IN>(g, LF3, i, j, k, lflux(w3, lDp, lDn, true));
 }
 template <class R, bool FIRST, bool STD>
 __global__ void __launch_bounds__(128) ka_bounds(const Prob<R> P, const AdjArr<R> A) {
@@ -266,7 +306,26 @@ __global__ void __launch_bounds__(128) ka_bounds(const Prob<R> P, const AdjArr<R
 // AIN: a = the caller's Courant numbers (gradient into gu); otherwise a = the
 // previous pass's limited velocities, read with the wall rule (gradient into
 // that pass's lambda_w).
-template <class R, bool AIN, bool IN>
+template <class R> __device__ __forceinline__ R negv(R x) { return -x; }
+template <> __device__ __forceinline__ double negv<double>(double x) { return neg_bits(x); }
+
+// The adjoint of one face's v = K*(xr-xl) - 0.03125*a*hm*cr4, with
+// K = (|a| - a*a*hm)/2 and cr4 = S*D [+ S'*D'], the 4-face sums S times the
+// unscaled rat4 differences D (4*cr of the forward's form).  U: hm == 1.
+template <class R, bool U>
+struct FaceAdj {
+  R la, lK, lcr4;
+  __device__ __forceinline__ FaceAdj(R lv, R a, R hm, R xl, R xrr, R cr4) {
+    const R K = (fabs(a) - hmul<U>(a * a, hm)) * R(0.5);
+    la = lv * ((dabs(a) - hmul<U>(R(2) * a, hm)) * (xrr - xl) * R(0.5) - hmul<U>(R(0.03125) * cr4, hm));
+    lK = lv * K;
+    lcr4 = negv(lv * hmul<U>(R(0.03125) * a, hm));
+  }
+};
+
+// U: the warp's face densities are all exactly 1.  PS: the pair sums of the
+// pass's input field are in cp/cn/q (kf_pairs), as in the forward stage.
+template <class R, bool AIN, bool IN, bool U = false, bool PS = false>
 __device__ __forceinline__ void ka_pseudo_cell(const Prob<R>& P, const AdjArr<R>& A, int i, int j, int k) {
   const Geo& g = P.g;
   const Arr<R>& X = P.xant;
@@ -279,114 +338,134 @@ __device__ __forceinline__ void ka_pseudo_cell(const Prob<R>& P, const AdjArr<R>
   // x faces
   if (IN || g.bx || i > 1) {
     const R lv = A.lv1.ld(i, j, k);
-    const R hm = P.hmx.ld(i, j, k), a = fx<R, AIN, IN>(g, U1, i, j, k);
+    const R hm = U ? R(1) : P.hmx.ld(i, j, k), a = fx<R, AIN, IN>(g, U1, i, j, k);
     const R xl = XX(i - 1, j, k), xrr = XX(i, j, k);
     const R S2 = fy<R, AIN, IN>(g, U2, i - 1, j, k) + fy<R, AIN, IN>(g, U2, i - 1, j + 1, k) +
                  fy<R, AIN, IN>(g, U2, i, j + 1, k) + fy<R, AIN, IN>(g, U2, i, j, k);
-    const R R2 = rat4(XX(i - 1, j - 1, k), XX(i, j - 1, k), XX(i - 1, j + 1, k), XX(i, j + 1, k));
-    R cr = S2 * R2, S3 = R(0), R3 = R(0);
+    const R D2 = PS ? P.cp.ld(i, j + 1, k) - P.cp.ld(i, j - 1, k)
+                    : dif4(XX(i - 1, j - 1, k), XX(i, j - 1, k), XX(i - 1, j + 1, k), XX(i, j + 1, k));
+    R cr4 = S2 * D2, S3 = R(0), D3 = R(0);
     if (zt) {
       S3 = fz<R, AIN, IN>(g, U3, i - 1, j, k) + fz<R, AIN, IN>(g, U3, i - 1, j, k + 1) +
            fz<R, AIN, IN>(g, U3, i, j, k + 1) + fz<R, AIN, IN>(g, U3, i, j, k);
-      R3 = rat4(XX(i - 1, j, k - 1), XX(i, j, k - 1), XX(i - 1, j, k + 1), XX(i, j, k + 1));
-      cr = cr + S3 * R3;
+      D3 = PS ? P.cp.ld(i, j, k + 1) - P.cp.ld(i, j, k - 1)
+              : dif4(XX(i - 1, j, k - 1), XX(i, j, k - 1), XX(i - 1, j, k + 1), XX(i, j, k + 1));
+      cr4 = cr4 + S3 * D3;
     }
-    const R K = (fabs(a) - a * a * hm) * R(0.5);
-    const R la = lv * ((dabs(a) - R(2) * a * hm) * (xrr - xl) * R(0.5) - R(0.125) * hm * cr);
-    fx_add<R, AIN, IN>(g, A.la1, i, j, k, la);
-    LX(i, j, k, lv * K);
-    LX(i - 1, j, k, -lv * K);
-    const R lcr = -lv * R(0.125) * a * hm;
-    const R lS2 = lcr * R2, lR2 = lcr * S2 * R(0.25);
+    const FaceAdj<R, U> f(lv, a, hm, xl, xrr, cr4);
+    fx_add<R, AIN, IN>(g, A.la1, i, j, k, f.la);
+    LX(i, j, k, f.lK);
+    LX(i - 1, j, k, negv(f.lK));
+    const R lS2 = f.lcr4 * D2, lR2 = f.lcr4 * S2, nR2 = negv(lR2);
     fy_add<R, AIN, IN>(g, A.la2, i - 1, j, k, lS2);
     fy_add<R, AIN, IN>(g, A.la2, i - 1, j + 1, k, lS2);
     fy_add<R, AIN, IN>(g, A.la2, i, j + 1, k, lS2);
     fy_add<R, AIN, IN>(g, A.la2, i, j, k, lS2);
-    LX(i, j + 1, k, lR2); LX(i - 1, j + 1, k, lR2); LX(i, j - 1, k, -lR2); LX(i - 1, j - 1, k, -lR2);
+    LX(i, j + 1, k, lR2); LX(i - 1, j + 1, k, lR2); LX(i, j - 1, k, nR2); LX(i - 1, j - 1, k, nR2);
     if (zt) {
-      const R lS3 = lcr * R3, lR3 = lcr * S3 * R(0.25);
+      const R lS3 = f.lcr4 * D3, lR3 = f.lcr4 * S3, nR3 = negv(lR3);
       fz_add<R, AIN, IN>(g, A.la3, i - 1, j, k, lS3);
       fz_add<R, AIN, IN>(g, A.la3, i - 1, j, k + 1, lS3);
       fz_add<R, AIN, IN>(g, A.la3, i, j, k + 1, lS3);
       fz_add<R, AIN, IN>(g, A.la3, i, j, k, lS3);
-      LX(i, j, k + 1, lR3); LX(i - 1, j, k + 1, lR3); LX(i, j, k - 1, -lR3); LX(i - 1, j, k - 1, -lR3);
+      LX(i, j, k + 1, lR3); LX(i - 1, j, k + 1, lR3); LX(i, j, k - 1, nR3); LX(i - 1, j, k - 1, nR3);
     }
   }
   // y faces
   if (IN || g.by || j > 1) {
     const R lv = A.lv2.ld(i, j, k);
-    const R hm = P.hmy.ld(i, j, k), a = fy<R, AIN, IN>(g, U2, i, j, k);
+    const R hm = U ? R(1) : P.hmy.ld(i, j, k), a = fy<R, AIN, IN>(g, U2, i, j, k);
     const R xl = XX(i, j - 1, k), xrr = XX(i, j, k);
     const R S1 = fx<R, AIN, IN>(g, U1, i, j - 1, k) + fx<R, AIN, IN>(g, U1, i, j, k) +
                  fx<R, AIN, IN>(g, U1, i + 1, j, k) + fx<R, AIN, IN>(g, U1, i + 1, j - 1, k);
-    const R R1 = rat4(XX(i - 1, j - 1, k), XX(i - 1, j, k), XX(i + 1, j - 1, k), XX(i + 1, j, k));
-    R cr = S1 * R1, S3 = R(0), R3 = R(0);
+    const R D1 = PS ? P.cn.ld(i + 1, j, k) - P.cn.ld(i - 1, j, k)
+                    : dif4(XX(i - 1, j - 1, k), XX(i - 1, j, k), XX(i + 1, j - 1, k), XX(i + 1, j, k));
+    R cr4 = S1 * D1, S3 = R(0), D3 = R(0);
     if (zt) {
       S3 = fz<R, AIN, IN>(g, U3, i, j - 1, k) + fz<R, AIN, IN>(g, U3, i, j, k) +
            fz<R, AIN, IN>(g, U3, i, j, k + 1) + fz<R, AIN, IN>(g, U3, i, j - 1, k + 1);
-      R3 = rat4(XX(i, j - 1, k - 1), XX(i, j, k - 1), XX(i, j - 1, k + 1), XX(i, j, k + 1));
-      cr = cr + S3 * R3;
+      D3 = PS ? P.cn.ld(i, j, k + 1) - P.cn.ld(i, j, k - 1)
+              : dif4(XX(i, j - 1, k - 1), XX(i, j, k - 1), XX(i, j - 1, k + 1), XX(i, j, k + 1));
+      cr4 = cr4 + S3 * D3;
     }
-    const R K = (fabs(a) - a * a * hm) * R(0.5);
-    const R la = lv * ((dabs(a) - R(2) * a * hm) * (xrr - xl) * R(0.5) - R(0.125) * hm * cr);
-    fy_add<R, AIN, IN>(g, A.la2, i, j, k, la);
-    LX(i, j, k, lv * K);
-    LX(i, j - 1, k, -lv * K);
-    const R lcr = -lv * R(0.125) * a * hm;
-    const R lS1 = lcr * R1, lR1 = lcr * S1 * R(0.25);
+    const FaceAdj<R, U> f(lv, a, hm, xl, xrr, cr4);
+    fy_add<R, AIN, IN>(g, A.la2, i, j, k, f.la);
+    LX(i, j, k, f.lK);
+    LX(i, j - 1, k, negv(f.lK));
+    const R lS1 = f.lcr4 * D1, lR1 = f.lcr4 * S1, nR1 = negv(lR1);
     fx_add<R, AIN, IN>(g, A.la1, i, j - 1, k, lS1);
     fx_add<R, AIN, IN>(g, A.la1, i, j, k, lS1);
     fx_add<R, AIN, IN>(g, A.la1, i + 1, j, k, lS1);
     fx_add<R, AIN, IN>(g, A.la1, i + 1, j - 1, k, lS1);
-    LX(i + 1, j, k, lR1); LX(i + 1, j - 1, k, lR1); LX(i - 1, j, k, -lR1); LX(i - 1, j - 1, k, -lR1);
+    LX(i + 1, j, k, lR1); LX(i + 1, j - 1, k, lR1); LX(i - 1, j, k, nR1); LX(i - 1, j - 1, k, nR1);
     if (zt) {
-      const R lS3 = lcr * R3, lR3 = lcr * S3 * R(0.25);
+      const R lS3 = f.lcr4 * D3, lR3 = f.lcr4 * S3, nR3 = negv(lR3);
       fz_add<R, AIN, IN>(g, A.la3, i, j - 1, k, lS3);
       fz_add<R, AIN, IN>(g, A.la3, i, j, k, lS3);
       fz_add<R, AIN, IN>(g, A.la3, i, j, k + 1, lS3);
       fz_add<R, AIN, IN>(g, A.la3, i, j - 1, k + 1, lS3);
-      LX(i, j, k + 1, lR3); LX(i, j - 1, k + 1, lR3); LX(i, j, k - 1, -lR3); LX(i, j - 1, k - 1, -lR3);
+      LX(i, j, k + 1, lR3); LX(i, j - 1, k + 1, lR3); LX(i, j, k - 1, nR3); LX(i, j - 1, k - 1, nR3);
     }
   }
   // z faces
   if (IN || g.bz || k > 1) {
     const R lv = A.lv3.ld(i, j, k);
-    const R hm = P.hmz.ld(i, j, k), a = fz<R, AIN, IN>(g, U3, i, j, k);
+    const R hm = U ? R(1) : P.hmz.ld(i, j, k), a = fz<R, AIN, IN>(g, U3, i, j, k);
     const R xl = XX(i, j, k - 1), xrr = XX(i, j, k);
     const R S1 = fx<R, AIN, IN>(g, U1, i, j, k - 1) + fx<R, AIN, IN>(g, U1, i, j, k) +
                  fx<R, AIN, IN>(g, U1, i + 1, j, k) + fx<R, AIN, IN>(g, U1, i + 1, j, k - 1);
-    const R R1 = rat4(XX(i - 1, j, k - 1), XX(i - 1, j, k), XX(i + 1, j, k - 1), XX(i + 1, j, k));
+    const R D1 = PS ? P.q.ld(i + 1, j, k) - P.q.ld(i - 1, j, k)
+                    : dif4(XX(i - 1, j, k - 1), XX(i - 1, j, k), XX(i + 1, j, k - 1), XX(i + 1, j, k));
     const R S2 = fy<R, AIN, IN>(g, U2, i, j, k - 1) + fy<R, AIN, IN>(g, U2, i, j + 1, k - 1) +
                  fy<R, AIN, IN>(g, U2, i, j + 1, k) + fy<R, AIN, IN>(g, U2, i, j, k);
-    const R R2 = rat4(XX(i, j - 1, k - 1), XX(i, j - 1, k), XX(i, j + 1, k - 1), XX(i, j + 1, k));
-    const R cr = S1 * R1 + S2 * R2;
-    const R K = (fabs(a) - a * a * hm) * R(0.5);
-    const R la = lv * ((dabs(a) - R(2) * a * hm) * (xrr - xl) * R(0.5) - R(0.125) * hm * cr);
-    fz_add<R, AIN, IN>(g, A.la3, i, j, k, la);
-    LX(i, j, k, lv * K);
-    LX(i, j, k - 1, -lv * K);
-    const R lcr = -lv * R(0.125) * a * hm;
-    const R lS1 = lcr * R1, lR1 = lcr * S1 * R(0.25);
+    const R D2 = PS ? P.q.ld(i, j + 1, k) - P.q.ld(i, j - 1, k)
+                    : dif4(XX(i, j - 1, k - 1), XX(i, j - 1, k), XX(i, j + 1, k - 1), XX(i, j + 1, k));
+    const R cr4 = S1 * D1 + S2 * D2;
+    const FaceAdj<R, U> f(lv, a, hm, xl, xrr, cr4);
+    fz_add<R, AIN, IN>(g, A.la3, i, j, k, f.la);
+    LX(i, j, k, f.lK);
+    LX(i, j, k - 1, negv(f.lK));
+    const R lS1 = f.lcr4 * D1, lR1 = f.lcr4 * S1, nR1 = negv(lR1);
     fx_add<R, AIN, IN>(g, A.la1, i, j, k - 1, lS1);
     fx_add<R, AIN, IN>(g, A.la1, i, j, k, lS1);
     fx_add<R, AIN, IN>(g, A.la1, i + 1, j, k, lS1);
     fx_add<R, AIN, IN>(g, A.la1, i + 1, j, k - 1, lS1);
-    LX(i + 1, j, k, lR1); LX(i + 1, j, k - 1, lR1); LX(i - 1, j, k, -lR1); LX(i - 1, j, k - 1, -lR1);
-    const R lS2 = lcr * R2, lR2 = lcr * S2 * R(0.25);
+    LX(i + 1, j, k, lR1); LX(i + 1, j, k - 1, lR1); LX(i - 1, j, k, nR1); LX(i - 1, j, k - 1, nR1);
+    const R lS2 = f.lcr4 * D2, lR2 = f.lcr4 * S2, nR2 = negv(lR2);
     fy_add<R, AIN, IN>(g, A.la2, i, j, k - 1, lS2);
     fy_add<R, AIN, IN>(g, A.la2, i, j + 1, k - 1, lS2);
     fy_add<R, AIN, IN>(g, A.la2, i, j + 1, k, lS2);
     fy_add<R, AIN, IN>(g, A.la2, i, j, k, lS2);
-    LX(i, j + 1, k, lR2); LX(i, j + 1, k - 1, lR2); LX(i, j - 1, k, -lR2); LX(i, j - 1, k - 1, -lR2);
+    LX(i, j + 1, k, lR2); LX(i, j + 1, k - 1, lR2); LX(i, j - 1, k, nR2); LX(i, j - 1, k - 1, nR2);
   }
 #undef XX
 #undef LX
 }
 template <class R, bool AIN>
 __global__ void __launch_bounds__(128) ka_pseudo(const Prob<R> P, const AdjArr<R> A) {
-#define C(IN) ka_pseudo_cell<R, AIN, IN>(P, A, i, j, k)
-  ADISPATCH(C)
-#undef C
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int k = blockIdx.z + 1;
+  const bool win = warp_interior(P.g, i, j, k);
+  if (i > P.g.np || j > P.g.mp) return;
+  if (!win) {
+    ka_pseudo_cell<R, AIN, false>(P, A, i, j, k);
+  } else if constexpr (sizeof(R) == 8) {
+    const bool unit = warp_unit_faces(P, i, j, k);
+    if (P.pairs) {
+      if (unit)
+        ka_pseudo_cell<R, AIN, true, true, true>(P, A, i, j, k);
+      else
+        ka_pseudo_cell<R, AIN, true, false, true>(P, A, i, j, k);
+    } else {
+      if (unit)
+        ka_pseudo_cell<R, AIN, true, true>(P, A, i, j, k);
+      else
+        ka_pseudo_cell<R, AIN, true>(P, A, i, j, k);
+    }
+  } else {
+    ka_pseudo_cell<R, AIN, true>(P, A, i, j, k);
+  }
 }
 
 // ---- standard form (antidiff3d-standard-gpubc.f90) ---------------------------
@@ -603,9 +682,15 @@ __global__ void __launch_bounds__(128) ka_pseudo_std(const Prob<R> P, const AdjA
 template <class R>
 __device__ __forceinline__ void flux_adj(R lF, R xl, R xr_, R u, bool l_var, const Arr<R>& Lx, int li, int lj,
                                          int lk, bool r_var, int ri, int rj, int rk, R* lu_out) {
-  if (l_var) addat(Lx, li, lj, lk, lF * pp(u));
-  if (r_var) addat(Lx, ri, rj, rk, -lF * pn(u));
-  *lu_out = lF * (dpp(u) * xl - dpn(u) * xr_);
+  // F = pp(u)*xl - pn(u)*xr: dF/dxl = pp(u), dF/dxr = -pn(u) (one of them
+  // is u, the other zero), dF/du = dpp(u)*xl - dpn(u)*xr
+  const R m = lF * u;
+  if (sgn(u)) {
+    if (r_var) addat(Lx, ri, rj, rk, m);
+  } else {
+    if (l_var) addat(Lx, li, lj, lk, m);
+  }
+  *lu_out = nonzero(u) ? lF * (sgn(u) ? xr_ : xl) : R(0);
 }
 
 template <class R, bool IN>
@@ -683,23 +768,86 @@ __global__ void __launch_bounds__(128) ka_seed(const Prob<R> P, const Arr<R> psi
   } else {                                                   \
     BODY(false);                                             \
   }
+// As FCELL, with the unit-density instantiation BODY(IN, U) for interior
+// warps whose densities are all exactly 1 (FP64).
+#define FCELL_U(BODY)                                        \
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;  \
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;  \
+  const int k = blockIdx.z + 1;                              \
+  const bool win = warp_interior(P.g, i, j, k);              \
+  if (i > P.g.np || j > P.g.mp) return;                      \
+  if (!win) {                                                \
+    BODY(false, false);                                      \
+  } else if (warp_unit_cell(P, i, j, k)) {                   \
+    BODY(true, true);                                        \
+  } else {                                                   \
+    BODY(true, false);                                       \
+  }
 template <class R>
 __global__ void __launch_bounds__(128) kf_upwind(const Prob<R> P) {
-#define B(IN) upwind_body<R, true, false, IN>(P, i, j, k)
-  FCELL(B)
+#define B(IN, U) upwind_body<R, true, false, IN, U>(P, i, j, k)
+  FCELL_U(B)
 #undef B
 }
+template <class R>
+__global__ void __launch_bounds__(128) kf_pairs(const Prob<R> P) {
+  ACELL
+  (void)g;
+  pairs_body<R>(P, i, j, k);
+}
+// the forward stage's dispatch: unit face densities and pair sums (FP64)
 template <class R, bool AIN>
 __global__ void __launch_bounds__(128) kf_pseudo(const Prob<R> P) {
-#define B(IN) pseudo_body<R, AIN, IN>(P, i, j, k)
-  FCELL(B)
-#undef B
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int k = blockIdx.z + 1;
+  const bool win = warp_interior(P.g, i, j, k);
+  if (i > P.g.np || j > P.g.mp) return;
+  if (!win) {
+    pseudo_body<R, AIN, false>(P, i, j, k);
+  } else if constexpr (sizeof(R) == 8) {
+    const bool unit = warp_unit_faces(P, i, j, k);
+    if (P.pairs) {
+      if (unit)
+        pseudo_body<R, AIN, true, true, true>(P, i, j, k);
+      else
+        pseudo_body<R, AIN, true, false, true>(P, i, j, k);
+    } else {
+      if (unit)
+        pseudo_body<R, AIN, true, true>(P, i, j, k);
+      else
+        pseudo_body<R, AIN, true>(P, i, j, k);
+    }
+  } else {
+    pseudo_body<R, AIN, true>(P, i, j, k);
+  }
 }
+// Ratios of at least 1 are recorded as RATIO_CAP (lim_ratio): the reverse
+// limiter's min3 selects neither form, and the reverse bounds kernel
+// recomputes its quotients from the recorded extrema and fluxes.
 template <class R, bool NONOS, bool FIRST, bool KEEP>
 __global__ void __launch_bounds__(128) kf_bounds(const Prob<R> P) {
-#define B(IN) bounds_body<R, NONOS, FIRST, KEEP, IN>(P, i, j, k)
-  FCELL(B)
+  if constexpr (NONOS && sizeof(R) == 8) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    const bool win = warp_interior(P.g, i, j, k);
+    const bool valid = i <= P.g.np && j <= P.g.mp;
+    RatioOps<R> r{};
+    if (valid) {
+      if (!win)
+        r = bounds_body<R, true, FIRST, KEEP, false, 2>(P, i, j, k);
+      else if (warp_unit_cell(P, i, j, k))
+        r = bounds_body<R, true, FIRST, KEEP, true, 2, true>(P, i, j, k);
+      else
+        r = bounds_body<R, true, FIRST, KEEP, true, 2>(P, i, j, k);
+    }
+    block_ratios(P, i, j, k, valid, r);
+  } else {
+#define B(IN, U) bounds_body<R, NONOS, FIRST, KEEP, IN, 1, U>(P, i, j, k)
+    FCELL_U(B)
 #undef B
+  }
 }
 template <class R, bool NONOS>
 __global__ void __launch_bounds__(128) kf_limit(const Prob<R> P) {
@@ -709,11 +857,12 @@ __global__ void __launch_bounds__(128) kf_limit(const Prob<R> P) {
 }
 template <class R>
 __global__ void __launch_bounds__(128) kf_update(const Prob<R> P) {
-#define B(IN) update_body<R, false, IN>(P, i, j, k)
-  FCELL(B)
+#define B(IN, U) update_body<R, false, IN, U>(P, i, j, k)
+  FCELL_U(B)
 #undef B
 }
 #undef FCELL
+#undef FCELL_U
 
 // The values of pass t: its input field, pseudo-velocities, ratios and
 // extrema from the records; `a` selects the "a" velocities the pass's
@@ -757,7 +906,14 @@ int run_step_adjoint(const Prob<R>& P, const AdjPlan<R>& A, int nonos, cudaStrea
   kf_upwind<R><<<grd, blk, 0, s>>>(F);
   n++;
   for (int t = 0; t < np_; t++) {
-    const Prob<R> Qa = pass_prob(P, A, t, true);
+    Prob<R> Qa = pass_prob(P, A, t, true);
+    // FP64 gauge: pair sums of the pass's input field into its cp/cn/q
+    // records, which the bounds kernel fills afterwards
+    Qa.pairs = (!P.stdf && sizeof(R) == 8) ? 1 : 0;
+    if (Qa.pairs) {
+      kf_pairs<R><<<grd, blk, 0, s>>>(Qa);
+      n++;
+    }
     if (t == 0) kf_pseudo<R, true><<<grd, blk, 0, s>>>(Qa);
     else kf_pseudo<R, false><<<grd, blk, 0, s>>>(Qa);
     const Prob<R> Q = pass_prob(P, A, t, false);
@@ -843,8 +999,16 @@ int run_step_adjoint(const Prob<R>& P, const AdjPlan<R>& A, int nonos, cudaStrea
       } else {
         ka_limit<R, false><<<grd, blk, 0, s>>>(Q, a);
       }
-      if (t == 0) ka_pseudo<R, true><<<grd, blk, 0, s>>>(Q, a);
-      else ka_pseudo<R, false><<<grd, blk, 0, s>>>(Q, a);
+      // the pass's cp/cn/q records are dead once the reverse bounds ran:
+      // they take the pair sums of its input field (FP64)
+      Prob<R> Qp = Q;
+      Qp.pairs = sizeof(R) == 8 ? 1 : 0;
+      if (Qp.pairs) {
+        kf_pairs<R><<<grd, blk, 0, s>>>(Qp);
+        n++;
+      }
+      if (t == 0) ka_pseudo<R, true><<<grd, blk, 0, s>>>(Qp, a);
+      else ka_pseudo<R, false><<<grd, blk, 0, s>>>(Qp, a);
     }
     n += 3;
   }

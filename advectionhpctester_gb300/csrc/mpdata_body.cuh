@@ -423,6 +423,64 @@ __device__ __forceinline__ RatioOps<R> bounds_body(const Prob<R>& P, int i, int 
   return {};
 }
 
+// The FP64 limiter ratios of a 32x4 block, divided together.  Only the
+// ratios below 1 need a quotient (a larger one is stored as RATIO_CAP, see
+// lim_ratio), and they are a few percent of the cells, scattered: a
+// warp dividing its own would run the division sequence (about ten FP64-pipe
+// instructions) whenever any of its lanes needs one.  Here the block packs its
+// operand pairs into shared memory, the first warps divide them, 32 at a time,
+// and every cell stores its two ratios.  Every thread of the block, inside
+// the domain or not, reaches the barriers.
+__device__ __forceinline__ void block_ratios(const Prob<double>& P, int i, int j, int k, bool valid,
+                                             const RatioOps<double>& r) {
+  __shared__ int s_cnt[4];
+  __shared__ double s_n[256], s_d[256];
+  const int lane = threadIdx.x, w = threadIdx.y;
+  const bool dp = valid && !ratio_ge1(r.np, r.dp), dn = valid && !ratio_ge1(r.nn, r.dn);
+  const unsigned bp = __ballot_sync(0xffffffffu, dp), bn = __ballot_sync(0xffffffffu, dn);
+  if (lane == 0) s_cnt[w] = __popc(bp) + __popc(bn);
+  __syncthreads();
+  int off = 0, total = 0;
+#pragma unroll
+  for (int v = 0; v < 4; v++) {
+    const int c = s_cnt[v];
+    off += v < w ? c : 0;
+    total += c;
+  }
+  const unsigned lt = (1u << lane) - 1u;
+  const int ip = off + __popc(bp & lt), in = off + __popc(bp) + __popc(bn & lt);
+  if (dp) {
+    s_n[ip] = r.np;
+    s_d[ip] = r.dp;
+  }
+  if (dn) {
+    s_n[in] = r.nn;
+    s_d[in] = r.dn;
+  }
+  __syncthreads();
+  for (int it = w * 32 + lane; it < total; it += 128) s_n[it] = s_n[it] / s_d[it];
+  __syncthreads();
+  if (valid) {
+    P.cp.at(i, j, k) = dp ? s_n[ip] : double(RATIO_CAP);
+    P.cn.at(i, j, k) = dn ? s_n[in] : double(RATIO_CAP);
+  }
+}
+
+// Pair sums of xant for the gauge pseudo-velocities of interior warps, which
+// read each of them from four faces: Sx = x(i)+x(i-1) into cp, Sy =
+// x(j)+x(j-1) into cn, Sz = x(k)+x(k-1) into q.  The operand order is that of
+// the rat4 sums (antidiff3d-gauge-gpubc.f90:89-203), so every difference of
+// two of them is the value rat4's own sums give.  cp, cn and q are free
+// until the limiter bounds stage rewrites them.
+template <class R>
+__device__ __forceinline__ void pairs_body(const Prob<R>& P, int i, int j, int k) {
+  const Arr<R>& X = P.xant;
+  const R x = X.ld(i, j, k);
+  if (i > 1) P.cp.at(i, j, k) = x + X.ld(i - 1, j, k);
+  if (j > 1) P.cn.at(i, j, k) = x + X.ld(i, j - 1, k);
+  if (k > 1) P.q.at(i, j, k) = x + X.ld(i, j, k - 1);
+}
+
 // ---- limited antidiffusive velocities and fluxes --------------------------
 // std: antidiff3d-standard-gpubc.f90:372-407 (sign-aware limited velocity,
 // donor flux of x/rhr); gauge: antidiff3d-gauge-gpubc.f90:343-363 (the

@@ -136,20 +136,26 @@ __device__ __forceinline__ float mul1(float x, float r) { return x * r; }
 __device__ __forceinline__ float div1(float x, float r) { return x / r; }
 __device__ __forceinline__ float rcp1(float r) { return 1.0f / r; }
 
-// Limiter ratio n/d (n >= 0, d >= ep > 0) where the only reader takes
-// min(1, n/d, ...): when n >= d and d is finite the IEEE quotient is >= 1, so
-// 1 is returned without dividing and the minimum is unchanged bit for bit.
-// NaN operands (n above +Inf, d not a positive finite number) divide as usual.
+// Limiter ratio n/d (n >= 0, d >= ep > 0) whose readers take min(1, n/d, ...):
+// when n >= d and d is finite the IEEE quotient is >= 1, and RATIO_CAP = 2 is
+// returned without dividing.  The forward minimum is 1 either way, bit for
+// bit; the adjoint's min3 never selects a ratio above 1, which is the
+// derivative of any quotient above 1 (a quotient of exactly 1, a tie with the
+// constant, is the one case whose subgradient it picks differently).  NaN
+// operands (n above +Inf, d not a positive finite number) divide as usual.
 // The test runs on the integer pipe: for non-negative numbers the bit
 // patterns order as the values do.
 __device__ __forceinline__ bool ratio_ge1(double n, double d) {
   const long long nb = __double_as_longlong(n), db = __double_as_longlong(d), inf = 0x7FF0000000000000LL;
   return db > 0 && db < inf && nb >= db && nb <= inf;
 }
-__device__ __forceinline__ double lim_ratio(double n, double d) { return ratio_ge1(n, d) ? 1.0 : div_call(n, d); }
+constexpr int RATIO_CAP = 2;
+__device__ __forceinline__ double lim_ratio(double n, double d) {
+  return ratio_ge1(n, d) ? double(RATIO_CAP) : div_call(n, d);
+}
 __device__ __forceinline__ float lim_ratio(float n, float d) {
   const int nb = __float_as_int(n), db = __float_as_int(d), inf = 0x7F800000;
-  if (db > 0 && db < inf && nb >= db && nb <= inf) return 1.0f;
+  if (db > 0 && db < inf && nb >= db && nb <= inf) return float(RATIO_CAP);
   return n / d;
 }
 

@@ -80,7 +80,7 @@ def stage_elems(stage, gauge, iord, precision=64):
 # (dram__bytes_read.sum + dram__bytes_write.sum, and
 # smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on.sum, per cell).
 # Both grow in proportion to the cells of a launch.
-NCU_PSEUDO = {64: {"dram_bytes_per_cell": 78.6, "fp64_inst_per_cell": 81.0},
+NCU_PSEUDO = {64: {"dram_bytes_per_cell": 100.2, "fp64_inst_per_cell": 60.6},
               32: {"dram_bytes_per_cell": 38.2, "fp64_inst_per_cell": 0.0}}
 # GB300 issues 2 FP64 instructions per SM per clock (1.25 TFLOP/s nominal FMA).
 FP64_INST_PER_SM_CLK = 2.0
