@@ -47,11 +47,41 @@ __device__ __forceinline__ void load_prob(Prob<R>& sP, const Prob<R>* __restrict
     }                                                                                        \
   }
 
+// As BATCH_TILE, with the unit-density instantiation BODY(IN, U) for interior
+// warps whose densities are all exactly 1 (FP64).
+#define BATCH_TILE_U(BODY)                                                                   \
+  __shared__ __align__(16) unsigned char sraw[sizeof(Prob<R>)];                              \
+  Prob<R>& P = *reinterpret_cast<Prob<R>*>(sraw);                                            \
+  const unsigned long long w = __ldg(tiles + blockIdx.x);                                    \
+  load_prob<R>(P, probs, (int)(w & 0xffffu));                                                \
+  __syncthreads();                                                                           \
+  const int i = (int)((w >> 16) & 0xffffu) * (int)blockDim.x + (int)threadIdx.x + 1;         \
+  const int j = (int)((w >> 32) & 0xffffu) * (int)blockDim.y + (int)threadIdx.y + 1;         \
+  const int k = (int)(w >> 48) + 1;                                                          \
+  const bool win = warp_interior(P.g, i, j, k);                                              \
+  if (i <= P.g.np && j <= P.g.mp) {                                                          \
+    if (!win) {                                                                              \
+      BODY(false, false);                                                                    \
+    } else if (warp_unit_cell(P, i, j, k)) {                                                 \
+      BODY(true, true);                                                                      \
+    } else {                                                                                 \
+      BODY(true, false);                                                                     \
+    }                                                                                        \
+  }
+
 #define BATCH_ARGS const Prob<R>* __restrict__ probs, const unsigned long long* __restrict__ tiles
 
 template <class R, bool ANTIDIFF, bool HALO>
 __global__ void __launch_bounds__(256) kb_upwind(BATCH_ARGS) {
-#define B(IN) upwind_body<R, ANTIDIFF, HALO, IN>(P, i, j, k)
+#define B(IN, U) upwind_body<R, ANTIDIFF, HALO, IN, U>(P, i, j, k)
+  BATCH_TILE_U(B)
+#undef B
+}
+// pair sums for the FP64 gauge problems (P.pairs), as k_pairs
+template <class R>
+__global__ void __launch_bounds__(256) kb_pairs(BATCH_ARGS) {
+#define B(IN) \
+  if (P.pairs) pairs_body<R>(P, i, j, k)
   BATCH_TILE(B)
 #undef B
 }
@@ -62,16 +92,67 @@ __global__ void __launch_bounds__(256) kb_copy(BATCH_ARGS) {
 #undef B
 }
 template <class R, bool AIN>
+__device__ __forceinline__ void pseudo_dispatch(const Prob<R>& P, int i, int j, int k, bool win) {
+  if (!win) {
+    pseudo_body<R, AIN, false>(P, i, j, k);
+  } else if constexpr (sizeof(R) == 8) {
+    const bool unit = warp_unit_faces(P, i, j, k);
+    if (P.pairs) {
+      if (unit)
+        pseudo_body<R, AIN, true, true, true>(P, i, j, k);
+      else
+        pseudo_body<R, AIN, true, false, true>(P, i, j, k);
+    } else {
+      if (unit)
+        pseudo_body<R, AIN, true, true>(P, i, j, k);
+      else
+        pseudo_body<R, AIN, true>(P, i, j, k);
+    }
+  } else {
+    pseudo_body<R, AIN, true>(P, i, j, k);
+  }
+}
+template <class R, bool AIN>
 __global__ void __launch_bounds__(256) kb_pseudo(BATCH_ARGS) {
-#define B(IN) pseudo_body<R, AIN, IN>(P, i, j, k)
-  BATCH_TILE(B)
-#undef B
+  __shared__ __align__(16) unsigned char sraw[sizeof(Prob<R>)];
+  Prob<R>& P = *reinterpret_cast<Prob<R>*>(sraw);
+  const unsigned long long w = __ldg(tiles + blockIdx.x);
+  load_prob<R>(P, probs, (int)(w & 0xffffu));
+  __syncthreads();
+  const int i = (int)((w >> 16) & 0xffffu) * (int)blockDim.x + (int)threadIdx.x + 1;
+  const int j = (int)((w >> 32) & 0xffffu) * (int)blockDim.y + (int)threadIdx.y + 1;
+  const int k = (int)(w >> 48) + 1;
+  const bool win = warp_interior(P.g, i, j, k);
+  if (i <= P.g.np && j <= P.g.mp) pseudo_dispatch<R, AIN>(P, i, j, k, win);
 }
 template <class R, bool NONOS, bool FIRST, bool KEEP>
 __global__ void __launch_bounds__(256) kb_bounds(BATCH_ARGS) {
-#define B(IN) bounds_body<R, NONOS, FIRST, KEEP, IN, true>(P, i, j, k)
-  BATCH_TILE(B)
+  if constexpr (NONOS && sizeof(R) == 8) {
+    __shared__ __align__(16) unsigned char sraw[sizeof(Prob<R>)];
+    Prob<R>& P = *reinterpret_cast<Prob<R>*>(sraw);
+    const unsigned long long w = __ldg(tiles + blockIdx.x);
+    load_prob<R>(P, probs, (int)(w & 0xffffu));
+    __syncthreads();
+    const int i = (int)((w >> 16) & 0xffffu) * (int)blockDim.x + (int)threadIdx.x + 1;
+    const int j = (int)((w >> 32) & 0xffffu) * (int)blockDim.y + (int)threadIdx.y + 1;
+    const int k = (int)(w >> 48) + 1;
+    const bool win = warp_interior(P.g, i, j, k);
+    const bool valid = i <= P.g.np && j <= P.g.mp;
+    RatioOps<R> r{};
+    if (valid) {
+      if (!win)
+        r = bounds_body<R, true, FIRST, KEEP, false, 2>(P, i, j, k);
+      else if (warp_unit_cell(P, i, j, k))
+        r = bounds_body<R, true, FIRST, KEEP, true, 2, true>(P, i, j, k);
+      else
+        r = bounds_body<R, true, FIRST, KEEP, true, 2>(P, i, j, k);
+    }
+    block_ratios(P, i, j, k, valid, r);
+  } else {
+#define B(IN, U) bounds_body<R, NONOS, FIRST, KEEP, IN, 1, U>(P, i, j, k)
+    BATCH_TILE_U(B)
 #undef B
+  }
 }
 template <class R, bool NONOS>
 __global__ void __launch_bounds__(256) kb_limit(BATCH_ARGS) {
@@ -81,8 +162,8 @@ __global__ void __launch_bounds__(256) kb_limit(BATCH_ARGS) {
 }
 template <class R, bool LAST>
 __global__ void __launch_bounds__(256) kb_update(BATCH_ARGS) {
-#define B(IN) update_body<R, LAST, IN>(P, i, j, k)
-  BATCH_TILE(B)
+#define B(IN, U) update_body<R, LAST, IN, U>(P, i, j, k)
+  BATCH_TILE_U(B)
 #undef B
 }
 
@@ -113,6 +194,7 @@ int run_batch(const BatchLaunch<R>& B, Prof* prof, cudaStream_t s) {
   const bool keep = B.iord > 2;
   for (int pass = 2; pass <= B.iord; pass++) {
     const bool first = (pass == 2), last = (pass == B.iord) && B.halo;
+    if (B.pairs) BLAUNCH(ST_PAIRS, (kb_pairs<R><<<G, blk, 0, s>>>(A)));
     if (first) BLAUNCH(ST_PSEUDO, (kb_pseudo<R, true><<<G, blk, 0, s>>>(A)));
     else BLAUNCH(ST_PSEUDO, (kb_pseudo<R, false><<<G, blk, 0, s>>>(A)));
     if (!B.nonos) BLAUNCH(ST_BOUNDS, (kb_bounds<R, false, true, false><<<G, blk, 0, s>>>(A)));

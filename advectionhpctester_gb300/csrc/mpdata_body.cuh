@@ -423,7 +423,8 @@ __device__ __forceinline__ RatioOps<R> bounds_body(const Prob<R>& P, int i, int 
   return {};
 }
 
-// The FP64 limiter ratios of a 32x4 block, divided together.  Only the
+// The FP64 limiter ratios of a block (whole warps, at most 256 threads),
+// divided together.  Only the
 // ratios below 1 need a quotient (a larger one is stored as RATIO_CAP, see
 // lim_ratio), and they are a few percent of the cells, scattered: a
 // warp dividing its own would run the division sequence (about ten FP64-pipe
@@ -433,16 +434,16 @@ __device__ __forceinline__ RatioOps<R> bounds_body(const Prob<R>& P, int i, int 
 // the domain or not, reaches the barriers.
 __device__ __forceinline__ void block_ratios(const Prob<double>& P, int i, int j, int k, bool valid,
                                              const RatioOps<double>& r) {
-  __shared__ int s_cnt[4];
-  __shared__ double s_n[256], s_d[256];
-  const int lane = threadIdx.x, w = threadIdx.y;
+  __shared__ int s_cnt[8];
+  __shared__ double s_n[512], s_d[512];
+  const int nt = blockDim.x * blockDim.y, tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const int lane = tid & 31, w = tid >> 5, nw = nt >> 5;
   const bool dp = valid && !ratio_ge1(r.np, r.dp), dn = valid && !ratio_ge1(r.nn, r.dn);
   const unsigned bp = __ballot_sync(0xffffffffu, dp), bn = __ballot_sync(0xffffffffu, dn);
   if (lane == 0) s_cnt[w] = __popc(bp) + __popc(bn);
   __syncthreads();
   int off = 0, total = 0;
-#pragma unroll
-  for (int v = 0; v < 4; v++) {
+  for (int v = 0; v < nw; v++) {
     const int c = s_cnt[v];
     off += v < w ? c : 0;
     total += c;
@@ -458,7 +459,7 @@ __device__ __forceinline__ void block_ratios(const Prob<double>& P, int i, int j
     s_d[in] = r.dn;
   }
   __syncthreads();
-  for (int it = w * 32 + lane; it < total; it += 128) s_n[it] = s_n[it] / s_d[it];
+  for (int it = tid; it < total; it += nt) s_n[it] = s_n[it] / s_d[it];
   __syncthreads();
   if (valid) {
     P.cp.at(i, j, k) = dp ? s_n[ip] : double(RATIO_CAP);

@@ -642,6 +642,9 @@ BatchLaunch<R> launch_of(const Batch* b, int halo) {
   L.iord = b->iord;
   L.nonos = b->nonos;
   L.halo = halo;
+  L.pairs = 0;
+  if (sizeof(R) == 8)
+    for (const mpdata_problem& q : b->pr) L.pairs |= q.gauge ? 1 : 0;
   return L;
 }
 
@@ -658,6 +661,7 @@ void write_prob(Batch* b, int p, void* psi, const void* u1, const void* u2, cons
   Prob<R> P = make_prob<R>(g, b->pr[p].gauge, (R*)psi, (const R*)u1, (const R*)u2, (const R*)u3,
                            (const R*)h, (const R*)rhr, (const R*)bcx, (const R*)bcy, base + b->foff[p],
                            b->ncell[p], base + b->voff[p], b->owner[p] == p ? 1 : 0);
+  P.pairs = (b->pr[p].gauge && sizeof(R) == 8) ? 1 : 0;  // kb_pairs fills cp/cn/q before kb_pseudo
   memcpy(b->table.data() + (size_t)p * sizeof(Prob<R>), &P, sizeof P);
 }
 

@@ -33,6 +33,7 @@ struct BatchLaunch {
   int bx, by;
   int iord, nonos;
   int halo;  // 0 while autotuning: psi (interior and halo) is not written
+  int pairs; // some FP64 gauge problem reads pair sums: launch kb_pairs
 };
 template <class R>
 int run_batch(const BatchLaunch<R>& B, Prof* prof, cudaStream_t stream);
