@@ -60,13 +60,15 @@ __global__ void __launch_bounds__(128) k_copy(const Prob<R> P) {
 // Minimum resident 128-thread blocks per SM asked of the register allocator
 // for the pseudo-velocity kernel, whose interior path keeps ~60 neighbour
 // loads in flight: FP32 is latency-bound and gains from 8 blocks (64
-// registers, a 16-byte spill); FP64 is FP64-pipe-bound and keeps its 80.
-// Build-time overridable for tuning sweeps.
+// registers, a 12-byte spill); FP64 takes 5 (at most 102 registers, no
+// spill; 4 percent faster at 512x512x128 than the 4 blocks its 100
+// registers allowed unbounded; 6 blocks spill).  Build-time overridable for
+// tuning sweeps.
 #ifndef MPDATA_MINB_PSEUDO_F32
 #define MPDATA_MINB_PSEUDO_F32 8
 #endif
 #ifndef MPDATA_MINB_PSEUDO_F64
-#define MPDATA_MINB_PSEUDO_F64 1
+#define MPDATA_MINB_PSEUDO_F64 5
 #endif
 template <class R>
 struct PseudoMinBlocks {
