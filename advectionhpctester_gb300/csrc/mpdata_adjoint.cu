@@ -795,9 +795,14 @@ __global__ void __launch_bounds__(128) kf_pairs(const Prob<R> P) {
   (void)g;
   pairs_body<R>(P, i, j, k);
 }
-// the forward stage's dispatch: unit face densities and pair sums (FP64)
+// the forward stage's dispatch: unit face densities and pair sums (FP64),
+// and the stage kernel's five resident blocks per SM for FP64
+template <class R>
+struct KfPseudoMinBlocks {
+  static constexpr int v = sizeof(R) == 8 ? 5 : 1;
+};
 template <class R, bool AIN>
-__global__ void __launch_bounds__(128) kf_pseudo(const Prob<R> P) {
+__global__ void __launch_bounds__(128, KfPseudoMinBlocks<R>::v) kf_pseudo(const Prob<R> P) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int k = blockIdx.z + 1;

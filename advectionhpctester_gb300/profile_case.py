@@ -3,12 +3,14 @@ allocations, for profilers (ncu) and quick timing.
 
   python -m advectionhpctester_gb300.profile_case --grid 384 384 64 --steps 2 \
       [--precision 64|32] [--std] [--iord 3] [--bc periodic|reference] \
-      [--workload random|deformational]
+      [--workload random|deformational] [--adjoint]
 
 random: seeded random fields with h, rhr in [0.8, 1.2]; deformational: the
 periodic deformational flow with unit densities (the benchmark's fields).
 
-Prints the CUDA-event time per step and the per-stage times.
+Prints the CUDA-event time per step and the per-stage times.  --adjoint
+times the step adjoint (lambda = psi, zero velocity gradients) after the
+forward steps and reports its time beside the forward step's.
 """
 import argparse
 import json
@@ -26,6 +28,7 @@ def main(argv=None):
     ap.add_argument("--iord", type=int, default=3)
     ap.add_argument("--bc", choices=["periodic", "reference"], default="periodic")
     ap.add_argument("--workload", choices=["random", "deformational"], default="random")
+    ap.add_argument("--adjoint", action="store_true", help="also time the step adjoint")
     a = ap.parse_args(argv)
 
     import torch
@@ -61,11 +64,27 @@ def main(argv=None):
     torch.cuda.synchronize()
     st = ws.stage_times()
     ms = e0.elapsed_time(e1) / a.steps
-    print(json.dumps({"grid": a.grid, "workload": a.workload, "precision": a.precision,
-                      "form": "std" if a.std else "gauge",
-                      "iord": a.iord, "bc": a.bc, "ms_per_step": round(ms, 4),
-                      "gcell_steps_per_s": round(nx * ny * nz / (ms * 1e-3) / 1e9, 4),
-                      "stages_ms": {k: round(v[0] / a.steps, 4) for k, v in st.items() if v[1]}}))
+    out = {"grid": a.grid, "workload": a.workload, "precision": a.precision,
+           "form": "std" if a.std else "gauge",
+           "iord": a.iord, "bc": a.bc, "ms_per_step": round(ms, 4),
+           "gcell_steps_per_s": round(nx * ny * nz / (ms * 1e-3) / 1e9, 4),
+           "stages_ms": {k: round(v[0] / a.steps, 4) for k, v in st.items() if v[1]}}
+    if a.adjoint:
+        lam = d["x"].clone()
+        gu = [torch.zeros_like(d[k]) for k in ("u1", "u2", "u3")]
+        adj = (d["x"], d["u1"], d["u2"], d["u3"], d["h"], d["rhr"], lam, *gu, d["bcx"], d["bcy"])
+        for _ in range(a.warmup):
+            ws.step_adjoint(*adj)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(a.steps):
+            ws.step_adjoint(*adj)
+        e1.record()
+        torch.cuda.synchronize()
+        ams = e0.elapsed_time(e1) / a.steps
+        out["adjoint_ms_per_step"] = round(ams, 4)
+        out["adjoint_over_forward"] = round(ams / ms, 3)
+    print(json.dumps(out))
     ws.close()
 
 
