@@ -62,6 +62,7 @@ SIGNATURES = {
     "mpdata_batch_step": ([P, P], I),
     "mpdata_batch_graph": ([P, I], I),
     "mpdata_batch_tune": ([P, P, ctypes.POINTER(I), ctypes.POINTER(I)], I),
+    "mpdata_batch_set_shape": ([P, I, I, P], I),
     "mpdata_batch_profile": ([P, I], I),
     "mpdata_batch_stage_times": ([P, I, ctypes.POINTER(D), ctypes.POINTER(ctypes.c_longlong)], I),
     "mpdata_mass_f64": ([ctypes.POINTER(MpdataGrid), P, P, P, ctypes.POINTER(D), P], I),

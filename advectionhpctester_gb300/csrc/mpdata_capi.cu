@@ -878,6 +878,15 @@ int mpdata_batch_tune(void* batch, void* stream, int* bx_out, int* by_out) {
   return MPDATA_OK;
 }
 
+int mpdata_batch_set_shape(void* batch, int bx, int by, void* stream) {
+  Batch* b = as_batch(batch);
+  if (!b) return MPDATA_E_WS;
+  if (bx < 1 || by < 1 || bx > 256 || by > 256) return MPDATA_E_OPTS;
+  const int nt = bx * by;
+  if (nt < 32 || nt > 256 || nt % 32) return MPDATA_E_OPTS;
+  return set_shape(b, bx, by, static_cast<cudaStream_t>(stream));
+}
+
 int mpdata_batch_profile(void* batch, int enable) {
   Batch* b = as_batch(batch);
   if (!b) return MPDATA_E_WS;

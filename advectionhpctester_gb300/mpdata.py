@@ -264,6 +264,11 @@ class Batch:
         check(self.lib.mpdata_batch_tune(self.handle, _stream(stream), bx, by), "mpdata_batch_tune")
         return bx.value, by.value
 
+    def shape(self, bx, by, stream=None):
+        """Tile shape bx x by (a multiple of 32, at most 256 threads) without timing."""
+        check(self.lib.mpdata_batch_set_shape(self.handle, int(bx), int(by), _stream(stream)),
+              "mpdata_batch_set_shape")
+
     def profile(self, enable=True):
         check(self.lib.mpdata_batch_profile(self.handle, 1 if enable else 0), "mpdata_batch_profile")
 

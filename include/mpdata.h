@@ -246,6 +246,11 @@ int mpdata_batch_graph(void* batch, int enable);
  * fastest, and caches it for batches of the same signature (precision, iord,
  * nonos, total cells, problem count).  Synchronises the stream. */
 int mpdata_batch_tune(void* batch, void* stream, int* bx, int* by);
+/* Sets the tile shape (block of bx*by cells, a multiple of 32 and at most
+ * 256 threads) without timing, e.g. a shape tuned earlier.  No reference
+ * counterpart.  Drops a captured graph.  MPDATA_E_OPTS for an invalid shape.
+ * Synchronises the stream. */
+int mpdata_batch_set_shape(void* batch, int bx, int by, void* stream);
 int mpdata_batch_profile(void* batch, int enable);
 int mpdata_batch_stage_times(void* batch, int nstages, double* total_ms, long long* launches);
 

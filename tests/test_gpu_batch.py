@@ -138,3 +138,34 @@ def test_batch_rejects_bad_input(M):
     with pytest.raises(M.MpdataError):  # step before the arrays are set
         b.step()
     b.close()
+
+
+@pytest.mark.parametrize("perturb", [False, True], ids=["unit", "one_cell_off"])
+@pytest.mark.parametrize("shape", [(32, 4), (16, 8)])
+def test_interior_tiles_unit_density(M, oracle, shape, perturb):
+    """Tracers on an 80-wide grid with h = rhr = 1 (one perturbed cell when
+    `perturb`): interior warps of the tile kernels take the unit-density
+    bodies, the pair sums and the block-compacted limiter ratios, for the
+    default and the 16x8 tile shapes.  Bit for bit against the oracle."""
+    ibc = (1, 1, 1)
+    fs = tracers(3, (80, 12, 8), ibc, seed=61)
+    for f in fs:
+        f.h[...] = 1.0
+        f.rhr[...] = 1.0
+        if perturb:
+            f.h[45, 5, 4] = 1.125
+            f.rhr[45, 5, 4] = 0.875
+    forms = [1, 0, 1]
+    probs = [dict(np=80, mp=12, lp=8, ibcx=1, ibcy=1, ibcz=1, gauge=g, velocity_group=3) for g in forms]
+    b = M.Batch(probs, iord=3)
+    b.shape(*shape)
+    ds = [dev(M, f) for f in fs]
+    shared = ds[0]
+    for p, d in enumerate(ds):
+        b.set(p, d["x"], shared["u1"], shared["u2"], shared["u3"], shared["h"], shared["rhr"], d["bcx"], d["bcy"])
+    for _ in range(3):
+        b.step()
+    for p, (f, d) in enumerate(zip(fs, ds)):
+        np.testing.assert_array_equal(M.to_numpy(d["x"]), oracle_steps(oracle, f, forms[p], 3, 3),
+                                      err_msg="tracer %d" % p)
+    b.close()
