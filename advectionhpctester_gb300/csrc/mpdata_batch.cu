@@ -93,6 +93,15 @@ __global__ void __launch_bounds__(256) kb_copy(BATCH_ARGS) {
 }
 template <class R, bool AIN>
 __device__ __forceinline__ void pseudo_dispatch(const Prob<R>& P, int i, int j, int k, bool win) {
+  if constexpr (AIN) {
+    if (win && P.gv) {  // first pass of a velocity group: velocity-only terms precomputed
+      if (P.pairs)
+        pseudo_body<R, AIN, true, false, true, true>(P, i, j, k);
+      else
+        pseudo_body<R, AIN, true, false, false, true>(P, i, j, k);
+      return;
+    }
+  }
   if (!win) {
     pseudo_body<R, AIN, false>(P, i, j, k);
   } else if constexpr (sizeof(R) == 8) {

@@ -26,10 +26,16 @@ struct Prob {
   int own_vel;  // 1 = this problem writes the velocity-derived scratch (hinv, hm*)
   int rho;      // density step of mpdata3d_rho_gauge_gpubc: no rhr, upwind fluxes kept
   int pairs;    // gauge pseudo-velocity: pair sums of xant in cp, cn, q (k_pairs)
+  int gv;       // batch velocity group: the velocity-only terms of the first
+                // pass's gauge pseudo-velocities are in gvf (the group owner's
+                // upwind stores them)
   Arr<R> psi, u1, u2, u3, h, rhr;
   const R* bcx;
   const R* bcy;
   Arr<R> hinv, hmx, hmy, hmz;  // may be shared by problems with one velocity
+  Arr<R> gvf[12];               // per face direction d = x, y, z (index 4d): the two
+                                // 4-face sums of the cross terms, (|a|-a*a*hm)/2 and
+                                // 0.03125*a*hm (velocity group, shared)
   Arr<R> xant, v1, v2, v3, f1, f2, f3, w1, w2, w3, cp, cn, mx, mn, q;
   // density step only: outputs and the upwind fluxes of the faces n+1
   Arr<R> x_incomp, rhoadv, rhr_out, pexe, pexr1, pexr2;
@@ -122,6 +128,45 @@ __device__ __forceinline__ bool warp_unit_cell(const Prob<R>& P, int i, int j, i
   }
 }
 
+// Velocity-only terms of the first corrective pass's gauge pseudo-velocities
+// (pseudo_form with AIN), stored by a velocity group's owner for all of the
+// group's fields: per face, the 4-face sums of the two cross terms in
+// pseudo_form's order, (|a| - a*a*hm)*0.5 and 0.03125*a*hm.  The half is
+// applied before the product with (x2-x1) instead of after it, which gives
+// the same bits unless a value is subnormal (scaling by a power of two
+// commutes with rounding).
+template <class R, bool IN>
+__device__ __forceinline__ void velgroup_body(const Prob<R>& P, int i, int j, int k, R hx, R hy, R hz) {
+  const Geo& g = P.g;
+#define AX(f, b, c) fx<R, true, IN>(g, P.u1, (f), (b), (c))
+#define AY(a, f, c) fy<R, true, IN>(g, P.u2, (a), (f), (c))
+#define AZ(a, b, f) fz<R, true, IN>(g, P.u3, (a), (b), (f))
+  if (IN || g.bx || i > 1) {
+    const R a = AX(i, j, k);
+    P.gvf[0].at(i, j, k) = AY(i - 1, j, k) + AY(i - 1, j + 1, k) + AY(i, j + 1, k) + AY(i, j, k);
+    P.gvf[1].at(i, j, k) = AZ(i - 1, j, k) + AZ(i - 1, j, k + 1) + AZ(i, j, k + 1) + AZ(i, j, k);
+    P.gvf[2].at(i, j, k) = (fabs(a) - a * a * hx) * R(0.5);
+    P.gvf[3].at(i, j, k) = R(0.03125) * a * hx;
+  }
+  if (IN || g.by || j > 1) {
+    const R a = AY(i, j, k);
+    P.gvf[4].at(i, j, k) = AX(i, j - 1, k) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j - 1, k);
+    P.gvf[5].at(i, j, k) = AZ(i, j - 1, k) + AZ(i, j, k) + AZ(i, j, k + 1) + AZ(i, j - 1, k + 1);
+    P.gvf[6].at(i, j, k) = (fabs(a) - a * a * hy) * R(0.5);
+    P.gvf[7].at(i, j, k) = R(0.03125) * a * hy;
+  }
+  if (IN || g.bz || k > 1) {
+    const R a = AZ(i, j, k);
+    P.gvf[8].at(i, j, k) = AX(i, j, k - 1) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j, k - 1);
+    P.gvf[9].at(i, j, k) = AY(i, j, k - 1) + AY(i, j + 1, k - 1) + AY(i, j + 1, k) + AY(i, j, k);
+    P.gvf[10].at(i, j, k) = (fabs(a) - a * a * hz) * R(0.5);
+    P.gvf[11].at(i, j, k) = R(0.03125) * a * hz;
+  }
+#undef AX
+#undef AY
+#undef AZ
+}
+
 // ---- upwind3d_gpubc (upwind3d-gpubc.f90:101-198) -------------------------
 // ANTIDIFF: an antidiffusive pass follows, so psi's open-wall halo ends the
 // step holding the zero-gradient copy of the old boundary values (written by
@@ -175,9 +220,11 @@ __device__ __forceinline__ void upwind_body(const Prob<R>& P, int i, int j, int 
     P.hinv.at(i, j, k) = hi;
     // reciprocal mean densities of the cell's lower faces, used by every
     // corrective pass of this step (hmx/hmy/hmz of antidiff3d-*-gpubc.f90)
-    if (IN || g.bx || i > 1) P.hmx.at(i, j, k) = rhm(P.h.ld(cx<IN>(g, i - 1), j, k), hc);
-    if (IN || g.by || j > 1) P.hmy.at(i, j, k) = rhm(P.h.ld(i, cy<IN>(g, j - 1), k), hc);
-    if (IN || g.bz || k > 1) P.hmz.at(i, j, k) = rhm(P.h.ld(i, j, cz<IN>(g, k - 1)), hc);
+    R hx = R(0), hy = R(0), hz = R(0);
+    if (IN || g.bx || i > 1) P.hmx.at(i, j, k) = hx = rhm(P.h.ld(cx<IN>(g, i - 1), j, k), hc);
+    if (IN || g.by || j > 1) P.hmy.at(i, j, k) = hy = rhm(P.h.ld(i, cy<IN>(g, j - 1), k), hc);
+    if (IN || g.bz || k > 1) P.hmz.at(i, j, k) = hz = rhm(P.h.ld(i, j, cz<IN>(g, k - 1)), hc);
+    if (P.gv) velgroup_body<R, IN>(P, i, j, k, hx, hy, hz);
   }
   if (HALO && !IN) {
     if (!g.bx) {
@@ -200,8 +247,10 @@ __device__ __forceinline__ void upwind_body(const Prob<R>& P, int i, int j, int 
 // previous pass's limited velocities w1..w3.  U: the three face reciprocal
 // densities of every cell of the warp are exactly 1 (warp_unit_faces).  PS
 // (gauge, interior warps): the pair sums of xant the rat4 terms start with
-// are read from cp, cn and q, where k_pairs stored them.
-template <class R, bool STD, bool AIN, bool IN = false, bool U = false, bool PS = false>
+// are read from cp, cn and q, where k_pairs stored them.  GV (gauge, first
+// pass, interior warps of a batch velocity group): the velocity-only terms
+// are read from gvf (velgroup_body).
+template <class R, bool STD, bool AIN, bool IN = false, bool U = false, bool PS = false, bool GV = false>
 __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int k) {
   const Geo& g = P.g;
   const Arr<R>& X = P.xant;
@@ -237,14 +286,17 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
     } else {
       const R d2 = PS ? P.cp.ld(i, j + 1, k) - P.cp.ld(i, j - 1, k)
                       : dif4(XX(i - 1, j - 1, k), XX(i, j - 1, k), XX(i - 1, j + 1, k), XX(i, j + 1, k));
-      const R c2 = (AY(i - 1, j, k) + AY(i - 1, j + 1, k) + AY(i, j + 1, k) + AY(i, j, k)) * d2;
+      const R c2 = (GV ? P.gvf[0].ld(i, j, k) : AY(i - 1, j, k) + AY(i - 1, j + 1, k) + AY(i, j + 1, k) + AY(i, j, k)) * d2;
       R cr = c2;
       if (zt) {
         const R d3 = PS ? P.cp.ld(i, j, k + 1) - P.cp.ld(i, j, k - 1)
                         : dif4(XX(i - 1, j, k - 1), XX(i, j, k - 1), XX(i - 1, j, k + 1), XX(i, j, k + 1));
-        cr = c2 + (AZ(i - 1, j, k) + AZ(i - 1, j, k + 1) + AZ(i, j, k + 1) + AZ(i, j, k)) * d3;
+        cr = c2 + (GV ? P.gvf[1].ld(i, j, k) : AZ(i - 1, j, k) + AZ(i - 1, j, k + 1) + AZ(i, j, k + 1) + AZ(i, j, k)) * d3;
       }
-      v = vdyf_u<U>(XX(i - 1, j, k), XX(i, j, k), a, hmx) - hmul<U>(R(0.03125) * a, hmx) * cr;
+      if (GV)
+        v = P.gvf[2].ld(i, j, k) * (XX(i, j, k) - XX(i - 1, j, k)) - P.gvf[3].ld(i, j, k) * cr;
+      else
+        v = vdyf_u<U>(XX(i - 1, j, k), XX(i, j, k), a, hmx) - hmul<U>(R(0.03125) * a, hmx) * cr;
     }
     P.v1.at(i, j, k) = v;
   }
@@ -271,14 +323,17 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
     } else {
       const R d1 = PS ? P.cn.ld(i + 1, j, k) - P.cn.ld(i - 1, j, k)
                       : dif4(XX(i - 1, j - 1, k), XX(i - 1, j, k), XX(i + 1, j - 1, k), XX(i + 1, j, k));
-      const R c1 = (AX(i, j - 1, k) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j - 1, k)) * d1;
+      const R c1 = (GV ? P.gvf[4].ld(i, j, k) : AX(i, j - 1, k) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j - 1, k)) * d1;
       R cr = c1;
       if (zt) {
         const R d3 = PS ? P.cn.ld(i, j, k + 1) - P.cn.ld(i, j, k - 1)
                         : dif4(XX(i, j - 1, k - 1), XX(i, j, k - 1), XX(i, j - 1, k + 1), XX(i, j, k + 1));
-        cr = c1 + (AZ(i, j - 1, k) + AZ(i, j, k) + AZ(i, j, k + 1) + AZ(i, j - 1, k + 1)) * d3;
+        cr = c1 + (GV ? P.gvf[5].ld(i, j, k) : AZ(i, j - 1, k) + AZ(i, j, k) + AZ(i, j, k + 1) + AZ(i, j - 1, k + 1)) * d3;
       }
-      v = vdyf_u<U>(XX(i, j - 1, k), XX(i, j, k), a, hmy) - hmul<U>(R(0.03125) * a, hmy) * cr;
+      if (GV)
+        v = P.gvf[6].ld(i, j, k) * (XX(i, j, k) - XX(i, j - 1, k)) - P.gvf[7].ld(i, j, k) * cr;
+      else
+        v = vdyf_u<U>(XX(i, j - 1, k), XX(i, j, k), a, hmy) - hmul<U>(R(0.03125) * a, hmy) * cr;
     }
     P.v2.at(i, j, k) = v;
   }
@@ -306,9 +361,12 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
                       : dif4(XX(i - 1, j, k - 1), XX(i - 1, j, k), XX(i + 1, j, k - 1), XX(i + 1, j, k));
       const R d2 = PS ? P.q.ld(i, j + 1, k) - P.q.ld(i, j - 1, k)
                       : dif4(XX(i, j - 1, k - 1), XX(i, j - 1, k), XX(i, j + 1, k - 1), XX(i, j + 1, k));
-      const R cr = (AX(i, j, k - 1) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j, k - 1)) * d1 +
-                   (AY(i, j, k - 1) + AY(i, j + 1, k - 1) + AY(i, j + 1, k) + AY(i, j, k)) * d2;
-      v = vdyf_u<U>(XX(i, j, k - 1), XX(i, j, k), a, hmz) - hmul<U>(R(0.03125) * a, hmz) * cr;
+      const R cr = (GV ? P.gvf[8].ld(i, j, k) : AX(i, j, k - 1) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j, k - 1)) * d1 +
+                   (GV ? P.gvf[9].ld(i, j, k) : AY(i, j, k - 1) + AY(i, j + 1, k - 1) + AY(i, j + 1, k) + AY(i, j, k)) * d2;
+      if (GV)
+        v = P.gvf[10].ld(i, j, k) * (XX(i, j, k) - XX(i, j, k - 1)) - P.gvf[11].ld(i, j, k) * cr;
+      else
+        v = vdyf_u<U>(XX(i, j, k - 1), XX(i, j, k), a, hmz) - hmul<U>(R(0.03125) * a, hmz) * cr;
     }
     P.v3.at(i, j, k) = v;
   }
@@ -318,12 +376,12 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
 #undef AZ
 }
 
-template <class R, bool AIN, bool IN = false, bool U = false, bool PS = false>
+template <class R, bool AIN, bool IN = false, bool U = false, bool PS = false, bool GV = false>
 __device__ __forceinline__ void pseudo_body(const Prob<R>& P, int i, int j, int k) {
   if (P.stdf)
     pseudo_form<R, true, AIN, IN, U>(P, i, j, k);
   else
-    pseudo_form<R, false, AIN, IN, U, PS>(P, i, j, k);
+    pseudo_form<R, false, AIN, IN, U, PS, GV>(P, i, j, k);
 }
 
 // ---- limiter bounds and ratios (std :256-348, gauge :238-324) -------------

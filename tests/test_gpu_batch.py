@@ -140,19 +140,22 @@ def test_batch_rejects_bad_input(M):
     b.close()
 
 
-@pytest.mark.parametrize("perturb", [False, True], ids=["unit", "one_cell_off"])
+@pytest.mark.parametrize("density", ["unit", "one_cell_off", "random"])
 @pytest.mark.parametrize("shape", [(32, 4), (16, 8)])
-def test_interior_tiles_unit_density(M, oracle, shape, perturb):
-    """Tracers on an 80-wide grid with h = rhr = 1 (one perturbed cell when
-    `perturb`): interior warps of the tile kernels take the unit-density
-    bodies, the pair sums and the block-compacted limiter ratios, for the
-    default and the 16x8 tile shapes.  Bit for bit against the oracle."""
+def test_interior_tiles_velocity_group(M, oracle, shape, density):
+    """Three tracers of one velocity group on an 80-wide grid: interior warps
+    of the tile kernels read the group's precomputed first-pass terms and the
+    pair sums, and take the unit-density bodies (h = rhr = 1, or all but one
+    cell) and the block-compacted limiter ratios, for the default and the 16x8
+    tile shapes.  Bit for bit against the oracle."""
     ibc = (1, 1, 1)
     fs = tracers(3, (80, 12, 8), ibc, seed=61)
     for f in fs:
+        if density == "random":
+            continue
         f.h[...] = 1.0
         f.rhr[...] = 1.0
-        if perturb:
+        if density == "one_cell_off":
             f.h[45, 5, 4] = 1.125
             f.rhr[45, 5, 4] = 0.875
     forms = [1, 0, 1]
