@@ -200,6 +200,14 @@ __device__ __forceinline__ void upwind_body(const Prob<R>& P, int i, int j, int 
     f3p = donor(x, psi.ld(i, j, cz<IN>(g, k + 1)), fz<R, true, IN>(g, P.u3, i, j, k + 1));
     f3 = donor(psi.ld(i, j, cz<IN>(g, k - 1)), x, P.u3.ld(i, j, k));
   }
+  // the loads of the face reciprocals' neighbour densities and of rhr come
+  // before the first store (see limit_form)
+  const bool hv = ANTIDIFF && P.own_vel;
+  const bool fxe = IN || g.bx || i > 1, fye = IN || g.by || j > 1, fze = IN || g.bz || k > 1;
+  const R hxm = hv && fxe ? P.h.ld(cx<IN>(g, i - 1), j, k) : R(0);
+  const R hym = hv && fye ? P.h.ld(i, cy<IN>(g, j - 1), k) : R(0);
+  const R hzm = hv && fze ? P.h.ld(i, j, cz<IN>(g, k - 1)) : R(0);
+  const R rh = (P.rho || U) ? R(1) : P.rhr.ld(i, j, k);
   if (P.rho) {
     // mpdata3d-rho-gauge-gpubc.f90:137-210: no rhr, division by h, fluxes kept;
     // rhoadv takes the input x_incomp (:121-123)
@@ -214,16 +222,16 @@ __device__ __forceinline__ void upwind_body(const Prob<R>& P, int i, int j, int 
     P.rhoadv.at(i, j, k) = P.x_incomp.ld(i, j, k);
   } else {
     const R sum = f1p - f1 + f2p - f2 + f3p - f3;
-    P.xant.at(i, j, k) = U ? x - sum : (x - sum * hi) * P.rhr.ld(i, j, k);
+    P.xant.at(i, j, k) = U ? x - sum : (x - sum * hi) * rh;
   }
-  if (ANTIDIFF && P.own_vel) {
+  if (hv) {
     P.hinv.at(i, j, k) = hi;
     // reciprocal mean densities of the cell's lower faces, used by every
     // corrective pass of this step (hmx/hmy/hmz of antidiff3d-*-gpubc.f90)
     R hx = R(0), hy = R(0), hz = R(0);
-    if (IN || g.bx || i > 1) P.hmx.at(i, j, k) = hx = rhm(P.h.ld(cx<IN>(g, i - 1), j, k), hc);
-    if (IN || g.by || j > 1) P.hmy.at(i, j, k) = hy = rhm(P.h.ld(i, cy<IN>(g, j - 1), k), hc);
-    if (IN || g.bz || k > 1) P.hmz.at(i, j, k) = hz = rhm(P.h.ld(i, j, cz<IN>(g, k - 1)), hc);
+    if (fxe) P.hmx.at(i, j, k) = hx = rhm(hxm, hc);
+    if (fye) P.hmy.at(i, j, k) = hy = rhm(hym, hc);
+    if (fze) P.hmz.at(i, j, k) = hz = rhm(hzm, hc);
     if (P.gv) velgroup_body<R, IN>(P, i, j, k, hx, hy, hz);
   }
   if (HALO && !IN) {
@@ -263,7 +271,10 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
 #define AX(f, b, c) fx<R, AIN, IN>(g, A1, (f), (b), (c))
 #define AY(a, f, c) fy<R, AIN, IN>(g, A2, (a), (f), (c))
 #define AZ(a, b, f) fz<R, AIN, IN>(g, A3, (a), (b), (f))
-  if (IN || g.bx || i > 1) {
+  // results held until every load is issued (see limit_form)
+  R vo[3] = {R(0), R(0), R(0)}, fo[3] = {R(0), R(0), R(0)};
+  const bool fxe = IN || g.bx || i > 1, fye = IN || g.by || j > 1, fze = IN || g.bz || k > 1;
+  if (fxe) {
     const R hmx = P.hmx.ld(i, j, k);
     const R a = AX(i, j, k);
     R v;
@@ -282,7 +293,7 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
                        fabs(XX(i - 1, j, k + 1)) + fabs(XX(i, j, k + 1)) + fabs(XX(i - 1, j, k - 1)) +
                            fabs(XX(i, j, k - 1)) + ep,
                        hmx);
-      P.f1.at(i, j, k) = donor(XX(i - 1, j, k), XX(i, j, k), v);
+      fo[0] = donor(XX(i - 1, j, k), XX(i, j, k), v);
     } else {
       const R d2 = PS ? P.cp.ld(i, j + 1, k) - P.cp.ld(i, j - 1, k)
                       : dif4(XX(i - 1, j - 1, k), XX(i, j - 1, k), XX(i - 1, j + 1, k), XX(i, j + 1, k));
@@ -298,9 +309,9 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
       else
         v = vdyf_u<U>(XX(i - 1, j, k), XX(i, j, k), a, hmx) - hmul<U>(R(0.03125) * a, hmx) * cr;
     }
-    P.v1.at(i, j, k) = v;
+    vo[0] = v;
   }
-  if (IN || g.by || j > 1) {
+  if (fye) {
     const R hmy = P.hmy.ld(i, j, k);
     const R a = AY(i, j, k);
     R v;
@@ -319,7 +330,7 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
                        fabs(XX(i, j - 1, k + 1)) + fabs(XX(i, j, k + 1)) + fabs(XX(i, j - 1, k - 1)) +
                            fabs(XX(i, j, k - 1)) + ep,
                        hmy);
-      P.f2.at(i, j, k) = donor(XX(i, j - 1, k), XX(i, j, k), v);
+      fo[1] = donor(XX(i, j - 1, k), XX(i, j, k), v);
     } else {
       const R d1 = PS ? P.cn.ld(i + 1, j, k) - P.cn.ld(i - 1, j, k)
                       : dif4(XX(i - 1, j - 1, k), XX(i - 1, j, k), XX(i + 1, j - 1, k), XX(i + 1, j, k));
@@ -335,9 +346,9 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
       else
         v = vdyf_u<U>(XX(i, j - 1, k), XX(i, j, k), a, hmy) - hmul<U>(R(0.03125) * a, hmy) * cr;
     }
-    P.v2.at(i, j, k) = v;
+    vo[1] = v;
   }
-  if (IN || g.bz || k > 1) {
+  if (fze) {
     const R hmz = P.hmz.ld(i, j, k);
     const R a = AZ(i, j, k);
     R v;
@@ -355,7 +366,7 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
                  fabs(XX(i, j + 1, k - 1)) + fabs(XX(i, j + 1, k)) + fabs(XX(i, j - 1, k - 1)) +
                      fabs(XX(i, j - 1, k)) + ep,
                  hmz);
-      P.f3.at(i, j, k) = donor(XX(i, j, k - 1), XX(i, j, k), v);
+      fo[2] = donor(XX(i, j, k - 1), XX(i, j, k), v);
     } else {
       const R d1 = PS ? P.q.ld(i + 1, j, k) - P.q.ld(i - 1, j, k)
                       : dif4(XX(i - 1, j, k - 1), XX(i - 1, j, k), XX(i + 1, j, k - 1), XX(i + 1, j, k));
@@ -368,7 +379,19 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
       else
         v = vdyf_u<U>(XX(i, j, k - 1), XX(i, j, k), a, hmz) - hmul<U>(R(0.03125) * a, hmz) * cr;
     }
-    P.v3.at(i, j, k) = v;
+    vo[2] = v;
+  }
+  if (fxe) {
+    P.v1.at(i, j, k) = vo[0];
+    if (STD) P.f1.at(i, j, k) = fo[0];
+  }
+  if (fye) {
+    P.v2.at(i, j, k) = vo[1];
+    if (STD) P.f2.at(i, j, k) = fo[1];
+  }
+  if (fze) {
+    P.v3.at(i, j, k) = vo[2];
+    if (STD) P.f3.at(i, j, k) = fo[2];
   }
 #undef XX
 #undef AX
@@ -403,8 +426,11 @@ __device__ __forceinline__ RatioOps<R> bounds_body(const Prob<R>& P, int i, int 
   const Geo& g = P.g;
   const Arr<R>& X = P.xant;
   const R x = X.ld(i, j, k);
-  P.q.at(i, j, k) = (P.rho || U) ? x : div1(x, P.rhr.ld(i, j, k));  // x/1 == x for the density step
-  if (!NONOS) return {};
+  const R qv = (P.rho || U) ? x : div1(x, P.rhr.ld(i, j, k));  // x/1 == x for the density step
+  if (!NONOS) {
+    P.q.at(i, j, k) = qv;
+    return {};
+  }
   const bool lo = IN || g.bz || k > 1, hi = IN || g.bz || k < g.lp;
   R ma, mi;
   if (FIRST) {
@@ -438,10 +464,6 @@ __device__ __forceinline__ RatioOps<R> bounds_body(const Prob<R>& P, int i, int 
     ma = mx2(P.mx.ld(i, j, k), e.max());
     mi = mn2(P.mn.ld(i, j, k), e.min());
   }
-  if (KEEP) {
-    P.mx.at(i, j, k) = ma;
-    P.mn.at(i, j, k) = mi;
-  }
   // fluxes for the bounds: std -> donor fluxes f*ns, gauge -> v itself
   const Arr<R>& F1 = P.stdf ? P.f1 : P.v1;
   const Arr<R>& F2 = P.stdf ? P.f2 : P.v2;
@@ -451,6 +473,12 @@ __device__ __forceinline__ RatioOps<R> bounds_body(const Prob<R>& P, int i, int 
   const R e2 = fy<R, false, IN>(g, F2, i, j + 1, k), w2 = fy<R, false, IN>(g, F2, i, j, k);
   const R e3 = fz<R, false, IN>(g, F3, i, j, k + 1), w3 = fz<R, false, IN>(g, F3, i, j, k);
   const R hc = U ? R(1) : P.h.ld(i, j, k);
+  // the stores follow every load (see limit_form)
+  P.q.at(i, j, k) = qv;
+  if (KEEP) {
+    P.mx.at(i, j, k) = ma;
+    P.mn.at(i, j, k) = mi;
+  }
   const R np_ = U ? ma - x : (ma - x) * hc, nn = U ? x - mi : (x - mi) * hc;
   R dp, dn;
   if constexpr (sizeof(R) == 8) {
@@ -553,43 +581,41 @@ template <class R, bool STD, bool NONOS, bool IN = false>
 __device__ __forceinline__ void limit_form(const Prob<R>& P, int i, int j, int k) {
   const Geo& g = P.g;
   const Arr<R>& X = P.xant;
+  // every load before the first store: the arrays may alias as far as the
+  // compiler knows, and a store would otherwise fence the next face's loads
   const R cpc = NONOS ? P.cp.ld(i, j, k) : R(0), cnc = NONOS ? P.cn.ld(i, j, k) : R(0);
   const R xc = X.ld(i, j, k), qc = STD ? P.q.ld(i, j, k) : R(0);
-  if (IN || g.bx || i > 1) {
-    const int im = IN ? i - 1 : wrapi(i - 1, g.np);
-    const R v = P.v1.ld(i, j, k);
-    R w = v;
-    if (NONOS) {
-      const R cpm = P.cp.ld(im, j, k), cnm = P.cn.ld(im, j, k);
-      w = STD ? vlim_std(v, min3(cpc, cnm), min3(cpm, cnc), X.ld(im, j, k), xc)
-              : donor(min3(cpc, cnm), min3(cpm, cnc), v);
-    }
-    P.w1.at(i, j, k) = w;
-    if (STD) P.f1.at(i, j, k) = donor(P.q.ld(im, j, k), qc, w);
+  const bool fx_ = IN || g.bx || i > 1, fy_ = IN || g.by || j > 1, fz_ = IN || g.bz || k > 1;
+  const int im = IN ? i - 1 : wrapi(i - 1, g.np), jm = IN ? j - 1 : wrapi(j - 1, g.mp),
+            km = IN ? k - 1 : wrapi(k - 1, g.lp);
+  R w[3] = {R(0), R(0), R(0)}, f[3] = {R(0), R(0), R(0)};
+#define LIMIT_FACE(d, V, I, J, K)                                                      \
+  {                                                                                    \
+    const R v = V.ld(i, j, k);                                                         \
+    R ww = v;                                                                          \
+    if (NONOS) {                                                                       \
+      const R cpm = P.cp.ld(I, J, K), cnm = P.cn.ld(I, J, K);                          \
+      ww = STD ? vlim_std(v, min3(cpc, cnm), min3(cpm, cnc), X.ld(I, J, K), xc)         \
+               : donor(min3(cpc, cnm), min3(cpm, cnc), v);                             \
+    }                                                                                  \
+    w[d] = ww;                                                                         \
+    if (STD) f[d] = donor(P.q.ld(I, J, K), qc, ww);                                    \
   }
-  if (IN || g.by || j > 1) {
-    const int jm = IN ? j - 1 : wrapi(j - 1, g.mp);
-    const R v = P.v2.ld(i, j, k);
-    R w = v;
-    if (NONOS) {
-      const R cpm = P.cp.ld(i, jm, k), cnm = P.cn.ld(i, jm, k);
-      w = STD ? vlim_std(v, min3(cpc, cnm), min3(cpm, cnc), X.ld(i, jm, k), xc)
-              : donor(min3(cpc, cnm), min3(cpm, cnc), v);
-    }
-    P.w2.at(i, j, k) = w;
-    if (STD) P.f2.at(i, j, k) = donor(P.q.ld(i, jm, k), qc, w);
+  if (fx_) LIMIT_FACE(0, P.v1, im, j, k)
+  if (fy_) LIMIT_FACE(1, P.v2, i, jm, k)
+  if (fz_) LIMIT_FACE(2, P.v3, i, j, km)
+#undef LIMIT_FACE
+  if (fx_) {
+    P.w1.at(i, j, k) = w[0];
+    if (STD) P.f1.at(i, j, k) = f[0];
   }
-  if (IN || g.bz || k > 1) {
-    const int km = IN ? k - 1 : wrapi(k - 1, g.lp);
-    const R v = P.v3.ld(i, j, k);
-    R w = v;
-    if (NONOS) {
-      const R cpm = P.cp.ld(i, j, km), cnm = P.cn.ld(i, j, km);
-      w = STD ? vlim_std(v, min3(cpc, cnm), min3(cpm, cnc), X.ld(i, j, km), xc)
-              : donor(min3(cpc, cnm), min3(cpm, cnc), v);
-    }
-    P.w3.at(i, j, k) = w;
-    if (STD) P.f3.at(i, j, k) = donor(P.q.ld(i, j, km), qc, w);
+  if (fy_) {
+    P.w2.at(i, j, k) = w[1];
+    if (STD) P.f2.at(i, j, k) = f[1];
+  }
+  if (fz_) {
+    P.w3.at(i, j, k) = w[2];
+    if (STD) P.f3.at(i, j, k) = f[2];
   }
 }
 

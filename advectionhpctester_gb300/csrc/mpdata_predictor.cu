@@ -18,13 +18,18 @@ __device__ __forceinline__ void pred_level_cell(long lev, long off, R* ox, R* oy
                                                 R hg3, R r) {
   R* o[3] = {ox, oy, oz};
   const R hg[3] = {hg1, hg2, hg3};
+  // the six loads first: a store could alias them as far as the compiler knows
+  R l0[3], l2[3];
 #pragma unroll
   for (int c = 0; c < 3; c++) {
-    R* p0 = o[c] + off;
-    const R a0 = U ? p0[0] : p0[0] * hc;
-    const R a2 = p0[2 * lev];
-    const R a1 = a0 + (R1 ? a0 - a2 : r * (a0 - a2));
-    p0[lev] = (a1 + a0) * hg[c];
+    l0[c] = o[c][off];
+    l2[c] = o[c][off + 2 * lev];
+  }
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const R a0 = U ? l0[c] : l0[c] * hc;
+    const R a1 = a0 + (R1 ? a0 - l2[c] : r * (a0 - l2[c]));
+    o[c][off + lev] = (a1 + a0) * hg[c];
   }
 }
 
@@ -68,16 +73,22 @@ __device__ __forceinline__ void roll_cell(long lev, R* ox, R* oy, R* oz, R* pu, 
   const R hc = U ? R(1) : h.ld(i, j, k);
   R* o[3] = {ox, oy, oz};
   R* p[3] = {pu, pv, pw};
+  R q0[3], p0[3] = {R(0), R(0), R(0)}, p2[3] = {R(0), R(0), R(0)};
+#pragma unroll
+  for (int c = 0; c < 3; c++) {  // loads first
+    q0[c] = o[c][off];
+    if (p[c]) {
+      p0[c] = p[c][off];
+      p2[c] = p[c][off + 2 * lev];
+    }
+  }
 #pragma unroll
   for (int c = 0; c < 3; c++) {
     if (p[c]) {
-      R* q = p[c] + off;
-      const R p0 = q[0], p2 = q[2 * lev];
-      q[lev] = p0 + r * (p0 - p2);
-      q[2 * lev] = p0;
+      p[c][off + lev] = p0[c] + r * (p0[c] - p2[c]);
+      p[c][off + 2 * lev] = p0[c];
     }
-    R* q = o[c] + off;
-    q[2 * lev] = U ? q[0] : q[0] * hc;
+    o[c][off + 2 * lev] = U ? q0[c] : q0[c] * hc;
   }
 }
 
@@ -93,47 +104,59 @@ __global__ void __launch_bounds__(128) k_pred_cgrid(Geo g, long lev, R* ox, R* o
   if (i > g.np + 1 || j > g.mp + 1) return;
   // level-1 views (ox etc. point at the logical (1,1,1) of level 0)
   const Arr<R> A1{ox + lev, h.sy, h.sz}, A2{oy + lev, h.sy, h.sz}, A3{oz + lev, h.sy, h.sz};
-  if (j <= g.mp && k <= g.lp) {
-    R a, b;
+  // every face's loads, then its stores (a store would fence later loads)
+  const bool e1 = j <= g.mp && k <= g.lp, e2 = i <= g.np && k <= g.lp, e3 = i <= g.np && j <= g.mp;
+  R a1 = R(0), b1 = R(0), a2 = R(0), b2 = R(0), a3 = R(0), b3 = R(0);
+  if (e1) {
     if (g.bx) {
       const int ii = i > g.np ? 1 : i;
-      a = A1.ld(ii, j, k);
-      b = A1.ld(wrapi(ii - 1, g.np), j, k);
+      a1 = A1.ld(ii, j, k);
+      b1 = A1.ld(wrapi(ii - 1, g.np), j, k);
     } else {
-      a = i <= g.np ? A1.ld(i, j, k) : R(2) * A1.ld(g.np, j, k) - A1.ld(g.np - 1, j, k);
-      b = i > 1 ? A1.ld(i - 1, j, k) : R(2) * A1.ld(1, j, k) - A1.ld(2, j, k);
-      if (i == 1) A1.at(0, j, k) = b;
-      if (i == g.np + 1) A1.at(g.np + 1, j, k) = a;
+      a1 = i <= g.np ? A1.ld(i, j, k) : R(2) * A1.ld(g.np, j, k) - A1.ld(g.np - 1, j, k);
+      b1 = i > 1 ? A1.ld(i - 1, j, k) : R(2) * A1.ld(1, j, k) - A1.ld(2, j, k);
     }
-    u1.at(i, j, k) = R(0.5) * (a + b);
   }
-  if (i <= g.np && k <= g.lp) {
-    R a, b;
+  if (e2) {
     if (g.by) {
       const int jj = j > g.mp ? 1 : j;
-      a = A2.ld(i, jj, k);
-      b = A2.ld(i, wrapi(jj - 1, g.mp), k);
+      a2 = A2.ld(i, jj, k);
+      b2 = A2.ld(i, wrapi(jj - 1, g.mp), k);
     } else {
-      a = j <= g.mp ? A2.ld(i, j, k) : R(2) * A2.ld(i, g.mp, k) - A2.ld(i, g.mp - 1, k);
-      b = j > 1 ? A2.ld(i, j - 1, k) : R(2) * A2.ld(i, 1, k) - A2.ld(i, 2, k);
-      if (j == 1) A2.at(i, 0, k) = b;
-      if (j == g.mp + 1) A2.at(i, g.mp + 1, k) = a;
+      a2 = j <= g.mp ? A2.ld(i, j, k) : R(2) * A2.ld(i, g.mp, k) - A2.ld(i, g.mp - 1, k);
+      b2 = j > 1 ? A2.ld(i, j - 1, k) : R(2) * A2.ld(i, 1, k) - A2.ld(i, 2, k);
     }
-    u2.at(i, j, k) = R(0.5) * (a + b);
   }
-  if (i <= g.np && j <= g.mp) {
-    R a, b;
+  if (e3) {
     if (g.bz) {
       const int kk = k > g.lp ? 1 : k;
-      a = A3.ld(i, j, kk);
-      b = A3.ld(i, j, wrapi(kk - 1, g.lp));
+      a3 = A3.ld(i, j, kk);
+      b3 = A3.ld(i, j, wrapi(kk - 1, g.lp));
     } else {
-      a = k <= g.lp ? A3.ld(i, j, k) : R(2) * A3.ld(i, j, g.lp) - A3.ld(i, j, g.lp - 1);
-      b = k > 1 ? A3.ld(i, j, k - 1) : R(2) * A3.ld(i, j, 1) - A3.ld(i, j, 2);
-      if (k == 1) A3.at(i, j, 0) = b;
-      if (k == g.lp + 1) A3.at(i, j, g.lp + 1) = a;
+      a3 = k <= g.lp ? A3.ld(i, j, k) : R(2) * A3.ld(i, j, g.lp) - A3.ld(i, j, g.lp - 1);
+      b3 = k > 1 ? A3.ld(i, j, k - 1) : R(2) * A3.ld(i, j, 1) - A3.ld(i, j, 2);
     }
-    u3.at(i, j, k) = R(0.5) * (a + b);
+  }
+  if (e1) {
+    if (!g.bx) {
+      if (i == 1) A1.at(0, j, k) = b1;
+      if (i == g.np + 1) A1.at(g.np + 1, j, k) = a1;
+    }
+    u1.at(i, j, k) = R(0.5) * (a1 + b1);
+  }
+  if (e2) {
+    if (!g.by) {
+      if (j == 1) A2.at(i, 0, k) = b2;
+      if (j == g.mp + 1) A2.at(i, g.mp + 1, k) = a2;
+    }
+    u2.at(i, j, k) = R(0.5) * (a2 + b2);
+  }
+  if (e3) {
+    if (!g.bz) {
+      if (k == 1) A3.at(i, j, 0) = b3;
+      if (k == g.lp + 1) A3.at(i, j, g.lp + 1) = a3;
+    }
+    u3.at(i, j, k) = R(0.5) * (a3 + b3);
   }
   if (rl) {
     if (unit)
