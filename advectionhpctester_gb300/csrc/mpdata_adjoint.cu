@@ -832,7 +832,7 @@ __global__ void __launch_bounds__(128, KfPseudoMinBlocks<R>::v) kf_pseudo(const 
 // recomputes its quotients from the recorded extrema and fluxes.
 template <class R, bool NONOS, bool FIRST, bool KEEP>
 __global__ void __launch_bounds__(128) kf_bounds(const Prob<R> P) {
-  if constexpr (NONOS && sizeof(R) == 8) {
+  if constexpr (NONOS && sizeof(R) == 8) {  // FP32: per-lane quotients are cheaper than the barriers
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     const int k = blockIdx.z + 1;

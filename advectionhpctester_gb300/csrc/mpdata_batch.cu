@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(256) kb_pseudo(BATCH_ARGS) {
 }
 template <class R, bool NONOS, bool FIRST, bool KEEP>
 __global__ void __launch_bounds__(256) kb_bounds(BATCH_ARGS) {
-  if constexpr (NONOS && sizeof(R) == 8) {
+  if constexpr (NONOS && sizeof(R) == 8) {  // FP32: per-lane quotients are cheaper than the barriers
     __shared__ __align__(16) unsigned char sraw[sizeof(Prob<R>)];
     Prob<R>& P = *reinterpret_cast<Prob<R>*>(sraw);
     const unsigned long long w = __ldg(tiles + blockIdx.x);

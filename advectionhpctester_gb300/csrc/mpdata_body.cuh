@@ -518,10 +518,11 @@ __device__ __forceinline__ RatioOps<R> bounds_body(const Prob<R>& P, int i, int 
 // operand pairs into shared memory, the first warps divide them, 32 at a time,
 // and every cell stores its two ratios.  Every thread of the block, inside
 // the domain or not, reaches the barriers.
-__device__ __forceinline__ void block_ratios(const Prob<double>& P, int i, int j, int k, bool valid,
-                                             const RatioOps<double>& r) {
+template <class R>
+__device__ __forceinline__ void block_ratios(const Prob<R>& P, int i, int j, int k, bool valid,
+                                             const RatioOps<R>& r) {
   __shared__ int s_cnt[8];
-  __shared__ double s_n[512], s_d[512];
+  __shared__ R s_n[512], s_d[512];
   const int nt = blockDim.x * blockDim.y, tid = threadIdx.y * blockDim.x + threadIdx.x;
   const int lane = tid & 31, w = tid >> 5, nw = nt >> 5;
   const bool dp = valid && !ratio_ge1(r.np, r.dp), dn = valid && !ratio_ge1(r.nn, r.dn);
@@ -548,8 +549,8 @@ __device__ __forceinline__ void block_ratios(const Prob<double>& P, int i, int j
   for (int it = tid; it < total; it += nt) s_n[it] = s_n[it] / s_d[it];
   __syncthreads();
   if (valid) {
-    P.cp.at(i, j, k) = dp ? s_n[ip] : double(RATIO_CAP);
-    P.cn.at(i, j, k) = dn ? s_n[in] : double(RATIO_CAP);
+    P.cp.at(i, j, k) = dp ? s_n[ip] : R(RATIO_CAP);
+    P.cn.at(i, j, k) = dn ? s_n[in] : R(RATIO_CAP);
   }
 }
 

@@ -153,11 +153,11 @@ constexpr int RATIO_CAP = 2;
 __device__ __forceinline__ double lim_ratio(double n, double d) {
   return ratio_ge1(n, d) ? double(RATIO_CAP) : div_call(n, d);
 }
-__device__ __forceinline__ float lim_ratio(float n, float d) {
+__device__ __forceinline__ bool ratio_ge1(float n, float d) {
   const int nb = __float_as_int(n), db = __float_as_int(d), inf = 0x7F800000;
-  if (db > 0 && db < inf && nb >= db && nb <= inf) return float(RATIO_CAP);
-  return n / d;
+  return db > 0 && db < inf && nb >= db && nb <= inf;
 }
+__device__ __forceinline__ float lim_ratio(float n, float d) { return ratio_ge1(n, d) ? float(RATIO_CAP) : n / d; }
 
 // ---- point operators (device forms of mpdataoperators.inc:50-96) ----
 __device__ __forceinline__ float donor(float y1, float y2, float a) { return pp(a) * y1 - pn(a) * y2; }

@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(128) k_pairs(const Prob<R> P) {
 }
 template <class R, bool NONOS, bool FIRST, bool KEEP>
 __global__ void __launch_bounds__(128) k_bounds(const Prob<R> P) {
-  if constexpr (NONOS && sizeof(R) == 8) {
+  if constexpr (NONOS && sizeof(R) == 8) {  // FP32: per-lane quotients are cheaper than the barriers
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     const int k = blockIdx.z + 1;
