@@ -73,7 +73,7 @@ __device__ __forceinline__ void load_prob(Prob<R>& sP, const Prob<R>* __restrict
 
 template <class R, bool ANTIDIFF, bool HALO>
 __global__ void __launch_bounds__(256) kb_upwind(BATCH_ARGS) {
-#define B(IN, U) upwind_body<R, ANTIDIFF, HALO, IN, U>(P, i, j, k)
+#define B(IN, U) upwind_body<R, ANTIDIFF, HALO, IN, U, false>(P, i, j, k)
   BATCH_TILE_U(B)
 #undef B
 }
@@ -96,29 +96,29 @@ __device__ __forceinline__ void pseudo_dispatch(const Prob<R>& P, int i, int j, 
   if constexpr (AIN) {
     if (win && P.gv) {  // first pass of a velocity group: velocity-only terms precomputed
       if (P.pairs)
-        pseudo_body<R, AIN, true, false, true, true>(P, i, j, k);
+        pseudo_body<R, AIN, true, false, true, true, false>(P, i, j, k);
       else
-        pseudo_body<R, AIN, true, false, false, true>(P, i, j, k);
+        pseudo_body<R, AIN, true, false, false, true, false>(P, i, j, k);
       return;
     }
   }
   if (!win) {
-    pseudo_body<R, AIN, false>(P, i, j, k);
+    pseudo_body<R, AIN, false, false, false, false, false>(P, i, j, k);
   } else if constexpr (sizeof(R) == 8) {
     const bool unit = warp_unit_faces(P, i, j, k);
     if (P.pairs) {
       if (unit)
-        pseudo_body<R, AIN, true, true, true>(P, i, j, k);
+        pseudo_body<R, AIN, true, true, true, false, false>(P, i, j, k);
       else
-        pseudo_body<R, AIN, true, false, true>(P, i, j, k);
+        pseudo_body<R, AIN, true, false, true, false, false>(P, i, j, k);
     } else {
       if (unit)
-        pseudo_body<R, AIN, true, true>(P, i, j, k);
+        pseudo_body<R, AIN, true, true, false, false, false>(P, i, j, k);
       else
-        pseudo_body<R, AIN, true>(P, i, j, k);
+        pseudo_body<R, AIN, true, false, false, false, false>(P, i, j, k);
     }
   } else {
-    pseudo_body<R, AIN, true>(P, i, j, k);
+    pseudo_body<R, AIN, true, false, false, false, false>(P, i, j, k);
   }
 }
 template <class R, bool AIN>
@@ -150,22 +150,22 @@ __global__ void __launch_bounds__(256) kb_bounds(BATCH_ARGS) {
     RatioOps<R> r{};
     if (valid) {
       if (!win)
-        r = bounds_body<R, true, FIRST, KEEP, false, 2>(P, i, j, k);
+        r = bounds_body<R, true, FIRST, KEEP, false, 2, false, false>(P, i, j, k);
       else if (warp_unit_cell(P, i, j, k))
-        r = bounds_body<R, true, FIRST, KEEP, true, 2, true>(P, i, j, k);
+        r = bounds_body<R, true, FIRST, KEEP, true, 2, true, false>(P, i, j, k);
       else
-        r = bounds_body<R, true, FIRST, KEEP, true, 2>(P, i, j, k);
+        r = bounds_body<R, true, FIRST, KEEP, true, 2, false, false>(P, i, j, k);
     }
     block_ratios(P, i, j, k, valid, r);
   } else {
-#define B(IN, U) bounds_body<R, NONOS, FIRST, KEEP, IN, 1, U>(P, i, j, k)
+#define B(IN, U) bounds_body<R, NONOS, FIRST, KEEP, IN, 1, U, false>(P, i, j, k)
     BATCH_TILE_U(B)
 #undef B
   }
 }
 template <class R, bool NONOS>
 __global__ void __launch_bounds__(256) kb_limit(BATCH_ARGS) {
-#define B(IN) limit_body<R, NONOS, IN>(P, i, j, k)
+#define B(IN) limit_body<R, NONOS, IN, false>(P, i, j, k)
   BATCH_TILE(B)
 #undef B
 }

@@ -172,7 +172,7 @@ __device__ __forceinline__ void velgroup_body(const Prob<R>& P, int i, int j, in
 // step holding the zero-gradient copy of the old boundary values (written by
 // cp_last_to_halo_xy in the antidiffusion); otherwise it keeps bcx/bcy.
 // HALO: write psi's halo at all (off while autotuning).
-template <class R, bool ANTIDIFF, bool HALO, bool IN = false, bool U = false>
+template <class R, bool ANTIDIFF, bool HALO, bool IN = false, bool U = false, bool DEFER = true>
 __device__ __forceinline__ void upwind_body(const Prob<R>& P, int i, int j, int k) {
   const Geo& g = P.g;
   const Arr<R>& psi = P.psi;
@@ -204,9 +204,12 @@ __device__ __forceinline__ void upwind_body(const Prob<R>& P, int i, int j, int 
   // before the first store (see limit_form)
   const bool hv = ANTIDIFF && P.own_vel;
   const bool fxe = IN || g.bx || i > 1, fye = IN || g.by || j > 1, fze = IN || g.bz || k > 1;
-  const R hxm = hv && fxe ? P.h.ld(cx<IN>(g, i - 1), j, k) : R(0);
-  const R hym = hv && fye ? P.h.ld(i, cy<IN>(g, j - 1), k) : R(0);
-  const R hzm = hv && fze ? P.h.ld(i, j, cz<IN>(g, k - 1)) : R(0);
+  R hxm = R(0), hym = R(0), hzm = R(0);
+  if (DEFER) {
+    hxm = hv && fxe ? P.h.ld(cx<IN>(g, i - 1), j, k) : R(0);
+    hym = hv && fye ? P.h.ld(i, cy<IN>(g, j - 1), k) : R(0);
+    hzm = hv && fze ? P.h.ld(i, j, cz<IN>(g, k - 1)) : R(0);
+  }
   const R rh = (P.rho || U) ? R(1) : P.rhr.ld(i, j, k);
   if (P.rho) {
     // mpdata3d-rho-gauge-gpubc.f90:137-210: no rhr, division by h, fluxes kept;
@@ -225,6 +228,11 @@ __device__ __forceinline__ void upwind_body(const Prob<R>& P, int i, int j, int 
     P.xant.at(i, j, k) = U ? x - sum : (x - sum * hi) * rh;
   }
   if (hv) {
+    if (!DEFER) {  // the batch kernels load these after the first store (fewer registers)
+      hxm = fxe ? P.h.ld(cx<IN>(g, i - 1), j, k) : R(0);
+      hym = fye ? P.h.ld(i, cy<IN>(g, j - 1), k) : R(0);
+      hzm = fze ? P.h.ld(i, j, cz<IN>(g, k - 1)) : R(0);
+    }
     P.hinv.at(i, j, k) = hi;
     // reciprocal mean densities of the cell's lower faces, used by every
     // corrective pass of this step (hmx/hmy/hmz of antidiff3d-*-gpubc.f90)
@@ -258,7 +266,8 @@ __device__ __forceinline__ void upwind_body(const Prob<R>& P, int i, int j, int 
 // are read from cp, cn and q, where k_pairs stored them.  GV (gauge, first
 // pass, interior warps of a batch velocity group): the velocity-only terms
 // are read from gvf (velgroup_body).
-template <class R, bool STD, bool AIN, bool IN = false, bool U = false, bool PS = false, bool GV = false>
+template <class R, bool STD, bool AIN, bool IN = false, bool U = false, bool PS = false, bool GV = false,
+          bool DEFER = true>
 __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int k) {
   const Geo& g = P.g;
   const Arr<R>& X = P.xant;
@@ -271,8 +280,21 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
 #define AX(f, b, c) fx<R, AIN, IN>(g, A1, (f), (b), (c))
 #define AY(a, f, c) fy<R, AIN, IN>(g, A2, (a), (f), (c))
 #define AZ(a, b, f) fz<R, AIN, IN>(g, A3, (a), (b), (f))
-  // results held until every load is issued (see limit_form)
+  // DEFER: results held until every load is issued (see limit_form); the
+  // batch kernels, whose launch bound admits 256 threads, store each face at
+  // once, which keeps their register count (and occupancy) lower
   R vo[3] = {R(0), R(0), R(0)}, fo[3] = {R(0), R(0), R(0)};
+  Arr<R> const* const va[3] = {&P.v1, &P.v2, &P.v3};
+  Arr<R> const* const fa[3] = {&P.f1, &P.f2, &P.f3};
+  auto put = [&](int d, R v, R f) {
+    if (DEFER) {
+      vo[d] = v;
+      fo[d] = f;
+    } else {
+      va[d]->at(i, j, k) = v;
+      if (STD) fa[d]->at(i, j, k) = f;
+    }
+  };
   const bool fxe = IN || g.bx || i > 1, fye = IN || g.by || j > 1, fze = IN || g.bz || k > 1;
   if (fxe) {
     const R hmx = P.hmx.ld(i, j, k);
@@ -293,7 +315,7 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
                        fabs(XX(i - 1, j, k + 1)) + fabs(XX(i, j, k + 1)) + fabs(XX(i - 1, j, k - 1)) +
                            fabs(XX(i, j, k - 1)) + ep,
                        hmx);
-      fo[0] = donor(XX(i - 1, j, k), XX(i, j, k), v);
+      put(0, v, donor(XX(i - 1, j, k), XX(i, j, k), v));
     } else {
       const R d2 = PS ? P.cp.ld(i, j + 1, k) - P.cp.ld(i, j - 1, k)
                       : dif4(XX(i - 1, j - 1, k), XX(i, j - 1, k), XX(i - 1, j + 1, k), XX(i, j + 1, k));
@@ -309,7 +331,7 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
       else
         v = vdyf_u<U>(XX(i - 1, j, k), XX(i, j, k), a, hmx) - hmul<U>(R(0.03125) * a, hmx) * cr;
     }
-    vo[0] = v;
+    if (!STD) put(0, v, R(0));
   }
   if (fye) {
     const R hmy = P.hmy.ld(i, j, k);
@@ -330,7 +352,7 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
                        fabs(XX(i, j - 1, k + 1)) + fabs(XX(i, j, k + 1)) + fabs(XX(i, j - 1, k - 1)) +
                            fabs(XX(i, j, k - 1)) + ep,
                        hmy);
-      fo[1] = donor(XX(i, j - 1, k), XX(i, j, k), v);
+      put(1, v, donor(XX(i, j - 1, k), XX(i, j, k), v));
     } else {
       const R d1 = PS ? P.cn.ld(i + 1, j, k) - P.cn.ld(i - 1, j, k)
                       : dif4(XX(i - 1, j - 1, k), XX(i - 1, j, k), XX(i + 1, j - 1, k), XX(i + 1, j, k));
@@ -346,7 +368,7 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
       else
         v = vdyf_u<U>(XX(i, j - 1, k), XX(i, j, k), a, hmy) - hmul<U>(R(0.03125) * a, hmy) * cr;
     }
-    vo[1] = v;
+    if (!STD) put(1, v, R(0));
   }
   if (fze) {
     const R hmz = P.hmz.ld(i, j, k);
@@ -366,7 +388,7 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
                  fabs(XX(i, j + 1, k - 1)) + fabs(XX(i, j + 1, k)) + fabs(XX(i, j - 1, k - 1)) +
                      fabs(XX(i, j - 1, k)) + ep,
                  hmz);
-      fo[2] = donor(XX(i, j, k - 1), XX(i, j, k), v);
+      put(2, v, donor(XX(i, j, k - 1), XX(i, j, k), v));
     } else {
       const R d1 = PS ? P.q.ld(i + 1, j, k) - P.q.ld(i - 1, j, k)
                       : dif4(XX(i - 1, j, k - 1), XX(i - 1, j, k), XX(i + 1, j, k - 1), XX(i + 1, j, k));
@@ -379,19 +401,21 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
       else
         v = vdyf_u<U>(XX(i, j, k - 1), XX(i, j, k), a, hmz) - hmul<U>(R(0.03125) * a, hmz) * cr;
     }
-    vo[2] = v;
+    if (!STD) put(2, v, R(0));
   }
-  if (fxe) {
-    P.v1.at(i, j, k) = vo[0];
-    if (STD) P.f1.at(i, j, k) = fo[0];
-  }
-  if (fye) {
-    P.v2.at(i, j, k) = vo[1];
-    if (STD) P.f2.at(i, j, k) = fo[1];
-  }
-  if (fze) {
-    P.v3.at(i, j, k) = vo[2];
-    if (STD) P.f3.at(i, j, k) = fo[2];
+  if (DEFER) {
+    if (fxe) {
+      P.v1.at(i, j, k) = vo[0];
+      if (STD) P.f1.at(i, j, k) = fo[0];
+    }
+    if (fye) {
+      P.v2.at(i, j, k) = vo[1];
+      if (STD) P.f2.at(i, j, k) = fo[1];
+    }
+    if (fze) {
+      P.v3.at(i, j, k) = vo[2];
+      if (STD) P.f3.at(i, j, k) = fo[2];
+    }
   }
 #undef XX
 #undef AX
@@ -399,12 +423,12 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
 #undef AZ
 }
 
-template <class R, bool AIN, bool IN = false, bool U = false, bool PS = false, bool GV = false>
+template <class R, bool AIN, bool IN = false, bool U = false, bool PS = false, bool GV = false, bool DEFER = true>
 __device__ __forceinline__ void pseudo_body(const Prob<R>& P, int i, int j, int k) {
   if (P.stdf)
-    pseudo_form<R, true, AIN, IN, U>(P, i, j, k);
+    pseudo_form<R, true, AIN, IN, U, false, false, DEFER>(P, i, j, k);
   else
-    pseudo_form<R, false, AIN, IN, U, PS, GV>(P, i, j, k);
+    pseudo_form<R, false, AIN, IN, U, PS, GV, DEFER>(P, i, j, k);
 }
 
 // ---- limiter bounds and ratios (std :256-348, gauge :238-324) -------------
@@ -421,16 +445,15 @@ template <class R>
 struct RatioOps {
   R np, dp, nn, dn;
 };
-template <class R, bool NONOS, bool FIRST, bool KEEP, bool IN = false, int CLM = 0, bool U = false>
+template <class R, bool NONOS, bool FIRST, bool KEEP, bool IN = false, int CLM = 0, bool U = false,
+          bool DEFER = true>
 __device__ __forceinline__ RatioOps<R> bounds_body(const Prob<R>& P, int i, int j, int k) {
   const Geo& g = P.g;
   const Arr<R>& X = P.xant;
   const R x = X.ld(i, j, k);
   const R qv = (P.rho || U) ? x : div1(x, P.rhr.ld(i, j, k));  // x/1 == x for the density step
-  if (!NONOS) {
-    P.q.at(i, j, k) = qv;
-    return {};
-  }
+  if (!NONOS || !DEFER) P.q.at(i, j, k) = qv;
+  if (!NONOS) return {};
   const bool lo = IN || g.bz || k > 1, hi = IN || g.bz || k < g.lp;
   R ma, mi;
   if (FIRST) {
@@ -464,6 +487,10 @@ __device__ __forceinline__ RatioOps<R> bounds_body(const Prob<R>& P, int i, int 
     ma = mx2(P.mx.ld(i, j, k), e.max());
     mi = mn2(P.mn.ld(i, j, k), e.min());
   }
+  if (KEEP && !DEFER) {
+    P.mx.at(i, j, k) = ma;
+    P.mn.at(i, j, k) = mi;
+  }
   // fluxes for the bounds: std -> donor fluxes f*ns, gauge -> v itself
   const Arr<R>& F1 = P.stdf ? P.f1 : P.v1;
   const Arr<R>& F2 = P.stdf ? P.f2 : P.v2;
@@ -473,11 +500,14 @@ __device__ __forceinline__ RatioOps<R> bounds_body(const Prob<R>& P, int i, int 
   const R e2 = fy<R, false, IN>(g, F2, i, j + 1, k), w2 = fy<R, false, IN>(g, F2, i, j, k);
   const R e3 = fz<R, false, IN>(g, F3, i, j, k + 1), w3 = fz<R, false, IN>(g, F3, i, j, k);
   const R hc = U ? R(1) : P.h.ld(i, j, k);
-  // the stores follow every load (see limit_form)
-  P.q.at(i, j, k) = qv;
-  if (KEEP) {
-    P.mx.at(i, j, k) = ma;
-    P.mn.at(i, j, k) = mi;
+  // DEFER: the stores follow every load (see limit_form); the batch kernels
+  // store early, which keeps their register count lower
+  if (DEFER) {
+    P.q.at(i, j, k) = qv;
+    if (KEEP) {
+      P.mx.at(i, j, k) = ma;
+      P.mn.at(i, j, k) = mi;
+    }
   }
   const R np_ = U ? ma - x : (ma - x) * hc, nn = U ? x - mi : (x - mi) * hc;
   R dp, dn;
@@ -578,7 +608,7 @@ __device__ __forceinline__ R vlim_std(R v, R a1, R a2, R xl, R xrr) {
   return donor(a1 * possign(xl) + a2 * possign(-xl), a2 * possign(xrr) + a1 * possign(-xrr), v);
 }
 
-template <class R, bool STD, bool NONOS, bool IN = false>
+template <class R, bool STD, bool NONOS, bool IN = false, bool DEFER = true>
 __device__ __forceinline__ void limit_form(const Prob<R>& P, int i, int j, int k) {
   const Geo& g = P.g;
   const Arr<R>& X = P.xant;
@@ -590,7 +620,7 @@ __device__ __forceinline__ void limit_form(const Prob<R>& P, int i, int j, int k
   const int im = IN ? i - 1 : wrapi(i - 1, g.np), jm = IN ? j - 1 : wrapi(j - 1, g.mp),
             km = IN ? k - 1 : wrapi(k - 1, g.lp);
   R w[3] = {R(0), R(0), R(0)}, f[3] = {R(0), R(0), R(0)};
-#define LIMIT_FACE(d, V, I, J, K)                                                      \
+#define LIMIT_FACE(d, V, WA, FA, I, J, K)                                              \
   {                                                                                    \
     const R v = V.ld(i, j, k);                                                         \
     R ww = v;                                                                          \
@@ -601,11 +631,16 @@ __device__ __forceinline__ void limit_form(const Prob<R>& P, int i, int j, int k
     }                                                                                  \
     w[d] = ww;                                                                         \
     if (STD) f[d] = donor(P.q.ld(I, J, K), qc, ww);                                    \
+    if (!DEFER) {                                                                      \
+      WA.at(i, j, k) = ww;                                                             \
+      if (STD) FA.at(i, j, k) = f[d];                                                  \
+    }                                                                                  \
   }
-  if (fx_) LIMIT_FACE(0, P.v1, im, j, k)
-  if (fy_) LIMIT_FACE(1, P.v2, i, jm, k)
-  if (fz_) LIMIT_FACE(2, P.v3, i, j, km)
+  if (fx_) LIMIT_FACE(0, P.v1, P.w1, P.f1, im, j, k)
+  if (fy_) LIMIT_FACE(1, P.v2, P.w2, P.f2, i, jm, k)
+  if (fz_) LIMIT_FACE(2, P.v3, P.w3, P.f3, i, j, km)
 #undef LIMIT_FACE
+  if (!DEFER) return;
   if (fx_) {
     P.w1.at(i, j, k) = w[0];
     if (STD) P.f1.at(i, j, k) = f[0];
@@ -620,12 +655,12 @@ __device__ __forceinline__ void limit_form(const Prob<R>& P, int i, int j, int k
   }
 }
 
-template <class R, bool NONOS, bool IN = false>
+template <class R, bool NONOS, bool IN = false, bool DEFER = true>
 __device__ __forceinline__ void limit_body(const Prob<R>& P, int i, int j, int k) {
   if (P.stdf)
-    limit_form<R, true, NONOS, IN>(P, i, j, k);
+    limit_form<R, true, NONOS, IN, DEFER>(P, i, j, k);
   else
-    limit_form<R, false, NONOS, IN>(P, i, j, k);
+    limit_form<R, false, NONOS, IN, DEFER>(P, i, j, k);
 }
 
 // ---- corrective update (std :431-459, gauge :364-368/396-400/423-427) -----
