@@ -603,9 +603,13 @@ __device__ __forceinline__ void pairs_body(const Prob<R>& P, int i, int j, int k
 // std: antidiff3d-standard-gpubc.f90:372-407 (sign-aware limited velocity,
 // donor flux of x/rhr); gauge: antidiff3d-gauge-gpubc.f90:343-363 (the
 // limited velocity is the flux).  Lower faces of each cell.
+// The reference's factors a1*possign(xl) + a2*possign(-xl) and
+// a2*possign(xrr) + a1*possign(-xrr) multiply by 1 and 0.  a1 and a2 are min3
+// values of non-negative ratios (never -0), so each factor is exactly a1 + +0
+// or +0 + a2, that is one of a1, a2 chosen by a sign bit.
 template <class R>
 __device__ __forceinline__ R vlim_std(R v, R a1, R a2, R xl, R xrr) {
-  return donor(a1 * possign(xl) + a2 * possign(-xl), a2 * possign(xrr) + a1 * possign(-xrr), v);
+  return donor(sgn(xl) ? a2 : a1, sgn(xrr) ? a1 : a2, v);
 }
 
 template <class R, bool STD, bool NONOS, bool IN = false, bool DEFER = true>
