@@ -94,11 +94,19 @@ __global__ void __launch_bounds__(256) kb_copy(BATCH_ARGS) {
 template <class R, bool AIN>
 __device__ __forceinline__ void pseudo_dispatch(const Prob<R>& P, int i, int j, int k, bool win) {
   if constexpr (AIN) {
-    if (win && P.gv) {  // first pass of a velocity group: velocity-only terms precomputed
-      if (P.pairs)
-        pseudo_body<R, AIN, true, false, true, true, false>(P, i, j, k);
-      else
-        pseudo_body<R, AIN, true, false, false, true, false>(P, i, j, k);
+    // first pass of a velocity group: its form's velocity-only terms are precomputed
+    if (win && (P.stdf ? (P.gv & 2) : (P.gv & 1))) {
+      if (warp_unit_faces(P, i, j, k)) {
+        if (P.pairs)
+          pseudo_body<R, AIN, true, true, true, true, false>(P, i, j, k);
+        else
+          pseudo_body<R, AIN, true, true, false, true, false>(P, i, j, k);
+      } else {
+        if (P.pairs)
+          pseudo_body<R, AIN, true, false, true, true, false>(P, i, j, k);
+        else
+          pseudo_body<R, AIN, true, false, false, true, false>(P, i, j, k);
+      }
       return;
     }
   }

@@ -27,8 +27,8 @@ struct Prob {
   int rho;      // density step of mpdata3d_rho_gauge_gpubc: no rhr, upwind fluxes kept
   int pairs;    // gauge pseudo-velocity: pair sums of xant in cp, cn, q (k_pairs)
   int gv;       // batch velocity group: the velocity-only terms of the first
-                // pass's gauge pseudo-velocities are in gvf (the group owner's
-                // upwind stores them)
+                // pass's pseudo-velocities, stored by the group owner's upwind:
+                // bit 0 the gauge form's (gvf), bit 1 the standard form's (gvs)
   Arr<R> psi, u1, u2, u3, h, rhr;
   const R* bcx;
   const R* bcy;
@@ -36,6 +36,8 @@ struct Prob {
   Arr<R> gvf[12];               // per face direction d = x, y, z (index 4d): the two
                                 // 4-face sums of the cross terms, (|a|-a*a*hm)/2 and
                                 // 0.03125*a*hm (velocity group, shared)
+  Arr<R> gvs[9];                // standard form, per face direction (index 3d):
+                                // |a|-a*a*hm and (0.125*a)*b of the two cross terms
   Arr<R> xant, v1, v2, v3, f1, f2, f3, w1, w2, w3, cp, cn, mx, mn, q;
   // density step only: outputs and the upwind fluxes of the faces n+1
   Arr<R> x_incomp, rhoadv, rhr_out, pexe, pexr1, pexr2;
@@ -103,6 +105,18 @@ __device__ __forceinline__ bool warp_interior(const Geo& g, int i, int j, int k)
   return __all_sync(0xffffffffu, in);
 }
 
+// The standard form's pseudo-velocity pieces with their velocity-only
+// factors precomputed (a batch velocity group, gvs): vdyfa with
+// ka = |a|-a*a*hm, vcorra with bc = (0.125*a)*b.  Same operations, same order.
+template <class R>
+__device__ __forceinline__ R vdyfa_k(R x1, R x2, R ka, R ep) {
+  return ka * (fabs(x2) - fabs(x1)) / (fabs(x2) + fabs(x1) + ep);
+}
+template <bool U, class R>
+__device__ __forceinline__ R vcorra_b(R bc, R y1, R y2, R hm) {
+  return -(hmul<U>(bc * y1, hm) / y2);
+}
+
 // True when hmx, hmy and hmz are exactly 1 at every cell of the warp (FP64
 // only; FP32 kernels are bound by instruction issue and keep the products).
 template <class R>
@@ -141,26 +155,59 @@ __device__ __forceinline__ void velgroup_body(const Prob<R>& P, int i, int j, in
 #define AX(f, b, c) fx<R, true, IN>(g, P.u1, (f), (b), (c))
 #define AY(a, f, c) fy<R, true, IN>(g, P.u2, (a), (f), (c))
 #define AZ(a, b, f) fz<R, true, IN>(g, P.u3, (a), (b), (f))
+  // the standard form's vdyfa factor |a|-a*a*hm and vcorra's (0.125*a)*b
+  // keep their own operation order (no scaling is moved)
+  const bool gg = P.gv & 1, gs = P.gv & 2;
   if (IN || g.bx || i > 1) {
     const R a = AX(i, j, k);
-    P.gvf[0].at(i, j, k) = AY(i - 1, j, k) + AY(i - 1, j + 1, k) + AY(i, j + 1, k) + AY(i, j, k);
-    P.gvf[1].at(i, j, k) = AZ(i - 1, j, k) + AZ(i - 1, j, k + 1) + AZ(i, j, k + 1) + AZ(i, j, k);
-    P.gvf[2].at(i, j, k) = (fabs(a) - a * a * hx) * R(0.5);
-    P.gvf[3].at(i, j, k) = R(0.03125) * a * hx;
+    const R b1 = AY(i - 1, j, k) + AY(i - 1, j + 1, k) + AY(i, j + 1, k) + AY(i, j, k);
+    const R b2 = AZ(i - 1, j, k) + AZ(i - 1, j, k + 1) + AZ(i, j, k + 1) + AZ(i, j, k);
+    const R ka = fabs(a) - a * a * hx;
+    if (gg) {
+      P.gvf[0].at(i, j, k) = b1;
+      P.gvf[1].at(i, j, k) = b2;
+      P.gvf[2].at(i, j, k) = ka * R(0.5);
+      P.gvf[3].at(i, j, k) = R(0.03125) * a * hx;
+    }
+    if (gs) {
+      P.gvs[0].at(i, j, k) = ka;
+      P.gvs[1].at(i, j, k) = R(0.125) * a * b1;
+      P.gvs[2].at(i, j, k) = R(0.125) * a * b2;
+    }
   }
   if (IN || g.by || j > 1) {
     const R a = AY(i, j, k);
-    P.gvf[4].at(i, j, k) = AX(i, j - 1, k) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j - 1, k);
-    P.gvf[5].at(i, j, k) = AZ(i, j - 1, k) + AZ(i, j, k) + AZ(i, j, k + 1) + AZ(i, j - 1, k + 1);
-    P.gvf[6].at(i, j, k) = (fabs(a) - a * a * hy) * R(0.5);
-    P.gvf[7].at(i, j, k) = R(0.03125) * a * hy;
+    const R b1 = AX(i, j - 1, k) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j - 1, k);
+    const R b2 = AZ(i, j - 1, k) + AZ(i, j, k) + AZ(i, j, k + 1) + AZ(i, j - 1, k + 1);
+    const R ka = fabs(a) - a * a * hy;
+    if (gg) {
+      P.gvf[4].at(i, j, k) = b1;
+      P.gvf[5].at(i, j, k) = b2;
+      P.gvf[6].at(i, j, k) = ka * R(0.5);
+      P.gvf[7].at(i, j, k) = R(0.03125) * a * hy;
+    }
+    if (gs) {
+      P.gvs[3].at(i, j, k) = ka;
+      P.gvs[4].at(i, j, k) = R(0.125) * a * b1;
+      P.gvs[5].at(i, j, k) = R(0.125) * a * b2;
+    }
   }
   if (IN || g.bz || k > 1) {
     const R a = AZ(i, j, k);
-    P.gvf[8].at(i, j, k) = AX(i, j, k - 1) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j, k - 1);
-    P.gvf[9].at(i, j, k) = AY(i, j, k - 1) + AY(i, j + 1, k - 1) + AY(i, j + 1, k) + AY(i, j, k);
-    P.gvf[10].at(i, j, k) = (fabs(a) - a * a * hz) * R(0.5);
-    P.gvf[11].at(i, j, k) = R(0.03125) * a * hz;
+    const R b1 = AX(i, j, k - 1) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j, k - 1);
+    const R b2 = AY(i, j, k - 1) + AY(i, j + 1, k - 1) + AY(i, j + 1, k) + AY(i, j, k);
+    const R ka = fabs(a) - a * a * hz;
+    if (gg) {
+      P.gvf[8].at(i, j, k) = b1;
+      P.gvf[9].at(i, j, k) = b2;
+      P.gvf[10].at(i, j, k) = ka * R(0.5);
+      P.gvf[11].at(i, j, k) = R(0.03125) * a * hz;
+    }
+    if (gs) {
+      P.gvs[6].at(i, j, k) = ka;
+      P.gvs[7].at(i, j, k) = R(0.125) * a * b1;
+      P.gvs[8].at(i, j, k) = R(0.125) * a * b2;
+    }
   }
 #undef AX
 #undef AY
@@ -301,20 +348,25 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
     const R a = AX(i, j, k);
     R v;
     if (STD) {
-      v = vdyfa_u<U>(XX(i - 1, j, k), XX(i, j, k), a, hmx, ep) +
-          vcorra_u<U>(a, AY(i - 1, j, k) + AY(i - 1, j + 1, k) + AY(i, j + 1, k) + AY(i, j, k),
-                 (fabs(XX(i - 1, j + 1, k)) + fabs(XX(i, j + 1, k))) -
-                     (fabs(XX(i - 1, j - 1, k)) + fabs(XX(i, j - 1, k))),
-                 fabs(XX(i - 1, j + 1, k)) + fabs(XX(i, j + 1, k)) + fabs(XX(i - 1, j - 1, k)) +
-                     fabs(XX(i, j - 1, k)) + ep,
-                 hmx);
-      if (zt)
-        v = v + vcorra_u<U>(a, AZ(i - 1, j, k) + AZ(i - 1, j, k + 1) + AZ(i, j, k + 1) + AZ(i, j, k),
-                       (fabs(XX(i - 1, j, k + 1)) + fabs(XX(i, j, k + 1))) -
-                           (fabs(XX(i - 1, j, k - 1)) + fabs(XX(i, j, k - 1))),
-                       fabs(XX(i - 1, j, k + 1)) + fabs(XX(i, j, k + 1)) + fabs(XX(i - 1, j, k - 1)) +
-                           fabs(XX(i, j, k - 1)) + ep,
-                       hmx);
+      const R y1 = (fabs(XX(i - 1, j + 1, k)) + fabs(XX(i, j + 1, k))) -
+                   (fabs(XX(i - 1, j - 1, k)) + fabs(XX(i, j - 1, k)));
+      const R y2 = fabs(XX(i - 1, j + 1, k)) + fabs(XX(i, j + 1, k)) + fabs(XX(i - 1, j - 1, k)) +
+                   fabs(XX(i, j - 1, k)) + ep;
+      if (GV)
+        v = vdyfa_k(XX(i - 1, j, k), XX(i, j, k), P.gvs[0].ld(i, j, k), ep) +
+            vcorra_b<U>(P.gvs[1].ld(i, j, k), y1, y2, hmx);
+      else
+        v = vdyfa_u<U>(XX(i - 1, j, k), XX(i, j, k), a, hmx, ep) +
+            vcorra_u<U>(a, AY(i - 1, j, k) + AY(i - 1, j + 1, k) + AY(i, j + 1, k) + AY(i, j, k), y1, y2, hmx);
+      if (zt) {
+        const R z1 = (fabs(XX(i - 1, j, k + 1)) + fabs(XX(i, j, k + 1))) -
+                     (fabs(XX(i - 1, j, k - 1)) + fabs(XX(i, j, k - 1)));
+        const R z2 = fabs(XX(i - 1, j, k + 1)) + fabs(XX(i, j, k + 1)) + fabs(XX(i - 1, j, k - 1)) +
+                     fabs(XX(i, j, k - 1)) + ep;
+        v = v + (GV ? vcorra_b<U>(P.gvs[2].ld(i, j, k), z1, z2, hmx)
+                    : vcorra_u<U>(a, AZ(i - 1, j, k) + AZ(i - 1, j, k + 1) + AZ(i, j, k + 1) + AZ(i, j, k), z1, z2,
+                                  hmx));
+      }
       put(0, v, donor(XX(i - 1, j, k), XX(i, j, k), v));
     } else {
       const R d2 = PS ? P.cp.ld(i, j + 1, k) - P.cp.ld(i, j - 1, k)
@@ -338,20 +390,25 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
     const R a = AY(i, j, k);
     R v;
     if (STD) {
-      v = vdyfa_u<U>(XX(i, j - 1, k), XX(i, j, k), a, hmy, ep) +
-          vcorra_u<U>(a, AX(i, j - 1, k) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j - 1, k),
-                 (fabs(XX(i + 1, j - 1, k)) + fabs(XX(i + 1, j, k))) -
-                     (fabs(XX(i - 1, j - 1, k)) + fabs(XX(i - 1, j, k))),
-                 fabs(XX(i + 1, j - 1, k)) + fabs(XX(i + 1, j, k)) + fabs(XX(i - 1, j - 1, k)) +
-                     fabs(XX(i - 1, j, k)) + ep,
-                 hmy);
-      if (zt)
-        v = v + vcorra_u<U>(a, AZ(i, j - 1, k) + AZ(i, j, k) + AZ(i, j, k + 1) + AZ(i, j - 1, k + 1),
-                       (fabs(XX(i, j - 1, k + 1)) + fabs(XX(i, j, k + 1))) -
-                           (fabs(XX(i, j - 1, k - 1)) + fabs(XX(i, j, k - 1))),
-                       fabs(XX(i, j - 1, k + 1)) + fabs(XX(i, j, k + 1)) + fabs(XX(i, j - 1, k - 1)) +
-                           fabs(XX(i, j, k - 1)) + ep,
-                       hmy);
+      const R y1 = (fabs(XX(i + 1, j - 1, k)) + fabs(XX(i + 1, j, k))) -
+                   (fabs(XX(i - 1, j - 1, k)) + fabs(XX(i - 1, j, k)));
+      const R y2 = fabs(XX(i + 1, j - 1, k)) + fabs(XX(i + 1, j, k)) + fabs(XX(i - 1, j - 1, k)) +
+                   fabs(XX(i - 1, j, k)) + ep;
+      if (GV)
+        v = vdyfa_k(XX(i, j - 1, k), XX(i, j, k), P.gvs[3].ld(i, j, k), ep) +
+            vcorra_b<U>(P.gvs[4].ld(i, j, k), y1, y2, hmy);
+      else
+        v = vdyfa_u<U>(XX(i, j - 1, k), XX(i, j, k), a, hmy, ep) +
+            vcorra_u<U>(a, AX(i, j - 1, k) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j - 1, k), y1, y2, hmy);
+      if (zt) {
+        const R z1 = (fabs(XX(i, j - 1, k + 1)) + fabs(XX(i, j, k + 1))) -
+                     (fabs(XX(i, j - 1, k - 1)) + fabs(XX(i, j, k - 1)));
+        const R z2 = fabs(XX(i, j - 1, k + 1)) + fabs(XX(i, j, k + 1)) + fabs(XX(i, j - 1, k - 1)) +
+                     fabs(XX(i, j, k - 1)) + ep;
+        v = v + (GV ? vcorra_b<U>(P.gvs[5].ld(i, j, k), z1, z2, hmy)
+                    : vcorra_u<U>(a, AZ(i, j - 1, k) + AZ(i, j, k) + AZ(i, j, k + 1) + AZ(i, j - 1, k + 1), z1, z2,
+                                  hmy));
+      }
       put(1, v, donor(XX(i, j - 1, k), XX(i, j, k), v));
     } else {
       const R d1 = PS ? P.cn.ld(i + 1, j, k) - P.cn.ld(i - 1, j, k)
@@ -375,19 +432,21 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
     const R a = AZ(i, j, k);
     R v;
     if (STD) {
-      v = vdyfa_u<U>(XX(i, j, k - 1), XX(i, j, k), a, hmz, ep) +
-          vcorra_u<U>(a, AX(i, j, k - 1) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j, k - 1),
-                 (fabs(XX(i + 1, j, k - 1)) + fabs(XX(i + 1, j, k))) -
-                     (fabs(XX(i - 1, j, k - 1)) + fabs(XX(i - 1, j, k))),
-                 fabs(XX(i + 1, j, k - 1)) + fabs(XX(i + 1, j, k)) + fabs(XX(i - 1, j, k - 1)) +
-                     fabs(XX(i - 1, j, k)) + ep,
-                 hmz) +
-          vcorra_u<U>(a, AY(i, j, k - 1) + AY(i, j + 1, k - 1) + AY(i, j + 1, k) + AY(i, j, k),
-                 (fabs(XX(i, j + 1, k - 1)) + fabs(XX(i, j + 1, k))) -
-                     (fabs(XX(i, j - 1, k - 1)) + fabs(XX(i, j - 1, k))),
-                 fabs(XX(i, j + 1, k - 1)) + fabs(XX(i, j + 1, k)) + fabs(XX(i, j - 1, k - 1)) +
-                     fabs(XX(i, j - 1, k)) + ep,
-                 hmz);
+      const R x1 = (fabs(XX(i + 1, j, k - 1)) + fabs(XX(i + 1, j, k))) -
+                   (fabs(XX(i - 1, j, k - 1)) + fabs(XX(i - 1, j, k)));
+      const R x2 = fabs(XX(i + 1, j, k - 1)) + fabs(XX(i + 1, j, k)) + fabs(XX(i - 1, j, k - 1)) +
+                   fabs(XX(i - 1, j, k)) + ep;
+      const R y1 = (fabs(XX(i, j + 1, k - 1)) + fabs(XX(i, j + 1, k))) -
+                   (fabs(XX(i, j - 1, k - 1)) + fabs(XX(i, j - 1, k)));
+      const R y2 = fabs(XX(i, j + 1, k - 1)) + fabs(XX(i, j + 1, k)) + fabs(XX(i, j - 1, k - 1)) +
+                   fabs(XX(i, j - 1, k)) + ep;
+      if (GV)
+        v = vdyfa_k(XX(i, j, k - 1), XX(i, j, k), P.gvs[6].ld(i, j, k), ep) +
+            vcorra_b<U>(P.gvs[7].ld(i, j, k), x1, x2, hmz) + vcorra_b<U>(P.gvs[8].ld(i, j, k), y1, y2, hmz);
+      else
+        v = vdyfa_u<U>(XX(i, j, k - 1), XX(i, j, k), a, hmz, ep) +
+            vcorra_u<U>(a, AX(i, j, k - 1) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j, k - 1), x1, x2, hmz) +
+            vcorra_u<U>(a, AY(i, j, k - 1) + AY(i, j + 1, k - 1) + AY(i, j + 1, k) + AY(i, j, k), y1, y2, hmz);
       put(2, v, donor(XX(i, j, k - 1), XX(i, j, k), v));
     } else {
       const R d1 = PS ? P.q.ld(i + 1, j, k) - P.q.ld(i - 1, j, k)
@@ -426,7 +485,7 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
 template <class R, bool AIN, bool IN = false, bool U = false, bool PS = false, bool GV = false, bool DEFER = true>
 __device__ __forceinline__ void pseudo_body(const Prob<R>& P, int i, int j, int k) {
   if (P.stdf)
-    pseudo_form<R, true, AIN, IN, U, false, false, DEFER>(P, i, j, k);
+    pseudo_form<R, true, AIN, IN, U, false, GV, DEFER>(P, i, j, k);
   else
     pseudo_form<R, false, AIN, IN, U, PS, GV, DEFER>(P, i, j, k);
 }

@@ -32,7 +32,8 @@ namespace {
 constexpr uint32_t WS_MAGIC = 0x4d504454u;  // "MPDT"
 constexpr int NFIELD = 15;  // per problem: xant v1..3 f1..3 w1..3 cp cn mx mn q
 constexpr int NVEL = 4;     // per velocity: hinv hmx hmy hmz
-constexpr int NGVEL = 12;   // per batch velocity group with several fields: gvf[12]
+constexpr int NGVEL = 12;   // per batch velocity group with several fields: gvf[12] (gauge)
+constexpr int NGVS = 9;     // ... and gvs[9] (standard form)
 constexpr int NSCRATCH = NFIELD + NVEL;
 
 // Pool-backed event timer: one (start, stop) pair per recorded launch,
@@ -542,7 +543,8 @@ struct Batch {
   std::vector<int> owner;       // first problem of each problem's velocity group
   std::vector<size_t> foff;     // element offset of each problem's field scratch
   std::vector<size_t> voff;     // element offset of each problem's velocity scratch
-  std::vector<int> gv;          // problem's velocity group precomputes its first-pass terms
+  std::vector<int> gv;          // problem's velocity group precomputes its first-pass terms:
+                                // bit 0 the gauge form's, bit 1 the standard form's
   std::vector<size_t> ncell;
   std::vector<int> given;       // arrays set for the problem
   std::vector<unsigned char> table;  // host image of the Prob table
@@ -664,11 +666,14 @@ void write_prob(Batch* b, int p, void* psi, const void* u1, const void* u2, cons
                            (const R*)h, (const R*)rhr, (const R*)bcx, (const R*)bcy, base + b->foff[p],
                            b->ncell[p], base + b->voff[p], b->owner[p] == p ? 1 : 0);
   P.pairs = (b->pr[p].gauge && sizeof(R) == 8) ? 1 : 0;  // kb_pairs fills cp/cn/q before kb_pseudo
-  if (b->gv[p]) {
-    P.gv = 1;
-    R* gbase = base + b->voff[p] + (size_t)NVEL * b->ncell[p];
+  P.gv = b->gv[p];
+  R* gbase = base + b->voff[p] + (size_t)NVEL * b->ncell[p];
+  if (P.gv & 1) {
     for (int s = 0; s < NGVEL; s++) P.gvf[s] = scratch_view<R>(gbase + (size_t)s * b->ncell[p], P.g);
+    gbase += (size_t)NGVEL * b->ncell[p];
   }
+  if (P.gv & 2)
+    for (int s = 0; s < NGVS; s++) P.gvs[s] = scratch_view<R>(gbase + (size_t)s * b->ncell[p], P.g);
   memcpy(b->table.data() + (size_t)p * sizeof(Prob<R>), &P, sizeof P);
 }
 
@@ -731,24 +736,24 @@ int mpdata_batch_create(int nprob, const mpdata_problem* probs, int ih, int iord
     b->foff[p] = off;
     off += (size_t)NFIELD * b->ncell[p];
   }
-  // a group of two or more fields with a gauge one shares the velocity-only
-  // terms of its first-pass gauge pseudo-velocities (velgroup_body)
+  // a group of two or more fields shares the velocity-only terms of its
+  // first-pass pseudo-velocities, for each form among its fields (velgroup_body)
   b->gv.assign(nprob, 0);
   {
-    std::vector<int> members(nprob, 0), gauge(nprob, 0);
+    std::vector<int> members(nprob, 0), forms(nprob, 0);
     for (int p = 0; p < nprob; p++) {
       members[b->owner[p]]++;
-      gauge[b->owner[p]] |= probs[p].gauge;
+      forms[b->owner[p]] |= probs[p].gauge ? 1 : 2;
     }
     for (int p = 0; p < nprob; p++) {
       const int o = b->owner[p];
-      b->gv[p] = (iord >= 2 && members[o] >= 2 && gauge[o]) ? 1 : 0;
+      b->gv[p] = (iord >= 2 && members[o] >= 2) ? forms[o] : 0;
     }
   }
   for (int p = 0; p < nprob; p++)
     if (b->owner[p] == p) {
       b->voff[p] = off;
-      off += (size_t)(NVEL + (b->gv[p] ? NGVEL : 0)) * b->ncell[p];
+      off += (size_t)(NVEL + ((b->gv[p] & 1) ? NGVEL : 0) + ((b->gv[p] & 2) ? NGVS : 0)) * b->ncell[p];
     }
   for (int p = 0; p < nprob; p++) b->voff[p] = b->voff[b->owner[p]];
   b->table.assign((size_t)nprob * b->pbytes, 0);

@@ -757,7 +757,7 @@ def run_batch_study(args, steps=100):
     """Batching: 64 periodic domains of uneven sizes (seed 3) in one
     batch (one CUDA-graph launch per step, tuned tile shape) against a loop of
     per-domain steps; FP64 and FP32.  Plus 16 tracers sharing one velocity on
-    256x256x64 against 16 separate steps."""
+    256x256x64 against 16 separate steps, in the gauge and the standard form."""
     import torch
     from advectionhpctester_gb300 import mpdata as M
     out = {}
@@ -804,28 +804,31 @@ def run_batch_study(args, steps=100):
             "launches_per_step": int(lps), "graph_launches_per_step": 1}
         del doms
         torch.cuda.empty_cache()
-    # 16 tracers sharing one velocity
+    # 16 tracers sharing one velocity, in the gauge form and in the standard
+    # form (the reference's multi-field step advects its scalars in the latter)
     rng = np.random.default_rng(16)
     base = make_domain_device((256, 256, 64), rng, torch.float64)
     tr = [base["psi"].clone() * (1.0 + 0.01 * k) for k in range(16)]
-    b = M.Batch([dict(np=256, mp=256, lp=64, gauge=1, velocity_group=0)] * 16, iord=2, nonos=1, precision=64)
-    for p in range(16):
-        b.set(p, tr[p], base["u1"], base["u2"], base["u3"], base["h"], base["rhr"])
-    b.graph(True)
-    ms_b = timed(b.step, steps)
-    w = M.Workspace(256, 256, 64, 1, 1, 1, 1, iord=2, nonos=1, gauge=1, precision=64)
-
-    def loop16():
-        for p in range(16):
-            w.step(tr[p], base["u1"], base["u2"], base["u3"], base["h"], base["rhr"])
-    ms_l = timed(loop16, steps)
-    w.close()
-    b.close()
     tc = 16 * 256 * 256 * 64
-    out["tracers16_fp64"] = {"tracer_cells": tc,
-                             "batch_gcell_steps_per_s": round(tc / (ms_b * 1e-3) / 1e9, 4),
-                             "loop_gcell_steps_per_s": round(tc / (ms_l * 1e-3) / 1e9, 4),
-                             "speedup_vs_loop": round(ms_l / ms_b, 3)}
+    for gauge, key in ((1, "tracers16_fp64"), (0, "tracers16_std_fp64")):
+        b = M.Batch([dict(np=256, mp=256, lp=64, gauge=gauge, velocity_group=0)] * 16, iord=2, nonos=1,
+                    precision=64)
+        for p in range(16):
+            b.set(p, tr[p], base["u1"], base["u2"], base["u3"], base["h"], base["rhr"])
+        b.graph(True)
+        ms_b = timed(b.step, steps)
+        w = M.Workspace(256, 256, 64, 1, 1, 1, 1, iord=2, nonos=1, gauge=gauge, precision=64)
+
+        def loop16():
+            for p in range(16):
+                w.step(tr[p], base["u1"], base["u2"], base["u3"], base["h"], base["rhr"])
+        ms_l = timed(loop16, steps)
+        w.close()
+        b.close()
+        out[key] = {"tracer_cells": tc, "form": "gauge" if gauge else "standard",
+                    "batch_gcell_steps_per_s": round(tc / (ms_b * 1e-3) / 1e9, 4),
+                    "loop_gcell_steps_per_s": round(tc / (ms_l * 1e-3) / 1e9, 4),
+                    "speedup_vs_loop": round(ms_l / ms_b, 3)}
     return out
 
 
