@@ -84,6 +84,13 @@ NCU_PSEUDO = {64: {"dram_bytes_per_cell": 100.2, "fp64_inst_per_cell": 60.6},
               32: {"dram_bytes_per_cell": 38.2, "fp64_inst_per_cell": 0.0}}
 # GB300 issues 2 FP64 instructions per SM per clock (1.25 TFLOP/s nominal FMA).
 FP64_INST_PER_SM_CLK = 2.0
+# FP64 flops per cell of one launch of each stage (DADD and DMUL 1, DFMA 2),
+# counted by ncu (smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on.sum)
+# on the deformational flow at unit density, 384x384x64, gauge iord=3.
+FP64_FLOPS_PER_CELL = {"upwind": 12.4, "pair_sums": 3.0, "pseudo_velocity": 60.6, "limiter_bounds": 11.7,
+                       "limited_flux": 3.0, "corrective_update": 6.2, "predictor_level": 12.0,
+                       "predictor_cgrid": 6.0}
+HBM_NOMINAL_GBS = 7900.0  # GB300 HBM3e, nominal
 
 
 def load_peaks():
@@ -309,6 +316,7 @@ def run_ours(args, ws, rank, local):
     traffic = int(ncu["dram_bytes_per_cell"] * cells) if ncu else None
     roof = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peak,
             "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+            "frac_nominal": round(achieved / HBM_NOMINAL_GBS, 4),
             "peak_source": peak_kind, "alg_bytes_per_launch": int(alg_bytes),
             "avg_launch_ms": round(avg_ms, 4),
             "traffic_source": "ncu DRAM bytes per cell of this kernel at 384x384x64, scaled by cells"}
@@ -317,9 +325,12 @@ def run_ours(args, ws, rank, local):
         mhz = clocks.get("sm_max_mhz") or 2070.0
         fp64_peak = FP64_INST_PER_SM_CLK * sms * mhz * 1e6 / 1e9
         fp64_ach = ncu["fp64_inst_per_cell"] * cells / (avg_ms * 1e-3) / 1e9
+        step_flops = sum(FP64_FLOPS_PER_CELL.get(k, 0.0) * v[1] for k, v in stages.items()) / args.steps
         roof["fp64_pipe"] = {"achieved": round(fp64_ach, 1), "peak": round(fp64_peak, 1),
                              "unit": "G FP64 inst/s", "frac": round(fp64_ach / fp64_peak, 4),
                              "inst_per_cell": ncu["fp64_inst_per_cell"],
+                             "step_fp64_flops_per_cell": round(step_flops, 1),
+                             "step_achieved_gflops": round(step_flops * value, 1),
                              "note": "the binding roof: 2 FP64 instructions per SM per clock at the "
                                      "sampled maximum SM clock; DRAM runs at the hbm frac"}
     stage_json = {k: {"ms_total": round(v[0], 3), "launches": int(v[1]),
@@ -367,6 +378,8 @@ def run_ours(args, ws, rank, local):
         result["batch"] = run_batch_study(args)
         torch.cuda.empty_cache()
         result["precision_768x768x160"] = run_precision_study(args, nsteps=args.precision_steps)
+        if not args.no_cpu_baseline:
+            result["config_baselines"] = run_config_baselines(args)
     return result
 
 
@@ -905,11 +918,17 @@ def oracle_slab(nx, ny, nz_slab, precision):
     return f, pats
 
 
-def time_oracle(nx, ny, nz_slab, steps, warmup, precision, threads, budget_s=None):
+def time_oracle(nx, ny, nz_slab, steps, warmup, precision, threads, budget_s=None, iord=3, psi_fn=None):
+    """CPU oracle Gcell-steps/s of the predictor + gauge step on a periodic
+    slab of the deformational flow; psi_fn(x, y, z) replaces the field."""
     from oracle import oracle as O
     O.lib()
     O.set_threads(threads)
     f, pats = oracle_slab(nx, ny, nz_slab, precision)
+    if psi_fn is not None:
+        from advectionhpctester_gb300 import workloads as W
+        c = lambda n: (np.arange(n) + 0.5) / n
+        W.interior(f.x)[...] = psi_fn(c(nx)[:, None, None], c(ny)[None, :, None], c(nz_slab)[None, None, :])
     g = O.grid(nx, ny, nz_slab, 1, 1, 1, 1)
     T = 200.0
     lev = f.x.shape + (3,)
@@ -924,7 +943,7 @@ def time_oracle(nx, ny, nz_slab, steps, warmup, precision, threads, budget_s=Non
         t0 = time.perf_counter()
         O.velprd(g, o[0], o[1], o[2], f.h, 1.0, 1.0, 1.0, 1.0, 1.0, f.u1, f.u2, f.u3)
         O.advec_dwarf(g, f.x, f.bcx, f.bcy, f.u1, f.u2, f.u3, f.rhr, f.h, legacyoptmode=4, t_adv=1,
-                      iord=3, nonos=1)
+                      iord=iord, nonos=1)
         return time.perf_counter() - t0
 
     for n in range(warmup):
@@ -936,6 +955,63 @@ def time_oracle(nx, ny, nz_slab, steps, warmup, precision, threads, budget_s=Non
         if budget_s is not None and total >= budget_s:
             break
     return nx * ny * nz_slab * done / total / 1e9, done, total
+
+
+def run_config_baselines(args):
+    """The CPU baselines of the configurations besides the headline, with the
+    GPU beside where the whole configuration fits a short run:
+    - config 1: 64x64x32 periodic solid-body rotation about z (max |u| 0.4),
+      psi = 1 + 4 exp(-r^2/32), standard form, iord=2, nonos, 100 steps, on the
+      GPU and on the CPU oracle with one thread and with all threads;
+    - config 4: the 768x768x160 box field (psi = 1 inside [0.25,0.75]^3, 0.1
+      outside) in the deformational flow, iord=2 with the predictor, on the
+      CPU oracle over a 768x768x16 slab."""
+    import torch
+    from oracle import oracle as O
+    from advectionhpctester_gb300 import mpdata as M
+    from advectionhpctester_gb300 import workloads as W
+    out = {}
+    n, steps = (64, 64, 32), 100
+    f = W.solid_body_z(*n, ih=1, courant=0.4, std=True)
+    d = {k: M.fortran_device(getattr(f, k)) for k in ("x", "u1", "u2", "u3", "h", "rhr")}
+    ws = M.Workspace(*n, 1, 1, 1, 1, iord=2, nonos=1, gauge=0, precision=64)
+    args_ = (d["x"], d["u1"], d["u2"], d["u3"], d["h"], d["rhr"])
+    for _ in range(3):
+        ws.step(*args_)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        ws.step(*args_)
+    e1.record()
+    torch.cuda.synchronize()
+    ws.close()
+    cells = n[0] * n[1] * n[2]
+    gpu = cells * steps / (e0.elapsed_time(e1) * 1e-3) / 1e9
+    cpu = {}
+    for threads in (1, os.cpu_count() or 1):
+        O.lib()
+        O.set_threads(threads)
+        g = f.copy()
+        t0 = time.perf_counter()
+        O.advec_dwarf(O.grid(*n, 1, 1, 1, 1), g.x, g.bcx, g.bcy, g.u1, g.u2, g.u3, g.rhr, g.h, t_adv=2,
+                      iord=2, nonos=1, nsteps=steps)
+        cpu[threads] = cells * steps / (time.perf_counter() - t0) / 1e9
+    out["config1_64x64x32_std_iord2_100steps"] = {
+        "gpu_gcell_steps_per_s": round(gpu, 4), "cpu_1_thread": round(cpu[1], 6),
+        "cpu_all_threads": round(cpu[max(cpu)], 6), "cpu_threads": max(cpu),
+        "note": "131072 cells: the GPU step is launch-bound at this size"}
+
+    def box(x, y, z):
+        inside = (x >= 0.25) & (x <= 0.75) & (y >= 0.25) & (y <= 0.75) & (z >= 0.25) & (z <= 0.75)
+        return np.where(inside, 1.0, 0.1)
+    for threads in (1, os.cpu_count() or 1):
+        v, done, total = time_oracle(768, 768, 16, 3, 1, 64, threads, budget_s=10.0, iord=2, psi_fn=box)
+        out.setdefault("config4_768x768x16_slab_iord2_cpu", {})[
+            "cpu_1_thread" if threads == 1 else "cpu_all_threads"] = round(v, 6)
+    out["config4_768x768x16_slab_iord2_cpu"]["cpu_threads"] = os.cpu_count() or 1
+    out["config4_768x768x16_slab_iord2_cpu"]["gpu_full_grid"] = "precision_768x768x160.fp64_gcell_steps_per_s"
+    return out
 
 
 def run_reference(args, ws, rank):
