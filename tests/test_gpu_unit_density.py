@@ -51,7 +51,7 @@ def zero_laden(n, ibc, seed, perturb):
 
 
 @pytest.mark.parametrize("perturb", [False, True], ids=["unit", "one_cell_off"])
-@pytest.mark.parametrize("iord", [2, 3])
+@pytest.mark.parametrize("iord", [2, 3, 5])
 @pytest.mark.parametrize("t_adv", [1, 2], ids=["gauge", "std"])
 @pytest.mark.parametrize("ibc", [(1, 1, 1), (0, 0, 0)], ids=["periodic", "walls"])
 def test_step_bits_with_zeros_and_unit_density(M, oracle, ibc, t_adv, iord, perturb):
