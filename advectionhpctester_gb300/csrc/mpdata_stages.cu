@@ -74,31 +74,46 @@ template <class R>
 struct PseudoMinBlocks {
   static constexpr int v = sizeof(R) == 4 ? MPDATA_MINB_PSEUDO_F32 : MPDATA_MINB_PSEUDO_F64;
 };
+// Whether the pseudo-velocity kernel issues every load before its stores
+// (DEFER, see limit_form) or stores each face at once (fewer registers).
+// FP64 measured the same either way, with 5 to 7 resident blocks (the FP64
+// pipe is the bound); FP32 gains from DEFER.
+#ifndef MPDATA_DEFER_PSEUDO_F64
+#define MPDATA_DEFER_PSEUDO_F64 1
+#endif
+#ifndef MPDATA_DEFER_PSEUDO_F32
+#define MPDATA_DEFER_PSEUDO_F32 1
+#endif
+template <class R>
+struct PseudoDefer {
+  static constexpr bool v = sizeof(R) == 4 ? MPDATA_DEFER_PSEUDO_F32 : MPDATA_DEFER_PSEUDO_F64;
+};
 
 template <class R, bool AIN>
 __global__ void __launch_bounds__(128, PseudoMinBlocks<R>::v) k_pseudo(const Prob<R> P) {
+  constexpr bool D = PseudoDefer<R>::v;
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int k = blockIdx.z + 1;
   const bool win = warp_interior(P.g, i, j, k);
   if (i > P.g.np || j > P.g.mp) return;
   if (!win) {
-    pseudo_body<R, AIN, false>(P, i, j, k);
+    pseudo_body<R, AIN, false, false, false, false, D>(P, i, j, k);
   } else if constexpr (sizeof(R) == 8) {
     const bool unit = warp_unit_faces(P, i, j, k);
     if (P.pairs) {
       if (unit)
-        pseudo_body<R, AIN, true, true, true>(P, i, j, k);
+        pseudo_body<R, AIN, true, true, true, false, D>(P, i, j, k);
       else
-        pseudo_body<R, AIN, true, false, true>(P, i, j, k);
+        pseudo_body<R, AIN, true, false, true, false, D>(P, i, j, k);
     } else {
       if (unit)
-        pseudo_body<R, AIN, true, true>(P, i, j, k);
+        pseudo_body<R, AIN, true, true, false, false, D>(P, i, j, k);
       else
-        pseudo_body<R, AIN, true>(P, i, j, k);
+        pseudo_body<R, AIN, true, false, false, false, D>(P, i, j, k);
     }
   } else {
-    pseudo_body<R, AIN, true>(P, i, j, k);
+    pseudo_body<R, AIN, true, false, false, false, D>(P, i, j, k);
   }
 }
 
