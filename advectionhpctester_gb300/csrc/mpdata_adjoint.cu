@@ -895,8 +895,13 @@ Prob<R> pass_prob(const Prob<R>& P, const AdjPlan<R>& A, int t, bool prev_w) {
   return Q;
 }
 
+// The forward records of one step (every pass's input field, velocities,
+// ratios and extrema) into A's record arrays.  out: when given, the last
+// pass's update also writes the step's output field there (interior cells),
+// so that a checkpointed reverse sweep rebuilds a segment and records it in
+// one pass.
 template <class R>
-int run_step_adjoint(const Prob<R>& P, const AdjPlan<R>& A, int nonos, cudaStream_t s) {
+int run_step_record(const Prob<R>& P, const AdjPlan<R>& A, int nonos, const Arr<R>* out, cudaStream_t s) {
   const Geo& g = P.g;
   const dim3 blk(32, 4, 1);
   const dim3 grd((g.np + 31) / 32, (g.mp + 3) / 4, g.lp);
@@ -904,8 +909,6 @@ int run_step_adjoint(const Prob<R>& P, const AdjPlan<R>& A, int nonos, cudaStrea
   const bool keep = np_ > 1;
   const size_t ncell = (size_t)g.np * g.mp * g.lp;
   int n = 0;
-  if (cudaMemsetAsync(A.acc, 0, A.acc_elems * sizeof(R), s) != cudaSuccess) return -5;
-  // ---- forward records
   Prob<R> F = P;
   F.xant = A.x[0];
   kf_upwind<R><<<grd, blk, 0, s>>>(F);
@@ -940,13 +943,27 @@ int run_step_adjoint(const Prob<R>& P, const AdjPlan<R>& A, int nonos, cudaStrea
     if (nonos) kf_limit<R, true><<<grd, blk, 0, s>>>(L);
     else kf_limit<R, false><<<grd, blk, 0, s>>>(L);
     n += 3;
-    if (t < np_ - 1) {
+    if (t < np_ - 1 || out) {
       Prob<R> U = L;
-      U.xant = A.x[t + 1];
+      U.xant = t < np_ - 1 ? A.x[t + 1] : *out;
       kf_update<R><<<grd, blk, 0, s>>>(U);
       n++;
     }
   }
+  add_launches(n);
+  return cudaGetLastError() == cudaSuccess ? 0 : -5;
+}
+
+// The reverse kernels of one recorded step: lambda of the step's output (A.lam)
+// becomes lambda of its input; the velocity gradients accumulate into A.gu*.
+template <class R>
+int run_step_reverse(const Prob<R>& P, const AdjPlan<R>& A, int nonos, cudaStream_t s) {
+  const Geo& g = P.g;
+  const dim3 blk(32, 4, 1);
+  const dim3 grd((g.np + 31) / 32, (g.mp + 3) / 4, g.lp);
+  const int np_ = A.npass;
+  int n = 0;
+  if (cudaMemsetAsync(A.acc, 0, A.acc_elems * sizeof(R), s) != cudaSuccess) return -5;
   // ---- reverse, last pass first
   for (int t = np_ - 1; t >= 0; t--) {
     if (t < np_ - 1 && cudaMemsetAsync(A.pass_acc, 0, A.pass_acc_elems * sizeof(R), s) != cudaSuccess) return -5;
@@ -1032,6 +1049,12 @@ int run_step_adjoint(const Prob<R>& P, const AdjPlan<R>& A, int nonos, cudaStrea
 }
 
 template <class R>
+int run_step_adjoint(const Prob<R>& P, const AdjPlan<R>& A, int nonos, cudaStream_t s) {
+  const int rc = run_step_record<R>(P, A, nonos, nullptr, s);
+  return rc ? rc : run_step_reverse<R>(P, A, nonos, s);
+}
+
+template <class R>
 int run_seed(const Prob<R>& P, const Arr<R>& psi, const Arr<R>& target, const Arr<R>& lam, cudaStream_t s) {
   const Geo& g = P.g;
   const dim3 blk(32, 4, 1);
@@ -1043,6 +1066,12 @@ int run_seed(const Prob<R>& P, const Arr<R>& psi, const Arr<R>& target, const Ar
 
 template int run_step_adjoint<double>(const Prob<double>&, const AdjPlan<double>&, int, cudaStream_t);
 template int run_step_adjoint<float>(const Prob<float>&, const AdjPlan<float>&, int, cudaStream_t);
+template int run_step_record<double>(const Prob<double>&, const AdjPlan<double>&, int, const Arr<double>*,
+                                     cudaStream_t);
+template int run_step_record<float>(const Prob<float>&, const AdjPlan<float>&, int, const Arr<float>*,
+                                    cudaStream_t);
+template int run_step_reverse<double>(const Prob<double>&, const AdjPlan<double>&, int, cudaStream_t);
+template int run_step_reverse<float>(const Prob<float>&, const AdjPlan<float>&, int, cudaStream_t);
 template int run_seed<double>(const Prob<double>&, const Arr<double>&, const Arr<double>&, const Arr<double>&, cudaStream_t);
 template int run_seed<float>(const Prob<float>&, const Arr<float>&, const Arr<float>&, const Arr<float>&, cudaStream_t);
 

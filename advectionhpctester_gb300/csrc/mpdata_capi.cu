@@ -1066,6 +1066,25 @@ int adj_plan(Workspace* w, Prob<R>* P, AdjPlan<R>* A, const R* psi_in, const R* 
   return MPDATA_OK;
 }
 
+// Points the record arrays of B at an arena of adj_record_fields fields of n
+// elements, in adj_plan's order (the accumulators stay shared).
+template <class R>
+void repoint_records(AdjPlan<R>* B, R* a, size_t n, const Geo& g) {
+  size_t f = 0;
+  auto next = [&]() { return scratch_view<R>(a + (f++) * n, g); };
+  for (int t = 0; t < B->npass; t++) {
+    B->x[t] = next();
+    for (int c = 0; c < 3; c++) B->v[t][c] = next();
+    for (int c = 0; c < 3; c++) B->w[t][c] = next();
+    B->cp[t] = next();
+    B->cn[t] = next();
+    B->mx[t] = next();
+    B->mn[t] = next();
+    for (int c = 0; c < 3; c++) B->fns[t][c] = next();
+    B->q[t] = next();
+  }
+}
+
 template <class R>
 int step_adjoint_impl(void* ws, const R* psi_in, const R* u1, const R* u2, const R* u3, const R* h, const R* rhr,
                       const R* bcx, const R* bcy, R* lambda, R* gu1, R* gu2, R* gu3, void* stream) {
@@ -1084,7 +1103,12 @@ int step_adjoint_impl(void* ws, const R* psi_in, const R* u1, const R* u2, const
 // checkpoints every `interval` steps (default ceil(sqrt(nsteps))): the
 // forward run keeps ceil(nsteps/interval) states; the reverse sweep rebuilds
 // each segment's states from its checkpoint and runs the step adjoints
-// backwards.  Peak extra memory: (checkpoints + interval) psi-sized arrays.
+// backwards.  When one record arena per step of a segment fits in half of
+// the free device memory, the rebuild runs the record kernels themselves
+// (each step's records and its output state in one pass) and the reverse
+// kernels read those records, so each step runs forward twice instead of
+// three times.  Peak extra memory: (checkpoints + interval) psi-sized arrays,
+// plus (interval - 1) record arenas when they are kept.
 template <class R>
 int adjoint_run_impl(void* ws, int nsteps, int interval, R* psi, const R* u1, const R* u2, const R* u3,
                      const R* h, const R* rhr, const R* bcx, const R* bcy, const R* target, double* J,
@@ -1121,10 +1145,26 @@ int adjoint_run_impl(void* ws, int nsteps, int interval, R* psi, const R* u1, co
     if (seg) cudaFreeAsync(seg, s);
     return MPDATA_E_CUDA;
   }
+  // one record arena per step of a segment (the workspace's own is the first)
+  const size_t nrec = adj_record_fields(w->o.iord);
+  const size_t rec_bytes = nrec * w->ncell * w->elem;
+  R* recs = nullptr;
+  {
+    size_t free_b = 0, total_b = 0;
+    if (K > 1 && cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && (size_t)(K - 1) * rec_bytes < free_b / 2 &&
+        cudaMallocAsync(&recs, (size_t)(K - 1) * rec_bytes, s) != cudaSuccess) {
+      cudaGetLastError();
+      recs = nullptr;
+    }
+  }
+  std::vector<AdjPlan<R>> plans;
+  if (recs) {
+    plans.assign((size_t)K, A);
+    for (int k = 1; k < K; k++) repoint_records<R>(&plans[k], recs + (size_t)(k - 1) * nrec * w->ncell, w->ncell, P.g);
+  }
   if (peak_bytes)
-    *peak_bytes = (long long)(pbytes * (nck + K)) +
-                  (long long)(w->ncell * w->elem *
-                              (NSCRATCH + adj_record_fields(w->o.iord) + adj_acc_fields(w->o.iord)));
+    *peak_bytes = (long long)(pbytes * (nck + K)) + (long long)(recs ? (size_t)(K - 1) * rec_bytes : 0) +
+                  (long long)(w->ncell * w->elem * (NSCRATCH + nrec + adj_acc_fields(w->o.iord)));
   R* base = static_cast<R*>(w->mem);
   auto fwd = [&](R* state) -> int {
     Prob<R> F = make_prob<R>(g, w->o.gauge, state, u1, u2, u3, h, rhr, bcx, bcy, base, w->ncell,
@@ -1154,6 +1194,26 @@ int adjoint_run_impl(void* ws, int nsteps, int interval, R* psi, const R* u1, co
       rc = MPDATA_E_CUDA;
       break;
     }
+    if (recs) {
+      // records of every step of the segment, each step's output into the next state
+      for (int n = n0; n < n1 && !rc; n++) {
+        R* src = seg + (size_t)(n - n0) * plen;
+        Prob<R> B = P;
+        B.psi = caller_view<R>(src, ih, sx, sy);
+        const bool more = n + 1 < n1;  // the segment's last output is the next checkpoint
+        const Arr<R> next = caller_view<R>(more ? src + plen : src, ih, sx, sy);
+        if (more && cudaMemcpyAsync(src + plen, src, pbytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+          rc = MPDATA_E_CUDA;
+        if (!rc && run_step_record<R>(B, plans[n - n0], w->o.nonos, more ? &next : nullptr, s))
+          rc = MPDATA_E_CUDA;
+      }
+      for (int n = n1 - 1; n >= n0 && !rc; n--) {
+        Prob<R> B = P;
+        B.psi = caller_view<R>(seg + (size_t)(n - n0) * plen, ih, sx, sy);
+        if (run_step_reverse<R>(B, plans[n - n0], w->o.nonos, s)) rc = MPDATA_E_CUDA;
+      }
+      continue;
+    }
     for (int n = n0 + 1; n < n1 && !rc; n++) {
       R* dst = seg + (size_t)(n - n0) * plen;
       if (cudaMemcpyAsync(dst, dst - plen, pbytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess || fwd(dst))
@@ -1168,6 +1228,7 @@ int adjoint_run_impl(void* ws, int nsteps, int interval, R* psi, const R* u1, co
   cudaFreeAsync(ck, s);
   cudaFreeAsync(seg, s);
   cudaFreeAsync(red, s);
+  if (recs) cudaFreeAsync(recs, s);
   if (!rc && cudaStreamSynchronize(s) != cudaSuccess) rc = MPDATA_E_CUDA;
   if (!rc) *J = 0.5 * out[0];
   return rc;

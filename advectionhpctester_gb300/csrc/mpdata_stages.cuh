@@ -120,6 +120,10 @@ inline size_t adj_acc_fields(int iord) { return (size_t)(iord - 1) * 6 + 12 + 1;
 template <class R>
 int run_step_adjoint(const Prob<R>& P, const AdjPlan<R>& A, int nonos, cudaStream_t s);
 template <class R>
+int run_step_record(const Prob<R>& P, const AdjPlan<R>& A, int nonos, const Arr<R>* out, cudaStream_t s);
+template <class R>
+int run_step_reverse(const Prob<R>& P, const AdjPlan<R>& A, int nonos, cudaStream_t s);
+template <class R>
 int run_seed(const Prob<R>& P, const Arr<R>& psi, const Arr<R>& target, const Arr<R>& lam, cudaStream_t s);
 
 unsigned long long launch_count();
