@@ -159,8 +159,12 @@ int mpdata_rho_gauge_f32(void* ws, float* ox, float* oy, float* oz, float* u, fl
  * with velocities held fixed; psi holds psi_0 on entry and psi_N on exit;
  * g_psi0 receives dJ/dpsi_0 and g_u1..g_u3 accumulate dJ/du.  States are
  * checkpointed every `interval` steps (0 = ceil(sqrt(nsteps))) and each
- * segment is recomputed in the reverse sweep; peak_bytes (may be NULL)
- * receives the device memory the run holds.  Synchronises the stream. */
+ * segment is recomputed in the reverse sweep.  When interval-1 extra record
+ * arenas (15*(iord-1) fields each) fit in half of the free device memory,
+ * the recomputation records every step of the segment once and the reverse
+ * kernels read those records; otherwise each step adjoint records its own
+ * step again.  peak_bytes (may be NULL) receives the device memory the run
+ * holds.  Synchronises the stream. */
 int mpdata_step_adjoint_f64(void* ws, const double* psi_in, const double* u1, const double* u2,
                             const double* u3, const double* h, const double* rhr, const double* bcx,
                             const double* bcy, double* lambda, double* g_u1, double* g_u2,
