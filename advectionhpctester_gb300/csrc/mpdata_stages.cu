@@ -46,8 +46,38 @@ namespace mpdata {
     BODY(true, false);                                      \
   }
 
+// Minimum resident 128-thread blocks per SM asked of the register allocator
+// for the upwind, limiter-bounds and limited-flux kernels.  An explicit bound
+// is always given: with none, or with 1, ptxas allots these kernels far more
+// registers (k_limit 32 -> 56, k_upwind 48 -> 78 in FP32) and they run
+// slower.  FP64 values from a sweep at 512x512x128 (upwind 8: -3%, bounds 12:
+// -13% with a 12-byte spill, limit 16: -7%); FP32 values keep the registers
+// its kernels had without a bound.  Build-time overridable for tuning sweeps.
+#ifndef MPDATA_MINB_UPWIND_F64
+#define MPDATA_MINB_UPWIND_F64 8
+#endif
+#ifndef MPDATA_MINB_BOUNDS_F64
+#define MPDATA_MINB_BOUNDS_F64 12
+#endif
+#ifndef MPDATA_MINB_LIMIT_F64
+#define MPDATA_MINB_LIMIT_F64 16
+#endif
+#ifndef MPDATA_MINB_UPWIND_F32
+#define MPDATA_MINB_UPWIND_F32 10
+#endif
+#ifndef MPDATA_MINB_BOUNDS_F32
+#define MPDATA_MINB_BOUNDS_F32 12
+#endif
+#ifndef MPDATA_MINB_LIMIT_F32
+#define MPDATA_MINB_LIMIT_F32 16
+#endif
+template <class R, int N64, int N32>
+struct MinBlocks {
+  static constexpr int v = sizeof(R) == 8 ? N64 : N32;
+};
+
 template <class R, bool ANTIDIFF>
-__global__ void __launch_bounds__(128) k_upwind(const Prob<R> P) {
+__global__ void __launch_bounds__(128, (MinBlocks<R, MPDATA_MINB_UPWIND_F64, MPDATA_MINB_UPWIND_F32>::v)) k_upwind(const Prob<R> P) {
 #define B(IN, U) upwind_body<R, ANTIDIFF, true, IN, U>(P, i, j, k)
   CELL_DISPATCH_U(B)
 #undef B
@@ -123,7 +153,7 @@ __global__ void __launch_bounds__(128) k_pairs(const Prob<R> P) {
   pairs_body<R>(P, i, j, k);
 }
 template <class R, bool NONOS, bool FIRST, bool KEEP>
-__global__ void __launch_bounds__(128) k_bounds(const Prob<R> P) {
+__global__ void __launch_bounds__(128, (MinBlocks<R, MPDATA_MINB_BOUNDS_F64, MPDATA_MINB_BOUNDS_F32>::v)) k_bounds(const Prob<R> P) {
   if constexpr (NONOS && sizeof(R) == 8) {  // FP32: per-lane quotients are cheaper than the barriers
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
@@ -147,7 +177,7 @@ __global__ void __launch_bounds__(128) k_bounds(const Prob<R> P) {
   }
 }
 template <class R, bool NONOS>
-__global__ void __launch_bounds__(128) k_limit(const Prob<R> P) {
+__global__ void __launch_bounds__(128, (MinBlocks<R, MPDATA_MINB_LIMIT_F64, MPDATA_MINB_LIMIT_F32>::v)) k_limit(const Prob<R> P) {
 #define B(IN) limit_body<R, NONOS, IN>(P, i, j, k)
   CELL_DISPATCH(B)
 #undef B
