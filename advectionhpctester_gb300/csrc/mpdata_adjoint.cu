@@ -32,6 +32,58 @@
 
 namespace mpdata {
 
+// Launch bounds of the reverse kernels: minimum resident 128-thread blocks
+// per SM (0: no explicit bound).  Build-time overridable for tuning sweeps;
+// a sweep of 6-16 blocks per kernel measured within 0.5% of no bound.
+#ifndef MPDATA_MINB_KA_PSEUDO
+#define MPDATA_MINB_KA_PSEUDO 0
+#endif
+#ifndef MPDATA_MINB_KA_BOUNDS
+#define MPDATA_MINB_KA_BOUNDS 0
+#endif
+#ifndef MPDATA_MINB_KA_UPWIND
+#define MPDATA_MINB_KA_UPWIND 0
+#endif
+#ifndef MPDATA_MINB_KA_LIMIT
+#define MPDATA_MINB_KA_LIMIT 0
+#endif
+#ifndef MPDATA_MINB_KA_UPDATE
+#define MPDATA_MINB_KA_UPDATE 0
+#endif
+#define KA_BOUND_(n) __launch_bounds__(128, n)
+#define KA_BOUND0 __launch_bounds__(128)
+#if MPDATA_MINB_KA_PSEUDO > 0
+#define KA_LB_PSEUDO KA_BOUND_(MPDATA_MINB_KA_PSEUDO)
+#else
+#define KA_LB_PSEUDO KA_BOUND0
+#endif
+#if MPDATA_MINB_KA_BOUNDS > 0
+#define KA_LB_BOUNDS KA_BOUND_(MPDATA_MINB_KA_BOUNDS)
+#else
+#define KA_LB_BOUNDS KA_BOUND0
+#endif
+#if MPDATA_MINB_KA_UPWIND > 0
+#define KA_LB_UPWIND KA_BOUND_(MPDATA_MINB_KA_UPWIND)
+#else
+#define KA_LB_UPWIND KA_BOUND0
+#endif
+#if MPDATA_MINB_KA_LIMIT > 0
+#define KA_LB_LIMIT KA_BOUND_(MPDATA_MINB_KA_LIMIT)
+#else
+#define KA_LB_LIMIT KA_BOUND0
+#endif
+#if MPDATA_MINB_KA_UPDATE > 0
+#define KA_LB_UPDATE KA_BOUND_(MPDATA_MINB_KA_UPDATE)
+#else
+#define KA_LB_UPDATE KA_BOUND0
+#endif
+// The record kernels run the forward stage bodies: the forward stage
+// kernels' bounds (FP64 / FP32).
+template <class R, int N64, int N32>
+struct KfMinBlocks {
+  static constexpr int v = sizeof(R) == 8 ? N64 : N32;
+};
+
 // ---- adjoints of the read maps --------------------------------------------
 // Adding a zero changes no accumulator (they start at +0), so zero
 // contributions, frequent where the limiter is inactive, skip the atomic; the
@@ -128,7 +180,7 @@ __device__ __forceinline__ void ka_update_cell(const Prob<R>& P, const AdjArr<R>
   fz_add<R, false, IN>(g, A.lw3, i, j, k, -lD);
 }
 template <class R>
-__global__ void __launch_bounds__(128) ka_update(const Prob<R> P, const AdjArr<R> A) {
+__global__ void KA_LB_UPDATE ka_update(const Prob<R> P, const AdjArr<R> A) {
 #define C(IN) ka_update_cell<R, IN>(P, A, i, j, k)
   ADISPATCH(C)
 #undef C
@@ -178,7 +230,7 @@ __device__ __forceinline__ void ka_limit_cell(const Prob<R>& P, const AdjArr<R>&
 #undef LIMIT_FACE
 }
 template <class R, bool NONOS>
-__global__ void __launch_bounds__(128) ka_limit(const Prob<R> P, const AdjArr<R> A) {
+__global__ void KA_LB_LIMIT ka_limit(const Prob<R> P, const AdjArr<R> A) {
 #define C(IN) ka_limit_cell<R, NONOS, IN>(P, A, i, j, k)
   ADISPATCH(C)
 #undef C
@@ -295,7 +347,7 @@ __device__ __forceinline__ void ka_bounds_cell(const Prob<R>& P, const AdjArr<R>
   fz_add<R, false, IN>(g, LF3, i, j, k, lflux(w3, lDp, lDn, true));
 }
 template <class R, bool FIRST, bool STD>
-__global__ void __launch_bounds__(128) ka_bounds(const Prob<R> P, const AdjArr<R> A) {
+__global__ void KA_LB_BOUNDS ka_bounds(const Prob<R> P, const AdjArr<R> A) {
 #define C(IN) ka_bounds_cell<R, FIRST, STD, IN>(P, A, i, j, k)
   ADISPATCH(C)
 #undef C
@@ -442,7 +494,7 @@ __device__ __forceinline__ void ka_pseudo_cell(const Prob<R>& P, const AdjArr<R>
 #undef LX
 }
 template <class R, bool AIN>
-__global__ void __launch_bounds__(128) ka_pseudo(const Prob<R> P, const AdjArr<R> A) {
+__global__ void KA_LB_PSEUDO ka_pseudo(const Prob<R> P, const AdjArr<R> A) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int k = blockIdx.z + 1;
@@ -735,7 +787,7 @@ __device__ __forceinline__ void ka_upwind_cell(const Prob<R>& P, const AdjArr<R>
   }
 }
 template <class R>
-__global__ void __launch_bounds__(128) ka_upwind(const Prob<R> P, const AdjArr<R> A) {
+__global__ void KA_LB_UPWIND ka_upwind(const Prob<R> P, const AdjArr<R> A) {
 #define C(IN) ka_upwind_cell<R, IN>(P, A, i, j, k)
   ADISPATCH(C)
 #undef C
@@ -784,7 +836,7 @@ __global__ void __launch_bounds__(128) ka_seed(const Prob<R> P, const Arr<R> psi
     BODY(true, false);                                       \
   }
 template <class R>
-__global__ void __launch_bounds__(128) kf_upwind(const Prob<R> P) {
+__global__ void __launch_bounds__(128, (KfMinBlocks<R, 8, 10>::v)) kf_upwind(const Prob<R> P) {
 #define B(IN, U) upwind_body<R, true, false, IN, U>(P, i, j, k)
   FCELL_U(B)
 #undef B
@@ -831,7 +883,7 @@ __global__ void __launch_bounds__(128, KfPseudoMinBlocks<R>::v) kf_pseudo(const 
 // limiter's min3 selects neither form, and the reverse bounds kernel
 // recomputes its quotients from the recorded extrema and fluxes.
 template <class R, bool NONOS, bool FIRST, bool KEEP>
-__global__ void __launch_bounds__(128) kf_bounds(const Prob<R> P) {
+__global__ void __launch_bounds__(128, (KfMinBlocks<R, 12, 12>::v)) kf_bounds(const Prob<R> P) {
   if constexpr (NONOS && sizeof(R) == 8) {  // FP32: per-lane quotients are cheaper than the barriers
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
@@ -855,7 +907,7 @@ __global__ void __launch_bounds__(128) kf_bounds(const Prob<R> P) {
   }
 }
 template <class R, bool NONOS>
-__global__ void __launch_bounds__(128) kf_limit(const Prob<R> P) {
+__global__ void __launch_bounds__(128, (KfMinBlocks<R, 16, 16>::v)) kf_limit(const Prob<R> P) {
 #define B(IN) limit_body<R, NONOS, IN>(P, i, j, k)
   FCELL(B)
 #undef B
