@@ -71,8 +71,37 @@ __device__ __forceinline__ void load_prob(Prob<R>& sP, const Prob<R>* __restrict
 
 #define BATCH_ARGS const Prob<R>* __restrict__ probs, const unsigned long long* __restrict__ tiles
 
+// Launch bounds of the tile kernels: minimum resident 256-thread blocks per
+// SM (0: no explicit bound), the single-problem kernels' register budgets in
+// 256-thread units.  Together they made the batch study 4-8% faster than no
+// bound.  Build-time overridable for tuning sweeps.
+#ifndef MPDATA_MINB_KB_UPWIND
+#define MPDATA_MINB_KB_UPWIND 4
+#endif
+#ifndef MPDATA_MINB_KB_BOUNDS
+#define MPDATA_MINB_KB_BOUNDS 6
+#endif
+#ifndef MPDATA_MINB_KB_LIMIT
+#define MPDATA_MINB_KB_LIMIT 8
+#endif
+#if MPDATA_MINB_KB_UPWIND > 0
+#define KB_LB_UPWIND __launch_bounds__(256, MPDATA_MINB_KB_UPWIND)
+#else
+#define KB_LB_UPWIND __launch_bounds__(256)
+#endif
+#if MPDATA_MINB_KB_BOUNDS > 0
+#define KB_LB_BOUNDS __launch_bounds__(256, MPDATA_MINB_KB_BOUNDS)
+#else
+#define KB_LB_BOUNDS __launch_bounds__(256)
+#endif
+#if MPDATA_MINB_KB_LIMIT > 0
+#define KB_LB_LIMIT __launch_bounds__(256, MPDATA_MINB_KB_LIMIT)
+#else
+#define KB_LB_LIMIT __launch_bounds__(256)
+#endif
+
 template <class R, bool ANTIDIFF, bool HALO>
-__global__ void __launch_bounds__(256) kb_upwind(BATCH_ARGS) {
+__global__ void KB_LB_UPWIND kb_upwind(BATCH_ARGS) {
 #define B(IN, U) upwind_body<R, ANTIDIFF, HALO, IN, U, false>(P, i, j, k)
   BATCH_TILE_U(B)
 #undef B
@@ -143,7 +172,7 @@ __global__ void __launch_bounds__(256) kb_pseudo(BATCH_ARGS) {
   if (i <= P.g.np && j <= P.g.mp) pseudo_dispatch<R, AIN>(P, i, j, k, win);
 }
 template <class R, bool NONOS, bool FIRST, bool KEEP>
-__global__ void __launch_bounds__(256) kb_bounds(BATCH_ARGS) {
+__global__ void KB_LB_BOUNDS kb_bounds(BATCH_ARGS) {
   if constexpr (NONOS && sizeof(R) == 8) {  // FP32: per-lane quotients are cheaper than the barriers
     __shared__ __align__(16) unsigned char sraw[sizeof(Prob<R>)];
     Prob<R>& P = *reinterpret_cast<Prob<R>*>(sraw);
@@ -172,7 +201,7 @@ __global__ void __launch_bounds__(256) kb_bounds(BATCH_ARGS) {
   }
 }
 template <class R, bool NONOS>
-__global__ void __launch_bounds__(256) kb_limit(BATCH_ARGS) {
+__global__ void KB_LB_LIMIT kb_limit(BATCH_ARGS) {
 #define B(IN) limit_body<R, NONOS, IN, false>(P, i, j, k)
   BATCH_TILE(B)
 #undef B
