@@ -51,8 +51,9 @@ namespace mpdata {
 // is always given: with none, or with 1, ptxas allots these kernels far more
 // registers (k_limit 32 -> 56, k_upwind 48 -> 78 in FP32) and they run
 // slower.  FP64 values from a sweep at 512x512x128 (upwind 8: -3%, bounds 12:
-// -13% with a 12-byte spill, limit 16: -7%); FP32 values keep the registers
-// its kernels had without a bound.  Build-time overridable for tuning sweeps.
+// -13% with a 12-byte spill, limit 16: -7%); FP32 from a sweep too (upwind
+// 12: -12%, bounds 16: -4%, limit 16 and pseudo 8 as they were).
+// Build-time overridable for tuning sweeps.
 #ifndef MPDATA_MINB_UPWIND_F64
 #define MPDATA_MINB_UPWIND_F64 8
 #endif
@@ -63,10 +64,10 @@ namespace mpdata {
 #define MPDATA_MINB_LIMIT_F64 16
 #endif
 #ifndef MPDATA_MINB_UPWIND_F32
-#define MPDATA_MINB_UPWIND_F32 10
+#define MPDATA_MINB_UPWIND_F32 12
 #endif
 #ifndef MPDATA_MINB_BOUNDS_F32
-#define MPDATA_MINB_BOUNDS_F32 12
+#define MPDATA_MINB_BOUNDS_F32 16
 #endif
 #ifndef MPDATA_MINB_LIMIT_F32
 #define MPDATA_MINB_LIMIT_F32 16
