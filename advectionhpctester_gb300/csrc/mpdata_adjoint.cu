@@ -387,19 +387,20 @@ __device__ __forceinline__ void ka_pseudo_cell(const Prob<R>& P, const AdjArr<R>
   const bool zt = IN || g.bz || (k > 1 && k < g.lp);
 #define XX(a, b, c) xr<R, IN>(g, X, (a), (b), (c))
 #define LX(a, b, c, v) xr_add<R, IN>(g, A.lxant, (a), (b), (c), (v))
+#define AX(f, b, c) fx<R, AIN, IN>(g, U1, (f), (b), (c))
+#define AY(a, f, c) fy<R, AIN, IN>(g, U2, (a), (f), (c))
+#define AZ(a, b, f) fz<R, AIN, IN>(g, U3, (a), (b), (f))
   // x faces
   if (IN || g.bx || i > 1) {
     const R lv = A.lv1.ld(i, j, k);
     const R hm = U ? R(1) : P.hmx.ld(i, j, k), a = fx<R, AIN, IN>(g, U1, i, j, k);
     const R xl = XX(i - 1, j, k), xrr = XX(i, j, k);
-    const R S2 = fy<R, AIN, IN>(g, U2, i - 1, j, k) + fy<R, AIN, IN>(g, U2, i - 1, j + 1, k) +
-                 fy<R, AIN, IN>(g, U2, i, j + 1, k) + fy<R, AIN, IN>(g, U2, i, j, k);
+    const R S2 = VSUM_2X;
     const R D2 = PS ? P.cp.ld(i, j + 1, k) - P.cp.ld(i, j - 1, k)
                     : dif4(XX(i - 1, j - 1, k), XX(i, j - 1, k), XX(i - 1, j + 1, k), XX(i, j + 1, k));
     R cr4 = S2 * D2, S3 = R(0), D3 = R(0);
     if (zt) {
-      S3 = fz<R, AIN, IN>(g, U3, i - 1, j, k) + fz<R, AIN, IN>(g, U3, i - 1, j, k + 1) +
-           fz<R, AIN, IN>(g, U3, i, j, k + 1) + fz<R, AIN, IN>(g, U3, i, j, k);
+      S3 = VSUM_3X;
       D3 = PS ? P.cp.ld(i, j, k + 1) - P.cp.ld(i, j, k - 1)
               : dif4(XX(i - 1, j, k - 1), XX(i, j, k - 1), XX(i - 1, j, k + 1), XX(i, j, k + 1));
       cr4 = cr4 + S3 * D3;
@@ -428,14 +429,12 @@ __device__ __forceinline__ void ka_pseudo_cell(const Prob<R>& P, const AdjArr<R>
     const R lv = A.lv2.ld(i, j, k);
     const R hm = U ? R(1) : P.hmy.ld(i, j, k), a = fy<R, AIN, IN>(g, U2, i, j, k);
     const R xl = XX(i, j - 1, k), xrr = XX(i, j, k);
-    const R S1 = fx<R, AIN, IN>(g, U1, i, j - 1, k) + fx<R, AIN, IN>(g, U1, i, j, k) +
-                 fx<R, AIN, IN>(g, U1, i + 1, j, k) + fx<R, AIN, IN>(g, U1, i + 1, j - 1, k);
+    const R S1 = VSUM_1Y;
     const R D1 = PS ? P.cn.ld(i + 1, j, k) - P.cn.ld(i - 1, j, k)
                     : dif4(XX(i - 1, j - 1, k), XX(i - 1, j, k), XX(i + 1, j - 1, k), XX(i + 1, j, k));
     R cr4 = S1 * D1, S3 = R(0), D3 = R(0);
     if (zt) {
-      S3 = fz<R, AIN, IN>(g, U3, i, j - 1, k) + fz<R, AIN, IN>(g, U3, i, j, k) +
-           fz<R, AIN, IN>(g, U3, i, j, k + 1) + fz<R, AIN, IN>(g, U3, i, j - 1, k + 1);
+      S3 = VSUM_3Y;
       D3 = PS ? P.cn.ld(i, j, k + 1) - P.cn.ld(i, j, k - 1)
               : dif4(XX(i, j - 1, k - 1), XX(i, j, k - 1), XX(i, j - 1, k + 1), XX(i, j, k + 1));
       cr4 = cr4 + S3 * D3;
@@ -464,12 +463,10 @@ __device__ __forceinline__ void ka_pseudo_cell(const Prob<R>& P, const AdjArr<R>
     const R lv = A.lv3.ld(i, j, k);
     const R hm = U ? R(1) : P.hmz.ld(i, j, k), a = fz<R, AIN, IN>(g, U3, i, j, k);
     const R xl = XX(i, j, k - 1), xrr = XX(i, j, k);
-    const R S1 = fx<R, AIN, IN>(g, U1, i, j, k - 1) + fx<R, AIN, IN>(g, U1, i, j, k) +
-                 fx<R, AIN, IN>(g, U1, i + 1, j, k) + fx<R, AIN, IN>(g, U1, i + 1, j, k - 1);
+    const R S1 = VSUM_1Z;
     const R D1 = PS ? P.q.ld(i + 1, j, k) - P.q.ld(i - 1, j, k)
                     : dif4(XX(i - 1, j, k - 1), XX(i - 1, j, k), XX(i + 1, j, k - 1), XX(i + 1, j, k));
-    const R S2 = fy<R, AIN, IN>(g, U2, i, j, k - 1) + fy<R, AIN, IN>(g, U2, i, j + 1, k - 1) +
-                 fy<R, AIN, IN>(g, U2, i, j + 1, k) + fy<R, AIN, IN>(g, U2, i, j, k);
+    const R S2 = VSUM_2Z;
     const R D2 = PS ? P.q.ld(i, j + 1, k) - P.q.ld(i, j - 1, k)
                     : dif4(XX(i, j - 1, k - 1), XX(i, j - 1, k), XX(i, j + 1, k - 1), XX(i, j + 1, k));
     const R cr4 = S1 * D1 + S2 * D2;
@@ -492,6 +489,9 @@ __device__ __forceinline__ void ka_pseudo_cell(const Prob<R>& P, const AdjArr<R>
   }
 #undef XX
 #undef LX
+#undef AX
+#undef AY
+#undef AZ
 }
 template <class R, bool AIN>
 __global__ void KA_LB_PSEUDO ka_pseudo(const Prob<R> P, const AdjArr<R> A) {
@@ -627,6 +627,9 @@ __device__ __forceinline__ void ka_pseudo_std_cell(const Prob<R>& P, const AdjAr
   addat(A.lxant, i, j, k, A.lq.ld(i, j, k) / P.rhr.ld(i, j, k));
 #define XX(a, b, c) xr<R, IN>(g, X, (a), (b), (c))
 #define LX(a, b, c, v) xr_add<R, IN>(g, A.lxant, (a), (b), (c), (v))
+#define AX(f, b, c) fx<R, AIN, IN>(g, U1, (f), (b), (c))
+#define AY(a, f, c) fy<R, AIN, IN>(g, U2, (a), (f), (c))
+#define AZ(a, b, f) fz<R, AIN, IN>(g, U3, (a), (b), (f))
   // the face's own velocity, donor flux and vdyfa; returns lambda of v after f*ns
 #define FACE_HEAD(LV, LF, V, AF, HM, XLI, XLJ, XLK)                                                     \
   const R v = V.ld(i, j, k), hm = HM.ld(i, j, k), a = AF;                                           \
@@ -642,8 +645,7 @@ __device__ __forceinline__ void ka_pseudo_std_cell(const Prob<R>& P, const AdjAr
   if (IN || g.bx || i > 1) {
     FACE_HEAD(A.lv1, A.lf1, P.v1, (fx<R, AIN, IN>(g, U1, i, j, k)), P.hmx, i - 1, j, k)
     {
-      const R b = fy<R, AIN, IN>(g, U2, i - 1, j, k) + fy<R, AIN, IN>(g, U2, i - 1, j + 1, k) +
-                  fy<R, AIN, IN>(g, U2, i, j + 1, k) + fy<R, AIN, IN>(g, U2, i, j, k);
+      const R b = VSUM_2X;
       const VcTerm<R> c = vcorra_adj<R, IN>(g, X, A.lxant, lv, a, b, hm, i - 1, j + 1, k, i, j + 1, k, i - 1, j - 1, k,
                                         i, j - 1, k);
       la += c.la;
@@ -653,8 +655,7 @@ __device__ __forceinline__ void ka_pseudo_std_cell(const Prob<R>& P, const AdjAr
       fy_add<R, AIN, IN>(g, A.la2, i, j, k, c.lb);
     }
     if (zt) {
-      const R b = fz<R, AIN, IN>(g, U3, i - 1, j, k) + fz<R, AIN, IN>(g, U3, i - 1, j, k + 1) +
-                  fz<R, AIN, IN>(g, U3, i, j, k + 1) + fz<R, AIN, IN>(g, U3, i, j, k);
+      const R b = VSUM_3X;
       const VcTerm<R> c = vcorra_adj<R, IN>(g, X, A.lxant, lv, a, b, hm, i - 1, j, k + 1, i, j, k + 1, i - 1, j, k - 1,
                                         i, j, k - 1);
       la += c.la;
@@ -668,8 +669,7 @@ __device__ __forceinline__ void ka_pseudo_std_cell(const Prob<R>& P, const AdjAr
   if (IN || g.by || j > 1) {
     FACE_HEAD(A.lv2, A.lf2, P.v2, (fy<R, AIN, IN>(g, U2, i, j, k)), P.hmy, i, j - 1, k)
     {
-      const R b = fx<R, AIN, IN>(g, U1, i, j - 1, k) + fx<R, AIN, IN>(g, U1, i, j, k) + fx<R, AIN, IN>(g, U1, i + 1, j, k) +
-                  fx<R, AIN, IN>(g, U1, i + 1, j - 1, k);
+      const R b = VSUM_1Y;
       const VcTerm<R> c = vcorra_adj<R, IN>(g, X, A.lxant, lv, a, b, hm, i + 1, j - 1, k, i + 1, j, k, i - 1, j - 1, k,
                                         i - 1, j, k);
       la += c.la;
@@ -679,8 +679,7 @@ __device__ __forceinline__ void ka_pseudo_std_cell(const Prob<R>& P, const AdjAr
       fx_add<R, AIN, IN>(g, A.la1, i + 1, j - 1, k, c.lb);
     }
     if (zt) {
-      const R b = fz<R, AIN, IN>(g, U3, i, j - 1, k) + fz<R, AIN, IN>(g, U3, i, j, k) + fz<R, AIN, IN>(g, U3, i, j, k + 1) +
-                  fz<R, AIN, IN>(g, U3, i, j - 1, k + 1);
+      const R b = VSUM_3Y;
       const VcTerm<R> c = vcorra_adj<R, IN>(g, X, A.lxant, lv, a, b, hm, i, j - 1, k + 1, i, j, k + 1, i, j - 1, k - 1,
                                         i, j, k - 1);
       la += c.la;
@@ -694,8 +693,7 @@ __device__ __forceinline__ void ka_pseudo_std_cell(const Prob<R>& P, const AdjAr
   if (IN || g.bz || k > 1) {
     FACE_HEAD(A.lv3, A.lf3, P.v3, (fz<R, AIN, IN>(g, U3, i, j, k)), P.hmz, i, j, k - 1)
     {
-      const R b = fx<R, AIN, IN>(g, U1, i, j, k - 1) + fx<R, AIN, IN>(g, U1, i, j, k) + fx<R, AIN, IN>(g, U1, i + 1, j, k) +
-                  fx<R, AIN, IN>(g, U1, i + 1, j, k - 1);
+      const R b = VSUM_1Z;
       const VcTerm<R> c = vcorra_adj<R, IN>(g, X, A.lxant, lv, a, b, hm, i + 1, j, k - 1, i + 1, j, k, i - 1, j, k - 1,
                                         i - 1, j, k);
       la += c.la;
@@ -705,8 +703,7 @@ __device__ __forceinline__ void ka_pseudo_std_cell(const Prob<R>& P, const AdjAr
       fx_add<R, AIN, IN>(g, A.la1, i + 1, j, k - 1, c.lb);
     }
     {
-      const R b = fy<R, AIN, IN>(g, U2, i, j, k - 1) + fy<R, AIN, IN>(g, U2, i, j + 1, k - 1) +
-                  fy<R, AIN, IN>(g, U2, i, j + 1, k) + fy<R, AIN, IN>(g, U2, i, j, k);
+      const R b = VSUM_2Z;
       const VcTerm<R> c = vcorra_adj<R, IN>(g, X, A.lxant, lv, a, b, hm, i, j + 1, k - 1, i, j + 1, k, i, j - 1, k - 1,
                                         i, j - 1, k);
       la += c.la;
@@ -720,6 +717,9 @@ __device__ __forceinline__ void ka_pseudo_std_cell(const Prob<R>& P, const AdjAr
 #undef FACE_HEAD
 #undef XX
 #undef LX
+#undef AX
+#undef AY
+#undef AZ
 }
 template <class R, bool AIN>
 __global__ void __launch_bounds__(128) ka_pseudo_std(const Prob<R> P, const AdjArr<R> A) {

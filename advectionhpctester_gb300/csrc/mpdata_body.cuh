@@ -105,6 +105,17 @@ __device__ __forceinline__ bool warp_interior(const Geo& g, int i, int j, int k)
   return __all_sync(0xffffffffu, in);
 }
 
+// Warp-uniform: every lane holds a cell that is on the grid and, on each
+// axis, either periodic or in [2, n-1].  Such warps read through the boundary
+// maps, which are then plain wraps, and may take the precomputed pair sums
+// (pairs_body fills the wrapped ones).  Every lane of a full warp calls it,
+// before any lane returns.
+__device__ __forceinline__ bool warp_periodic_interior(const Geo& g, int i, int j, int k) {
+  const bool ok = i <= g.np && j <= g.mp && (g.bx || (i >= 2 && i < g.np)) && (g.by || (j >= 2 && j < g.mp)) &&
+                  (g.bz || (k >= 2 && k < g.lp));
+  return __all_sync(0xffffffffu, ok);
+}
+
 // The standard form's pseudo-velocity pieces with their velocity-only
 // factors precomputed (a batch velocity group, gvs): vdyfa with
 // ka = |a|-a*a*hm, vcorra with bc = (0.125*a)*b.  Same operations, same order.
@@ -142,6 +153,18 @@ __device__ __forceinline__ bool warp_unit_cell(const Prob<R>& P, int i, int j, i
   }
 }
 
+// The 4-face velocity sums of the cross terms as two cell-centred pairs, the
+// lower cell first: the oracle's fixed order for the reference's
+// unparenthesised sums (antidiff3d-gauge-gpubc.f90:163-203).  The pair of
+// cell c along the velocity's own axis is, for the y velocity, a2(c)+a2(c+y).
+// The user defines the face accessors AX, AY, AZ and the cell (i, j, k).
+#define VSUM_2X ((AY(i - 1, j, k) + AY(i - 1, j + 1, k)) + (AY(i, j, k) + AY(i, j + 1, k)))
+#define VSUM_3X ((AZ(i - 1, j, k) + AZ(i - 1, j, k + 1)) + (AZ(i, j, k) + AZ(i, j, k + 1)))
+#define VSUM_1Y ((AX(i, j - 1, k) + AX(i + 1, j - 1, k)) + (AX(i, j, k) + AX(i + 1, j, k)))
+#define VSUM_3Y ((AZ(i, j - 1, k) + AZ(i, j - 1, k + 1)) + (AZ(i, j, k) + AZ(i, j, k + 1)))
+#define VSUM_1Z ((AX(i, j, k - 1) + AX(i + 1, j, k - 1)) + (AX(i, j, k) + AX(i + 1, j, k)))
+#define VSUM_2Z ((AY(i, j, k - 1) + AY(i, j + 1, k - 1)) + (AY(i, j, k) + AY(i, j + 1, k)))
+
 // Velocity-only terms of the first corrective pass's gauge pseudo-velocities
 // (pseudo_form with AIN), stored by a velocity group's owner for all of the
 // group's fields: per face, the 4-face sums of the two cross terms in
@@ -160,8 +183,8 @@ __device__ __forceinline__ void velgroup_body(const Prob<R>& P, int i, int j, in
   const bool gg = P.gv & 1, gs = P.gv & 2;
   if (IN || g.bx || i > 1) {
     const R a = AX(i, j, k);
-    const R b1 = AY(i - 1, j, k) + AY(i - 1, j + 1, k) + AY(i, j + 1, k) + AY(i, j, k);
-    const R b2 = AZ(i - 1, j, k) + AZ(i - 1, j, k + 1) + AZ(i, j, k + 1) + AZ(i, j, k);
+    const R b1 = VSUM_2X;
+    const R b2 = VSUM_3X;
     const R ka = fabs(a) - a * a * hx;
     if (gg) {
       P.gvf[0].at(i, j, k) = b1;
@@ -177,8 +200,8 @@ __device__ __forceinline__ void velgroup_body(const Prob<R>& P, int i, int j, in
   }
   if (IN || g.by || j > 1) {
     const R a = AY(i, j, k);
-    const R b1 = AX(i, j - 1, k) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j - 1, k);
-    const R b2 = AZ(i, j - 1, k) + AZ(i, j, k) + AZ(i, j, k + 1) + AZ(i, j - 1, k + 1);
+    const R b1 = VSUM_1Y;
+    const R b2 = VSUM_3Y;
     const R ka = fabs(a) - a * a * hy;
     if (gg) {
       P.gvf[4].at(i, j, k) = b1;
@@ -194,8 +217,8 @@ __device__ __forceinline__ void velgroup_body(const Prob<R>& P, int i, int j, in
   }
   if (IN || g.bz || k > 1) {
     const R a = AZ(i, j, k);
-    const R b1 = AX(i, j, k - 1) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j, k - 1);
-    const R b2 = AY(i, j, k - 1) + AY(i, j + 1, k - 1) + AY(i, j + 1, k) + AY(i, j, k);
+    const R b1 = VSUM_1Z;
+    const R b2 = VSUM_2Z;
     const R ka = fabs(a) - a * a * hz;
     if (gg) {
       P.gvf[8].at(i, j, k) = b1;
@@ -312,9 +335,11 @@ __device__ __forceinline__ void upwind_body(const Prob<R>& P, int i, int j, int 
 // (gauge, interior warps): the pair sums of xant the rat4 terms start with
 // are read from cp, cn and q, where k_pairs stored them.  GV (gauge, first
 // pass, interior warps of a batch velocity group): the velocity-only terms
-// are read from gvf (velgroup_body).
+// are read from gvf (velgroup_body).  PV (gauge, interior warps, with PS):
+// the velocities' cell-centred pairs of the 4-face sums are read from f1..f3,
+// where k_pairs stored them.
 template <class R, bool STD, bool AIN, bool IN = false, bool U = false, bool PS = false, bool GV = false,
-          bool DEFER = true>
+          bool DEFER = true, bool PV = false>
 __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int k) {
   const Geo& g = P.g;
   const Arr<R>& X = P.xant;
@@ -327,6 +352,15 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
 #define AX(f, b, c) fx<R, AIN, IN>(g, A1, (f), (b), (c))
 #define AY(a, f, c) fy<R, AIN, IN>(g, A2, (a), (f), (c))
 #define AZ(a, b, f) fz<R, AIN, IN>(g, A3, (a), (b), (f))
+#define MX(a) cx<IN>(g, (a))
+#define MY(a) cy<IN>(g, (a))
+#define MZ(a) cz<IN>(g, (a))
+#define S2X (PV ? P.f2.ld(MX(i - 1), j, k) + P.f2.ld(i, j, k) : VSUM_2X)
+#define S3X (PV ? P.f3.ld(MX(i - 1), j, k) + P.f3.ld(i, j, k) : VSUM_3X)
+#define S1Y (PV ? P.f1.ld(i, MY(j - 1), k) + P.f1.ld(i, j, k) : VSUM_1Y)
+#define S3Y (PV ? P.f3.ld(i, MY(j - 1), k) + P.f3.ld(i, j, k) : VSUM_3Y)
+#define S1Z (PV ? P.f1.ld(i, j, MZ(k - 1)) + P.f1.ld(i, j, k) : VSUM_1Z)
+#define S2Z (PV ? P.f2.ld(i, j, MZ(k - 1)) + P.f2.ld(i, j, k) : VSUM_2Z)
   // DEFER: results held until every load is issued (see limit_form); the
   // batch kernels, whose launch bound admits 256 threads, store each face at
   // once, which keeps their register count (and occupancy) lower
@@ -357,26 +391,26 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
             vcorra_b<U>(P.gvs[1].ld(i, j, k), y1, y2, hmx);
       else
         v = vdyfa_u<U>(XX(i - 1, j, k), XX(i, j, k), a, hmx, ep) +
-            vcorra_u<U>(a, AY(i - 1, j, k) + AY(i - 1, j + 1, k) + AY(i, j + 1, k) + AY(i, j, k), y1, y2, hmx);
+            vcorra_u<U>(a, S2X, y1, y2, hmx);
       if (zt) {
         const R z1 = (fabs(XX(i - 1, j, k + 1)) + fabs(XX(i, j, k + 1))) -
                      (fabs(XX(i - 1, j, k - 1)) + fabs(XX(i, j, k - 1)));
         const R z2 = fabs(XX(i - 1, j, k + 1)) + fabs(XX(i, j, k + 1)) + fabs(XX(i - 1, j, k - 1)) +
                      fabs(XX(i, j, k - 1)) + ep;
         v = v + (GV ? vcorra_b<U>(P.gvs[2].ld(i, j, k), z1, z2, hmx)
-                    : vcorra_u<U>(a, AZ(i - 1, j, k) + AZ(i - 1, j, k + 1) + AZ(i, j, k + 1) + AZ(i, j, k), z1, z2,
+                    : vcorra_u<U>(a, S3X, z1, z2,
                                   hmx));
       }
       put(0, v, donor(XX(i - 1, j, k), XX(i, j, k), v));
     } else {
-      const R d2 = PS ? P.cp.ld(i, j + 1, k) - P.cp.ld(i, j - 1, k)
+      const R d2 = PS ? P.cp.ld(i, MY(j + 1), k) - P.cp.ld(i, MY(j - 1), k)
                       : dif4(XX(i - 1, j - 1, k), XX(i, j - 1, k), XX(i - 1, j + 1, k), XX(i, j + 1, k));
-      const R c2 = (GV ? P.gvf[0].ld(i, j, k) : AY(i - 1, j, k) + AY(i - 1, j + 1, k) + AY(i, j + 1, k) + AY(i, j, k)) * d2;
+      const R c2 = (GV ? P.gvf[0].ld(i, j, k) : S2X) * d2;
       R cr = c2;
       if (zt) {
-        const R d3 = PS ? P.cp.ld(i, j, k + 1) - P.cp.ld(i, j, k - 1)
+        const R d3 = PS ? P.cp.ld(i, j, MZ(k + 1)) - P.cp.ld(i, j, MZ(k - 1))
                         : dif4(XX(i - 1, j, k - 1), XX(i, j, k - 1), XX(i - 1, j, k + 1), XX(i, j, k + 1));
-        cr = c2 + (GV ? P.gvf[1].ld(i, j, k) : AZ(i - 1, j, k) + AZ(i - 1, j, k + 1) + AZ(i, j, k + 1) + AZ(i, j, k)) * d3;
+        cr = c2 + (GV ? P.gvf[1].ld(i, j, k) : S3X) * d3;
       }
       if (GV)
         v = P.gvf[2].ld(i, j, k) * (XX(i, j, k) - XX(i - 1, j, k)) - P.gvf[3].ld(i, j, k) * cr;
@@ -399,26 +433,26 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
             vcorra_b<U>(P.gvs[4].ld(i, j, k), y1, y2, hmy);
       else
         v = vdyfa_u<U>(XX(i, j - 1, k), XX(i, j, k), a, hmy, ep) +
-            vcorra_u<U>(a, AX(i, j - 1, k) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j - 1, k), y1, y2, hmy);
+            vcorra_u<U>(a, S1Y, y1, y2, hmy);
       if (zt) {
         const R z1 = (fabs(XX(i, j - 1, k + 1)) + fabs(XX(i, j, k + 1))) -
                      (fabs(XX(i, j - 1, k - 1)) + fabs(XX(i, j, k - 1)));
         const R z2 = fabs(XX(i, j - 1, k + 1)) + fabs(XX(i, j, k + 1)) + fabs(XX(i, j - 1, k - 1)) +
                      fabs(XX(i, j, k - 1)) + ep;
         v = v + (GV ? vcorra_b<U>(P.gvs[5].ld(i, j, k), z1, z2, hmy)
-                    : vcorra_u<U>(a, AZ(i, j - 1, k) + AZ(i, j, k) + AZ(i, j, k + 1) + AZ(i, j - 1, k + 1), z1, z2,
+                    : vcorra_u<U>(a, S3Y, z1, z2,
                                   hmy));
       }
       put(1, v, donor(XX(i, j - 1, k), XX(i, j, k), v));
     } else {
-      const R d1 = PS ? P.cn.ld(i + 1, j, k) - P.cn.ld(i - 1, j, k)
+      const R d1 = PS ? P.cn.ld(MX(i + 1), j, k) - P.cn.ld(MX(i - 1), j, k)
                       : dif4(XX(i - 1, j - 1, k), XX(i - 1, j, k), XX(i + 1, j - 1, k), XX(i + 1, j, k));
-      const R c1 = (GV ? P.gvf[4].ld(i, j, k) : AX(i, j - 1, k) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j - 1, k)) * d1;
+      const R c1 = (GV ? P.gvf[4].ld(i, j, k) : S1Y) * d1;
       R cr = c1;
       if (zt) {
-        const R d3 = PS ? P.cn.ld(i, j, k + 1) - P.cn.ld(i, j, k - 1)
+        const R d3 = PS ? P.cn.ld(i, j, MZ(k + 1)) - P.cn.ld(i, j, MZ(k - 1))
                         : dif4(XX(i, j - 1, k - 1), XX(i, j, k - 1), XX(i, j - 1, k + 1), XX(i, j, k + 1));
-        cr = c1 + (GV ? P.gvf[5].ld(i, j, k) : AZ(i, j - 1, k) + AZ(i, j, k) + AZ(i, j, k + 1) + AZ(i, j - 1, k + 1)) * d3;
+        cr = c1 + (GV ? P.gvf[5].ld(i, j, k) : S3Y) * d3;
       }
       if (GV)
         v = P.gvf[6].ld(i, j, k) * (XX(i, j, k) - XX(i, j - 1, k)) - P.gvf[7].ld(i, j, k) * cr;
@@ -445,16 +479,16 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
             vcorra_b<U>(P.gvs[7].ld(i, j, k), x1, x2, hmz) + vcorra_b<U>(P.gvs[8].ld(i, j, k), y1, y2, hmz);
       else
         v = vdyfa_u<U>(XX(i, j, k - 1), XX(i, j, k), a, hmz, ep) +
-            vcorra_u<U>(a, AX(i, j, k - 1) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j, k - 1), x1, x2, hmz) +
-            vcorra_u<U>(a, AY(i, j, k - 1) + AY(i, j + 1, k - 1) + AY(i, j + 1, k) + AY(i, j, k), y1, y2, hmz);
+            vcorra_u<U>(a, S1Z, x1, x2, hmz) +
+            vcorra_u<U>(a, S2Z, y1, y2, hmz);
       put(2, v, donor(XX(i, j, k - 1), XX(i, j, k), v));
     } else {
-      const R d1 = PS ? P.q.ld(i + 1, j, k) - P.q.ld(i - 1, j, k)
+      const R d1 = PS ? P.q.ld(MX(i + 1), j, k) - P.q.ld(MX(i - 1), j, k)
                       : dif4(XX(i - 1, j, k - 1), XX(i - 1, j, k), XX(i + 1, j, k - 1), XX(i + 1, j, k));
-      const R d2 = PS ? P.q.ld(i, j + 1, k) - P.q.ld(i, j - 1, k)
+      const R d2 = PS ? P.q.ld(i, MY(j + 1), k) - P.q.ld(i, MY(j - 1), k)
                       : dif4(XX(i, j - 1, k - 1), XX(i, j - 1, k), XX(i, j + 1, k - 1), XX(i, j + 1, k));
-      const R cr = (GV ? P.gvf[8].ld(i, j, k) : AX(i, j, k - 1) + AX(i, j, k) + AX(i + 1, j, k) + AX(i + 1, j, k - 1)) * d1 +
-                   (GV ? P.gvf[9].ld(i, j, k) : AY(i, j, k - 1) + AY(i, j + 1, k - 1) + AY(i, j + 1, k) + AY(i, j, k)) * d2;
+      const R cr = (GV ? P.gvf[8].ld(i, j, k) : S1Z) * d1 +
+                   (GV ? P.gvf[9].ld(i, j, k) : S2Z) * d2;
       if (GV)
         v = P.gvf[10].ld(i, j, k) * (XX(i, j, k) - XX(i, j, k - 1)) - P.gvf[11].ld(i, j, k) * cr;
       else
@@ -476,18 +510,28 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
       if (STD) P.f3.at(i, j, k) = fo[2];
     }
   }
+#undef MX
+#undef MY
+#undef MZ
+#undef S2X
+#undef S3X
+#undef S1Y
+#undef S3Y
+#undef S1Z
+#undef S2Z
 #undef XX
 #undef AX
 #undef AY
 #undef AZ
 }
 
-template <class R, bool AIN, bool IN = false, bool U = false, bool PS = false, bool GV = false, bool DEFER = true>
+template <class R, bool AIN, bool IN = false, bool U = false, bool PS = false, bool GV = false, bool DEFER = true,
+          bool PV = false>
 __device__ __forceinline__ void pseudo_body(const Prob<R>& P, int i, int j, int k) {
   if (P.stdf)
     pseudo_form<R, true, AIN, IN, U, false, GV, DEFER>(P, i, j, k);
   else
-    pseudo_form<R, false, AIN, IN, U, PS, GV, DEFER>(P, i, j, k);
+    pseudo_form<R, false, AIN, IN, U, PS, GV, DEFER, PV>(P, i, j, k);
 }
 
 // ---- limiter bounds and ratios (std :256-348, gauge :238-324) -------------
@@ -648,14 +692,34 @@ __device__ __forceinline__ void block_ratios(const Prob<R>& P, int i, int j, int
 // x(j)+x(j-1) into cn, Sz = x(k)+x(k-1) into q.  The operand order is that of
 // the rat4 sums (antidiff3d-gauge-gpubc.f90:89-203), so every difference of
 // two of them is the value rat4's own sums give.  cp, cn and q are free
-// until the limiter bounds stage rewrites them.
-template <class R>
+// until the limiter bounds stage rewrites them.  A periodic axis also gets
+// the wrapped pair of its first cell (x(1)+x(n)).  PV: also the pass
+// velocities' cell-centred pairs of the 4-face sums (VSUM_*), a1(i)+a1(i+1)
+// into f1, a2(j)+a2(j+1) into f2, a3(k)+a3(k+1) into f3, which the gauge form
+// leaves unused outside the density step.  The face reads take the boundary
+// rules, so the pairs interior warps read are the sums their faces give.
+template <class R, bool AIN = true, bool PV = false>
 __device__ __forceinline__ void pairs_body(const Prob<R>& P, int i, int j, int k) {
+  const Geo& g = P.g;
   const Arr<R>& X = P.xant;
   const R x = X.ld(i, j, k);
-  if (i > 1) P.cp.at(i, j, k) = x + X.ld(i - 1, j, k);
-  if (j > 1) P.cn.at(i, j, k) = x + X.ld(i, j - 1, k);
-  if (k > 1) P.q.at(i, j, k) = x + X.ld(i, j, k - 1);
+  R a1 = R(0), a2 = R(0), a3 = R(0);
+  if (PV) {
+    const Arr<R>& A1 = AIN ? P.u1 : P.w1;
+    const Arr<R>& A2 = AIN ? P.u2 : P.w2;
+    const Arr<R>& A3 = AIN ? P.u3 : P.w3;
+    a1 = fx<R, AIN>(g, A1, i, j, k) + fx<R, AIN>(g, A1, i + 1, j, k);
+    a2 = fy<R, AIN>(g, A2, i, j, k) + fy<R, AIN>(g, A2, i, j + 1, k);
+    a3 = fz<R, AIN>(g, A3, i, j, k) + fz<R, AIN>(g, A3, i, j, k + 1);
+  }
+  if (i > 1 || g.bx) P.cp.at(i, j, k) = x + X.ld(i > 1 ? i - 1 : g.np, j, k);
+  if (j > 1 || g.by) P.cn.at(i, j, k) = x + X.ld(i, j > 1 ? j - 1 : g.mp, k);
+  if (k > 1 || g.bz) P.q.at(i, j, k) = x + X.ld(i, j, k > 1 ? k - 1 : g.lp);
+  if (PV) {
+    P.f1.at(i, j, k) = a1;
+    P.f2.at(i, j, k) = a2;
+    P.f3.at(i, j, k) = a3;
+  }
 }
 
 // ---- limited antidiffusive velocities and fluxes --------------------------

@@ -127,12 +127,31 @@ __global__ void __launch_bounds__(128, PseudoMinBlocks<R>::v) k_pseudo(const Pro
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int k = blockIdx.z + 1;
   const bool win = warp_interior(P.g, i, j, k);
+  // FP64 with every pair sum stored: warps on a periodic seam read them too,
+  // through the wrap maps
+  bool pin = false;
+  if constexpr (sizeof(R) == 8)
+    if (!win && P.pairs == 2) pin = warp_periodic_interior(P.g, i, j, k);
   if (i > P.g.np || j > P.g.mp) return;
   if (!win) {
+    if constexpr (sizeof(R) == 8) {
+      if (pin) {
+        if (warp_unit_faces(P, i, j, k))
+          pseudo_body<R, AIN, false, true, true, false, D, true>(P, i, j, k);
+        else
+          pseudo_body<R, AIN, false, false, true, false, D, true>(P, i, j, k);
+        return;
+      }
+    }
     pseudo_body<R, AIN, false, false, false, false, D>(P, i, j, k);
   } else if constexpr (sizeof(R) == 8) {
     const bool unit = warp_unit_faces(P, i, j, k);
-    if (P.pairs) {
+    if (P.pairs == 2) {
+      if (unit)
+        pseudo_body<R, AIN, true, true, true, false, D, true>(P, i, j, k);
+      else
+        pseudo_body<R, AIN, true, false, true, false, D, true>(P, i, j, k);
+    } else if (P.pairs) {
       if (unit)
         pseudo_body<R, AIN, true, true, true, false, D>(P, i, j, k);
       else
@@ -148,10 +167,10 @@ __global__ void __launch_bounds__(128, PseudoMinBlocks<R>::v) k_pseudo(const Pro
   }
 }
 
-template <class R>
+template <class R, bool AIN, bool PV>
 __global__ void __launch_bounds__(128) k_pairs(const Prob<R> P) {
   CELL_INDEX
-  pairs_body<R>(P, i, j, k);
+  pairs_body<R, AIN, PV>(P, i, j, k);
 }
 template <class R, bool NONOS, bool FIRST, bool KEEP>
 __global__ void __launch_bounds__(128, (MinBlocks<R, MPDATA_MINB_BOUNDS_F64, MPDATA_MINB_BOUNDS_F32>::v)) k_bounds(const Prob<R> P) {
@@ -223,12 +242,16 @@ int run_step(const Prob<R>& P, int iord, int nonos, Prof* prof, cudaStream_t s) 
   }
   LAUNCH(ST_UPWIND, (k_upwind<R, true><<<grd, blk, 0, s>>>(P)));
   const bool keep = iord > 2;
-  // FP64 gauge form: the pseudo-velocity stage reads precomputed pair sums
+  // FP64 gauge form: the pseudo-velocity stage reads precomputed pair sums of
+  // xant (pairs 1) and, outside the density step, whose upwind fluxes hold
+  // f1..f3, of the pass velocities too (pairs 2)
   Prob<R> Q = P;
-  Q.pairs = (!P.stdf && sizeof(R) == 8) ? 1 : 0;
+  Q.pairs = (!P.stdf && sizeof(R) == 8) ? (P.rho ? 1 : 2) : 0;
   for (int pass = 2; pass <= iord; pass++) {
     const bool first = (pass == 2), last = (pass == iord);
-    if (Q.pairs) LAUNCH(ST_PAIRS, (k_pairs<R><<<grd, blk, 0, s>>>(Q)));
+    if (Q.pairs == 2 && first) LAUNCH(ST_PAIRS, (k_pairs<R, true, true><<<grd, blk, 0, s>>>(Q)));
+    else if (Q.pairs == 2) LAUNCH(ST_PAIRS, (k_pairs<R, false, true><<<grd, blk, 0, s>>>(Q)));
+    else if (Q.pairs) LAUNCH(ST_PAIRS, (k_pairs<R, true, false><<<grd, blk, 0, s>>>(Q)));
     if (first) LAUNCH(ST_PSEUDO, (k_pseudo<R, true><<<grd, blk, 0, s>>>(Q)));
     else LAUNCH(ST_PSEUDO, (k_pseudo<R, false><<<grd, blk, 0, s>>>(Q)));
     if (!nonos) LAUNCH(ST_BOUNDS, (k_bounds<R, false, true, false><<<grd, blk, 0, s>>>(P)));

@@ -278,6 +278,15 @@ void upwind(const Dims& d, Buf<R>& xin, Buf<R>& u1, Buf<R>& u2, Buf<R>& u3, Buf<
       }
 }
 
+// The 4-face velocity sums of the cross terms (u2(i-1,j)+u2(i-1,j+1)+u2(i,j+1)
+// +u2(i,j) and its five siblings) carry no parentheses in the reference, and
+// Fortran may evaluate an unparenthesised sum in any mathematically equivalent
+// order; the reference's own builds reassociate (-Ofast, -O3, CMakeLists.txt:
+// 64-76).  This restatement fixes one order: the sum of two cell-centred pairs,
+// (a(c) + a(c+e)) + (a(c') + a(c'+e)), lower cell first, where a(c)+a(c+e) is
+// the cell's pair of faces along the velocity's own axis.  Every sum of the
+// pass then shares those pairs.
+
 // Whether plane k carries the z cross terms in the x/y pseudo-velocities:
 // the reference's k=1 and k=lp kernels drop them (antidiff3d-*-gpubc.f90).
 inline bool zterm(const Dims& d, int k) { return d.bz || (k > 1 && k < d.lp); }
@@ -295,14 +304,14 @@ void pseudo_std(const Dims& d, Buf<R>& x, Buf<R>& a1, Buf<R>& a2, Buf<R>& a3, Bu
         if (i >= i0) {
           const R hmx = R(1) / (R(0.5) * (h(i - 1, j, k) + h(i, j, k)));
           R v = vdyfa(x(i - 1, j, k), x(i, j, k), a1(i, j, k), hmx, ep) +
-                vcorra(a1(i, j, k), a2(i - 1, j, k) + a2(i - 1, j + 1, k) + a2(i, j + 1, k) + a2(i, j, k),
+                vcorra(a1(i, j, k), (a2(i - 1, j, k) + a2(i - 1, j + 1, k)) + (a2(i, j, k) + a2(i, j + 1, k)),
                        (absv(x(i - 1, j + 1, k)) + absv(x(i, j + 1, k))) -
                            (absv(x(i - 1, j - 1, k)) + absv(x(i, j - 1, k))),
                        absv(x(i - 1, j + 1, k)) + absv(x(i, j + 1, k)) +
                            absv(x(i - 1, j - 1, k)) + absv(x(i, j - 1, k)) + ep,
                        hmx);
           if (zt)
-            v = v + vcorra(a1(i, j, k), a3(i - 1, j, k) + a3(i - 1, j, k + 1) + a3(i, j, k + 1) + a3(i, j, k),
+            v = v + vcorra(a1(i, j, k), (a3(i - 1, j, k) + a3(i - 1, j, k + 1)) + (a3(i, j, k) + a3(i, j, k + 1)),
                            (absv(x(i - 1, j, k + 1)) + absv(x(i, j, k + 1))) -
                                (absv(x(i - 1, j, k - 1)) + absv(x(i, j, k - 1))),
                            absv(x(i - 1, j, k + 1)) + absv(x(i, j, k + 1)) +
@@ -314,14 +323,14 @@ void pseudo_std(const Dims& d, Buf<R>& x, Buf<R>& a1, Buf<R>& a2, Buf<R>& a3, Bu
         if (j >= j0) {
           const R hmy = R(1) / (R(0.5) * (h(i, j - 1, k) + h(i, j, k)));
           R v = vdyfa(x(i, j - 1, k), x(i, j, k), a2(i, j, k), hmy, ep) +
-                vcorra(a2(i, j, k), a1(i, j - 1, k) + a1(i, j, k) + a1(i + 1, j, k) + a1(i + 1, j - 1, k),
+                vcorra(a2(i, j, k), (a1(i, j - 1, k) + a1(i + 1, j - 1, k)) + (a1(i, j, k) + a1(i + 1, j, k)),
                        (absv(x(i + 1, j - 1, k)) + absv(x(i + 1, j, k))) -
                            (absv(x(i - 1, j - 1, k)) + absv(x(i - 1, j, k))),
                        absv(x(i + 1, j - 1, k)) + absv(x(i + 1, j, k)) +
                            absv(x(i - 1, j - 1, k)) + absv(x(i - 1, j, k)) + ep,
                        hmy);
           if (zt)
-            v = v + vcorra(a2(i, j, k), a3(i, j - 1, k) + a3(i, j, k) + a3(i, j, k + 1) + a3(i, j - 1, k + 1),
+            v = v + vcorra(a2(i, j, k), (a3(i, j - 1, k) + a3(i, j - 1, k + 1)) + (a3(i, j, k) + a3(i, j, k + 1)),
                            (absv(x(i, j - 1, k + 1)) + absv(x(i, j, k + 1))) -
                                (absv(x(i, j - 1, k - 1)) + absv(x(i, j, k - 1))),
                            absv(x(i, j - 1, k + 1)) + absv(x(i, j, k + 1)) +
@@ -333,13 +342,13 @@ void pseudo_std(const Dims& d, Buf<R>& x, Buf<R>& a1, Buf<R>& a2, Buf<R>& a3, Bu
         if (k >= k0) {
           const R hmz = R(1) / (R(0.5) * (h(i, j, k - 1) + h(i, j, k)));
           const R v = vdyfa(x(i, j, k - 1), x(i, j, k), a3(i, j, k), hmz, ep) +
-                      vcorra(a3(i, j, k), a1(i, j, k - 1) + a1(i, j, k) + a1(i + 1, j, k) + a1(i + 1, j, k - 1),
+                      vcorra(a3(i, j, k), (a1(i, j, k - 1) + a1(i + 1, j, k - 1)) + (a1(i, j, k) + a1(i + 1, j, k)),
                              (absv(x(i + 1, j, k - 1)) + absv(x(i + 1, j, k))) -
                                  (absv(x(i - 1, j, k - 1)) + absv(x(i - 1, j, k))),
                              absv(x(i + 1, j, k - 1)) + absv(x(i + 1, j, k)) +
                                  absv(x(i - 1, j, k - 1)) + absv(x(i - 1, j, k)) + ep,
                              hmz) +
-                      vcorra(a3(i, j, k), a2(i, j, k - 1) + a2(i, j + 1, k - 1) + a2(i, j + 1, k) + a2(i, j, k),
+                      vcorra(a3(i, j, k), (a2(i, j, k - 1) + a2(i, j + 1, k - 1)) + (a2(i, j, k) + a2(i, j + 1, k)),
                              (absv(x(i, j + 1, k - 1)) + absv(x(i, j + 1, k))) -
                                  (absv(x(i, j - 1, k - 1)) + absv(x(i, j - 1, k))),
                              absv(x(i, j + 1, k - 1)) + absv(x(i, j + 1, k)) +
@@ -366,31 +375,31 @@ void pseudo_gauge(const Dims& d, Buf<R>& x, Buf<R>& a1, Buf<R>& a2, Buf<R>& a3, 
       for (int i = 1; i <= d.np; i++) {
         if (i >= i0) {
           const R hmx = R(1) / (R(0.5) * (h(i - 1, j, k) + h(i, j, k)));
-          const R c2 = (a2(i - 1, j, k) + a2(i - 1, j + 1, k) + a2(i, j + 1, k) + a2(i, j, k)) *
+          const R c2 = ((a2(i - 1, j, k) + a2(i - 1, j + 1, k)) + (a2(i, j, k) + a2(i, j + 1, k))) *
                        rat4(x(i - 1, j - 1, k), x(i, j - 1, k), x(i - 1, j + 1, k), x(i, j + 1, k));
           R cr = c2;
           if (zt)
-            cr = c2 + (a3(i - 1, j, k) + a3(i - 1, j, k + 1) + a3(i, j, k + 1) + a3(i, j, k)) *
+            cr = c2 + ((a3(i - 1, j, k) + a3(i - 1, j, k + 1)) + (a3(i, j, k) + a3(i, j, k + 1))) *
                           rat4(x(i - 1, j, k - 1), x(i, j, k - 1), x(i - 1, j, k + 1), x(i, j, k + 1));
           v1(i, j, k) = vdyf(x(i - 1, j, k), x(i, j, k), a1(i, j, k), hmx) -
                         R(0.125) * a1(i, j, k) * hmx * cr;
         }
         if (j >= j0) {
           const R hmy = R(1) / (R(0.5) * (h(i, j - 1, k) + h(i, j, k)));
-          const R c1 = (a1(i, j - 1, k) + a1(i, j, k) + a1(i + 1, j, k) + a1(i + 1, j - 1, k)) *
+          const R c1 = ((a1(i, j - 1, k) + a1(i + 1, j - 1, k)) + (a1(i, j, k) + a1(i + 1, j, k))) *
                        rat4(x(i - 1, j - 1, k), x(i - 1, j, k), x(i + 1, j - 1, k), x(i + 1, j, k));
           R cr = c1;
           if (zt)
-            cr = c1 + (a3(i, j - 1, k) + a3(i, j, k) + a3(i, j, k + 1) + a3(i, j - 1, k + 1)) *
+            cr = c1 + ((a3(i, j - 1, k) + a3(i, j - 1, k + 1)) + (a3(i, j, k) + a3(i, j, k + 1))) *
                           rat4(x(i, j - 1, k - 1), x(i, j, k - 1), x(i, j - 1, k + 1), x(i, j, k + 1));
           v2(i, j, k) = vdyf(x(i, j - 1, k), x(i, j, k), a2(i, j, k), hmy) -
                         R(0.125) * a2(i, j, k) * hmy * cr;
         }
         if (k >= k0) {
           const R hmz = R(1) / (R(0.5) * (h(i, j, k - 1) + h(i, j, k)));
-          const R cr = (a1(i, j, k - 1) + a1(i, j, k) + a1(i + 1, j, k) + a1(i + 1, j, k - 1)) *
+          const R cr = ((a1(i, j, k - 1) + a1(i + 1, j, k - 1)) + (a1(i, j, k) + a1(i + 1, j, k))) *
                            rat4(x(i - 1, j, k - 1), x(i - 1, j, k), x(i + 1, j, k - 1), x(i + 1, j, k)) +
-                       (a2(i, j, k - 1) + a2(i, j + 1, k - 1) + a2(i, j + 1, k) + a2(i, j, k)) *
+                       ((a2(i, j, k - 1) + a2(i, j + 1, k - 1)) + (a2(i, j, k) + a2(i, j + 1, k))) *
                            rat4(x(i, j - 1, k - 1), x(i, j - 1, k), x(i, j + 1, k - 1), x(i, j + 1, k));
           v3(i, j, k) = vdyf(x(i, j, k - 1), x(i, j, k), a3(i, j, k), hmz) -
                         R(0.125) * a3(i, j, k) * hmz * cr;
