@@ -377,7 +377,9 @@ struct FaceAdj {
 
 // U: the warp's face densities are all exactly 1.  PS: the pair sums of the
 // pass's input field are in cp/cn/q (kf_pairs), as in the forward stage.
-template <class R, bool AIN, bool IN, bool U = false, bool PS = false>
+// PV (with PS): the velocities' cell-centred pairs are in f1..f3.  Without IN
+// (a warp on a periodic seam) the stored pairs are read through the wrap maps.
+template <class R, bool AIN, bool IN, bool U = false, bool PS = false, bool PV = false>
 __device__ __forceinline__ void ka_pseudo_cell(const Prob<R>& P, const AdjArr<R>& A, int i, int j, int k) {
   const Geo& g = P.g;
   const Arr<R>& X = P.xant;
@@ -390,18 +392,27 @@ __device__ __forceinline__ void ka_pseudo_cell(const Prob<R>& P, const AdjArr<R>
 #define AX(f, b, c) fx<R, AIN, IN>(g, U1, (f), (b), (c))
 #define AY(a, f, c) fy<R, AIN, IN>(g, U2, (a), (f), (c))
 #define AZ(a, b, f) fz<R, AIN, IN>(g, U3, (a), (b), (f))
+#define MX(a) cx<IN>(g, (a))
+#define MY(a) cy<IN>(g, (a))
+#define MZ(a) cz<IN>(g, (a))
+#define S2X_ (PV ? P.f2.ld(MX(i - 1), j, k) + P.f2.ld(i, j, k) : VSUM_2X)
+#define S3X_ (PV ? P.f3.ld(MX(i - 1), j, k) + P.f3.ld(i, j, k) : VSUM_3X)
+#define S1Y_ (PV ? P.f1.ld(i, MY(j - 1), k) + P.f1.ld(i, j, k) : VSUM_1Y)
+#define S3Y_ (PV ? P.f3.ld(i, MY(j - 1), k) + P.f3.ld(i, j, k) : VSUM_3Y)
+#define S1Z_ (PV ? P.f1.ld(i, j, MZ(k - 1)) + P.f1.ld(i, j, k) : VSUM_1Z)
+#define S2Z_ (PV ? P.f2.ld(i, j, MZ(k - 1)) + P.f2.ld(i, j, k) : VSUM_2Z)
   // x faces
   if (IN || g.bx || i > 1) {
     const R lv = A.lv1.ld(i, j, k);
     const R hm = U ? R(1) : P.hmx.ld(i, j, k), a = fx<R, AIN, IN>(g, U1, i, j, k);
     const R xl = XX(i - 1, j, k), xrr = XX(i, j, k);
-    const R S2 = VSUM_2X;
-    const R D2 = PS ? P.cp.ld(i, j + 1, k) - P.cp.ld(i, j - 1, k)
+    const R S2 = S2X_;
+    const R D2 = PS ? P.cp.ld(i, MY(j + 1), k) - P.cp.ld(i, MY(j - 1), k)
                     : dif4(XX(i - 1, j - 1, k), XX(i, j - 1, k), XX(i - 1, j + 1, k), XX(i, j + 1, k));
     R cr4 = S2 * D2, S3 = R(0), D3 = R(0);
     if (zt) {
-      S3 = VSUM_3X;
-      D3 = PS ? P.cp.ld(i, j, k + 1) - P.cp.ld(i, j, k - 1)
+      S3 = S3X_;
+      D3 = PS ? P.cp.ld(i, j, MZ(k + 1)) - P.cp.ld(i, j, MZ(k - 1))
               : dif4(XX(i - 1, j, k - 1), XX(i, j, k - 1), XX(i - 1, j, k + 1), XX(i, j, k + 1));
       cr4 = cr4 + S3 * D3;
     }
@@ -429,13 +440,13 @@ __device__ __forceinline__ void ka_pseudo_cell(const Prob<R>& P, const AdjArr<R>
     const R lv = A.lv2.ld(i, j, k);
     const R hm = U ? R(1) : P.hmy.ld(i, j, k), a = fy<R, AIN, IN>(g, U2, i, j, k);
     const R xl = XX(i, j - 1, k), xrr = XX(i, j, k);
-    const R S1 = VSUM_1Y;
-    const R D1 = PS ? P.cn.ld(i + 1, j, k) - P.cn.ld(i - 1, j, k)
+    const R S1 = S1Y_;
+    const R D1 = PS ? P.cn.ld(MX(i + 1), j, k) - P.cn.ld(MX(i - 1), j, k)
                     : dif4(XX(i - 1, j - 1, k), XX(i - 1, j, k), XX(i + 1, j - 1, k), XX(i + 1, j, k));
     R cr4 = S1 * D1, S3 = R(0), D3 = R(0);
     if (zt) {
-      S3 = VSUM_3Y;
-      D3 = PS ? P.cn.ld(i, j, k + 1) - P.cn.ld(i, j, k - 1)
+      S3 = S3Y_;
+      D3 = PS ? P.cn.ld(i, j, MZ(k + 1)) - P.cn.ld(i, j, MZ(k - 1))
               : dif4(XX(i, j - 1, k - 1), XX(i, j, k - 1), XX(i, j - 1, k + 1), XX(i, j, k + 1));
       cr4 = cr4 + S3 * D3;
     }
@@ -463,11 +474,11 @@ __device__ __forceinline__ void ka_pseudo_cell(const Prob<R>& P, const AdjArr<R>
     const R lv = A.lv3.ld(i, j, k);
     const R hm = U ? R(1) : P.hmz.ld(i, j, k), a = fz<R, AIN, IN>(g, U3, i, j, k);
     const R xl = XX(i, j, k - 1), xrr = XX(i, j, k);
-    const R S1 = VSUM_1Z;
-    const R D1 = PS ? P.q.ld(i + 1, j, k) - P.q.ld(i - 1, j, k)
+    const R S1 = S1Z_;
+    const R D1 = PS ? P.q.ld(MX(i + 1), j, k) - P.q.ld(MX(i - 1), j, k)
                     : dif4(XX(i - 1, j, k - 1), XX(i - 1, j, k), XX(i + 1, j, k - 1), XX(i + 1, j, k));
-    const R S2 = VSUM_2Z;
-    const R D2 = PS ? P.q.ld(i, j + 1, k) - P.q.ld(i, j - 1, k)
+    const R S2 = S2Z_;
+    const R D2 = PS ? P.q.ld(i, MY(j + 1), k) - P.q.ld(i, MY(j - 1), k)
                     : dif4(XX(i, j - 1, k - 1), XX(i, j - 1, k), XX(i, j + 1, k - 1), XX(i, j + 1, k));
     const R cr4 = S1 * D1 + S2 * D2;
     const FaceAdj<R, U> f(lv, a, hm, xl, xrr, cr4);
@@ -492,6 +503,15 @@ __device__ __forceinline__ void ka_pseudo_cell(const Prob<R>& P, const AdjArr<R>
 #undef AX
 #undef AY
 #undef AZ
+#undef MX
+#undef MY
+#undef MZ
+#undef S2X_
+#undef S3X_
+#undef S1Y_
+#undef S3Y_
+#undef S1Z_
+#undef S2Z_
 }
 template <class R, bool AIN>
 __global__ void KA_LB_PSEUDO ka_pseudo(const Prob<R> P, const AdjArr<R> A) {
@@ -499,12 +519,30 @@ __global__ void KA_LB_PSEUDO ka_pseudo(const Prob<R> P, const AdjArr<R> A) {
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int k = blockIdx.z + 1;
   const bool win = warp_interior(P.g, i, j, k);
+  // every pair sum stored (pairs 2): warps on a periodic seam read them too
+  bool pin = false;
+  if constexpr (sizeof(R) == 8)
+    if (!win && P.pairs == 2) pin = warp_periodic_interior(P.g, i, j, k);
   if (i > P.g.np || j > P.g.mp) return;
   if (!win) {
+    if constexpr (sizeof(R) == 8) {
+      if (pin) {
+        if (warp_unit_faces(P, i, j, k))
+          ka_pseudo_cell<R, AIN, false, true, true, true>(P, A, i, j, k);
+        else
+          ka_pseudo_cell<R, AIN, false, false, true, true>(P, A, i, j, k);
+        return;
+      }
+    }
     ka_pseudo_cell<R, AIN, false>(P, A, i, j, k);
   } else if constexpr (sizeof(R) == 8) {
     const bool unit = warp_unit_faces(P, i, j, k);
-    if (P.pairs) {
+    if (P.pairs == 2) {
+      if (unit)
+        ka_pseudo_cell<R, AIN, true, true, true, true>(P, A, i, j, k);
+      else
+        ka_pseudo_cell<R, AIN, true, false, true, true>(P, A, i, j, k);
+    } else if (P.pairs) {
       if (unit)
         ka_pseudo_cell<R, AIN, true, true, true>(P, A, i, j, k);
       else
@@ -841,11 +879,11 @@ __global__ void __launch_bounds__(128, (KfMinBlocks<R, 8, 10>::v)) kf_upwind(con
   FCELL_U(B)
 #undef B
 }
-template <class R>
+template <class R, bool AIN, bool PV>
 __global__ void __launch_bounds__(128) kf_pairs(const Prob<R> P) {
   ACELL
   (void)g;
-  pairs_body<R>(P, i, j, k);
+  pairs_body<R, AIN, PV>(P, i, j, k);
 }
 // the forward stage's dispatch: unit face densities and pair sums (FP64),
 // and the stage kernel's five resident blocks per SM for FP64
@@ -859,12 +897,29 @@ __global__ void __launch_bounds__(128, KfPseudoMinBlocks<R>::v) kf_pseudo(const 
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int k = blockIdx.z + 1;
   const bool win = warp_interior(P.g, i, j, k);
+  bool pin = false;
+  if constexpr (sizeof(R) == 8)
+    if (!win && P.pairs == 2) pin = warp_periodic_interior(P.g, i, j, k);
   if (i > P.g.np || j > P.g.mp) return;
   if (!win) {
+    if constexpr (sizeof(R) == 8) {
+      if (pin) {
+        if (warp_unit_faces(P, i, j, k))
+          pseudo_body<R, AIN, false, true, true, false, true, true>(P, i, j, k);
+        else
+          pseudo_body<R, AIN, false, false, true, false, true, true>(P, i, j, k);
+        return;
+      }
+    }
     pseudo_body<R, AIN, false>(P, i, j, k);
   } else if constexpr (sizeof(R) == 8) {
     const bool unit = warp_unit_faces(P, i, j, k);
-    if (P.pairs) {
+    if (P.pairs == 2) {
+      if (unit)
+        pseudo_body<R, AIN, true, true, true, false, true, true>(P, i, j, k);
+      else
+        pseudo_body<R, AIN, true, false, true, false, true, true>(P, i, j, k);
+    } else if (P.pairs) {
       if (unit)
         pseudo_body<R, AIN, true, true, true>(P, i, j, k);
       else
@@ -968,10 +1023,15 @@ int run_step_record(const Prob<R>& P, const AdjPlan<R>& A, int nonos, const Arr<
   for (int t = 0; t < np_; t++) {
     Prob<R> Qa = pass_prob(P, A, t, true);
     // FP64 gauge: pair sums of the pass's input field into its cp/cn/q
-    // records, which the bounds kernel fills afterwards
-    Qa.pairs = (!P.stdf && sizeof(R) == 8) ? 1 : 0;
+    // records, which the bounds kernel fills afterwards, and the velocity
+    // pairs into the workspace's f1..f3 (unused by the gauge form)
+    Qa.pairs = (!P.stdf && sizeof(R) == 8) ? 2 : 0;
     if (Qa.pairs) {
-      kf_pairs<R><<<grd, blk, 0, s>>>(Qa);
+      Qa.f1 = P.f1;
+      Qa.f2 = P.f2;
+      Qa.f3 = P.f3;
+      if (t == 0) kf_pairs<R, true, true><<<grd, blk, 0, s>>>(Qa);
+      else kf_pairs<R, false, true><<<grd, blk, 0, s>>>(Qa);
       n++;
     }
     if (t == 0) kf_pseudo<R, true><<<grd, blk, 0, s>>>(Qa);
@@ -1074,11 +1134,16 @@ int run_step_reverse(const Prob<R>& P, const AdjPlan<R>& A, int nonos, cudaStrea
         ka_limit<R, false><<<grd, blk, 0, s>>>(Q, a);
       }
       // the pass's cp/cn/q records are dead once the reverse bounds ran:
-      // they take the pair sums of its input field (FP64)
+      // they take the pair sums of its input field, and the workspace's
+      // f1..f3 the velocity pairs (FP64)
       Prob<R> Qp = Q;
-      Qp.pairs = sizeof(R) == 8 ? 1 : 0;
+      Qp.pairs = sizeof(R) == 8 ? 2 : 0;
       if (Qp.pairs) {
-        kf_pairs<R><<<grd, blk, 0, s>>>(Qp);
+        Qp.f1 = P.f1;
+        Qp.f2 = P.f2;
+        Qp.f3 = P.f3;
+        if (t == 0) kf_pairs<R, true, true><<<grd, blk, 0, s>>>(Qp);
+        else kf_pairs<R, false, true><<<grd, blk, 0, s>>>(Qp);
         n++;
       }
       if (t == 0) ka_pseudo<R, true><<<grd, blk, 0, s>>>(Qp, a);

@@ -106,11 +106,20 @@ __global__ void KB_LB_UPWIND kb_upwind(BATCH_ARGS) {
   BATCH_TILE_U(B)
 #undef B
 }
-// pair sums for the FP64 gauge problems (P.pairs), as k_pairs
+// pair sums for the FP64 gauge problems (P.pairs), as k_pairs, with the
+// velocity pairs except in the first pass of a gauge velocity group, whose
+// interior warps read the group's precomputed sums (gvf) instead
 template <class R>
+__device__ __forceinline__ bool batch_vpairs(const Prob<R>& P, bool ain) {
+  return P.pairs && !(ain && (P.gv & 1));
+}
+template <class R, bool AIN>
 __global__ void __launch_bounds__(256) kb_pairs(BATCH_ARGS) {
-#define B(IN) \
-  if (P.pairs) pairs_body<R>(P, i, j, k)
+#define B(IN)                                    \
+  if (batch_vpairs(P, AIN))                      \
+    pairs_body<R, AIN, true>(P, i, j, k);        \
+  else if (P.pairs)                              \
+    pairs_body<R, AIN, false>(P, i, j, k)
   BATCH_TILE(B)
 #undef B
 }
@@ -121,7 +130,7 @@ __global__ void __launch_bounds__(256) kb_copy(BATCH_ARGS) {
 #undef B
 }
 template <class R, bool AIN>
-__device__ __forceinline__ void pseudo_dispatch(const Prob<R>& P, int i, int j, int k, bool win) {
+__device__ __forceinline__ void pseudo_dispatch(const Prob<R>& P, int i, int j, int k, bool win, bool pin) {
   if constexpr (AIN) {
     // first pass of a velocity group: its form's velocity-only terms are precomputed
     if (win && (P.stdf ? (P.gv & 2) : (P.gv & 1))) {
@@ -140,14 +149,23 @@ __device__ __forceinline__ void pseudo_dispatch(const Prob<R>& P, int i, int j, 
     }
   }
   if (!win) {
+    if constexpr (sizeof(R) == 8) {
+      if (pin) {  // a periodic seam: the stored pairs through the wrap maps
+        if (warp_unit_faces(P, i, j, k))
+          pseudo_body<R, AIN, false, true, true, false, false, true>(P, i, j, k);
+        else
+          pseudo_body<R, AIN, false, false, true, false, false, true>(P, i, j, k);
+        return;
+      }
+    }
     pseudo_body<R, AIN, false, false, false, false, false>(P, i, j, k);
   } else if constexpr (sizeof(R) == 8) {
     const bool unit = warp_unit_faces(P, i, j, k);
-    if (P.pairs) {
+    if (P.pairs) {  // outside the group branch above, the velocity pairs are stored too
       if (unit)
-        pseudo_body<R, AIN, true, true, true, false, false>(P, i, j, k);
+        pseudo_body<R, AIN, true, true, true, false, false, true>(P, i, j, k);
       else
-        pseudo_body<R, AIN, true, false, true, false, false>(P, i, j, k);
+        pseudo_body<R, AIN, true, false, true, false, false, true>(P, i, j, k);
     } else {
       if (unit)
         pseudo_body<R, AIN, true, true, false, false, false>(P, i, j, k);
@@ -169,7 +187,12 @@ __global__ void __launch_bounds__(256) kb_pseudo(BATCH_ARGS) {
   const int j = (int)((w >> 32) & 0xffffu) * (int)blockDim.y + (int)threadIdx.y + 1;
   const int k = (int)(w >> 48) + 1;
   const bool win = warp_interior(P.g, i, j, k);
-  if (i <= P.g.np && j <= P.g.mp) pseudo_dispatch<R, AIN>(P, i, j, k, win);
+  // FP64 problems with every pair sum stored: warps on a periodic seam read
+  // them through the wrap maps (P is the block's problem: uniform)
+  bool pin = false;
+  if constexpr (sizeof(R) == 8)
+    if (!win && batch_vpairs(P, AIN)) pin = warp_periodic_interior(P.g, i, j, k);
+  if (i <= P.g.np && j <= P.g.mp) pseudo_dispatch<R, AIN>(P, i, j, k, win, pin);
 }
 template <class R, bool NONOS, bool FIRST, bool KEEP>
 __global__ void KB_LB_BOUNDS kb_bounds(BATCH_ARGS) {
@@ -240,7 +263,8 @@ int run_batch(const BatchLaunch<R>& B, Prof* prof, cudaStream_t s) {
   const bool keep = B.iord > 2;
   for (int pass = 2; pass <= B.iord; pass++) {
     const bool first = (pass == 2), last = (pass == B.iord) && B.halo;
-    if (B.pairs) BLAUNCH(ST_PAIRS, (kb_pairs<R><<<G, blk, 0, s>>>(A)));
+    if (B.pairs && first) BLAUNCH(ST_PAIRS, (kb_pairs<R, true><<<G, blk, 0, s>>>(A)));
+    else if (B.pairs) BLAUNCH(ST_PAIRS, (kb_pairs<R, false><<<G, blk, 0, s>>>(A)));
     if (first) BLAUNCH(ST_PSEUDO, (kb_pseudo<R, true><<<G, blk, 0, s>>>(A)));
     else BLAUNCH(ST_PSEUDO, (kb_pseudo<R, false><<<G, blk, 0, s>>>(A)));
     if (!B.nonos) BLAUNCH(ST_BOUNDS, (kb_bounds<R, false, true, false><<<G, blk, 0, s>>>(A)));

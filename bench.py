@@ -54,11 +54,11 @@ def stage_elems(stage, gauge, iord, precision=64):
     if stage == "upwind":
         return 11.0                                   # psi,u1..3,h,rhr -> xant,1/h,hmx,hmy,hmz
     if stage == "pair_sums":
-        return 4.0                                    # xant -> Sx,Sy,Sz
+        return 10.0                                   # xant,a1..3 -> Sx,Sy,Sz, velocity pairs C1..C3
     if stage == "pseudo_velocity":
         if not gauge:
             return 13.0                               # xant,a1..3,hm1..3 -> v1..3,f1..3
-        return 13.0 if pairs else 10.0                # xant,a1..3,hm1..3 (+Sx,Sy,Sz) -> v1..3
+        return 16.0 if pairs else 10.0                # xant,a1..3,hm1..3 (+Sx,Sy,Sz,C1..C3) -> v1..3
     if stage == "limiter_bounds":
         first = 10.0 + (2.0 if keep else 0.0)         # xant,rhr,psi,F1..3,h -> q,cp,cn (+mx,mn kept)
         later = 13.0                                  # xant,rhr,mx,mn,F1..3,h -> q,mx,mn,cp,cn
@@ -80,14 +80,14 @@ def stage_elems(stage, gauge, iord, precision=64):
 # (dram__bytes_read.sum + dram__bytes_write.sum, and
 # smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on.sum, per cell).
 # Both grow in proportion to the cells of a launch.
-NCU_PSEUDO = {64: {"dram_bytes_per_cell": 100.2, "fp64_inst_per_cell": 60.6},
+NCU_PSEUDO = {64: {"dram_bytes_per_cell": 127.7, "fp64_inst_per_cell": 45.0},
               32: {"dram_bytes_per_cell": 38.2, "fp64_inst_per_cell": 0.0}}
 # GB300 issues 2 FP64 instructions per SM per clock (1.25 TFLOP/s nominal FMA).
 FP64_INST_PER_SM_CLK = 2.0
 # FP64 flops per cell of one launch of each stage (DADD and DMUL 1, DFMA 2),
 # counted by ncu (smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on.sum)
 # on the deformational flow at unit density, 384x384x64, gauge iord=3.
-FP64_FLOPS_PER_CELL = {"upwind": 12.4, "pair_sums": 3.0, "pseudo_velocity": 60.6, "limiter_bounds": 11.7,
+FP64_FLOPS_PER_CELL = {"upwind": 12.4, "pair_sums": 6.0, "pseudo_velocity": 45.0, "limiter_bounds": 11.7,
                        "limited_flux": 3.0, "corrective_update": 6.2, "predictor_level": 12.0,
                        "predictor_cgrid": 6.0}
 HBM_NOMINAL_GBS = 7900.0  # GB300 HBM3e, nominal
