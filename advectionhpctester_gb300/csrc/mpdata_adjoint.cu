@@ -521,18 +521,15 @@ __global__ void KA_LB_PSEUDO ka_pseudo(const Prob<R> P, const AdjArr<R> A) {
   const bool win = warp_interior(P.g, i, j, k);
   // every pair sum stored (pairs 2): warps on a periodic seam read them too
   bool pin = false;
-  if constexpr (sizeof(R) == 8)
-    if (!win && P.pairs == 2) pin = warp_periodic_interior(P.g, i, j, k);
+  if (!win && P.pairs == 2) pin = warp_periodic_interior(P.g, i, j, k);
   if (i > P.g.np || j > P.g.mp) return;
   if (!win) {
-    if constexpr (sizeof(R) == 8) {
-      if (pin) {
-        if (warp_unit_faces(P, i, j, k))
-          ka_pseudo_cell<R, AIN, false, true, true, true>(P, A, i, j, k);
-        else
-          ka_pseudo_cell<R, AIN, false, false, true, true>(P, A, i, j, k);
-        return;
-      }
+    if (pin) {
+      if (warp_unit_faces(P, i, j, k))
+        ka_pseudo_cell<R, AIN, false, true, true, true>(P, A, i, j, k);
+      else
+        ka_pseudo_cell<R, AIN, false, false, true, true>(P, A, i, j, k);
+      return;
     }
     ka_pseudo_cell<R, AIN, false>(P, A, i, j, k);
   } else if constexpr (sizeof(R) == 8) {
@@ -553,6 +550,8 @@ __global__ void KA_LB_PSEUDO ka_pseudo(const Prob<R> P, const AdjArr<R> A) {
       else
         ka_pseudo_cell<R, AIN, true>(P, A, i, j, k);
     }
+  } else if (P.pairs == 2) {  // FP32: the stored pairs save issue slots
+    ka_pseudo_cell<R, AIN, true, false, true, true>(P, A, i, j, k);
   } else {
     ka_pseudo_cell<R, AIN, true>(P, A, i, j, k);
   }
@@ -1137,7 +1136,7 @@ int run_step_reverse(const Prob<R>& P, const AdjPlan<R>& A, int nonos, cudaStrea
       // they take the pair sums of its input field, and the workspace's
       // f1..f3 the velocity pairs (FP64)
       Prob<R> Qp = Q;
-      Qp.pairs = sizeof(R) == 8 ? 2 : 0;
+      Qp.pairs = 2;
       if (Qp.pairs) {
         Qp.f1 = P.f1;
         Qp.f2 = P.f2;
