@@ -25,7 +25,9 @@ struct Prob {
   int stdf;     // 1 = standard form (t_adv=2), 0 = infinite gauge (t_adv=1)
   int own_vel;  // 1 = this problem writes the velocity-derived scratch (hinv, hm*)
   int rho;      // density step of mpdata3d_rho_gauge_gpubc: no rhr, upwind fluxes kept
-  int pairs;    // gauge pseudo-velocity: pair sums of xant in cp, cn, q (k_pairs)
+  int pairs;    // gauge pseudo-velocity: 1 = pair sums of xant in cp, cn, q
+                // (k_pairs); 2 = also the pass velocities' cell-centred pairs
+                // in f1..f3, which lets periodic-seam warps take the pair path
   int gv;       // batch velocity group: the velocity-only terms of the first
                 // pass's pseudo-velocities, stored by the group owner's upwind:
                 // bit 0 the gauge form's (gvf), bit 1 the standard form's (gvs)
