@@ -378,7 +378,8 @@ struct FaceAdj {
 // U: the warp's face densities are all exactly 1.  PS: the pair sums of the
 // pass's input field are in cp/cn/q (kf_pairs), as in the forward stage.
 // PV (with PS): the velocities' cell-centred pairs are in f1..f3.  Without IN
-// (a warp on a periodic seam) the stored pairs are read through the wrap maps.
+// (a full warp at a boundary) the stored pairs are read through the boundary
+// maps of the values they sum, as in pseudo_form.
 template <class R, bool AIN, bool IN, bool U = false, bool PS = false, bool PV = false>
 __device__ __forceinline__ void ka_pseudo_cell(const Prob<R>& P, const AdjArr<R>& A, int i, int j, int k) {
   const Geo& g = P.g;
@@ -395,6 +396,8 @@ __device__ __forceinline__ void ka_pseudo_cell(const Prob<R>& P, const AdjArr<R>
 #define MX(a) cx<IN>(g, (a))
 #define MY(a) cy<IN>(g, (a))
 #define MZ(a) cz<IN>(g, (a))
+#define QX(a) xmx<IN>(g, (a))
+#define QY(a) xmy<IN>(g, (a))
 #define S2X_ (PV ? P.f2.ld(MX(i - 1), j, k) + P.f2.ld(i, j, k) : VSUM_2X)
 #define S3X_ (PV ? P.f3.ld(MX(i - 1), j, k) + P.f3.ld(i, j, k) : VSUM_3X)
 #define S1Y_ (PV ? P.f1.ld(i, MY(j - 1), k) + P.f1.ld(i, j, k) : VSUM_1Y)
@@ -407,7 +410,7 @@ __device__ __forceinline__ void ka_pseudo_cell(const Prob<R>& P, const AdjArr<R>
     const R hm = U ? R(1) : P.hmx.ld(i, j, k), a = fx<R, AIN, IN>(g, U1, i, j, k);
     const R xl = XX(i - 1, j, k), xrr = XX(i, j, k);
     const R S2 = S2X_;
-    const R D2 = PS ? P.cp.ld(i, MY(j + 1), k) - P.cp.ld(i, MY(j - 1), k)
+    const R D2 = PS ? P.cp.ld(i, QY(j + 1), k) - P.cp.ld(i, QY(j - 1), k)
                     : dif4(XX(i - 1, j - 1, k), XX(i, j - 1, k), XX(i - 1, j + 1, k), XX(i, j + 1, k));
     R cr4 = S2 * D2, S3 = R(0), D3 = R(0);
     if (zt) {
@@ -441,7 +444,7 @@ __device__ __forceinline__ void ka_pseudo_cell(const Prob<R>& P, const AdjArr<R>
     const R hm = U ? R(1) : P.hmy.ld(i, j, k), a = fy<R, AIN, IN>(g, U2, i, j, k);
     const R xl = XX(i, j - 1, k), xrr = XX(i, j, k);
     const R S1 = S1Y_;
-    const R D1 = PS ? P.cn.ld(MX(i + 1), j, k) - P.cn.ld(MX(i - 1), j, k)
+    const R D1 = PS ? P.cn.ld(QX(i + 1), j, k) - P.cn.ld(QX(i - 1), j, k)
                     : dif4(XX(i - 1, j - 1, k), XX(i - 1, j, k), XX(i + 1, j - 1, k), XX(i + 1, j, k));
     R cr4 = S1 * D1, S3 = R(0), D3 = R(0);
     if (zt) {
@@ -475,10 +478,10 @@ __device__ __forceinline__ void ka_pseudo_cell(const Prob<R>& P, const AdjArr<R>
     const R hm = U ? R(1) : P.hmz.ld(i, j, k), a = fz<R, AIN, IN>(g, U3, i, j, k);
     const R xl = XX(i, j, k - 1), xrr = XX(i, j, k);
     const R S1 = S1Z_;
-    const R D1 = PS ? P.q.ld(MX(i + 1), j, k) - P.q.ld(MX(i - 1), j, k)
+    const R D1 = PS ? P.q.ld(QX(i + 1), j, k) - P.q.ld(QX(i - 1), j, k)
                     : dif4(XX(i - 1, j, k - 1), XX(i - 1, j, k), XX(i + 1, j, k - 1), XX(i + 1, j, k));
     const R S2 = S2Z_;
-    const R D2 = PS ? P.q.ld(i, MY(j + 1), k) - P.q.ld(i, MY(j - 1), k)
+    const R D2 = PS ? P.q.ld(i, QY(j + 1), k) - P.q.ld(i, QY(j - 1), k)
                     : dif4(XX(i, j - 1, k - 1), XX(i, j - 1, k), XX(i, j + 1, k - 1), XX(i, j + 1, k));
     const R cr4 = S1 * D1 + S2 * D2;
     const FaceAdj<R, U> f(lv, a, hm, xl, xrr, cr4);
@@ -506,6 +509,8 @@ __device__ __forceinline__ void ka_pseudo_cell(const Prob<R>& P, const AdjArr<R>
 #undef MX
 #undef MY
 #undef MZ
+#undef QX
+#undef QY
 #undef S2X_
 #undef S3X_
 #undef S1Y_
@@ -519,9 +524,9 @@ __global__ void KA_LB_PSEUDO ka_pseudo(const Prob<R> P, const AdjArr<R> A) {
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int k = blockIdx.z + 1;
   const bool win = warp_interior(P.g, i, j, k);
-  // every pair sum stored (pairs 2): warps on a periodic seam read them too
+  // every pair sum stored (pairs 2): full warps at a boundary read them too
   bool pin = false;
-  if (!win && P.pairs == 2) pin = warp_periodic_interior(P.g, i, j, k);
+  if (!win && P.pairs == 2) pin = warp_on_grid(P.g, i, j);
   if (i > P.g.np || j > P.g.mp) return;
   if (!win) {
     if (pin) {
@@ -898,7 +903,7 @@ __global__ void __launch_bounds__(128, KfPseudoMinBlocks<R>::v) kf_pseudo(const 
   const bool win = warp_interior(P.g, i, j, k);
   bool pin = false;
   if constexpr (sizeof(R) == 8)
-    if (!win && P.pairs == 2) pin = warp_periodic_interior(P.g, i, j, k);
+    if (!win && P.pairs == 2) pin = warp_on_grid(P.g, i, j);
   if (i > P.g.np || j > P.g.mp) return;
   if (!win) {
     if constexpr (sizeof(R) == 8) {

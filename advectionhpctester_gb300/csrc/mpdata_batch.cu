@@ -150,7 +150,7 @@ __device__ __forceinline__ void pseudo_dispatch(const Prob<R>& P, int i, int j, 
   }
   if (!win) {
     if constexpr (sizeof(R) == 8) {
-      if (pin) {  // a periodic seam: the stored pairs through the wrap maps
+      if (pin) {  // a full warp at a boundary: the stored pairs through the boundary maps
         if (warp_unit_faces(P, i, j, k))
           pseudo_body<R, AIN, false, true, true, false, false, true>(P, i, j, k);
         else
@@ -187,11 +187,11 @@ __global__ void __launch_bounds__(256) kb_pseudo(BATCH_ARGS) {
   const int j = (int)((w >> 32) & 0xffffu) * (int)blockDim.y + (int)threadIdx.y + 1;
   const int k = (int)(w >> 48) + 1;
   const bool win = warp_interior(P.g, i, j, k);
-  // FP64 problems with every pair sum stored: warps on a periodic seam read
-  // them through the wrap maps (P is the block's problem: uniform)
+  // FP64 problems with every pair sum stored: full warps at a boundary read
+  // them through the boundary maps (P is the block's problem: uniform)
   bool pin = false;
   if constexpr (sizeof(R) == 8)
-    if (!win && batch_vpairs(P, AIN)) pin = warp_periodic_interior(P.g, i, j, k);
+    if (!win && batch_vpairs(P, AIN)) pin = warp_on_grid(P.g, i, j);
   if (i <= P.g.np && j <= P.g.mp) pseudo_dispatch<R, AIN>(P, i, j, k, win, pin);
 }
 template <class R, bool NONOS, bool FIRST, bool KEEP>

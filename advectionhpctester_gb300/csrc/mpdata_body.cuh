@@ -27,7 +27,7 @@ struct Prob {
   int rho;      // density step of mpdata3d_rho_gauge_gpubc: no rhr, upwind fluxes kept
   int pairs;    // gauge pseudo-velocity: 1 = pair sums of xant in cp, cn, q
                 // (k_pairs); 2 = also the pass velocities' cell-centred pairs
-                // in f1..f3, which lets periodic-seam warps take the pair path
+                // in f1..f3, which lets full warps at a boundary take the pair path
   int gv;       // batch velocity group: the velocity-only terms of the first
                 // pass's pseudo-velocities, stored by the group owner's upwind:
                 // bit 0 the gauge form's (gvf), bit 1 the standard form's (gvs)
@@ -59,11 +59,17 @@ __device__ __forceinline__ int cy(const Geo& g, int j) { return IN ? j : (g.by ?
 template <bool IN = false>
 __device__ __forceinline__ int cz(const Geo& g, int k) { return IN ? k : (g.bz ? wrapi(k, g.lp) : clampi(k, g.lp)); }
 
+// the xant halo rule's x and y maps: a wrap, or the reflection of a wall
+template <bool IN = false>
+__device__ __forceinline__ int xmx(const Geo& g, int i) { return IN ? i : (g.bx ? wrapi(i, g.np) : refl(i, g.np)); }
+template <bool IN = false>
+__device__ __forceinline__ int xmy(const Geo& g, int j) { return IN ? j : (g.by ? wrapi(j, g.mp) : refl(j, g.mp)); }
+
 // the current (antidiffused) field with the xant halo rule
 template <class R, bool IN = false>
 __device__ __forceinline__ R xr(const Geo& g, const Arr<R>& X, int i, int j, int k) {
   if (IN) return X.ld(i, j, k);
-  return X.ld(g.bx ? wrapi(i, g.np) : refl(i, g.np), g.by ? wrapi(j, g.mp) : refl(j, g.mp), cz(g, k));
+  return X.ld(xmx(g, i), xmy(g, j), cz(g, k));
 }
 
 // Face fields.  AIN = the caller's C-grid Courant numbers (faces 1..n+1 are
@@ -107,15 +113,13 @@ __device__ __forceinline__ bool warp_interior(const Geo& g, int i, int j, int k)
   return __all_sync(0xffffffffu, in);
 }
 
-// Warp-uniform: every lane holds a cell that is on the grid and, on each
-// axis, either periodic or in [2, n-1].  Such warps read through the boundary
-// maps, which are then plain wraps, and may take the precomputed pair sums
-// (pairs_body fills the wrapped ones).  Every lane of a full warp calls it,
-// before any lane returns.
-__device__ __forceinline__ bool warp_periodic_interior(const Geo& g, int i, int j, int k) {
-  const bool ok = i <= g.np && j <= g.mp && (g.bx || (i >= 2 && i < g.np)) && (g.by || (j >= 2 && j < g.mp)) &&
-                  (g.bz || (k >= 2 && k < g.lp));
-  return __all_sync(0xffffffffu, ok);
+// Warp-uniform: every lane holds a cell of the grid.  Such a warp may take
+// the precomputed pair sums outside the interior too: it reads them through
+// the same boundary maps as the values they sum (pairs_body fills the wrapped
+// pairs of periodic axes; a wall needs no pair beyond [1, n]).  Every lane of
+// a full warp calls it, before any lane returns.
+__device__ __forceinline__ bool warp_on_grid(const Geo& g, int i, int j) {
+  return __all_sync(0xffffffffu, i <= g.np && j <= g.mp);
 }
 
 // The standard form's pseudo-velocity pieces with their velocity-only
@@ -337,9 +341,11 @@ __device__ __forceinline__ void upwind_body(const Prob<R>& P, int i, int j, int 
 // (gauge, interior warps): the pair sums of xant the rat4 terms start with
 // are read from cp, cn and q, where k_pairs stored them.  GV (gauge, first
 // pass, interior warps of a batch velocity group): the velocity-only terms
-// are read from gvf (velgroup_body).  PV (gauge, interior warps, with PS):
-// the velocities' cell-centred pairs of the 4-face sums are read from f1..f3,
-// where k_pairs stored them.
+// are read from gvf (velgroup_body).  PV (gauge, with PS): the velocities'
+// cell-centred pairs of the 4-face sums are read from f1..f3, where k_pairs
+// stored them.  Without IN (a full warp at a boundary), PS reads the xant
+// pairs through the xant halo maps and PV the velocity pairs through the
+// face maps, so each stored pair is the sum the generic body forms there.
 template <class R, bool STD, bool AIN, bool IN = false, bool U = false, bool PS = false, bool GV = false,
           bool DEFER = true, bool PV = false>
 __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int k) {
@@ -357,6 +363,8 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
 #define MX(a) cx<IN>(g, (a))
 #define MY(a) cy<IN>(g, (a))
 #define MZ(a) cz<IN>(g, (a))
+#define QX(a) xmx<IN>(g, (a))
+#define QY(a) xmy<IN>(g, (a))
 #define S2X (PV ? P.f2.ld(MX(i - 1), j, k) + P.f2.ld(i, j, k) : VSUM_2X)
 #define S3X (PV ? P.f3.ld(MX(i - 1), j, k) + P.f3.ld(i, j, k) : VSUM_3X)
 #define S1Y (PV ? P.f1.ld(i, MY(j - 1), k) + P.f1.ld(i, j, k) : VSUM_1Y)
@@ -405,7 +413,7 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
       }
       put(0, v, donor(XX(i - 1, j, k), XX(i, j, k), v));
     } else {
-      const R d2 = PS ? P.cp.ld(i, MY(j + 1), k) - P.cp.ld(i, MY(j - 1), k)
+      const R d2 = PS ? P.cp.ld(i, QY(j + 1), k) - P.cp.ld(i, QY(j - 1), k)
                       : dif4(XX(i - 1, j - 1, k), XX(i, j - 1, k), XX(i - 1, j + 1, k), XX(i, j + 1, k));
       const R c2 = (GV ? P.gvf[0].ld(i, j, k) : S2X) * d2;
       R cr = c2;
@@ -447,7 +455,7 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
       }
       put(1, v, donor(XX(i, j - 1, k), XX(i, j, k), v));
     } else {
-      const R d1 = PS ? P.cn.ld(MX(i + 1), j, k) - P.cn.ld(MX(i - 1), j, k)
+      const R d1 = PS ? P.cn.ld(QX(i + 1), j, k) - P.cn.ld(QX(i - 1), j, k)
                       : dif4(XX(i - 1, j - 1, k), XX(i - 1, j, k), XX(i + 1, j - 1, k), XX(i + 1, j, k));
       const R c1 = (GV ? P.gvf[4].ld(i, j, k) : S1Y) * d1;
       R cr = c1;
@@ -485,9 +493,9 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
             vcorra_u<U>(a, S2Z, y1, y2, hmz);
       put(2, v, donor(XX(i, j, k - 1), XX(i, j, k), v));
     } else {
-      const R d1 = PS ? P.q.ld(MX(i + 1), j, k) - P.q.ld(MX(i - 1), j, k)
+      const R d1 = PS ? P.q.ld(QX(i + 1), j, k) - P.q.ld(QX(i - 1), j, k)
                       : dif4(XX(i - 1, j, k - 1), XX(i - 1, j, k), XX(i + 1, j, k - 1), XX(i + 1, j, k));
-      const R d2 = PS ? P.q.ld(i, MY(j + 1), k) - P.q.ld(i, MY(j - 1), k)
+      const R d2 = PS ? P.q.ld(i, QY(j + 1), k) - P.q.ld(i, QY(j - 1), k)
                       : dif4(XX(i, j - 1, k - 1), XX(i, j - 1, k), XX(i, j + 1, k - 1), XX(i, j + 1, k));
       const R cr = (GV ? P.gvf[8].ld(i, j, k) : S1Z) * d1 +
                    (GV ? P.gvf[9].ld(i, j, k) : S2Z) * d2;
@@ -515,6 +523,8 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
 #undef MX
 #undef MY
 #undef MZ
+#undef QX
+#undef QY
 #undef S2X
 #undef S3X
 #undef S1Y

@@ -127,11 +127,11 @@ __global__ void __launch_bounds__(128, PseudoMinBlocks<R>::v) k_pseudo(const Pro
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int k = blockIdx.z + 1;
   const bool win = warp_interior(P.g, i, j, k);
-  // FP64 with every pair sum stored: warps on a periodic seam read them too,
-  // through the wrap maps
+  // FP64 with every pair sum stored: full warps at a boundary read them too,
+  // through the boundary maps
   bool pin = false;
   if constexpr (sizeof(R) == 8)
-    if (!win && P.pairs == 2) pin = warp_periodic_interior(P.g, i, j, k);
+    if (!win && P.pairs == 2) pin = warp_on_grid(P.g, i, j);
   if (i > P.g.np || j > P.g.mp) return;
   if (!win) {
     if constexpr (sizeof(R) == 8) {
