@@ -1,9 +1,9 @@
-"""Warps on a periodic seam.  A 96-wide grid puts whole warps at i = 1 and
-i = np, and mixed boundary flags put a seam on one axis while the walls of the
-others keep their warps in [2, n-1].  In the FP64 gauge form such warps read
-the stored pair sums of xant and of the pass velocities through the wrap maps.
-The step and the batch must match the oracle bit for bit, the adjoint to
-rounding (its atomic sums have no fixed order)."""
+"""Full warps at a boundary.  A 96-wide grid puts whole warps at i = 1 and
+i = np, and the boundary flags mix periodic seams and walls on every axis.  In
+the FP64 gauge form such warps read the stored pair sums of xant (through the
+xant halo maps: wrap or reflection) and of the pass velocities (through the
+face maps).  The step and the batch must match the oracle bit for bit, the
+adjoint to rounding (its atomic sums have no fixed order)."""
 import numpy as np
 import pytest
 
