@@ -287,6 +287,21 @@ void upwind(const Dims& d, Buf<R>& xin, Buf<R>& u1, Buf<R>& u2, Buf<R>& u3, Buf<
 // the cell's pair of faces along the velocity's own axis.  Every sum of the
 // pass then shares those pairs.
 
+// Literal mode (orc_set_literal_sums): the six sums are evaluated left to
+// right in the order the reference writes their terms, ((t1+t2)+t3)+t4,
+// which is the order an unoptimised Fortran build takes.  It exists to
+// measure how far the fixed pair order moves a field; the default (0) is the
+// pair order that the CUDA kernels reproduce bit for bit.
+int g_literal_sums = 0;
+// t1..t4 in the reference's written order.  s12: the pair form is
+// (t1+t2)+(t3+t4); s14: the pair form is (t1+t4)+(t2+t3).
+template <class R> inline R s12(R t1, R t2, R t3, R t4) {
+  return g_literal_sums ? ((t1 + t2) + t3) + t4 : (t1 + t2) + (t3 + t4);
+}
+template <class R> inline R s14(R t1, R t2, R t3, R t4) {
+  return g_literal_sums ? ((t1 + t2) + t3) + t4 : (t1 + t4) + (t2 + t3);
+}
+
 // Whether plane k carries the z cross terms in the x/y pseudo-velocities:
 // the reference's k=1 and k=lp kernels drop them (antidiff3d-*-gpubc.f90).
 inline bool zterm(const Dims& d, int k) { return d.bz || (k > 1 && k < d.lp); }
@@ -304,14 +319,14 @@ void pseudo_std(const Dims& d, Buf<R>& x, Buf<R>& a1, Buf<R>& a2, Buf<R>& a3, Bu
         if (i >= i0) {
           const R hmx = R(1) / (R(0.5) * (h(i - 1, j, k) + h(i, j, k)));
           R v = vdyfa(x(i - 1, j, k), x(i, j, k), a1(i, j, k), hmx, ep) +
-                vcorra(a1(i, j, k), (a2(i - 1, j, k) + a2(i - 1, j + 1, k)) + (a2(i, j, k) + a2(i, j + 1, k)),
+                vcorra(a1(i, j, k), s12(a2(i - 1, j, k), a2(i - 1, j + 1, k), a2(i, j + 1, k), a2(i, j, k)),
                        (absv(x(i - 1, j + 1, k)) + absv(x(i, j + 1, k))) -
                            (absv(x(i - 1, j - 1, k)) + absv(x(i, j - 1, k))),
                        absv(x(i - 1, j + 1, k)) + absv(x(i, j + 1, k)) +
                            absv(x(i - 1, j - 1, k)) + absv(x(i, j - 1, k)) + ep,
                        hmx);
           if (zt)
-            v = v + vcorra(a1(i, j, k), (a3(i - 1, j, k) + a3(i - 1, j, k + 1)) + (a3(i, j, k) + a3(i, j, k + 1)),
+            v = v + vcorra(a1(i, j, k), s12(a3(i - 1, j, k), a3(i - 1, j, k + 1), a3(i, j, k + 1), a3(i, j, k)),
                            (absv(x(i - 1, j, k + 1)) + absv(x(i, j, k + 1))) -
                                (absv(x(i - 1, j, k - 1)) + absv(x(i, j, k - 1))),
                            absv(x(i - 1, j, k + 1)) + absv(x(i, j, k + 1)) +
@@ -323,14 +338,14 @@ void pseudo_std(const Dims& d, Buf<R>& x, Buf<R>& a1, Buf<R>& a2, Buf<R>& a3, Bu
         if (j >= j0) {
           const R hmy = R(1) / (R(0.5) * (h(i, j - 1, k) + h(i, j, k)));
           R v = vdyfa(x(i, j - 1, k), x(i, j, k), a2(i, j, k), hmy, ep) +
-                vcorra(a2(i, j, k), (a1(i, j - 1, k) + a1(i + 1, j - 1, k)) + (a1(i, j, k) + a1(i + 1, j, k)),
+                vcorra(a2(i, j, k), s14(a1(i, j - 1, k), a1(i, j, k), a1(i + 1, j, k), a1(i + 1, j - 1, k)),
                        (absv(x(i + 1, j - 1, k)) + absv(x(i + 1, j, k))) -
                            (absv(x(i - 1, j - 1, k)) + absv(x(i - 1, j, k))),
                        absv(x(i + 1, j - 1, k)) + absv(x(i + 1, j, k)) +
                            absv(x(i - 1, j - 1, k)) + absv(x(i - 1, j, k)) + ep,
                        hmy);
           if (zt)
-            v = v + vcorra(a2(i, j, k), (a3(i, j - 1, k) + a3(i, j - 1, k + 1)) + (a3(i, j, k) + a3(i, j, k + 1)),
+            v = v + vcorra(a2(i, j, k), s14(a3(i, j - 1, k), a3(i, j, k), a3(i, j, k + 1), a3(i, j - 1, k + 1)),
                            (absv(x(i, j - 1, k + 1)) + absv(x(i, j, k + 1))) -
                                (absv(x(i, j - 1, k - 1)) + absv(x(i, j, k - 1))),
                            absv(x(i, j - 1, k + 1)) + absv(x(i, j, k + 1)) +
@@ -342,13 +357,13 @@ void pseudo_std(const Dims& d, Buf<R>& x, Buf<R>& a1, Buf<R>& a2, Buf<R>& a3, Bu
         if (k >= k0) {
           const R hmz = R(1) / (R(0.5) * (h(i, j, k - 1) + h(i, j, k)));
           const R v = vdyfa(x(i, j, k - 1), x(i, j, k), a3(i, j, k), hmz, ep) +
-                      vcorra(a3(i, j, k), (a1(i, j, k - 1) + a1(i + 1, j, k - 1)) + (a1(i, j, k) + a1(i + 1, j, k)),
+                      vcorra(a3(i, j, k), s14(a1(i, j, k - 1), a1(i, j, k), a1(i + 1, j, k), a1(i + 1, j, k - 1)),
                              (absv(x(i + 1, j, k - 1)) + absv(x(i + 1, j, k))) -
                                  (absv(x(i - 1, j, k - 1)) + absv(x(i - 1, j, k))),
                              absv(x(i + 1, j, k - 1)) + absv(x(i + 1, j, k)) +
                                  absv(x(i - 1, j, k - 1)) + absv(x(i - 1, j, k)) + ep,
                              hmz) +
-                      vcorra(a3(i, j, k), (a2(i, j, k - 1) + a2(i, j + 1, k - 1)) + (a2(i, j, k) + a2(i, j + 1, k)),
+                      vcorra(a3(i, j, k), s12(a2(i, j, k - 1), a2(i, j + 1, k - 1), a2(i, j + 1, k), a2(i, j, k)),
                              (absv(x(i, j + 1, k - 1)) + absv(x(i, j + 1, k))) -
                                  (absv(x(i, j - 1, k - 1)) + absv(x(i, j - 1, k))),
                              absv(x(i, j + 1, k - 1)) + absv(x(i, j + 1, k)) +
@@ -375,31 +390,31 @@ void pseudo_gauge(const Dims& d, Buf<R>& x, Buf<R>& a1, Buf<R>& a2, Buf<R>& a3, 
       for (int i = 1; i <= d.np; i++) {
         if (i >= i0) {
           const R hmx = R(1) / (R(0.5) * (h(i - 1, j, k) + h(i, j, k)));
-          const R c2 = ((a2(i - 1, j, k) + a2(i - 1, j + 1, k)) + (a2(i, j, k) + a2(i, j + 1, k))) *
+          const R c2 = (s12(a2(i - 1, j, k), a2(i - 1, j + 1, k), a2(i, j + 1, k), a2(i, j, k))) *
                        rat4(x(i - 1, j - 1, k), x(i, j - 1, k), x(i - 1, j + 1, k), x(i, j + 1, k));
           R cr = c2;
           if (zt)
-            cr = c2 + ((a3(i - 1, j, k) + a3(i - 1, j, k + 1)) + (a3(i, j, k) + a3(i, j, k + 1))) *
+            cr = c2 + (s12(a3(i - 1, j, k), a3(i - 1, j, k + 1), a3(i, j, k + 1), a3(i, j, k))) *
                           rat4(x(i - 1, j, k - 1), x(i, j, k - 1), x(i - 1, j, k + 1), x(i, j, k + 1));
           v1(i, j, k) = vdyf(x(i - 1, j, k), x(i, j, k), a1(i, j, k), hmx) -
                         R(0.125) * a1(i, j, k) * hmx * cr;
         }
         if (j >= j0) {
           const R hmy = R(1) / (R(0.5) * (h(i, j - 1, k) + h(i, j, k)));
-          const R c1 = ((a1(i, j - 1, k) + a1(i + 1, j - 1, k)) + (a1(i, j, k) + a1(i + 1, j, k))) *
+          const R c1 = (s14(a1(i, j - 1, k), a1(i, j, k), a1(i + 1, j, k), a1(i + 1, j - 1, k))) *
                        rat4(x(i - 1, j - 1, k), x(i - 1, j, k), x(i + 1, j - 1, k), x(i + 1, j, k));
           R cr = c1;
           if (zt)
-            cr = c1 + ((a3(i, j - 1, k) + a3(i, j - 1, k + 1)) + (a3(i, j, k) + a3(i, j, k + 1))) *
+            cr = c1 + (s14(a3(i, j - 1, k), a3(i, j, k), a3(i, j, k + 1), a3(i, j - 1, k + 1))) *
                           rat4(x(i, j - 1, k - 1), x(i, j, k - 1), x(i, j - 1, k + 1), x(i, j, k + 1));
           v2(i, j, k) = vdyf(x(i, j - 1, k), x(i, j, k), a2(i, j, k), hmy) -
                         R(0.125) * a2(i, j, k) * hmy * cr;
         }
         if (k >= k0) {
           const R hmz = R(1) / (R(0.5) * (h(i, j, k - 1) + h(i, j, k)));
-          const R cr = ((a1(i, j, k - 1) + a1(i + 1, j, k - 1)) + (a1(i, j, k) + a1(i + 1, j, k))) *
+          const R cr = (s14(a1(i, j, k - 1), a1(i, j, k), a1(i + 1, j, k), a1(i + 1, j, k - 1))) *
                            rat4(x(i - 1, j, k - 1), x(i - 1, j, k), x(i + 1, j, k - 1), x(i + 1, j, k)) +
-                       ((a2(i, j, k - 1) + a2(i, j + 1, k - 1)) + (a2(i, j, k) + a2(i, j + 1, k))) *
+                       (s12(a2(i, j, k - 1), a2(i, j + 1, k - 1), a2(i, j + 1, k), a2(i, j, k))) *
                            rat4(x(i, j - 1, k - 1), x(i, j - 1, k), x(i, j + 1, k - 1), x(i, j + 1, k));
           v3(i, j, k) = vdyf(x(i, j, k - 1), x(i, j, k), a3(i, j, k), hmz) -
                         R(0.125) * a3(i, j, k) * hmz * cr;
@@ -1084,6 +1099,7 @@ int rho_gauge(const orc_grid* g, R* ox, R* oy, R* oz, R* pu, R* pv, R* pw, R* u1
 extern "C" {
 
 void orc_set_threads(int n) { g_threads = n < 1 ? 1 : n; }
+void orc_set_literal_sums(int on) { g_literal_sums = on ? 1 : 0; }
 int orc_get_threads(void) { return g_threads; }
 
 int orc_advec_dwarf_f64(const orc_grid* g, int opt, int t_adv, int iord, int nonos, double* x,

@@ -144,6 +144,13 @@ int orc_tangent_adjoint_f64(const orc_grid* g, int t_adv, int iord, int nonos, i
                             const double* dx0, const double* du1, const double* du2, const double* du3,
                             double* dJ_tl);
 
+/* Order of the cross terms' 4-face velocity sums in the pseudo-velocities.
+ * 0 (default): the pair order (a(c)+a(c+e)) + (a(c')+a(c'+e)) that the CUDA
+ * kernels reproduce bit for bit.  1: left to right in the order the reference
+ * writes the terms (antidiff3d-gauge-gpubc.f90:163-203,
+ * antidiff3d-standard-gpubc.f90:99-157), to measure the gap between the two. */
+void orc_set_literal_sums(int on);
+
 /* Threads used by the OpenMP loops (1 = the serial reference build). */
 void orc_set_threads(int n);
 int orc_get_threads(void);

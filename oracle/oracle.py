@@ -64,6 +64,7 @@ def lib():
             f.argtypes = ([ctypes.POINTER(OrcGrid), ctypes.POINTER(I), ctypes.POINTER(I), I, ctypes.POINTER(R),
                            ctypes.POINTER(R), I, I, I, R, R] + [P] * 10 + [R] * 4 + [P])
             f.restype = I
+        _lib.orc_set_literal_sums.argtypes = [I]
         _lib.orc_set_threads.argtypes = [I]
         _lib.orc_get_threads.restype = I
     return _lib
@@ -71,6 +72,12 @@ def lib():
 
 def set_threads(n):
     lib().orc_set_threads(int(n))
+
+
+def set_literal_sums(on):
+    """1: evaluate the 4-face velocity sums left to right in the reference's
+    written order; 0: the pair order the CUDA kernels reproduce."""
+    lib().orc_set_literal_sums(1 if on else 0)
 
 
 def _ptr(a, dtype):
