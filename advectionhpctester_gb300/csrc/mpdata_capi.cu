@@ -13,6 +13,7 @@
 
 #include "../../include/mpdata.h"
 #include "mpdata_common.cuh"
+#include "mpdata_fused.cuh"
 #include "mpdata_stages.cuh"
 
 using namespace mpdata;
@@ -94,6 +95,13 @@ struct Workspace {
   cudaStream_t last;
   EventProf* prof;
   void* adj;  // adjoint scratch (10 fields), allocated on first use
+  // fused single-precision path (periodic gauge grids): its arena shares
+  // `mem` with the stage path's scratch, which it never needs at the same time
+  bool fused;
+  int fz_px, fz_kchunk;
+  int fz_mx, fz_mn;    // arena fields holding the last fused step's extrema (-1: none)
+  bool fz_extrema;     // the last step ran fused: the extrema live in the arena
+  alignas(64) CUtensorMap fz_map;
 };
 
 int check_grid(const mpdata_grid* g) {
@@ -171,6 +179,27 @@ int step_impl(void* ws, R* psi, const R* u1, const R* u2, const R* u3, const R* 
   R* base = static_cast<R*>(w->mem);
   Prob<R> P = make_prob<R>(w->g, w->o.gauge, psi, u1, u2, u3, h, rhr, bcx, bcy, base, w->ncell,
                            base + (size_t)NFIELD * w->ncell, 1);
+  if constexpr (sizeof(R) == 4) {
+    if (w->fused) {
+      FusedPlan F;
+      F.g = P.g;
+      F.psi = P.psi;
+      F.u1 = P.u1;
+      F.u2 = P.u2;
+      F.u3 = P.u3;
+      F.h = P.h;
+      F.rhr = P.rhr;
+      F.arena = base;
+      F.px = w->fz_px;
+      F.fs = (long)w->fz_px * w->g.mp * w->g.lp;
+      F.kchunk = w->fz_kchunk;
+      F.err = w->d_err;
+      F.tmap = &w->fz_map;
+      w->fz_extrema = true;
+      return run_step_fused(F, w->o.iord, w->prof, s, &w->fz_mx, &w->fz_mn) == 0 ? MPDATA_OK : MPDATA_E_CUDA;
+    }
+  }
+  w->fz_extrema = false;
   return run_step<R>(P, w->o.iord, w->o.nonos, w->prof, s) == 0 ? MPDATA_OK : MPDATA_E_CUDA;
 }
 
@@ -239,6 +268,7 @@ int rho_impl(void* ws, R* ox, R* oy, R* oz, R* u, R* v, R* wv, R* u1, R* u2, R* 
   P.f1hi = hi;
   P.f2hi = hi + (size_t)g.mp * g.lp;
   P.f3hi = hi + (size_t)g.mp * g.lp + (size_t)g.np * g.lp;
+  w->fz_extrema = false;
   return run_step<R>(P, liner ? 1 : w->o.iord, w->o.nonos, w->prof, s) == 0 ? MPDATA_OK : MPDATA_E_CUDA;
 }
 
@@ -307,6 +337,12 @@ int count_violations(Workspace* w, const void* psi, double tol, unsigned long lo
   R* x = const_cast<R*>(static_cast<const R*>(psi));
   const Prob<R> P = make_prob<R>(w->g, w->o.gauge, x, x, x, x, x, x, nullptr, nullptr, base, w->ncell,
                                  base + (size_t)NFIELD * w->ncell, 1);
+  if (w->fz_extrema && w->fz_mx >= 0) {  // the last step ran fused: its extrema are arena fields
+    const long fs = (long)w->fz_px * w->g.mp * w->g.lp;
+    const Arr<R> mx{base + (size_t)w->fz_mx * fs, w->fz_px, w->fz_px * w->g.mp};
+    const Arr<R> mn{base + (size_t)w->fz_mn * fs, w->fz_px, w->fz_px * w->g.mp};
+    return run_bound_violations<R>(P.g, P.psi, mx, mn, tol, d, s) ? MPDATA_E_CUDA : MPDATA_OK;
+  }
   return run_bound_violations<R>(P.g, P.psi, P.mx, P.mn, tol, d, s) ? MPDATA_E_CUDA : MPDATA_OK;
 }
 }  // namespace
@@ -333,7 +369,16 @@ int mpdata_ws_create(const mpdata_grid* grid, const mpdata_opts* opts, void** ws
   w->prof = nullptr;
   w->adj = nullptr;
   w->nhi = (size_t)grid->mp * grid->lp + (size_t)grid->np * grid->lp + (size_t)grid->np * grid->mp;
-  if (cudaMalloc(&w->mem, (w->ncell * NSCRATCH + w->nhi) * w->elem) != cudaSuccess) {
+  w->fused = fused_eligible(geo_of(*grid), opts->precision, opts->gauge, opts->nonos, opts->iord, 0);
+  w->fz_mx = w->fz_mn = -1;
+  w->fz_extrema = false;
+  size_t elems = w->ncell * NSCRATCH + w->nhi;
+  if (w->fused) {
+    w->fz_kchunk = fused_kchunk(geo_of(*grid));
+    const size_t fz = fused_arena_elems(geo_of(*grid), &w->fz_px);
+    if (fz > elems) elems = fz;
+  }
+  if (cudaMalloc(&w->mem, elems * w->elem) != cudaSuccess) {
     cudaGetLastError();
     delete w;
     return MPDATA_E_CUDA;
@@ -341,6 +386,12 @@ int mpdata_ws_create(const mpdata_grid* grid, const mpdata_opts* opts, void** ws
   if (cudaMalloc(&w->d_err, sizeof(int)) != cudaSuccess || cudaMemset(w->d_err, 0, sizeof(int)) != cudaSuccess) {
     cudaGetLastError();
     cudaFree(w->mem);
+    delete w;
+    return MPDATA_E_CUDA;
+  }
+  if (w->fused && fused_make_tmap(&w->fz_map, static_cast<float*>(w->mem), w->fz_px, geo_of(*grid))) {
+    cudaFree(w->mem);
+    cudaFree(w->d_err);
     delete w;
     return MPDATA_E_CUDA;
   }
@@ -503,7 +554,8 @@ int mpdata_ws_stage_times(void* ws, int nstages, double* total_ms, long long* la
 const char* mpdata_stage_name(int stage) {
   static const char* names[NSTAGE] = {"upwind", "pseudo_velocity", "limiter_bounds", "limited_flux",
                                       "corrective_update", "copy", "predictor_level",
-                                      "predictor_cgrid", "density_outputs", "pair_sums"};
+                                      "predictor_cgrid", "density_outputs", "pair_sums",
+                                      "fused_upwind_pseudo", "fused_pseudo", "fused_limit_update"};
   return (stage >= 0 && stage < NSTAGE) ? names[stage] : "";
 }
 

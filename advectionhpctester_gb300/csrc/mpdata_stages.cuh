@@ -6,7 +6,7 @@ namespace mpdata {
 
 // Stage ids for the optional per-launch CUDA-event timing.
 enum Stage { ST_UPWIND = 0, ST_PSEUDO, ST_BOUNDS, ST_LIMIT, ST_UPDATE, ST_COPY, ST_PRED_LEVEL,
-             ST_PRED_CGRID, ST_RHO_OUT, ST_PAIRS, NSTAGE };
+             ST_PRED_CGRID, ST_RHO_OUT, ST_PAIRS, ST_FZ_UPWIND_PSEUDO, ST_FZ_PSEUDO, ST_FZ_LIMIT, NSTAGE };
 
 // Records a pair of CUDA events around each launch when enabled (the events
 // live on the launching stream, so they time exactly that kernel).
