@@ -21,6 +21,9 @@ INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-I" + INCLUDE, "-I" + CSRC]
+# Extra nvcc flags for tuning sweeps (e.g. "-DMPDATA_FZ_TY=16"); a build with
+# them is never up to date with a default build.
+EXTRA = os.environ.get("MPDATA_NVCC_EXTRA", "").split()
 
 
 def nvcc():
@@ -42,7 +45,7 @@ def _deps():
 
 
 def up_to_date():
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or EXTRA:
         return False
     t = os.path.getmtime(LIB)
     return all(os.path.getmtime(d) <= t for d in _deps())
@@ -59,7 +62,7 @@ def build(force=False, verbose=False):
     for src in _sources():
         obj = os.path.join(OUT, os.path.basename(src)[:-3] + ".o")
         objs.append(obj)
-        cmds.append([exe, *NVCC_FLAGS, "-c", src, "-o", obj])
+        cmds.append([exe, *NVCC_FLAGS, *EXTRA, "-c", src, "-o", obj])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)

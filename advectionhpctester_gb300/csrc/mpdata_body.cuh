@@ -571,7 +571,47 @@ __device__ __forceinline__ RatioOps<R> bounds_body(const Prob<R>& P, int i, int 
   if (!NONOS) return {};
   const bool lo = IN || g.bz || k > 1, hi = IN || g.bz || k < g.lp;
   R ma, mi;
-  if (FIRST) {
+  if constexpr (sizeof(R) == 4) {
+    // FP32 compares with IEEE selects, whose ties between +0 and -0 keep
+    // the earlier operand: fold in the oracle's (and the reference's) tree
+    // order so that every tie goes the same way
+    if (FIRST) {
+      const Arr<R>& xin = P.psi;
+      const int im = cx<IN>(g, i - 1), ip = cx<IN>(g, i + 1);
+      const int jm = cy<IN>(g, j - 1), jp = cy<IN>(g, j + 1);
+      const R a0 = xin.ld(im, j, k), a1 = xin.ld(i, j, k), a2 = xin.ld(ip, j, k), a3 = xin.ld(i, jm, k),
+              a4 = xin.ld(i, jp, k);
+      ma = mx2(mx2(mx2(a0, a1), mx2(a2, a3)), a4);
+      mi = mn2(mn2(mn2(a0, a1), mn2(a2, a3)), a4);
+      if (lo) {
+        const R a5 = xin.ld(i, j, cz<IN>(g, k - 1));
+        ma = mx2(ma, a5);
+        mi = mn2(mi, a5);
+      }
+      if (hi) {
+        const R a6 = xin.ld(i, j, cz<IN>(g, k + 1));
+        ma = mx2(ma, a6);
+        mi = mn2(mi, a6);
+      }
+    } else {
+      ma = P.mx.ld(i, j, k);
+      mi = P.mn.ld(i, j, k);
+    }
+    const R b0 = xr<R, IN>(g, X, i - 1, j, k), b2 = xr<R, IN>(g, X, i + 1, j, k),
+            b3 = xr<R, IN>(g, X, i, j - 1, k), b4 = xr<R, IN>(g, X, i, j + 1, k);
+    ma = mx2(mx2(mx2(ma, b0), mx2(x, b2)), mx2(b3, b4));
+    mi = mn2(mn2(mn2(mi, b0), mn2(x, b2)), mn2(b3, b4));
+    if (lo) {
+      const R b5 = X.ld(i, j, cz<IN>(g, k - 1));
+      ma = mx2(ma, b5);
+      mi = mn2(mi, b5);
+    }
+    if (hi) {
+      const R b6 = X.ld(i, j, cz<IN>(g, k + 1));
+      ma = mx2(ma, b6);
+      mi = mn2(mi, b6);
+    }
+  } else if (FIRST) {
     const Arr<R>& xin = P.psi;
     const int im = cx<IN>(g, i - 1), ip = cx<IN>(g, i + 1);
     const int jm = cy<IN>(g, j - 1), jp = cy<IN>(g, j + 1);

@@ -40,14 +40,32 @@
 namespace mpdata {
 namespace {
 
-constexpr int TX = 32, TY = 8, NT = TX * TY;  // tile of output cells, one thread each
-constexpr int HX = 4, HY = 2;                 // staged halo columns and rows
-constexpr int P = TX + 2 * HX;                // plane pitch: 40
-constexpr int NR = TY + 2 * HY;               // plane rows: 12
-constexpr int PLANE = P * NR;                 // 480 cells, 1920 bytes
-constexpr uint32_t BOX_BYTES = PLANE * 4;
-constexpr int NRING1 = 2 * (TX + 2) + 2 * TY;  // the tile's one-cell ring: 84 cells
-constexpr int NRINGW = TX + TY;                // faces beyond the tile's last row / column: 40
+// Tile heights (build-time, for tuning sweeps).  A tile of 32 x TY cells is
+// one block of 32*TY threads, one output cell each; 1024 threads stay
+// resident per SM (four blocks of 8 rows, two of 16).  The upwind+pseudo
+// kernel, bound by shared-memory traffic, measured 13% faster with 16 rows
+// (its one-cell ring of recomputed upwind cells is a smaller share); the
+// other two measured 4-15% faster with 8 rows.
+#ifndef MPDATA_FZ_TY_UP
+#define MPDATA_FZ_TY_UP 16
+#endif
+#ifndef MPDATA_FZ_TY
+#define MPDATA_FZ_TY 8
+#endif
+constexpr int TX = 32;
+constexpr int HX = 4, HY = 2;   // staged halo columns and rows
+constexpr int P = TX + 2 * HX;  // plane pitch: 40
+template <int TY>
+struct Tl {
+  static constexpr int NT = TX * TY;                     // threads = output cells per plane
+  static constexpr int MINB = 1024 / NT;                 // resident blocks per SM asked of ptxas
+  static constexpr int NR = TY + 2 * HY;                 // staged rows
+  static constexpr int PLANE = P * NR;                   // staged cells per plane
+  static constexpr uint32_t BOX_BYTES = PLANE * 4;
+  static constexpr int NRING1 = 2 * (TX + 2) + 2 * TY;  // the tile's one-cell ring
+  static constexpr int NRINGW = TX + TY;                // faces beyond the tile's last row / column
+};
+constexpr int TY_UP = MPDATA_FZ_TY_UP, TY2 = MPDATA_FZ_TY;
 
 __device__ __forceinline__ int wrapn(int i, int n) {
   int r = (i - 1) % n;
@@ -75,16 +93,17 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* m, uint32_t bytes) {
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* m, uint32_t parity) {
   uint32_t ok;
   asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n\t}"
       : "=r"(ok)
-      : "r"(smem_u32(m)), "r"(parity)
+      : "r"(smem_u32(m)), "r"(parity), "r"(1000000u)
       : "memory");
   return ok != 0;
 }
-// Bounded wait on an mbarrier phase: false when the limit ran out (each
-// try_wait suspends for a bounded time, so the limit is a few seconds).
+// Bounded wait on an mbarrier phase: false when the limit ran out.  Each
+// try_wait suspends the thread until the phase completes or about 1 ms has
+// passed, so a waiting warp issues almost nothing and the limit is seconds.
 __device__ __forceinline__ bool mbar_wait(uint64_t* m, uint32_t parity) {
-  for (int it = 0; it < (1 << 22); it++)
+  for (int it = 0; it < 4096; it++)
     if (mbar_try_wait(m, parity)) return true;
   return false;
 }
@@ -125,7 +144,9 @@ struct Box {
   int i0, j0, i1, j1;
   bool two;
 };
+template <int TY>
 __device__ __forceinline__ Box box_cells(const Geo& g, int x0, int y0, int t) {
+  constexpr int NT = Tl<TY>::NT, PLANE = Tl<TY>::PLANE;
   Box b;
   b.i0 = wrapn(x0 - HX + t % P, g.np);
   b.j0 = wrapn(y0 - HY + t / P, g.mp);
@@ -135,21 +156,30 @@ __device__ __forceinline__ Box box_cells(const Geo& g, int x0, int y0, int t) {
   b.j1 = wrapn(y0 - HY + e / P, g.mp);
   return b;
 }
-// a plane of a caller array (any strides) into a staged plane
-__device__ __forceinline__ void stage_caller(float* dst, const Arr<float>& A, int kw, const Box& b, int t) {
-  const float* base = A.p + (long)(kw - 1) * A.sz;
-  cp_async4(dst + t, base + (b.i0 - 1) + (long)(b.j0 - 1) * A.sy);
-  if (b.two) cp_async4(dst + t + NT, base + (b.i1 - 1) + (long)(b.j1 - 1) * A.sy);
+// In-plane offsets of the thread's two box cells in a layout with row
+// stride sy (every plane of every array used here is below 2^31 elements).
+struct Offs {
+  int o0, o1;
+};
+__device__ __forceinline__ Offs box_offs(const Box& b, int sy) {
+  return Offs{(b.i0 - 1) + (b.j0 - 1) * sy, (b.i1 - 1) + (b.j1 - 1) * sy};
 }
-// a plane of an arena field through the wrapped coordinates (seam tiles)
-__device__ __forceinline__ void stage_arena(float* dst, const float* fbase, int px, int mp, int kw, const Box& b,
-                                            int t) {
-  const float* base = fbase + (long)(kw - 1) * px * mp;
-  cp_async4(dst + t, base + (b.i0 - 1) + (long)(b.j0 - 1) * px);
-  if (b.two) cp_async4(dst + t + NT, base + (b.i1 - 1) + (long)(b.j1 - 1) * px);
+// the thread's two box cells of one plane (base = the plane's cell (1,1))
+template <int NT>
+__device__ __forceinline__ void stage2(float* dst, const float* base, const Offs& o, bool two, int t) {
+  cp_async4(dst + t, base + o.o0);
+  if (two) cp_async4(dst + t + NT, base + o.o1);
 }
+__device__ __forceinline__ const float* caller_plane(const Arr<float>& A, int kw) {
+  return A.p + (long)(kw - 1) * A.sz;
+}
+// the wrapped plane after kw
+__device__ __forceinline__ int next_plane(int kw, int lp) { return kw == lp ? 1 : kw + 1; }
+__device__ __forceinline__ int mod3(int a) { return a >= 3 ? a - 3 : a; }  // a in [0, 5]
+__device__ __forceinline__ bool is1(float v) { return __float_as_int(v) == 0x3f800000; }
 
 // smem index of ring cell q of the tile's one-cell ring
+template <int TY>
 __device__ __forceinline__ int ring1_index(int q) {
   int c, r;
   if (q < TX + 2) {
@@ -167,19 +197,23 @@ __device__ __forceinline__ int ring1_index(int q) {
 }
 // Faces the tile's update reads beyond its cells: the y faces of the row past
 // the tile (q < TX) and the x faces of the column past it.
+template <int TY>
 __device__ __forceinline__ int ringw_index(int q) {
   return q < TX ? (HY + TY) * P + HX + q : (HY + (q - TX)) * P + HX + TX;
 }
 
 // ---- the stage arithmetic on staged planes (FP32 bodies, interior path) ----
+// U: every density the stage reads is exactly 1 (block-uniform), so the
+// products and quotients by it are dropped; x*1 == x/1 == x and
+// 2/(1+1) == 1 hold exactly in IEEE arithmetic, so no bit changes.
 
 // upwind3d_gpubc at smem cell b of plane k: x0/xm/xp = psi at k, k-1, k+1;
-// w3p = u3 at k+1 (the cell's upper face).
+// a3p = u3 at k+1 (the cell's upper face).
+template <bool U>
 __device__ __forceinline__ float upwind_cell(int b, const float* x0, const float* xm, const float* xp,
                                              const float* a1, const float* a2, const float* a3, const float* a3p,
                                              const float* h, const float* rh) {
   const float x = x0[b];
-  const float hi = 1.0f / h[b];
   const float f1p = donor(x, x0[b + 1], a1[b + 1]);
   const float f1 = donor(x0[b - 1], x, a1[b]);
   const float f2p = donor(x, x0[b + P], a2[b + P]);
@@ -187,90 +221,120 @@ __device__ __forceinline__ float upwind_cell(int b, const float* x0, const float
   const float f3p = donor(x, xp[b], a3p[b]);
   const float f3 = donor(xm[b], x, a3[b]);
   const float sum = f1p - f1 + f2p - f2 + f3p - f3;
+  if (U) return x - sum;
+  const float hi = 1.0f / h[b];
   return (x - sum * hi) * rh[b];
 }
 
 // Gauge pseudo-velocities of the cell's three lower faces at plane k:
 // X at k-1, k, k+1; A1, A2 (x and y velocities) at k-1, k; A3 at k, k+1;
 // h at k-1, k.  pseudo_form<float, false, ...> with IN.
+template <bool U>
 __device__ __forceinline__ void pseudo_cell(int b, const float* xm, const float* x0, const float* xp,
                                             const float* a1m, const float* a10, const float* a2m,
                                             const float* a20, const float* a30, const float* a3p,
                                             const float* hm, const float* h0, float& v1, float& v2, float& v3) {
   const float xc = x0[b];
   {  // x face
-    const float hmx = 2.0f / (h0[b - 1] + h0[b]);
+    const float hmx = U ? 1.0f : 2.0f / (h0[b - 1] + h0[b]);
     const float a = a10[b];
     const float d2 = (x0[b + P] + x0[b - 1 + P]) - (x0[b - P] + x0[b - 1 - P]);
     const float s2 = (a20[b - 1] + a20[b - 1 + P]) + (a20[b] + a20[b + P]);
     const float d3 = (xp[b] + xp[b - 1]) - (xm[b] + xm[b - 1]);
     const float s3 = (a30[b - 1] + a3p[b - 1]) + (a30[b] + a3p[b]);
     const float cr = s2 * d2 + s3 * d3;
-    v1 = (fabsf(a) - a * a * hmx) * (xc - x0[b - 1]) * 0.5f - 0.03125f * a * hmx * cr;
+    v1 = (fabsf(a) - hmul<U>(a * a, hmx)) * (xc - x0[b - 1]) * 0.5f - hmul<U>(0.03125f * a, hmx) * cr;
   }
   {  // y face
-    const float hmy = 2.0f / (h0[b - P] + h0[b]);
+    const float hmy = U ? 1.0f : 2.0f / (h0[b - P] + h0[b]);
     const float a = a20[b];
     const float d1 = (x0[b + 1] + x0[b + 1 - P]) - (x0[b - 1] + x0[b - 1 - P]);
     const float s1 = (a10[b - P] + a10[b + 1 - P]) + (a10[b] + a10[b + 1]);
     const float d3 = (xp[b] + xp[b - P]) - (xm[b] + xm[b - P]);
     const float s3 = (a30[b - P] + a3p[b - P]) + (a30[b] + a3p[b]);
     const float cr = s1 * d1 + s3 * d3;
-    v2 = (fabsf(a) - a * a * hmy) * (xc - x0[b - P]) * 0.5f - 0.03125f * a * hmy * cr;
+    v2 = (fabsf(a) - hmul<U>(a * a, hmy)) * (xc - x0[b - P]) * 0.5f - hmul<U>(0.03125f * a, hmy) * cr;
   }
   {  // z face
-    const float hmz = 2.0f / (hm[b] + h0[b]);
+    const float hmz = U ? 1.0f : 2.0f / (hm[b] + h0[b]);
     const float a = a30[b];
     const float d1 = (x0[b + 1] + xm[b + 1]) - (x0[b - 1] + xm[b - 1]);
     const float d2 = (x0[b + P] + xm[b + P]) - (x0[b - P] + xm[b - P]);
     const float s1 = (a1m[b] + a1m[b + 1]) + (a10[b] + a10[b + 1]);
     const float s2 = (a2m[b] + a2m[b + P]) + (a20[b] + a20[b + P]);
     const float cr = s1 * d1 + s2 * d2;
-    v3 = (fabsf(a) - a * a * hmz) * (xc - xm[b]) * 0.5f - 0.03125f * a * hmz * cr;
+    v3 = (fabsf(a) - hmul<U>(a * a, hmz)) * (xc - xm[b]) * 0.5f - hmul<U>(0.03125f * a, hmz) * cr;
+  }
+}
+
+// NaN-propagating max and min (one instruction each).
+__device__ __forceinline__ float maxn(float a, float b) {
+  float r;
+  asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ float minn(float a, float b) {
+  float r;
+  asm("min.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+  return r;
+}
+
+// Star extrema of the limiter bounds.  The reference folds them with
+// compare-and-select in a fixed tree (ties between +0 and -0 keep the earlier
+// operand; a NaN propagates from some positions and not from others).  The
+// fast path takes max/min instructions, which give the same bits whenever no
+// operand is a NaN and the result is not a zero: the largest value is then
+// unique.  Otherwise the select tree runs in the reference's order.
+template <bool FIRST>
+__device__ __forceinline__ void star_extrema(int b, const float* xm, const float* x0, const float* xp,
+                                             const float* s0, const float* sm, const float* sp, float& ma,
+                                             float& mi) {
+  const float x = x0[b];
+  const float b0 = x0[b - 1], b2 = x0[b + 1], b3 = x0[b - P], b4 = x0[b + P], b5 = xm[b], b6 = xp[b];
+  float m0, n0;  // extrema folded before the current field's star
+  float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f, a4 = 0.f, a5 = 0.f, a6 = 0.f;
+  if (FIRST) {
+    a0 = s0[b - 1];
+    a1 = s0[b];
+    a2 = s0[b + 1];
+    a3 = s0[b - P];
+    a4 = s0[b + P];
+    a5 = sm[b];
+    a6 = sp[b];
+    m0 = maxn(maxn(maxn(maxn(maxn(maxn(a0, a1), a2), a3), a4), a5), a6);
+    n0 = minn(minn(minn(minn(minn(minn(a0, a1), a2), a3), a4), a5), a6);
+  } else {
+    m0 = s0[b];
+    n0 = sm[b];
+  }
+  ma = maxn(maxn(maxn(maxn(maxn(maxn(maxn(m0, b0), x), b2), b3), b4), b5), b6);
+  mi = minn(minn(minn(minn(minn(minn(minn(n0, b0), x), b2), b3), b4), b5), b6);
+  if (ma == 0.0f || mi == 0.0f || ma != ma || mi != mi) {
+    if (FIRST) {
+      m0 = mx2(mx2(mx2(mx2(mx2(a0, a1), mx2(a2, a3)), a4), a5), a6);
+      n0 = mn2(mn2(mn2(mn2(mn2(a0, a1), mn2(a2, a3)), a4), a5), a6);
+    } else {
+      m0 = s0[b];
+      n0 = sm[b];
+    }
+    ma = mx2(mx2(mx2(mx2(mx2(m0, b0), mx2(x, b2)), mx2(b3, b4)), b5), b6);
+    mi = mn2(mn2(mn2(mn2(mn2(n0, b0), mn2(x, b2)), mn2(b3, b4)), b5), b6);
   }
 }
 
 // Limiter bounds and ratios of cell b at plane k (bounds_body, FP32, IN):
 // FIRST folds the star of x_in (s0/sm/sp) before the field's own star;
 // later passes start from the running extrema (s0 = mx, sm = mn at k).
-template <bool FIRST>
+template <bool FIRST, bool U>
 __device__ __forceinline__ void bounds_cell(int b, const float* xm, const float* x0, const float* xp,
                                             const float* s0, const float* sm, const float* sp, const float* v1,
                                             const float* v2, const float* v3, const float* v3p, const float* h,
                                             float& cp, float& cn, float& ma, float& mi) {
+  star_extrema<FIRST>(b, xm, x0, xp, s0, sm, sp, ma, mi);
   const float x = x0[b];
-  if (FIRST) {
-    Extrema<float> e(s0[b]);
-    e.add(s0[b - 1]);
-    e.add(s0[b + 1]);
-    e.add(s0[b - P]);
-    e.add(s0[b + P]);
-    e.add(sm[b]);
-    e.add(sp[b]);
-    e.add(x);
-    e.add(x0[b - 1]);
-    e.add(x0[b + 1]);
-    e.add(x0[b - P]);
-    e.add(x0[b + P]);
-    e.add(xm[b]);
-    e.add(xp[b]);
-    ma = e.max();
-    mi = e.min();
-  } else {
-    Extrema<float> e(x);
-    e.add(x0[b - 1]);
-    e.add(x0[b + 1]);
-    e.add(x0[b - P]);
-    e.add(x0[b + P]);
-    e.add(xm[b]);
-    e.add(xp[b]);
-    ma = mx2(s0[b], e.max());
-    mi = mn2(sm[b], e.min());
-  }
   const float e1 = v1[b + 1], w1 = v1[b], e2 = v2[b + P], w2 = v2[b], e3 = v3p[b], w3 = v3[b];
-  const float hc = h[b];
   const float ep = Eps<float>::v;
-  const float np_ = (ma - x) * hc, nn = (x - mi) * hc;
+  const float np_ = U ? ma - x : (ma - x) * h[b], nn = U ? x - mi : (x - mi) * h[b];
   const float dp = pn(e1) + pp(w1) + pn(e2) + pp(w2) + pn(e3) + pp(w3) + ep;
   const float dn = pp(e1) + pn(w1) + pp(e2) + pn(w2) + pp(e3) + pn(w3) + ep;
   cp = lim_ratio(np_, dp);
@@ -278,10 +342,12 @@ __device__ __forceinline__ void bounds_cell(int b, const float* xm, const float*
 }
 
 // ---- K1: upwind + first-pass pseudo-velocities ----------------------------
-// smem planes: psi 4, u1 4, u2 4, u3 4, h 4, rhr 2, xant 3
-constexpr int K1_PLANES = 25;
+// smem planes: psi 4, u1 4, u2 4, u3 4, h 4, rhr 2, xant 4
+constexpr int K1_PLANES = 26;
 
-__global__ void __launch_bounds__(NT, 4) k_fz_upwind_pseudo(const FzArgs A) {
+template <int TY>
+__global__ void __launch_bounds__(Tl<TY>::NT, Tl<TY>::MINB) k_fz_upwind_pseudo(const FzArgs A) {
+  constexpr int NT = Tl<TY>::NT, PLANE = Tl<TY>::PLANE, NRING1 = Tl<TY>::NRING1;
   float* const sm = smem_base();
   float* const PSI = sm;
   float* const U1 = PSI + 4 * PLANE;
@@ -296,118 +362,142 @@ __global__ void __launch_bounds__(NT, 4) k_fz_upwind_pseudo(const FzArgs A) {
   const int kb = blockIdx.z * A.kchunk + 1;
   if (kb > g.lp) return;
   const int ke = min(g.lp, kb + A.kchunk - 1);
-  const Box bx = box_cells(g, x0, y0, t);
+  const Box bx = box_cells<TY>(g, x0, y0, t);
+  const bool two = bx.two;
+  const Offs os = box_offs(bx, A.psi.sy), o1 = box_offs(bx, A.u1.sy), o2 = box_offs(bx, A.u2.sy);
   const int b = (ty + HY) * P + tx + HX;
-  const int br = t < NRING1 ? ring1_index(t) : -1;
+  const int br = t < NRING1 ? ring1_index<TY>(t) : -1;
   const int ig = x0 + tx, jg = y0 + ty;
   const bool own = ig <= g.np && jg <= g.mp;
   const long pl = (long)A.px * g.mp;
   const long go = (long)(ig - 1) + (long)(jg - 1) * A.px;
-  float* const fxin = A.arena + FZ_XIN * A.fs;
-  float* const fxa = A.arena + FZ_X0 * A.fs;
-  float* const fv1 = A.arena + FZ_V1 * A.fs;
-  float* const fv2 = A.arena + FZ_V2 * A.fs;
-  float* const fv3 = A.arena + FZ_V3 * A.fs;
-#define ST4(R, F, k) stage_caller(R + slot<4>(k) * PLANE, A.F, wrapn((k), g.lp), bx, t)
-#define ST2(R, F, k) stage_caller(R + slot<2>(k) * PLANE, A.F, wrapn((k), g.lp), bx, t)
+  float* const fxin = A.arena + FZ_XIN * A.fs + go;
+  float* const fxa = A.arena + FZ_X0 * A.fs + go;
+  float* const fv1 = A.arena + FZ_V1 * A.fs + go;
+  float* const fv2 = A.arena + FZ_V2 * A.fs + go;
+  float* const fv3 = A.arena + FZ_V3 * A.fs + go;
+#define S4(k) (((k) + 12) & 3)
+#define S2(k) ((k) & 1)
   // what the first step (ko = kb-2) reads and does not stage itself
-  for (int k = kb - 2; k <= kb; k++) ST4(PSI, psi, k);
-  for (int k = kb - 1; k <= kb; k++) ST4(U3, u3, k);
-  ST4(U1, u1, kb - 1);
-  ST4(U2, u2, kb - 1);
-  ST4(H, h, kb - 1);
-  ST2(RH, rhr, kb - 1);
+  {
+    int kw = wrapn(kb - 2, g.lp);
+    for (int k = kb - 2; k <= kb; k++, kw = next_plane(kw, g.lp)) {
+      stage2<NT>(PSI + S4(k) * PLANE, caller_plane(A.psi, kw), os, two, t);
+      if (k >= kb - 1) stage2<NT>(U3 + S4(k) * PLANE, caller_plane(A.u3, kw), os, two, t);
+      if (k == kb - 1) {
+        stage2<NT>(U1 + S4(k) * PLANE, caller_plane(A.u1, kw), o1, two, t);
+        stage2<NT>(U2 + S4(k) * PLANE, caller_plane(A.u2, kw), o2, two, t);
+        stage2<NT>(H + S4(k) * PLANE, caller_plane(A.h, kw), os, two, t);
+        stage2<NT>(RH + S2(k) * PLANE, caller_plane(A.rhr, kw), os, two, t);
+      }
+    }
+  }
   cp_commit();
+  int kw3 = wrapn(kb + 1, g.lp), kw2 = wrapn(kb, g.lp);  // wrapped planes ko+3 and ko+2
+  unsigned umask = 0;  // bit d: h and rhr of plane ko+1-d are exactly 1 on the whole box
   for (int ko = kb - 2; ko <= ke; ko++) {
     cp_wait_all();
-    __syncthreads();
+    bool one = is1(H[S4(ko + 1) * PLANE + t]) && is1(RH[S2(ko + 1) * PLANE + t]);
+    if (two) one = one && is1(H[S4(ko + 1) * PLANE + t + NT]) && is1(RH[S2(ko + 1) * PLANE + t + NT]);
+    umask = (umask << 1) | (__syncthreads_and(one) ? 1u : 0u);
+    const bool unit = umask & 1u;                 // the upwind at ko+1: h and rhr at ko+1
+    const bool unit_ps = (umask & 6u) == 6u;      // the pseudo-velocities at ko: h at ko-1 and ko
     if (ko < ke) {
-      ST4(PSI, psi, ko + 3);
-      ST4(U3, u3, ko + 3);
-      ST4(U1, u1, ko + 2);
-      ST4(U2, u2, ko + 2);
-      ST4(H, h, ko + 2);
-      ST2(RH, rhr, ko + 2);
+      stage2<NT>(PSI + S4(ko + 3) * PLANE, caller_plane(A.psi, kw3), os, two, t);
+      stage2<NT>(U3 + S4(ko + 3) * PLANE, caller_plane(A.u3, kw3), os, two, t);
+      stage2<NT>(U1 + S4(ko + 2) * PLANE, caller_plane(A.u1, kw2), o1, two, t);
+      stage2<NT>(U2 + S4(ko + 2) * PLANE, caller_plane(A.u2, kw2), o2, two, t);
+      stage2<NT>(H + S4(ko + 2) * PLANE, caller_plane(A.h, kw2), os, two, t);
+      stage2<NT>(RH + S2(ko + 2) * PLANE, caller_plane(A.rhr, kw2), os, two, t);
       cp_commit();
+      kw3 = next_plane(kw3, g.lp);
+      kw2 = next_plane(kw2, g.lp);
     }
     {  // xant at plane ko+1 on the tile and its ring
       const int k = ko + 1;
-      const float* p0 = PSI + slot<4>(k) * PLANE;
-      const float* pm = PSI + slot<4>(k - 1) * PLANE;
-      const float* pp_ = PSI + slot<4>(k + 1) * PLANE;
-      const float* a1 = U1 + slot<4>(k) * PLANE;
-      const float* a2 = U2 + slot<4>(k) * PLANE;
-      const float* a3 = U3 + slot<4>(k) * PLANE;
-      const float* a3p = U3 + slot<4>(k + 1) * PLANE;
-      const float* h = H + slot<4>(k) * PLANE;
-      const float* rh = RH + slot<2>(k) * PLANE;
-      float* xa = XA + slot<3>(k) * PLANE;
-      const float v = upwind_cell(b, p0, pm, pp_, a1, a2, a3, a3p, h, rh);
+      const float* p0 = PSI + S4(k) * PLANE;
+      const float* pm = PSI + S4(k - 1) * PLANE;
+      const float* pp_ = PSI + S4(k + 1) * PLANE;
+      const float* a1 = U1 + S4(k) * PLANE;
+      const float* a2 = U2 + S4(k) * PLANE;
+      const float* a3 = U3 + S4(k) * PLANE;
+      const float* a3p = U3 + S4(k + 1) * PLANE;
+      const float* h = H + S4(k) * PLANE;
+      const float* rh = RH + S2(k) * PLANE;
+      float* xa = XA + S4(k) * PLANE;
+      float v;
+      if (unit) {
+        v = upwind_cell<true>(b, p0, pm, pp_, a1, a2, a3, a3p, h, rh);
+        if (br >= 0) xa[br] = upwind_cell<true>(br, p0, pm, pp_, a1, a2, a3, a3p, h, rh);
+      } else {
+        v = upwind_cell<false>(b, p0, pm, pp_, a1, a2, a3, a3p, h, rh);
+        if (br >= 0) xa[br] = upwind_cell<false>(br, p0, pm, pp_, a1, a2, a3, a3p, h, rh);
+      }
       xa[b] = v;
-      if (br >= 0) xa[br] = upwind_cell(br, p0, pm, pp_, a1, a2, a3, a3p, h, rh);
       if (own && k >= kb && k <= ke) {
-        fxa[go + (k - 1) * pl] = v;
-        fxin[go + (k - 1) * pl] = p0[b];
+        fxa[(k - 1) * pl] = v;
+        fxin[(k - 1) * pl] = p0[b];
       }
     }
     __syncthreads();
     if (ko >= kb) {
       float v1, v2, v3;
-      pseudo_cell(b, XA + slot<3>(ko - 1) * PLANE, XA + slot<3>(ko) * PLANE, XA + slot<3>(ko + 1) * PLANE,
-                  U1 + slot<4>(ko - 1) * PLANE, U1 + slot<4>(ko) * PLANE, U2 + slot<4>(ko - 1) * PLANE,
-                  U2 + slot<4>(ko) * PLANE, U3 + slot<4>(ko) * PLANE, U3 + slot<4>(ko + 1) * PLANE,
-                  H + slot<4>(ko - 1) * PLANE, H + slot<4>(ko) * PLANE, v1, v2, v3);
+      const float *xm = XA + S4(ko - 1) * PLANE, *xc = XA + S4(ko) * PLANE, *xp = XA + S4(ko + 1) * PLANE;
+      const float *a1m = U1 + S4(ko - 1) * PLANE, *a10 = U1 + S4(ko) * PLANE;
+      const float *a2m = U2 + S4(ko - 1) * PLANE, *a20 = U2 + S4(ko) * PLANE;
+      const float *a30 = U3 + S4(ko) * PLANE, *a3p = U3 + S4(ko + 1) * PLANE;
+      const float *hm = H + S4(ko - 1) * PLANE, *h0 = H + S4(ko) * PLANE;
+      if (unit_ps)
+        pseudo_cell<true>(b, xm, xc, xp, a1m, a10, a2m, a20, a30, a3p, hm, h0, v1, v2, v3);
+      else
+        pseudo_cell<false>(b, xm, xc, xp, a1m, a10, a2m, a20, a30, a3p, hm, h0, v1, v2, v3);
       if (own) {
-        const long o = go + (ko - 1) * pl;
+        const long o = (ko - 1) * pl;
         fv1[o] = v1;
         fv2[o] = v2;
         fv3[o] = v3;
       }
     }
   }
-#undef ST4
-#undef ST2
 }
 
 // ---- staging of arena fields: TMA on interior tiles, wrapped cp.async else ----
+template <int NT>
 struct Stager {
   const CUtensorMap* map;
   const float* arena;
   long fs;
-  int px, mp, lp;
+  long pl;     // elements per arena plane
   int xc, yc;  // box origin (0-based) of the tile
-  bool tma;
-  Box bx;
+  bool tma, two;
+  Offs o;      // the thread's two box cells in the arena layout (seam tiles)
   int t;
-  __device__ __forceinline__ void plane(float* dst, int f, int k, uint64_t* m) const {
-    const int kw = wrapn(k, lp);
+  // plane kw (1-based, wrapped) of arena field f into dst
+  __device__ __forceinline__ void plane(float* dst, int f, int kw, uint64_t* m) const {
     if (tma) {
       if (t == 0) tma_box(dst, map, xc, yc, kw - 1, f, m);
     } else {
-      stage_arena(dst, arena + f * fs, px, mp, kw, bx, t);
+      stage2<NT>(dst, arena + f * fs + (kw - 1) * pl, o, two, t);
     }
   }
 };
 
 // Interior tile: every staged box lies inside the grid, so TMA needs no wrap.
+template <int TY>
 __device__ __forceinline__ bool tile_inside(const Geo& g) {
   return blockIdx.x >= 1 && (int)blockIdx.x * TX + TX + HX <= g.np && blockIdx.y >= 1 &&
          (int)blockIdx.y * TY + TY + HY <= g.mp;
 }
 
-// Waits for the staging of the previous iteration (cp.async groups of this
-// thread, and the TMA phase of the block), then the block barrier.  Returns
-// false (in every thread) when a TMA wait ran out: the error word is set.
-__device__ __forceinline__ bool stage_sync(bool tma, uint64_t* mbar, int n, int* s_abort, int* err) {
-  cp_wait_all();
+// Waits for the TMA phase of the previous iteration (bounded); false when the
+// limit ran out, after setting the block's abort flag and the error word.
+__device__ __forceinline__ void tma_wait(bool tma, uint64_t* mbar, int n, int* s_abort, int* err) {
   if (tma && n >= 1) {
     if (!mbar_wait(&mbar[(n - 1) & 1], ((n - 1) >> 1) & 1)) {
       *s_abort = 1;
       atomicOr(err, 2);
     }
   }
-  __syncthreads();
-  return *s_abort == 0;
 }
 
 // ---- K2: limiter bounds + limited velocities + update of one pass ----------
@@ -416,8 +506,11 @@ __device__ __forceinline__ bool stage_sync(bool tma, uint64_t* mbar, int n, int*
 constexpr int K2_PLANES = 26;
 constexpr int K2_TILES = 4;
 
-template <bool FIRST, bool LAST, bool KEEP>
-__global__ void __launch_bounds__(NT, 4) k_fz_limit(const FzArgs A, const __grid_constant__ CUtensorMap tm) {
+template <int TY, bool FIRST, bool LAST, bool KEEP>
+__global__ void __launch_bounds__(Tl<TY>::NT, Tl<TY>::MINB)
+    k_fz_limit(const FzArgs A, const __grid_constant__ CUtensorMap tm) {
+  constexpr int NT = Tl<TY>::NT, PLANE = Tl<TY>::PLANE, NRING1 = Tl<TY>::NRING1, NRINGW = Tl<TY>::NRINGW;
+  constexpr uint32_t BOX_BYTES = Tl<TY>::BOX_BYTES;
   float* const sm = smem_base();
   float* const X = sm;
   float* const S = X + 4 * PLANE;
@@ -439,16 +532,25 @@ __global__ void __launch_bounds__(NT, 4) k_fz_limit(const FzArgs A, const __grid
   const int kb = blockIdx.z * A.kchunk + 1;
   if (kb > g.lp) return;
   const int ke = min(g.lp, kb + A.kchunk - 1);
-  const bool tma = tile_inside(g);
-  const Stager st{&tm, A.arena, A.fs, A.px, g.mp, g.lp, x0 - 1 - HX, y0 - 1 - HY, tma, box_cells(g, x0, y0, t), t};
+  const bool tma = tile_inside<TY>(g);
+  const Box bx = box_cells<TY>(g, x0, y0, t);
+  const bool two = bx.two;
+  const long pl = (long)A.px * g.mp;
+  const Stager<NT> st{&tm, A.arena, A.fs, pl, x0 - 1 - HX, y0 - 1 - HY, tma, two, box_offs(bx, A.px), t};
+  const Offs oh = box_offs(bx, A.h.sy);
   const int b = (ty + HY) * P + tx + HX;
-  const int br = t < NRING1 ? ring1_index(t) : -1;
-  const int bw = t < NRINGW ? ringw_index(t) : -1;
+  const int br = t < NRING1 ? ring1_index<TY>(t) : -1;
+  const int bw = t < NRINGW ? ringw_index<TY>(t) : -1;
   const int ig = x0 + tx, jg = y0 + ty;
   const bool own = ig <= g.np && jg <= g.mp;
-  const int ipw = wrapn(ig, g.np), jpw = wrapn(jg, g.mp);
-  const long pl = (long)A.px * g.mp;
+  const int orh = (wrapn(ig, g.np) - 1) + (wrapn(jg, g.mp) - 1) * A.rhr.sy;
   const long go = (long)(ig - 1) + (long)(jg - 1) * A.px;
+  float* const fmx = A.arena + A.fmx_out * A.fs + go;
+  float* const fmn = A.arena + A.fmn_out * A.fs + go;
+  float* const fw1 = A.arena + FZ_W1 * A.fs + go;
+  float* const fw2 = A.arena + FZ_W2 * A.fs + go;
+  float* const fw3 = A.arena + FZ_W3 * A.fs + go;
+  float* const fout = A.arena + A.fout * A.fs + go;
   if (t == 0) {
     s_abort = 0;
     mbar_init(&mbar[0], 1);
@@ -458,77 +560,100 @@ __global__ void __launch_bounds__(NT, 4) k_fz_limit(const FzArgs A, const __grid
   __syncthreads();
   constexpr int NBOX_PRO = FIRST ? 10 : 9;  // boxes staged before the first step
   constexpr int NBOX = FIRST ? 5 : 6;       // boxes staged by each step
-  const int fs_ = FIRST ? FZ_XIN : A.fmx_in;
+  const int fsx = FIRST ? FZ_XIN : A.fmx_in;
+#define S4(k) (((k) + 12) & 3)
+#define S2(k) ((k) & 1)
   // staging of the first step's reads
   if (tma && t == 0) mbar_expect_tx(&mbar[0], NBOX_PRO * BOX_BYTES);
-  for (int k = kb - 2; k <= kb; k++) {
-    st.plane(X + slot<4>(k) * PLANE, A.fin, k, &mbar[0]);
-    if (FIRST) st.plane(S + slot<4>(k) * PLANE, FZ_XIN, k, &mbar[0]);
+  {
+    int kw = wrapn(kb - 2, g.lp);
+    for (int k = kb - 2; k <= kb; k++, kw = next_plane(kw, g.lp)) {
+      st.plane(X + S4(k) * PLANE, A.fin, kw, &mbar[0]);
+      if (FIRST) st.plane(S + S4(k) * PLANE, FZ_XIN, kw, &mbar[0]);
+      if (k >= kb - 1) st.plane(V3 + mod3(k - kb + 5) * PLANE, FZ_V3, kw, &mbar[0]);
+      if (k == kb - 1) {
+        st.plane(V1 + S2(k) * PLANE, FZ_V1, kw, &mbar[0]);
+        st.plane(V2 + S2(k) * PLANE, FZ_V2, kw, &mbar[0]);
+        if (!FIRST) {
+          st.plane(S + S2(k) * PLANE, fsx, kw, &mbar[0]);
+          st.plane(S + (2 + S2(k)) * PLANE, A.fmn_in, kw, &mbar[0]);
+        }
+        stage2<NT>(H + mod3(k - kb + 5) * PLANE, caller_plane(A.h, kw), oh, two, t);
+      }
+    }
   }
-  for (int k = kb - 1; k <= kb; k++) st.plane(V3 + slot<3>(k) * PLANE, FZ_V3, k, &mbar[0]);
-  st.plane(V1 + slot<2>(kb - 1) * PLANE, FZ_V1, kb - 1, &mbar[0]);
-  st.plane(V2 + slot<2>(kb - 1) * PLANE, FZ_V2, kb - 1, &mbar[0]);
-  if (!FIRST) {
-    st.plane(S + slot<2>(kb - 1) * PLANE, fs_, kb - 1, &mbar[0]);
-    st.plane(S + (2 + slot<2>(kb - 1)) * PLANE, A.fmn_in, kb - 1, &mbar[0]);
-  }
-  stage_caller(H + slot<3>(kb - 1) * PLANE, A.h, wrapn(kb - 1, g.lp), st.bx, t);
   cp_commit();
+  // ring slots of the 3-plane rings: r3 = slot of plane ko (planes ko-kb+5 mod 3)
+  int r3 = 0;  // plane ko = kb-2 has slot (kb-2-kb+5) mod 3 = 0
+  int kw3 = wrapn(kb + 1, g.lp), kw2 = wrapn(kb, g.lp), kw1 = wrapn(kb - 1, g.lp);  // planes ko+3, +2, +1
   for (int ko = kb - 2; ko <= ke; ko++) {
     const int n = ko - kb + 3;
-    if (!stage_sync(tma, mbar, n, &s_abort, A.err)) return;
+    const int q0 = r3, q1 = mod3(r3 + 1), q2 = mod3(r3 + 2);  // slots of planes ko, ko+1, ko+2 (= ko-1)
+    cp_wait_all();
+    tma_wait(tma, mbar, n, &s_abort, A.err);
+    // densities of this step (h at ko and ko+1, rhr at ko) all exactly 1?
+    bool one = is1(H[q0 * PLANE + t]) && is1(H[q1 * PLANE + t]) && is1(RH[S2(ko) * NT + t]);
+    if (two) one = one && is1(H[q0 * PLANE + t + NT]) && is1(H[q1 * PLANE + t + NT]);
+    const bool unit = __syncthreads_and(one);
+    if (s_abort) return;
     if (ko < ke) {
       uint64_t* m = &mbar[n & 1];
       if (tma && t == 0) mbar_expect_tx(m, NBOX * BOX_BYTES);
-      st.plane(X + slot<4>(ko + 3) * PLANE, A.fin, ko + 3, m);
-      if (FIRST) st.plane(S + slot<4>(ko + 3) * PLANE, FZ_XIN, ko + 3, m);
-      st.plane(V3 + slot<3>(ko + 3) * PLANE, FZ_V3, ko + 3, m);
-      st.plane(V1 + slot<2>(ko + 2) * PLANE, FZ_V1, ko + 2, m);
-      st.plane(V2 + slot<2>(ko + 2) * PLANE, FZ_V2, ko + 2, m);
+      st.plane(X + S4(ko + 3) * PLANE, A.fin, kw3, m);
+      if (FIRST) st.plane(S + S4(ko + 3) * PLANE, FZ_XIN, kw3, m);
+      st.plane(V3 + q0 * PLANE, FZ_V3, kw3, m);  // plane ko+3 takes the slot of ko
+      st.plane(V1 + S2(ko + 2) * PLANE, FZ_V1, kw2, m);
+      st.plane(V2 + S2(ko + 2) * PLANE, FZ_V2, kw2, m);
       if (!FIRST) {
-        st.plane(S + slot<2>(ko + 2) * PLANE, fs_, ko + 2, m);
-        st.plane(S + (2 + slot<2>(ko + 2)) * PLANE, A.fmn_in, ko + 2, m);
+        st.plane(S + S2(ko + 2) * PLANE, fsx, kw2, m);
+        st.plane(S + (2 + S2(ko + 2)) * PLANE, A.fmn_in, kw2, m);
       }
-      stage_caller(H + slot<3>(ko + 2) * PLANE, A.h, wrapn(ko + 2, g.lp), st.bx, t);
-      {
-        const int kw = wrapn(ko + 1, g.lp);
-        cp_async4(RH + slot<2>(ko + 1) * NT + t, &A.rhr.p[A.rhr.off(ipw, jpw, kw)]);
-      }
+      stage2<NT>(H + q2 * PLANE, caller_plane(A.h, kw2), oh, two, t);  // plane ko+2 takes the slot of ko-1
+      cp_async4(RH + S2(ko + 1) * NT + t, caller_plane(A.rhr, kw1) + orh);
       cp_commit();
+      kw3 = next_plane(kw3, g.lp);
+      kw2 = next_plane(kw2, g.lp);
+      kw1 = next_plane(kw1, g.lp);
     }
     // limiter bounds and ratios at plane ko+1, on the tile and its ring
     const int kc = ko + 1;
     {
-      const float* xm = X + slot<4>(kc - 1) * PLANE;
-      const float* xc = X + slot<4>(kc) * PLANE;
-      const float* xp = X + slot<4>(kc + 1) * PLANE;
+      const float* xm = X + S4(kc - 1) * PLANE;
+      const float* xc = X + S4(kc) * PLANE;
+      const float* xp = X + S4(kc + 1) * PLANE;
       const float *s0, *s1, *s2;
       if (FIRST) {
-        s0 = S + slot<4>(kc) * PLANE;
-        s1 = S + slot<4>(kc - 1) * PLANE;
-        s2 = S + slot<4>(kc + 1) * PLANE;
+        s0 = S + S4(kc) * PLANE;
+        s1 = S + S4(kc - 1) * PLANE;
+        s2 = S + S4(kc + 1) * PLANE;
       } else {
-        s0 = S + slot<2>(kc) * PLANE;        // mx
-        s1 = S + (2 + slot<2>(kc)) * PLANE;  // mn
+        s0 = S + S2(kc) * PLANE;        // mx
+        s1 = S + (2 + S2(kc)) * PLANE;  // mn
         s2 = nullptr;
       }
-      const float* v1 = V1 + slot<2>(kc) * PLANE;
-      const float* v2 = V2 + slot<2>(kc) * PLANE;
-      const float* v3 = V3 + slot<3>(kc) * PLANE;
-      const float* v3p = V3 + slot<3>(kc + 1) * PLANE;
-      const float* h = H + slot<3>(kc) * PLANE;
-      float* cp = CP + slot<2>(kc) * PLANE;
-      float* cn = CN + slot<2>(kc) * PLANE;
+      const float* v1 = V1 + S2(kc) * PLANE;
+      const float* v2 = V2 + S2(kc) * PLANE;
+      const float* v3 = V3 + q1 * PLANE;
+      const float* v3p = V3 + q2 * PLANE;
+      const float* h = H + q1 * PLANE;
+      float* cp = CP + S2(kc) * PLANE;
+      float* cn = CN + S2(kc) * PLANE;
       float rp, rn, ma, mi;
-      bounds_cell<FIRST>(b, xm, xc, xp, s0, s1, s2, v1, v2, v3, v3p, h, rp, rn, ma, mi);
+      if (unit)
+        bounds_cell<FIRST, true>(b, xm, xc, xp, s0, s1, s2, v1, v2, v3, v3p, h, rp, rn, ma, mi);
+      else
+        bounds_cell<FIRST, false>(b, xm, xc, xp, s0, s1, s2, v1, v2, v3, v3p, h, rp, rn, ma, mi);
       cp[b] = rp;
       cn[b] = rn;
       if (KEEP && own && kc >= kb && kc <= ke) {
-        A.arena[A.fmx_out * A.fs + go + (kc - 1) * pl] = ma;
-        A.arena[A.fmn_out * A.fs + go + (kc - 1) * pl] = mi;
+        fmx[(kc - 1) * pl] = ma;
+        fmn[(kc - 1) * pl] = mi;
       }
       if (br >= 0) {
-        bounds_cell<FIRST>(br, xm, xc, xp, s0, s1, s2, v1, v2, v3, v3p, h, rp, rn, ma, mi);
+        if (unit)
+          bounds_cell<FIRST, true>(br, xm, xc, xp, s0, s1, s2, v1, v2, v3, v3p, h, rp, rn, ma, mi);
+        else
+          bounds_cell<FIRST, false>(br, xm, xc, xp, s0, s1, s2, v1, v2, v3, v3p, h, rp, rn, ma, mi);
         cp[br] = rp;
         cn[br] = rn;
       }
@@ -536,27 +661,27 @@ __global__ void __launch_bounds__(NT, 4) k_fz_limit(const FzArgs A, const __grid
     __syncthreads();
     // limited velocities at plane ko+1 (limit_form, gauge, nonos)
     if (kc >= kb) {
-      const float* cp = CP + slot<2>(kc) * PLANE;
-      const float* cn = CN + slot<2>(kc) * PLANE;
-      const float* cpm = CP + slot<2>(kc - 1) * PLANE;
-      const float* cnm = CN + slot<2>(kc - 1) * PLANE;
-      const float* v1 = V1 + slot<2>(kc) * PLANE;
-      const float* v2 = V2 + slot<2>(kc) * PLANE;
-      const float* v3 = V3 + slot<3>(kc) * PLANE;
-      float* w1 = W1 + slot<2>(kc) * PLANE;
-      float* w2 = W2 + slot<2>(kc) * PLANE;
+      const float* cp = CP + S2(kc) * PLANE;
+      const float* cn = CN + S2(kc) * PLANE;
+      const float* cpm = CP + S2(kc - 1) * PLANE;
+      const float* cnm = CN + S2(kc - 1) * PLANE;
+      const float* v1 = V1 + S2(kc) * PLANE;
+      const float* v2 = V2 + S2(kc) * PLANE;
+      const float* v3 = V3 + q1 * PLANE;
+      float* w1 = W1 + S2(kc) * PLANE;
+      float* w2 = W2 + S2(kc) * PLANE;
       const float cpc = cp[b], cnc = cn[b];
       const float r1 = donor(min3(cpc, cn[b - 1]), min3(cp[b - 1], cnc), v1[b]);
       const float r2 = donor(min3(cpc, cn[b - P]), min3(cp[b - P], cnc), v2[b]);
-      const float r3 = donor(min3(cpc, cnm[b]), min3(cpm[b], cnc), v3[b]);
+      const float r3v = donor(min3(cpc, cnm[b]), min3(cpm[b], cnc), v3[b]);
       w1[b] = r1;
       w2[b] = r2;
-      W3[slot<2>(kc) * NT + t] = r3;
+      W3[S2(kc) * NT + t] = r3v;
       if (!LAST && own && kc <= ke) {
-        const long o = go + (kc - 1) * pl;
-        A.arena[FZ_W1 * A.fs + o] = r1;
-        A.arena[FZ_W2 * A.fs + o] = r2;
-        A.arena[FZ_W3 * A.fs + o] = r3;
+        const long o = (kc - 1) * pl;
+        fw1[o] = r1;
+        fw2[o] = r2;
+        fw3[o] = r3v;
       }
       if (bw >= 0) {
         const float cq = cp[bw], nq = cn[bw];
@@ -569,37 +694,46 @@ __global__ void __launch_bounds__(NT, 4) k_fz_limit(const FzArgs A, const __grid
     __syncthreads();
     // corrective update of plane ko (update_body, gauge)
     if (ko >= kb) {
-      const float* w1 = W1 + slot<2>(ko) * PLANE;
-      const float* w2 = W2 + slot<2>(ko) * PLANE;
-      const float* w3 = W3 + slot<2>(ko) * NT;
-      const float* w3p = W3 + slot<2>(ko + 1) * NT;
-      const float* xc = X + slot<4>(ko) * PLANE;
-      const float* h = H + slot<3>(ko) * PLANE;
-      const float rh = RH[slot<2>(ko) * NT + t];
+      const float* w1 = W1 + S2(ko) * PLANE;
+      const float* w2 = W2 + S2(ko) * PLANE;
+      const float* w3 = W3 + S2(ko) * NT;
+      const float* w3p = W3 + S2(ko + 1) * NT;
+      const float xc = X[S4(ko) * PLANE + b];
       const float d = w1[b + 1] - w1[b] + w2[b + P] - w2[b] + w3p[t] - w3[t];
-      const float q = xc[b] / rh;
-      const float out = (q - d / h[b]) * rh;
+      float out;
+      if (unit) {
+        out = xc - d;
+      } else {
+        const float rh = RH[S2(ko) * NT + t];
+        const float q = xc / rh;
+        out = (q - d / H[q0 * PLANE + b]) * rh;
+      }
       if (own) {
         if (LAST)
           A.psi.at(ig, jg, ko) = out;
         else
-          A.arena[A.fout * A.fs + go + (ko - 1) * pl] = out;
+          fout[(ko - 1) * pl] = out;
       }
     }
+    r3 = q1;
   }
 }
 
 // ---- K3: pseudo-velocities of a later pass ---------------------------------
-// smem planes: x 4, w1 3, w2 3, w3 3, h 3
-constexpr int K3_PLANES = 16;
+// smem planes: x 4, w1 4, w2 4, w3 4, h 4
+constexpr int K3_PLANES = 20;
 
-__global__ void __launch_bounds__(NT, 4) k_fz_pseudo(const FzArgs A, const __grid_constant__ CUtensorMap tm) {
+template <int TY>
+__global__ void __launch_bounds__(Tl<TY>::NT, Tl<TY>::MINB)
+    k_fz_pseudo(const FzArgs A, const __grid_constant__ CUtensorMap tm) {
+  constexpr int NT = Tl<TY>::NT, PLANE = Tl<TY>::PLANE;
+  constexpr uint32_t BOX_BYTES = Tl<TY>::BOX_BYTES;
   float* const sm = smem_base();
   float* const X = sm;
   float* const A1 = X + 4 * PLANE;
-  float* const A2 = A1 + 3 * PLANE;
-  float* const A3 = A2 + 3 * PLANE;
-  float* const H = A3 + 3 * PLANE;
+  float* const A2 = A1 + 4 * PLANE;
+  float* const A3 = A2 + 4 * PLANE;
+  float* const H = A3 + 4 * PLANE;
   __shared__ __align__(8) uint64_t mbar[2];
   __shared__ int s_abort;
   const Geo& g = A.g;
@@ -608,13 +742,19 @@ __global__ void __launch_bounds__(NT, 4) k_fz_pseudo(const FzArgs A, const __gri
   const int kb = blockIdx.z * A.kchunk + 1;
   if (kb > g.lp) return;
   const int ke = min(g.lp, kb + A.kchunk - 1);
-  const bool tma = tile_inside(g);
-  const Stager st{&tm, A.arena, A.fs, A.px, g.mp, g.lp, x0 - 1 - HX, y0 - 1 - HY, tma, box_cells(g, x0, y0, t), t};
+  const bool tma = tile_inside<TY>(g);
+  const Box bx = box_cells<TY>(g, x0, y0, t);
+  const bool two = bx.two;
+  const long pl = (long)A.px * g.mp;
+  const Stager<NT> st{&tm, A.arena, A.fs, pl, x0 - 1 - HX, y0 - 1 - HY, tma, two, box_offs(bx, A.px), t};
+  const Offs oh = box_offs(bx, A.h.sy);
   const int b = (ty + HY) * P + tx + HX;
   const int ig = x0 + tx, jg = y0 + ty;
   const bool own = ig <= g.np && jg <= g.mp;
-  const long pl = (long)A.px * g.mp;
   const long go = (long)(ig - 1) + (long)(jg - 1) * A.px;
+  float* const fv1 = A.arena + FZ_V1 * A.fs + go;
+  float* const fv2 = A.arena + FZ_V2 * A.fs + go;
+  float* const fv3 = A.arena + FZ_V3 * A.fs + go;
   if (t == 0) {
     s_abort = 0;
     mbar_init(&mbar[0], 1);
@@ -623,44 +763,64 @@ __global__ void __launch_bounds__(NT, 4) k_fz_pseudo(const FzArgs A, const __gri
   }
   __syncthreads();
   if (tma && t == 0) mbar_expect_tx(&mbar[0], 9 * BOX_BYTES);
-  for (int k = kb - 1; k <= kb + 1; k++) st.plane(X + slot<4>(k) * PLANE, A.fin, k, &mbar[0]);
-  for (int k = kb; k <= kb + 1; k++) st.plane(A3 + slot<3>(k) * PLANE, FZ_W3, k, &mbar[0]);
-  for (int k = kb - 1; k <= kb; k++) {
-    st.plane(A1 + slot<3>(k) * PLANE, FZ_W1, k, &mbar[0]);
-    st.plane(A2 + slot<3>(k) * PLANE, FZ_W2, k, &mbar[0]);
-    stage_caller(H + slot<3>(k) * PLANE, A.h, wrapn(k, g.lp), st.bx, t);
+  {
+    int kw = wrapn(kb - 1, g.lp);
+    for (int k = kb - 1; k <= kb + 1; k++, kw = next_plane(kw, g.lp)) {
+      st.plane(X + S4(k) * PLANE, A.fin, kw, &mbar[0]);
+      if (k >= kb) st.plane(A3 + S4(k) * PLANE, FZ_W3, kw, &mbar[0]);
+      if (k <= kb) {
+        st.plane(A1 + S4(k) * PLANE, FZ_W1, kw, &mbar[0]);
+        st.plane(A2 + S4(k) * PLANE, FZ_W2, kw, &mbar[0]);
+        stage2<NT>(H + S4(k) * PLANE, caller_plane(A.h, kw), oh, two, t);
+      }
+    }
   }
   cp_commit();
+  int kw2 = wrapn(kb + 2, g.lp), kw1 = wrapn(kb + 1, g.lp);  // planes ko+2, ko+1
   for (int ko = kb; ko <= ke; ko++) {
     const int n = ko - kb + 1;
-    if (!stage_sync(tma, mbar, n, &s_abort, A.err)) return;
+    cp_wait_all();
+    tma_wait(tma, mbar, n, &s_abort, A.err);
+    bool one = is1(H[S4(ko - 1) * PLANE + t]) && is1(H[S4(ko) * PLANE + t]);
+    if (two) one = one && is1(H[S4(ko - 1) * PLANE + t + NT]) && is1(H[S4(ko) * PLANE + t + NT]);
+    const bool unit = __syncthreads_and(one);
+    if (s_abort) return;
     if (ko < ke) {
       uint64_t* m = &mbar[n & 1];
       if (tma && t == 0) mbar_expect_tx(m, 4 * BOX_BYTES);
-      st.plane(X + slot<4>(ko + 2) * PLANE, A.fin, ko + 2, m);
-      st.plane(A3 + slot<3>(ko + 2) * PLANE, FZ_W3, ko + 2, m);
-      st.plane(A1 + slot<3>(ko + 1) * PLANE, FZ_W1, ko + 1, m);
-      st.plane(A2 + slot<3>(ko + 1) * PLANE, FZ_W2, ko + 1, m);
-      stage_caller(H + slot<3>(ko + 1) * PLANE, A.h, wrapn(ko + 1, g.lp), st.bx, t);
+      st.plane(X + S4(ko + 2) * PLANE, A.fin, kw2, m);
+      st.plane(A3 + S4(ko + 2) * PLANE, FZ_W3, kw2, m);
+      st.plane(A1 + S4(ko + 1) * PLANE, FZ_W1, kw1, m);
+      st.plane(A2 + S4(ko + 1) * PLANE, FZ_W2, kw1, m);
+      stage2<NT>(H + S4(ko + 1) * PLANE, caller_plane(A.h, kw1), oh, two, t);
       cp_commit();
+      kw2 = next_plane(kw2, g.lp);
+      kw1 = next_plane(kw1, g.lp);
     }
     float v1, v2, v3;
-    pseudo_cell(b, X + slot<4>(ko - 1) * PLANE, X + slot<4>(ko) * PLANE, X + slot<4>(ko + 1) * PLANE,
-                A1 + slot<3>(ko - 1) * PLANE, A1 + slot<3>(ko) * PLANE, A2 + slot<3>(ko - 1) * PLANE,
-                A2 + slot<3>(ko) * PLANE, A3 + slot<3>(ko) * PLANE, A3 + slot<3>(ko + 1) * PLANE,
-                H + slot<3>(ko - 1) * PLANE, H + slot<3>(ko) * PLANE, v1, v2, v3);
+    const float *xm = X + S4(ko - 1) * PLANE, *xc = X + S4(ko) * PLANE, *xp = X + S4(ko + 1) * PLANE;
+    const float *a1m = A1 + S4(ko - 1) * PLANE, *a10 = A1 + S4(ko) * PLANE;
+    const float *a2m = A2 + S4(ko - 1) * PLANE, *a20 = A2 + S4(ko) * PLANE;
+    const float *a30 = A3 + S4(ko) * PLANE, *a3p = A3 + S4(ko + 1) * PLANE;
+    const float *hm = H + S4(ko - 1) * PLANE, *h0 = H + S4(ko) * PLANE;
+    if (unit)
+      pseudo_cell<true>(b, xm, xc, xp, a1m, a10, a2m, a20, a30, a3p, hm, h0, v1, v2, v3);
+    else
+      pseudo_cell<false>(b, xm, xc, xp, a1m, a10, a2m, a20, a30, a3p, hm, h0, v1, v2, v3);
     if (own) {
-      const long o = go + (ko - 1) * pl;
-      A.arena[FZ_V1 * A.fs + o] = v1;
-      A.arena[FZ_V2 * A.fs + o] = v2;
-      A.arena[FZ_V3 * A.fs + o] = v3;
+      const long o = (ko - 1) * pl;
+      fv1[o] = v1;
+      fv2[o] = v2;
+      fv3[o] = v3;
     }
   }
+#undef S4
+#undef S2
 }
 
-constexpr size_t K1_SMEM = (size_t)K1_PLANES * PLANE * 4 + 128;
-constexpr size_t K2_SMEM = (size_t)K2_PLANES * PLANE * 4 + (size_t)K2_TILES * NT * 4 + 128;
-constexpr size_t K3_SMEM = (size_t)K3_PLANES * PLANE * 4 + 128;
+constexpr size_t K1_SMEM = (size_t)K1_PLANES * Tl<TY_UP>::PLANE * 4 + 128;
+constexpr size_t K2_SMEM = (size_t)K2_PLANES * Tl<TY2>::PLANE * 4 + (size_t)K2_TILES * Tl<TY2>::NT * 4 + 128;
+constexpr size_t K3_SMEM = (size_t)K3_PLANES * Tl<TY2>::PLANE * 4 + 128;
 
 template <class K>
 int set_smem(K kernel, size_t bytes) {
@@ -671,12 +831,12 @@ int set_smem(K kernel, size_t bytes) {
 int init_kernels() {
   static int rc = [] {
     int r = 0;
-    r |= set_smem(k_fz_upwind_pseudo, K1_SMEM);
-    r |= set_smem(k_fz_limit<true, true, false>, K2_SMEM);
-    r |= set_smem(k_fz_limit<true, false, true>, K2_SMEM);
-    r |= set_smem(k_fz_limit<false, false, true>, K2_SMEM);
-    r |= set_smem(k_fz_limit<false, true, true>, K2_SMEM);
-    r |= set_smem(k_fz_pseudo, K3_SMEM);
+    r |= set_smem(k_fz_upwind_pseudo<TY_UP>, K1_SMEM);
+    r |= set_smem(k_fz_limit<TY2, true, true, false>, K2_SMEM);
+    r |= set_smem(k_fz_limit<TY2, true, false, true>, K2_SMEM);
+    r |= set_smem(k_fz_limit<TY2, false, false, true>, K2_SMEM);
+    r |= set_smem(k_fz_limit<TY2, false, true, true>, K2_SMEM);
+    r |= set_smem(k_fz_pseudo<TY2>, K3_SMEM);
     return r;
   }();
   return rc;
@@ -714,7 +874,7 @@ int fused_make_tmap(CUtensorMap* map, float* arena, int px, const Geo& g) {
   if (!enc) return -5;
   const cuuint64_t dims[4] = {(cuuint64_t)px, (cuuint64_t)g.mp, (cuuint64_t)g.lp, (cuuint64_t)FZ_NF};
   const cuuint64_t strides[3] = {(cuuint64_t)px * 4, (cuuint64_t)px * g.mp * 4, (cuuint64_t)px * g.mp * g.lp * 4};
-  const cuuint32_t box[4] = {(cuuint32_t)P, (cuuint32_t)NR, 1, 1};
+  const cuuint32_t box[4] = {(cuuint32_t)P, (cuuint32_t)Tl<TY2>::NR, 1, 1};
   const cuuint32_t estr[4] = {1, 1, 1, 1};
   const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, arena, dims, strides, box, estr,
                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -729,8 +889,8 @@ int fused_kchunk(const Geo& g) {
   }
   // enough blocks for several waves of 4 resident blocks on every SM, with
   // chunks long enough that the march's start-up planes stay a small share
-  const long tiles = (long)((g.np + TX - 1) / TX) * ((g.mp + TY - 1) / TY);
-  const long want = 152L * 4 * 6;  // about six waves
+  const long tiles = (long)((g.np + TX - 1) / TX) * ((g.mp + TY2 - 1) / TY2);
+  const long want = 152L * Tl<TY2>::MINB * 6;  // about six waves
   int nz = (int)((want + tiles - 1) / tiles);
   if (nz < 1) nz = 1;
   int kc = (g.lp + nz - 1) / nz;
@@ -769,22 +929,23 @@ int run_step_fused(const FusedPlan& F, int iord, Prof* prof, cudaStream_t s, int
   A.fmn_in = FZ_MN0;
   A.fmx_out = FZ_MX0;
   A.fmn_out = FZ_MN0;
-  const dim3 grid((g.np + TX - 1) / TX, (g.mp + TY - 1) / TY, (g.lp + F.kchunk - 1) / F.kchunk);
-  const dim3 blk(NT);
+  const int nz = (g.lp + F.kchunk - 1) / F.kchunk;
+  const dim3 grid1((g.np + TX - 1) / TX, (g.mp + TY_UP - 1) / TY_UP, nz), blk1(Tl<TY_UP>::NT);
+  const dim3 grid((g.np + TX - 1) / TX, (g.mp + TY2 - 1) / TY2, nz), blk(Tl<TY2>::NT);
   const CUtensorMap& tm = *F.tmap;
-  FZ_LAUNCH(ST_FZ_UPWIND_PSEUDO, (k_fz_upwind_pseudo<<<grid, blk, K1_SMEM, s>>>(A)));
+  FZ_LAUNCH(ST_FZ_UPWIND_PSEUDO, (k_fz_upwind_pseudo<TY_UP><<<grid1, blk1, K1_SMEM, s>>>(A)));
   *mx_field = *mn_field = -1;
   for (int pass = 2; pass <= iord; pass++) {
     const bool first = pass == 2, last = pass == iord;
-    if (!first) FZ_LAUNCH(ST_FZ_PSEUDO, (k_fz_pseudo<<<grid, blk, K3_SMEM, s>>>(A, tm)));
+    if (!first) FZ_LAUNCH(ST_FZ_PSEUDO, (k_fz_pseudo<TY2><<<grid, blk, K3_SMEM, s>>>(A, tm)));
     if (first && last)
-      FZ_LAUNCH(ST_FZ_LIMIT, (k_fz_limit<true, true, false><<<grid, blk, K2_SMEM, s>>>(A, tm)));
+      FZ_LAUNCH(ST_FZ_LIMIT, (k_fz_limit<TY2, true, true, false><<<grid, blk, K2_SMEM, s>>>(A, tm)));
     else if (first)
-      FZ_LAUNCH(ST_FZ_LIMIT, (k_fz_limit<true, false, true><<<grid, blk, K2_SMEM, s>>>(A, tm)));
+      FZ_LAUNCH(ST_FZ_LIMIT, (k_fz_limit<TY2, true, false, true><<<grid, blk, K2_SMEM, s>>>(A, tm)));
     else if (!last)
-      FZ_LAUNCH(ST_FZ_LIMIT, (k_fz_limit<false, false, true><<<grid, blk, K2_SMEM, s>>>(A, tm)));
+      FZ_LAUNCH(ST_FZ_LIMIT, (k_fz_limit<TY2, false, false, true><<<grid, blk, K2_SMEM, s>>>(A, tm)));
     else
-      FZ_LAUNCH(ST_FZ_LIMIT, (k_fz_limit<false, true, true><<<grid, blk, K2_SMEM, s>>>(A, tm)));
+      FZ_LAUNCH(ST_FZ_LIMIT, (k_fz_limit<TY2, false, true, true><<<grid, blk, K2_SMEM, s>>>(A, tm)));
     if (iord > 2) {
       *mx_field = A.fmx_out;
       *mn_field = A.fmn_out;
