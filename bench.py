@@ -46,6 +46,10 @@ UNIT = "Gcell-steps/s"
 #   update   r q rhr h|hinv F1..3             w out                     7
 #   predictor level  r o0 x3 o2 x3 h  w o1 x3                            10
 #   predictor cgrid  r o1 x3 o0 x3 h  w u1..3 o2 x3                      13
+# The fused single-precision step (periodic gauge grids):
+#   fused_upwind_pseudo  r psi u1..3 h rhr     w x_in xant v1..3           11
+#   fused_pseudo         r x w1..3 h           w v1..3                      8
+#   fused_limit_update   r x x_in|mx,mn v1..3 h rhr  w x (w1..3) (mx mn)  11..15
 def stage_elems(stage, gauge, iord, precision=64):
     """Compulsory fields read + written per cell by one launch of a stage
     (interior cells, each field once; ncu DRAM bytes agree within 4%)."""
@@ -72,7 +76,25 @@ def stage_elems(stage, gauge, iord, precision=64):
         return 10.0
     if stage == "predictor_cgrid":
         return 13.0
+    if stage == "fused_upwind_pseudo":
+        return 11.0
+    if stage == "fused_pseudo":
+        return 8.0
+    if stage == "fused_limit_update":
+        n = max(iord - 1, 1)                          # passes: first, middle..., last
+        first = 7.0 + 1.0 + (3.0 + 2.0 if n > 1 else 0.0)      # + x_out, w1..3 and mx,mn when more follow
+        later = 8.0 + 1.0 + 2.0 + 3.0                            # mx,mn in; x_out, mx,mn, w1..3 out
+        last = 8.0 + 1.0 + 2.0                                   # mx,mn in; psi, mx,mn out
+        if n == 1:
+            return first
+        return (first + later * (n - 2) + last) / n
     return 2.0
+
+
+# Compulsory DRAM bytes per interior cell of one whole step (read psi, h, rhr
+# and the six A-grid momenta of the two time levels the predictor needs;
+# write psi), per element size: the floor of any implementation of the step.
+STEP_COMPULSORY_ELEMS = 11.0
 
 
 # DRAM bytes and FP64 instructions per cell of the dominant kernel (k_pseudo,
@@ -82,6 +104,10 @@ def stage_elems(stage, gauge, iord, precision=64):
 # Both grow in proportion to the cells of a launch.
 NCU_PSEUDO = {64: {"dram_bytes_per_cell": 127.7, "fp64_inst_per_cell": 45.0},
               32: {"dram_bytes_per_cell": 38.2, "fp64_inst_per_cell": 0.0}}
+# The same for the dominant fused single-precision kernel (the first pass's
+# fused_limit_update) at 384x384x64: DRAM bytes and issued warp instructions
+# per cell (smsp__inst_executed.sum * 32 / cells) and the issue-active share.
+NCU_FUSED_LIMIT = {"dram_bytes_per_cell": 49.9, "inst_per_cell": 613.0, "issue_active": 0.775}
 # GB300 issues 2 FP64 instructions per SM per clock (1.25 TFLOP/s nominal FMA).
 FP64_INST_PER_SM_CLK = 2.0
 # FP64 flops per cell of one launch of each stage (DADD and DMUL 1, DFMA 2),
@@ -90,7 +116,44 @@ FP64_INST_PER_SM_CLK = 2.0
 FP64_FLOPS_PER_CELL = {"upwind": 12.4, "pair_sums": 6.0, "pseudo_velocity": 45.0, "limiter_bounds": 11.7,
                        "limited_flux": 3.0, "corrective_update": 6.2, "predictor_level": 12.0,
                        "predictor_cgrid": 6.0}
+# FP32 arithmetic instructions (FADD, FMUL, FFMA) per cell of one launch of
+# each fused single-precision kernel, counted by ncu
+# (smsp__sass_thread_inst_executed_op_{fadd,fmul,ffma}_pred_on) on the
+# deformational flow at unit density, 384x384x64; the predictor's from its
+# FP64 twin (the same arithmetic).
+FP32_INST_PER_CELL = {"fused_upwind_pseudo": 102.5, "fused_pseudo": 90.0, "fused_limit_update": 52.0,
+                      "predictor_level": 12.0, "predictor_cgrid": 6.0}
+FP32_LANES_PER_SM_CLK = 128.0
 HBM_NOMINAL_GBS = 7900.0  # GB300 HBM3e, nominal
+
+
+def step_roofs(stages, steps, ms_step, cells, precision, peak, sm_mhz, sms):
+    """Step-level roofline: the compulsory bytes of the whole step against
+    HBM, and the attainable floor max(HBM time, arithmetic-pipe time) with
+    the pipe that binds each precision on GB300 (FP64: 2 instructions per SM
+    per clock; FP32: 128 lanes per SM per clock) at the sampled SM clock."""
+    elem = 8 if precision == 64 else 4
+    comp = STEP_COMPULSORY_ELEMS * elem
+    t = ms_step * 1e-3
+    t_hbm = comp * cells / (peak * 1e9)
+    if precision == 64:
+        inst = sum(FP64_FLOPS_PER_CELL.get(k, 0.0) * v[1] for k, v in stages.items()) / steps
+        rate, pipe = FP64_INST_PER_SM_CLK * sms * sm_mhz * 1e6, "fp64_pipe"
+    else:
+        inst = sum(FP32_INST_PER_CELL.get(k, 0.0) * v[1] for k, v in stages.items()) / steps
+        rate, pipe = FP32_LANES_PER_SM_CLK * sms * sm_mhz * 1e6, "fp32_pipe"
+    t_pipe = inst * cells / rate
+    lib_ms = sum(v[0] for v in stages.values()) / steps
+    return {"compulsory_bytes_per_cell": comp,
+            "step_compulsory_frac": round(t_hbm / t, 4),
+            "arith_inst_per_cell": round(inst, 1),
+            "attainable_roof": "hbm" if t_hbm >= t_pipe else pipe,
+            "attainable_ms_per_step": round(max(t_hbm, t_pipe) * 1e3, 4),
+            "step_attainable_frac": round(max(t_hbm, t_pipe) / t, 4),
+            "library_ms_per_step": round(lib_ms, 4),
+            "note": "compulsory: read psi, h, rhr and the six A-grid momenta, write psi; attainable: "
+                    "max(compulsory bytes / HBM peak, arithmetic instructions / %s rate); "
+                    "library_ms_per_step: predictor + step kernels alone (profiled pass)" % pipe}
 
 
 def load_peaks():
@@ -284,7 +347,6 @@ def run_ours(args, ws, rank, local):
         arm.step(n)
     torch.cuda.synchronize()
     # timed region: inputs (268 MB per FP64 field) exceed the 129 MB L2, no flush needed
-    arm.ws.profile(True)
     l0 = M.launch_count()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier(ws)
@@ -299,9 +361,10 @@ def run_ours(args, ws, rank, local):
     launches = M.launch_count() - l0
     ms = e0.elapsed_time(e1)
     ms_max = max_over_ranks(ms, ws)
-    stages = arm.ws.stage_times()
-    arm.ws.profile(False)
     clocks = clk.summary()
+    # per-stage kernel times from a separate profiled pass (event pairs around
+    # every launch), so that the timed region above carries no events
+    stages = profiled_stages(arm, args.warmup + args.steps, args.steps)
     value = ws * cells * args.steps / (ms_max * 1e-3) / 1e9
 
     # roofline of the dominant kernel
@@ -320,8 +383,10 @@ def run_ours(args, ws, rank, local):
             "peak_source": peak_kind, "alg_bytes_per_launch": int(alg_bytes),
             "avg_launch_ms": round(avg_ms, 4),
             "traffic_source": "ncu DRAM bytes per cell of this kernel at 384x384x64, scaled by cells"}
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    roof.update(step_roofs(stages, args.steps, ms_max / args.steps, cells, args.precision, peak,
+                           clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0, sms))
     if args.precision == 64 and ncu:
-        sms = torch.cuda.get_device_properties(local).multi_processor_count
         mhz = clocks.get("sm_max_mhz") or 2070.0
         fp64_peak = FP64_INST_PER_SM_CLK * sms * mhz * 1e6 / 1e9
         fp64_ach = ncu["fp64_inst_per_cell"] * cells / (avg_ms * 1e-3) / 1e9
@@ -350,8 +415,12 @@ def run_ours(args, ws, rank, local):
                           "l2": "each field %.0f MB > 129 MB L2; no flush" % (cells * elem / 1e6),
                           "parallelism": "replicas" if ws > 1 else "single"},
                   roofline=roof, gpu_launches=int(launches), clocks=clocks, stages=stage_json,
-                  step_alg_bytes=int(step_alg),
-                  step_hbm_frac=round(step_alg / (ms_max / args.steps * 1e-3) / 1e9 / peak, 4))
+                  stage_io={"bytes_per_step": int(step_alg),
+                            "bytes_per_cell": round(step_alg / cells, 1),
+                            "gbs": round(step_alg / (ms_max / args.steps * 1e-3) / 1e9, 1),
+                            "note": "every stage kernel's own inputs and outputs, intermediates "
+                                    "included; a traffic figure, not a roofline (the compulsory "
+                                    "bytes are roofline.compulsory_bytes_per_cell)"})
     mass1 = M.mass(arm.psi, arm.h)
     result["mass_rel_drift"] = (mass1 - mass0) / mass0
     # the last step's output against the running extrema its limiter kept (h = rhr = 1 here)
@@ -359,7 +428,7 @@ def run_ours(args, ws, rank, local):
     result["limiter_bound_violations"] = {"count": arm.ws.bound_violations(arm.psi, tol), "cells": cells,
                                           "tol": tol, "step": "the last timed step"}
     if rank == 0 and ws == 1 and not args.no_extras and args.precision == 64:
-        result["fp32"] = run_fp32_study(args, host, arm, ms_max / args.steps, mass0)
+        result["fp32"] = run_fp32_study(args, host, arm, ms_max / args.steps, mass0, peak, peak_kind, sms)
     if rank == 0 and ws == 1 and not args.no_extras:
         result["variable_density"] = run_density_study(args, host, ms_max / args.steps)
     if not args.no_e2e:
@@ -383,9 +452,23 @@ def run_ours(args, ws, rank, local):
     return result
 
 
-def run_fp32_study(args, host, arm64, ms64, mass0):
+def profiled_stages(arm, n0, steps):
+    """Per-stage kernel times of `steps` further steps with an event pair
+    around every launch; the field keeps advancing (steps n0, n0+1, ...)."""
+    import torch
+    torch.cuda.synchronize()
+    arm.ws.profile(True)
+    for n in range(n0, n0 + steps):
+        arm.step(n)
+    stages = arm.ws.stage_times()
+    arm.ws.profile(False)
+    return stages
+
+
+def run_fp32_study(args, host, arm64, ms64, mass0, peak, peak_kind, sms):
     """Same workload and steps in FP32 (the precision study): speedup
-    over the FP64 run, error against it, and FP64-compensated mass drift."""
+    over the FP64 run, error against it, FP64-compensated mass drift, and
+    the roofline of the FP32 step (its dominant kernel and the whole step)."""
     import torch
     M = arm64.M
     nx, ny, nz = args.grid
@@ -394,20 +477,51 @@ def run_fp32_study(args, host, arm64, ms64, mass0):
         arm.step(n)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for n in range(args.warmup, args.warmup + args.steps):
-        arm.step(n)
-    e1.record()
-    torch.cuda.synchronize()
+    l0 = M.launch_count()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        e0.record()
+        for n in range(args.warmup, args.warmup + args.steps):
+            arm.step(n)
+        e1.record()
+        torch.cuda.synchronize()
+    launches = M.launch_count() - l0
+    clocks = clk.summary()
     ms = e0.elapsed_time(e1) / args.steps
+    # the profiled pass also brings the field to the FP64 run's step count
+    # (it ran warmup + steps timed steps and as many profiled ones)
+    stages = profiled_stages(arm, args.warmup + args.steps, args.steps)
+    steps_compared = args.warmup + 2 * args.steps
     linf, l2, bmax, bl2 = M.error_norms(arm.psi, arm64.psi)
     m32 = M.mass(arm.psi, arm.h)
     cells = nx * ny * nz
+    dom = max(stages.items(), key=lambda kv: kv[1][0])
+    name, (tot_ms, nl) = dom
+    avg_ms = tot_ms / max(nl, 1)
+    alg = stage_elems(name, True, 3, 32) * 4 * cells
+    achieved = alg / (avg_ms * 1e-3) / 1e9
+    fused = name.startswith("fused")
+    roof = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "peak_source": peak_kind, "alg_bytes_per_launch": int(alg),
+            "avg_launch_ms": round(avg_ms, 4),
+            "traffic": int(NCU_FUSED_LIMIT["dram_bytes_per_cell"] * cells) if name == "fused_limit_update" else None,
+            "traffic_source": "ncu DRAM bytes per cell of this kernel at 384x384x64, scaled by cells"}
+    if name == "fused_limit_update":
+        roof["issue"] = {"inst_per_cell": NCU_FUSED_LIMIT["inst_per_cell"],
+                         "issue_active": NCU_FUSED_LIMIT["issue_active"],
+                         "note": "ncu at 384x384x64: the kernel is bound by instruction issue "
+                                 "(shared-memory loads, selects, address arithmetic), not by DRAM"}
+    roof.update(step_roofs(stages, args.steps, ms, cells, 32, peak,
+                           clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0, sms))
     out = {"value": round(cells / (ms * 1e-3) / 1e9, 4), "unit": UNIT, "ms_per_step": round(ms, 4),
            "speedup_vs_fp64": round(ms64 / ms, 3),
            "linf_rel_err_vs_fp64": linf / bmax, "l2_rel_err_vs_fp64": l2 / bl2,
-           "steps_compared": args.warmup + args.steps,
+           "steps_compared": steps_compared,
            "mass_rel_drift": (m32 - mass0) / mass0,
+           "path": "fused z-marching kernels (TMA-staged tiles)" if fused else "stage kernels",
+           "gpu_launches_per_step": round(launches / args.steps, 2),
+           "roofline": roof, "clocks": clocks,
+           "stages": {k: {"ms_per_step": round(v[0] / args.steps, 4), "launches_per_step": v[1] / args.steps}
+                      for k, v in stages.items() if v[1]},
            "note": "FP32 stencil arithmetic, FP64 Neumaier-compensated mass and norms"}
     arm.ws.close()
     return out
