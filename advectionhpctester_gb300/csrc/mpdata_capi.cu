@@ -4,6 +4,7 @@
 // options, advec.f90:174,203,210).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -615,6 +616,18 @@ struct Batch {
   cudaStream_t cap;             // private stream used only for graph capture
   EventProf* prof;
   cudaStream_t last;
+  // problems on the fused single-precision kernels (FP32 periodic gauge
+  // problems, as single steps take them): one launch per fused kernel for
+  // all of them; the others run on the tile kernels above
+  std::vector<int> fzi;            // index in the fused table, or -1
+  int nfz;
+  std::vector<FusedArgs> fz_args;  // host image of the fused table
+  void* d_fz;
+  void* d_maps;                    // one tensor map per fused problem
+  unsigned long long* d_items_up;  // work items of the upwind+pseudo kernel
+  unsigned long long* d_items;     // ... of the other fused kernels
+  int n_items_up, n_items;
+  int* d_err;
 };
 
 Batch* as_batch(void* p) {
@@ -635,15 +648,17 @@ mpdata_grid grid_of(const Batch* b, int p) {
 int set_shape(Batch* b, int bx, int by, cudaStream_t s) {
   long long total = 0;
   for (int p = 0; p < b->nprob; p++) {
+    if (b->fzi[p] >= 0) continue;  // on the fused kernels
     const mpdata_problem& q = b->pr[p];
     const long long ntx = (q.np + bx - 1) / bx, nty = (q.mp + by - 1) / by;
     if (ntx > 65536 || nty > 65536) return MPDATA_E_DIMS;
     total += ntx * nty * q.lp;
   }
-  if (total < 1 || total > 0x7fffffffLL) return MPDATA_E_TOO_LARGE;
+  if (total > 0x7fffffffLL) return MPDATA_E_TOO_LARGE;
   std::vector<unsigned long long> list;
   list.reserve((size_t)total);
   for (int p = 0; p < b->nprob; p++) {
+    if (b->fzi[p] >= 0) continue;
     const mpdata_problem& q = b->pr[p];
     const int ntx = (q.np + bx - 1) / bx, nty = (q.mp + by - 1) / by;
     for (int k = 0; k < q.lp; k++)
@@ -652,15 +667,15 @@ int set_shape(Batch* b, int bx, int by, cudaStream_t s) {
           list.push_back((unsigned long long)p | ((unsigned long long)tx << 16) |
                          ((unsigned long long)ty << 32) | ((unsigned long long)k << 48));
   }
-  if (list.size() > b->tiles_cap) {
+  if (!list.empty() && list.size() > b->tiles_cap) {
     if (b->d_tiles && cudaFree(b->d_tiles) != cudaSuccess) return MPDATA_E_CUDA;
     b->d_tiles = nullptr;
     b->tiles_cap = 0;
     if (cudaMalloc(&b->d_tiles, list.size() * sizeof(unsigned long long)) != cudaSuccess) return MPDATA_E_CUDA;
     b->tiles_cap = list.size();
   }
-  if (cudaMemcpyAsync(b->d_tiles, list.data(), list.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice,
-                      s) != cudaSuccess)
+  if (!list.empty() && cudaMemcpyAsync(b->d_tiles, list.data(), list.size() * sizeof(unsigned long long),
+                                       cudaMemcpyHostToDevice, s) != cudaSuccess)
     return MPDATA_E_CUDA;
   if (cudaStreamSynchronize(s) != cudaSuccess) return MPDATA_E_CUDA;  // list is a local buffer
   b->bx = bx;
@@ -682,6 +697,12 @@ int upload_table(Batch* b, cudaStream_t s) {
   memcpy(b->h_stage, b->table.data(), b->table.size());
   if (cudaMemcpyAsync(b->d_table, b->h_stage, b->table.size(), cudaMemcpyHostToDevice, s) != cudaSuccess)
     return MPDATA_E_CUDA;
+  if (b->nfz) {
+    const size_t fb = b->fz_args.size() * sizeof(FusedArgs);
+    memcpy(b->h_stage + b->table.size(), b->fz_args.data(), fb);
+    if (cudaMemcpyAsync(b->d_fz, b->h_stage + b->table.size(), fb, cudaMemcpyHostToDevice, s) != cudaSuccess)
+      return MPDATA_E_CUDA;
+  }
   if (cudaEventRecord(b->upload_done, s) != cudaSuccess) return MPDATA_E_CUDA;
   b->dirty = false;
   return MPDATA_OK;
@@ -704,9 +725,19 @@ BatchLaunch<R> launch_of(const Batch* b, int halo) {
   return L;
 }
 
+// halo = 0 (the autotuner's steps write scratch only): the fused kernels,
+// whose last pass writes psi, do not run
 int batch_run(Batch* b, int halo, Prof* prof, cudaStream_t s) {
-  if (b->precision == 64) return run_batch<double>(launch_of<double>(b, halo), prof, s) ? MPDATA_E_CUDA : MPDATA_OK;
-  return run_batch<float>(launch_of<float>(b, halo), prof, s) ? MPDATA_E_CUDA : MPDATA_OK;
+  if (b->ntiles > 0) {
+    const int rc = b->precision == 64 ? run_batch<double>(launch_of<double>(b, halo), prof, s)
+                                      : run_batch<float>(launch_of<float>(b, halo), prof, s);
+    if (rc) return MPDATA_E_CUDA;
+  }
+  if (halo && b->nfz &&
+      run_batch_fused(static_cast<const FusedArgs*>(b->d_fz), static_cast<const CUtensorMap*>(b->d_maps),
+                      b->d_items_up, b->n_items_up, b->d_items, b->n_items, b->iord, prof, s))
+    return MPDATA_E_CUDA;
+  return MPDATA_OK;
 }
 
 template <class R>
@@ -727,6 +758,26 @@ void write_prob(Batch* b, int p, void* psi, const void* u1, const void* u2, cons
   if (P.gv & 2)
     for (int s = 0; s < NGVS; s++) P.gvs[s] = scratch_view<R>(gbase + (size_t)s * b->ncell[p], P.g);
   memcpy(b->table.data() + (size_t)p * sizeof(Prob<R>), &P, sizeof P);
+  if constexpr (sizeof(R) == 4) {
+    const int f = b->fzi[p];
+    if (f >= 0) {
+      FusedPlan F;
+      F.g = P.g;
+      F.psi = P.psi;
+      F.u1 = P.u1;
+      F.u2 = P.u2;
+      F.u3 = P.u3;
+      F.h = P.h;
+      F.rhr = P.rhr;
+      F.arena = base + b->foff[p];
+      fused_arena_elems(P.g, &F.px);
+      F.fs = (long)F.px * P.g.mp * P.g.lp;
+      F.kchunk = fused_kchunk(P.g);
+      F.err = b->d_err;
+      F.tmap = nullptr;
+      b->fz_args[f] = fused_args(F);
+    }
+  }
 }
 
 // tuned block shapes per (precision, iord, nonos, cells), shared by batches
@@ -768,6 +819,12 @@ int mpdata_batch_create(int nprob, const mpdata_problem* probs, int ih, int iord
   b->voff.resize(nprob);
   b->ncell.resize(nprob);
   b->given.assign(nprob, 0);
+  b->fzi.assign(nprob, -1);
+  b->nfz = 0;
+  b->d_fz = b->d_maps = nullptr;
+  b->d_items_up = b->d_items = nullptr;
+  b->n_items_up = b->n_items = 0;
+  b->d_err = nullptr;
   size_t off = 0;
   for (int p = 0; p < nprob; p++) {
     const mpdata_problem& q = probs[p];
@@ -776,9 +833,12 @@ int mpdata_batch_create(int nprob, const mpdata_problem* probs, int ih, int iord
     rc = check_grid(&g);
     if (rc) { delete b; return rc; }
     b->ncell[p] = (size_t)q.np * q.mp * q.lp;
+    if (fused_eligible(geo_of(g), precision, q.gauge, nonos, iord, 0)) b->fzi[p] = b->nfz++;
+    // a velocity group is shared within the fused problems or within the others
     int own = p;
     for (int r = 0; r < p; r++)
-      if (probs[r].velocity_group == q.velocity_group && b->owner[r] == r) { own = r; break; }
+      if (probs[r].velocity_group == q.velocity_group && b->owner[r] == r &&
+          (b->fzi[r] >= 0) == (b->fzi[p] >= 0)) { own = r; break; }
     if (own != p) {  // sharing a velocity needs the same grid and boundaries
       const mpdata_problem& o2 = probs[own];
       if (o2.np != q.np || o2.mp != q.mp || o2.lp != q.lp || o2.ibcx != q.ibcx || o2.ibcy != q.ibcy ||
@@ -786,7 +846,9 @@ int mpdata_batch_create(int nprob, const mpdata_problem* probs, int ih, int iord
     }
     b->owner[p] = own;
     b->foff[p] = off;
-    off += (size_t)NFIELD * b->ncell[p];
+    size_t nf = (size_t)NFIELD * b->ncell[p];
+    if (b->fzi[p] >= 0) nf = std::max(nf, fused_arena_elems(geo_of(g), nullptr));
+    off += (nf + 63) / 64 * 64;  // 256-byte aligned regions (TMA wants 16)
   }
   // a group of two or more fields shares the velocity-only terms of its
   // first-pass pseudo-velocities, for each form among its fields (velgroup_body)
@@ -809,6 +871,7 @@ int mpdata_batch_create(int nprob, const mpdata_problem* probs, int ih, int iord
     }
   for (int p = 0; p < nprob; p++) b->voff[p] = b->voff[b->owner[p]];
   b->table.assign((size_t)nprob * b->pbytes, 0);
+  b->fz_args.assign(b->nfz, FusedArgs{});
   b->mem = b->d_table = nullptr;
   b->h_stage = nullptr;
   b->d_tiles = nullptr;
@@ -823,10 +886,38 @@ int mpdata_batch_create(int nprob, const mpdata_problem* probs, int ih, int iord
   b->dirty = true;
   bool ok = cudaMalloc(&b->mem, off * b->elem) == cudaSuccess &&
             cudaMalloc(&b->d_table, b->table.size()) == cudaSuccess &&
-            cudaMallocHost(&b->h_stage, b->table.size()) == cudaSuccess &&
+            cudaMallocHost(&b->h_stage, b->table.size() + b->nfz * sizeof(FusedArgs)) == cudaSuccess &&
             cudaEventCreateWithFlags(&b->upload_done, cudaEventDisableTiming) == cudaSuccess &&
             cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking) == cudaSuccess;
   b->magic = BATCH_MAGIC;
+  if (ok && b->nfz) {
+    // fused problems: argument table, tensor maps of their arenas, work items
+    std::vector<CUtensorMap> maps(b->nfz);
+    std::vector<unsigned long long> up, rest;
+    for (int p = 0; p < nprob && ok; p++) {
+      const int f = b->fzi[p];
+      if (f < 0) continue;
+      const Geo g = geo_of(grid_of(b, p));
+      int px = 0;
+      fused_arena_elems(g, &px);
+      ok = fused_make_tmap(&maps[f], static_cast<float*>(b->mem) + b->foff[p], px, g) == 0;
+      fused_items(g, fused_kchunk(g), f, up, rest);
+    }
+    ok = ok && up.size() < 0x7fffffffu && rest.size() < 0x7fffffffu && fused_init() == 0 &&
+         cudaMalloc(&b->d_fz, b->nfz * sizeof(FusedArgs)) == cudaSuccess &&
+         cudaMalloc(&b->d_maps, b->nfz * sizeof(CUtensorMap)) == cudaSuccess &&
+         cudaMalloc(&b->d_items_up, up.size() * sizeof(unsigned long long)) == cudaSuccess &&
+         cudaMalloc(&b->d_items, rest.size() * sizeof(unsigned long long)) == cudaSuccess &&
+         cudaMalloc(&b->d_err, sizeof(int)) == cudaSuccess && cudaMemset(b->d_err, 0, sizeof(int)) == cudaSuccess &&
+         cudaMemcpy(b->d_maps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice) ==
+             cudaSuccess &&
+         cudaMemcpy(b->d_items_up, up.data(), up.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice) ==
+             cudaSuccess &&
+         cudaMemcpy(b->d_items, rest.data(), rest.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice) ==
+             cudaSuccess;
+    b->n_items_up = (int)up.size();
+    b->n_items = (int)rest.size();
+  }
   if (ok) {
     // default shape, or the tuned one for this batch signature
     int bx = 32, by = 4;
@@ -859,6 +950,11 @@ int mpdata_batch_destroy(void* batch) {
   cudaFreeHost(b->h_stage);
   cudaFree(b->d_tiles);
   cudaFree(b->d_table);
+  cudaFree(b->d_fz);
+  cudaFree(b->d_maps);
+  cudaFree(b->d_items_up);
+  cudaFree(b->d_items);
+  cudaFree(b->d_err);
   cudaError_t e = cudaFree(b->mem);
   delete b;
   return e == cudaSuccess ? MPDATA_OK : MPDATA_E_CUDA;
@@ -919,6 +1015,11 @@ int mpdata_batch_tune(void* batch, void* stream, int* bx_out, int* by_out) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   int rc = upload_table(b, s);
   if (rc) return rc;
+  if (b->ntiles == 0) {  // every problem runs on the fused kernels: no tile shape to choose
+    if (bx_out) *bx_out = b->bx;
+    if (by_out) *by_out = b->by;
+    return MPDATA_OK;
+  }
   static const int shapes[][2] = {{32, 4}, {32, 8}, {64, 2}, {64, 4}, {128, 1}, {128, 2}, {16, 8}};
   cudaEvent_t e0, e1;
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return MPDATA_E_CUDA;

@@ -126,16 +126,21 @@ __device__ __forceinline__ float* smem_base() {
   return reinterpret_cast<float*>(smem_raw + ((128u - (off & 127u)) & 127u));
 }
 
-struct FzArgs {
-  Geo g;
-  Arr<float> psi, u1, u2, u3, h, rhr;
-  float* arena;
-  int px;
-  long fs;
-  int kchunk;
-  int fin, fout;                      // pass input / output field
-  int fmx_in, fmn_in, fmx_out, fmn_out;
-  int* err;
+typedef FusedArgs FzArgs;
+
+// The fields of one pass: which arena fields hold its input field, its
+// output field and the running extrema it reads and writes (the same for
+// every problem of a batch).
+struct FzPass {
+  int fin, fout, fmx_in, fmn_in, fmx_out, fmn_out;
+  __device__ __forceinline__ void apply(FzArgs& a) const {
+    a.fin = fin;
+    a.fout = fout;
+    a.fmx_in = fmx_in;
+    a.fmn_in = fmn_in;
+    a.fmx_out = fmx_out;
+    a.fmn_out = fmn_out;
+  }
 };
 
 // The two staged cells of thread t: box cells t and t+NT (the second exists
@@ -345,8 +350,14 @@ __device__ __forceinline__ void bounds_cell(int b, const float* xm, const float*
 // smem planes: psi 4, u1 4, u2 4, u3 4, h 4, rhr 2, xant 4
 constexpr int K1_PLANES = 26;
 
+// Each kernel is a device body over one work item (tile bxi, byi of the
+// problem's grid, z chunk bzi) and two entry points: a grid over one
+// problem's tiles and chunks (arguments as kernel parameters), and a grid
+// over a batch's work list (one packed item per block: problem in bits 0-15,
+// bxi 16-31, byi 32-47, bzi 48-63), whose block stages its problem's
+// arguments in shared memory.
 template <int TY>
-__global__ void __launch_bounds__(Tl<TY>::NT, Tl<TY>::MINB) k_fz_upwind_pseudo(const FzArgs A) {
+__device__ __forceinline__ void body_upwind_pseudo(const FzArgs& A, int bxi, int byi, int bzi) {
   constexpr int NT = Tl<TY>::NT, PLANE = Tl<TY>::PLANE, NRING1 = Tl<TY>::NRING1;
   float* const sm = smem_base();
   float* const PSI = sm;
@@ -358,8 +369,8 @@ __global__ void __launch_bounds__(Tl<TY>::NT, Tl<TY>::MINB) k_fz_upwind_pseudo(c
   float* const XA = RH + 2 * PLANE;
   const Geo& g = A.g;
   const int t = threadIdx.x, tx = t % TX, ty = t / TX;
-  const int x0 = blockIdx.x * TX + 1, y0 = blockIdx.y * TY + 1;
-  const int kb = blockIdx.z * A.kchunk + 1;
+  const int x0 = bxi * TX + 1, y0 = byi * TY + 1;
+  const int kb = bzi * A.kchunk + 1;
   if (kb > g.lp) return;
   const int ke = min(g.lp, kb + A.kchunk - 1);
   const Box bx = box_cells<TY>(g, x0, y0, t);
@@ -461,6 +472,30 @@ __global__ void __launch_bounds__(Tl<TY>::NT, Tl<TY>::MINB) k_fz_upwind_pseudo(c
   }
 }
 
+template <int TY>
+__global__ void __launch_bounds__(Tl<TY>::NT, Tl<TY>::MINB) k_fz_upwind_pseudo(const FzArgs A) {
+  body_upwind_pseudo<TY>(A, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// One work item of a batch.
+struct Item {
+  int p, bxi, byi, bzi;
+};
+__device__ __forceinline__ Item item_of(const unsigned long long* items) {
+  const unsigned long long w = items[blockIdx.x];
+  return Item{(int)(w & 0xffffu), (int)((w >> 16) & 0xffffu), (int)((w >> 32) & 0xffffu), (int)(w >> 48)};
+}
+
+template <int TY>
+__global__ void __launch_bounds__(Tl<TY>::NT, Tl<TY>::MINB)
+    kb_fz_upwind_pseudo(const FzArgs* __restrict__ probs, const unsigned long long* __restrict__ items) {
+  __shared__ FzArgs sa;
+  const Item it = item_of(items);
+  if (threadIdx.x == 0) sa = probs[it.p];
+  __syncthreads();
+  body_upwind_pseudo<TY>(sa, it.bxi, it.byi, it.bzi);
+}
+
 // ---- staging of arena fields: TMA on interior tiles, wrapped cp.async else ----
 template <int NT>
 struct Stager {
@@ -484,9 +519,8 @@ struct Stager {
 
 // Interior tile: every staged box lies inside the grid, so TMA needs no wrap.
 template <int TY>
-__device__ __forceinline__ bool tile_inside(const Geo& g) {
-  return blockIdx.x >= 1 && (int)blockIdx.x * TX + TX + HX <= g.np && blockIdx.y >= 1 &&
-         (int)blockIdx.y * TY + TY + HY <= g.mp;
+__device__ __forceinline__ bool tile_inside(const Geo& g, int bxi, int byi) {
+  return bxi >= 1 && bxi * TX + TX + HX <= g.np && byi >= 1 && byi * TY + TY + HY <= g.mp;
 }
 
 // Waits for the TMA phase of the previous iteration (bounded); false when the
@@ -507,8 +541,7 @@ constexpr int K2_PLANES = 26;
 constexpr int K2_TILES = 4;
 
 template <int TY, bool FIRST, bool LAST, bool KEEP>
-__global__ void __launch_bounds__(Tl<TY>::NT, Tl<TY>::MINB)
-    k_fz_limit(const FzArgs A, const __grid_constant__ CUtensorMap tm) {
+__device__ __forceinline__ void body_limit(const FzArgs& A, const CUtensorMap* tm, int bxi, int byi, int bzi) {
   constexpr int NT = Tl<TY>::NT, PLANE = Tl<TY>::PLANE, NRING1 = Tl<TY>::NRING1, NRINGW = Tl<TY>::NRINGW;
   constexpr uint32_t BOX_BYTES = Tl<TY>::BOX_BYTES;
   float* const sm = smem_base();
@@ -528,15 +561,15 @@ __global__ void __launch_bounds__(Tl<TY>::NT, Tl<TY>::MINB)
   __shared__ int s_abort;
   const Geo& g = A.g;
   const int t = threadIdx.x, tx = t % TX, ty = t / TX;
-  const int x0 = blockIdx.x * TX + 1, y0 = blockIdx.y * TY + 1;
-  const int kb = blockIdx.z * A.kchunk + 1;
+  const int x0 = bxi * TX + 1, y0 = byi * TY + 1;
+  const int kb = bzi * A.kchunk + 1;
   if (kb > g.lp) return;
   const int ke = min(g.lp, kb + A.kchunk - 1);
-  const bool tma = tile_inside<TY>(g);
+  const bool tma = tile_inside<TY>(g, bxi, byi);
   const Box bx = box_cells<TY>(g, x0, y0, t);
   const bool two = bx.two;
   const long pl = (long)A.px * g.mp;
-  const Stager<NT> st{&tm, A.arena, A.fs, pl, x0 - 1 - HX, y0 - 1 - HY, tma, two, box_offs(bx, A.px), t};
+  const Stager<NT> st{tm, A.arena, A.fs, pl, x0 - 1 - HX, y0 - 1 - HY, tma, two, box_offs(bx, A.px), t};
   const Offs oh = box_offs(bx, A.h.sy);
   const int b = (ty + HY) * P + tx + HX;
   const int br = t < NRING1 ? ring1_index<TY>(t) : -1;
@@ -724,8 +757,7 @@ __global__ void __launch_bounds__(Tl<TY>::NT, Tl<TY>::MINB)
 constexpr int K3_PLANES = 20;
 
 template <int TY>
-__global__ void __launch_bounds__(Tl<TY>::NT, Tl<TY>::MINB)
-    k_fz_pseudo(const FzArgs A, const __grid_constant__ CUtensorMap tm) {
+__device__ __forceinline__ void body_pseudo(const FzArgs& A, const CUtensorMap* tm, int bxi, int byi, int bzi) {
   constexpr int NT = Tl<TY>::NT, PLANE = Tl<TY>::PLANE;
   constexpr uint32_t BOX_BYTES = Tl<TY>::BOX_BYTES;
   float* const sm = smem_base();
@@ -738,15 +770,15 @@ __global__ void __launch_bounds__(Tl<TY>::NT, Tl<TY>::MINB)
   __shared__ int s_abort;
   const Geo& g = A.g;
   const int t = threadIdx.x, tx = t % TX, ty = t / TX;
-  const int x0 = blockIdx.x * TX + 1, y0 = blockIdx.y * TY + 1;
-  const int kb = blockIdx.z * A.kchunk + 1;
+  const int x0 = bxi * TX + 1, y0 = byi * TY + 1;
+  const int kb = bzi * A.kchunk + 1;
   if (kb > g.lp) return;
   const int ke = min(g.lp, kb + A.kchunk - 1);
-  const bool tma = tile_inside<TY>(g);
+  const bool tma = tile_inside<TY>(g, bxi, byi);
   const Box bx = box_cells<TY>(g, x0, y0, t);
   const bool two = bx.two;
   const long pl = (long)A.px * g.mp;
-  const Stager<NT> st{&tm, A.arena, A.fs, pl, x0 - 1 - HX, y0 - 1 - HY, tma, two, box_offs(bx, A.px), t};
+  const Stager<NT> st{tm, A.arena, A.fs, pl, x0 - 1 - HX, y0 - 1 - HY, tma, two, box_offs(bx, A.px), t};
   const Offs oh = box_offs(bx, A.h.sy);
   const int b = (ty + HY) * P + tx + HX;
   const int ig = x0 + tx, jg = y0 + ty;
@@ -818,6 +850,43 @@ __global__ void __launch_bounds__(Tl<TY>::NT, Tl<TY>::MINB)
 #undef S2
 }
 
+template <int TY, bool FIRST, bool LAST, bool KEEP>
+__global__ void __launch_bounds__(Tl<TY>::NT, Tl<TY>::MINB)
+    k_fz_limit(const FzArgs A, const __grid_constant__ CUtensorMap tm) {
+  body_limit<TY, FIRST, LAST, KEEP>(A, &tm, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+template <int TY, bool FIRST, bool LAST, bool KEEP>
+__global__ void __launch_bounds__(Tl<TY>::NT, Tl<TY>::MINB)
+    kb_fz_limit(const FzArgs* __restrict__ probs, const CUtensorMap* __restrict__ maps,
+                const unsigned long long* __restrict__ items, FzPass pass) {
+  __shared__ FzArgs sa;
+  const Item it = item_of(items);
+  if (threadIdx.x == 0) {
+    sa = probs[it.p];
+    pass.apply(sa);
+  }
+  __syncthreads();
+  body_limit<TY, FIRST, LAST, KEEP>(sa, maps + it.p, it.bxi, it.byi, it.bzi);
+}
+template <int TY>
+__global__ void __launch_bounds__(Tl<TY>::NT, Tl<TY>::MINB)
+    k_fz_pseudo(const FzArgs A, const __grid_constant__ CUtensorMap tm) {
+  body_pseudo<TY>(A, &tm, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+template <int TY>
+__global__ void __launch_bounds__(Tl<TY>::NT, Tl<TY>::MINB)
+    kb_fz_pseudo(const FzArgs* __restrict__ probs, const CUtensorMap* __restrict__ maps,
+                 const unsigned long long* __restrict__ items, FzPass pass) {
+  __shared__ FzArgs sa;
+  const Item it = item_of(items);
+  if (threadIdx.x == 0) {
+    sa = probs[it.p];
+    pass.apply(sa);
+  }
+  __syncthreads();
+  body_pseudo<TY>(sa, maps + it.p, it.bxi, it.byi, it.bzi);
+}
+
 constexpr size_t K1_SMEM = (size_t)K1_PLANES * Tl<TY_UP>::PLANE * 4 + 128;
 constexpr size_t K2_SMEM = (size_t)K2_PLANES * Tl<TY2>::PLANE * 4 + (size_t)K2_TILES * Tl<TY2>::NT * 4 + 128;
 constexpr size_t K3_SMEM = (size_t)K3_PLANES * Tl<TY2>::PLANE * 4 + 128;
@@ -831,6 +900,12 @@ int set_smem(K kernel, size_t bytes) {
 int init_kernels() {
   static int rc = [] {
     int r = 0;
+    r |= set_smem(kb_fz_upwind_pseudo<TY_UP>, K1_SMEM);
+    r |= set_smem(kb_fz_limit<TY2, true, true, false>, K2_SMEM);
+    r |= set_smem(kb_fz_limit<TY2, true, false, true>, K2_SMEM);
+    r |= set_smem(kb_fz_limit<TY2, false, false, true>, K2_SMEM);
+    r |= set_smem(kb_fz_limit<TY2, false, true, true>, K2_SMEM);
+    r |= set_smem(kb_fz_pseudo<TY2>, K3_SMEM);
     r |= set_smem(k_fz_upwind_pseudo<TY_UP>, K1_SMEM);
     r |= set_smem(k_fz_limit<TY2, true, true, false>, K2_SMEM);
     r |= set_smem(k_fz_limit<TY2, true, false, true>, K2_SMEM);
@@ -907,11 +982,9 @@ int fused_kchunk(const Geo& g) {
     add_launches(1);                       \
   } while (0)
 
-int run_step_fused(const FusedPlan& F, int iord, Prof* prof, cudaStream_t s, int* mx_field, int* mn_field) {
-  if (init_kernels()) return -5;
-  const Geo& g = F.g;
+FusedArgs fused_args(const FusedPlan& F) {
   FzArgs A;
-  A.g = g;
+  A.g = F.g;
   A.psi = F.psi;
   A.u1 = F.u1;
   A.u2 = F.u2;
@@ -923,12 +996,71 @@ int run_step_fused(const FusedPlan& F, int iord, Prof* prof, cudaStream_t s, int
   A.fs = F.fs;
   A.kchunk = F.kchunk;
   A.err = F.err;
-  A.fin = FZ_X0;
+  A.fin = FZ_X0;  // the first pass reads the upwind field and writes X1
   A.fout = FZ_X1;
   A.fmx_in = FZ_MX0;
   A.fmn_in = FZ_MN0;
   A.fmx_out = FZ_MX0;
   A.fmn_out = FZ_MN0;
+  return A;
+}
+
+int fused_init() { return init_kernels(); }
+
+void fused_items(const Geo& g, int kchunk, int p, std::vector<unsigned long long>& up,
+                 std::vector<unsigned long long>& rest) {
+  const int nz = (g.lp + kchunk - 1) / kchunk;
+  const int ntx = (g.np + TX - 1) / TX;
+  const int nty1 = (g.mp + TY_UP - 1) / TY_UP, nty2 = (g.mp + TY2 - 1) / TY2;
+  for (int z = 0; z < nz; z++) {
+    for (int y = 0; y < nty1; y++)
+      for (int x = 0; x < ntx; x++)
+        up.push_back((unsigned long long)p | ((unsigned long long)x << 16) | ((unsigned long long)y << 32) |
+                     ((unsigned long long)z << 48));
+    for (int y = 0; y < nty2; y++)
+      for (int x = 0; x < ntx; x++)
+        rest.push_back((unsigned long long)p | ((unsigned long long)x << 16) | ((unsigned long long)y << 32) |
+                       ((unsigned long long)z << 48));
+  }
+}
+
+// the arena fields of the next pass: it reads this pass's output field and extrema
+static void next_pass(int& fin, int& fout, int& mxi, int& mni, int& mxo, int& mno) {
+  fin = fout;
+  fout = fout == FZ_X1 ? FZ_X0 : FZ_X1;
+  mxi = mxo;
+  mni = mno;
+  mxo = mxo == FZ_MX0 ? FZ_MX1 : FZ_MX0;
+  mno = mno == FZ_MN0 ? FZ_MN1 : FZ_MN0;
+}
+
+int run_batch_fused(const FusedArgs* probs, const CUtensorMap* maps, const unsigned long long* items_up, int n_up,
+                    const unsigned long long* items, int n, int iord, Prof* prof, cudaStream_t s) {
+  if (init_kernels()) return -5;
+  if (n_up < 1 || n < 1) return 0;
+  const dim3 blk1(Tl<TY_UP>::NT), blk(Tl<TY2>::NT);
+  FZ_LAUNCH(ST_FZ_UPWIND_PSEUDO, (kb_fz_upwind_pseudo<TY_UP><<<n_up, blk1, K1_SMEM, s>>>(probs, items_up)));
+  FzPass ps{FZ_X0, FZ_X1, FZ_MX0, FZ_MN0, FZ_MX0, FZ_MN0};
+  for (int pass = 2; pass <= iord; pass++) {
+    const bool first = pass == 2, last = pass == iord;
+    if (!first) FZ_LAUNCH(ST_FZ_PSEUDO, (kb_fz_pseudo<TY2><<<n, blk, K3_SMEM, s>>>(probs, maps, items, ps)));
+    if (first && last)
+      FZ_LAUNCH(ST_FZ_LIMIT, (kb_fz_limit<TY2, true, true, false><<<n, blk, K2_SMEM, s>>>(probs, maps, items, ps)));
+    else if (first)
+      FZ_LAUNCH(ST_FZ_LIMIT, (kb_fz_limit<TY2, true, false, true><<<n, blk, K2_SMEM, s>>>(probs, maps, items, ps)));
+    else if (!last)
+      FZ_LAUNCH(ST_FZ_LIMIT, (kb_fz_limit<TY2, false, false, true><<<n, blk, K2_SMEM, s>>>(probs, maps, items, ps)));
+    else
+      FZ_LAUNCH(ST_FZ_LIMIT, (kb_fz_limit<TY2, false, true, true><<<n, blk, K2_SMEM, s>>>(probs, maps, items, ps)));
+    next_pass(ps.fin, ps.fout, ps.fmx_in, ps.fmn_in, ps.fmx_out, ps.fmn_out);
+  }
+  return cudaGetLastError() == cudaSuccess ? 0 : -5;
+}
+
+int run_step_fused(const FusedPlan& F, int iord, Prof* prof, cudaStream_t s, int* mx_field, int* mn_field) {
+  if (init_kernels()) return -5;
+  const Geo& g = F.g;
+  FzArgs A = fused_args(F);
   const int nz = (g.lp + F.kchunk - 1) / F.kchunk;
   const dim3 grid1((g.np + TX - 1) / TX, (g.mp + TY_UP - 1) / TY_UP, nz), blk1(Tl<TY_UP>::NT);
   const dim3 grid((g.np + TX - 1) / TX, (g.mp + TY2 - 1) / TY2, nz), blk(Tl<TY2>::NT);

@@ -2,6 +2,8 @@
 #pragma once
 #include <cuda.h>
 
+#include <vector>
+
 #include "mpdata_stages.cuh"
 
 namespace mpdata {
@@ -13,6 +15,20 @@ namespace mpdata {
 // extrema.
 enum FusedField { FZ_XIN = 0, FZ_X0, FZ_X1, FZ_V1, FZ_V2, FZ_V3, FZ_W1, FZ_W2, FZ_W3, FZ_MX0, FZ_MN0, FZ_MX1,
                   FZ_MN1, FZ_NF };
+
+// Arguments of the fused kernels for one problem: caller arrays, the arena,
+// the z-march chunk, and the arena fields of the current pass.
+struct FusedArgs {
+  Geo g;
+  Arr<float> psi, u1, u2, u3, h, rhr;
+  float* arena;
+  int px;
+  long fs;
+  int kchunk;
+  int fin, fout;                      // pass input / output field
+  int fmx_in, fmn_in, fmx_out, fmn_out;
+  int* err;
+};
 
 struct FusedPlan {
   Geo g;
@@ -37,5 +53,18 @@ int fused_kchunk(const Geo& g);
 // One step; on return *mx_field / *mn_field name the arena fields that hold
 // the running extrema of the step (-1 when iord = 2 keeps none).
 int run_step_fused(const FusedPlan& F, int iord, Prof* prof, cudaStream_t s, int* mx_field, int* mn_field);
+
+// Batches.  Each problem of the fused table gets work items (a tile of the
+// upwind+pseudo kernel's height, or of the other kernels' height, and a z
+// chunk) packed as problem | tile x << 16 | tile y << 32 | chunk << 48; one
+// launch per fused kernel then covers every problem.
+FusedArgs fused_args(const FusedPlan& F);
+void fused_items(const Geo& g, int kchunk, int p, std::vector<unsigned long long>& up,
+                 std::vector<unsigned long long>& rest);
+int fused_init();
+// One step of every problem of the table (device arrays: args, tensor maps,
+// the two item lists).
+int run_batch_fused(const FusedArgs* probs, const CUtensorMap* maps, const unsigned long long* items_up, int n_up,
+                    const unsigned long long* items, int n, int iord, Prof* prof, cudaStream_t s);
 
 }  // namespace mpdata

@@ -172,3 +172,74 @@ def test_interior_tiles_velocity_group(M, oracle, shape, density):
         np.testing.assert_array_equal(M.to_numpy(d["x"]), oracle_steps(oracle, f, forms[p], 3, 3),
                                       err_msg="tracer %d" % p)
     b.close()
+
+
+def dev32(M, f):
+    return {k: M.fortran_device(getattr(f, k), dtype=np.float32) for k in
+            ("x", "u1", "u2", "u3", "h", "rhr", "bcx", "bcy")}
+
+
+@pytest.mark.parametrize("iord", [2, 3])
+def test_fp32_batch_fused_and_tile_problems(M, oracle, iord):
+    """FP32: periodic gauge problems of uneven sizes (and a velocity group of
+    three tracers) run on the fused kernels, one launch per kernel for all of
+    them; walls and the standard form run on the tile kernels of the same
+    batch.  Tuning leaves every psi untouched; graph replay and eager steps
+    give each problem the FP32 oracle's bits."""
+    import torch
+    specs = [((200, 40, 12), (1, 1, 1), 1, None), ((37, 23, 9), (1, 1, 1), 1, None),
+             ((5, 3, 2), (1, 1, 1), 1, None), ((72, 48, 10), (1, 1, 1), 1, 4), ((72, 48, 10), (1, 1, 1), 1, 4),
+             ((72, 48, 10), (1, 1, 1), 1, 4), ((24, 20, 6), (0, 0, 0), 1, None), ((30, 16, 5), (1, 1, 1), 0, None),
+             ((40, 12, 6), (1, 0, 1), 1, None)]
+    fs = []
+    for q, (n, ibc, g, grp) in enumerate(specs):
+        seed = 400 if grp is not None else 300 + q
+        f = W.random_fields(*n, ibc=ibc, seed=seed, courant=0.3, dtype=np.float32)
+        if grp is not None:  # tracers of one velocity: own psi, shared u, h, rhr
+            f.x[...] = np.random.default_rng(500 + q).uniform(0.5, 1.5, f.x.shape).astype(np.float32)
+        fs.append(f)
+    probs = [dict(np=n[0], mp=n[1], lp=n[2], ibcx=ibc[0], ibcy=ibc[1], ibcz=ibc[2], gauge=g,
+                  velocity_group=grp if grp is not None else 100 + q)
+             for q, (n, ibc, g, grp) in enumerate(specs)]
+    b = M.Batch(probs, iord=iord, nonos=1, precision=32)
+    ds = [dev32(M, f) for f in fs]
+    shared = ds[3]
+    for p, d in enumerate(ds):
+        v = shared if specs[p][3] is not None else d
+        b.set(p, d["x"], v["u1"], v["u2"], v["u3"], v["h"], v["rhr"], d["bcx"], d["bcy"])
+    before = [d["x"].clone() for d in ds]
+    b.tune()
+    for d, x0 in zip(ds, before):
+        assert torch.equal(d["x"], x0)
+    b.step()
+    b.graph(True)
+    b.step()
+    b.step()
+    torch.cuda.synchronize()
+    for p, (f, d) in enumerate(zip(fs, ds)):
+        g = f if specs[p][3] is None else fs[3]
+        ref = f.copy()
+        for k in ("u1", "u2", "u3", "h", "rhr"):
+            getattr(ref, k)[...] = getattr(g, k)
+        want = oracle_steps(oracle, ref, specs[p][2], iord, 3)
+        np.testing.assert_array_equal(W.interior(M.to_numpy(d["x"])), W.interior(want), err_msg="problem %d" % p)
+    b.close()
+
+
+def test_fp32_batch_all_fused_launches(M, oracle):
+    """A batch whose problems all take the fused kernels launches each fused
+    kernel once per pass for all of them (iord=3: four launches a step)."""
+    specs = [(64, 32, 16), (32, 32, 32), (96, 24, 8)]
+    fs = [W.random_fields(*n, ibc=(1, 1, 1), seed=600 + q, courant=0.3, dtype=np.float32)
+          for q, n in enumerate(specs)]
+    b = M.Batch([dict(np=n[0], mp=n[1], lp=n[2]) for n in specs], iord=3, nonos=1, precision=32)
+    ds = [dev32(M, f) for f in fs]
+    for p, d in enumerate(ds):
+        b.set(p, d["x"], d["u1"], d["u2"], d["u3"], d["h"], d["rhr"])
+    l0 = M.launch_count()
+    b.step()
+    assert M.launch_count() - l0 == 4
+    b.step()
+    for p, (f, d) in enumerate(zip(fs, ds)):
+        np.testing.assert_array_equal(W.interior(M.to_numpy(d["x"])), W.interior(oracle_steps(oracle, f, 1, 3, 2)))
+    b.close()
