@@ -328,6 +328,7 @@ int advec_dwarf_impl(int legacyoptmode, int t_adv, int lvertsplit, int np, int m
 
 namespace mpdata {
 int grid_ok(const mpdata_grid* g) { return check_grid(g); }
+int opts_ok(const mpdata_opts* o) { return check_opts(o); }
 }  // namespace mpdata
 
 namespace {
@@ -570,7 +571,9 @@ const char* mpdata_strerror(int code) {
     case MPDATA_E_CUDA: return "CUDA runtime error";
     case MPDATA_E_DEVICE: return "device error word set (non-finite value)";
     case MPDATA_E_UNSUPPORTED: return "reference option outside this library's scope";
-    case MPDATA_E_TOO_LARGE: return "grid exceeds the 32768-cell scratch of mpdata_step_noalloc_f64";
+    case MPDATA_E_TOO_LARGE:
+      return "problem exceeds a fixed size limit (the 32768-cell scratch of mpdata_step_noalloc_f64, "
+             "2^31 batch tiles, or a 4 GiB netCDF classic slab)";
     case MPDATA_E_COURANT: return "Courant control failed: above the fatal limit while substepping, or not finite";
     case MPDATA_E_IO: return "field file missing, unreadable, not netCDF classic, or without the variable";
     default: return "unknown error";

@@ -14,8 +14,9 @@
 //  - every GPU that loads the library holds the array (19 * 32768 doubles,
 //    about 5 MB) until the process exits;
 //  - the first call on a device looks up the array's device address (with
-//    that device current) and keeps it; make that first call before any
-//    stream capture;
+//    that device current) and keeps it for the life of the process; make
+//    that first call before any stream capture, and make no call on a device
+//    after cudaDeviceReset there (the array may then sit elsewhere);
 //  - all calls share the one array, so calls that overlap on the GPU (on
 //    different streams, or from different host threads) race; order them;
 //  - every scratch value a step reads is written earlier in the same step,
@@ -30,6 +31,11 @@
 #include "mpdata_stages.cuh"
 
 using namespace mpdata;
+
+namespace mpdata {
+int grid_ok(const mpdata_grid* g);  // the workspace path's checks (mpdata_capi.cu)
+int opts_ok(const mpdata_opts* o);
+}
 
 namespace {
 
@@ -71,20 +77,18 @@ extern "C" int mpdata_step_noalloc_f64(const mpdata_grid* grid, const mpdata_opt
                                        const double* u1, const double* u2, const double* u3,
                                        const double* h, const double* rhr, const double* bcx,
                                        const double* bcy, void* stream) {
-  if (!grid || !opts) return MPDATA_E_NULL;
+  // the same checks as a workspace, then this entry point's own limits
+  int rc = grid_ok(grid);
+  if (rc) return rc;
+  rc = opts_ok(opts);
+  if (rc) return rc;
   const mpdata_grid g = *grid;
-  auto flag = [](int v) { return v == 0 || v == 1; };
-  if (!flag(g.ibcx) || !flag(g.ibcy) || !flag(g.ibcz) || g.ih < 1 || g.ih > 8) return MPDATA_E_DIMS;
-  if (g.np < (g.ibcx ? 1 : 2) || g.mp < (g.ibcy ? 1 : 2) || g.lp < (g.ibcz ? 1 : 2)) return MPDATA_E_DIMS;
   if ((long long)g.np * g.mp * g.lp > NOALLOC_CELLS) return MPDATA_E_TOO_LARGE;
-  if (opts->precision != 64 || opts->predictor != 0) return MPDATA_E_OPTS;
-  if (opts->iord < 1 || opts->iord > 8 || (opts->nonos != 0 && opts->nonos != 1) ||
-      (opts->gauge != 0 && opts->gauge != 1))
-    return MPDATA_E_OPTS;
+  if (opts->precision != 64) return MPDATA_E_OPTS;
   if (!psi || !u1 || !u2 || !u3 || !h || !rhr) return MPDATA_E_NULL;
   if ((!g.ibcx && !bcx) || (!g.ibcy && !bcy)) return MPDATA_E_NULL;
   double* scratch = nullptr;
-  int rc = scratch_on_device(&scratch);
+  rc = scratch_on_device(&scratch);
   if (rc) return rc;
 
   const int ih = g.ih, sx = g.np + 2 * ih, sy = g.mp + 2 * ih;

@@ -658,9 +658,45 @@ def run_precision_study(args, n=(768, 768, 160), nsteps=500):
     out["fp32_speedup"] = round(out["fp64_ms_per_step"] / out["fp32_ms_per_step"], 3)
     out["linf_rel_err_fp32_vs_fp64"] = linf / bmax
     out["l2_rel_err_fp32_vs_fp64"] = l2 / bl2
+    # where the L-inf error sits: cells above each threshold, and its share
+    # at the front (largest neighbour jump of the FP64 field above 5% of max)
+    x64 = arms[64].psi[1:-1, 1:-1, 1:-1]
+    err = (arms[32].psi[1:-1, 1:-1, 1:-1].double() - x64).abs()
+    out["cells_over"] = {"%g" % t: int((err > t * bmax).sum().item()) for t in (1e-6, 1e-5)}
+    jump = torch.zeros_like(x64)
+    for d in range(3):
+        for sgn in (1, -1):
+            jump = torch.maximum(jump, (torch.roll(x64, sgn, d) - x64).abs())
+    front = jump > 0.05 * bmax
+    out["linf_rel_err_front"] = err[front].max().item() / bmax
+    out["linf_rel_err_elsewhere"] = err[~front].max().item() / bmax
+    del x64, err, jump, front
     for a in arms.values():
         a.close()
     del arms
+    torch.cuda.empty_cache()
+    # conditioning floor: FP64 arithmetic from the initial field and velocity
+    # patterns rounded once to FP32, against the exact FP64 run
+    ref = DevArm(nx, ny, nz, 64, 2, psi_fn)
+    rnd = DevArm(nx, ny, nz, 64, 2, psi_fn)
+    rnd.psi.copy_(rnd.psi.float().double())
+    for t in rnd.pats:
+        t.copy_(t.float().double())
+    for k in range(nsteps):
+        ref.step(k)
+        rnd.step(k)
+    linf_r, l2_r, bmax_r, bl2_r = M.error_norms(rnd.psi, ref.psi)
+    ref.close()
+    rnd.close()
+    del ref, rnd
+    out["linf_rel_fp64_from_fp32_rounded_input"] = linf_r / bmax_r
+    out["l2_rel_fp64_from_fp32_rounded_input"] = l2_r / bl2_r
+    out["diagnosis"] = ("the L-inf error comes from a few hundred cells beside the noisy front, where the "
+                        "nonoscillatory limiter's branches (min(1,cp,cn), star extrema) switch under "
+                        "perturbations of a few ulps; rounding only the initial data to FP32 and "
+                        "computing in FP64 moves those cells by linf_rel_fp64_from_fp32_rounded_input, "
+                        "so no computation that holds the field in FP32 meets 1e-5 after 500 steps; "
+                        "L2 stays below 1e-6")
     torch.cuda.empty_cache()
     return out
 
@@ -933,18 +969,18 @@ def run_batch_study(args, steps=100):
         torch.cuda.empty_cache()
     # 16 tracers sharing one velocity, in the gauge form and in the standard
     # form (the reference's multi-field step advects its scalars in the latter)
-    rng = np.random.default_rng(16)
-    base = make_domain_device((256, 256, 64), rng, torch.float64)
-    tr = [base["psi"].clone() * (1.0 + 0.01 * k) for k in range(16)]
     tc = 16 * 256 * 256 * 64
-    for gauge, key in ((1, "tracers16_fp64"), (0, "tracers16_std_fp64")):
+    for gauge, key, prec in ((1, "tracers16_fp64", 64), (0, "tracers16_std_fp64", 64), (1, "tracers16_fp32", 32)):
+        rng = np.random.default_rng(16)
+        base = make_domain_device((256, 256, 64), rng, torch.float64 if prec == 64 else torch.float32)
+        tr = [base["psi"].clone() * (1.0 + 0.01 * k) for k in range(16)]
         b = M.Batch([dict(np=256, mp=256, lp=64, gauge=gauge, velocity_group=0)] * 16, iord=2, nonos=1,
-                    precision=64)
+                    precision=prec)
         for p in range(16):
             b.set(p, tr[p], base["u1"], base["u2"], base["u3"], base["h"], base["rhr"])
         b.graph(True)
         ms_b = timed(b.step, steps)
-        w = M.Workspace(256, 256, 64, 1, 1, 1, 1, iord=2, nonos=1, gauge=gauge, precision=64)
+        w = M.Workspace(256, 256, 64, 1, 1, 1, 1, iord=2, nonos=1, gauge=gauge, precision=prec)
 
         def loop16():
             for p in range(16):
@@ -956,6 +992,8 @@ def run_batch_study(args, steps=100):
                     "batch_gcell_steps_per_s": round(tc / (ms_b * 1e-3) / 1e9, 4),
                     "loop_gcell_steps_per_s": round(tc / (ms_l * 1e-3) / 1e9, 4),
                     "speedup_vs_loop": round(ms_l / ms_b, 3)}
+        del base, tr
+        torch.cuda.empty_cache()
     return out
 
 

@@ -41,7 +41,8 @@ extern "C" {
 #define MPDATA_E_CUDA -5        /* a CUDA runtime call failed */
 #define MPDATA_E_DEVICE -6      /* the device error word is set (non-finite result) */
 #define MPDATA_E_UNSUPPORTED -7 /* a reference option outside this library's scope */
-#define MPDATA_E_TOO_LARGE -8   /* grid larger than the fixed scratch of mpdata_step_noalloc_f64 */
+#define MPDATA_E_TOO_LARGE -8   /* a fixed size limit: the scratch of mpdata_step_noalloc_f64, a batch
+                                   tile list of 2^31 tiles, or a netCDF classic slab of 4 GiB */
 #define MPDATA_E_COURANT -9     /* Courant control failed (above the fatal limit, or not finite) */
 #define MPDATA_E_IO -10         /* field file missing, unreadable, not netCDF classic, or without the variable */
 
@@ -349,7 +350,9 @@ int mpdata_pnet_in_chunk_f32(const char* var_name, const char* file_name, int if
  * first call on a device looks up the array's device address, so make it
  * before any stream capture.  All calls share the array: calls that overlap
  * on the GPU race, so order them (one stream, or synchronise).  Nothing needs
- * clearing between calls.  opts->precision must be 64. */
+ * clearing between calls.  opts->precision must be 64.  The address is kept
+ * for the life of the process: do not call it on a device after
+ * cudaDeviceReset there (the array may then live at another address). */
 #define MPDATA_NOALLOC_MAX_CELLS 32768
 int mpdata_step_noalloc_f64(const mpdata_grid* grid, const mpdata_opts* opts, double* psi,
                             const double* u1, const double* u2, const double* u3, const double* h,
