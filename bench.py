@@ -795,6 +795,9 @@ def fd_checks(M, f, tg, d, target, nsteps, ndirs, nx, ny, nz, iord):
     gu = [torch.zeros_like(d[k]) for k in ("u1", "u2", "u3")]
     ws0.adjoint_run(nsteps, psi, d["u1"], d["u2"], d["u3"], d["h"], d["rhr"], target, gx, *gu)
     out["limiter_off_N%d" % nsteps] = adjoint_fd_check(ws0, d, target, gx, gu, nsteps, ndirs, nx, ny, nz)
+    # the Taylor sweep's optimum (truncation ~ eps^2 above it, round-off ~ 1/eps below)
+    out["limiter_off_N%d_eps1e-4" % nsteps] = adjoint_fd_check(ws0, d, target, gx, gu, nsteps, ndirs, nx, ny, nz,
+                                                               eps=1e-4)
     ws0.close()
     noisy = f.x.copy()
     W.interior(noisy)[...] += 1e-3 * np.random.default_rng(7).random((nx, ny, nz))
@@ -828,7 +831,8 @@ def adjoint_fd_check(ws, d, target, gx, gu, nsteps, ndirs, nx, ny, nz, eps=1e-6)
             ws.step(psi, u[0], u[1], u[2], d["h"], d["rhr"])
         return inner(psi).clone()
 
-    errs = []
+    errs, errs_g = [], []
+    gnorm = math.sqrt(float((gx * gx).sum()) + sum(float((g * g).sum()) for g in gu))
     u0 = [d["u1"], d["u2"], d["u3"]]
     tin = inner(target)
     for n in range(ndirs):
@@ -852,8 +856,10 @@ def adjoint_fd_check(ws, d, target, gx, gu, nsteps, ndirs, nx, ny, nz, eps=1e-6)
         pp_, pm_ = final(*shifted(1.0)), final(*shifted(-1.0))
         fd = float((0.5 * (pp_ - pm_) * (pp_ + pm_ - 2.0 * tin)).sum()) / (2 * eps)
         errs.append(abs(fd - dot) / max(abs(dot), 1e-300))
+        errs_g.append(abs(fd - dot) / max(gnorm, 1e-300))
     errs = sorted(errs)
-    return {"directions": ndirs, "eps": eps, "max_rel_err": errs[-1], "median_rel_err": errs[len(errs) // 2]}
+    return {"directions": ndirs, "eps": eps, "max_rel_err": errs[-1], "median_rel_err": errs[len(errs) // 2],
+            "max_err_over_grad_norm": max(errs_g)}
 
 
 def batch_domains(seed=3, count=64):
