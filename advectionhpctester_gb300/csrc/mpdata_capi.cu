@@ -167,6 +167,34 @@ Prob<R> make_prob(const mpdata_grid& g, int gauge, R* psi, const R* u1, const R*
   return P;
 }
 
+// One step of the workspace's problem P: the fused single-precision kernels
+// when the workspace qualifies, else the stage kernels (same bits).
+template <class R>
+int ws_step(Workspace* w, const Prob<R>& P, Prof* prof, cudaStream_t s) {
+  if constexpr (sizeof(R) == 4) {
+    if (w->fused) {
+      FusedPlan F;
+      F.g = P.g;
+      F.psi = P.psi;
+      F.u1 = P.u1;
+      F.u2 = P.u2;
+      F.u3 = P.u3;
+      F.h = P.h;
+      F.rhr = P.rhr;
+      F.arena = static_cast<float*>(w->mem);
+      F.px = w->fz_px;
+      F.fs = (long)w->fz_px * w->g.mp * w->g.lp;
+      F.kchunk = w->fz_kchunk;
+      F.err = w->d_err;
+      F.tmap = &w->fz_map;
+      w->fz_extrema = true;
+      return run_step_fused(F, w->o.iord, prof, s, &w->fz_mx, &w->fz_mn) == 0 ? MPDATA_OK : MPDATA_E_CUDA;
+    }
+  }
+  w->fz_extrema = false;
+  return run_step<R>(P, w->o.iord, w->o.nonos, prof, s) == 0 ? MPDATA_OK : MPDATA_E_CUDA;
+}
+
 template <class R>
 int step_impl(void* ws, R* psi, const R* u1, const R* u2, const R* u3, const R* h, const R* rhr,
               const R* bcx, const R* bcy, void* stream) {
@@ -180,28 +208,7 @@ int step_impl(void* ws, R* psi, const R* u1, const R* u2, const R* u3, const R* 
   R* base = static_cast<R*>(w->mem);
   Prob<R> P = make_prob<R>(w->g, w->o.gauge, psi, u1, u2, u3, h, rhr, bcx, bcy, base, w->ncell,
                            base + (size_t)NFIELD * w->ncell, 1);
-  if constexpr (sizeof(R) == 4) {
-    if (w->fused) {
-      FusedPlan F;
-      F.g = P.g;
-      F.psi = P.psi;
-      F.u1 = P.u1;
-      F.u2 = P.u2;
-      F.u3 = P.u3;
-      F.h = P.h;
-      F.rhr = P.rhr;
-      F.arena = base;
-      F.px = w->fz_px;
-      F.fs = (long)w->fz_px * w->g.mp * w->g.lp;
-      F.kchunk = w->fz_kchunk;
-      F.err = w->d_err;
-      F.tmap = &w->fz_map;
-      w->fz_extrema = true;
-      return run_step_fused(F, w->o.iord, w->prof, s, &w->fz_mx, &w->fz_mn) == 0 ? MPDATA_OK : MPDATA_E_CUDA;
-    }
-  }
-  w->fz_extrema = false;
-  return run_step<R>(P, w->o.iord, w->o.nonos, w->prof, s) == 0 ? MPDATA_OK : MPDATA_E_CUDA;
+  return ws_step<R>(w, P, w->prof, s);
 }
 
 template <class R>
@@ -1325,7 +1332,7 @@ int adjoint_run_impl(void* ws, int nsteps, int interval, R* psi, const R* u1, co
   auto fwd = [&](R* state) -> int {
     Prob<R> F = make_prob<R>(g, w->o.gauge, state, u1, u2, u3, h, rhr, bcx, bcy, base, w->ncell,
                              base + (size_t)NFIELD * w->ncell, 1);
-    return run_step<R>(F, w->o.iord, w->o.nonos, nullptr, s);
+    return ws_step<R>(w, F, nullptr, s);
   };
   // forward sweep with checkpoints
   for (int n = 0; n < nsteps && !rc; n++) {
@@ -1372,7 +1379,7 @@ int adjoint_run_impl(void* ws, int nsteps, int interval, R* psi, const R* u1, co
     }
     for (int n = n0 + 1; n < n1 && !rc; n++) {
       R* dst = seg + (size_t)(n - n0) * plen;
-      if (cudaMemcpyAsync(dst, dst - plen, pbytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess || fwd(dst))
+      if (cudaMemcpyAsync(dst, dst - plen, pbytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess || fwd(dst) != 0)
         rc = MPDATA_E_CUDA;
     }
     for (int n = n1 - 1; n >= n0 && !rc; n--) {
