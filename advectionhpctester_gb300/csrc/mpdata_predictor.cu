@@ -166,6 +166,30 @@ __global__ void __launch_bounds__(128) k_pred_cgrid(Geo g, long lev, R* ox, R* o
   }
 }
 
+// velprd_traj0 and the driver's level roll in one pass over the cells (the
+// whole predictor's first launch): the roll reads only the cell's own
+// level-0 momenta and density, which the n+1/2 momenta read too, and writes
+// level 2 after the cell's level 2 has been read, so the C-grid averaging
+// that follows reads level 1 alone.
+template <class R, bool R1>
+__global__ void __launch_bounds__(128) k_pred_level_roll(Geo g, long lev, R* ox, R* oy, R* oz, R* pu, R* pv,
+                                                         R* pw, Arr<R> h, R hg1, R hg2, R hg3, R r) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int k = blockIdx.z + 1;
+  const bool live = i <= g.np && j <= g.mp;
+  const bool unit = warp_unit_h<R>(live, h, i, j, k);
+  if (!live) return;
+  const long off = (long)(i - 1) + (long)(j - 1) * h.sy + (long)(k - 1) * h.sz;
+  if (unit) {
+    pred_level_cell<R, true, R1>(lev, off, ox, oy, oz, R(1), hg1, hg2, hg3, r);
+    roll_cell<R, true>(lev, ox, oy, oz, pu, pv, pw, h, r, i, j, k);
+  } else {
+    pred_level_cell<R, false, R1>(lev, off, ox, oy, oz, h.ld(i, j, k), hg1, hg2, hg3, r);
+    roll_cell<R>(lev, ox, oy, oz, pu, pv, pw, h, r, i, j, k);
+  }
+}
+
 template <class R>
 __global__ void __launch_bounds__(128) k_pred_roll(Geo g, long lev, R* ox, R* oy, R* oz, R* pu, R* pv, R* pw,
                                                    Arr<R> h, R r) {
@@ -279,9 +303,29 @@ int run_pred_parts(const PredPlan<R>& P, bool level, bool cgrid, bool roll, cuda
   return cudaGetLastError() == cudaSuccess ? 0 : -5;
 }
 
+// The whole predictor: n+1/2 momenta and level roll in one launch, then the
+// C-grid averaging of level 1.
 template <class R>
 int run_predictor(const PredPlan<R>& P, cudaStream_t s) {
-  return run_pred_parts<R>(P, true, true, true, s);
+  const Geo& g = P.g;
+  const dim3 blk(32, 4, 1);
+  const dim3 g1((g.np + 31) / 32, (g.mp + 3) / 4, g.lp);
+  const dim3 g2((g.np + 1 + 31) / 32, (g.mp + 1 + 3) / 4, g.lp + 1);
+  const R hg1 = R(0.5) * P.gc1, hg2 = R(0.5) * P.gc2, hg3 = R(0.5) * P.gc3;
+  if (P.prof) P.prof->begin(ST_PRED_LEVEL, s);
+  if (P.dt_ratio == R(1))
+    k_pred_level_roll<R, true><<<g1, blk, 0, s>>>(g, P.lev, P.ox, P.oy, P.oz, P.u, P.v, P.w, P.h, hg1, hg2, hg3,
+                                                 P.dt_ratio);
+  else
+    k_pred_level_roll<R, false><<<g1, blk, 0, s>>>(g, P.lev, P.ox, P.oy, P.oz, P.u, P.v, P.w, P.h, hg1, hg2, hg3,
+                                                  P.dt_ratio);
+  if (P.prof) P.prof->end(ST_PRED_LEVEL, s);
+  if (P.prof) P.prof->begin(ST_PRED_CGRID, s);
+  k_pred_cgrid<R, false><<<g2, blk, 0, s>>>(g, P.lev, P.ox, P.oy, P.oz, P.u, P.v, P.w, P.h, P.u1, P.u2, P.u3,
+                                            P.dt_ratio);
+  if (P.prof) P.prof->end(ST_PRED_CGRID, s);
+  add_launches(2);
+  return cudaGetLastError() == cudaSuccess ? 0 : -5;
 }
 
 template <class R>

@@ -44,8 +44,8 @@ UNIT = "Gcell-steps/s"
 #   bounds   r xant psi|mx,mn h rhr F1..3     w q cp cn (+mx mn)        10..13
 #   limit    r cp cn v1..3 (+xant q)          w w1..3 (+f1..3)          8 (13 std)
 #   update   r q rhr h|hinv F1..3             w out                     7
-#   predictor level  r o0 x3 o2 x3 h  w o1 x3                            10
-#   predictor cgrid  r o1 x3 o0 x3 h  w u1..3 o2 x3                      13
+#   predictor level  r o0 x3 o2 x3 h  w o1 x3 o2 x3 (the level roll)     13
+#   predictor cgrid  r o1 x3          w u1..3                             6
 # The fused single-precision step (periodic gauge grids):
 #   fused_upwind_pseudo  r psi u1..3 h rhr     w x_in xant v1..3           11
 #   fused_pseudo         r x w1..3 h           w v1..3                      8
@@ -73,9 +73,9 @@ def stage_elems(stage, gauge, iord, precision=64):
     if stage == "corrective_update":
         return 7.0                                    # w1..3 (f1..3),q,h (1/h),rhr -> psi
     if stage == "predictor_level":
-        return 10.0
-    if stage == "predictor_cgrid":
         return 13.0
+    if stage == "predictor_cgrid":
+        return 6.0
     if stage == "fused_upwind_pseudo":
         return 11.0
     if stage == "fused_pseudo":
@@ -731,6 +731,7 @@ def run_adjoint_study(args, n=(256, 256, 64), nsteps=200, iord=2, fd_dirs=32):
     out = {"workload": "adjoint_%dx%dx%d_periodic_gauge_iord%d_nonos_N%d" % (nx, ny, nz, iord, nsteps),
            "checkpoint_interval": int(math.ceil(math.sqrt(nsteps)))}
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    grads = {}
     for prec, dt in ((64, torch.float64), (32, torch.float32)):
         d = {k: M.fortran_device(getattr(f, k), dtype=np.float64 if prec == 64 else np.float32)
              for k in ("x", "u1", "u2", "u3", "h", "rhr")}
@@ -769,6 +770,17 @@ def run_adjoint_study(args, n=(256, 256, 64), nsteps=200, iord=2, fd_dirs=32):
                "run_ms": round(run_ms, 2), "run_over_forward": round(run_ms / fwd_ms, 3),
                "adjoint_gcell_steps_per_s": round(cells * nsteps / (run_ms * 1e-3) / 1e9, 4),
                "peak_bytes": int(peak), "J": J}
+        grads[prec] = [gx.double()] + [g.double() for g in gu]
+        if prec == 32:
+            # the FP32 gradient against the FP64 one (central differences of an
+            # FP32 J of about 1e6 resolve nothing at eps = 1e-6)
+            num = math.sqrt(sum(float(((a - b) ** 2).sum()) for a, b in zip(grads[32], grads[64])))
+            den = math.sqrt(sum(float((b ** 2).sum()) for b in grads[64]))
+            lmax = max(float((a - b).abs().max()) for a, b in zip(grads[32], grads[64]))
+            gmax = max(float(b.abs().max()) for b in grads[64])
+            res["grad_vs_fp64"] = {"l2_rel": num / den, "linf_rel": lmax / gmax,
+                                   "note": "dJ/dpsi_0 and dJ/du1..u3 of the FP32 run against the FP64 run's"}
+            del grads
         if prec == 64 and fd_dirs:
             res["fd_check"] = fd_checks(M, f, tg, d, target, nsteps, fd_dirs, nx, ny, nz, iord)
         out["fp%d" % prec] = res
