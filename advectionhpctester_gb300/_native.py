@@ -42,6 +42,8 @@ SIGNATURES = {
     "mpdata_release_cached": ([], I),
     "mpdata_velprd_f64": ([P] * 8 + [D] * 5 + [P] * 4, I),
     "mpdata_velprd_f32": ([P] * 8 + [F] * 5 + [P] * 4, I),
+    "mpdata_velprd_adjoint_f64": ([P, P] + [D] * 5 + [P] * 7, I),
+    "mpdata_velprd_adjoint_f32": ([P, P] + [F] * 5 + [P] * 7, I),
     "mpdata_rho_gauge_f64": ([P] * 20 + [D] * 5 + [I, P], I),
     "mpdata_rho_gauge_f32": ([P] * 20 + [F] * 5 + [I, P], I),
     "mpdata_step_adjoint_f64": ([P] * 14, I),

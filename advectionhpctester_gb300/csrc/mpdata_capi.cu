@@ -246,6 +246,40 @@ int velprd_impl(void* ws, R* ox, R* oy, R* oz, R* u, R* v, R* wv, const R* h, R 
   return run_predictor<R>(P, s) == 0 ? MPDATA_OK : MPDATA_E_CUDA;
 }
 
+// The predictor's transpose (run_pred_adjoint): the plan's level stacks and
+// C-grid arrays are the gradient arrays.
+template <class R>
+int velprd_adjoint_impl(void* ws, const R* h, R dxi, R dyi, R dzi, R dt, R dt_ratio, const R* gu1, const R* gu2,
+                        const R* gu3, R* gox, R* goy, R* goz, void* stream) {
+  Workspace* w = as_ws(ws);
+  if (!w) return MPDATA_E_WS;
+  if (w->elem != sizeof(R)) return MPDATA_E_WS;
+  if (!h || !gu1 || !gu2 || !gu3 || !gox || !goy || !goz) return MPDATA_E_NULL;
+  const mpdata_grid& g = w->g;
+  const int ih = g.ih;
+  const int sx = g.np + 2 * ih, sy = g.mp + 2 * ih, sz = g.lp + 2 * ih;
+  const long off = ih + (long)ih * sx + (long)ih * sx * sy;
+  PredPlan<R> P;
+  P.g = geo_of(g);
+  P.lev = (long)sx * sy * sz;
+  P.ox = gox + off;
+  P.oy = goy + off;
+  P.oz = goz + off;
+  P.u = P.v = P.w = nullptr;
+  P.h = caller_view<R>(const_cast<R*>(h), ih, sx, sy);
+  P.u1 = caller_view<R>(const_cast<R*>(gu1), ih, sx + 1, sy);
+  P.u2 = caller_view<R>(const_cast<R*>(gu2), ih, sx, sy + 1);
+  P.u3 = caller_view<R>(const_cast<R*>(gu3), ih, sx, sy);
+  P.gc1 = dt * dxi;
+  P.gc2 = dt * dyi;
+  P.gc3 = dt * dzi;
+  P.dt_ratio = dt_ratio;
+  P.prof = nullptr;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  w->last = s;
+  return run_pred_adjoint<R>(P, s) == 0 ? MPDATA_OK : MPDATA_E_CUDA;
+}
+
 // mpdata3d_rho_gauge_gpubc: predictor, density step, outputs.
 template <class R>
 int rho_impl(void* ws, R* ox, R* oy, R* oz, R* u, R* v, R* wv, R* u1, R* u2, R* u3, R* x_in, R* x_incomp,
@@ -479,6 +513,17 @@ int mpdata_velprd_f32(void* ws, float* ox, float* oy, float* oz, float* u, float
                       const float* h, float dxi, float dyi, float dzi, float dt, float dt_ratio,
                       float* u1, float* u2, float* u3, void* stream) {
   return velprd_impl<float>(ws, ox, oy, oz, u, v, w, h, dxi, dyi, dzi, dt, dt_ratio, u1, u2, u3, stream);
+}
+
+int mpdata_velprd_adjoint_f64(void* ws, const double* h, double dxi, double dyi, double dzi, double dt,
+                              double dt_ratio, const double* g_u1, const double* g_u2, const double* g_u3,
+                              double* g_ox, double* g_oy, double* g_oz, void* stream) {
+  return velprd_adjoint_impl<double>(ws, h, dxi, dyi, dzi, dt, dt_ratio, g_u1, g_u2, g_u3, g_ox, g_oy, g_oz, stream);
+}
+int mpdata_velprd_adjoint_f32(void* ws, const float* h, float dxi, float dyi, float dzi, float dt, float dt_ratio,
+                              const float* g_u1, const float* g_u2, const float* g_u3, float* g_ox, float* g_oy,
+                              float* g_oz, void* stream) {
+  return velprd_adjoint_impl<float>(ws, h, dxi, dyi, dzi, dt, dt_ratio, g_u1, g_u2, g_u3, g_ox, g_oy, g_oz, stream);
 }
 
 int mpdata_rho_gauge_f64(void* ws, double* ox, double* oy, double* oz, double* u, double* v, double* w,

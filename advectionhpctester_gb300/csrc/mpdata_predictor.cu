@@ -200,6 +200,72 @@ __global__ void __launch_bounds__(128) k_pred_roll(Geo g, long lev, R* ox, R* oy
   roll_cell<R>(lev, ox, oy, oz, pu, pv, pw, h, r, i, j, k);
 }
 
+// ---- adjoint of the predictor ----------------------------------------------
+// The predictor is linear in the momenta of levels 0 and 2 (h and the time
+// steps held fixed): per component, a0 = l0*h, a1 = a0 + r*(a0 - l2),
+// A = (a1 + a0)*hg (level 1, module_velprd.f90:60-83), u(f) = 0.5*(A(f) + A(f-1))
+// on the C grid with the periodic wrap or the open-wall extrapolation
+// 2A(1) - A(2) (:197-361), and the roll writes l0*h into level 2
+// (velprd_driver.f90:254-270).  Its transpose, gathered per cell (no atomics):
+// dJ/dA(c) collects the faces that read A(c), then dJ/dl0 += (2 + r)*hg*h*dJ/dA
+// + h*dJ/d(level 2 written), and dJ/d(level 2 read) = -r*hg*dJ/dA.
+
+// dJ/dA at cell c of an axis of n cells from the face gradients gf(1..n+1).
+template <class R, class F>
+__device__ __forceinline__ R face_gather(const F& gf, int c, int n, bool per) {
+  R s = R(0.5) * (gf(c) + gf(c + 1));  // face c reads A(c) as its upper cell, face c+1 as its lower
+  if (per) {
+    if (c == n) s = s + R(0.5) * gf(1);      // face 1's lower cell wraps to n
+    if (c == 1) s = s + R(0.5) * gf(n + 1);  // face n+1 is face 1: its upper cell is 1
+  } else {
+    if (c == 1) s = s + gf(1);               // face 1's lower value 2A(1) - A(2)
+    if (c == 2) s = s - R(0.5) * gf(1);
+    if (c == n) s = s + gf(n + 1);           // face n+1's upper value 2A(n) - A(n-1)
+    if (c == n - 1) s = s - R(0.5) * gf(n + 1);
+  }
+  return s;
+}
+
+// gx/gy/gz: gradient level stacks laid out as ox/oy/oz (logical (1,1,1) of
+// level 0); gu1..gu3: dJ/du on the C grid.  In: level 1 = dJ/d(level 1),
+// level 2 = dJ/d(level 2 as the roll wrote it); out: level 0 accumulates
+// dJ/d(level 0), level 2 = dJ/d(level 2 as the predictor read it).
+template <class R>
+__global__ void __launch_bounds__(128) k_pred_adjoint(Geo g, long lev, R* gx, R* gy, R* gz, Arr<R> h, Arr<R> gu1,
+                                                      Arr<R> gu2, Arr<R> gu3, R hg1, R hg2, R hg3, R r) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int k = blockIdx.z + 1;
+  if (i > g.np || j > g.mp) return;
+  const long off = (long)(i - 1) + (long)(j - 1) * h.sy + (long)(k - 1) * h.sz;
+  const R hc = h.ld(i, j, k);
+  const R ga[3] = {face_gather<R>([&](int f) { return gu1.ld(f, j, k); }, i, g.np, g.bx != 0),
+                   face_gather<R>([&](int f) { return gu2.ld(i, f, k); }, j, g.mp, g.by != 0),
+                   face_gather<R>([&](int f) { return gu3.ld(i, j, f); }, k, g.lp, g.bz != 0)};
+  R* o[3] = {gx, gy, gz};
+  const R hg[3] = {hg1, hg2, hg3};
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const R a = ga[c] + o[c][off + lev];  // plus dJ/d(level 1) itself
+    const R g2 = o[c][off + 2 * lev];
+    o[c][off] = o[c][off] + (R(2) + r) * hg[c] * hc * a + hc * g2;
+    o[c][off + 2 * lev] = -r * hg[c] * a;
+  }
+}
+
+template <class R>
+int run_pred_adjoint(const PredPlan<R>& P, cudaStream_t s) {
+  const Geo& g = P.g;
+  const dim3 blk(32, 4, 1);
+  const dim3 grd((g.np + 31) / 32, (g.mp + 3) / 4, g.lp);
+  k_pred_adjoint<R><<<grd, blk, 0, s>>>(g, P.lev, P.ox, P.oy, P.oz, P.h, P.u1, P.u2, P.u3, R(0.5) * P.gc1,
+                                        R(0.5) * P.gc2, R(0.5) * P.gc3, P.dt_ratio);
+  add_launches(1);
+  return cudaGetLastError() == cudaSuccess ? 0 : -5;
+}
+template int run_pred_adjoint<double>(const PredPlan<double>&, cudaStream_t);
+template int run_pred_adjoint<float>(const PredPlan<float>&, cudaStream_t);
+
 // compute_courants (common/diagutils.f90:588-672): the maxima over the
 // interior of |a_x|+|a_y|+|a_z|, the three pair sums and the three
 // components, where a = gc*ox(level 0) (LEV2 false) or ox(level 1)/h (LEV2

@@ -69,6 +69,10 @@ int run_courants(const PredPlan<R>& plan, int level, R dxi, R dyi, R dzi, R dt, 
                  cudaStream_t stream);
 template <class R>
 int run_halve(R* p, long n, cudaStream_t stream);
+// Adjoint of run_predictor: plan.ox/oy/oz are the gradient level stacks,
+// plan.u1..u3 the C-grid gradients dJ/du (see k_pred_adjoint).
+template <class R>
+int run_pred_adjoint(const PredPlan<R>& plan, cudaStream_t stream);
 
 // Adjoint of one step (mpdata_adjoint.cu), gauge form, iord >= 2.
 // Reverse-kernel arguments of one corrective pass: where each adjoint lives.

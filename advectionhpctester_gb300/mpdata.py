@@ -139,6 +139,19 @@ class Workspace:
                  _ptr(u2, d, s["u2"], "u2"), _ptr(u3, d, s["u3"], "u3"), _stream(stream)),
               "mpdata_velprd")
 
+    def velprd_adjoint(self, gox, goy, goz, h, dxi, dyi, dzi, dt, dt_ratio, gu1, gu2, gu3, stream=None):
+        """Adjoint of velprd (mpdata_velprd_adjoint_*): gu1..gu3 hold dJ/du;
+        gox/goy/goz are (..., 3) gradient stacks (level 1: dJ/d(level 1), level
+        2: dJ/d(the rolled level 2) on entry); level 0 accumulates dJ/d(level 0)
+        and level 2 becomes dJ/d(the level 2 read)."""
+        s, d = self.shapes, self.dtype
+        lev = s["psi"] + (3,)
+        fn = self.lib.mpdata_velprd_adjoint_f64 if self.opts.precision == 64 else self.lib.mpdata_velprd_adjoint_f32
+        check(fn(self.handle, _ptr(h, d, s["psi"], "h"), dxi, dyi, dzi, dt, dt_ratio, _ptr(gu1, d, s["u1"], "gu1"),
+                 _ptr(gu2, d, s["u2"], "gu2"), _ptr(gu3, d, s["u3"], "gu3"), _ptr(gox, d, lev, "gox"),
+                 _ptr(goy, d, lev, "goy"), _ptr(goz, d, lev, "goz"), _stream(stream)),
+              "mpdata_velprd_adjoint")
+
     def rho_gauge(self, ox, oy, oz, u1, u2, u3, x_in, x_incomp, h, rhoadv, rhr, pexe, pexr1, pexr2,
                   dxi, dyi, dzi, dt, dt_ratio, bcx=None, bcy=None, liner=0, u=None, v=None, w=None,
                   stream=None):

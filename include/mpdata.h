@@ -121,6 +121,24 @@ int mpdata_velprd_f32(void* ws, float* ox, float* oy, float* oz, float* u, float
                       const float* h, float dxi, float dyi, float dzi, float dt, float dt_ratio,
                       float* u1, float* u2, float* u3, void* stream);
 
+/* Adjoint of mpdata_velprd_* (no reference code): gradients with respect to
+ * the A-grid momenta.  The predictor is linear in the momenta of levels 0
+ * and 2 for fixed h, dt and dt_ratio (module_velprd.f90:58-83,197-361, the
+ * level roll of velprd_driver.f90:254-270); this is its transpose.  g_u1..g_u3
+ * hold dJ/du1..u3 (C-grid shaped, faces 1..n+1).  g_ox/g_oy/g_oz are
+ * gradient stacks laid out as ox/oy/oz; on entry level 1 holds dJ/d(level 1)
+ * and level 2 dJ/d(the level 2 the roll writes) (zero when J does not read
+ * them); on exit level 0 has dJ/d(level 0) ADDED and level 2 holds dJ/d(the
+ * level 2 the predictor read), so calls chain backwards over steps like the
+ * forward's level roll.  Interior cells only; gradients with respect to h and
+ * the physical velocity stacks are not formed. */
+int mpdata_velprd_adjoint_f64(void* ws, const double* h, double dxi, double dyi, double dzi, double dt,
+                              double dt_ratio, const double* g_u1, const double* g_u2, const double* g_u3,
+                              double* g_ox, double* g_oy, double* g_oz, void* stream);
+int mpdata_velprd_adjoint_f32(void* ws, const float* h, float dxi, float dyi, float dzi, float dt,
+                              float dt_ratio, const float* g_u1, const float* g_u2, const float* g_u3,
+                              float* g_ox, float* g_oy, float* g_oz, void* stream);
+
 /* Density step of the dycore, mpdata3d_rho_gauge_gpubc
  * (advection/src_algorithms/mpdata3d-rho-gauge-gpubc.f90:23-622): the
  * predictor (as mpdata_velprd_*), then rhoadv = x_incomp, an upwind pass
