@@ -237,21 +237,20 @@ __global__ void KA_LB_LIMIT ka_limit(const Prob<R> P, const AdjArr<R> A) {
 }
 
 // ---- bounds: cp = (mx-x)h/Dp, cn = (x-mn)h/Dn -------------------------------
-// The extrema are re-folded in the oracle's order (mx2/mn2 trees) so ties go
-// to the same operand: element ids 0..6 are x_in, 7..13 xant.
-// FP64 values compare through their order keys on the integer pipe (equal
-// values tie the same way; -0 orders below +0, as in the forward's folds).
-__device__ __forceinline__ long long ord_key(double v) { return okey(v); }
-__device__ __forceinline__ float ord_key(float v) { return v; }
+// The extrema are re-folded in the oracle's order (mx2/mn2 trees) with the
+// compare-and-select's own semantics (ties, +0 == -0 included, keep the
+// second operand), so each goes to the same operand: element ids 0..6 are
+// x_in, 7..13 xant.  FP64 values compare on the integer pipe (ieee_gt).
+__device__ __forceinline__ bool arg_gt(double a, double b) { return ieee_gt(a, b); }
+__device__ __forceinline__ bool arg_gt(float a, float b) { return a > b; }
 template <class R>
 struct Arg {
   R v;
-  decltype(ord_key(R(0))) key;
   int id;
 };
-template <class R> __device__ __forceinline__ Arg<R> mkarg(R v, int id) { return Arg<R>{v, ord_key(v), id}; }
-template <class R> __device__ __forceinline__ Arg<R> amax(Arg<R> a, Arg<R> b) { return a.key > b.key ? a : b; }
-template <class R> __device__ __forceinline__ Arg<R> amin(Arg<R> a, Arg<R> b) { return a.key < b.key ? a : b; }
+template <class R> __device__ __forceinline__ Arg<R> mkarg(R v, int id) { return Arg<R>{v, id}; }
+template <class R> __device__ __forceinline__ Arg<R> amax(Arg<R> a, Arg<R> b) { return arg_gt(a.v, b.v) ? a : b; }
+template <class R> __device__ __forceinline__ Arg<R> amin(Arg<R> a, Arg<R> b) { return arg_gt(b.v, a.v) ? a : b; }
 
 // Adjoint of the bounds' denominators onto one flux f: Dp holds pn(f) and
 // Dn pp(f) for an outflow face (e), the reverse for an inflow face (w); a

@@ -195,13 +195,13 @@ __device__ __forceinline__ void velgroup_body(const Prob<R>& P, int i, int j, in
     if (gg) {
       P.gvf[0].at(i, j, k) = b1;
       P.gvf[1].at(i, j, k) = b2;
-      P.gvf[2].at(i, j, k) = ka * R(0.5);
-      P.gvf[3].at(i, j, k) = R(0.03125) * a * hx;
+      P.gvf[2].at(i, j, k) = scale_down<1>(ka);
+      P.gvf[3].at(i, j, k) = scale_down<5>(a) * hx;
     }
     if (gs) {
       P.gvs[0].at(i, j, k) = ka;
-      P.gvs[1].at(i, j, k) = R(0.125) * a * b1;
-      P.gvs[2].at(i, j, k) = R(0.125) * a * b2;
+      P.gvs[1].at(i, j, k) = scale_down<3>(a) * b1;
+      P.gvs[2].at(i, j, k) = scale_down<3>(a) * b2;
     }
   }
   if (IN || g.by || j > 1) {
@@ -212,13 +212,13 @@ __device__ __forceinline__ void velgroup_body(const Prob<R>& P, int i, int j, in
     if (gg) {
       P.gvf[4].at(i, j, k) = b1;
       P.gvf[5].at(i, j, k) = b2;
-      P.gvf[6].at(i, j, k) = ka * R(0.5);
-      P.gvf[7].at(i, j, k) = R(0.03125) * a * hy;
+      P.gvf[6].at(i, j, k) = scale_down<1>(ka);
+      P.gvf[7].at(i, j, k) = scale_down<5>(a) * hy;
     }
     if (gs) {
       P.gvs[3].at(i, j, k) = ka;
-      P.gvs[4].at(i, j, k) = R(0.125) * a * b1;
-      P.gvs[5].at(i, j, k) = R(0.125) * a * b2;
+      P.gvs[4].at(i, j, k) = scale_down<3>(a) * b1;
+      P.gvs[5].at(i, j, k) = scale_down<3>(a) * b2;
     }
   }
   if (IN || g.bz || k > 1) {
@@ -229,13 +229,13 @@ __device__ __forceinline__ void velgroup_body(const Prob<R>& P, int i, int j, in
     if (gg) {
       P.gvf[8].at(i, j, k) = b1;
       P.gvf[9].at(i, j, k) = b2;
-      P.gvf[10].at(i, j, k) = ka * R(0.5);
-      P.gvf[11].at(i, j, k) = R(0.03125) * a * hz;
+      P.gvf[10].at(i, j, k) = scale_down<1>(ka);
+      P.gvf[11].at(i, j, k) = scale_down<5>(a) * hz;
     }
     if (gs) {
       P.gvs[6].at(i, j, k) = ka;
-      P.gvs[7].at(i, j, k) = R(0.125) * a * b1;
-      P.gvs[8].at(i, j, k) = R(0.125) * a * b2;
+      P.gvs[7].at(i, j, k) = scale_down<3>(a) * b1;
+      P.gvs[8].at(i, j, k) = scale_down<3>(a) * b2;
     }
   }
 #undef AX
@@ -425,7 +425,7 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
       if (GV)
         v = P.gvf[2].ld(i, j, k) * (XX(i, j, k) - XX(i - 1, j, k)) - P.gvf[3].ld(i, j, k) * cr;
       else
-        v = vdyf_u<U>(XX(i - 1, j, k), XX(i, j, k), a, hmx) - hmul<U>(R(0.03125) * a, hmx) * cr;
+        v = vdyf_u<U>(XX(i - 1, j, k), XX(i, j, k), a, hmx) - hmul<U>(scale_down<5>(a), hmx) * cr;
     }
     if (!STD) put(0, v, R(0));
   }
@@ -467,7 +467,7 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
       if (GV)
         v = P.gvf[6].ld(i, j, k) * (XX(i, j, k) - XX(i, j - 1, k)) - P.gvf[7].ld(i, j, k) * cr;
       else
-        v = vdyf_u<U>(XX(i, j - 1, k), XX(i, j, k), a, hmy) - hmul<U>(R(0.03125) * a, hmy) * cr;
+        v = vdyf_u<U>(XX(i, j - 1, k), XX(i, j, k), a, hmy) - hmul<U>(scale_down<5>(a), hmy) * cr;
     }
     if (!STD) put(1, v, R(0));
   }
@@ -502,7 +502,7 @@ __device__ __forceinline__ void pseudo_form(const Prob<R>& P, int i, int j, int 
       if (GV)
         v = P.gvf[10].ld(i, j, k) * (XX(i, j, k) - XX(i, j, k - 1)) - P.gvf[11].ld(i, j, k) * cr;
       else
-        v = vdyf_u<U>(XX(i, j, k - 1), XX(i, j, k), a, hmz) - hmul<U>(R(0.03125) * a, hmz) * cr;
+        v = vdyf_u<U>(XX(i, j, k - 1), XX(i, j, k), a, hmz) - hmul<U>(scale_down<5>(a), hmz) * cr;
     }
     if (!STD) put(2, v, R(0));
   }
@@ -571,10 +571,10 @@ __device__ __forceinline__ RatioOps<R> bounds_body(const Prob<R>& P, int i, int 
   if (!NONOS) return {};
   const bool lo = IN || g.bz || k > 1, hi = IN || g.bz || k < g.lp;
   R ma, mi;
-  if constexpr (sizeof(R) == 4) {
-    // FP32 compares with IEEE selects, whose ties between +0 and -0 keep
-    // the earlier operand: fold in the oracle's (and the reference's) tree
-    // order so that every tie goes the same way
+  // the reference's compare-and-select folds in its tree order, whose ties
+  // between +0 and -0 keep the earlier operand (FP32 always; FP64 when the
+  // key-order extrema below may differ from them)
+  auto tree = [&]() {
     if (FIRST) {
       const Arr<R>& xin = P.psi;
       const int im = cx<IN>(g, i - 1), ip = cx<IN>(g, i + 1);
@@ -611,36 +611,44 @@ __device__ __forceinline__ RatioOps<R> bounds_body(const Prob<R>& P, int i, int 
       ma = mx2(ma, b6);
       mi = mn2(mi, b6);
     }
-  } else if (FIRST) {
-    const Arr<R>& xin = P.psi;
-    const int im = cx<IN>(g, i - 1), ip = cx<IN>(g, i + 1);
-    const int jm = cy<IN>(g, j - 1), jp = cy<IN>(g, j + 1);
-    Extrema<R> e(xin.ld(i, j, k));
-    e.add(xin.ld(im, j, k));
-    e.add(xin.ld(ip, j, k));
-    e.add(xin.ld(i, jm, k));
-    e.add(xin.ld(i, jp, k));
-    if (lo) e.add(xin.ld(i, j, cz<IN>(g, k - 1)));
-    if (hi) e.add(xin.ld(i, j, cz<IN>(g, k + 1)));
-    e.add(x);
-    e.add(xr<R, IN>(g, X, i - 1, j, k));
-    e.add(xr<R, IN>(g, X, i + 1, j, k));
-    e.add(xr<R, IN>(g, X, i, j - 1, k));
-    e.add(xr<R, IN>(g, X, i, j + 1, k));
-    if (lo) e.add(X.ld(i, j, cz<IN>(g, k - 1)));
-    if (hi) e.add(X.ld(i, j, cz<IN>(g, k + 1)));
-    ma = e.max();
-    mi = e.min();
+  };
+  if constexpr (sizeof(R) == 4) {
+    tree();
   } else {
-    Extrema<R> e(x);
-    e.add(xr<R, IN>(g, X, i - 1, j, k));
-    e.add(xr<R, IN>(g, X, i + 1, j, k));
-    e.add(xr<R, IN>(g, X, i, j - 1, k));
-    e.add(xr<R, IN>(g, X, i, j + 1, k));
-    if (lo) e.add(X.ld(i, j, cz<IN>(g, k - 1)));
-    if (hi) e.add(X.ld(i, j, cz<IN>(g, k + 1)));
-    ma = mx2(P.mx.ld(i, j, k), e.max());
-    mi = mn2(P.mn.ld(i, j, k), e.min());
+    // FP64: key order on the integer pipe, then the tree where an extremum
+    // is a zero or a NaN, the only cases in which the two can differ
+    if (FIRST) {
+      const Arr<R>& xin = P.psi;
+      const int im = cx<IN>(g, i - 1), ip = cx<IN>(g, i + 1);
+      const int jm = cy<IN>(g, j - 1), jp = cy<IN>(g, j + 1);
+      Extrema<R> e(xin.ld(i, j, k));
+      e.add(xin.ld(im, j, k));
+      e.add(xin.ld(ip, j, k));
+      e.add(xin.ld(i, jm, k));
+      e.add(xin.ld(i, jp, k));
+      if (lo) e.add(xin.ld(i, j, cz<IN>(g, k - 1)));
+      if (hi) e.add(xin.ld(i, j, cz<IN>(g, k + 1)));
+      e.add(x);
+      e.add(xr<R, IN>(g, X, i - 1, j, k));
+      e.add(xr<R, IN>(g, X, i + 1, j, k));
+      e.add(xr<R, IN>(g, X, i, j - 1, k));
+      e.add(xr<R, IN>(g, X, i, j + 1, k));
+      if (lo) e.add(X.ld(i, j, cz<IN>(g, k - 1)));
+      if (hi) e.add(X.ld(i, j, cz<IN>(g, k + 1)));
+      ma = e.max();
+      mi = e.min();
+    } else {
+      Extrema<R> e(x);
+      e.add(xr<R, IN>(g, X, i - 1, j, k));
+      e.add(xr<R, IN>(g, X, i + 1, j, k));
+      e.add(xr<R, IN>(g, X, i, j - 1, k));
+      e.add(xr<R, IN>(g, X, i, j + 1, k));
+      if (lo) e.add(X.ld(i, j, cz<IN>(g, k - 1)));
+      if (hi) e.add(X.ld(i, j, cz<IN>(g, k + 1)));
+      ma = mx2k(P.mx.ld(i, j, k), e.max());
+      mi = mn2k(P.mn.ld(i, j, k), e.min());
+    }
+    if (zero_or_nan(ma) || zero_or_nan(mi)) tree();
   }
   if (KEEP && !DEFER) {
     P.mx.at(i, j, k) = ma;

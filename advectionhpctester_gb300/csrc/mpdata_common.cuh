@@ -54,9 +54,10 @@ __device__ __forceinline__ int clampi(int i, int n) { return i < 1 ? 1 : (i > n 
 // retires about 2 operations per SM per clock, while the integer pipe retires
 // about 64.  For doubles these selects therefore work on the bit patterns:
 // the order key of x is its bits with the magnitude bits flipped when the
-// sign is set, so signed 64-bit order of keys is IEEE order of values.  Each
-// returns one of its inputs (or +0) bit for bit, as the floating-point forms
-// do; the only difference is that -0 orders below +0.  Float keeps the
+// sign is set, so signed 64-bit order of keys is IEEE order of values, except
+// that -0 orders below +0 and a NaN orders beyond the infinities.  The
+// selects below return what the reference's compare-and-select returns, bit
+// for bit, and use the keys alone where the two orders agree.  Float keeps the
 // native FP32 compares (cheap on the FP32/ALU pipes).
 __device__ __forceinline__ long long okey(double x) {
   const long long b = __double_as_longlong(x);
@@ -86,17 +87,63 @@ __device__ __forceinline__ bool nonzero_bits(double y) {
   return ((hi << 1) | lo) != 0u;
 }
 
+// Products by a power of two 2^-s on the integer pipe.  When x is a normal
+// number whose exponent field e satisfies s < e < 0x7FF, x*2^-s is a normal
+// number with the same significand and e-s as its exponent field: the FP64
+// multiplication rounds nothing there, so lowering the field gives its bits.
+// A zero keeps its sign (0*2^-s = 0).  Subnormal results and subnormal,
+// infinite or NaN operands take the multiplication itself, behind a call so
+// that it is branched around.  Float multiplies (its pipe is not the bound).
+static __device__ __noinline__ double mul_call(double x, double y) { return x * y; }
+__device__ __forceinline__ double scale_down(double x, int s, double k) {  // k = 2^-s, 1 <= s <= 60
+  const int hi = __double2hiint(x), lo = __double2loint(x);
+  const unsigned e = ((unsigned)hi >> 20) & 0x7FFu;
+  if (e - (unsigned)(s + 1) < (unsigned)(0x7FE - s)) return __hiloint2double(hi - (s << 20), lo);
+  if ((((unsigned)hi << 1) | (unsigned)lo) == 0u) return x;
+  return mul_call(x, k);
+}
+template <int S>
+__device__ __forceinline__ double scale_down(double x) {
+  return scale_down(x, S, 1.0 / (double)(1LL << S));
+}
+template <int S>
+__device__ __forceinline__ float scale_down(float x) {
+  return x * (1.0f / (float)(1 << S));
+}
+
 // pp(y) = max(0,y), pn(y) = -min(0,y)  (mpdataoperators.inc:50-59)
 __device__ __forceinline__ double pp(double y) { return sgn(y) ? 0.0 : y; }
 __device__ __forceinline__ double pn(double y) { return sgn(y) ? neg_bits(y) : 0.0; }
 __device__ __forceinline__ float pp(float y) { return y > 0.f ? y : 0.f; }
 __device__ __forceinline__ float pn(float y) { return y < 0.f ? -y : 0.f; }
-__device__ __forceinline__ double mx2(double a, double b) { return okey(a) > okey(b) ? a : b; }
-__device__ __forceinline__ double mn2(double a, double b) { return okey(a) < okey(b) ? a : b; }
+// a > b as the FP64 compare gives it, on the integer pipe: false when either
+// operand is a NaN or both are zeros (+0 == -0), else the order of the keys.
+__device__ __forceinline__ bool ieee_gt(double a, double b) {
+  const unsigned long long ka = (unsigned long long)__double_as_longlong(a) << 1,
+                           kb = (unsigned long long)__double_as_longlong(b) << 1;  // magnitudes, doubled
+  const unsigned long long inf2 = 0xFFE0000000000000ULL;
+  if (ka > inf2 || kb > inf2 || (ka | kb) == 0ULL) return false;
+  return okey(a) > okey(b);
+}
+// The reference's compare-and-select max and min (a > b ? a : b, a < b ?
+// a : b): ties and NaNs keep the second operand.
+__device__ __forceinline__ double mx2(double a, double b) { return ieee_gt(a, b) ? a : b; }
+__device__ __forceinline__ double mn2(double a, double b) { return ieee_gt(b, a) ? a : b; }
 __device__ __forceinline__ float mx2(float a, float b) { return a > b ? a : b; }
 __device__ __forceinline__ float mn2(float a, float b) { return a < b ? a : b; }
+// The same selects in the order of the keys alone, which differs from them
+// only when both operands are zeros of opposite signs (-0 orders below +0) or
+// an operand is a NaN.
+__device__ __forceinline__ double mx2k(double a, double b) { return okey(a) > okey(b) ? a : b; }
+__device__ __forceinline__ double mn2k(double a, double b) { return okey(a) < okey(b) ? a : b; }
+// x is a zero or a NaN (the extrema the key order may pick differently)
+__device__ __forceinline__ bool zero_or_nan(double x) {
+  return ((unsigned long long)__double_as_longlong(x) << 1) - 1ULL >= 0xFFE0000000000000ULL;
+}
 
-// Running max and min over a set of values (the limiter's 7-point stars).
+// Running max and min over a set of values (the limiter's 7-point stars), in
+// key order for doubles: exact whenever the extremum found is neither a zero
+// nor a NaN (it is then the one value of its bits in the set).
 template <class R> struct Extrema;
 template <> struct Extrema<double> {
   long long kx, kn;
@@ -174,16 +221,16 @@ __device__ __forceinline__ double donor(double y1, double y2, double a) {
   return (sgn(y1) && !sgn(y2)) ? -0.0 : 0.0;
 }
 template <class R> __device__ __forceinline__ R vdyf(R x1, R x2, R a, R rinv) {
-  return (fabs(a) - mul1(a * a, rinv)) * (x2 - x1) * R(0.5);
+  return scale_down<1>((fabs(a) - mul1(a * a, rinv)) * (x2 - x1));
 }
 template <class R> __device__ __forceinline__ R rat4(R z0, R z1, R z2, R z3) {
-  return ((z3 + z2) - (z1 + z0)) * R(0.25);
+  return scale_down<2>((z3 + z2) - (z1 + z0));
 }
 template <class R> __device__ __forceinline__ R vdyfa(R x1, R x2, R a, R rinv, R ep) {
   return (fabs(a) - mul1(a * a, rinv)) * (fabs(x2) - fabs(x1)) / (fabs(x2) + fabs(x1) + ep);
 }
 template <class R> __device__ __forceinline__ R vcorra(R a, R b, R y1, R y2, R rinv) {
-  return -(mul1(R(0.125) * a * b * y1, rinv) / y2);
+  return -(mul1(scale_down<3>(a) * b * y1, rinv) / y2);
 }
 // Forms of the pseudo-velocity operators for the stage kernels.  U: every face
 // density of the warp is exactly 1, so the products by it are dropped (exact,
@@ -194,17 +241,32 @@ template <class R> __device__ __forceinline__ R vcorra(R a, R b, R y1, R y2, R r
 // FP64, 2^-126 in FP32), and differs by at most a subnormal ulp otherwise.
 template <bool U, class R> __device__ __forceinline__ R hmul(R x, R hm) { return U ? x : x * hm; }
 template <bool U, class R> __device__ __forceinline__ R vdyf_u(R x1, R x2, R a, R hm) {
-  return (fabs(a) - hmul<U>(a * a, hm)) * (x2 - x1) * R(0.5);
+  return scale_down<1>((fabs(a) - hmul<U>(a * a, hm)) * (x2 - x1));
 }
 template <bool U, class R> __device__ __forceinline__ R vdyfa_u(R x1, R x2, R a, R hm, R ep) {
   return (fabs(a) - hmul<U>(a * a, hm)) * (fabs(x2) - fabs(x1)) / (fabs(x2) + fabs(x1) + ep);
 }
 template <bool U, class R> __device__ __forceinline__ R vcorra_u(R a, R b, R y1, R y2, R hm) {
-  return -(hmul<U>(R(0.125) * a * b * y1, hm) / y2);
+  return -(hmul<U>(scale_down<3>(a) * b * y1, hm) / y2);
 }
 template <class R> __device__ __forceinline__ R dif4(R z0, R z1, R z2, R z3) { return (z3 + z2) - (z1 + z0); }
 template <class R> __device__ __forceinline__ R possign(R x) { return sgn(x) ? R(0) : R(1); }
-template <class R> __device__ __forceinline__ R min3(R a, R b) { return mn2(mn2(R(1), a), b); }
+// min3(a, b) = mn2(mn2(1, a), b).  For doubles whose high words are both
+// below 0x7FF00000 (non-negative, finite: the limiter's ratios) the raw bit
+// patterns order as the values do, +0 included, so two integer compares give
+// the result; anything else (a sign bit, an infinity, a NaN) takes the
+// compares' own semantics.
+__device__ __forceinline__ float min3(float a, float b) { return mn2(mn2(1.0f, a), b); }
+static __device__ __noinline__ double min3_exact(double a, double b) { return mn2(mn2(1.0, a), b); }
+__device__ __forceinline__ double min3(double a, double b) {
+  const unsigned ha = (unsigned)__double2hiint(a), hb = (unsigned)__double2hiint(b);
+  if ((ha > hb ? ha : hb) < 0x7FF00000u) {
+    const long long ba = __double_as_longlong(a), bb = __double_as_longlong(b), one = 0x3FF0000000000000LL;
+    const long long t = one < ba ? one : ba;
+    return __longlong_as_double(t < bb ? t : bb);
+  }
+  return min3_exact(a, b);
+}
 // 1/(0.5*(h1+h2)) == 2/(h1+h2) exactly: the halving is an exact scaling.
 __device__ __forceinline__ double rhm(double h1, double h2) {
   return is_one(h1) && is_one(h2) ? 1.0 : div_call(2.0, h1 + h2);

@@ -3,21 +3,45 @@
 // and the Courant-number maxima the driver steers substepping and adaptive
 // time steps with (common/diagutils.f90:588-672).  Strict IEEE, same
 // expression order as the reference.
+#include <cmath>
+
 #include "mpdata_common.cuh"
 #include "mpdata_stages.cuh"
 
 namespace mpdata {
 
 // n+1/2 momenta times dt/dx into level 1 (module_velprd.f90:60-83):
-// 0.5*(a1+a0)*gc, taken as (a1+a0)*hgc with hgc = 0.5*gc formed on the host
-// (scaling by 0.5 commutes with rounding unless a value is subnormal).  R1:
-// the time-step ratio r is exactly 1, so r*(a0-a2) is a0-a2.  A warp whose
-// densities are all exactly 1 takes a0 = ox(level 0) without the product.
+// 0.5*(a1+a0)*gc in the reference's order.  The halving runs on the integer
+// pipe (scale_down); the product by gc is skipped when gc is exactly 1 and is
+// another scale_down when gc is 2^-s (FP64).  R1: the time-step ratio r is
+// exactly 1, so r*(a0-a2) is a0-a2.  A warp whose densities are all exactly
+// 1 takes a0 = ox(level 0) without the product.
+template <class R>
+struct GcK {
+  R k[3];
+  int s[3];  // -1: k == 1; s >= 1: k == 2^-s (FP64); 0: multiply
+};
+template <class R>
+GcK<R> gc_factors(R gc1, R gc2, R gc3) {
+  GcK<R> f;
+  const R gc[3] = {gc1, gc2, gc3};
+  for (int c = 0; c < 3; c++) {
+    f.k[c] = gc[c];
+    int e = 0;
+    const double m = std::frexp((double)gc[c], &e);  // gc = m*2^e, m in [0.5, 1)
+    f.s[c] = gc[c] == R(1) ? -1 : (sizeof(R) == 8 && m == 0.5 && 1 - e >= 1 && 1 - e <= 60) ? 1 - e : 0;
+  }
+  return f;
+}
+__device__ __forceinline__ double mul_gc(double x, double k, int s) {
+  return s < 0 ? x : (s ? scale_down(x, s, k) : x * k);
+}
+__device__ __forceinline__ float mul_gc(float x, float k, int s) { return s < 0 ? x : x * k; }
+
 template <class R, bool U, bool R1>
-__device__ __forceinline__ void pred_level_cell(long lev, long off, R* ox, R* oy, R* oz, R hc, R hg1, R hg2,
-                                                R hg3, R r) {
+__device__ __forceinline__ void pred_level_cell(long lev, long off, R* ox, R* oy, R* oz, R hc, const GcK<R>& gc,
+                                                R r) {
   R* o[3] = {ox, oy, oz};
-  const R hg[3] = {hg1, hg2, hg3};
   // the six loads first: a store could alias them as far as the compiler knows
   R l0[3], l2[3];
 #pragma unroll
@@ -29,7 +53,7 @@ __device__ __forceinline__ void pred_level_cell(long lev, long off, R* ox, R* oy
   for (int c = 0; c < 3; c++) {
     const R a0 = U ? l0[c] : l0[c] * hc;
     const R a1 = a0 + (R1 ? a0 - l2[c] : r * (a0 - l2[c]));
-    o[c][off + lev] = (a1 + a0) * hg[c];
+    o[c][off + lev] = mul_gc(scale_down<1>(a1 + a0), gc.k[c], gc.s[c]);
   }
 }
 
@@ -46,7 +70,7 @@ __device__ __forceinline__ bool warp_unit_h(bool live, const Arr<R>& h, int i, i
 
 template <class R, bool R1>
 __global__ void __launch_bounds__(128) k_pred_level(Geo g, long lev, R* ox, R* oy, R* oz, Arr<R> h,
-                                                    R hg1, R hg2, R hg3, R r) {
+                                                    GcK<R> gc, R r) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int k = blockIdx.z + 1;
@@ -56,9 +80,9 @@ __global__ void __launch_bounds__(128) k_pred_level(Geo g, long lev, R* ox, R* o
   // ox/oy/oz point at the logical (1,1,1) of level 0; levels are psi-shaped
   const long off = (long)(i - 1) + (long)(j - 1) * h.sy + (long)(k - 1) * h.sz;
   if (unit)
-    pred_level_cell<R, true, R1>(lev, off, ox, oy, oz, R(1), hg1, hg2, hg3, r);
+    pred_level_cell<R, true, R1>(lev, off, ox, oy, oz, R(1), gc, r);
   else
-    pred_level_cell<R, false, R1>(lev, off, ox, oy, oz, h.ld(i, j, k), hg1, hg2, hg3, r);
+    pred_level_cell<R, false, R1>(lev, off, ox, oy, oz, h.ld(i, j, k), gc, r);
 }
 
 // C-grid averaging with the open-wall extrapolation 2a(1)-a(2)
@@ -142,21 +166,21 @@ __global__ void __launch_bounds__(128) k_pred_cgrid(Geo g, long lev, R* ox, R* o
       if (i == 1) A1.at(0, j, k) = b1;
       if (i == g.np + 1) A1.at(g.np + 1, j, k) = a1;
     }
-    u1.at(i, j, k) = R(0.5) * (a1 + b1);
+    u1.at(i, j, k) = scale_down<1>(a1 + b1);
   }
   if (e2) {
     if (!g.by) {
       if (j == 1) A2.at(i, 0, k) = b2;
       if (j == g.mp + 1) A2.at(i, g.mp + 1, k) = a2;
     }
-    u2.at(i, j, k) = R(0.5) * (a2 + b2);
+    u2.at(i, j, k) = scale_down<1>(a2 + b2);
   }
   if (e3) {
     if (!g.bz) {
       if (k == 1) A3.at(i, j, 0) = b3;
       if (k == g.lp + 1) A3.at(i, j, g.lp + 1) = a3;
     }
-    u3.at(i, j, k) = R(0.5) * (a3 + b3);
+    u3.at(i, j, k) = scale_down<1>(a3 + b3);
   }
   if (rl) {
     if (unit)
@@ -173,7 +197,7 @@ __global__ void __launch_bounds__(128) k_pred_cgrid(Geo g, long lev, R* ox, R* o
 // that follows reads level 1 alone.
 template <class R, bool R1>
 __global__ void __launch_bounds__(128) k_pred_level_roll(Geo g, long lev, R* ox, R* oy, R* oz, R* pu, R* pv,
-                                                         R* pw, Arr<R> h, R hg1, R hg2, R hg3, R r) {
+                                                         R* pw, Arr<R> h, GcK<R> gc, R r) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int k = blockIdx.z + 1;
@@ -182,10 +206,10 @@ __global__ void __launch_bounds__(128) k_pred_level_roll(Geo g, long lev, R* ox,
   if (!live) return;
   const long off = (long)(i - 1) + (long)(j - 1) * h.sy + (long)(k - 1) * h.sz;
   if (unit) {
-    pred_level_cell<R, true, R1>(lev, off, ox, oy, oz, R(1), hg1, hg2, hg3, r);
+    pred_level_cell<R, true, R1>(lev, off, ox, oy, oz, R(1), gc, r);
     roll_cell<R, true>(lev, ox, oy, oz, pu, pv, pw, h, r, i, j, k);
   } else {
-    pred_level_cell<R, false, R1>(lev, off, ox, oy, oz, h.ld(i, j, k), hg1, hg2, hg3, r);
+    pred_level_cell<R, false, R1>(lev, off, ox, oy, oz, h.ld(i, j, k), gc, r);
     roll_cell<R>(lev, ox, oy, oz, pu, pv, pw, h, r, i, j, k);
   }
 }
@@ -343,11 +367,11 @@ int run_pred_parts(const PredPlan<R>& P, bool level, bool cgrid, bool roll, cuda
   int n = 0;
   if (level) {
     if (P.prof) P.prof->begin(ST_PRED_LEVEL, s);
-    const R hg1 = R(0.5) * P.gc1, hg2 = R(0.5) * P.gc2, hg3 = R(0.5) * P.gc3;
+    const GcK<R> gc = gc_factors(P.gc1, P.gc2, P.gc3);
     if (P.dt_ratio == R(1))
-      k_pred_level<R, true><<<g1, blk, 0, s>>>(g, P.lev, P.ox, P.oy, P.oz, P.h, hg1, hg2, hg3, P.dt_ratio);
+      k_pred_level<R, true><<<g1, blk, 0, s>>>(g, P.lev, P.ox, P.oy, P.oz, P.h, gc, P.dt_ratio);
     else
-      k_pred_level<R, false><<<g1, blk, 0, s>>>(g, P.lev, P.ox, P.oy, P.oz, P.h, hg1, hg2, hg3, P.dt_ratio);
+      k_pred_level<R, false><<<g1, blk, 0, s>>>(g, P.lev, P.ox, P.oy, P.oz, P.h, gc, P.dt_ratio);
     if (P.prof) P.prof->end(ST_PRED_LEVEL, s);
     n++;
   }
@@ -377,13 +401,13 @@ int run_predictor(const PredPlan<R>& P, cudaStream_t s) {
   const dim3 blk(32, 4, 1);
   const dim3 g1((g.np + 31) / 32, (g.mp + 3) / 4, g.lp);
   const dim3 g2((g.np + 1 + 31) / 32, (g.mp + 1 + 3) / 4, g.lp + 1);
-  const R hg1 = R(0.5) * P.gc1, hg2 = R(0.5) * P.gc2, hg3 = R(0.5) * P.gc3;
+  const GcK<R> gc = gc_factors(P.gc1, P.gc2, P.gc3);
   if (P.prof) P.prof->begin(ST_PRED_LEVEL, s);
   if (P.dt_ratio == R(1))
-    k_pred_level_roll<R, true><<<g1, blk, 0, s>>>(g, P.lev, P.ox, P.oy, P.oz, P.u, P.v, P.w, P.h, hg1, hg2, hg3,
+    k_pred_level_roll<R, true><<<g1, blk, 0, s>>>(g, P.lev, P.ox, P.oy, P.oz, P.u, P.v, P.w, P.h, gc,
                                                  P.dt_ratio);
   else
-    k_pred_level_roll<R, false><<<g1, blk, 0, s>>>(g, P.lev, P.ox, P.oy, P.oz, P.u, P.v, P.w, P.h, hg1, hg2, hg3,
+    k_pred_level_roll<R, false><<<g1, blk, 0, s>>>(g, P.lev, P.ox, P.oy, P.oz, P.u, P.v, P.w, P.h, gc,
                                                   P.dt_ratio);
   if (P.prof) P.prof->end(ST_PRED_LEVEL, s);
   if (P.prof) P.prof->begin(ST_PRED_CGRID, s);
