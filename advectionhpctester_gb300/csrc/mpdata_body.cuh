@@ -560,6 +560,61 @@ template <class R>
 struct RatioOps {
   R np, dp, nn, dn;
 };
+// The limiter's star extrema folded with the reference's compare-and-select
+// in its tree order, whose ties between +0 and -0 keep the earlier operand
+// (bounds_body: FP32 always, FP64 where its key-order extrema may differ).
+template <class R>
+struct MaMi {
+  R ma, mi;
+};
+template <class R, bool FIRST, bool IN>
+__device__ __forceinline__ MaMi<R> tree_extrema(const Geo& g, const Arr<R>& xin, const Arr<R>& X,
+                                                const Arr<R>& mxa, const Arr<R>& mna, int i, int j, int k, R x,
+                                                bool lo, bool hi) {
+  R ma, mi;
+  if (FIRST) {
+    const int im = cx<IN>(g, i - 1), ip = cx<IN>(g, i + 1);
+    const int jm = cy<IN>(g, j - 1), jp = cy<IN>(g, j + 1);
+    const R a0 = xin.ld(im, j, k), a1 = xin.ld(i, j, k), a2 = xin.ld(ip, j, k), a3 = xin.ld(i, jm, k),
+            a4 = xin.ld(i, jp, k);
+    ma = mx2(mx2(mx2(a0, a1), mx2(a2, a3)), a4);
+    mi = mn2(mn2(mn2(a0, a1), mn2(a2, a3)), a4);
+    if (lo) {
+      const R a5 = xin.ld(i, j, cz<IN>(g, k - 1));
+      ma = mx2(ma, a5);
+      mi = mn2(mi, a5);
+    }
+    if (hi) {
+      const R a6 = xin.ld(i, j, cz<IN>(g, k + 1));
+      ma = mx2(ma, a6);
+      mi = mn2(mi, a6);
+    }
+  } else {
+    ma = mxa.ld(i, j, k);
+    mi = mna.ld(i, j, k);
+  }
+  const R b0 = xr<R, IN>(g, X, i - 1, j, k), b2 = xr<R, IN>(g, X, i + 1, j, k),
+          b3 = xr<R, IN>(g, X, i, j - 1, k), b4 = xr<R, IN>(g, X, i, j + 1, k);
+  ma = mx2(mx2(mx2(ma, b0), mx2(x, b2)), mx2(b3, b4));
+  mi = mn2(mn2(mn2(mi, b0), mn2(x, b2)), mn2(b3, b4));
+  if (lo) {
+    const R b5 = X.ld(i, j, cz<IN>(g, k - 1));
+    ma = mx2(ma, b5);
+    mi = mn2(mi, b5);
+  }
+  if (hi) {
+    const R b6 = X.ld(i, j, cz<IN>(g, k + 1));
+    ma = mx2(ma, b6);
+    mi = mn2(mi, b6);
+  }
+  return MaMi<R>{ma, mi};
+}
+// The same behind a call: the FP64 kernels branch around it.
+template <class R, bool FIRST, bool IN>
+static __device__ __noinline__ MaMi<R> tree_extrema_call(Geo g, Arr<R> xin, Arr<R> X, Arr<R> mxa, Arr<R> mna,
+                                                         int i, int j, int k, R x, bool lo, bool hi) {
+  return tree_extrema<R, FIRST, IN>(g, xin, X, mxa, mna, i, j, k, x, lo, hi);
+}
 template <class R, bool NONOS, bool FIRST, bool KEEP, bool IN = false, int CLM = 0, bool U = false,
           bool DEFER = true>
 __device__ __forceinline__ RatioOps<R> bounds_body(const Prob<R>& P, int i, int j, int k) {
@@ -571,52 +626,13 @@ __device__ __forceinline__ RatioOps<R> bounds_body(const Prob<R>& P, int i, int 
   if (!NONOS) return {};
   const bool lo = IN || g.bz || k > 1, hi = IN || g.bz || k < g.lp;
   R ma, mi;
-  // the reference's compare-and-select folds in its tree order, whose ties
-  // between +0 and -0 keep the earlier operand (FP32 always; FP64 when the
-  // key-order extrema below may differ from them)
-  auto tree = [&]() {
-    if (FIRST) {
-      const Arr<R>& xin = P.psi;
-      const int im = cx<IN>(g, i - 1), ip = cx<IN>(g, i + 1);
-      const int jm = cy<IN>(g, j - 1), jp = cy<IN>(g, j + 1);
-      const R a0 = xin.ld(im, j, k), a1 = xin.ld(i, j, k), a2 = xin.ld(ip, j, k), a3 = xin.ld(i, jm, k),
-              a4 = xin.ld(i, jp, k);
-      ma = mx2(mx2(mx2(a0, a1), mx2(a2, a3)), a4);
-      mi = mn2(mn2(mn2(a0, a1), mn2(a2, a3)), a4);
-      if (lo) {
-        const R a5 = xin.ld(i, j, cz<IN>(g, k - 1));
-        ma = mx2(ma, a5);
-        mi = mn2(mi, a5);
-      }
-      if (hi) {
-        const R a6 = xin.ld(i, j, cz<IN>(g, k + 1));
-        ma = mx2(ma, a6);
-        mi = mn2(mi, a6);
-      }
-    } else {
-      ma = P.mx.ld(i, j, k);
-      mi = P.mn.ld(i, j, k);
-    }
-    const R b0 = xr<R, IN>(g, X, i - 1, j, k), b2 = xr<R, IN>(g, X, i + 1, j, k),
-            b3 = xr<R, IN>(g, X, i, j - 1, k), b4 = xr<R, IN>(g, X, i, j + 1, k);
-    ma = mx2(mx2(mx2(ma, b0), mx2(x, b2)), mx2(b3, b4));
-    mi = mn2(mn2(mn2(mi, b0), mn2(x, b2)), mn2(b3, b4));
-    if (lo) {
-      const R b5 = X.ld(i, j, cz<IN>(g, k - 1));
-      ma = mx2(ma, b5);
-      mi = mn2(mi, b5);
-    }
-    if (hi) {
-      const R b6 = X.ld(i, j, cz<IN>(g, k + 1));
-      ma = mx2(ma, b6);
-      mi = mn2(mi, b6);
-    }
-  };
   if constexpr (sizeof(R) == 4) {
-    tree();
+    const MaMi<R> t = tree_extrema<R, FIRST, IN>(g, P.psi, X, P.mx, P.mn, i, j, k, x, lo, hi);
+    ma = t.ma;
+    mi = t.mi;
   } else {
     // FP64: key order on the integer pipe, then the tree where an extremum
-    // is a zero or a NaN, the only cases in which the two can differ
+    // may be a zero or a NaN, the only cases in which the two can differ
     if (FIRST) {
       const Arr<R>& xin = P.psi;
       const int im = cx<IN>(g, i - 1), ip = cx<IN>(g, i + 1);
@@ -648,7 +664,11 @@ __device__ __forceinline__ RatioOps<R> bounds_body(const Prob<R>& P, int i, int 
       ma = mx2k(P.mx.ld(i, j, k), e.max());
       mi = mn2k(P.mn.ld(i, j, k), e.min());
     }
-    if (zero_or_nan(ma) || zero_or_nan(mi)) tree();
+    if (zero_nan_hi(ma) || zero_nan_hi(mi)) {
+      const MaMi<R> t = tree_extrema_call<R, FIRST, IN>(g, P.psi, X, P.mx, P.mn, i, j, k, x, lo, hi);
+      ma = t.ma;
+      mi = t.mi;
+    }
   }
   if (KEEP && !DEFER) {
     P.mx.at(i, j, k) = ma;

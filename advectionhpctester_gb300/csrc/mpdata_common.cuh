@@ -136,9 +136,11 @@ __device__ __forceinline__ float mn2(float a, float b) { return a < b ? a : b; }
 // an operand is a NaN.
 __device__ __forceinline__ double mx2k(double a, double b) { return okey(a) > okey(b) ? a : b; }
 __device__ __forceinline__ double mn2k(double a, double b) { return okey(a) < okey(b) ? a : b; }
-// x is a zero or a NaN (the extrema the key order may pick differently)
-__device__ __forceinline__ bool zero_or_nan(double x) {
-  return ((unsigned long long)__double_as_longlong(x) << 1) - 1ULL >= 0xFFE0000000000000ULL;
+// A test of the high word that holds for every zero and NaN (the extrema
+// the key order may pick differently): x is a zero, an infinity, a NaN, or a
+// subnormal number whose high word has no significand bit (|x| < 2^-1042).
+__device__ __forceinline__ bool zero_nan_hi(double x) {
+  return ((unsigned)__double2hiint(x) & 0x7FFFFFFFu) - 1u >= 0x7FEFFFFFu;
 }
 
 // Running max and min over a set of values (the limiter's 7-point stars), in

@@ -102,7 +102,7 @@ STEP_COMPULSORY_ELEMS = 11.0
 # (dram__bytes_read.sum + dram__bytes_write.sum, and
 # smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on.sum, per cell).
 # Both grow in proportion to the cells of a launch.
-NCU_PSEUDO = {64: {"dram_bytes_per_cell": 127.7, "fp64_inst_per_cell": 45.0},
+NCU_PSEUDO = {64: {"dram_bytes_per_cell": 127.8, "fp64_inst_per_cell": 39.0},
               32: {"dram_bytes_per_cell": 38.2, "fp64_inst_per_cell": 0.0}}
 # The same for the dominant fused single-precision kernel (the first pass's
 # fused_limit_update) at 384x384x64: DRAM bytes and issued warp instructions
@@ -113,14 +113,15 @@ FP64_INST_PER_SM_CLK = 2.0
 # FP64 flops per cell of one launch of each stage (DADD and DMUL 1, DFMA 2),
 # counted by ncu (smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on.sum)
 # on the deformational flow at unit density, 384x384x64, gauge iord=3.
-FP64_FLOPS_PER_CELL = {"upwind": 12.4, "pair_sums": 6.0, "pseudo_velocity": 45.0, "limiter_bounds": 11.7,
-                       "limited_flux": 3.0, "corrective_update": 6.2, "predictor_level": 12.0,
-                       "predictor_cgrid": 6.0}
+FP64_FLOPS_PER_CELL = {"upwind": 12.4, "pair_sums": 6.0, "pseudo_velocity": 39.0, "limiter_bounds": 11.7,
+                       "limited_flux": 3.0, "corrective_update": 6.2, "predictor_level": 9.0,
+                       "predictor_cgrid": 3.0}
 # FP32 arithmetic instructions (FADD, FMUL, FFMA) per cell of one launch of
 # each fused single-precision kernel, counted by ncu
 # (smsp__sass_thread_inst_executed_op_{fadd,fmul,ffma}_pred_on) on the
 # deformational flow at unit density, 384x384x64; the predictor's from its
-# FP64 twin (the same arithmetic).
+# source (per component, three adds and the product by 0.5 of the n+1/2
+# momenta, one add and one product by 0.5 of the C-grid average).
 FP32_INST_PER_CELL = {"fused_upwind_pseudo": 102.5, "fused_pseudo": 90.0, "fused_limit_update": 52.0,
                       "predictor_level": 12.0, "predictor_cgrid": 6.0}
 FP32_LANES_PER_SM_CLK = 128.0
