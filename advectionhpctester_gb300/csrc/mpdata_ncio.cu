@@ -1,16 +1,15 @@
 // Field output and input in the netCDF classic format, 64-bit offset
 // variant (CDF-2): the single-rank path of pnet_out_chunk
-// (common/mpi_parallel.f90:7481-8176) for the full 3-D modes, and the read
-// back of one frame for restarts.
+// (common/mpi_parallel.f90:7481-8176) in every mode it documents, and the
+// read back of one frame for restarts.
 //
 // pnet_out_chunk(var_name, file_name, imode, ia1, ia2, ia3, ifrmd, imem, var,
 // np, mp, lp, ih): at ifrmd == 0 it creates the file (NF_64BIT_OFFSET) if it
-// does not exist, defines the dimensions x, y, z (np, mp, lp) and the
-// unlimited t if absent, and defines var_name if absent (:7596-7715); then it
-// writes the interior of var as frame ifrmd+1 (:7746-7756).  imode 0 writes a
-// float (x,y,z,t) variable, 1 a double one, 34 a float (x,y,z) variable
-// without time.  Fortran dimension order (x,y,z,t) is netCDF's (t,z,y,x), so
-// x varies fastest in the file, as in the caller's array.
+// does not exist, defines the dimensions the mode uses and the unlimited t if
+// absent, and defines var_name if absent (:7596-7715); then it writes the
+// mode's part of var as frame ifrmd+1 (:7746-8170; make_plan below lists the
+// modes).  Fortran dimension order (x,y,z,t) is netCDF's (t,z,y,x), so x
+// varies fastest in the file, as in the caller's array.
 //
 // The file format follows the published netCDF classic format
 // specification: a big-endian header (magic "CDF\2", record count,
@@ -357,55 +356,206 @@ int find_var(const Model& m, const char* name) {
   return -1;
 }
 
-// ---- interior gather to big-endian bytes ---------------------------------
-template <class R, class T>
-__global__ void k_pack_be(const R* base, int ih, int sx, int sy, int np, int mp, int lp, unsigned char* out) {
-  const long n = (long)np * mp * lp;
-  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
-    const int i = (int)(t % np);
-    const long r = t / np;
-    const int j = (int)(r % mp), k = (int)(r / mp);
-    const T v = (T)base[(long)(i + ih) + (long)(j + ih) * sx + (long)(k + ih) * sx * sy];
-    unsigned char* o = out + t * (long)sizeof(T);
-    const unsigned long long b = sizeof(T) == 8 ? (unsigned long long)__double_as_longlong((double)v)
-                                                : (unsigned long long)__float_as_uint((float)v);
-#pragma unroll
-    for (int q = 0; q < (int)sizeof(T); q++) o[q] = (unsigned char)(b >> (8 * ((int)sizeof(T) - 1 - q)));
+// ---- what one call defines and writes --------------------------------------
+// pnet_out_chunk on a single rank: every edge flag is set, the rank sits at
+// position 1 along each axis and at no sub-domain offset.  Per imode
+// (:7548-7573 lengths, :7606-7640 dimensions, :7671-7712 the variable,
+// :7746-7846 starts and counts, :7847-8170 the data):
+//  0, 1   the interior, float / double (x,y,z,t)
+//  2-4    the staggered block var(1:np+ia1, 1:mp+ia2, 1:lp+ia3), double, with
+//         dimensions of those lengths (var declared with the ia*imem extents)
+//  6-8    the right, top and sky halo strips var(np+1:np+ih, ...) at offset
+//         ih of a 2*ih-long dimension (on one rank the left, bottom and
+//         ground strips are overwritten before the single write)
+//  9      var(np-ih+1:np, mp-ih+1:mp, lp-ih+1:lp) at offset ih of 2*ih-long
+//         dimensions (the corner indices the reference forms on one rank)
+//  10, 13 the xy plane at k = ia3 (written when (ia3-1)/lp == 0) or k = 1,
+//         double (x,y,t), no z dimension defined
+//  11, 12 the xz plane at j = ia2, the yz plane at i = ia1, through single
+//         precision into a double (x,z,t) / (y,z,t) variable
+//  20-22  the z line at (ia1,ia2), the y line at (ia1,ia3), the x line at
+//         (ia2,ia3), float (z,t) / (y,t) / (x,t)
+//  30     a float (t) variable, defined and never written
+//  34     the interior, float (x,y,z), no time
+//  35     the plane k = 1-ih (the ground halo), double (x,y), no time
+// Planes and lines are written only when (ia-1)/n == 0 for each fixed index
+// (the rank-position tests); otherwise nothing is written.  Modes 3 and 4
+// fill their temporaries over a block smaller than the one they write for
+// some offset combinations (unset or out-of-range elements in the
+// reference); here the block the counts describe is written from var.
+struct Plan {
+  bool def[3];                // define x, y, z when absent
+  unsigned long long len[3];  // with these lengths
+  unsigned type;              // the variable's type when it is defined
+  unsigned axes;              // its spatial dimensions: bit 0 x, 1 y, 2 z
+  bool rec;                   // it has the record dimension t
+  bool sp;                    // the values pass through single precision
+  bool write;                 // anything is written
+  int b0[3], cnt[3];          // the box of var: first index (1-based), count
+  int st[3];                  // its start in the variable (0-based)
+};
+
+bool make_plan(int imode, int ia1, int ia2, int ia3, int np, int mp, int lp, int ih, Plan& p) {
+  p = Plan{};
+  for (int a = 0; a < 3; a++) {
+    p.def[a] = true;
+    p.b0[a] = 1;
   }
-}
-
-template <class R, class T>
-void pack_host(const R* base, int ih, int sx, int sy, int np, int mp, int lp, unsigned char* out) {
-  long t = 0;
-  for (int k = 0; k < lp; k++)
-    for (int j = 0; j < mp; j++)
-      for (int i = 0; i < np; i++, t++) {
-        const T v = (T)base[(long)(i + ih) + (long)(j + ih) * sx + (long)(k + ih) * (long)sx * sy];
-        unsigned long long b = 0;
-        std::memcpy(&b, &v, sizeof(T));
-        for (int q = 0; q < (int)sizeof(T); q++)
-          out[t * sizeof(T) + q] = (unsigned char)(b >> (8 * ((int)sizeof(T) - 1 - q)));
+  p.len[0] = np;
+  p.len[1] = mp;
+  p.len[2] = lp;
+  p.cnt[0] = np;
+  p.cnt[1] = mp;
+  p.cnt[2] = lp;
+  p.axes = 7u;
+  p.rec = true;
+  p.write = true;
+  p.type = NC_DOUBLE;
+  // the rank-position tests of the planes and lines (:7847-7854)
+  const bool in1 = (ia1 - 1) / np == 0, in2 = (ia2 - 1) / mp == 0, in3 = (ia3 - 1) / lp == 0;
+  switch (imode) {
+    case 0:
+      p.type = NC_FLOAT;
+      p.sp = true;
+      break;
+    case 1:
+      break;
+    case 2: case 3: case 4:
+      p.len[0] = (unsigned long long)(np + ia1);
+      p.len[1] = (unsigned long long)(mp + ia2);
+      p.len[2] = (unsigned long long)(lp + ia3);
+      p.cnt[0] = np + ia1;
+      p.cnt[1] = mp + ia2;
+      p.cnt[2] = lp + ia3;
+      break;
+    case 6: case 7: case 8: {
+      const int a = imode - 6;
+      p.len[a] = 2ULL * ih;
+      p.b0[a] = (a == 0 ? np : a == 1 ? mp : lp) + 1;
+      p.cnt[a] = ih;
+      p.st[a] = ih;
+      break;
+    }
+    case 9: {
+      const int n[3] = {np, mp, lp};
+      for (int a = 0; a < 3; a++) {
+        p.len[a] = 2ULL * ih;
+        p.b0[a] = n[a] - ih + 1;
+        p.cnt[a] = ih;
+        p.st[a] = ih;
       }
+      break;
+    }
+    case 10: case 13:
+      p.def[2] = false;
+      p.axes = 3u;
+      p.b0[2] = imode == 10 ? ia3 : 1;
+      p.cnt[2] = 1;
+      p.write = imode == 13 || in3;
+      break;
+    case 11:
+      p.def[1] = false;
+      p.axes = 5u;
+      p.sp = true;
+      p.b0[1] = ia2;
+      p.cnt[1] = 1;
+      p.write = in2;
+      break;
+    case 12:
+      p.def[0] = false;
+      p.axes = 6u;
+      p.sp = true;
+      p.b0[0] = ia1;
+      p.cnt[0] = 1;
+      p.write = in1;
+      break;
+    case 20: case 21: case 22: {
+      const int keep = imode == 20 ? 2 : imode == 21 ? 1 : 0;  // the line's axis
+      const int fix[3] = {ia1, ia2, ia3};
+      const bool in[3] = {in1, in2, in3};
+      p.type = NC_FLOAT;
+      p.sp = true;
+      p.axes = 1u << keep;
+      p.write = true;
+      for (int a = 0; a < 3; a++)
+        if (a != keep) {
+          p.def[a] = false;
+          p.b0[a] = fix[a];
+          p.cnt[a] = 1;
+          p.write = p.write && in[a];
+        }
+      break;
+    }
+    case 30:
+      for (int a = 0; a < 3; a++) p.def[a] = false;
+      p.axes = 0u;
+      p.type = NC_FLOAT;
+      p.write = false;
+      break;
+    case 34:
+      p.type = NC_FLOAT;
+      p.sp = true;
+      p.rec = false;
+      break;
+    case 35:
+      p.rec = false;
+      p.axes = 3u;
+      p.b0[2] = 1 - ih;
+      p.cnt[2] = 1;
+      break;
+    default:
+      return false;
+  }
+  return true;
 }
 
-// the interior of a psi-shaped caller array as big-endian T values
-template <class R, class T>
-int gather(const R* var, int np, int mp, int lp, int ih, int on_device, void* stream,
-           std::vector<unsigned char>& out) {
-  const int sx = np + 2 * ih, sy = mp + 2 * ih;
-  const size_t bytes = (size_t)np * mp * lp * sizeof(T);
-  out.resize(bytes);
+// ---- box gather to big-endian bytes ----------------------------------------
+// Element e of the box (x fastest) of a caller array whose allocation starts
+// at base (index 1-ih on each axis, row strides sx, sx*sy), as the value of
+// buffer type B converted to the file type T.
+struct Box {
+  long o0;  // offset of the box's first element from base
+  int cx, cy, cz;
+  long sy, sz;  // element strides of y and z
+};
+template <class R, class B, class T>
+__device__ __host__ inline void put_be(const R* base, const Box& b, long e, unsigned char* out) {
+  const int i = (int)(e % b.cx);
+  const long r = e / b.cx;
+  const int j = (int)(r % b.cy), k = (int)(r / b.cy);
+  const T v = (T)(B)base[b.o0 + i + j * b.sy + k * b.sz];
+  unsigned long long bits = 0;
+#if defined(__CUDA_ARCH__)
+  bits = sizeof(T) == 8 ? (unsigned long long)__double_as_longlong((double)v) : (unsigned long long)__float_as_uint((float)v);
+#else
+  std::memcpy(&bits, &v, sizeof(T));
+#endif
+  unsigned char* o = out + e * (long)sizeof(T);
+  for (int q = 0; q < (int)sizeof(T); q++) o[q] = (unsigned char)(bits >> (8 * ((int)sizeof(T) - 1 - q)));
+}
+template <class R, class B, class T>
+__global__ void k_pack_be(const R* base, Box b, unsigned char* out) {
+  const long n = (long)b.cx * b.cy * b.cz;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x)
+    put_be<R, B, T>(base, b, e, out);
+}
+
+template <class R, class B, class T>
+int gather(const R* var, const Box& b, int on_device, void* stream, std::vector<unsigned char>& out) {
+  const long n = (long)b.cx * b.cy * b.cz;
+  out.resize((size_t)n * sizeof(T));
   if (!on_device) {
-    pack_host<R, T>(var, ih, sx, sy, np, mp, lp, out.data());
+    for (long e = 0; e < n; e++) put_be<R, B, T>(var, b, e, out.data());
     return MPDATA_OK;
   }
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   unsigned char* d = nullptr;
-  if (cudaMallocAsync(&d, bytes, s) != cudaSuccess) return MPDATA_E_CUDA;
-  k_pack_be<R, T><<<1216, 256, 0, s>>>(var, ih, sx, sy, np, mp, lp, d);
+  if (cudaMallocAsync(&d, out.size(), s) != cudaSuccess) return MPDATA_E_CUDA;
+  const long blocks = (n + 255) / 256;
+  k_pack_be<R, B, T><<<(unsigned)(blocks < 1216 ? (blocks < 1 ? 1 : blocks) : 1216), 256, 0, s>>>(var, b, d);
   mpdata::add_launches(1);
   int rc = cudaGetLastError() == cudaSuccess ? MPDATA_OK : MPDATA_E_CUDA;
-  if (rc == MPDATA_OK && cudaMemcpyAsync(out.data(), d, bytes, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+  if (rc == MPDATA_OK && cudaMemcpyAsync(out.data(), d, out.size(), cudaMemcpyDeviceToHost, s) != cudaSuccess)
     rc = MPDATA_E_CUDA;
   cudaFreeAsync(d, s);
   if (cudaStreamSynchronize(s) != cudaSuccess) rc = MPDATA_E_CUDA;
@@ -413,14 +563,19 @@ int gather(const R* var, int np, int mp, int lp, int ih, int on_device, void* st
 }
 
 template <class R>
-int out_chunk(const char* var_name, const char* file_name, int imode, int ifrmd, const R* var, int np, int mp,
-              int lp, int ih, int on_device, void* stream) {
+int out_chunk(const char* var_name, const char* file_name, int imode, int ia1, int ia2, int ia3, int ifrmd,
+              int imem, const R* var, int np, int mp, int lp, int ih, int on_device, void* stream) {
   if (!var_name || !file_name || !var) return MPDATA_E_NULL;
-  if (imode != 0 && imode != 1 && imode != 34) return MPDATA_E_UNSUPPORTED;
   if (np < 1 || mp < 1 || lp < 1 || ih < 0 || ifrmd < 0 || !*var_name) return MPDATA_E_DIMS;
-  const unsigned type = imode == 1 ? NC_DOUBLE : NC_FLOAT;
-  const unsigned long long slab = (unsigned long long)np * mp * lp * type_size(type);
-  if (slab > 0xfffffffcULL) return MPDATA_E_TOO_LARGE;  // a CDF-2 slab size is 32-bit
+  Plan pl;
+  if (!make_plan(imode, ia1, ia2, ia3, np, mp, lp, ih, pl)) return MPDATA_E_UNSUPPORTED;
+  // the caller's array: var(1-ih:n+ia*imem+ih) on each axis (:7510-7512)
+  const long ext[3] = {(long)np + (long)ia1 * imem, (long)mp + (long)ia2 * imem, (long)lp + (long)ia3 * imem};
+  for (int a = 0; a < 3; a++) {
+    if (ext[a] < 1 || pl.len[a] < 1) return MPDATA_E_DIMS;
+    if (pl.write && (pl.cnt[a] < 1 || pl.b0[a] < 1 - ih || (long)pl.b0[a] + pl.cnt[a] - 1 > ext[a] + ih))
+      return MPDATA_E_DIMS;
+  }
   const std::string path(file_name);
   std::vector<unsigned char> bytes;
   Model m;
@@ -431,13 +586,13 @@ int out_chunk(const char* var_name, const char* file_name, int imode, int ifrmd,
   int vi = find_var(m, var_name);
   if (ifrmd == 0) {  // :7596-7715: dimensions and the variable are defined only at frame 0
     const char* dn[3] = {"x", "y", "z"};
-    const unsigned long long dl[3] = {(unsigned long long)np, (unsigned long long)mp, (unsigned long long)lp};
     int did[4];
-    for (int d = 0; d < 3; d++) {
-      did[d] = find_dim(m, dn[d]);
-      if (did[d] < 0) {
-        m.dims.push_back(Dim{dn[d], dl[d]});
-        did[d] = (int)m.dims.size() - 1;
+    for (int a = 0; a < 3; a++) {
+      did[a] = find_dim(m, dn[a]);
+      if (did[a] < 0 && pl.def[a]) {
+        if (pl.len[a] > 0xffffffffULL) return MPDATA_E_TOO_LARGE;
+        m.dims.push_back(Dim{dn[a], pl.len[a]});
+        did[a] = (int)m.dims.size() - 1;
         changed = true;
       }
     }
@@ -450,14 +605,17 @@ int out_chunk(const char* var_name, const char* file_name, int imode, int ifrmd,
     if (vi < 0) {
       Var v;
       v.name = var_name;
-      if (imode != 34) v.dims.push_back((unsigned)did[3]);
-      v.dims.push_back((unsigned)did[2]);
-      v.dims.push_back((unsigned)did[1]);
-      v.dims.push_back((unsigned)did[0]);
-      v.type = type;
+      if (pl.rec) v.dims.push_back((unsigned)did[3]);
+      for (int a = 2; a >= 0; a--)
+        if (pl.axes >> a & 1u) {
+          if (did[a] < 0) return MPDATA_E_DIMS;  // the mode uses a dimension it does not define
+          v.dims.push_back((unsigned)did[a]);
+        }
+      v.type = pl.type;
       v.begin = 0;
       m.vars.push_back(v);
       m.vars.back().vsize = slab_bytes(m, m.vars.back());
+      if (m.vars.back().vsize > 0xfffffffcULL) return MPDATA_E_TOO_LARGE;  // a CDF-2 slab size is 32-bit
       vi = (int)m.vars.size() - 1;
       changed = true;
     }
@@ -465,29 +623,75 @@ int out_chunk(const char* var_name, const char* file_name, int imode, int ifrmd,
   if (vi < 0) return MPDATA_E_IO;  // the reference's write to an undefined variable fails
   Var& v = m.vars[vi];
   const bool rec = is_rec(m, v);
-  // the variable's shape must be the caller's interior, in the caller's precision mode
+  // the variable's spatial lengths along x, y, z (1 where it has no such
+  // dimension); its dimensions must run t, z, y, x and hold the box
+  unsigned long long L[3] = {1, 1, 1};
   {
-    const size_t nd = v.dims.size();
-    if (nd < 3 || m.dims[v.dims[nd - 1]].len != (unsigned long long)np ||
-        m.dims[v.dims[nd - 2]].len != (unsigned long long)mp || m.dims[v.dims[nd - 3]].len != (unsigned long long)lp ||
-        (rec ? nd != 4 : nd != 3) || v.type != type || rec == (imode == 34))
-      return MPDATA_E_DIMS;
+    int last = 3;
+    for (size_t d = rec ? 1 : 0; d < v.dims.size(); d++) {
+      const std::string& nm = m.dims[v.dims[d]].name;
+      const int a = nm == "x" ? 0 : nm == "y" ? 1 : nm == "z" ? 2 : -1;
+      if (a < 0 || a >= last || m.dims[v.dims[d]].len == 0) return MPDATA_E_DIMS;
+      L[a] = m.dims[v.dims[d]].len;
+      last = a;
+    }
+    if (rec != pl.rec || (v.type != NC_FLOAT && v.type != NC_DOUBLE)) return MPDATA_E_DIMS;
+    if (pl.write)
+      for (int a = 0; a < 3; a++)
+        if ((unsigned long long)pl.st[a] + (unsigned long long)pl.cnt[a] > L[a]) return MPDATA_E_DIMS;
   }
   std::vector<unsigned char> data;
-  int rc = imode == 1 ? gather<R, double>(var, np, mp, lp, ih, on_device, stream, data)
-                      : gather<R, float>(var, np, mp, lp, ih, on_device, stream, data);
-  if (rc) return rc;
-  data.resize(v.vsize, 0);
-  if (changed) {
-    rc = rewrite(path, old, bytes, m);
+  if (pl.write) {
+    const long sx = ext[0] + 2L * ih, sy = ext[1] + 2L * ih;
+    const Box b{(long)(pl.b0[0] - 1 + ih) + (long)(pl.b0[1] - 1 + ih) * sx + (long)(pl.b0[2] - 1 + ih) * sx * sy,
+                pl.cnt[0], pl.cnt[1], pl.cnt[2], sx, sx * sy};
+    int rc;
+    if (v.type == NC_DOUBLE)
+      rc = pl.sp ? gather<R, float, double>(var, b, on_device, stream, data)
+                 : gather<R, double, double>(var, b, on_device, stream, data);
+    else
+      rc = pl.sp ? gather<R, float, float>(var, b, on_device, stream, data)
+                 : gather<R, double, float>(var, b, on_device, stream, data);
     if (rc) return rc;
   }
-  // in place: extend the records with fill values if needed, then write the slab
+  if (changed) {
+    const int rc = rewrite(path, old, bytes, m);
+    if (rc) return rc;
+  }
+  if (!pl.write) return MPDATA_OK;
+  const bool whole = pl.st[0] == 0 && pl.st[1] == 0 && pl.st[2] == 0 && (unsigned long long)pl.cnt[0] == L[0] &&
+                     (unsigned long long)pl.cnt[1] == L[1] && (unsigned long long)pl.cnt[2] == L[2];
   const unsigned long long r = rec ? (unsigned long long)ifrmd : 0;
   FILE* f = std::fopen(path.c_str(), "r+b");
   if (!f) return MPDATA_E_IO;
   bool ok = true;
-  if (rec && r + 1 > m.numrecs) {
+  const size_t len = rec ? (size_t)(rec_bytes(m) < v.vsize ? rec_bytes(m) : v.vsize) : (size_t)v.vsize;
+  const unsigned long long off = rec ? rec_offset(m, v, r) : v.begin;
+  const bool fresh = rec && r + 1 > m.numrecs;
+  std::vector<unsigned char> slab;
+  if (whole) {
+    slab.swap(data);
+    slab.resize(len, 0);
+  } else {  // a box inside the slab: start from what the slab holds (fill values if new)
+    if (fresh) {
+      slab = fill_slab(v);
+    } else {
+      slab.resize(len);
+      ok = std::fseek(f, (long)off, SEEK_SET) == 0 && std::fread(slab.data(), 1, len, f) == len;
+    }
+    slab.resize(len, 0);
+    const size_t ts = type_size(v.type);
+    size_t e = 0;
+    for (int k = 0; k < pl.cnt[2]; k++)
+      for (int j = 0; j < pl.cnt[1]; j++) {
+        const unsigned long long row = ((unsigned long long)(pl.st[2] + k) * L[1] + (unsigned long long)(pl.st[1] + j)) * L[0] +
+                                       (unsigned long long)pl.st[0];
+        std::memcpy(&slab[row * ts], &data[e * ts], (size_t)pl.cnt[0] * ts);
+        e += (size_t)pl.cnt[0];
+      }
+  }
+  // extend the records with fill values if needed, then write the slab
+  if (ok && fresh) {
     for (unsigned long long q = m.numrecs; q <= r && ok; q++)
       for (const Var& w : m.vars)
         if (is_rec(m, w) && !(&w == &v && q == r)) {
@@ -500,8 +704,7 @@ int out_chunk(const char* var_name, const char* file_name, int imode, int ifrmd,
                                  (unsigned char)(m.numrecs >> 8), (unsigned char)m.numrecs};
     ok = ok && pwrite_at(f, 4, nr, 4);
   }
-  const size_t len = rec ? (size_t)(rec_bytes(m) < v.vsize ? rec_bytes(m) : v.vsize) : (size_t)v.vsize;
-  ok = ok && pwrite_at(f, rec ? rec_offset(m, v, r) : v.begin, data.data(), len);
+  ok = ok && pwrite_at(f, off, slab.data(), len);
   if (std::fclose(f) != 0) ok = false;
   return ok ? MPDATA_OK : MPDATA_E_IO;
 }
@@ -572,14 +775,14 @@ extern "C" {
 int mpdata_pnet_out_chunk_f64(const char* var_name, const char* file_name, int imode, int ia1, int ia2, int ia3,
                               int ifrmd, int imem, const double* var, int np, int mp, int lp, int ih,
                               int on_device, void* stream) {
-  (void)ia1; (void)ia2; (void)ia3; (void)imem;  // staggered modes 2-4 only
-  return out_chunk<double>(var_name, file_name, imode, ifrmd, var, np, mp, lp, ih, on_device, stream);
+  return out_chunk<double>(var_name, file_name, imode, ia1, ia2, ia3, ifrmd, imem, var, np, mp, lp, ih, on_device,
+                           stream);
 }
 int mpdata_pnet_out_chunk_f32(const char* var_name, const char* file_name, int imode, int ia1, int ia2, int ia3,
                               int ifrmd, int imem, const float* var, int np, int mp, int lp, int ih, int on_device,
                               void* stream) {
-  (void)ia1; (void)ia2; (void)ia3; (void)imem;
-  return out_chunk<float>(var_name, file_name, imode, ifrmd, var, np, mp, lp, ih, on_device, stream);
+  return out_chunk<float>(var_name, file_name, imode, ia1, ia2, ia3, ifrmd, imem, var, np, mp, lp, ih, on_device,
+                          stream);
 }
 int mpdata_pnet_in_chunk_f64(const char* var_name, const char* file_name, int ifrmd, double* var, int np, int mp,
                              int lp, int ih, int on_device, void* stream) {

@@ -91,15 +91,16 @@ __global__ void __launch_bounds__(128) k_copy(const Prob<R> P) {
 // Minimum resident 128-thread blocks per SM asked of the register allocator
 // for the pseudo-velocity kernel, whose interior path keeps ~60 neighbour
 // loads in flight: FP32 is latency-bound and gains from 8 blocks (64
-// registers, a 12-byte spill); FP64 takes 5 (at most 102 registers, no
-// spill; 4 percent faster at 512x512x128 than the 4 blocks its 100
-// registers allowed unbounded; 6 blocks spill).  Build-time overridable for
-// tuning sweeps.
+// registers, a 12-byte spill); FP64 takes 7 (72 registers, an 8-byte spill),
+// which measured 5.02 ms per headline step at 512x512x128 against 5.32 with
+// 5 blocks (88 registers) and 5.06 with 6 (80): the FP64 pipe waits on its
+// loads (8 long-scoreboard stalls per issue at 5 blocks).  Build-time
+// overridable for tuning sweeps.
 #ifndef MPDATA_MINB_PSEUDO_F32
 #define MPDATA_MINB_PSEUDO_F32 8
 #endif
 #ifndef MPDATA_MINB_PSEUDO_F64
-#define MPDATA_MINB_PSEUDO_F64 5
+#define MPDATA_MINB_PSEUDO_F64 7
 #endif
 template <class R>
 struct PseudoMinBlocks {

@@ -427,16 +427,20 @@ def velprd_driver(state, ox, oy, oz, u, v, w, uadv, vadv, wadv, h, ipoles, ibcx,
     return tuple(diag)
 
 
-def pnet_out_chunk(var_name, file_name, imode, ifrmd, var, np_, mp, lp, ih, stream=None):
-    """pnet_out_chunk (common/mpi_parallel.f90:7481) for the full 3-D modes
-    (imode 0 float, 1 double, 34 float without time) from a psi-shaped
-    Fortran-ordered CUDA tensor or numpy array; writes netCDF classic
+def pnet_out_chunk(var_name, file_name, imode, ifrmd, var, np_, mp, lp, ih, ia1=0, ia2=0, ia3=0, imem=0,
+                   stream=None):
+    """pnet_out_chunk (common/mpi_parallel.f90:7481) from a Fortran-ordered
+    CUDA tensor or numpy array of extents n+ia*imem+2*ih per axis (psi-shaped
+    when imem is 0): the full 3-D modes (0 float, 1 double, 34 float without
+    time), the staggered blocks 2-4, the halo strips 6-9, the planes 10-13 and
+    35, the lines 20-22 and the point variable 30; writes netCDF classic
     (64-bit offset)."""
     lib = _native.load()
     dev = torch is not None and isinstance(var, torch.Tensor)
     if dev:
         d = var.dtype
-        ptr = _ptr(var, d, shapes(np_, mp, lp, ih)["psi"], "var")
+        shape = (np_ + ia1 * imem + 2 * ih, mp + ia2 * imem + 2 * ih, lp + ia3 * imem + 2 * ih)
+        ptr = _ptr(var, d, shape, "var")
         f64 = d == torch.float64
     else:
         if not var.flags.f_contiguous:
@@ -444,8 +448,9 @@ def pnet_out_chunk(var_name, file_name, imode, ifrmd, var, np_, mp, lp, ih, stre
         ptr = var.ctypes.data
         f64 = var.dtype == np.float64
     fn = lib.mpdata_pnet_out_chunk_f64 if f64 else lib.mpdata_pnet_out_chunk_f32
-    check(fn(var_name.encode(), str(file_name).encode(), int(imode), 0, 0, 0, int(ifrmd), 0, ptr, np_, mp, lp,
-             ih, 1 if dev else 0, _stream(stream) if dev else None), "mpdata_pnet_out_chunk")
+    check(fn(var_name.encode(), str(file_name).encode(), int(imode), int(ia1), int(ia2), int(ia3), int(ifrmd),
+             int(imem), ptr, np_, mp, lp, ih, 1 if dev else 0, _stream(stream) if dev else None),
+          "mpdata_pnet_out_chunk")
 
 
 def pnet_in_chunk(var_name, file_name, ifrmd, var, np_, mp, lp, ih, stream=None):

@@ -333,15 +333,25 @@ int mpdata_velprd_driver_f32(int* nsubsteps, int* nsubsteps_o, int lsubstepping,
 /* ---- field output and input (netCDF classic, 64-bit offset) --------------
  * pnet_out_chunk (common/mpi_parallel.f90:7481-8176), single rank, same
  * argument order plus on_device (1: var is a device pointer, 0: host) and
- * stream.  imode 0 writes the interior of the psi-shaped var as a float
- * (x,y,z,t) variable, 1 as a double one, 34 as a float (x,y,z) variable; the
- * other modes (staggered, halo, planes, lines, points) return
- * MPDATA_E_UNSUPPORTED, and ia1..ia3/imem are unused.  At ifrmd == 0 the
- * file, the dimensions x, y, z, t (unlimited) and the variable are created if
- * absent; the interior is written as frame ifrmd+1 (record ifrmd).  Frames
- * between the last record and ifrmd hold the netCDF default fill value.  A
- * variable's slab must stay below 4 GiB (MPDATA_E_TOO_LARGE).  Files are
- * readable by any netCDF-3 reader.  Synchronises the stream. */
+ * stream.  var has extents n+ia*imem+2*ih per axis (psi-shaped for imem 0).
+ * imode: 0/1 the interior as float/double (x,y,z,t); 2-4 the staggered
+ * block var(1:n+ia) as double with dimensions n+ia; 6-8 the right, top, sky
+ * halo strips at offset ih of 2*ih-long dimensions and 9 var(n-ih+1:n) at
+ * offset ih on each axis (what one rank writes); 10/13 the xy plane k = ia3 /
+ * k = 1 as double (x,y,t); 11/12 the xz plane j = ia2 / yz plane i = ia1
+ * through single precision into double (x,z,t) / (y,z,t); 20/21/22 the z, y,
+ * x lines through (ia1,ia2), (ia1,ia3), (ia2,ia3) as float; 30 a float (t)
+ * variable, never written; 34 the interior as float (x,y,z); 35 the plane
+ * k = 1-ih as double (x,y).  A plane or line whose fixed index has
+ * (ia-1)/n != 0 lies on another rank: nothing is written.  Other modes return
+ * MPDATA_E_UNSUPPORTED.  At ifrmd == 0 the file, the dimensions the mode uses
+ * (x, y, z with the mode's lengths, t unlimited) and the variable are created
+ * if absent; existing dimensions are reused, and a write that does not fit
+ * the variable or the array returns MPDATA_E_DIMS.  Values convert to the
+ * variable's type.  Frames between the last record and ifrmd hold the netCDF
+ * default fill value, as do the parts of a slab no call wrote.  A variable's
+ * slab must stay below 4 GiB (MPDATA_E_TOO_LARGE).  Files are readable by
+ * any netCDF-3 reader.  Synchronises the stream. */
 int mpdata_pnet_out_chunk_f64(const char* var_name, const char* file_name, int imode, int ia1,
                               int ia2, int ia3, int ifrmd, int imem, const double* var, int np,
                               int mp, int lp, int ih, int on_device, void* stream);

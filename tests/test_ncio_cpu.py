@@ -94,10 +94,15 @@ def test_read_back_into_interior(native_lib, tmp_path):
 def test_errors(native_lib, tmp_path):
     lib, p = native_lib, tmp_path / "tape.nc"
     a = field(50)
-    assert out(lib, "x", p, 2, 0, a) == -7          # staggered mode: unsupported
+    assert out(lib, "x", p, 5, 0, a) == -7          # not a pnet_out_chunk mode
     assert out(lib, "x", p, 1, 3, a) == -10         # frame > 0 of a variable never defined
     assert out(lib, "x", p, 1, 0, a) == 0
-    assert out(lib, "x", p, 0, 1, a.astype(np.float32, order="F")) == -1   # float into the double variable
+    # mode 0 into the double variable: the single-precision buffer converts to
+    # double, as PnetCDF's put_vara_real does
+    assert out(lib, "x", p, 0, 1, a) == 0
+    v, _, _ = read(p)
+    np.testing.assert_array_equal(v["x"][1], interior(a).astype(np.float32).astype(np.float64).transpose(2, 1, 0))
+    assert out(lib, "x", p, 34, 1, a) == -1         # a static mode into the record variable
     assert lib.mpdata_pnet_in_chunk_f64(b"x", str(p).encode(), 4, a.ctypes.data, NP, MP, LP, IH, 0, None) == -10
     assert lib.mpdata_pnet_in_chunk_f64(b"x", str(tmp_path / "none.nc").encode(), 0, a.ctypes.data, NP, MP, LP,
                                         IH, 0, None) == -10
