@@ -46,6 +46,8 @@ SIGNATURES = {
     "mpdata_velprd_adjoint_f32": ([P, P] + [F] * 5 + [P] * 7, I),
     "mpdata_rho_gauge_f64": ([P] * 20 + [D] * 5 + [I, P], I),
     "mpdata_rho_gauge_f32": ([P] * 20 + [F] * 5 + [I, P], I),
+    "mpdata_rho_gauge_adjoint_f64": ([P] * 24, I),
+    "mpdata_rho_gauge_adjoint_f32": ([P] * 24, I),
     "mpdata_step_adjoint_f64": ([P] * 14, I),
     "mpdata_step_adjoint_f32": ([P] * 14, I),
     "mpdata_adjoint_run_f64": ([P, I, I] + [P] * 9 + [ctypes.POINTER(D)] + [P] * 4 +

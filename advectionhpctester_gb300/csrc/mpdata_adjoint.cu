@@ -786,7 +786,12 @@ __device__ __forceinline__ void flux_adj(R lF, R xl, R xr_, R u, bool l_var, con
   *lu_out = nonzero(u) ? lF * (sgn(u) ? xr_ : xl) : R(0);
 }
 
-template <class R, bool IN>
+// MF (density step): the step also outputs each face's upwind flux as part
+// of its mass flux: the lower face's flux of every cell (u1(i), u2(j), u3(k))
+// and the upper face's of the last cell along each axis (u1(np+1), ...).
+// Their cotangents add to the fluxes' own; at a z wall the flux stored for
+// face 1 is -F3(2) and the one for face lp+1 is -F3(lp).
+template <class R, bool IN, bool MF = false>
 __device__ __forceinline__ void ka_upwind_cell(const Prob<R>& P, const AdjArr<R>& A, int i, int j, int k) {
   const Geo& g = P.g;
   const Arr<R>& psi = P.psi;
@@ -804,34 +809,84 @@ __device__ __forceinline__ void ka_upwind_cell(const Prob<R>& P, const AdjArr<R>
   const R xjm = jm_var ? psi.ld(i, jm, k) : P.bcy[by0];
   const R xjp = jp_var ? psi.ld(i, jp, k) : P.bcy[by0 + bys];
   R lu;
+  // the mass fluxes' cotangents of the fluxes this cell computes (MF)
+  R m1 = R(0), m1p = R(0), m2 = R(0), m2p = R(0), m3 = R(0), m3p = R(0);
+  if (MF) {
+    m1 = A.lm1.ld(i, j, k);
+    m2 = A.lm2.ld(i, j, k);
+    m3 = A.lm3.ld(i, j, k);
+    if (!IN && i == g.np) m1p = A.lm1.ld(g.np + 1, j, k);
+    if (!IN && j == g.mp) m2p = A.lm2.ld(i, g.mp + 1, k);
+    if (!IN && k == g.lp) m3p = A.lm3.ld(i, j, g.lp + 1);
+  }
   // x faces: D = F1(i+1) - F1(i) + ...
-  flux_adj(lD, x, xip, fx<R, true, IN>(g, P.u1, i + 1, j, k), true, A.lx, i, j, k, ip_var, ip, j, k, &lu);
+  flux_adj(lD + m1p, x, xip, fx<R, true, IN>(g, P.u1, i + 1, j, k), true, A.lx, i, j, k, ip_var, ip, j, k, &lu);
   fx_add<R, true, IN>(g, A.gu1, i + 1, j, k, lu);
-  flux_adj(-lD, xim, x, P.u1.ld(i, j, k), im_var, A.lx, im, j, k, true, i, j, k, &lu);
+  flux_adj(-lD + m1, xim, x, P.u1.ld(i, j, k), im_var, A.lx, im, j, k, true, i, j, k, &lu);
   fx_add<R, true, IN>(g, A.gu1, i, j, k, lu);
-  flux_adj(lD, x, xjp, fy<R, true, IN>(g, P.u2, i, j + 1, k), true, A.lx, i, j, k, jp_var, i, jp, k, &lu);
+  flux_adj(lD + m2p, x, xjp, fy<R, true, IN>(g, P.u2, i, j + 1, k), true, A.lx, i, j, k, jp_var, i, jp, k, &lu);
   fy_add<R, true, IN>(g, A.gu2, i, j + 1, k, lu);
-  flux_adj(-lD, xjm, x, P.u2.ld(i, j, k), jm_var, A.lx, i, jm, k, true, i, j, k, &lu);
+  flux_adj(-lD + m2, xjm, x, P.u2.ld(i, j, k), jm_var, A.lx, i, jm, k, true, i, j, k, &lu);
   fy_add<R, true, IN>(g, A.gu2, i, j, k, lu);
-  if (!IN && !g.bz && k == 1) {  // F3(1) = -F3(2): D = ... + 2*F3(2)
-    flux_adj(R(2) * lD, x, psi.ld(i, j, k + 1), P.u3.ld(i, j, k + 1), true, A.lx, i, j, k, true, i, j, k + 1, &lu);
+  if (!IN && !g.bz && k == 1) {  // F3(1) = -F3(2): D = ... + 2*F3(2); the flux stored for face 1 is -F3(2)
+    flux_adj(R(2) * lD - m3, x, psi.ld(i, j, k + 1), P.u3.ld(i, j, k + 1), true, A.lx, i, j, k, true, i, j, k + 1,
+             &lu);
     addat(A.gu3, i, j, k + 1, lu);
-  } else if (!IN && !g.bz && k == g.lp) {  // F3(lp+1) = -F3(lp): D = ... - 2*F3(lp)
-    flux_adj(-R(2) * lD, psi.ld(i, j, k - 1), x, P.u3.ld(i, j, k), true, A.lx, i, j, k - 1, true, i, j, k, &lu);
+  } else if (!IN && !g.bz && k == g.lp) {  // F3(lp+1) = -F3(lp): D = ... - 2*F3(lp); face lp+1 stores -F3(lp)
+    flux_adj(-R(2) * lD + m3 - m3p, psi.ld(i, j, k - 1), x, P.u3.ld(i, j, k), true, A.lx, i, j, k - 1, true, i, j,
+             k, &lu);
     addat(A.gu3, i, j, k, lu);
   } else {
     const int kp = cz<IN>(g, k + 1), km = cz<IN>(g, k - 1);
-    flux_adj(lD, x, psi.ld(i, j, kp), fz<R, true, IN>(g, P.u3, i, j, k + 1), true, A.lx, i, j, k, true, i, j, kp, &lu);
+    flux_adj(lD + m3p, x, psi.ld(i, j, kp), fz<R, true, IN>(g, P.u3, i, j, k + 1), true, A.lx, i, j, k, true, i,
+             j, kp, &lu);
     fz_add<R, true, IN>(g, A.gu3, i, j, k + 1, lu);
-    flux_adj(-lD, psi.ld(i, j, km), x, P.u3.ld(i, j, k), true, A.lx, i, j, km, true, i, j, k, &lu);
+    flux_adj(-lD + m3, psi.ld(i, j, km), x, P.u3.ld(i, j, k), true, A.lx, i, j, km, true, i, j, k, &lu);
     fz_add<R, true, IN>(g, A.gu3, i, j, k, lu);
   }
 }
-template <class R>
+template <class R, bool MF = false>
 __global__ void KA_LB_UPWIND ka_upwind(const Prob<R> P, const AdjArr<R> A) {
-#define C(IN) ka_upwind_cell<R, IN>(P, A, i, j, k)
+#define C(IN) ka_upwind_cell<R, IN, MF>(P, A, i, j, k)
   ADISPATCH(C)
 #undef C
+}
+
+// Density step: the mass flux of every face adds the last pass's limited
+// flux as the forward reads it (fx/fy/fz of the stored faces: the periodic
+// wrap, the zero open walls, the mirrored z faces), so its cotangent goes to
+// that flux's adjoint through the same read maps.
+template <class R>
+__global__ void __launch_bounds__(128) ka_mass_to_w(const Prob<R> P, const AdjArr<R> A) {
+  ACELL
+  fx_add<R, false>(g, A.lw1, i, j, k, A.lm1.ld(i, j, k));
+  fy_add<R, false>(g, A.lw2, i, j, k, A.lm2.ld(i, j, k));
+  fz_add<R, false>(g, A.lw3, i, j, k, A.lm3.ld(i, j, k));
+  if (i == g.np) fx_add<R, false>(g, A.lw1, g.np + 1, j, k, A.lm1.ld(g.np + 1, j, k));
+  if (j == g.mp) fy_add<R, false>(g, A.lw2, i, g.mp + 1, k, A.lm2.ld(i, g.mp + 1, k));
+  if (k == g.lp) fz_add<R, false>(g, A.lw3, i, j, g.lp + 1, A.lm3.ld(i, j, g.lp + 1));
+}
+
+// Reverse of the density step's outputs (rho_out_body): x_incomp = x*h,
+// pexr1 = x_incomp*pexe, pexr2 = x_incomp, rhr = rhoadv/x_incomp with rhoadv
+// the x_incomp input.  lam (dJ/dpsi after the step) gains h*dJ/dx_incomp;
+// g_xinc and g_pexe receive dJ/d(x_incomp input) and dJ/dpexe.  Null
+// cotangent arrays are zeros.
+template <class R>
+__global__ void __launch_bounds__(128) ka_rho_out(const Prob<R> P, const Arr<R> out, const Arr<R> lxc,
+                                                  const Arr<R> lp1, const Arr<R> lp2, const Arr<R> lrh, Arr<R> lam,
+                                                  Arr<R> g_xinc, Arr<R> g_pexe) {
+  ACELL
+  (void)g;
+  const R h = P.h.ld(i, j, k);
+  const R xc = out.ld(i, j, k) * h;
+  const R pe = P.pexe.ld(i, j, k), ra = P.x_incomp.ld(i, j, k);
+  const R a_xc = lxc.p ? lxc.ld(i, j, k) : R(0), a_p1 = lp1.p ? lp1.ld(i, j, k) : R(0),
+          a_p2 = lp2.p ? lp2.ld(i, j, k) : R(0), a_rh = lrh.p ? lrh.ld(i, j, k) : R(0);
+  const R l_xc = a_xc + a_p1 * pe + a_p2 - a_rh * (ra / xc) / xc;
+  lam.at(i, j, k) = lam.ld(i, j, k) + l_xc * h;
+  g_xinc.at(i, j, k) = a_rh / xc;
+  g_pexe.at(i, j, k) = a_p1 * xc;
 }
 
 template <class R>
@@ -1079,6 +1134,17 @@ int run_step_reverse(const Prob<R>& P, const AdjPlan<R>& A, int nonos, cudaStrea
   const int np_ = A.npass;
   int n = 0;
   if (cudaMemsetAsync(A.acc, 0, A.acc_elems * sizeof(R), s) != cudaSuccess) return -5;
+  if (A.rho && A.lm1.p) {  // the density step's mass fluxes read the last pass's limited fluxes
+    AdjArr<R> m{};
+    m.lw1 = A.lw[np_ - 1][0];
+    m.lw2 = A.lw[np_ - 1][1];
+    m.lw3 = A.lw[np_ - 1][2];
+    m.lm1 = A.lm1;
+    m.lm2 = A.lm2;
+    m.lm3 = A.lm3;
+    ka_mass_to_w<R><<<grd, blk, 0, s>>>(P, m);
+    n++;
+  }
   // ---- reverse, last pass first
   for (int t = np_ - 1; t >= 0; t--) {
     if (t < np_ - 1 && cudaMemsetAsync(A.pass_acc, 0, A.pass_acc_elems * sizeof(R), s) != cudaSuccess) return -5;
@@ -1161,7 +1227,14 @@ int run_step_reverse(const Prob<R>& P, const AdjPlan<R>& A, int nonos, cudaStrea
   a0.gu2 = A.gu2;
   a0.gu3 = A.gu3;
   a0.lam = A.lam;
-  ka_upwind<R><<<grd, blk, 0, s>>>(P, a0);
+  if (A.rho && A.lm1.p) {
+    a0.lm1 = A.lm1;
+    a0.lm2 = A.lm2;
+    a0.lm3 = A.lm3;
+    ka_upwind<R, true><<<grd, blk, 0, s>>>(P, a0);
+  } else {
+    ka_upwind<R><<<grd, blk, 0, s>>>(P, a0);
+  }
   ka_store<R><<<grd, blk, 0, s>>>(P, a0);
   n += 2;
   add_launches(n);
@@ -1172,6 +1245,18 @@ template <class R>
 int run_step_adjoint(const Prob<R>& P, const AdjPlan<R>& A, int nonos, cudaStream_t s) {
   const int rc = run_step_record<R>(P, A, nonos, nullptr, s);
   return rc ? rc : run_step_reverse<R>(P, A, nonos, s);
+}
+
+template <class R>
+int run_rho_out_adjoint(const Prob<R>& P, const Arr<R>& out, const Arr<R>& lxc, const Arr<R>& lp1,
+                        const Arr<R>& lp2, const Arr<R>& lrh, const Arr<R>& lam, const Arr<R>& g_xinc,
+                        const Arr<R>& g_pexe, cudaStream_t s) {
+  const Geo& g = P.g;
+  const dim3 blk(32, 4, 1);
+  const dim3 grd((g.np + 31) / 32, (g.mp + 3) / 4, g.lp);
+  ka_rho_out<R><<<grd, blk, 0, s>>>(P, out, lxc, lp1, lp2, lrh, lam, g_xinc, g_pexe);
+  add_launches(1);
+  return cudaGetLastError() == cudaSuccess ? 0 : -5;
 }
 
 template <class R>
@@ -1192,6 +1277,12 @@ template int run_step_record<float>(const Prob<float>&, const AdjPlan<float>&, i
                                     cudaStream_t);
 template int run_step_reverse<double>(const Prob<double>&, const AdjPlan<double>&, int, cudaStream_t);
 template int run_step_reverse<float>(const Prob<float>&, const AdjPlan<float>&, int, cudaStream_t);
+template int run_rho_out_adjoint<double>(const Prob<double>&, const Arr<double>&, const Arr<double>&,
+                                         const Arr<double>&, const Arr<double>&, const Arr<double>&,
+                                         const Arr<double>&, const Arr<double>&, const Arr<double>&, cudaStream_t);
+template int run_rho_out_adjoint<float>(const Prob<float>&, const Arr<float>&, const Arr<float>&, const Arr<float>&,
+                                        const Arr<float>&, const Arr<float>&, const Arr<float>&, const Arr<float>&,
+                                        const Arr<float>&, cudaStream_t);
 template int run_seed<double>(const Prob<double>&, const Arr<double>&, const Arr<double>&, const Arr<double>&, cudaStream_t);
 template int run_seed<float>(const Prob<float>&, const Arr<float>&, const Arr<float>&, const Arr<float>&, cudaStream_t);
 

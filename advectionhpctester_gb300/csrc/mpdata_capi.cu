@@ -1271,6 +1271,8 @@ int adj_plan(Workspace* w, Prob<R>* P, AdjPlan<R>* A, const R* psi_in, const R* 
   A->gu1 = caller_view<R>(gu1, ih, sx + 1, sy);
   A->gu2 = caller_view<R>(gu2, ih, sx, sy + 1);
   A->gu3 = caller_view<R>(gu3, ih, sx, sy);
+  A->rho = false;
+  A->lm1 = A->lm2 = A->lm3 = Arr<R>{nullptr, 0, 0};
   return MPDATA_OK;
 }
 
@@ -1442,9 +1444,94 @@ int adjoint_run_impl(void* ws, int nsteps, int interval, R* psi, const R* u1, co
   return rc;
 }
 
+template <class R>
+__global__ void __launch_bounds__(256) k_fill(R* p, size_t n, R v) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+    p[t] = v;
+}
+
+// Adjoint of the density step after its predictor: the forward is recorded
+// with the density step's arithmetic (upwind without rhr, division by h),
+// the outputs' reverse turns the x_incomp, pexr and rhr cotangents into one
+// of psi, and the step's reverse adds the mass fluxes' cotangents to the
+// upwind and last limited fluxes.  The reverse kernels read a field of ones
+// as rhr (the density step has none).
+template <class R>
+int rho_adjoint_impl(void* ws, const R* u1, const R* u2, const R* u3, const R* x_in, const R* x_incomp, const R* h,
+                     const R* pexe, const R* bcx, const R* bcy, R* lambda, const R* l_u1, const R* l_u2,
+                     const R* l_u3, const R* l_xincomp, const R* l_pexr1, const R* l_pexr2, const R* l_rhr, R* g_u1,
+                     R* g_u2, R* g_u3, R* g_xincomp, R* g_pexe, void* stream) {
+  Workspace* w = as_ws(ws);
+  if (!w) return MPDATA_E_WS;
+  if (w->elem != sizeof(R)) return MPDATA_E_WS;
+  if (!w->o.gauge) return MPDATA_E_OPTS;  // the reference's density step is the gauge form
+  if (!x_incomp || !pexe || !g_xincomp || !g_pexe) return MPDATA_E_NULL;
+  if ((l_u1 || l_u2 || l_u3) && !(l_u1 && l_u2 && l_u3)) return MPDATA_E_NULL;
+  const mpdata_grid& g = w->g;
+  const int ih = g.ih, sx = g.np + 2 * ih, sy = g.mp + 2 * ih;
+  const size_t plen = (size_t)sx * sy * (g.lp + 2 * ih);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  R* buf = nullptr;  // rhr's ones (psi-shaped), then the step's output field (interior)
+  if (cudaMallocAsync(&buf, (plen + w->ncell) * sizeof(R), s) != cudaSuccess) {
+    cudaGetLastError();
+    return MPDATA_E_CUDA;
+  }
+  k_fill<R><<<1216, 256, 0, s>>>(buf, plen, R(1));
+  add_launches(1);
+  Prob<R> P;
+  AdjPlan<R> A;
+  int rc = adj_plan<R>(w, &P, &A, x_in, u1, u2, u3, h, buf, bcx, bcy, lambda, g_u1, g_u2, g_u3);
+  if (!rc) {
+    w->last = s;
+    P.rho = 1;
+    P.x_incomp = caller_view<R>(const_cast<R*>(x_incomp), ih, sx, sy);
+    P.pexe = caller_view<R>(const_cast<R*>(pexe), ih, sx, sy);
+    P.rhoadv = A.lq;  // the recorded upwind copies x_incomp there; the reverse clears it
+    R* hi = static_cast<R*>(w->mem) + (size_t)NSCRATCH * w->ncell;
+    P.f1hi = hi;
+    P.f2hi = hi + (size_t)g.mp * g.lp;
+    P.f3hi = hi + (size_t)g.mp * g.lp + (size_t)g.np * g.lp;
+    A.rho = true;
+    if (l_u1) {
+      A.lm1 = caller_view<R>(const_cast<R*>(l_u1), ih, sx + 1, sy);
+      A.lm2 = caller_view<R>(const_cast<R*>(l_u2), ih, sx, sy + 1);
+      A.lm3 = caller_view<R>(const_cast<R*>(l_u3), ih, sx, sy);
+    }
+    const Arr<R> out = scratch_view<R>(buf + plen, P.g);
+    auto cv = [&](const R* p) { return p ? caller_view<R>(const_cast<R*>(p), ih, sx, sy) : Arr<R>{nullptr, 0, 0}; };
+    if (run_step_record<R>(P, A, w->o.nonos, &out, s) ||
+        run_rho_out_adjoint<R>(P, out, cv(l_xincomp), cv(l_pexr1), cv(l_pexr2), cv(l_rhr), A.lam,
+                               caller_view<R>(g_xincomp, ih, sx, sy), caller_view<R>(g_pexe, ih, sx, sy), s) ||
+        run_step_reverse<R>(P, A, w->o.nonos, s))
+      rc = MPDATA_E_CUDA;
+  }
+  cudaFreeAsync(buf, s);
+  return rc;
+}
+
 }  // namespace
 
 extern "C" {
+
+int mpdata_rho_gauge_adjoint_f64(void* ws, const double* u1, const double* u2, const double* u3,
+                                 const double* x_in, const double* x_incomp, const double* h,
+                                 const double* pexe, const double* bcx, const double* bcy, double* lambda,
+                                 const double* l_u1, const double* l_u2, const double* l_u3,
+                                 const double* l_xincomp, const double* l_pexr1, const double* l_pexr2,
+                                 const double* l_rhr, double* g_u1, double* g_u2, double* g_u3,
+                                 double* g_xincomp, double* g_pexe, void* stream) {
+  return rho_adjoint_impl<double>(ws, u1, u2, u3, x_in, x_incomp, h, pexe, bcx, bcy, lambda, l_u1, l_u2, l_u3,
+                                  l_xincomp, l_pexr1, l_pexr2, l_rhr, g_u1, g_u2, g_u3, g_xincomp, g_pexe, stream);
+}
+int mpdata_rho_gauge_adjoint_f32(void* ws, const float* u1, const float* u2, const float* u3, const float* x_in,
+                                 const float* x_incomp, const float* h, const float* pexe, const float* bcx,
+                                 const float* bcy, float* lambda, const float* l_u1, const float* l_u2,
+                                 const float* l_u3, const float* l_xincomp, const float* l_pexr1,
+                                 const float* l_pexr2, const float* l_rhr, float* g_u1, float* g_u2, float* g_u3,
+                                 float* g_xincomp, float* g_pexe, void* stream) {
+  return rho_adjoint_impl<float>(ws, u1, u2, u3, x_in, x_incomp, h, pexe, bcx, bcy, lambda, l_u1, l_u2, l_u3,
+                                 l_xincomp, l_pexr1, l_pexr2, l_rhr, g_u1, g_u2, g_u3, g_xincomp, g_pexe, stream);
+}
 
 int mpdata_step_adjoint_f64(void* ws, const double* psi_in, const double* u1, const double* u2,
                             const double* u3, const double* h, const double* rhr, const double* bcx,

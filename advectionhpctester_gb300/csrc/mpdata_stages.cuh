@@ -93,6 +93,8 @@ struct AdjArr {
   Arr<R> lg1, lg2, lg3;     // adjoints of the limited donor fluxes of x/rhr
   Arr<R> lf1, lf2, lf3;     // adjoints of the unlimited donor fluxes f*ns
   Arr<R> lq;                // adjoint of q = x/rhr
+  // density step: cotangents of its mass fluxes (caller C-grid arrays, faces 1..n+1)
+  Arr<R> lm1, lm2, lm3;
 };
 
 // Arena of the step adjoint: per-pass forward records and accumulators.
@@ -114,6 +116,11 @@ struct AdjPlan {
   R* acc;                                       // the accumulators, contiguous
   size_t acc_elems, pass_acc_elems;             // all of them; the per-pass block (lv, lcp, lcn)
   R* pass_acc;
+  // density step (mpdata_rho_gauge_adjoint_*): the upwind divides by h
+  // without rhr, and the mass fluxes (upwind flux + the last pass's limited
+  // flux on every face) take the cotangents lm1..lm3 (p null when absent)
+  bool rho;
+  Arr<R> lm1, lm2, lm3;
 };
 // Fields of the arena for iord passes: records, then accumulators.
 // records per pass: x, v*3, w*3, cp, cn, mx, mn, fns*3, q
@@ -129,6 +136,13 @@ template <class R>
 int run_step_reverse(const Prob<R>& P, const AdjPlan<R>& A, int nonos, cudaStream_t s);
 template <class R>
 int run_seed(const Prob<R>& P, const Arr<R>& psi, const Arr<R>& target, const Arr<R>& lam, cudaStream_t s);
+// Reverse of the density step's outputs (x_incomp, pexr1/2, rhr) from the
+// step's output field `out`: adds h*dJ/dx_incomp into lam and writes
+// dJ/d(x_incomp input) and dJ/dpexe (null cotangent arrays are zeros).
+template <class R>
+int run_rho_out_adjoint(const Prob<R>& P, const Arr<R>& out, const Arr<R>& lxc, const Arr<R>& lp1,
+                        const Arr<R>& lp2, const Arr<R>& lrh, const Arr<R>& lam, const Arr<R>& g_xinc,
+                        const Arr<R>& g_pexe, cudaStream_t s);
 
 unsigned long long launch_count();
 void add_launches(int n);

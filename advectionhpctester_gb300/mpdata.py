@@ -173,6 +173,28 @@ class Workspace:
     # the reference's name for the density step
     mpdata3d_rho_gauge_gpubc = rho_gauge
 
+    def rho_gauge_adjoint(self, u1, u2, u3, x_in, x_incomp, h, pexe, lam, g_u1, g_u2, g_u3, g_xincomp, g_pexe,
+                          l_u1=None, l_u2=None, l_u3=None, l_xincomp=None, l_pexr1=None, l_pexr2=None,
+                          l_rhr=None, bcx=None, bcy=None, stream=None):
+        """Reverse of the density step after its predictor (mpdata_rho_gauge_adjoint_*):
+        u1..u3 are the C-grid Courant numbers the step advected with, x_in and
+        x_incomp its inputs.  lam (dJ/dpsi after the step) becomes dJ/dpsi
+        before it; the l_* cotangents of the mass fluxes, x_incomp, pexr1,
+        pexr2 and rhr (None: zero) enter too.  dJ/du is added into
+        g_u1..g_u3; g_xincomp and g_pexe receive dJ/d(x_incomp input) and
+        dJ/dpexe on the interior."""
+        s, d = self.shapes, self.dtype
+        fn = (self.lib.mpdata_rho_gauge_adjoint_f64 if self.opts.precision == 64
+              else self.lib.mpdata_rho_gauge_adjoint_f32)
+        ps = lambda t, n: _ptr(t, d, s["psi"], n)
+        check(fn(self.handle, _ptr(u1, d, s["u1"], "u1"), _ptr(u2, d, s["u2"], "u2"), _ptr(u3, d, s["u3"], "u3"),
+                 ps(x_in, "x_in"), ps(x_incomp, "x_incomp"), ps(h, "h"), ps(pexe, "pexe"),
+                 _ptr(bcx, d, s["bcx"], "bcx"), _ptr(bcy, d, s["bcy"], "bcy"), ps(lam, "lam"),
+                 _ptr(l_u1, d, s["u1"], "l_u1"), _ptr(l_u2, d, s["u2"], "l_u2"), _ptr(l_u3, d, s["u3"], "l_u3"),
+                 ps(l_xincomp, "l_xincomp"), ps(l_pexr1, "l_pexr1"), ps(l_pexr2, "l_pexr2"), ps(l_rhr, "l_rhr"),
+                 _ptr(g_u1, d, s["u1"], "g_u1"), _ptr(g_u2, d, s["u2"], "g_u2"), _ptr(g_u3, d, s["u3"], "g_u3"),
+                 ps(g_xincomp, "g_xincomp"), ps(g_pexe, "g_pexe"), _stream(stream)), "mpdata_rho_gauge_adjoint")
+
     def step_adjoint(self, psi_in, u1, u2, u3, h, rhr, lam, g_u1, g_u2, g_u3, bcx=None, bcy=None,
                      stream=None):
         """Reverse of one step: lam (dJ/dpsi_new) becomes dJ/dpsi_in; dJ/du is

@@ -192,6 +192,33 @@ int mpdata_step_adjoint_f32(void* ws, const float* psi_in, const float* u1, cons
                             const float* u3, const float* h, const float* rhr, const float* bcx,
                             const float* bcy, float* lambda, float* g_u1, float* g_u2, float* g_u3,
                             void* stream);
+/* Adjoint of the density step after its predictor: the reverse of
+ * mpdata_rho_gauge_* from the C-grid Courant numbers u1..u3 it advects with
+ * (the predictor's output; mpdata_velprd_adjoint_* carries dJ/du on to the
+ * momenta).  Inputs as the forward read them: u1..u3, x_in (psi at the start
+ * of the step), x_incomp (its input, which the step copies into rhoadv), h,
+ * pexe, bcx, bcy.  Cotangents of the step's outputs: lambda (dJ/dpsi after
+ * the step; on exit dJ/dpsi before it), l_u1..l_u3 (the mass fluxes on faces
+ * 1..n+1; all three or none), l_xincomp, l_pexr1, l_pexr2, l_rhr (any may be
+ * NULL: zero).  g_u1..g_u3 accumulate dJ/du; g_xincomp and g_pexe receive
+ * dJ/d(x_incomp input) and dJ/dpexe on the interior.  h is held fixed.  The
+ * workspace must be gauge (MPDATA_E_OPTS) with iord >= 2; the forward is
+ * recomputed into the adjoint arena.  Results match the FP64 AD oracle to
+ * rounding. */
+int mpdata_rho_gauge_adjoint_f64(void* ws, const double* u1, const double* u2, const double* u3,
+                                 const double* x_in, const double* x_incomp, const double* h,
+                                 const double* pexe, const double* bcx, const double* bcy, double* lambda,
+                                 const double* l_u1, const double* l_u2, const double* l_u3,
+                                 const double* l_xincomp, const double* l_pexr1, const double* l_pexr2,
+                                 const double* l_rhr, double* g_u1, double* g_u2, double* g_u3,
+                                 double* g_xincomp, double* g_pexe, void* stream);
+int mpdata_rho_gauge_adjoint_f32(void* ws, const float* u1, const float* u2, const float* u3,
+                                 const float* x_in, const float* x_incomp, const float* h,
+                                 const float* pexe, const float* bcx, const float* bcy, float* lambda,
+                                 const float* l_u1, const float* l_u2, const float* l_u3,
+                                 const float* l_xincomp, const float* l_pexr1, const float* l_pexr2,
+                                 const float* l_rhr, float* g_u1, float* g_u2, float* g_u3,
+                                 float* g_xincomp, float* g_pexe, void* stream);
 int mpdata_adjoint_run_f64(void* ws, int nsteps, int interval, double* psi, const double* u1,
                            const double* u2, const double* u3, const double* h, const double* rhr,
                            const double* bcx, const double* bcy, const double* target, double* J,

@@ -570,6 +570,11 @@ template <class R>
 int rho_gauge(const orc_grid* g, R* ox, R* oy, R* oz, R* pu, R* pv, R* pw, R* u1o, R* u2o, R* u3o,
               R* x_in, R* x_incomp, const R* h_in, R* rhoadv, R* rhr_out, const R* pexe, R* pexr1,
               R* pexr2, const R* bcx, const R* bcy, R dxi, R dyi, R dzi, R dt, R dt_ratio, int liner);
+// The density step after the predictor: u1o..u3o hold the C-grid Courant
+// numbers on entry and the mass fluxes on exit.
+template <class R>
+int rho_step(const orc_grid* g, R* u1o, R* u2o, R* u3o, R* x_in, R* x_incomp, const R* h_in, R* rhoadv,
+             R* rhr_out, const R* pexe, R* pexr1, R* pexr2, const R* bcx, const R* bcy, int liner);
 
 bool dims_ok(const orc_grid* g) {
   if (!g) return false;
@@ -981,6 +986,13 @@ int rho_gauge(const orc_grid* g, R* ox, R* oy, R* oz, R* pu, R* pv, R* pw, R* u1
   // velprd_driver (:106-111): predictor into u1..u3, level roll
   int rc = velprd<R>(g, ox, oy, oz, pu, pv, pw, h_in, dxi, dyi, dzi, dt, dt_ratio, u1o, u2o, u3o);
   if (rc) return rc;
+  return rho_step<R>(g, u1o, u2o, u3o, x_in, x_incomp, h_in, rhoadv, rhr_out, pexe, pexr1, pexr2, bcx, bcy, liner);
+}
+
+template <class R>
+int rho_step(const orc_grid* g, R* u1o, R* u2o, R* u3o, R* x_in, R* x_incomp, const R* h_in, R* rhoadv,
+             R* rhr_out, const R* pexe, R* pexr1, R* pexr2, const R* bcx, const R* bcy, int liner) {
+  const Dims d{g->np, g->mp, g->lp, g->ih, g->ibcx, g->ibcy, g->ibcz};
   const R ep = R(1e-10);
   const int NX = d.np + 2, NY = d.mp + 2, NZ = d.lp + 2, ih = d.ih;
   const int SX = d.np + 2 * ih, SY = d.mp + 2 * ih;
@@ -1180,6 +1192,17 @@ int orc_tangent_adjoint_f64(const orc_grid* g, int t_adv, int iord, int nonos, i
                             const double* dx0, const double* du1, const double* du2, const double* du3,
                             double* dJ_tl);
 
+// The density step after its predictor (rho_step): u1..u3 hold the C-grid
+// Courant numbers on entry and the mass fluxes on exit.
+int orc_rho_step_f64(const orc_grid* g, double* u1, double* u2, double* u3, double* x_in, double* x_incomp,
+                     const double* h, double* rhoadv, double* rhr, const double* pexe, double* pexr1,
+                     double* pexr2, const double* bcx, const double* bcy, int liner) {
+  if (!dims_ok(g)) return -1;
+  if (!u1 || !u2 || !u3 || !x_in || !x_incomp || !h || !rhoadv || !rhr || !pexe || !pexr1 || !pexr2) return -3;
+  if ((!g->ibcx && !bcx) || (!g->ibcy && !bcy)) return -3;
+  return rho_step<double>(g, u1, u2, u3, x_in, x_incomp, h, rhoadv, rhr, pexe, pexr1, pexr2, bcx, bcy, liner);
+}
+
 // Un-checkpointed FP64 adjoint by reverse-mode AD of the oracle's own step:
 // J = 0.5*sum((x_N - target)^2) over the interior after nsteps steps with a
 // fixed velocity; gradients with respect to x_0 (interior) and every element
@@ -1276,6 +1299,104 @@ int orc_tangent_adjoint_f64(const orc_grid* g, int t_adv, int iord, int nonos, i
   for (long e = 0; e < n1; e++) gu1[e] = adj[uid1 + e];
   for (long e = 0; e < n2; e++) gu2[e] = adj[uid2 + e];
   for (long e = 0; e < n3; e++) gu3[e] = adj[uid3 + e];
+  g_tape = nullptr;
+  g_threads = saved;
+  return 0;
+}
+
+// Reverse-mode AD of the density step after its predictor (rho_step): the
+// checker of mpdata_rho_gauge_adjoint_*.  The step's outputs, psi (x_in),
+// x_incomp, pexr1, pexr2 and rhr on the interior and the mass fluxes u1..u3 on
+// the faces 1..n+1, are seeded with the given cotangents (NULL: zero); the
+// gradients are with respect to the interior of the input psi, every element
+// of the C-grid Courant numbers u1..u3, and the interiors of the x_incomp
+// input and of pexe.  h, bcx and bcy are constants.  Single-threaded (one
+// global tape).
+int orc_rho_adjoint_f64(const orc_grid* g, const double* u1, const double* u2, const double* u3,
+                        const double* x_in, const double* x_incomp, const double* h, const double* pexe,
+                        const double* bcx, const double* bcy, const double* l_x, const double* l_u1,
+                        const double* l_u2, const double* l_u3, const double* l_xinc, const double* l_p1,
+                        const double* l_p2, const double* l_rhr, double* g_x, double* g_u1, double* g_u2,
+                        double* g_u3, double* g_xinc, double* g_pexe) {
+  if (!dims_ok(g)) return -1;
+  if (!u1 || !u2 || !u3 || !x_in || !x_incomp || !h || !pexe || !g_x || !g_u1 || !g_u2 || !g_u3 || !g_xinc ||
+      !g_pexe)
+    return -3;
+  if ((!g->ibcx && !bcx) || (!g->ibcy && !bcy)) return -3;
+  const int ih = g->ih;
+  const long SX = g->np + 2 * ih, SY = g->mp + 2 * ih, SZ = g->lp + 2 * ih;
+  const long nps = SX * SY * SZ, n1 = (SX + 1) * SY * SZ, n2 = SX * (SY + 1) * SZ, n3 = SX * SY * (SZ + 1);
+  Tape tape;
+  g_tape = &tape;
+  const int saved = g_threads;
+  g_threads = 1;
+  auto var = [&](double v) { AD r(v); r.id = tape.push(-1, 0.0, -1, 0.0); return r; };
+  auto interior = [&](long e) {
+    const long i = e % SX, j = (e / SX) % SY, k = e / (SX * SY);
+    return i >= ih && i < ih + g->np && j >= ih && j < ih + g->mp && k >= ih && k < ih + g->lp;
+  };
+  std::vector<AD> X(nps), XC(nps), H(nps), PE(nps), RA(nps), RO(nps), P1(nps), P2(nps), U1(n1), U2(n2), U3(n3);
+  std::vector<AD> BX(bcx ? (size_t)g->mp * g->lp * 2 : 0), BY(bcy ? (size_t)g->np * g->lp * 2 : 0);
+  std::vector<int> xid(nps, -1), cid(nps, -1), pid(nps, -1);
+  for (long e = 0; e < nps; e++) {
+    const bool in = interior(e);
+    X[e] = in ? var(x_in[e]) : AD(x_in[e]);
+    XC[e] = in ? var(x_incomp[e]) : AD(x_incomp[e]);
+    PE[e] = in ? var(pexe[e]) : AD(pexe[e]);
+    xid[e] = X[e].id;
+    cid[e] = XC[e].id;
+    pid[e] = PE[e].id;
+    H[e] = AD(h[e]);
+  }
+  for (long e = 0; e < n1; e++) U1[e] = var(u1[e]);
+  for (long e = 0; e < n2; e++) U2[e] = var(u2[e]);
+  for (long e = 0; e < n3; e++) U3[e] = var(u3[e]);
+  for (size_t e = 0; e < BX.size(); e++) BX[e] = AD(bcx[e]);
+  for (size_t e = 0; e < BY.size(); e++) BY[e] = AD(bcy[e]);
+  const int uid1 = U1[0].id, uid2 = U2[0].id, uid3 = U3[0].id;
+  const int rc = rho_step<AD>(g, U1.data(), U2.data(), U3.data(), X.data(), XC.data(), H.data(), RA.data(),
+                              RO.data(), PE.data(), P1.data(), P2.data(), bcx ? BX.data() : nullptr,
+                              bcy ? BY.data() : nullptr, 0);
+  if (rc) {
+    g_tape = nullptr;
+    g_threads = saved;
+    return rc;
+  }
+  std::vector<double> adj(tape.a.size(), 0.0);
+  auto seed = [&](const AD& a, const double* c, long e) {
+    if (c && a.id >= 0) adj[a.id] += c[e];
+  };
+  for (long e = 0; e < nps; e++) {
+    if (!interior(e)) continue;
+    seed(X[e], l_x, e);
+    seed(XC[e], l_xinc, e);
+    seed(P1[e], l_p1, e);
+    seed(P2[e], l_p2, e);
+    seed(RO[e], l_rhr, e);
+  }
+  // the mass fluxes: faces 1..n+1 along their own axis
+  for (int k = 1; k <= g->lp + 1; k++)
+    for (int j = 1; j <= g->mp + 1; j++)
+      for (int i = 1; i <= g->np + 1; i++) {
+        const long i0 = i - 1 + ih, j0 = j - 1 + ih, k0 = k - 1 + ih;
+        if (j <= g->mp && k <= g->lp) seed(U1[i0 + j0 * (SX + 1) + k0 * (SX + 1) * SY], l_u1, i0 + j0 * (SX + 1) + k0 * (SX + 1) * SY);
+        if (i <= g->np && k <= g->lp) seed(U2[i0 + j0 * SX + k0 * SX * (SY + 1)], l_u2, i0 + j0 * SX + k0 * SX * (SY + 1));
+        if (i <= g->np && j <= g->mp) seed(U3[i0 + j0 * SX + k0 * SX * SY], l_u3, i0 + j0 * SX + k0 * SX * SY);
+      }
+  for (long n = (long)tape.a.size() - 1; n >= 0; n--) {
+    const double an = adj[n];
+    if (an == 0.0) continue;
+    if (tape.a[n] >= 0) adj[tape.a[n]] += tape.da[n] * an;
+    if (tape.b[n] >= 0) adj[tape.b[n]] += tape.db[n] * an;
+  }
+  for (long e = 0; e < nps; e++) {
+    g_x[e] = xid[e] >= 0 ? adj[xid[e]] : 0.0;
+    g_xinc[e] = cid[e] >= 0 ? adj[cid[e]] : 0.0;
+    g_pexe[e] = pid[e] >= 0 ? adj[pid[e]] : 0.0;
+  }
+  for (long e = 0; e < n1; e++) g_u1[e] = adj[uid1 + e];
+  for (long e = 0; e < n2; e++) g_u2[e] = adj[uid2 + e];
+  for (long e = 0; e < n3; e++) g_u3[e] = adj[uid3 + e];
   g_tape = nullptr;
   g_threads = saved;
   return 0;

@@ -135,6 +135,25 @@ int orc_adjoint_f64(const orc_grid* g, int t_adv, int iord, int nonos, int nstep
                     const double* u3, const double* rhr, const double* h, const double* target,
                     double* J, double* xN, double* gx0, double* gu1, double* gu2, double* gu3);
 
+/* The density step of orc_rho_gauge_f64 after its predictor: u1..u3 hold the
+ * C-grid Courant numbers on entry and the mass fluxes on exit. */
+int orc_rho_step_f64(const orc_grid* g, double* u1, double* u2, double* u3, double* x_in, double* x_incomp,
+                     const double* h, double* rhoadv, double* rhr, const double* pexe, double* pexr1,
+                     double* pexr2, const double* bcx, const double* bcy, int liner);
+
+/* Reverse-mode AD of the density step after its predictor (the step of
+ * orc_rho_gauge_f64 from the C-grid Courant numbers on): the outputs psi,
+ * x_incomp, pexr1, pexr2, rhr (interiors) and the mass fluxes u1..u3 (faces
+ * 1..n+1) take the cotangents l_* (NULL: zero); returns dJ/dpsi_in and
+ * dJ/dx_incomp_in, dJ/dpexe (interiors, psi-shaped) and dJ/du1..u3 (every
+ * element, C-grid shaped).  h, bcx, bcy are constants. */
+int orc_rho_adjoint_f64(const orc_grid* g, const double* u1, const double* u2, const double* u3,
+                        const double* x_in, const double* x_incomp, const double* h, const double* pexe,
+                        const double* bcx, const double* bcy, const double* l_x, const double* l_u1,
+                        const double* l_u2, const double* l_u3, const double* l_xinc, const double* l_p1,
+                        const double* l_p2, const double* l_rhr, double* g_x, double* g_u1, double* g_u2,
+                        double* g_u3, double* g_xinc, double* g_pexe);
+
 /* orc_adjoint_f64 plus the tangent-linear model on the same tape: dJ_tl =
  * sum((x_N - target) * dx_N) for the directions dx0, du1..du3. */
 int orc_tangent_adjoint_f64(const orc_grid* g, int t_adv, int iord, int nonos, int nsteps, const double* x0,

@@ -54,6 +54,10 @@ def lib():
         _lib.orc_adjoint_f64.restype = I
         _lib.orc_tangent_adjoint_f64.argtypes = [ctypes.POINTER(OrcGrid), I, I, I, I] + [P] * 20
         _lib.orc_tangent_adjoint_f64.restype = I
+        _lib.orc_rho_adjoint_f64.argtypes = [ctypes.POINTER(OrcGrid)] + [P] * 23
+        _lib.orc_rho_step_f64.argtypes = [ctypes.POINTER(OrcGrid)] + [P] * 13 + [I]
+        _lib.orc_rho_step_f64.restype = I
+        _lib.orc_rho_adjoint_f64.restype = I
         _lib.orc_a_to_c_f64.argtypes = [ctypes.POINTER(OrcGrid)] + [P] * 6
         _lib.orc_a_to_c_f64.restype = I
         for name, R in (("f64", D), ("f32", F)):
@@ -167,6 +171,34 @@ def rho_gauge(g, ox, oy, oz, u1, u2, u3, x_in, x_incomp, h, rhoadv, rhr, pexe, p
                                  _ptr(bcx, d), _ptr(bcy, d), dxi, dyi, dzi, dt, dt_ratio, int(liner))
     if rc != 0:
         raise ValueError("oracle rho_gauge failed with code %d" % rc)
+
+
+def rho_step(g, u1, u2, u3, x_in, x_incomp, h, rhoadv, rhr, pexe, pexr1, pexr2, bcx, bcy, liner=0):
+    """The density step after its predictor, in place (u1..u3 become the mass fluxes)."""
+    d = np.float64
+    rc = lib().orc_rho_step_f64(ctypes.byref(g), _ptr(u1, d), _ptr(u2, d), _ptr(u3, d), _ptr(x_in, d),
+                                _ptr(x_incomp, d), _ptr(h, d), _ptr(rhoadv, d), _ptr(rhr, d), _ptr(pexe, d),
+                                _ptr(pexr1, d), _ptr(pexr2, d), _ptr(bcx, d), _ptr(bcy, d), int(liner))
+    if rc != 0:
+        raise ValueError("oracle rho_step failed with code %d" % rc)
+
+
+def rho_adjoint(g, u1, u2, u3, x_in, x_incomp, h, pexe, bcx, bcy, l_x=None, l_u1=None, l_u2=None, l_u3=None,
+                l_xinc=None, l_p1=None, l_p2=None, l_rhr=None):
+    """Reverse-mode AD of the density step after its predictor: returns
+    (dJ/dpsi_in, dJ/du1, dJ/du2, dJ/du3, dJ/dx_incomp_in, dJ/dpexe) for the
+    output cotangents l_* (None: zero)."""
+    d = np.float64
+    gx, gc, gp = (np.zeros_like(x_in, order="F") for _ in range(3))
+    g1, g2, g3 = (np.zeros_like(a, order="F") for a in (u1, u2, u3))
+    rc = lib().orc_rho_adjoint_f64(ctypes.byref(g), _ptr(u1, d), _ptr(u2, d), _ptr(u3, d), _ptr(x_in, d),
+                                   _ptr(x_incomp, d), _ptr(h, d), _ptr(pexe, d), _ptr(bcx, d), _ptr(bcy, d),
+                                   _ptr(l_x, d), _ptr(l_u1, d), _ptr(l_u2, d), _ptr(l_u3, d), _ptr(l_xinc, d),
+                                   _ptr(l_p1, d), _ptr(l_p2, d), _ptr(l_rhr, d), _ptr(gx, d), _ptr(g1, d),
+                                   _ptr(g2, d), _ptr(g3, d), _ptr(gc, d), _ptr(gp, d))
+    if rc != 0:
+        raise ValueError("oracle rho_adjoint failed with code %d" % rc)
+    return gx, g1, g2, g3, gc, gp
 
 
 def adjoint(g, x0, bcx, bcy, u1, u2, u3, rhr, h, target, t_adv=1, iord=2, nonos=1, nsteps=1):
