@@ -367,10 +367,12 @@ template <class R, bool U>
 struct FaceAdj {
   R la, lK, lcr4;
   __device__ __forceinline__ FaceAdj(R lv, R a, R hm, R xl, R xrr, R cr4) {
-    const R K = (fabs(a) - hmul<U>(a * a, hm)) * R(0.5);
-    la = lv * ((dabs(a) - hmul<U>(R(2) * a, hm)) * (xrr - xl) * R(0.5) - hmul<U>(R(0.03125) * cr4, hm));
+    // the products by powers of two run on the integer pipe (scale_down/up)
+    const R K = scale_down<1>(fabs(a) - hmul<U>(a * a, hm));
+    la = lv * (scale_down<1>((dabs(a) - hmul<U>(scale_up<1>(a), hm)) * (xrr - xl)) -
+               hmul<U>(scale_down<5>(cr4), hm));
     lK = lv * K;
-    lcr4 = negv(lv * hmul<U>(R(0.03125) * a, hm));
+    lcr4 = negv(lv * hmul<U>(scale_down<5>(a), hm));
   }
 };
 
@@ -944,10 +946,10 @@ __global__ void __launch_bounds__(128) kf_pairs(const Prob<R> P) {
   pairs_body<R, AIN, PV>(P, i, j, k);
 }
 // the forward stage's dispatch: unit face densities and pair sums (FP64),
-// and the stage kernel's five resident blocks per SM for FP64
+// and the stage kernel's seven resident blocks per SM for FP64
 template <class R>
 struct KfPseudoMinBlocks {
-  static constexpr int v = sizeof(R) == 8 ? 5 : 1;
+  static constexpr int v = sizeof(R) == 8 ? 7 : 1;
 };
 template <class R, bool AIN>
 __global__ void __launch_bounds__(128, KfPseudoMinBlocks<R>::v) kf_pseudo(const Prob<R> P) {

@@ -110,6 +110,20 @@ template <int S>
 __device__ __forceinline__ float scale_down(float x) {
   return x * (1.0f / (float)(1 << S));
 }
+// Products by 2^S the same way: a normal x whose exponent field e satisfies
+// e + S < 0x7FF gains S in the field; zeros pass, everything else multiplies.
+template <int S>
+__device__ __forceinline__ double scale_up(double x) {
+  const int hi = __double2hiint(x), lo = __double2loint(x);
+  const unsigned e = ((unsigned)hi >> 20) & 0x7FFu;
+  if (e - 1u < (unsigned)(0x7FE - S)) return __hiloint2double(hi + (S << 20), lo);
+  if ((((unsigned)hi << 1) | (unsigned)lo) == 0u) return x;
+  return mul_call(x, (double)(1LL << S));
+}
+template <int S>
+__device__ __forceinline__ float scale_up(float x) {
+  return x * (float)(1 << S);
+}
 
 // pp(y) = max(0,y), pn(y) = -min(0,y)  (mpdataoperators.inc:50-59)
 __device__ __forceinline__ double pp(double y) { return sgn(y) ? 0.0 : y; }

@@ -190,6 +190,74 @@ __global__ void __launch_bounds__(128) k_pred_cgrid(Geo g, long lev, R* ox, R* o
   }
 }
 
+// SMs of the current device (queried once).
+int num_sms() {
+  static int n = 0;
+  if (n < 1) {
+    int dev = 0, v = 0;
+    n = (cudaGetDevice(&dev) == cudaSuccess &&
+         cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0)
+            ? v
+            : 152;
+  }
+  return n;
+}
+
+// The C-grid averaging of level 1 (velprdA_to_C, module_velprd.f90:197-361)
+// as a march up the z columns: each thread owns the (i, j) column of a chunk
+// of planes and keeps the level-1 value of the plane below in a register, so
+// every plane is read once for the z faces.  The thread of the last cell in x
+// (y) also forms the face np+1 (mp+1), and the top chunk the faces lp+1.
+// Faces, wall extrapolations 2a(1)-a(2) and their halo writes are those of
+// k_pred_cgrid, expression for expression.
+template <class R>
+__global__ void __launch_bounds__(256, 6) k_pred_cgrid_z(Geo g, long lev, R* ox, R* oy, R* oz, Arr<R> h, Arr<R> u1,
+                                                      Arr<R> u2, Arr<R> u3, int kchunk) {
+  const int i = blockIdx.x * 32 + threadIdx.x + 1;
+  const int j = blockIdx.y * 8 + threadIdx.y + 1;
+  const int kb = blockIdx.z * kchunk + 1;
+  if (i > g.np || j > g.mp || kb > g.lp) return;
+  const int ke = min(g.lp, kb + kchunk - 1);
+  const Arr<R> A1{ox + lev, h.sy, h.sz}, A2{oy + lev, h.sy, h.sz}, A3{oz + lev, h.sy, h.sz};
+  const bool xe = i == g.np, ye = j == g.mp;
+  // level 1 below the chunk: the lower value of face kb
+  R b3;
+  if (kb > 1)
+    b3 = A3.ld(i, j, kb - 1);
+  else
+    b3 = g.bz ? A3.ld(i, j, g.lp) : R(2) * A3.ld(i, j, 1) - A3.ld(i, j, 2);
+  if (!g.bz && kb == 1) A3.at(i, j, 0) = b3;
+  for (int k = kb; k <= ke; k++) {
+    const R a1 = A1.ld(i, j, k);
+    const R b1 = i > 1 ? A1.ld(i - 1, j, k) : (g.bx ? A1.ld(g.np, j, k) : R(2) * A1.ld(1, j, k) - A1.ld(2, j, k));
+    const R a2 = A2.ld(i, j, k);
+    const R b2 = j > 1 ? A2.ld(i, j - 1, k) : (g.by ? A2.ld(i, g.mp, k) : R(2) * A2.ld(i, 1, k) - A2.ld(i, 2, k));
+    const R a3 = A3.ld(i, j, k);
+    R a1e = R(0), a2e = R(0);
+    if (xe) a1e = g.bx ? A1.ld(1, j, k) : R(2) * A1.ld(g.np, j, k) - A1.ld(g.np - 1, j, k);
+    if (ye) a2e = g.by ? A2.ld(i, 1, k) : R(2) * A2.ld(i, g.mp, k) - A2.ld(i, g.mp - 1, k);
+    if (!g.bx && i == 1) A1.at(0, j, k) = b1;
+    if (!g.by && j == 1) A2.at(i, 0, k) = b2;
+    u1.at(i, j, k) = scale_down<1>(a1 + b1);
+    u2.at(i, j, k) = scale_down<1>(a2 + b2);
+    u3.at(i, j, k) = scale_down<1>(a3 + b3);
+    if (xe) {
+      if (!g.bx) A1.at(g.np + 1, j, k) = a1e;
+      u1.at(g.np + 1, j, k) = scale_down<1>(a1e + a1);
+    }
+    if (ye) {
+      if (!g.by) A2.at(i, g.mp + 1, k) = a2e;
+      u2.at(i, g.mp + 1, k) = scale_down<1>(a2e + a2);
+    }
+    b3 = a3;
+  }
+  if (ke == g.lp) {  // the top faces lp+1
+    const R a3e = g.bz ? A3.ld(i, j, 1) : R(2) * A3.ld(i, j, g.lp) - A3.ld(i, j, g.lp - 1);
+    if (!g.bz) A3.at(i, j, g.lp + 1) = a3e;
+    u3.at(i, j, g.lp + 1) = scale_down<1>(a3e + b3);
+  }
+}
+
 // velprd_traj0 and the driver's level roll in one pass over the cells (the
 // whole predictor's first launch): the roll reads only the cell's own
 // level-0 momenta and density, which the n+1/2 momenta read too, and writes
@@ -411,8 +479,20 @@ int run_predictor(const PredPlan<R>& P, cudaStream_t s) {
                                                   P.dt_ratio);
   if (P.prof) P.prof->end(ST_PRED_LEVEL, s);
   if (P.prof) P.prof->begin(ST_PRED_CGRID, s);
-  k_pred_cgrid<R, false><<<g2, blk, 0, s>>>(g, P.lev, P.ox, P.oy, P.oz, P.u, P.v, P.w, P.h, P.u1, P.u2, P.u3,
-                                            P.dt_ratio);
+  if constexpr (sizeof(R) == 4) {
+    // FP32: the z-march (0.188 against 0.226 ms per step at 512x512x128), about
+    // four waves of the 6 resident 256-thread blocks per SM (40 registers)
+    const int gx = (g.np + 31) / 32, gy = (g.mp + 7) / 8;
+    int nch = (4 * 6 * num_sms() + gx * gy - 1) / (gx * gy);
+    nch = nch < 1 ? 1 : (nch > g.lp ? g.lp : nch);
+    const int kchunk = (g.lp + nch - 1) / nch;
+    const dim3 grid(gx, gy, (g.lp + kchunk - 1) / kchunk);
+    k_pred_cgrid_z<R><<<grid, dim3(32, 8, 1), 0, s>>>(g, P.lev, P.ox, P.oy, P.oz, P.h, P.u1, P.u2, P.u3, kchunk);
+  } else {
+    // FP64: the per-cell kernel (0.272 against the z-march's 0.301 ms)
+    k_pred_cgrid<R, false><<<g2, blk, 0, s>>>(g, P.lev, P.ox, P.oy, P.oz, P.u, P.v, P.w, P.h, P.u1, P.u2, P.u3,
+                                              P.dt_ratio);
+  }
   if (P.prof) P.prof->end(ST_PRED_CGRID, s);
   add_launches(2);
   return cudaGetLastError() == cudaSuccess ? 0 : -5;
