@@ -128,8 +128,16 @@ __device__ __forceinline__ float scale_up(float x) {
 // pp(y) = max(0,y), pn(y) = -min(0,y)  (mpdataoperators.inc:50-59)
 __device__ __forceinline__ double pp(double y) { return sgn(y) ? 0.0 : y; }
 __device__ __forceinline__ double pn(double y) { return sgn(y) ? neg_bits(y) : 0.0; }
-__device__ __forceinline__ float pp(float y) { return y > 0.f ? y : 0.f; }
-__device__ __forceinline__ float pn(float y) { return y < 0.f ? -y : 0.f; }
+// FP32: one max instruction each.  PTX max.f32 orders -0 below +0 and
+// returns the other operand for a NaN, so max(y, +0) is y > 0 ? y : +0 and
+// max(-y, +0) is y < 0 ? -y : +0 for every y, zeros and NaNs included.
+__device__ __forceinline__ float fmax0(float y) {
+  float r;
+  asm("max.f32 %0, %1, 0f00000000;" : "=f"(r) : "f"(y));
+  return r;
+}
+__device__ __forceinline__ float pp(float y) { return fmax0(y); }
+__device__ __forceinline__ float pn(float y) { return fmax0(-y); }
 // a > b as the FP64 compare gives it, on the integer pipe: false when either
 // operand is a NaN or both are zeros (+0 == -0), else the order of the keys.
 __device__ __forceinline__ bool ieee_gt(double a, double b) {
@@ -216,9 +224,11 @@ constexpr int RATIO_CAP = 2;
 __device__ __forceinline__ double lim_ratio(double n, double d) {
   return ratio_ge1(n, d) ? double(RATIO_CAP) : div_call(n, d);
 }
+// FP32: d in (0, +Inf) as bits [1, 0x7F7FFFFF] and n in [d, +Inf] as bits,
+// each one unsigned range test (n with its sign bit set fails the second).
 __device__ __forceinline__ bool ratio_ge1(float n, float d) {
-  const int nb = __float_as_int(n), db = __float_as_int(d), inf = 0x7F800000;
-  return db > 0 && db < inf && nb >= db && nb <= inf;
+  const unsigned nb = __float_as_uint(n), db = __float_as_uint(d);
+  return db - 1u < 0x7F7FFFFFu && nb - db <= 0x7F800000u - db;
 }
 __device__ __forceinline__ float lim_ratio(float n, float d) { return ratio_ge1(n, d) ? float(RATIO_CAP) : n / d; }
 

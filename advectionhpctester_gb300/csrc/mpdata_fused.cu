@@ -515,6 +515,14 @@ struct Stager {
       stage2<NT>(dst, arena + f * fs + (kw - 1) * pl, o, two, t);
     }
   }
+  // the two forms separately, for a step that stages several planes under one
+  // branch (box: thread 0 of an interior tile; cp: every thread of a seam tile)
+  __device__ __forceinline__ void box(float* dst, int f, int kw, uint64_t* m) const {
+    tma_box(dst, map, xc, yc, kw - 1, f, m);
+  }
+  __device__ __forceinline__ void cp(float* dst, int f, int kw) const {
+    stage2<NT>(dst, arena + f * fs + (kw - 1) * pl, o, two, t);
+  }
 };
 
 // Interior tile: every staged box lies inside the grid, so TMA needs no wrap.
@@ -631,15 +639,36 @@ __device__ __forceinline__ void body_limit(const FzArgs& A, const CUtensorMap* t
     if (s_abort) return;
     if (ko < ke) {
       uint64_t* m = &mbar[n & 1];
-      if (tma && t == 0) mbar_expect_tx(m, NBOX * BOX_BYTES);
-      st.plane(X + S4(ko + 3) * PLANE, A.fin, kw3, m);
-      if (FIRST) st.plane(S + S4(ko + 3) * PLANE, FZ_XIN, kw3, m);
-      st.plane(V3 + q0 * PLANE, FZ_V3, kw3, m);  // plane ko+3 takes the slot of ko
-      st.plane(V1 + S2(ko + 2) * PLANE, FZ_V1, kw2, m);
-      st.plane(V2 + S2(ko + 2) * PLANE, FZ_V2, kw2, m);
-      if (!FIRST) {
-        st.plane(S + S2(ko + 2) * PLANE, fsx, kw2, m);
-        st.plane(S + (2 + S2(ko + 2)) * PLANE, A.fmn_in, kw2, m);
+      float* const dx = X + S4(ko + 3) * PLANE;
+      float* const ds = S + S4(ko + 3) * PLANE;
+      float* const d3 = V3 + q0 * PLANE;  // plane ko+3 takes the slot of ko
+      float* const d1 = V1 + S2(ko + 2) * PLANE;
+      float* const d2 = V2 + S2(ko + 2) * PLANE;
+      float* const dmx = S + S2(ko + 2) * PLANE;
+      float* const dmn = S + (2 + S2(ko + 2)) * PLANE;
+      if (tma) {
+        if (t == 0) {
+          mbar_expect_tx(m, NBOX * BOX_BYTES);
+          st.box(dx, A.fin, kw3, m);
+          if (FIRST) st.box(ds, FZ_XIN, kw3, m);
+          st.box(d3, FZ_V3, kw3, m);
+          st.box(d1, FZ_V1, kw2, m);
+          st.box(d2, FZ_V2, kw2, m);
+          if (!FIRST) {
+            st.box(dmx, fsx, kw2, m);
+            st.box(dmn, A.fmn_in, kw2, m);
+          }
+        }
+      } else {
+        st.cp(dx, A.fin, kw3);
+        if (FIRST) st.cp(ds, FZ_XIN, kw3);
+        st.cp(d3, FZ_V3, kw3);
+        st.cp(d1, FZ_V1, kw2);
+        st.cp(d2, FZ_V2, kw2);
+        if (!FIRST) {
+          st.cp(dmx, fsx, kw2);
+          st.cp(dmn, A.fmn_in, kw2);
+        }
       }
       stage2<NT>(H + q2 * PLANE, caller_plane(A.h, kw2), oh, two, t);  // plane ko+2 takes the slot of ko-1
       cp_async4(RH + S2(ko + 1) * NT + t, caller_plane(A.rhr, kw1) + orh);
@@ -819,11 +848,24 @@ __device__ __forceinline__ void body_pseudo(const FzArgs& A, const CUtensorMap* 
     if (s_abort) return;
     if (ko < ke) {
       uint64_t* m = &mbar[n & 1];
-      if (tma && t == 0) mbar_expect_tx(m, 4 * BOX_BYTES);
-      st.plane(X + S4(ko + 2) * PLANE, A.fin, kw2, m);
-      st.plane(A3 + S4(ko + 2) * PLANE, FZ_W3, kw2, m);
-      st.plane(A1 + S4(ko + 1) * PLANE, FZ_W1, kw1, m);
-      st.plane(A2 + S4(ko + 1) * PLANE, FZ_W2, kw1, m);
+      float* const dx = X + S4(ko + 2) * PLANE;
+      float* const d3 = A3 + S4(ko + 2) * PLANE;
+      float* const d1 = A1 + S4(ko + 1) * PLANE;
+      float* const d2 = A2 + S4(ko + 1) * PLANE;
+      if (tma) {
+        if (t == 0) {
+          mbar_expect_tx(m, 4 * BOX_BYTES);
+          st.box(dx, A.fin, kw2, m);
+          st.box(d3, FZ_W3, kw2, m);
+          st.box(d1, FZ_W1, kw1, m);
+          st.box(d2, FZ_W2, kw1, m);
+        }
+      } else {
+        st.cp(dx, A.fin, kw2);
+        st.cp(d3, FZ_W3, kw2);
+        st.cp(d1, FZ_W1, kw1);
+        st.cp(d2, FZ_W2, kw1);
+      }
       stage2<NT>(H + S4(ko + 1) * PLANE, caller_plane(A.h, kw1), oh, two, t);
       cp_commit();
       kw2 = next_plane(kw2, g.lp);
