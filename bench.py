@@ -107,7 +107,7 @@ NCU_PSEUDO = {64: {"dram_bytes_per_cell": 127.8, "fp64_inst_per_cell": 39.0},
 # The same for the dominant fused single-precision kernel (the first pass's
 # fused_limit_update) at 384x384x64: DRAM bytes and issued warp instructions
 # per cell (smsp__inst_executed.sum * 32 / cells) and the issue-active share.
-NCU_FUSED_LIMIT = {"dram_bytes_per_cell": 49.9, "inst_per_cell": 613.0, "issue_active": 0.775}
+NCU_FUSED_LIMIT = {"dram_bytes_per_cell": 50.0, "inst_per_cell": 577.0, "issue_active": 0.748}
 # GB300 issues 2 FP64 instructions per SM per clock (1.25 TFLOP/s nominal FMA).
 FP64_INST_PER_SM_CLK = 2.0
 # FP64 flops per cell of one launch of each stage (DADD and DMUL 1, DFMA 2),
