@@ -102,6 +102,25 @@ def test_edge_sizes_reference_bc(M, oracle, n):
     np.testing.assert_array_equal(out, g.x)
 
 
+@pytest.mark.parametrize("unit", [False, True], ids=["variable_density", "unit_density"])
+@pytest.mark.parametrize("n", [(40, 36, 17), (36, 40, 35)])
+@pytest.mark.parametrize("ibc", [(1, 1, 1), (0, 0, 0), (1, 0, 1)])
+def test_fp64_gauge_plane_chunks(M, oracle, n, ibc, unit):
+    """FP64 gauge steps whose pseudo-velocity kernel marches chunks of 16
+    planes: a last chunk of one plane (lp 17) or three (lp 35), the wall or
+    wrapped planes 1 and lp, warps at the x and y edges, and warps whose faces
+    are all of unit density or not; bit for bit against the oracle."""
+    f = W.random_fields(*n, ibc=ibc, seed=sum(n) + 7 * ibc[0] + 3 * ibc[1])
+    if unit:
+        f.h[...] = 1.0
+        f.rhr[...] = 1.0
+    g = f.copy()
+    out = run_gpu(M, f, t_adv=1, iord=3, steps=2)
+    oracle.advec_dwarf(oracle.grid(g.np, g.mp, g.lp, 1, *ibc), g.x, g.bcx, g.bcy, g.u1, g.u2, g.u3,
+                       g.rhr, g.h, t_adv=1, iord=3, nsteps=2)
+    np.testing.assert_array_equal(out, g.x)
+
+
 @pytest.mark.parametrize("gauge", [1, 0])
 @pytest.mark.parametrize("ibc", [(1, 1, 1), (0, 0, 0)])
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
