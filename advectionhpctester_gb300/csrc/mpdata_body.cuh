@@ -723,9 +723,9 @@ __device__ __forceinline__ RatioOps<R> bounds_body(const Prob<R>& P, int i, int 
 }
 
 // The FP64 limiter ratios of a block (whole warps, at most 256 threads),
-// divided together.  Only the
-// ratios below 1 need a quotient (a larger one is stored as RATIO_CAP, see
-// lim_ratio), and they are a few percent of the cells, scattered: a
+// divided together.  Only the ratios below 1 need a quotient (a larger one
+// is stored as RATIO_CAP, see lim_ratio), and they are a few percent of the
+// cells, scattered: a
 // warp dividing its own would run the division sequence (about ten FP64-pipe
 // instructions) whenever any of its lanes needs one.  Here the block packs its
 // operand pairs into shared memory, the first warps divide them, 32 at a time,
@@ -759,7 +759,12 @@ __device__ __forceinline__ void block_ratios(const Prob<R>& P, int i, int j, int
     s_d[in] = r.dn;
   }
   __syncthreads();
-  for (int it = tid; it < total; it += nt) s_n[it] = s_n[it] / s_d[it];
+  // a zero numerator is its own quotient: on a zero background whole warps
+  // of the packed list skip the division
+  for (int it = tid; it < total; it += nt) {
+    const R n = s_n[it], d = s_d[it];
+    if (!ratio_zero(n, d)) s_n[it] = n / d;
+  }
   __syncthreads();
   if (valid) {
     P.cp.at(i, j, k) = dp ? s_n[ip] : R(RATIO_CAP);

@@ -224,6 +224,14 @@ constexpr int RATIO_CAP = 2;
 __device__ __forceinline__ double lim_ratio(double n, double d) {
   return ratio_ge1(n, d) ? double(RATIO_CAP) : div_call(n, d);
 }
+// n/d is n itself when n is a zero and d a positive finite number (IEEE
+// 0/d is a zero with the sign of n).  A field on an exactly zero background
+// has two such ratios at every background cell, where x equals its star's
+// minimum and maximum.
+__device__ __forceinline__ bool ratio_zero(double n, double d) {
+  const long long db = __double_as_longlong(d), inf = 0x7FF0000000000000LL;
+  return ((unsigned long long)__double_as_longlong(n) << 1) == 0ULL && db > 0 && db < inf;
+}
 // FP32: d in (0, +Inf) as bits [1, 0x7F7FFFFF] and n in [d, +Inf] as bits,
 // each one unsigned range test (n with its sign bit set fails the second).
 __device__ __forceinline__ bool ratio_ge1(float n, float d) {

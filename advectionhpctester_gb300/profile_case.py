@@ -3,10 +3,11 @@ allocations, for profilers (ncu) and quick timing.
 
   python -m advectionhpctester_gb300.profile_case --grid 384 384 64 --steps 2 \
       [--precision 64|32] [--std] [--iord 3] [--bc periodic|reference] \
-      [--workload random|deformational] [--adjoint]
+      [--workload random|deformational|balls] [--adjoint]
 
 random: seeded random fields with h, rhr in [0.8, 1.2]; deformational: the
-periodic deformational flow with unit densities (the benchmark's fields).
+periodic deformational flow with unit densities (the benchmark's fields);
+balls: the same flow carrying two balls on an exactly zero background.
 
 Prints the CUDA-event time per step and the per-stage times.  --adjoint
 times the step adjoint (lambda = psi, zero velocity gradients) after the
@@ -27,7 +28,7 @@ def main(argv=None):
     ap.add_argument("--std", action="store_true", help="standard form (default: gauge)")
     ap.add_argument("--iord", type=int, default=3)
     ap.add_argument("--bc", choices=["periodic", "reference"], default="periodic")
-    ap.add_argument("--workload", choices=["random", "deformational"], default="random")
+    ap.add_argument("--workload", choices=["random", "deformational", "balls"], default="random")
     ap.add_argument("--adjoint", action="store_true", help="also time the step adjoint")
     a = ap.parse_args(argv)
 
@@ -41,10 +42,10 @@ def main(argv=None):
     nx, ny, nz = a.grid
     ibc = (1, 1, 1) if a.bc == "periodic" else (0, 0, 0)
     dnp = np.float64 if a.precision == 64 else np.float32
-    if a.workload == "deformational":
+    if a.workload in ("deformational", "balls"):
         if a.bc != "periodic":
             ap.error("the deformational workload is periodic")
-        f = W.deformational(nx, ny, nz, dtype=dnp)
+        f = W.deformational(nx, ny, nz, dtype=dnp, balls=a.workload == "balls")
     else:
         f = W.random_fields(nx, ny, nz, ibc=ibc, seed=1, courant=0.25, dtype=dnp)
     d = {k: M.fortran_device(getattr(f, k)) for k in ("x", "u1", "u2", "u3", "h", "rhr", "bcx", "bcy")}

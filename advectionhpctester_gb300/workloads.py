@@ -212,20 +212,25 @@ def deformational_agrid(np_, mp, lp, t, T, courant=0.5):
 
 
 def deformational(np_=512, mp=512, lp=128, ih=1, courant=0.5, seed=20261203, dtype=np.float64,
-                  nsteps=200):
+                  nsteps=200, balls=False):
     """Periodic deformational-flow workload: psi ~ U[1,2] (seeded) plus two
     Gaussian cones (amplitude 1, sigma 0.05 L); C-grid Courant numbers are the
-    periodic face averages of the A-grid flow at t=0."""
+    periodic face averages of the A-grid flow at t=0.  balls: psi is instead
+    two balls of value 4 (radius 0.15 L) on an exactly zero background, as in
+    the reference's rotating-sphere test."""
     f = Fields(np_, mp, lp, ih, 1, 1, 1, np.float64)
     rng = np.random.default_rng(seed)
     x = (np.arange(np_) + 0.5) / np_
     y = (np.arange(mp) + 0.5) / mp
     z = (np.arange(lp) + 0.5) / lp
-    psi = 1.0 + rng.random((np_, mp, lp))
+    psi = np.zeros((np_, mp, lp)) if balls else 1.0 + rng.random((np_, mp, lp))
     for (cx, cy, cz) in ((0.35, 0.35, 0.5), (0.65, 0.65, 0.5)):
         r2 = ((x - cx)[:, None, None] ** 2 + (y - cy)[None, :, None] ** 2
               + (z - cz)[None, None, :] ** 2)
-        psi += np.exp(-r2 / (2 * 0.05 ** 2))
+        if balls:
+            psi[r2 <= 0.15 ** 2] = 4.0
+        else:
+            psi += np.exp(-r2 / (2 * 0.05 ** 2))
     interior(f.x, ih)[...] = psi
     ua, va, wa = deformational_agrid(np_, mp, lp, 0.0, float(nsteps))
     set_c_grid_periodic(f, ua, va, wa)
